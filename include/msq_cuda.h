@@ -1,0 +1,216 @@
+/*
+ * msq_cuda.h — C ABI of the GB300 (sm_103a) SPD matrix-square-root pipeline.
+ *
+ * This is the drop-in boundary a `cuda_backend` beside the reference's
+ * `metal_backend` / `accelerate_backend` binds to.  Every entry point takes
+ * plain pointers and sizes, returns an int status (MSQ_OK on success) and
+ * never throws.  Device buffers are allocated and owned by the caller; all
+ * matrices are column-major (element (row, column) at row + column * n),
+ * exactly as in the reference (`PreparedMatrix.values`, src/experiment.hpp:18).
+ * Work is enqueued on the context's stream (msq_set_stream); calls are
+ * stream-ordered, and only the calls that return host values synchronise.
+ *
+ * Status codes map onto the reference's error convention: a nonzero status is
+ * what `fail()` (src/core.cpp:7-9) raises; msq_last_error() gives the text.
+ * Numerical outcomes (not converged, rejected basis, ...) are NOT errors; they
+ * are reported in msq_solve_result, as the reference reports them in
+ * `CaseResult.status` / `termination_reason` (src/experiment.hpp:64-125).
+ */
+#ifndef MSQ_CUDA_H
+#define MSQ_CUDA_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ------------------------------------------------------ */
+enum {
+  MSQ_OK = 0,
+  MSQ_ERR_INVALID_ARGUMENT = 1, /* bad size, format, null or misaligned ptr */
+  MSQ_ERR_CUDA = 2,             /* a CUDA runtime/driver call failed        */
+  MSQ_ERR_DEVICE_STATUS = 3,    /* a kernel reported an error flag (bounded
+                                   wait expired, index out of range)         */
+  MSQ_ERR_UNSUPPORTED = 4       /* valid request this build does not serve  */
+};
+
+/* ---- storage formats ----------------------------------------------------
+ * Ids 0..7 equal the reference's HostStorageCodec (src/precision.hpp:24-33),
+ * so `static_cast<int>(spec.host_storage)` selects the same codec.
+ * MSQ_FMT_FP8_E4M3FN_ROWSCALE has no reference counterpart: E4M3FN codes of
+ * x / s_row with one FP32 scale s_row = max|row| / 448 per contiguous row.  */
+typedef enum {
+  MSQ_FMT_FP32 = 0,
+  MSQ_FMT_BF16 = 1,
+  MSQ_FMT_FP8_E4M3FN = 2,
+  MSQ_FMT_FP8_E5M2 = 3,
+  MSQ_FMT_MXFP8_E4M3FN = 4,
+  MSQ_FMT_MXFP8_E5M2 = 5,
+  MSQ_FMT_FP4_E2M1 = 6,
+  MSQ_FMT_MXFP4_E2M1 = 7,
+  MSQ_FMT_FP8_E4M3FN_ROWSCALE = 8
+} msq_format;
+
+typedef struct msq_ctx msq_ctx;
+
+/* ---- context --------------------------------------------------------------
+ * Replaces the RAII `MetalRuntime` (src/metal_runtime.hpp:69-76): owns the
+ * device binding, the stream and the kernels' small persistent state.      */
+int msq_create(msq_ctx **out, int device);
+void msq_destroy(msq_ctx *ctx);
+const char *msq_last_error(const msq_ctx *ctx);
+/* `stream` is a cudaStream_t (NULL = legacy default stream). */
+int msq_set_stream(msq_ctx *ctx, void *stream);
+int msq_synchronize(msq_ctx *ctx);
+/* Number of this library's kernel launches enqueued so far on `ctx`. */
+uint64_t msq_launch_count(const msq_ctx *ctx);
+
+/* ---- codecs (the benchmark spec (b)) ---------------------------------------------
+ * Byte sizes: storageBytes / scaleBytes (src/configuration.cpp:188-213).
+ * For MSQ_FMT_FP8_E4M3FN_ROWSCALE the scale plane is 4 bytes per row.      */
+size_t msq_storage_bytes(int format, size_t elements);
+size_t msq_scale_bytes(int format, size_t elements, size_t row_length);
+
+/* Encode `elements` FP32 values (device pointer) into `values` (+ `scales`
+ * for MX / row-scaled formats).  Bit-exact with the reference host codec
+ * copyToStorage (src/storage_codecs.cpp:249-321).  `row_length` is used
+ * only by the row-scaled format (elements % row_length must be 0).        */
+int msq_encode(msq_ctx *ctx, int format, const float *source, size_t elements,
+               size_t row_length, uint8_t *values, uint8_t *scales);
+/* Decode back to FP32; bit-exact with storageValueAt
+ * (src/storage_codecs.cpp:323-374) for every index.                       */
+int msq_decode(msq_ctx *ctx, int format, const uint8_t *values,
+               const uint8_t *scales, size_t elements, size_t row_length,
+               float *output);
+
+/* ---- batched layout -------------------------------------------------------
+ * A batch is `count` square matrices of orders n[i], packed back to back:
+ * matrix i starts at element offset[i] (offsets are in elements; each
+ * matrix occupies n[i]*n[i] elements, column-major).  `n` and `offset` are
+ * HOST arrays; the library uploads them once per distinct batch layout.   */
+
+/* ---- Jacobi eigensolver (the benchmark spec (a)) -----------------------------------
+ * Replaces MetalRuntime::symmetricJacobi (src/metal_runtime.cpp:584-646) and
+ * makeJacobiSchedule (src/metal_solver.cpp:50-79).  Parallel-order
+ * (round-robin) two-sided cyclic Jacobi, FP32 storage, FP64 rotation angles
+ * and FP64 off-norm.  Sweeps stop once off(A) <= tolerance * ||A||_F or
+ * after max_sweeps.  In: matrices (FP32).  Out: vectors (FP32, column j =
+ * eigenvector j), eigenvalues (FP32, n[i] per matrix at value offset
+ * eig_offset[i] = sum of previous n), sweeps_done / off_ratio per matrix
+ * (device arrays, may be NULL).  `matrices` is overwritten (the converged,
+ * nearly diagonal matrix).                                                 */
+int msq_jacobi_batched(msq_ctx *ctx, float *matrices, float *vectors,
+                       float *eigenvalues, const int32_t *n,
+                       const int64_t *offset, int count, double tolerance,
+                       int max_sweeps, int32_t *sweeps_done, float *off_ratio);
+
+/* ---- reconstruction (the benchmark spec (c)) ---------------------------------------
+ * X = V diag(sqrt(lambda)) V^T per matrix, written as the symmetric product
+ * X = W W^T with W = V diag(lambda^(1/4)).  Replaces reconstructTiled /
+ * reconstructLowFactorTiled (src/metal_runtime.cpp:429-534).
+ * msq_make_factor builds W^T in K-major order (row i of W contiguous) from V
+ * and lambda, FP32.  msq_reconstruct consumes W^T in `format`:
+ *   MSQ_FMT_FP32        SIMT FP32 GEMM (the plain FP32 path)
+ *   MSQ_FMT_BF16        tcgen05 kind::f16 MMA, FP32 accumulate in TMEM
+ *   MSQ_FMT_FP8_E4M3FN_ROWSCALE  tcgen05 kind::f8f6f4 (E4M3 x E4M3),
+ *                       row scales applied in the epilogue
+ * `values`/`scales` hold the encoded W^T (scales only for row-scaled).
+ * Output X (FP32) uses the same batched layout as the input.              */
+int msq_make_factor(msq_ctx *ctx, const float *vectors,
+                    const float *eigenvalues, const int32_t *n,
+                    const int64_t *offset, int count, float *factor_t);
+int msq_reconstruct(msq_ctx *ctx, int format, const void *values,
+                    const float *scales, const int32_t *n,
+                    const int64_t *offset, int count, float *root);
+
+/* ---- residual and Sylvester correction (the benchmark spec (d)) --------------------
+ * msq_residual: R = A - X*X with X = (x_hi + x_lo) in float-float (about 48
+ * bits, the reference's WorkingFloat, metal_mixed_sqrt.metal:1268-1317);
+ * writes R as FP32 (may be NULL) and per-matrix ||R||_F^2, ||A||_F^2 (FP64,
+ * device, 2 per matrix).  x_lo may be NULL (treated as zero).
+ * msq_sylvester_sweep: one frozen-basis correction of
+ * refineUpdateAndMeasure (src/metal_runtime.cpp:847-966):
+ *   C = (V^T R V) o H, H_ij = 1/(s_i + s_j) recomputed from s = sqrt(lambda),
+ *   E = V C V^T,  X <- X + (E + E^T)/2 (float-float add into x_hi/x_lo).
+ * `gemm_format` selects the correction GEMMs: MSQ_FMT_FP32 (SIMT FP32) or
+ * MSQ_FMT_BF16 (tcgen05 split-BF16, three products, FP32 accumulate).
+ * `workspace` must hold 2 * sum(n^2) floats.                               */
+int msq_residual(msq_ctx *ctx, const float *a, const float *x_hi,
+                 const float *x_lo, const int32_t *n, const int64_t *offset,
+                 int count, float *residual, double *norms);
+int msq_sylvester_sweep(msq_ctx *ctx, int gemm_format, const float *vectors,
+                        const float *eigenvalues, const float *residual,
+                        const int32_t *n, const int64_t *offset, int count,
+                        float *x_hi, float *x_lo, float *workspace);
+
+/* ---- whole-pipeline batched solve ------------------------------------------
+ * The GPU-resident solve of solveGpuResidentSpd (src/metal_solver.cpp:92-336)
+ * over a batch: Jacobi -> (quantize W) -> reconstruct -> Sylvester sweeps ->
+ * final float-float residual, per-matrix plan, with FP32 fallback for every
+ * matrix whose final residual misses `tolerance` (plan MSQ_PLAN_FP32).     */
+typedef enum {
+  MSQ_PLAN_FP32 = 0,   /* Jacobi to 1e-7, FP32 reconstruction, no sweeps    */
+  MSQ_PLAN_BF16 = 1,   /* BF16 W, tcgen05 reconstruction                    */
+  MSQ_PLAN_FP8 = 2,    /* FP8-E4M3 W with per-row FP32 scale               */
+  MSQ_PLAN_MXFP4 = 3   /* MXFP4 W (E2M1 + E8M0 per 32 along K)              */
+} msq_plan_format;
+
+typedef struct {
+  int32_t format;        /* msq_plan_format                                  */
+  int32_t sweeps;        /* Sylvester correction sweeps (0, 1, 2)            */
+  double jacobi_tolerance; /* off(A) <= jacobi_tolerance * ||A||_F           */
+  int32_t jacobi_max_sweeps;
+  int32_t reserved;
+} msq_plan;
+
+typedef struct {
+  double final_residual;   /* ||A - X^2||_F / ||A||_F, float-float         */
+  double initial_residual; /* residual of the reconstruction X0            */
+  int32_t jacobi_sweeps;
+  int32_t corrections;     /* Sylvester sweeps applied                     */
+  int32_t accepted;        /* 1: the plan met the tolerance; 0: fell back  */
+  int32_t fallback;        /* 1: result comes from the FP32 fallback       */
+} msq_solve_result;
+
+/* a: FP32 matrices (device, batched layout); root: FP32 output (device).
+ * plans: HOST array of `count` plans (NULL = MSQ_PLAN_FP32 for all).
+ * results: HOST array of `count` results (may be NULL).                   */
+int msq_solve_batched(msq_ctx *ctx, const float *a, const int32_t *n,
+                      const int64_t *offset, int count, const msq_plan *plans,
+                      double tolerance, float *root, msq_solve_result *results);
+
+/* ---- learned plan selector -------------------------------------------------
+ * MLP 16 -> 64 -> 64 -> 8 (ReLU), BF16 weights, FP32 accumulation.  The
+ * reference picks plans by fixed rules (runAdaptiveMetalCase,
+ * src/metal_solver.cpp:976-1001; the cond < 1000 rule of
+ * 3_spectral/spectral.cpp:837-838); this network replaces those rules.
+ * msq_features: 16 per-matrix features from A (device) into `features`
+ * (device, FP32, 16 per matrix).  Parameters live in one FP32 master array
+ * (device) of MSQ_MLP_PARAMS floats; the kernels read its BF16 copy.       */
+#define MSQ_MLP_IN 16
+#define MSQ_MLP_HIDDEN 64
+#define MSQ_MLP_OUT 8
+#define MSQ_MLP_PARAMS \
+  (MSQ_MLP_IN * MSQ_MLP_HIDDEN + MSQ_MLP_HIDDEN + \
+   MSQ_MLP_HIDDEN * MSQ_MLP_HIDDEN + MSQ_MLP_HIDDEN + \
+   MSQ_MLP_HIDDEN * MSQ_MLP_OUT + MSQ_MLP_OUT)
+int msq_features(msq_ctx *ctx, const float *a, const int32_t *n,
+                 const int64_t *offset, int count, float *features);
+int msq_mlp_forward(msq_ctx *ctx, const float *params, const float *features,
+                    int rows, float *logits);
+/* Softmax cross-entropy over masked targets: grad_params += dL/dparams.
+ * targets: per row, 8 floats in [0,1] (1 = plan acceptable) weighted by
+ * `costs`; see the implementation for the exact loss.  loss: device scalar. */
+int msq_mlp_backward(msq_ctx *ctx, const float *params, const float *features,
+                     const float *targets, int rows, float *grad_params,
+                     float *loss);
+int msq_mlp_step(msq_ctx *ctx, float *params, const float *grad_params,
+                 float *adam_m, float *adam_v, int step, float learning_rate);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* MSQ_CUDA_H */

@@ -1,0 +1,189 @@
+// Device encoders/decoders for the storage formats of the reference's host
+// codec (src/storage_codecs.cpp).  Each function is a bit-exact restatement:
+//
+//  * floatToBf16 (src/storage_codecs.cpp:16-28): round-half-even on the top
+//    16 bits, quiet bit forced for NaN — the same integer steps.
+//  * floatToFp8E4M3Fn / floatToFp8E5M2 / floatToFp4E2M1 (:96-136) pick the
+//    nearest finite code by a linear scan with ties to the even code
+//    (nearestFiniteCode :79-94).  Neighbouring codes are within a factor of
+//    two, so the scan's FP32 distances are exact for the two candidates that
+//    bracket the input and the scan equals round-to-nearest-even on the
+//    value.  Here that rounding is done with integer arithmetic on the FP32
+//    bits: exponent rebias plus RNE of the dropped mantissa bits, and
+//    rint(x * 2^(M - emin)) below the smallest normal.  Saturation, infinity
+//    and NaN rules are the reference's, branch for branch.
+//  * MX scale (mxScaleExponent :148-162): e = clamp(ilogb(max finite |x|) -
+//    emax, -127, 128), 0 for an all-zero block; elements are enc(x / 2^e).
+//    x * 2^-e is computed as a multiplication by the normal float 2^-e,
+//    which rounds exactly like the reference's division by 2^e.
+//  * Decoders (:30-77, :323-374) build the FP32 bits directly; MX decode is
+//    an exact ldexp (all products are representable).
+#pragma once
+
+#include <cstdint>
+
+namespace msq {
+
+__device__ __forceinline__ uint16_t encodeBf16(float value) {
+  const uint32_t bits = __float_as_uint(value);
+  uint32_t rounded = bits >> 16;
+  const uint32_t remainder = bits & 0xffffu;
+  if (remainder > 0x8000u || (remainder == 0x8000u && (rounded & 1u) != 0)) {
+    ++rounded;
+  }
+  if ((bits & 0x7f800000u) == 0x7f800000u && (bits & 0x007fffffu) != 0) {
+    rounded |= 0x0040u;
+  }
+  return static_cast<uint16_t>(rounded);
+}
+
+__device__ __forceinline__ float decodeBf16(uint16_t value) {
+  return __uint_as_float(static_cast<uint32_t>(value) << 16);
+}
+
+// Round a finite, positive magnitude that is not above the format's largest
+// finite value to the nearest code (ties to even).  kMant = mantissa bits,
+// kBias = exponent bias; codes are (exponent_field << kMant) | mantissa.
+template <int kMant, int kBias>
+__device__ __forceinline__ uint32_t roundMagnitude(float magnitude) {
+  constexpr int kEmin = 1 - kBias;  // exponent of the smallest normal
+  const uint32_t bits = __float_as_uint(magnitude);
+  const int exponent = static_cast<int>(bits >> 23) - 127;
+  if (exponent < kEmin) {
+    // Subnormal region of the target: multiples of 2^(kEmin - kMant).
+    // The scaling is exact; rint rounds half to even.
+    const float scaled = magnitude * __uint_as_float(
+                                         static_cast<uint32_t>(127 + kMant - kEmin) << 23);
+    return static_cast<uint32_t>(rintf(scaled));
+  }
+  const uint32_t mantissa = bits & 0x007fffffu;
+  constexpr int kDrop = 23 - kMant;
+  uint32_t code = (static_cast<uint32_t>(exponent + kBias) << kMant) |
+                  (mantissa >> kDrop);
+  const uint32_t remainder = mantissa & ((1u << kDrop) - 1u);
+  constexpr uint32_t kHalf = 1u << (kDrop - 1);
+  if (remainder > kHalf || (remainder == kHalf && (code & 1u) != 0)) {
+    ++code;  // carries into the exponent field, as the code order requires
+  }
+  return code;
+}
+
+// floatToFp8E4M3Fn (src/storage_codecs.cpp:96-108)
+__device__ __forceinline__ uint8_t encodeE4M3(float value) {
+  const uint32_t bits = __float_as_uint(value);
+  const uint32_t sign = (bits >> 24) & 0x80u;
+  const float magnitude = fabsf(value);
+  if (magnitude != magnitude) return static_cast<uint8_t>(sign | 0x7fu);
+  if (magnitude == 0.0f) return static_cast<uint8_t>(sign);
+  if (magnitude > 448.0f) return static_cast<uint8_t>(sign | 0x7eu);  // incl. inf
+  return static_cast<uint8_t>(sign | roundMagnitude<3, 7>(magnitude));
+}
+
+// floatToFp8E5M2 (src/storage_codecs.cpp:110-125)
+__device__ __forceinline__ uint8_t encodeE5M2(float value) {
+  const uint32_t bits = __float_as_uint(value);
+  const uint32_t sign = (bits >> 24) & 0x80u;
+  const float magnitude = fabsf(value);
+  if (magnitude != magnitude) return static_cast<uint8_t>(sign | 0x7eu);
+  if (magnitude == 0.0f) return static_cast<uint8_t>(sign);
+  if (isinf(magnitude)) return static_cast<uint8_t>(sign | 0x7cu);
+  if (magnitude > 57344.0f) return static_cast<uint8_t>(sign | 0x7bu);
+  return static_cast<uint8_t>(sign | roundMagnitude<2, 15>(magnitude));
+}
+
+// floatToFp4E2M1 (src/storage_codecs.cpp:127-136); 4-bit code in the low nibble
+__device__ __forceinline__ uint32_t encodeE2M1(float value) {
+  const uint32_t bits = __float_as_uint(value);
+  const uint32_t sign = (bits >> 28) & 0x8u;
+  const float magnitude = fabsf(value);
+  if (magnitude != magnitude || magnitude == 0.0f) return sign;
+  if (magnitude > 6.0f) return sign | 0x7u;  // incl. inf
+  return sign | roundMagnitude<1, 1>(magnitude);
+}
+
+__device__ __forceinline__ float signedNan(uint32_t negative) {
+  return __uint_as_float(0x7fc00000u | (negative ? 0x80000000u : 0u));
+}
+
+// fp8E4M3FnToFloat (src/storage_codecs.cpp:37-49)
+__device__ __forceinline__ float decodeE4M3(uint32_t code) {
+  const uint32_t sign = (code & 0x80u) << 24;
+  const uint32_t exponent = (code >> 3) & 0xfu;
+  const uint32_t fraction = code & 0x7u;
+  if (exponent == 0xfu && fraction == 0x7u) return signedNan(sign);
+  if (exponent == 0) {
+    // fraction * 2^-9, exact
+    return __uint_as_float(sign | __float_as_uint(static_cast<float>(fraction) *
+                                                  0.001953125f));
+  }
+  return __uint_as_float(sign | ((exponent + 120u) << 23) | (fraction << 20));
+}
+
+// fp8E5M2ToFloat (src/storage_codecs.cpp:51-66)
+__device__ __forceinline__ float decodeE5M2(uint32_t code) {
+  const uint32_t sign = (code & 0x80u) << 24;
+  const uint32_t exponent = (code >> 2) & 0x1fu;
+  const uint32_t fraction = code & 0x3u;
+  if (exponent == 0x1fu) {
+    return fraction == 0 ? __uint_as_float(sign | 0x7f800000u) : signedNan(sign);
+  }
+  if (exponent == 0) {
+    return __uint_as_float(sign | __float_as_uint(static_cast<float>(fraction) *
+                                                  1.52587890625e-05f));
+  }
+  return __uint_as_float(sign | ((exponent + 112u) << 23) | (fraction << 21));
+}
+
+// fp4E2M1ToFloat (src/storage_codecs.cpp:68-77); code in the low nibble
+__device__ __forceinline__ float decodeE2M1(uint32_t code) {
+  const uint32_t sign = (code & 0x8u) << 28;
+  const uint32_t exponent = (code >> 1) & 0x3u;
+  const uint32_t fraction = code & 0x1u;
+  if (exponent == 0) {
+    return __uint_as_float(sign | (fraction ? 0x3f000000u : 0u));
+  }
+  return __uint_as_float(sign | ((exponent + 126u) << 23) | (fraction << 22));
+}
+
+// ilogb of a finite, nonzero magnitude (normal or subnormal FP32).
+__device__ __forceinline__ int ilogbFinite(float magnitude) {
+  const uint32_t bits = __float_as_uint(magnitude) & 0x7fffffffu;
+  const int field = static_cast<int>(bits >> 23);
+  if (field != 0) return field - 127;
+  return (31 - __clz(static_cast<int>(bits))) - 149;
+}
+
+// mxScaleExponent (src/storage_codecs.cpp:148-162) from a block maximum of
+// finite magnitudes (0 when the block holds no nonzero finite value).
+__device__ __forceinline__ int mxExponent(float block_maximum, int emax) {
+  if (block_maximum == 0.0f) return 0;
+  int e = ilogbFinite(block_maximum) - emax;
+  e = e < -127 ? -127 : e;
+  e = e > 128 ? 128 : e;
+  return e;
+}
+
+// 2^k as a float for k in [-126, 127].
+__device__ __forceinline__ float exp2Int(int k) {
+  return __uint_as_float(static_cast<uint32_t>(k + 127) << 23);
+}
+
+// x / 2^e as the reference computes it (value_at(index) / scale); e is in
+// [-127, 125] for every finite block, so 2^-e is a normal float and one
+// correctly rounded multiplication gives the same result as the division.
+__device__ __forceinline__ float mxDivide(float x, int e) {
+  if (e >= -126 && e <= 126) return x * exp2Int(-e);
+  // e == -127: 2^127 is normal;  e > 126 cannot come from a finite block.
+  return e < 0 ? x * 1.7014118346046923e38f : __fdiv_rn(x, 8.507059173023462e37f);
+}
+
+// Exact ldexp of a decoded element (<= 4 significant bits) by scale - 127,
+// the reference's std::ldexp(decoded, scale - 127).
+__device__ __forceinline__ float mxScale(float decoded, uint32_t scale_byte) {
+  if (decoded != decoded) return decoded;  // NaN bits already canonical
+  const int k = static_cast<int>(scale_byte) - 127;  // [-127, 128]
+  const int half = k / 2;
+  return (decoded * exp2Int(half)) * exp2Int(k - half);
+}
+
+}  // namespace msq

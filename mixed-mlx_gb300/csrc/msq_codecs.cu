@@ -1,0 +1,433 @@
+// Codec kernels: FP32 <-> BF16 / FP8 E4M3FN / FP8 E5M2 / MXFP8 / FP4 E2M1 /
+// MXFP4 / FP8 E4M3FN with a per-row FP32 scale.
+//
+// Replaces the reference's per-element quantize/decode kernels
+// (metal_mixed_sqrt.metal:384-1259, 1661-1909) and is bit-exact with its host
+// codec copyToStorage / storageValueAt (src/storage_codecs.cpp:249-374).
+// HBM-bound streaming work: every thread owns 8 consecutive elements
+// (two 16-byte loads), an MX block of 32 elements is owned by 4 adjacent
+// lanes that agree on the block maximum through two xor-shuffles, and grids
+// are a multiple of the SM count with a grid-stride loop.
+#include "msq_codec_device.cuh"
+#include "msq_internal.cuh"
+
+namespace msq {
+namespace {
+
+constexpr int kThreads = 256;
+constexpr int kGroup = 8;  // elements per thread
+
+struct Group {
+  float v[kGroup];
+};
+
+__device__ __forceinline__ Group loadGroup(const float *__restrict__ source,
+                                           size_t base, size_t elements,
+                                           bool vector_ok) {
+  Group g;
+  if (vector_ok && base + kGroup <= elements) {
+    const float4 a = __ldcs(reinterpret_cast<const float4 *>(source + base));
+    const float4 b = __ldcs(reinterpret_cast<const float4 *>(source + base + 4));
+    g.v[0] = a.x; g.v[1] = a.y; g.v[2] = a.z; g.v[3] = a.w;
+    g.v[4] = b.x; g.v[5] = b.y; g.v[6] = b.z; g.v[7] = b.w;
+  } else {
+#pragma unroll
+    for (int i = 0; i < kGroup; ++i) {
+      g.v[i] = base + i < elements ? source[base + i] : 0.0f;
+    }
+  }
+  return g;
+}
+
+__device__ __forceinline__ void storeGroup(float *__restrict__ output,
+                                           size_t base, size_t elements,
+                                           bool vector_ok, const Group &g) {
+  if (vector_ok && base + kGroup <= elements) {
+    __stcs(reinterpret_cast<float4 *>(output + base),
+           make_float4(g.v[0], g.v[1], g.v[2], g.v[3]));
+    __stcs(reinterpret_cast<float4 *>(output + base + 4),
+           make_float4(g.v[4], g.v[5], g.v[6], g.v[7]));
+  } else {
+#pragma unroll
+    for (int i = 0; i < kGroup; ++i) {
+      if (base + i < elements) output[base + i] = g.v[i];
+    }
+  }
+}
+
+__device__ __forceinline__ float groupMaxFinite(const Group &g) {
+  float m = 0.0f;
+#pragma unroll
+  for (int i = 0; i < kGroup; ++i) {
+    const float a = fabsf(g.v[i]);
+    if (a <= 3.402823466e38f) m = fmaxf(m, a);  // finite only (NaN fails)
+  }
+  return m;
+}
+
+// Writes `count` bytes of `packed` (little-endian) at byte offset `at`.
+__device__ __forceinline__ void storeBytes(uint8_t *__restrict__ out, size_t at,
+                                           uint64_t packed, int count,
+                                           bool vector_ok) {
+  if (vector_ok && count == 8) {
+    *reinterpret_cast<uint64_t *>(out + at) = packed;
+  } else if (vector_ok && count == 4) {
+    *reinterpret_cast<uint32_t *>(out + at) = static_cast<uint32_t>(packed);
+  } else {
+    for (int i = 0; i < count; ++i) {
+      out[at + i] = static_cast<uint8_t>(packed >> (8 * i));
+    }
+  }
+}
+
+// ---------------------------------------------------------------- encoders
+
+template <int kFormat>
+__global__ void __launch_bounds__(kThreads)
+encodeScalarKernel(const float *__restrict__ source, size_t elements,
+                   uint8_t *__restrict__ values, uint8_t *__restrict__ scales,
+                   bool vector_ok) {
+  const size_t groups = (elements + kGroup - 1) / kGroup;
+  for (size_t group = blockIdx.x * static_cast<size_t>(blockDim.x) + threadIdx.x;
+       group < groups; group += static_cast<size_t>(gridDim.x) * blockDim.x) {
+    const size_t base = group * kGroup;
+    const Group g = loadGroup(source, base, elements, vector_ok);
+    const size_t valid = elements - base < kGroup ? elements - base : kGroup;
+    if constexpr (kFormat == MSQ_FMT_BF16) {
+      uint16_t h[kGroup];
+#pragma unroll
+      for (int i = 0; i < kGroup; ++i) h[i] = encodeBf16(g.v[i]);
+      uint16_t *out = reinterpret_cast<uint16_t *>(values);
+      if (vector_ok && valid == kGroup) {
+        uint4 packed;
+        packed.x = h[0] | (static_cast<uint32_t>(h[1]) << 16);
+        packed.y = h[2] | (static_cast<uint32_t>(h[3]) << 16);
+        packed.z = h[4] | (static_cast<uint32_t>(h[5]) << 16);
+        packed.w = h[6] | (static_cast<uint32_t>(h[7]) << 16);
+        __stcs(reinterpret_cast<uint4 *>(out + base), packed);
+      } else {
+        for (size_t i = 0; i < valid; ++i) out[base + i] = h[i];
+      }
+    } else if constexpr (kFormat == MSQ_FMT_FP8_E4M3FN ||
+                         kFormat == MSQ_FMT_FP8_E5M2) {
+      uint64_t packed = 0;
+#pragma unroll
+      for (int i = 0; i < kGroup; ++i) {
+        const uint32_t code = kFormat == MSQ_FMT_FP8_E4M3FN ? encodeE4M3(g.v[i])
+                                                           : encodeE5M2(g.v[i]);
+        packed |= static_cast<uint64_t>(code) << (8 * i);
+      }
+      storeBytes(values, base, packed, static_cast<int>(valid), vector_ok);
+    } else if constexpr (kFormat == MSQ_FMT_FP4_E2M1) {
+      // packFp4 (src/storage_codecs.cpp:138-146): low nibble = even index,
+      // the pad nibble of an odd tail is the code of +0 (= 0).
+      uint64_t packed = 0;
+#pragma unroll
+      for (int i = 0; i < kGroup; ++i) {
+        packed |= static_cast<uint64_t>(encodeE2M1(g.v[i])) << (4 * i);
+      }
+      storeBytes(values, base / 2, packed, static_cast<int>((valid + 1) / 2),
+                 vector_ok);
+    }
+    (void)scales;
+  }
+}
+
+// MX formats: 4 lanes x 8 elements per 32-element scale block.
+template <int kFormat>
+__global__ void __launch_bounds__(kThreads)
+encodeMxKernel(const float *__restrict__ source, size_t elements,
+               uint8_t *__restrict__ values, uint8_t *__restrict__ scales,
+               bool vector_ok) {
+  constexpr int kEmax = kFormat == MSQ_FMT_MXFP8_E4M3FN ? 8
+                        : kFormat == MSQ_FMT_MXFP8_E5M2 ? 15
+                                                        : 2;
+  const size_t blocks = (elements + 31) / 32;
+  const size_t groups = blocks * 4;  // whole blocks; lanes 0-3 share one
+  const size_t stride = static_cast<size_t>(gridDim.x) * blockDim.x;
+  // The loop condition is taken on the warp's first group so all 32 lanes
+  // run the same iterations (the full-mask shuffles need every lane).
+  const size_t first = blockIdx.x * static_cast<size_t>(blockDim.x) + threadIdx.x;
+  const size_t lane = threadIdx.x % 32;
+  for (size_t group = first; group - lane < groups; group += stride) {
+    const bool active = group < groups;
+    const size_t base = group * kGroup;
+    Group g;
+    if (active) {
+      g = loadGroup(source, base, elements, vector_ok);
+    } else {
+#pragma unroll
+      for (int i = 0; i < kGroup; ++i) g.v[i] = 0.0f;
+    }
+    float m = groupMaxFinite(g);
+    m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, 1));
+    m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, 2));
+    if (!active || base >= elements) continue;
+    const int e = mxExponent(m, kEmax);
+    const size_t valid = elements - base < kGroup ? elements - base : kGroup;
+    if (group % 4 == 0) scales[group / 4] = static_cast<uint8_t>(e + 127);
+    if constexpr (kFormat == MSQ_FMT_MXFP4_E2M1) {
+      uint64_t packed = 0;
+#pragma unroll
+      for (int i = 0; i < kGroup; ++i) {
+        packed |= static_cast<uint64_t>(encodeE2M1(mxDivide(g.v[i], e))) << (4 * i);
+      }
+      storeBytes(values, base / 2, packed, static_cast<int>((valid + 1) / 2),
+                 vector_ok);
+    } else {
+      uint64_t packed = 0;
+#pragma unroll
+      for (int i = 0; i < kGroup; ++i) {
+        const float scaled = mxDivide(g.v[i], e);
+        const uint32_t code = kFormat == MSQ_FMT_MXFP8_E4M3FN ? encodeE4M3(scaled)
+                                                              : encodeE5M2(scaled);
+        packed |= static_cast<uint64_t>(code) << (8 * i);
+      }
+      storeBytes(values, base, packed, static_cast<int>(valid), vector_ok);
+    }
+  }
+}
+
+// FP8 E4M3FN with one FP32 scale per contiguous row: s = max|row| / 448
+// (1 when the row has no nonzero finite value), code = E4M3(x / s).  One warp
+// per row: a max pass, then an encode pass (the row is re-read from L1/L2).
+__global__ void __launch_bounds__(kThreads)
+encodeRowScaleKernel(const float *__restrict__ source, size_t rows,
+                     size_t row_length, uint8_t *__restrict__ values,
+                     float *__restrict__ scales) {
+  const int lane = threadIdx.x % 32;
+  const size_t warps = static_cast<size_t>(gridDim.x) * (blockDim.x / 32);
+  for (size_t row = blockIdx.x * static_cast<size_t>(blockDim.x / 32) + threadIdx.x / 32;
+       row < rows; row += warps) {
+    const float *in = source + row * row_length;
+    float m = 0.0f;
+    for (size_t i = lane; i < row_length; i += 32) {
+      const float a = fabsf(in[i]);
+      if (a <= 3.402823466e38f) m = fmaxf(m, a);
+    }
+#pragma unroll
+    for (int s = 16; s > 0; s >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, s));
+    const float scale = m == 0.0f ? 1.0f : __fdiv_rn(m, 448.0f);
+    if (lane == 0) scales[row] = scale;
+    uint8_t *out = values + row * row_length;
+    for (size_t i = lane; i < row_length; i += 32) {
+      out[i] = encodeE4M3(__fdiv_rn(in[i], scale));
+    }
+  }
+}
+
+// ---------------------------------------------------------------- decoders
+
+template <int kFormat>
+__global__ void __launch_bounds__(kThreads)
+decodeKernel(const uint8_t *__restrict__ values, const uint8_t *__restrict__ scales,
+             size_t elements, float *__restrict__ output, bool vector_ok) {
+  const size_t groups = (elements + kGroup - 1) / kGroup;
+  for (size_t group = blockIdx.x * static_cast<size_t>(blockDim.x) + threadIdx.x;
+       group < groups; group += static_cast<size_t>(gridDim.x) * blockDim.x) {
+    const size_t base = group * kGroup;
+    const size_t valid = elements - base < kGroup ? elements - base : kGroup;
+    const bool full = vector_ok && valid == kGroup;
+    Group g;
+    if constexpr (kFormat == MSQ_FMT_BF16) {
+      const uint16_t *in = reinterpret_cast<const uint16_t *>(values);
+      if (full) {
+        const uint4 p = __ldcs(reinterpret_cast<const uint4 *>(in + base));
+        const uint32_t w[4] = {p.x, p.y, p.z, p.w};
+#pragma unroll
+        for (int i = 0; i < 4; ++i) {
+          g.v[2 * i] = decodeBf16(static_cast<uint16_t>(w[i] & 0xffffu));
+          g.v[2 * i + 1] = decodeBf16(static_cast<uint16_t>(w[i] >> 16));
+        }
+      } else {
+        for (int i = 0; i < kGroup; ++i)
+          g.v[i] = i < static_cast<int>(valid) ? decodeBf16(in[base + i]) : 0.0f;
+      }
+    } else if constexpr (kFormat == MSQ_FMT_FP4_E2M1 ||
+                         kFormat == MSQ_FMT_MXFP4_E2M1) {
+      uint32_t packed = 0;
+      if (full) {
+        packed = *reinterpret_cast<const uint32_t *>(values + base / 2);
+      } else {
+        for (size_t i = 0; i < (valid + 1) / 2; ++i)
+          packed |= static_cast<uint32_t>(values[base / 2 + i]) << (8 * i);
+      }
+      const uint32_t scale = kFormat == MSQ_FMT_MXFP4_E2M1 ? scales[base / 32] : 127u;
+#pragma unroll
+      for (int i = 0; i < kGroup; ++i) {
+        const float d = decodeE2M1((packed >> (4 * i)) & 0xfu);
+        g.v[i] = kFormat == MSQ_FMT_MXFP4_E2M1 ? mxScale(d, scale) : d;
+      }
+    } else {
+      uint64_t packed = 0;
+      if (full) {
+        packed = *reinterpret_cast<const uint64_t *>(values + base);
+      } else {
+        for (size_t i = 0; i < valid; ++i)
+          packed |= static_cast<uint64_t>(values[base + i]) << (8 * i);
+      }
+      constexpr bool kMx = kFormat == MSQ_FMT_MXFP8_E4M3FN ||
+                           kFormat == MSQ_FMT_MXFP8_E5M2;
+      constexpr bool kE4M3 = kFormat == MSQ_FMT_FP8_E4M3FN ||
+                             kFormat == MSQ_FMT_MXFP8_E4M3FN;
+      const uint32_t scale = kMx ? scales[base / 32] : 127u;
+#pragma unroll
+      for (int i = 0; i < kGroup; ++i) {
+        const uint32_t code = static_cast<uint32_t>(packed >> (8 * i)) & 0xffu;
+        const float d = kE4M3 ? decodeE4M3(code) : decodeE5M2(code);
+        g.v[i] = kMx ? mxScale(d, scale) : d;
+      }
+    }
+    storeGroup(output, base, elements, vector_ok, g);
+  }
+}
+
+__global__ void __launch_bounds__(kThreads)
+decodeRowScaleKernel(const uint8_t *__restrict__ values,
+                     const float *__restrict__ scales, size_t elements,
+                     size_t row_length, float *__restrict__ output) {
+  for (size_t i = blockIdx.x * static_cast<size_t>(blockDim.x) + threadIdx.x;
+       i < elements; i += static_cast<size_t>(gridDim.x) * blockDim.x) {
+    output[i] = decodeE4M3(values[i]) * scales[i / row_length];
+  }
+}
+
+bool aligned16(const void *p) {
+  return (reinterpret_cast<uintptr_t>(p) & 15u) == 0;
+}
+
+}  // namespace
+}  // namespace msq
+
+using namespace msq;
+
+extern "C" size_t msq_storage_bytes(int format, size_t elements) {
+  switch (format) {
+    case MSQ_FMT_FP32: return elements * 4;
+    case MSQ_FMT_BF16: return elements * 2;
+    case MSQ_FMT_FP8_E4M3FN:
+    case MSQ_FMT_FP8_E5M2:
+    case MSQ_FMT_MXFP8_E4M3FN:
+    case MSQ_FMT_MXFP8_E5M2:
+    case MSQ_FMT_FP8_E4M3FN_ROWSCALE: return elements;
+    case MSQ_FMT_FP4_E2M1:
+    case MSQ_FMT_MXFP4_E2M1: return (elements * 4 + 7) / 8;
+    default: return 0;
+  }
+}
+
+extern "C" size_t msq_scale_bytes(int format, size_t elements, size_t row_length) {
+  switch (format) {
+    case MSQ_FMT_MXFP8_E4M3FN:
+    case MSQ_FMT_MXFP8_E5M2:
+    case MSQ_FMT_MXFP4_E2M1: return (elements + 31) / 32;
+    case MSQ_FMT_FP8_E4M3FN_ROWSCALE:
+      return row_length == 0 ? 0 : (elements / row_length) * sizeof(float);
+    default: return 0;
+  }
+}
+
+extern "C" int msq_encode(msq_ctx *ctx, int format, const float *source,
+                          size_t elements, size_t row_length, uint8_t *values,
+                          uint8_t *scales) {
+  if (ctx == nullptr) return MSQ_ERR_INVALID_ARGUMENT;
+  if (elements == 0) return MSQ_OK;
+  if (source == nullptr || values == nullptr) {
+    return setError(ctx, MSQ_ERR_INVALID_ARGUMENT, "msq_encode: null buffer");
+  }
+  const bool needs_scales = msq_scale_bytes(format, elements, row_length ? row_length : 1) != 0;
+  if (needs_scales && scales == nullptr) {
+    return setError(ctx, MSQ_ERR_INVALID_ARGUMENT,
+                    "msq_encode: this format requires a scale plane");
+  }
+  const bool vec = aligned16(source) && aligned16(values);
+  const size_t groups = (elements + kGroup - 1) / kGroup;
+  const unsigned grid = gridFor(groups, kThreads);
+  cudaStream_t s = ctx->stream;
+  switch (format) {
+    case MSQ_FMT_FP32:
+      return cudaCheck(ctx, cudaMemcpyAsync(values, source, elements * 4,
+                                            cudaMemcpyDeviceToDevice, s),
+                       "msq_encode fp32 copy");
+    case MSQ_FMT_BF16:
+      encodeScalarKernel<MSQ_FMT_BF16><<<grid, kThreads, 0, s>>>(source, elements, values, scales, vec);
+      break;
+    case MSQ_FMT_FP8_E4M3FN:
+      encodeScalarKernel<MSQ_FMT_FP8_E4M3FN><<<grid, kThreads, 0, s>>>(source, elements, values, scales, vec);
+      break;
+    case MSQ_FMT_FP8_E5M2:
+      encodeScalarKernel<MSQ_FMT_FP8_E5M2><<<grid, kThreads, 0, s>>>(source, elements, values, scales, vec);
+      break;
+    case MSQ_FMT_FP4_E2M1:
+      encodeScalarKernel<MSQ_FMT_FP4_E2M1><<<grid, kThreads, 0, s>>>(source, elements, values, scales, vec);
+      break;
+    case MSQ_FMT_MXFP8_E4M3FN:
+      encodeMxKernel<MSQ_FMT_MXFP8_E4M3FN><<<gridFor((elements + 31) / 32 * 4, kThreads), kThreads, 0, s>>>(source, elements, values, scales, vec);
+      break;
+    case MSQ_FMT_MXFP8_E5M2:
+      encodeMxKernel<MSQ_FMT_MXFP8_E5M2><<<gridFor((elements + 31) / 32 * 4, kThreads), kThreads, 0, s>>>(source, elements, values, scales, vec);
+      break;
+    case MSQ_FMT_MXFP4_E2M1:
+      encodeMxKernel<MSQ_FMT_MXFP4_E2M1><<<gridFor((elements + 31) / 32 * 4, kThreads), kThreads, 0, s>>>(source, elements, values, scales, vec);
+      break;
+    case MSQ_FMT_FP8_E4M3FN_ROWSCALE: {
+      if (row_length == 0 || elements % row_length != 0) {
+        return setError(ctx, MSQ_ERR_INVALID_ARGUMENT,
+                        "msq_encode: elements must be a multiple of row_length");
+      }
+      const size_t rows = elements / row_length;
+      encodeRowScaleKernel<<<gridFor(rows * 32, kThreads), kThreads, 0, s>>>(
+          source, rows, row_length, values, reinterpret_cast<float *>(scales));
+      break;
+    }
+    default:
+      return setError(ctx, MSQ_ERR_INVALID_ARGUMENT, "msq_encode: unknown format");
+  }
+  return launched(ctx, "msq_encode");
+}
+
+extern "C" int msq_decode(msq_ctx *ctx, int format, const uint8_t *values,
+                          const uint8_t *scales, size_t elements,
+                          size_t row_length, float *output) {
+  if (ctx == nullptr) return MSQ_ERR_INVALID_ARGUMENT;
+  if (elements == 0) return MSQ_OK;
+  if (values == nullptr || output == nullptr) {
+    return setError(ctx, MSQ_ERR_INVALID_ARGUMENT, "msq_decode: null buffer");
+  }
+  const bool needs_scales = msq_scale_bytes(format, elements, row_length ? row_length : 1) != 0;
+  if (needs_scales && scales == nullptr) {
+    return setError(ctx, MSQ_ERR_INVALID_ARGUMENT,
+                    "msq_decode: this format requires a scale plane");
+  }
+  const bool vec = aligned16(values) && aligned16(output);
+  const size_t groups = (elements + kGroup - 1) / kGroup;
+  const unsigned grid = gridFor(groups, kThreads);
+  cudaStream_t s = ctx->stream;
+  switch (format) {
+    case MSQ_FMT_FP32:
+      return cudaCheck(ctx, cudaMemcpyAsync(output, values, elements * 4,
+                                            cudaMemcpyDeviceToDevice, s),
+                       "msq_decode fp32 copy");
+#define MSQ_DECODE_CASE(F) \
+    case F: decodeKernel<F><<<grid, kThreads, 0, s>>>(values, scales, elements, output, vec); break;
+    MSQ_DECODE_CASE(MSQ_FMT_BF16)
+    MSQ_DECODE_CASE(MSQ_FMT_FP8_E4M3FN)
+    MSQ_DECODE_CASE(MSQ_FMT_FP8_E5M2)
+    MSQ_DECODE_CASE(MSQ_FMT_MXFP8_E4M3FN)
+    MSQ_DECODE_CASE(MSQ_FMT_MXFP8_E5M2)
+    MSQ_DECODE_CASE(MSQ_FMT_FP4_E2M1)
+    MSQ_DECODE_CASE(MSQ_FMT_MXFP4_E2M1)
+#undef MSQ_DECODE_CASE
+    case MSQ_FMT_FP8_E4M3FN_ROWSCALE:
+      if (row_length == 0 || elements % row_length != 0) {
+        return setError(ctx, MSQ_ERR_INVALID_ARGUMENT,
+                        "msq_decode: elements must be a multiple of row_length");
+      }
+      decodeRowScaleKernel<<<gridFor(elements, kThreads), kThreads, 0, s>>>(
+          values, reinterpret_cast<const float *>(scales), elements, row_length, output);
+      break;
+    default:
+      return setError(ctx, MSQ_ERR_INVALID_ARGUMENT, "msq_decode: unknown format");
+  }
+  return launched(ctx, "msq_decode");
+}

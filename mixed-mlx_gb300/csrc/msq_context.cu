@@ -1,0 +1,184 @@
+// Context, error handling, batch-layout upload and scratch management.
+#include "msq_internal.cuh"
+
+#include <cstring>
+#include <string>
+
+namespace msq {
+
+int setError(msq_ctx *ctx, int code, const std::string &message) {
+  if (ctx != nullptr) ctx->error = message;
+  return code;
+}
+
+int cudaCheck(msq_ctx *ctx, cudaError_t status, const char *what) {
+  if (status == cudaSuccess) return MSQ_OK;
+  return setError(ctx, MSQ_ERR_CUDA,
+                  std::string(what) + ": " + cudaGetErrorString(status));
+}
+
+int launched(msq_ctx *ctx, const char *what) {
+  ++ctx->launches;
+  return cudaCheck(ctx, cudaGetLastError(), what);
+}
+
+int checkDeviceStatus(msq_ctx *ctx) {
+  int status = 0;
+  MSQ_TRY(cudaCheck(ctx,
+                    cudaMemcpyAsync(&status, ctx->d_status, sizeof(int),
+                                    cudaMemcpyDeviceToHost, ctx->stream),
+                    "device status read"));
+  MSQ_TRY(cudaCheck(ctx, cudaStreamSynchronize(ctx->stream), "device status sync"));
+  if (status != kStatusOk) {
+    MSQ_TRY(cudaCheck(ctx, cudaMemsetAsync(ctx->d_status, 0, sizeof(int), ctx->stream),
+                      "device status reset"));
+    const char *why = status == kStatusMbarrierTimeout   ? "bounded mbarrier wait expired"
+                      : status == kStatusTmemAllocFailed ? "TMEM allocation failed"
+                      : status == kStatusBadOrder        ? "matrix order outside kernel limits"
+                                                         : "kernel reported an error";
+    return setError(ctx, MSQ_ERR_DEVICE_STATUS,
+                    std::string("device status ") + std::to_string(status) + ": " + why);
+  }
+  return MSQ_OK;
+}
+
+static uint64_t hashLayout(const int32_t *n, const int64_t *offset, int count) {
+  uint64_t h = 1469598103934665603ull ^ static_cast<uint64_t>(count);
+  for (int i = 0; i < count; ++i) {
+    h = (h ^ static_cast<uint64_t>(n[i])) * 1099511628211ull;
+    h = (h ^ static_cast<uint64_t>(offset[i])) * 1099511628211ull;
+  }
+  return h;
+}
+
+const DeviceBatch *prepareBatch(msq_ctx *ctx, const int32_t *n,
+                                const int64_t *offset, int count) {
+  if (count <= 0 || n == nullptr || offset == nullptr) {
+    setError(ctx, MSQ_ERR_INVALID_ARGUMENT, "batch: empty or null layout");
+    return nullptr;
+  }
+  const uint64_t key = hashLayout(n, offset, count);
+  for (DeviceBatch *b : ctx->batches) {
+    if (b->key == key && b->count == count &&
+        std::memcmp(b->host_n.data(), n, count * sizeof(int32_t)) == 0 &&
+        std::memcmp(b->host_offset.data(), offset, count * sizeof(int64_t)) == 0) {
+      return b;
+    }
+  }
+  auto *b = new DeviceBatch;
+  b->count = count;
+  b->key = key;
+  b->host_n.assign(n, n + count);
+  b->host_offset.assign(offset, offset + count);
+  b->host_eig_offset.resize(count);
+  int64_t eig = 0;
+  for (int i = 0; i < count; ++i) {
+    if (n[i] < 1 || offset[i] < 0) {
+      delete b;
+      setError(ctx, MSQ_ERR_INVALID_ARGUMENT, "batch: order < 1 or negative offset");
+      return nullptr;
+    }
+    b->host_eig_offset[i] = eig;
+    eig += n[i];
+    b->total_elements += static_cast<int64_t>(n[i]) * n[i];
+    if (n[i] > b->max_n) b->max_n = n[i];
+  }
+  b->total_order = eig;
+  const size_t bytes = count * (sizeof(int32_t) + 2 * sizeof(int64_t));
+  char *device = nullptr;
+  if (cudaCheck(ctx, cudaMalloc(&device, bytes + 64), "batch upload alloc") != MSQ_OK) {
+    delete b;
+    return nullptr;
+  }
+  b->offset = reinterpret_cast<int64_t *>(device);
+  b->eig_offset = b->offset + count;
+  b->n = reinterpret_cast<int32_t *>(b->eig_offset + count);
+  // Synchronous copies: the layout is uploaded once and then reused.
+  if (cudaCheck(ctx, cudaMemcpy(b->offset, offset, count * sizeof(int64_t), cudaMemcpyHostToDevice), "batch upload") != MSQ_OK ||
+      cudaCheck(ctx, cudaMemcpy(b->eig_offset, b->host_eig_offset.data(), count * sizeof(int64_t), cudaMemcpyHostToDevice), "batch upload") != MSQ_OK ||
+      cudaCheck(ctx, cudaMemcpy(b->n, n, count * sizeof(int32_t), cudaMemcpyHostToDevice), "batch upload") != MSQ_OK) {
+    cudaFree(device);
+    delete b;
+    return nullptr;
+  }
+  if (ctx->batches.size() >= 8) {
+    DeviceBatch *old = ctx->batches.front();
+    cudaFree(old->offset);
+    delete old;
+    ctx->batches.erase(ctx->batches.begin());
+  }
+  ctx->batches.push_back(b);
+  return b;
+}
+
+void *scratch(msq_ctx *ctx, size_t bytes) {
+  if (bytes <= ctx->scratch_bytes) return ctx->scratch;
+  if (ctx->scratch != nullptr) {
+    cudaStreamSynchronize(ctx->stream);
+    cudaFree(ctx->scratch);
+    ctx->scratch = nullptr;
+    ctx->scratch_bytes = 0;
+  }
+  const size_t rounded = (bytes + (1u << 20) - 1) & ~static_cast<size_t>((1u << 20) - 1);
+  if (cudaCheck(ctx, cudaMalloc(&ctx->scratch, rounded), "scratch alloc") != MSQ_OK) {
+    ctx->scratch = nullptr;
+    return nullptr;
+  }
+  ctx->scratch_bytes = rounded;
+  return ctx->scratch;
+}
+
+}  // namespace msq
+
+using namespace msq;
+
+extern "C" int msq_create(msq_ctx **out, int device) {
+  if (out == nullptr) return MSQ_ERR_INVALID_ARGUMENT;
+  *out = nullptr;
+  auto *ctx = new msq_ctx;
+  ctx->device = device;
+  if (cudaCheck(ctx, cudaSetDevice(device), "cudaSetDevice") != MSQ_OK ||
+      cudaCheck(ctx, cudaMalloc(&ctx->d_status, 256), "status alloc") != MSQ_OK ||
+      cudaCheck(ctx, cudaMemset(ctx->d_status, 0, 256), "status reset") != MSQ_OK) {
+    static thread_local std::string last;
+    last = ctx->error;
+    delete ctx;
+    return MSQ_ERR_CUDA;
+  }
+  *out = ctx;
+  return MSQ_OK;
+}
+
+extern "C" void msq_destroy(msq_ctx *ctx) {
+  if (ctx == nullptr) return;
+  cudaSetDevice(ctx->device);
+  if (ctx->stream != nullptr) cudaStreamSynchronize(ctx->stream);
+  else cudaDeviceSynchronize();
+  for (DeviceBatch *b : ctx->batches) {
+    cudaFree(b->offset);
+    delete b;
+  }
+  if (ctx->scratch != nullptr) cudaFree(ctx->scratch);
+  if (ctx->d_status != nullptr) cudaFree(ctx->d_status);
+  delete ctx;
+}
+
+extern "C" const char *msq_last_error(const msq_ctx *ctx) {
+  return ctx == nullptr ? "null context" : ctx->error.c_str();
+}
+
+extern "C" int msq_set_stream(msq_ctx *ctx, void *stream) {
+  if (ctx == nullptr) return MSQ_ERR_INVALID_ARGUMENT;
+  ctx->stream = static_cast<cudaStream_t>(stream);
+  return MSQ_OK;
+}
+
+extern "C" int msq_synchronize(msq_ctx *ctx) {
+  if (ctx == nullptr) return MSQ_ERR_INVALID_ARGUMENT;
+  MSQ_TRY(cudaCheck(ctx, cudaStreamSynchronize(ctx->stream), "msq_synchronize"));
+  return checkDeviceStatus(ctx);
+}
+
+extern "C" uint64_t msq_launch_count(const msq_ctx *ctx) {
+  return ctx == nullptr ? 0 : ctx->launches;
+}

@@ -1,0 +1,90 @@
+// Internal declarations shared by the CUDA translation units of libmsq_cuda.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstddef>
+#include <cstdint>
+#include <string>
+#include <vector>
+
+#include "../../include/msq_cuda.h"
+
+namespace msq {
+
+// GB300: 152 SMs on two dies.  Grids of streaming kernels are sized as a
+// multiple of this so every SM gets the same number of resident CTAs.
+constexpr int kSmCount = 152;
+
+// Device-side status words (one int each) written by kernels that bound a
+// wait or check an index; read back by msq_check_device_status().
+enum DeviceStatus : int {
+  kStatusOk = 0,
+  kStatusJacobiOrderTooLarge = 1,
+  kStatusMbarrierTimeout = 2,
+  kStatusTmemAllocFailed = 3,
+  kStatusBadOrder = 4,
+};
+
+// Batched layout uploaded to the device once per distinct (n, offset) set.
+struct DeviceBatch {
+  int count = 0;
+  int32_t *n = nullptr;         // [count]
+  int64_t *offset = nullptr;    // [count] element offset of matrix i
+  int64_t *eig_offset = nullptr;// [count] prefix sum of n
+  int64_t total_elements = 0;   // sum n^2
+  int64_t total_order = 0;      // sum n
+  int max_n = 0;
+  uint64_t key = 0;
+  std::vector<int32_t> host_n;
+  std::vector<int64_t> host_offset;
+  std::vector<int64_t> host_eig_offset;
+};
+
+}  // namespace msq
+
+struct msq_ctx {
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  std::string error;
+  uint64_t launches = 0;
+  int *d_status = nullptr;  // device status word
+  // Grow-only scratch owned by the context (freed in msq_destroy).
+  void *scratch = nullptr;
+  size_t scratch_bytes = 0;
+  // Batch layouts cached by content hash (small: a few entries).
+  std::vector<msq::DeviceBatch *> batches;
+};
+
+namespace msq {
+
+int setError(msq_ctx *ctx, int code, const std::string &message);
+int cudaCheck(msq_ctx *ctx, cudaError_t status, const char *what);
+// Checks the last launch error and counts one launch.
+int launched(msq_ctx *ctx, const char *what);
+// Returns MSQ_ERR_DEVICE_STATUS (and resets the word) if a kernel set it.
+int checkDeviceStatus(msq_ctx *ctx);
+// Uploads (or finds cached) the batch layout; null on error (ctx->error set).
+const DeviceBatch *prepareBatch(msq_ctx *ctx, const int32_t *n,
+                                const int64_t *offset, int count);
+// Grow-only context scratch, stream-ordered.
+void *scratch(msq_ctx *ctx, size_t bytes);
+
+inline unsigned gridFor(size_t work_items, unsigned threads,
+                        unsigned ctas_per_sm = 8) {
+  size_t blocks = (work_items + threads - 1) / threads;
+  const size_t cap = static_cast<size_t>(kSmCount) * ctas_per_sm;
+  if (blocks > cap) blocks = cap;
+  if (blocks == 0) blocks = 1;
+  return static_cast<unsigned>(blocks);
+}
+
+}  // namespace msq
+
+#define MSQ_TRY(expr)               \
+  do {                              \
+    const int msq_status_ = (expr); \
+    if (msq_status_ != MSQ_OK) {    \
+      return msq_status_;           \
+    }                               \
+  } while (0)

@@ -1,0 +1,370 @@
+/*
+ * msq_oracle.c — CPU restatement of the reference's algorithms for the SPD
+ * square-root hot path.  TEST INFRASTRUCTURE: only tests/, the smoke check
+ * and bench.py's CPU-baseline leg load this library, and only as the checker
+ * (or as the timed CPU baseline); the product path never calls it.
+ *
+ * Pinned against the reference itself: tests/golden holds vectors produced by
+ * the reference's own host codec (oracle/_ref, compiled from the reference
+ * sources) and tests/test_oracle.py checks this file against them.
+ *
+ * Contents
+ *  - codecs: the reference host codec (src/storage_codecs.cpp) restated with
+ *    its linear nearest-code scan, so it is independent of the integer
+ *    rounding the CUDA kernels use;
+ *  - the FP8-E4M3 per-row-scale format (no reference counterpart);
+ *  - the parallel-order two-sided Jacobi of metal_mixed_sqrt.metal:1319-1444
+ *    with the round-robin schedule of src/metal_solver.cpp:50-79, angles in
+ *    FP64, FP32 storage, convergence-tested;
+ *  - the float-float ("WorkingFloat") residual of
+ *    metal_mixed_sqrt.metal:1278-1317, 1927-1942.
+ */
+#include <math.h>
+#include <stdint.h>
+#include <stdlib.h>
+#include <string.h>
+
+/* ------------------------------------------------------------------ codecs */
+
+/* floatToBf16, src/storage_codecs.cpp:16-28 */
+uint16_t msqo_encode_bf16(float value) {
+  uint32_t bits;
+  memcpy(&bits, &value, 4);
+  uint32_t rounded = bits >> 16;
+  uint32_t remainder = bits & 0xffffu;
+  if (remainder > 0x8000u || (remainder == 0x8000u && (rounded & 1u) != 0))
+    ++rounded;
+  if ((bits & 0x7f800000u) == 0x7f800000u && (bits & 0x007fffffu) != 0)
+    rounded |= 0x0040u;
+  return (uint16_t)rounded;
+}
+
+/* bf16ToFloat, :30-35 */
+float msqo_decode_bf16(uint16_t value) {
+  uint32_t bits = (uint32_t)value << 16;
+  float f;
+  memcpy(&f, &bits, 4);
+  return f;
+}
+
+/* fp8E4M3FnToFloat, :37-49 */
+float msqo_decode_e4m3(uint8_t value) {
+  float sign = (value & 0x80u) == 0 ? 1.0f : -1.0f;
+  unsigned exponent = (value >> 3) & 0x0fu, fraction = value & 0x07u;
+  if (exponent == 0x0fu && fraction == 0x07u) return copysignf(NAN, sign);
+  float magnitude = exponent == 0
+                        ? ldexpf((float)fraction, -9)
+                        : ldexpf(1.0f + (float)fraction / 8.0f, (int)exponent - 7);
+  return copysignf(magnitude, sign);
+}
+
+/* fp8E5M2ToFloat, :51-66 */
+float msqo_decode_e5m2(uint8_t value) {
+  float sign = (value & 0x80u) == 0 ? 1.0f : -1.0f;
+  unsigned exponent = (value >> 2) & 0x1fu, fraction = value & 0x03u;
+  if (exponent == 0x1fu)
+    return fraction == 0 ? copysignf(INFINITY, sign) : copysignf(NAN, sign);
+  float magnitude = exponent == 0
+                        ? ldexpf((float)fraction, -16)
+                        : ldexpf(1.0f + (float)fraction / 4.0f, (int)exponent - 15);
+  return copysignf(magnitude, sign);
+}
+
+/* fp4E2M1ToFloat, :68-77 */
+float msqo_decode_e2m1(uint8_t value) {
+  float sign = (value & 0x08u) == 0 ? 1.0f : -1.0f;
+  unsigned exponent = (value >> 1) & 0x03u, fraction = value & 0x01u;
+  float magnitude = exponent == 0
+                        ? (float)fraction * 0.5f
+                        : ldexpf(1.0f + (float)fraction * 0.5f, (int)exponent - 1);
+  return copysignf(magnitude, sign);
+}
+
+/* nearestFiniteCode, :79-94: scan all finite codes, ties to the even code */
+static uint8_t nearest_code(float magnitude, unsigned maximum_code,
+                            float (*decode)(uint8_t)) {
+  uint8_t nearest = 0;
+  float best = fabsf(magnitude - decode(0));
+  for (unsigned code = 1; code <= maximum_code; ++code) {
+    float distance = fabsf(magnitude - decode((uint8_t)code));
+    if (distance < best || (distance == best && (code & 1u) == 0 && (nearest & 1u) != 0)) {
+      nearest = (uint8_t)code;
+      best = distance;
+    }
+  }
+  return nearest;
+}
+
+/* floatToFp8E4M3Fn, :96-108 */
+uint8_t msqo_encode_e4m3(float value) {
+  uint8_t sign = signbit(value) ? 0x80u : 0u;
+  if (isnan(value)) return sign | 0x7fu;
+  if (value == 0.0f) return sign;
+  if (isinf(value) || fabsf(value) > 448.0f) return sign | 0x7eu;
+  return sign | nearest_code(fabsf(value), 0x7eu, msqo_decode_e4m3);
+}
+
+/* floatToFp8E5M2, :110-125 */
+uint8_t msqo_encode_e5m2(float value) {
+  uint8_t sign = signbit(value) ? 0x80u : 0u;
+  if (isnan(value)) return sign | 0x7eu;
+  if (value == 0.0f) return sign;
+  if (isinf(value)) return sign | 0x7cu;
+  if (fabsf(value) > 57344.0f) return sign | 0x7bu;
+  return sign | nearest_code(fabsf(value), 0x7bu, msqo_decode_e5m2);
+}
+
+/* floatToFp4E2M1, :127-136 */
+uint8_t msqo_encode_e2m1(float value) {
+  uint8_t sign = signbit(value) ? 0x08u : 0u;
+  if (isnan(value) || value == 0.0f) return sign;
+  if (isinf(value) || fabsf(value) > 6.0f) return sign | 0x07u;
+  return sign | nearest_code(fabsf(value), 0x07u, msqo_decode_e2m1);
+}
+
+/* mxScaleExponent, :148-162 */
+static int mx_exponent(const float *v, size_t begin, size_t end, int emax) {
+  float maximum = 0.0f;
+  for (size_t i = begin; i < end; ++i)
+    if (isfinite(v[i]) && fabsf(v[i]) > maximum) maximum = fabsf(v[i]);
+  if (maximum == 0.0f) return 0;
+  int e = ilogbf(maximum) - emax;
+  return e < -127 ? -127 : (e > 128 ? 128 : e);
+}
+
+/* Format ids follow HostStorageCodec (src/precision.hpp:24-33) plus 8 =
+ * FP8-E4M3 with a per-row FP32 scale. */
+size_t msqo_storage_bytes(int format, size_t elements) {
+  switch (format) {
+    case 0: return elements * 4;
+    case 1: return elements * 2;
+    case 6: case 7: return (elements * 4 + 7) / 8;
+    default: return elements;
+  }
+}
+
+/* copyValuesToStorage + packFp4/packMxfp8/packMxfp4, :138-313.
+ * row_length is used only by format 8. Returns 0 on success. */
+int msqo_encode(int format, const float *src, size_t elements, size_t row_length,
+                uint8_t *values, uint8_t *scales) {
+  switch (format) {
+    case 0: memcpy(values, src, elements * 4); return 0;
+    case 1:
+      for (size_t i = 0; i < elements; ++i) ((uint16_t *)values)[i] = msqo_encode_bf16(src[i]);
+      return 0;
+    case 2: for (size_t i = 0; i < elements; ++i) values[i] = msqo_encode_e4m3(src[i]); return 0;
+    case 3: for (size_t i = 0; i < elements; ++i) values[i] = msqo_encode_e5m2(src[i]); return 0;
+    case 4: case 5: {
+      int emax = format == 4 ? 8 : 15;
+      for (size_t b = 0, blk = 0; b < elements; b += 32, ++blk) {
+        size_t end = b + 32 < elements ? b + 32 : elements;
+        int e = mx_exponent(src, b, end, emax);
+        scales[blk] = (uint8_t)(e + 127);
+        float scale = ldexpf(1.0f, e);
+        for (size_t i = b; i < end; ++i)
+          values[i] = format == 4 ? msqo_encode_e4m3(src[i] / scale) : msqo_encode_e5m2(src[i] / scale);
+      }
+      return 0;
+    }
+    case 6:
+      for (size_t i = 0; i < elements; i += 2) {
+        uint8_t lo = msqo_encode_e2m1(src[i]);
+        uint8_t hi = i + 1 < elements ? msqo_encode_e2m1(src[i + 1]) : 0u;
+        values[i / 2] = (uint8_t)(lo | (hi << 4));
+      }
+      return 0;
+    case 7:
+      for (size_t b = 0, blk = 0; b < elements; b += 32, ++blk) {
+        size_t end = b + 32 < elements ? b + 32 : elements;
+        int e = mx_exponent(src, b, end, 2);
+        scales[blk] = (uint8_t)(e + 127);
+        float scale = ldexpf(1.0f, e);
+        for (size_t i = b; i < end; i += 2) {
+          uint8_t lo = msqo_encode_e2m1(src[i] / scale);
+          uint8_t hi = i + 1 < end ? msqo_encode_e2m1(src[i + 1] / scale) : 0u;
+          values[i / 2] = (uint8_t)(lo | (hi << 4));
+        }
+      }
+      return 0;
+    case 8: {
+      if (row_length == 0 || elements % row_length) return 1;
+      float *row_scales = (float *)scales;
+      for (size_t r = 0; r < elements / row_length; ++r) {
+        const float *row = src + r * row_length;
+        float m = 0.0f;
+        for (size_t i = 0; i < row_length; ++i)
+          if (isfinite(row[i]) && fabsf(row[i]) > m) m = fabsf(row[i]);
+        float s = m == 0.0f ? 1.0f : m / 448.0f;
+        row_scales[r] = s;
+        for (size_t i = 0; i < row_length; ++i) values[r * row_length + i] = msqo_encode_e4m3(row[i] / s);
+      }
+      return 0;
+    }
+    default: return 1;
+  }
+}
+
+/* storageValueAt, :323-374, for every index */
+int msqo_decode(int format, const uint8_t *values, const uint8_t *scales,
+                size_t elements, size_t row_length, float *out) {
+  for (size_t i = 0; i < elements; ++i) {
+    switch (format) {
+      case 0: memcpy(&out[i], values + 4 * i, 4); break;
+      case 1: out[i] = msqo_decode_bf16(((const uint16_t *)values)[i]); break;
+      case 2: out[i] = msqo_decode_e4m3(values[i]); break;
+      case 3: out[i] = msqo_decode_e5m2(values[i]); break;
+      case 4: out[i] = ldexpf(msqo_decode_e4m3(values[i]), (int)scales[i / 32] - 127); break;
+      case 5: out[i] = ldexpf(msqo_decode_e5m2(values[i]), (int)scales[i / 32] - 127); break;
+      case 6: out[i] = msqo_decode_e2m1((values[i / 2] >> ((i & 1u) * 4)) & 0x0fu); break;
+      case 7:
+        out[i] = ldexpf(msqo_decode_e2m1((values[i / 2] >> ((i & 1u) * 4)) & 0x0fu),
+                        (int)scales[i / 32] - 127);
+        break;
+      case 8:
+        if (row_length == 0) return 1;
+        out[i] = msqo_decode_e4m3(values[i]) * ((const float *)scales)[i / row_length];
+        break;
+      default: return 1;
+    }
+  }
+  return 0;
+}
+
+/* ---------------------------------------------------------------- Jacobi */
+
+/* Round-robin ("chess tournament") pairing of makeJacobiSchedule
+ * (src/metal_solver.cpp:50-79) computed arithmetically: participants are
+ * rotated right by one (slot 0 fixed) after every round, so in round r slot k
+ * (k >= 1) holds participant 1 + ((k - 1 - r) mod (m - 1)), m = padded order.
+ * Pair j joins slots j and m-1-j. */
+static unsigned rr_slot(unsigned slot, unsigned round, unsigned m) {
+  if (slot == 0) return 0;
+  unsigned k = (slot - 1 + (m - 1) - (round % (m - 1))) % (m - 1);
+  return 1 + k;
+}
+
+void msqo_jacobi_pair(unsigned order, unsigned round, unsigned pair,
+                      unsigned *p, unsigned *q) {
+  unsigned m = order + (order & 1u);
+  unsigned a = rr_slot(pair, round, m), b = rr_slot(m - 1 - pair, round, m);
+  *p = a < b ? a : b;
+  *q = a < b ? b : a;
+}
+
+/* One parallel-order cyclic Jacobi solve of the symmetric FP32 matrix a
+ * (n x n, column-major, overwritten), vectors v (n x n), eigenvalues w.
+ * Per round: angles of all disjoint pairs from the round's start matrix in
+ * FP64 (the reference computes them in FP32, metal_mixed_sqrt.metal:
+ * 1331-1361: tau = (a_qq - a_pp) / (2 a_pq), t = sign(tau) / (|tau| +
+ * sqrt(1 + tau^2)), c = 1/sqrt(1 + t^2), s = t c), then A <- J^T A J and
+ * V <- V J with the 4-term update of :1363-1411.  Sweeps continue until
+ * off(A) <= tol * ||A||_F (FP64) or max_sweeps.  Returns sweeps done. */
+int msqo_jacobi(float *a, float *v, float *w, unsigned n, double tol,
+                int max_sweeps, double *off_ratio) {
+  unsigned m = n + (n & 1u);
+  unsigned pairs = m / 2;
+  float *next = (float *)malloc(sizeof(float) * n * n);
+  float *vn = (float *)malloc(sizeof(float) * n * n);
+  float *c = (float *)malloc(sizeof(float) * (m + 1));
+  float *s = (float *)malloc(sizeof(float) * (m + 1));
+  unsigned *partner = (unsigned *)malloc(sizeof(unsigned) * (m + 1));
+  for (unsigned j = 0; j < n; ++j)
+    for (unsigned i = 0; i < n; ++i) v[i + j * n] = i == j ? 1.0f : 0.0f;
+  double norm2 = 0.0;
+  for (size_t i = 0; i < (size_t)n * n; ++i) norm2 += (double)a[i] * a[i];
+  double norm = sqrt(norm2);
+  int sweeps = 0;
+  double ratio = 0.0;
+  for (;;) {
+    double off2 = 0.0;
+    for (unsigned j = 0; j < n; ++j)
+      for (unsigned i = 0; i < n; ++i)
+        if (i != j) off2 += (double)a[i + j * n] * a[i + j * n];
+    ratio = norm > 0 ? sqrt(off2) / norm : 0.0;
+    if (ratio <= tol || sweeps >= max_sweeps) break;
+    for (unsigned round = 0; round + 1 < m; ++round) {
+      for (unsigned k = 0; k < pairs; ++k) {
+        unsigned p, q;
+        msqo_jacobi_pair(n, round, k, &p, &q);
+        partner[p] = q;
+        partner[q] = p;
+        double cs = 1.0, sn = 0.0;
+        if (q < n) {
+          double app = a[p + p * n], aqq = a[q + q * n];
+          double apq = 0.5 * ((double)a[p + q * n] + (double)a[q + p * n]);
+          if (apq != 0.0) {
+            double tau = (aqq - app) / (2.0 * apq);
+            double t = copysign(1.0 / (fabs(tau) + sqrt(1.0 + tau * tau)), tau);
+            cs = 1.0 / sqrt(1.0 + t * t);
+            sn = t * cs;
+          }
+        }
+        /* rotation seen from p: (c, -s); from q: (c, +s) */
+        c[p] = (float)cs; s[p] = (float)-sn;
+        c[q] = (float)cs; s[q] = (float)sn;
+      }
+      for (unsigned col = 0; col < n; ++col) {
+        unsigned cp = partner[col] < n ? partner[col] : col;
+        float cc = c[col], cs_ = partner[col] < n ? s[col] : 0.0f;
+        for (unsigned row = 0; row < n; ++row) {
+          unsigned rp = partner[row] < n ? partner[row] : row;
+          float rc = c[row], rs = partner[row] < n ? s[row] : 0.0f;
+          next[row + col * n] = rc * cc * a[row + col * n] + rs * cc * a[rp + col * n] +
+                                rc * cs_ * a[row + cp * n] + rs * cs_ * a[rp + cp * n];
+          vn[row + col * n] = cc * v[row + col * n] + cs_ * v[row + cp * n];
+        }
+      }
+      memcpy(a, next, sizeof(float) * n * n);
+      memcpy(v, vn, sizeof(float) * n * n);
+    }
+    ++sweeps;
+  }
+  for (unsigned i = 0; i < n; ++i) w[i] = a[i + i * n];
+  if (off_ratio) *off_ratio = ratio;
+  free(next); free(vn); free(c); free(s); free(partner);
+  return sweeps;
+}
+
+/* --------------------------------------------------- float-float residual */
+
+typedef struct { float hi, lo; } ff;
+
+static ff ff_norm(float hi, float lo) { float s = hi + lo; ff r = {s, lo - (s - hi)}; return r; }
+
+/* working_add, metal_mixed_sqrt.metal:1285-1291 */
+static ff ff_add(ff a, ff b) {
+  float s = a.hi + b.hi, vr = s - a.hi;
+  float e = (a.hi - (s - vr)) + (b.hi - vr) + a.lo + b.lo;
+  return ff_norm(s, e);
+}
+
+/* working_multiply, :1293-1299 */
+static ff ff_mul(ff a, ff b) {
+  float p = a.hi * b.hi;
+  float e = fmaf(a.hi, b.hi, -p) + a.hi * b.lo + a.lo * b.hi + a.lo * b.lo;
+  return ff_norm(p, e);
+}
+
+/* working_residual, :1927-1942: R = A - X X in float-float; returns
+ * ||R||_F / ||A||_F accumulated in FP64. */
+double msqo_ff_residual(const float *a, const float *x_hi, const float *x_lo,
+                        unsigned n, float *r_out) {
+  double rn = 0.0, an = 0.0;
+  for (unsigned col = 0; col < n; ++col)
+    for (unsigned row = 0; row < n; ++row) {
+      ff sum = {0.0f, 0.0f};
+      for (unsigned k = 0; k < n; ++k) {
+        ff l = {x_hi[row + k * n], x_lo ? x_lo[row + k * n] : 0.0f};
+        ff r = {x_hi[k + col * n], x_lo ? x_lo[k + col * n] : 0.0f};
+        sum = ff_add(sum, ff_mul(l, r));
+      }
+      ff m = {a[row + col * n], 0.0f};
+      ff neg = {-sum.hi, -sum.lo};
+      ff res = ff_add(m, neg);
+      double rv = (double)res.hi + res.lo;
+      if (r_out) r_out[row + col * n] = res.hi + res.lo;
+      rn += rv * rv;
+      an += (double)a[row + col * n] * a[row + col * n];
+    }
+  return sqrt(rn / an);
+}

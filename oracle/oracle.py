@@ -1,0 +1,328 @@
+"""CPU oracle for the SPD square-root hot path — TEST INFRASTRUCTURE.
+
+Only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg import
+this module, and only as the checker (or as the timed CPU baseline).  The
+product (libmsq_cuda.so and its Python host layer) never imports it.
+
+Parts
+  * libmsq_oracle.so (msq_oracle.c, built by build_oracle()): the reference
+    host codecs restated with their linear nearest-code scan, the
+    parallel-order Jacobi and the float-float residual.
+  * numpy restatements of the reference's FP64 oracle and definitions
+    (src/numerics.cpp, src/accelerate_backend.cpp:555-607) and of its CPU
+    plain method runAccelerateCase (src/accelerate_backend.cpp:803-1091).
+  * seeded generators for the workload families (Gaussian-QR, Wishart,
+    clustered, power-law) and the reference's controlled family
+    (makeSpdMatrix, src/numerics.cpp:141-195).
+  * ref(): the reference's own compiled CPU code (oracle/_ref/libmsq_ref.so,
+    built from the reference sources where they exist), used to pin the
+    restatements; absent where the reference tree is absent.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+import subprocess
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ORACLE_LIB = os.path.join(HERE, "libmsq_oracle.so")
+REF_LIB = os.path.join(HERE, "_ref", "libmsq_ref.so")
+
+_P = ctypes.c_void_p
+
+
+def build_oracle() -> str:
+    src = os.path.join(HERE, "msq_oracle.c")
+    if (not os.path.exists(ORACLE_LIB) or
+            os.path.getmtime(ORACLE_LIB) < os.path.getmtime(src)):
+        subprocess.run(["gcc", "-O2", "-std=c11", "-fPIC", "-shared", "-ffp-contract=off",
+                        src, "-o", ORACLE_LIB, "-lm"], check=True)
+    return ORACLE_LIB
+
+
+_ORACLE = None
+
+
+def olib() -> ctypes.CDLL:
+    global _ORACLE
+    if _ORACLE is None:
+        build_oracle()
+        lib = ctypes.CDLL(ORACLE_LIB)
+        lib.msqo_encode.argtypes = [ctypes.c_int, _P, ctypes.c_size_t, ctypes.c_size_t, _P, _P]
+        lib.msqo_decode.argtypes = [ctypes.c_int, _P, _P, ctypes.c_size_t, ctypes.c_size_t, _P]
+        lib.msqo_storage_bytes.argtypes = [ctypes.c_int, ctypes.c_size_t]
+        lib.msqo_storage_bytes.restype = ctypes.c_size_t
+        lib.msqo_jacobi.argtypes = [_P, _P, _P, ctypes.c_uint, ctypes.c_double, ctypes.c_int,
+                                    ctypes.POINTER(ctypes.c_double)]
+        lib.msqo_jacobi_pair.argtypes = [ctypes.c_uint, ctypes.c_uint, ctypes.c_uint,
+                                         ctypes.POINTER(ctypes.c_uint), ctypes.POINTER(ctypes.c_uint)]
+        lib.msqo_ff_residual.argtypes = [_P, _P, _P, ctypes.c_uint, _P]
+        lib.msqo_ff_residual.restype = ctypes.c_double
+        _ORACLE = lib
+    return _ORACLE
+
+
+def scale_bytes(fmt: int, elements: int, row_length: int = 0) -> int:
+    if fmt in (4, 5, 7):
+        return (elements + 31) // 32
+    if fmt == 8:
+        return (elements // row_length) * 4
+    return 0
+
+
+def encode(fmt: int, x: np.ndarray, row_length: int = 0):
+    """copyToStorage restated: returns (values uint8, scales uint8 | None)."""
+    x = np.ascontiguousarray(x, dtype=np.float32)
+    n = x.size
+    values = np.zeros(max(olib().msqo_storage_bytes(fmt, n), 1), dtype=np.uint8)
+    sb = scale_bytes(fmt, n, row_length)
+    scales = np.zeros(max(sb, 1), dtype=np.uint8)
+    rc = olib().msqo_encode(fmt, x.ctypes.data, n, row_length, values.ctypes.data,
+                            scales.ctypes.data)
+    if rc:
+        raise ValueError("oracle encode failed")
+    return values[:olib().msqo_storage_bytes(fmt, n)], (scales[:sb] if sb else None)
+
+
+def decode(fmt: int, values: np.ndarray, scales, elements: int, row_length: int = 0):
+    """storageValueAt restated for every index."""
+    out = np.zeros(elements, dtype=np.float32)
+    values = np.ascontiguousarray(values, dtype=np.uint8)
+    sc = np.ascontiguousarray(scales, dtype=np.uint8) if scales is not None else np.zeros(1, np.uint8)
+    rc = olib().msqo_decode(fmt, values.ctypes.data, sc.ctypes.data, elements, row_length,
+                            out.ctypes.data)
+    if rc:
+        raise ValueError("oracle decode failed")
+    return out
+
+
+def jacobi_pair(order: int, rnd: int, pair: int) -> tuple[int, int]:
+    p, q = ctypes.c_uint(), ctypes.c_uint()
+    olib().msqo_jacobi_pair(order, rnd, pair, ctypes.byref(p), ctypes.byref(q))
+    return p.value, q.value
+
+
+def jacobi(a: np.ndarray, tol: float = 1e-7, max_sweeps: int = 15):
+    """Parallel-order two-sided Jacobi (FP32 storage, FP64 angles)."""
+    n = a.shape[0]
+    A = np.asfortranarray(a, dtype=np.float32).copy(order="F")
+    V = np.zeros((n, n), dtype=np.float32, order="F")
+    w = np.zeros(n, dtype=np.float32)
+    ratio = ctypes.c_double()
+    sweeps = olib().msqo_jacobi(A.ctypes.data, V.ctypes.data, w.ctypes.data, n, tol, max_sweeps,
+                                ctypes.byref(ratio))
+    return w, V, sweeps, ratio.value
+
+
+def ff_residual(a: np.ndarray, x_hi: np.ndarray, x_lo=None):
+    """float-float residual R = A - X X; returns (relative norm, R)."""
+    n = a.shape[0]
+    A = np.asfortranarray(a, dtype=np.float32)
+    H = np.asfortranarray(x_hi, dtype=np.float32)
+    L = np.asfortranarray(x_lo, dtype=np.float32) if x_lo is not None else None
+    R = np.zeros((n, n), dtype=np.float32, order="F")
+    rel = olib().msqo_ff_residual(A.ctypes.data, H.ctypes.data,
+                                  L.ctypes.data if L is not None else None, n, R.ctypes.data)
+    return rel, R
+
+
+# ---------------------------------------------------------------- FP64 oracle
+
+def reference_root(a: np.ndarray) -> np.ndarray:
+    """symmetricReferenceRoot (src/accelerate_backend.cpp:594-607): FP64
+    eigendecomposition, V diag(sqrt(lambda)) V^T, symmetrised."""
+    a = np.asarray(a, dtype=np.float64)
+    w, v = np.linalg.eigh(a)
+    if not np.all(w > 0):
+        raise ValueError("The FP64 reference has a nonpositive eigenvalue.")
+    root = (v * np.sqrt(w)) @ v.T
+    return 0.5 * (root + root.T)
+
+
+def relative_residual(a: np.ndarray, x: np.ndarray) -> float:
+    """relativeResidual (src/numerics.cpp:213-228): ||A - X X^T||_F/||A||_F."""
+    a = np.asarray(a, dtype=np.float64)
+    x = np.asarray(x, dtype=np.float64)
+    return float(np.linalg.norm(a - x @ x.T) / np.linalg.norm(a))
+
+
+def relative_error(x: np.ndarray, ref: np.ndarray) -> float:
+    """relativeError (src/numerics.cpp:230-240)."""
+    x = np.asarray(x, dtype=np.float64)
+    ref = np.asarray(ref, dtype=np.float64)
+    return float(np.linalg.norm(x - ref) / np.linalg.norm(ref))
+
+
+# ---------------------------------------------------------------- generators
+
+def _orthogonal(n: int, rng: np.random.Generator) -> np.ndarray:
+    g = rng.standard_normal((n, n))
+    q, r = np.linalg.qr(g)
+    return q * np.sign(np.diag(r))
+
+
+def spd_from_spectrum(lam: np.ndarray, rng: np.random.Generator) -> np.ndarray:
+    q = _orthogonal(lam.size, rng)
+    a = (q * lam) @ q.T
+    return 0.5 * (a + a.T)
+
+
+def loguniform_spectrum(n: int, cond: float, rng: np.random.Generator) -> np.ndarray:
+    lam = np.exp(rng.uniform(np.log(1.0 / cond), 0.0, n))
+    if n >= 2:
+        lam[0], lam[-1] = 1.0 / cond, 1.0
+    return lam
+
+
+def spd_loguniform(n: int, cond: float, seed: int) -> np.ndarray:
+    """A = Q diag(lambda) Q^T, Q from QR of a seeded N(0,1) matrix (sign-fixed),
+    lambda log-uniform on [1/cond, 1]."""
+    rng = np.random.default_rng(seed)
+    return spd_from_spectrum(loguniform_spectrum(n, cond, rng), rng)
+
+
+def spd_clustered(n: int, cond: float, seed: int) -> np.ndarray:
+    """90% of lambda in [0.9, 1.1], 10% log-uniform down to 1/cond."""
+    rng = np.random.default_rng(seed)
+    k = max(1, n // 10)
+    lam = np.concatenate([rng.uniform(0.9, 1.1, n - k),
+                          np.exp(rng.uniform(np.log(1.0 / cond), np.log(0.9), k))])
+    lam[-1] = 1.0 / cond
+    return spd_from_spectrum(lam, rng)
+
+
+def spd_power_law(n: int, seed: int) -> np.ndarray:
+    """lambda_i proportional to i^-2."""
+    rng = np.random.default_rng(seed)
+    lam = 1.0 / np.arange(1, n + 1, dtype=np.float64) ** 2
+    return spd_from_spectrum(lam, rng)
+
+
+def wishart(n: int, seed: int, ratio: int = 2, shift: float = 1e-6) -> np.ndarray:
+    """A = X^T X / m + shift I, X ~ N(0,1) of shape m x n, m = ratio * n."""
+    rng = np.random.default_rng(seed)
+    m = ratio * n
+    x = rng.standard_normal((m, n))
+    a = x.T @ x / m + shift * np.eye(n)
+    return 0.5 * (a + a.T)
+
+
+def wishart_orders(count: int, lo: int, hi: int, seed: int) -> np.ndarray:
+    """n log-uniform integer in [lo, hi]."""
+    rng = np.random.default_rng(seed)
+    n = np.floor(np.exp(rng.uniform(np.log(lo), np.log(hi + 1), count))).astype(np.int32)
+    return np.clip(n, lo, hi)
+
+
+def controlled(n: int, cond: float) -> np.ndarray:
+    """makeSpdMatrix (src/numerics.cpp:141-195): deterministic sin/cos basis,
+    Gram-Schmidt, geometric eigenvalues cond^(k/(n-1))."""
+    rows = np.arange(n, dtype=np.float64)[:, None]
+    cols = np.arange(n, dtype=np.float64)[None, :]
+    v = np.sin(0.173 * (rows + 1) * (cols + 2)) + np.cos(0.117 * (rows + 3) * (cols + 1))
+    for c in range(n):
+        for p in range(c):
+            v[:, c] -= (v[:, p] @ v[:, c]) * v[:, p]
+        v[:, c] /= np.linalg.norm(v[:, c])
+    lam = np.exp(np.log(cond) * np.arange(n) / max(1, n - 1))
+    return (v * lam) @ v.T
+
+
+# ------------------------------------------------- CPU plain method (port)
+
+def plain_method(a: np.ndarray, max_corrections: int = 12, tol: float = 1e-12):
+    """runAccelerateCase, symmetric branch (src/accelerate_backend.cpp:803-1091):
+    FP32 ssyevd -> X0 = (V diag s) V^T in FP32 -> FP64 residual -> frozen-basis
+    corrections C = (V^T R V) o 1/(s_i+s_j), E = V C V^T until residual <= tol.
+    Returns (root FP64, residual history)."""
+    import scipy.linalg as sla
+    a = np.asarray(a, dtype=np.float64)
+    n = a.shape[0]
+    w, v = sla.eigh(a.astype(np.float32), driver="evd", overwrite_a=False, check_finite=False)
+    if not np.all(w > 0):
+        raise ValueError("Accelerate ssyevd returned a nonpositive eigenvalue.")
+    s = np.sqrt(w).astype(np.float32)
+    v = v.astype(np.float32)
+    x0 = (v * s) @ v.T
+    root = x0.astype(np.float64)
+    root = 0.5 * (root + root.T)
+    denom = (s[:, None] + s[None, :]).astype(np.float32)
+    anorm = np.linalg.norm(a)
+
+    def residual(x):
+        r = a - x @ x.T
+        return r, float(np.linalg.norm(r) / anorm)
+
+    r, res = residual(root)
+    history = [res]
+    it = 0
+    while res > tol and it < max_corrections and np.isfinite(res):
+        r32 = r.astype(np.float32)
+        c = v.T @ (r32 @ v)
+        c = (0.5 * (c + c.T)) / denom
+        e = (v @ c) @ v.T
+        root = root + e.astype(np.float64)
+        root = 0.5 * (root + root.T)
+        it += 1
+        r, res = residual(root)
+        history.append(res)
+    return root, history
+
+
+# ------------------------------------------- the reference's own CPU code
+
+_REF = None
+
+
+def ref_available() -> bool:
+    return os.path.exists(REF_LIB)
+
+
+def ref() -> ctypes.CDLL:
+    """The reference's CPU path compiled from its own sources (x86 build
+    container only)."""
+    global _REF
+    if _REF is None:
+        lib = ctypes.CDLL(REF_LIB)
+        lib.ref_last_error.restype = ctypes.c_char_p
+        lib.ref_storage_bytes.argtypes = [ctypes.c_int, ctypes.c_size_t]
+        lib.ref_storage_bytes.restype = ctypes.c_size_t
+        lib.ref_scale_bytes.argtypes = [ctypes.c_int, ctypes.c_size_t]
+        lib.ref_scale_bytes.restype = ctypes.c_size_t
+        lib.ref_encode.argtypes = [ctypes.c_int, _P, ctypes.c_size_t, _P, _P]
+        lib.ref_decode.argtypes = [ctypes.c_int, _P, _P, ctypes.c_size_t, _P]
+        lib.ref_make_spd.argtypes = [ctypes.c_size_t, ctypes.c_double, _P]
+        lib.ref_reference_root.argtypes = [_P, ctypes.c_size_t, _P]
+        lib.ref_relative_residual.argtypes = [_P, _P, ctypes.c_size_t]
+        lib.ref_relative_residual.restype = ctypes.c_double
+        lib.ref_relative_error.argtypes = [_P, _P, ctypes.c_size_t]
+        lib.ref_relative_error.restype = ctypes.c_double
+        lib.ref_run_accelerate.argtypes = [_P, ctypes.c_size_t, ctypes.c_double, ctypes.c_size_t,
+                                           ctypes.c_double, _P, _P, ctypes.c_size_t]
+        _REF = lib
+    return _REF
+
+
+def ref_encode(fmt: int, x: np.ndarray):
+    lib = ref()
+    x = np.ascontiguousarray(x, dtype=np.float32)
+    n = x.size
+    values = np.zeros(max(lib.ref_storage_bytes(fmt, n), 1), dtype=np.uint8)
+    sb = lib.ref_scale_bytes(fmt, n)
+    scales = np.zeros(max(sb, 1), dtype=np.uint8)
+    if lib.ref_encode(fmt, x.ctypes.data, n, values.ctypes.data, scales.ctypes.data if sb else None):
+        raise ValueError(lib.ref_last_error().decode())
+    return values[:lib.ref_storage_bytes(fmt, n)], (scales[:sb] if sb else None)
+
+
+def ref_decode(fmt: int, values: np.ndarray, scales, elements: int):
+    lib = ref()
+    out = np.zeros(elements, dtype=np.float32)
+    values = np.ascontiguousarray(values, dtype=np.uint8)
+    sc = np.ascontiguousarray(scales, dtype=np.uint8) if scales is not None else None
+    if lib.ref_decode(fmt, values.ctypes.data, sc.ctypes.data if sc is not None else None,
+                      elements, out.ctypes.data):
+        raise ValueError(lib.ref_last_error().decode())
+    return out

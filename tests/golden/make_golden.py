@@ -1,0 +1,113 @@
+"""Generate tests/golden/*.npz from the reference's own CPU code.
+
+Runs only where the reference sources are present: oracle/Makefile compiles
+them (src/storage_codecs.cpp, src/numerics.cpp, src/accelerate_backend.cpp,
+...) into oracle/_ref/libmsq_ref.so, and this script records their outputs:
+
+  codecs.npz     inputs (specials, boundary values, the fixture rule of
+                 tests/matrix_codec.cpp:39-78, N(0,1), Student-t(3), wide
+                 sign*2^U(-30,30), midpoints of every code pair and their
+                 float neighbours) with the reference's encoded values,
+                 scale planes and decoded FP32 bits for codecs 0..7.
+  numerics.npz   makeSpdMatrix(n, cond) outputs, symmetricReferenceRoot of
+                 them, and runAccelerateCase (src/accelerate_backend.cpp:
+                 803-1091) residual/forward-error histories.
+
+Usage: make -C oracle && python tests/golden/make_golden.py
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, os.path.join(HERE, "..", "..", "oracle"))
+import oracle as O  # noqa: E402
+
+F32 = np.float32
+
+
+def fixture_matrix(order: int) -> np.ndarray:
+    """The boundary fixture rule of tests/matrix_codec.cpp:39-78 (restated)."""
+    values = np.array([0.0, -0.0, 0.125, 0.25, 0.375, 0.5, 0.625, 0.75, 0.875, 1.0,
+                       1.00048828125, 1.00146484375, 1.0625, 1.1875, 1.25, 1.375, 1.75,
+                       1.875, 2.0, 2.125, 2.5, 2.75, 3.0, 3.5, 4.0, 4.5, 5.0, 5.5, 6.0, 6.5,
+                       7.0, 7.5], dtype=F32)
+    src = np.zeros(order * order, dtype=F32)
+    for col in range(1, order):
+        for row in range(1, order):
+            e = (row % 7) - 3 + 2 * (col // 32) + (col % 3) - 1
+            v = np.ldexp(values[(13 * row + 7 * col) % 32], e).astype(F32)
+            if (row + col) % 2:
+                v = -v
+            src[row + col * order] = v
+    bounds = [-0.0, 2.0 ** -25, 3 * 2.0 ** -25, 2.0 ** -17, 3 * 2.0 ** -17, 2.0 ** -10,
+              3 * 2.0 ** -10, 448.0, 464.0, -464.0, 57344.0, 61440.0, 65504.0, 65520.0]
+    for i, b in enumerate(bounds):
+        src[(i + 1) + (i + 2) * order] = F32(b)
+    return src
+
+
+def codec_inputs() -> np.ndarray:
+    rng = np.random.default_rng(20261203)
+    f = np.finfo(F32)
+    specials = np.array([0.0, -0.0, np.inf, -np.inf, np.nan, -np.nan, f.max, -f.max, f.tiny,
+                         -f.tiny, 2.0 ** -149, -2.0 ** -149, 2.0 ** -133, 1.0, -1.0, 6.1, 512.0,
+                         1.0625, 1.1875], dtype=F32)
+    parts = [specials, fixture_matrix(96)]
+    for fmt in (2, 3):
+        v = O.decode(fmt, np.arange(256, dtype=np.uint8), None, 256).astype(np.float64)
+        v = np.unique(np.abs(v[np.isfinite(v)]))
+        mid = ((v[1:] + v[:-1]) / 2).astype(F32)
+        parts += [mid, np.nextafter(mid, F32(np.inf)), np.nextafter(mid, F32(-np.inf)), -mid]
+    v4 = np.array([0, 0.5, 1, 1.5, 2, 3, 4, 6], dtype=np.float64)
+    mid = ((v4[1:] + v4[:-1]) / 2).astype(F32)
+    parts += [mid, np.nextafter(mid, F32(np.inf)), np.nextafter(mid, F32(-np.inf)), -mid]
+    parts += [rng.standard_normal(4096).astype(F32), rng.standard_t(3, 4096).astype(F32),
+              (np.sign(rng.standard_normal(4096)) * 2.0 ** rng.uniform(-30, 30, 4096)).astype(F32)]
+    x = np.concatenate(parts).astype(F32)
+    # pad to a multiple of 32 plus a ragged tail of 7 (exercise partial blocks)
+    pad = (-x.size) % 32 + 7
+    return np.concatenate([x, rng.standard_normal(pad).astype(F32)])
+
+
+def main() -> None:
+    if not O.ref_available():
+        raise SystemExit("oracle/_ref/libmsq_ref.so missing: run `make -C oracle` first")
+    lib = O.ref()
+    assert lib.ref_check_codecs() == 0, lib.ref_last_error()
+    x = codec_inputs()
+    out = {"x": x}
+    for fmt in range(8):
+        v, s = O.ref_encode(fmt, x)
+        d = O.ref_decode(fmt, v, s, x.size)
+        out[f"values_{fmt}"] = v
+        out[f"scales_{fmt}"] = s if s is not None else np.zeros(0, np.uint8)
+        out[f"decoded_bits_{fmt}"] = d.view(np.uint32)
+    np.savez_compressed(os.path.join(HERE, "codecs.npz"), **out)
+
+    num = {}
+    for n, cond in [(16, 10.0), (64, 1e3), (96, 1e2)]:
+        a = np.zeros(n * n)
+        assert lib.ref_make_spd(n, cond, a.ctypes.data) == 0
+        root = np.zeros(n * n)
+        assert lib.ref_reference_root(a.ctypes.data, n, root.ctypes.data) == 0
+        summary = np.zeros(8)
+        hist = np.zeros(2 * 16)
+        assert lib.ref_run_accelerate(a.ctypes.data, n, cond, 12, 1e-12, summary.ctypes.data,
+                                      hist.ctypes.data, 16) == 0, lib.ref_last_error()
+        key = f"n{n}"
+        num[f"{key}_a"] = a
+        num[f"{key}_root"] = root
+        num[f"{key}_summary"] = summary
+        num[f"{key}_history"] = hist[:2 * (int(summary[2]) + 1)]
+        num[f"{key}_cond"] = np.array([cond])
+    np.savez_compressed(os.path.join(HERE, "numerics.npz"), **num)
+    print("wrote", os.path.join(HERE, "codecs.npz"), os.path.join(HERE, "numerics.npz"))
+
+
+if __name__ == "__main__":
+    main()

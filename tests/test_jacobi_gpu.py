@@ -1,0 +1,77 @@
+"""GPU Jacobi parity: eigenpairs against the FP64 oracle and the CPU
+restatement of the reference's parallel-order Jacobi."""
+import numpy as np
+import pytest
+
+import oracle as O
+
+pytestmark = pytest.mark.gpu
+
+
+def _run(ctx, msq, mats, tol=1e-7, max_sweeps=15):
+    import torch
+    b = msq.Batch.from_orders([m.shape[0] for m in mats])
+    a = torch.from_numpy(b.pack(mats)).cuda()
+    v, w, sweeps, off = ctx.jacobi(a, b, tol, max_sweeps)
+    torch.cuda.synchronize()
+    ctx.synchronize()
+    vs = b.unpack(v.cpu().numpy())
+    eo = b.eig_offset
+    ws = [w.cpu().numpy()[eo[i]:eo[i] + b.n[i]].astype(np.float64) for i in range(b.count)]
+    return vs, ws, sweeps.cpu().numpy(), off.cpu().numpy(), b.unpack(a.cpu().numpy())
+
+
+@pytest.mark.parametrize("n", [1, 2, 3, 16, 17, 31, 32, 33, 96, 128, 255, 256, 336])
+def test_single_matrix_eigenpairs(ctx, msq, n):
+    a = O.spd_loguniform(n, 1e3, seed=100 + n)
+    vs, ws, sweeps, off, af = _run(ctx, msq, [a])
+    v, w = vs[0], ws[0]
+    ref = np.linalg.eigvalsh(a)
+    scale = np.abs(ref).max()
+    np.testing.assert_allclose(np.sort(w), ref, rtol=0, atol=5e-6 * scale)
+    np.testing.assert_allclose(v.T @ v, np.eye(n), atol=5e-6 * max(1, np.sqrt(n) / 4))
+    # A V = V diag(w)
+    resid = np.linalg.norm(a @ v - v * w) / np.linalg.norm(a)
+    assert resid < 1e-5
+    assert off[0] <= 1e-7 or n == 1
+    # the converged matrix is written back, nearly diagonal
+    assert np.linalg.norm(af[0] - np.diag(np.diag(af[0]))) <= 1e-6 * np.linalg.norm(a)
+
+
+@pytest.mark.parametrize("n", [337, 400, 512])
+def test_global_path_orders(ctx, msq, n):
+    a = O.wishart(n, seed=n)
+    vs, ws, sweeps, off, _ = _run(ctx, msq, [a])
+    ref = np.linalg.eigvalsh(a)
+    np.testing.assert_allclose(np.sort(ws[0]), ref, rtol=0, atol=5e-6 * np.abs(ref).max())
+    assert np.linalg.norm(a @ vs[0] - vs[0] * ws[0]) / np.linalg.norm(a) < 2e-5
+
+
+def test_matches_cpu_restatement_sweep_for_sweep(ctx, msq):
+    """Same pairing, same FP64 angle formula, FP32 storage: the GPU and the CPU
+    restatement take the same number of sweeps and agree to FP32 rounding."""
+    for n in (8, 24, 65):
+        a = O.spd_loguniform(n, 1e2, seed=n)
+        w_o, v_o, sw_o, off_o = O.jacobi(a, 1e-7, 15)
+        vs, ws, sweeps, off, _ = _run(ctx, msq, [a])
+        assert sweeps[0] == sw_o
+        np.testing.assert_allclose(ws[0], w_o, rtol=0, atol=1e-5 * np.abs(w_o).max())
+
+
+def test_uneven_batch(ctx, msq):
+    rng = np.random.default_rng(9)
+    orders = O.wishart_orders(64, 16, 512, seed=4)
+    mats = [O.wishart(int(n), seed=i) for i, n in enumerate(orders)]
+    vs, ws, sweeps, off, _ = _run(ctx, msq, mats)
+    for a, v, w in zip(mats, vs, ws):
+        ref = np.linalg.eigvalsh(a)
+        np.testing.assert_allclose(np.sort(w), ref, rtol=0, atol=1e-5 * np.abs(ref).max())
+    assert np.all(off <= 1e-7)
+
+
+def test_sweep_budget_and_tolerance(ctx, msq):
+    a = O.spd_loguniform(64, 1e4, seed=1)
+    _, _, sweeps, off, _ = _run(ctx, msq, [a], tol=1e-7, max_sweeps=2)
+    assert sweeps[0] == 2 and off[0] > 1e-7
+    _, _, sweeps, off, _ = _run(ctx, msq, [a], tol=1e-2, max_sweeps=15)
+    assert off[0] <= 1e-2 and sweeps[0] < 8
