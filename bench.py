@@ -1,0 +1,370 @@
+"""Benchmark: batched SPD square roots on one GB300 (or N replicas).
+
+Workload (the batched configuration the throughput target is stated on):
+4096 Wishart covariances A = X^T X / m + 1e-6 I, X ~ N(0,1) of shape m x n,
+m = 2n, n log-uniform integer in [16, 512], FP32 input, seeded.  One step =
+one msq_solve_batched call over the whole batch with the low-bit plan (BF16
+factor on tcgen05 + Sylvester sweeps, FP32 fallback for any matrix whose
+float-float residual misses 1e-5).  value = matrices meeting
+||A - X^2||_F/||A||_F <= 1e-5 per second.  The plain FP32 path (Jacobi to
+1e-7, FP32 reconstruction) is timed beside it as the denominator of the
+low-bit speed-up.
+
+Usage: python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+Under torchrun each rank solves its own batch (weak scaling, no collective
+on the data path); rank 0 prints one JSON line.
+"""
+from __future__ import annotations
+
+import argparse
+import importlib
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = ("SPD sqrt solves/s at rel. residual ≤1e-5: low-bit+Sylvester vs plain FP32, "
+          "1×GB300")
+TOL = 1e-5
+COUNT = 4096
+N_LO, N_HI = 16, 512
+
+
+def workload_orders(count: int, seed: int) -> np.ndarray:
+    rng = np.random.default_rng(seed)
+    n = np.floor(np.exp(rng.uniform(np.log(N_LO), np.log(N_HI + 1), count))).astype(np.int32)
+    return np.clip(n, N_LO, N_HI)
+
+
+def make_batch(msq, torch, orders, seed, device):
+    """Wishart matrices generated on the GPU (FP64), stored FP32, packed."""
+    batch = msq.Batch.from_orders(orders)
+    flat = torch.zeros(batch.total, dtype=torch.float32, device=device)
+    g = torch.Generator(device=device).manual_seed(seed)
+    for i, n in enumerate(orders):
+        n = int(n)
+        x = torch.randn(2 * n, n, generator=g, device=device, dtype=torch.float64)
+        a = x.T @ x / (2 * n) + 1e-6 * torch.eye(n, device=device, dtype=torch.float64)
+        a = 0.5 * (a + a.T)
+        o = int(batch.offset[i])
+        flat[o:o + n * n] = a.T.reshape(-1).to(torch.float32)  # column-major
+    return batch, flat
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+    QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device: int):
+        self.device = device
+        self.proc = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.QUERY}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except OSError:
+            self.proc = None
+        return self
+
+    def __exit__(self, *exc):
+        self.lines = []
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                out, _ = self.proc.communicate(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+                out, _ = self.proc.communicate()
+            self.lines = [l for l in out.splitlines() if l.strip()]
+
+    def summary(self) -> dict:
+        sm, mx, reasons = [], 0.0, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in getattr(self, "lines", []):
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                mx = max(mx, float(parts[2]))
+            except ValueError:
+                continue
+            for name, flag in zip(names, parts[5:9]):
+                if flag.lower().startswith("active"):
+                    reasons.add(name)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": mx or None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def cpu_baseline(oracle, mats, budget_s: float) -> dict:
+    """The reference's CPU plain method (runAccelerateCase restated in the
+    oracle) on a stratified sample of the batch, bounded to ~budget_s."""
+    order = np.argsort([m.shape[0] for m in mats])
+    stride = max(1, len(order) // 64)
+    sample = order[::stride]
+    rng = np.random.default_rng(0)
+    rng.shuffle(sample)
+    done, t_used, ok = 0, 0.0, 0
+    for idx in sample:
+        t0 = time.perf_counter()
+        root, hist = oracle.plain_method(mats[idx], 12, TOL)
+        t_used += time.perf_counter() - t0
+        done += 1
+        ok += hist[-1] <= TOL
+        if t_used > budget_s:
+            break
+    # scale the stratified sample's mean time to the whole batch
+    per_solve = t_used / done
+    cores = os.cpu_count() or 1
+    return {"value": (ok / done) / per_solve, "unit": "solves/s", "cores": cores,
+            "kind": "port",
+            "sample": f"{done} of {len(mats)} matrices (stratified by n), "
+                      f"{t_used:.1f}s, OpenBLAS threads={os.environ.get('OPENBLAS_NUM_THREADS', cores)}"}
+
+
+def run_reference(args):
+    """--impl reference: the reference's CPU path (oracle port of
+    runAccelerateCase; the reference's own build is x86-only here) on the
+    host cores, same metric and workload, bounded samples per step."""
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle as O
+    orders = workload_orders(COUNT, 1234)
+    rng = np.random.default_rng(7)
+    pick = rng.choice(COUNT, 48, replace=False)
+    mats = {int(i): O.wishart(int(orders[i]), seed=int(i)) for i in pick}
+    for _ in range(args.warmup):
+        O.plain_method(mats[int(pick[0])], 12, TOL)
+    times, oks = [], 0
+    for step in range(args.steps):
+        t0 = time.perf_counter()
+        done = 0
+        for i in pick:
+            root, hist = O.plain_method(mats[int(i)], 12, TOL)
+            oks += hist[-1] <= TOL
+            done += 1
+            if time.perf_counter() - t0 > 20:
+                break
+        times.append((time.perf_counter() - t0) / done)
+    per_solve = statistics.mean(times)
+    value = 1.0 / per_solve
+    cores = os.cpu_count() or 1
+    line = {"metric": METRIC, "value": value, "unit": "solves/s", "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": per_solve * COUNT * 1e3,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "fp32",
+            "data": "synthetic", "impl": "reference",
+            "config": {"workload": f"{COUNT} Wishart SPD (m=2n), n log-uniform [{N_LO},{N_HI}], tol 1e-5"},
+            "cpu_baseline": {"value": value, "unit": "solves/s", "cores": cores, "kind": "port",
+                             "sample": f"48 random matrices of the batch per step, <=20 s per step"},
+            "e2e": {"value": value, "unit": "solves/s", "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def timing_report(msq, ctx) -> dict:
+    import ctypes
+    buf = ctypes.create_string_buffer(1 << 16)
+    msq.lib().msq_timing_end(ctx.handle, buf, len(buf))
+    rows = {}
+    for line in buf.value.decode().splitlines():
+        name, cnt, ms = line.split("\t")
+        rows[name] = (int(cnt), float(ms))
+    return rows
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--count", type=int, default=COUNT)
+    ap.add_argument("--sweeps", type=int, default=1)
+    ap.add_argument("--jacobi-tol", type=float, default=1e-4)
+    ap.add_argument("--no-cpu", action="store_true")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        return run_reference(args)
+
+    import torch
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    torch.cuda.set_device(local)
+    device = torch.device("cuda", local)
+    msq = importlib.import_module("mixed-mlx_gb300")
+    ctx = msq.Context(local)
+    stream = torch.cuda.current_stream(device)
+
+    orders = workload_orders(args.count, 1234 + rank)
+    batch, a = make_batch(msq, torch, orders, 99 + rank, device)
+    torch.cuda.synchronize()
+    low_plan = [msq.plan(msq.PLAN_BF16, args.sweeps, args.jacobi_tol, 15)] * batch.count
+    fp32_plan = [msq.plan(msq.PLAN_FP32, 0, 1e-7, 15)] * batch.count
+    root = torch.empty_like(a)
+
+    def barrier():
+        if world > 1:
+            torch.distributed.barrier()
+        torch.cuda.synchronize()
+
+    def timed(plans, steps, warmup, collect_timing=False):
+        for _ in range(warmup):
+            ctx.solve_batched(a, batch, plans, TOL, out=root)
+        barrier()
+        start, end = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        l0 = ctx.launches
+        if collect_timing:
+            msq.lib().msq_timing_begin(ctx.handle)
+        accepted = []
+        start.record(stream)
+        for _ in range(steps):
+            _, res = ctx.solve_batched(a, batch, plans, TOL, out=root)
+            accepted.append(sum(r.final_residual <= TOL for r in res))
+        end.record(stream)
+        barrier()
+        rows = timing_report(msq, ctx) if collect_timing else {}
+        ms = start.elapsed_time(end) / steps
+        return ms, statistics.mean(accepted), ctx.launches - l0, res, rows
+
+    # plain FP32 path (denominator)
+    ms_plain, acc_plain, _, res_plain, _ = timed(fp32_plan, max(1, args.steps // 2), 1)
+    # low-bit + Sylvester path (headline), clocks sampled while it runs
+    with ClockSampler(local) as clocks:
+        ms, acc, launches, res, rows = timed(low_plan, args.steps, args.warmup, True)
+    # max over ranks
+    t = torch.tensor([ms], device=device)
+    if world > 1:
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+    ms_max = float(t.item())
+    value = acc * world / (ms_max / 1e3)
+
+    # end to end: pinned host input, H2D + solve + D2H of the roots per step
+    host_in = torch.empty(batch.total, dtype=torch.float32, pin_memory=True)
+    host_in.copy_(a.cpu())
+    host_out = torch.empty(batch.total, dtype=torch.float32, pin_memory=True)
+    a_e2e = torch.empty_like(a)
+    ctx.solve_batched(a, batch, low_plan, TOL, out=root)
+    barrier()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e2e_steps = max(1, args.steps // 2)
+    e2e_acc = []
+    e0.record(stream)
+    for _ in range(e2e_steps):
+        a_e2e.copy_(host_in, non_blocking=True)
+        _, r_e = ctx.solve_batched(a_e2e, batch, low_plan, TOL, out=root)
+        host_out.copy_(root, non_blocking=True)
+        e2e_acc.append(sum(r.final_residual <= TOL for r in r_e))
+    e1.record(stream)
+    barrier()
+    e2e_ms = e0.elapsed_time(e1) / e2e_steps
+    e2e_value = statistics.mean(e2e_acc) * world / (e2e_ms / 1e3)
+
+    if rank != 0:
+        if world > 1:
+            torch.distributed.barrier()
+        return
+
+    # accuracy vs the FP64 oracle on a stratified sample (outside timing)
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle as O
+    roots = root.cpu().numpy()
+    a_host = a.cpu().numpy()
+    mats = batch.unpack(a_host)
+    xs = batch.unpack(roots)
+    idx = np.argsort(orders)[:: max(1, batch.count // 128)]
+    errs = [O.relative_error(xs[i], O.reference_root(mats[i])) for i in idx]
+    resid = [O.relative_residual(mats[i], xs[i]) for i in idx]
+    fallback = sum(r.fallback for r in res)
+
+    # roofline of the dominant kernel (largest share of the timed region)
+    top = max(rows.items(), key=lambda kv: kv[1][1]) if rows else ("", (0, 0.0))
+    total_ms = sum(v[1] for v in rows.values()) or 1.0
+    sweeps = np.array([r.jacobi_sweeps for r in res], dtype=np.float64)
+    n64 = orders.astype(np.float64)
+    peaks = {}
+    try:
+        peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+    except OSError:
+        pass
+    hbm = peaks.get("hbm_gbs", 6800.0)
+    bf16 = peaks.get("bf16_tflops", 1900.0)
+    name, (cnt, tot) = top
+    avg_ms = tot / max(cnt, 1)
+    if name.startswith("jacobi sweep"):
+        # 16 n^2 bytes per sweep (FP32 A and V read + written once: the
+        # blocked-streaming ideal), per launch = total over the step / launches
+        per_step_bytes = float(np.sum(16.0 * n64 ** 2 * sweeps))
+        per_launch = per_step_bytes * args.steps / max(cnt, 1)
+        achieved = per_launch / (avg_ms / 1e3) / 1e9
+        roof = {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",
+                "frac": achieved / hbm, "traffic": None, "kernel": name}
+    elif name.startswith("jacobi replay"):
+        per_step_bytes = float(np.sum(8.0 * n64 ** 2 * sweeps))
+        per_launch = per_step_bytes * args.steps / max(cnt, 1)
+        achieved = per_launch / (avg_ms / 1e3) / 1e9
+        roof = {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",
+                "frac": achieved / hbm, "traffic": None, "kernel": name}
+    else:
+        flops = float(np.sum(2.0 * n64 ** 3))
+        achieved = flops / (avg_ms / 1e3) / 1e12
+        roof = {"bound": "tensor", "achieved": achieved, "peak": bf16, "unit": "TFLOP/s",
+                "frac": achieved / bf16, "traffic": None, "kernel": name}
+    roof["share"] = tot / total_ms
+    roof["peak_source"] = "measured (MEASURED_PEAKS.json)" if peaks else "fallback"
+
+    cpu = None
+    if not args.no_cpu:
+        cpu = cpu_baseline(O, mats, 15.0)
+
+    line = {
+        "metric": METRIC, "value": value, "unit": "solves/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_max,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "bf16",
+        "data": "synthetic (seeded Wishart, generated on device)",
+        "config": {"workload": f"{batch.count} Wishart SPD A=X^T X/m+1e-6 I (m=2n), n log-uniform "
+                               f"[{N_LO},{N_HI}], FP32 input, BF16 plan + {args.sweeps} Sylvester "
+                               f"sweep(s), FP32 fallback, tol 1e-5",
+                   "matrices": batch.count, "sum_n3": float(np.sum(n64 ** 3)),
+                   "l2": "inputs larger than L2 (%.0f MB)" % (batch.total * 4 / 1e6),
+                   "jacobi_tolerance": args.jacobi_tol},
+        "e2e": {"value": e2e_value, "unit": "solves/s", "ms_per_step": e2e_ms,
+                "h2d_bytes_per_step": batch.total * 4, "d2h_bytes_per_step": batch.total * 4},
+        "roofline": roof,
+        "cpu_baseline": cpu,
+        "clocks": clocks.summary(),
+        "gpu_launches": launches,
+        "plain_fp32": {"value": acc_plain * world / (ms_plain / 1e3), "ms_per_step": ms_plain,
+                       "accepted": acc_plain},
+        "speedup_vs_plain_fp32": (value / (acc_plain * world / (ms_plain / 1e3))) if acc_plain else None,
+        "accepted": acc, "fallback": int(fallback),
+        "error_vs_fp64": {"p50": float(np.percentile(errs, 50)), "p99": float(np.percentile(errs, 99)),
+                          "residual_p50": float(np.percentile(resid, 50)),
+                          "residual_p99": float(np.percentile(resid, 99)),
+                          "sample": len(idx)},
+        "kernels": {k: {"launches": v[0], "ms": v[1], "share": v[1] / total_ms} for k, v in rows.items()},
+    }
+    print(json.dumps(line), flush=True)
+    if world > 1:
+        torch.distributed.barrier()
+
+
+if __name__ == "__main__":
+    main()

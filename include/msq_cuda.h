@@ -66,6 +66,13 @@ int msq_set_stream(msq_ctx *ctx, void *stream);
 int msq_synchronize(msq_ctx *ctx);
 /* Number of this library's kernel launches enqueued so far on `ctx`. */
 uint64_t msq_launch_count(const msq_ctx *ctx);
+/* Launch timing for profiling: between begin and end, an event is recorded
+ * on the context's stream after every launch; end synchronises and writes one
+ * line per kernel name, "name<TAB>launches<TAB>total_ms", into `out`.  The
+ * duration of a launch is the gap to the previous event, so stream-ordered
+ * copies issued between launches count toward the next launch. */
+int msq_timing_begin(msq_ctx *ctx);
+int msq_timing_end(msq_ctx *ctx, char *out, size_t capacity);
 
 /* ---- codecs (the benchmark spec (b)) ---------------------------------------------
  * Byte sizes: storageBytes / scaleBytes (src/configuration.cpp:188-213).

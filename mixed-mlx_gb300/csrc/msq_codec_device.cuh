@@ -172,9 +172,21 @@ __device__ __forceinline__ float exp2Int(int k) {
 // [-127, 125] for every finite block, so 2^-e is a normal float and one
 // correctly rounded multiplication gives the same result as the division.
 __device__ __forceinline__ float mxDivide(float x, int e) {
+  // A NaN keeps its sign through the reference's host division (x86 and
+  // Arm propagate the NaN operand); the GPU multiply would canonicalise it.
+  if (x != x) return x;
   if (e >= -126 && e <= 126) return x * exp2Int(-e);
   // e == -127: 2^127 is normal;  e > 126 cannot come from a finite block.
   return e < 0 ? x * 1.7014118346046923e38f : __fdiv_rn(x, 8.507059173023462e37f);
+}
+
+// Row-scaled FP8 (no reference counterpart): x / s rounded once, NaN kept
+// with its sign as a host division keeps it; decode is code * s.
+__device__ __forceinline__ float rowDivide(float x, float s) {
+  return x != x ? x : __fdiv_rn(x, s);
+}
+__device__ __forceinline__ float rowScaleDecode(float decoded, float s) {
+  return decoded != decoded ? decoded : decoded * s;
 }
 
 // Exact ldexp of a decoded element (<= 4 significant bits) by scale - 127,

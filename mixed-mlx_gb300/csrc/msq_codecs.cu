@@ -211,7 +211,7 @@ encodeRowScaleKernel(const float *__restrict__ source, size_t rows,
     if (lane == 0) scales[row] = scale;
     uint8_t *out = values + row * row_length;
     for (size_t i = lane; i < row_length; i += 32) {
-      out[i] = encodeE4M3(__fdiv_rn(in[i], scale));
+      out[i] = encodeE4M3(rowDivide(in[i], scale));
     }
   }
 }
@@ -288,7 +288,7 @@ decodeRowScaleKernel(const uint8_t *__restrict__ values,
                      size_t row_length, float *__restrict__ output) {
   for (size_t i = blockIdx.x * static_cast<size_t>(blockDim.x) + threadIdx.x;
        i < elements; i += static_cast<size_t>(gridDim.x) * blockDim.x) {
-    output[i] = decodeE4M3(values[i]) * scales[i / row_length];
+    output[i] = rowScaleDecode(decodeE4M3(values[i]), scales[i / row_length]);
   }
 }
 

@@ -17,9 +17,26 @@ int cudaCheck(msq_ctx *ctx, cudaError_t status, const char *what) {
                   std::string(what) + ": " + cudaGetErrorString(status));
 }
 
+static cudaEvent_t takeEvent(msq_ctx *ctx) {
+  if (ctx->event_pool.empty()) {
+    cudaEvent_t e = nullptr;
+    cudaEventCreate(&e);
+    return e;
+  }
+  cudaEvent_t e = ctx->event_pool.back();
+  ctx->event_pool.pop_back();
+  return e;
+}
+
 int launched(msq_ctx *ctx, const char *what) {
   ++ctx->launches;
-  return cudaCheck(ctx, cudaGetLastError(), what);
+  const int status = cudaCheck(ctx, cudaGetLastError(), what);
+  if (status == MSQ_OK && ctx->timing) {
+    cudaEvent_t e = takeEvent(ctx);
+    cudaEventRecord(e, ctx->stream);
+    ctx->timing_events.emplace_back(what, e);
+  }
+  return status;
 }
 
 int checkDeviceStatus(msq_ctx *ctx) {
@@ -103,6 +120,7 @@ const DeviceBatch *prepareBatch(msq_ctx *ctx, const int32_t *n,
   }
   if (ctx->batches.size() >= 8) {
     DeviceBatch *old = ctx->batches.front();
+    for (auto &w : old->work_cache) cudaFree(w.work);
     cudaFree(old->offset);
     delete old;
     ctx->batches.erase(ctx->batches.begin());
@@ -111,21 +129,21 @@ const DeviceBatch *prepareBatch(msq_ctx *ctx, const int32_t *n,
   return b;
 }
 
-void *scratch(msq_ctx *ctx, size_t bytes) {
-  if (bytes <= ctx->scratch_bytes) return ctx->scratch;
-  if (ctx->scratch != nullptr) {
+void *scratch(msq_ctx *ctx, size_t bytes, int slot) {
+  if (bytes <= ctx->scratch_bytes[slot]) return ctx->scratch[slot];
+  if (ctx->scratch[slot] != nullptr) {
     cudaStreamSynchronize(ctx->stream);
-    cudaFree(ctx->scratch);
-    ctx->scratch = nullptr;
-    ctx->scratch_bytes = 0;
+    cudaFree(ctx->scratch[slot]);
+    ctx->scratch[slot] = nullptr;
+    ctx->scratch_bytes[slot] = 0;
   }
   const size_t rounded = (bytes + (1u << 20) - 1) & ~static_cast<size_t>((1u << 20) - 1);
-  if (cudaCheck(ctx, cudaMalloc(&ctx->scratch, rounded), "scratch alloc") != MSQ_OK) {
-    ctx->scratch = nullptr;
+  if (cudaCheck(ctx, cudaMalloc(&ctx->scratch[slot], rounded), "scratch alloc") != MSQ_OK) {
+    ctx->scratch[slot] = nullptr;
     return nullptr;
   }
-  ctx->scratch_bytes = rounded;
-  return ctx->scratch;
+  ctx->scratch_bytes[slot] = rounded;
+  return ctx->scratch[slot];
 }
 
 }  // namespace msq
@@ -155,11 +173,15 @@ extern "C" void msq_destroy(msq_ctx *ctx) {
   if (ctx->stream != nullptr) cudaStreamSynchronize(ctx->stream);
   else cudaDeviceSynchronize();
   for (DeviceBatch *b : ctx->batches) {
+    for (auto &w : b->work_cache) cudaFree(w.work);
     cudaFree(b->offset);
     delete b;
   }
-  if (ctx->scratch != nullptr) cudaFree(ctx->scratch);
+  for (int slot = 0; slot < 4; ++slot)
+    if (ctx->scratch[slot] != nullptr) cudaFree(ctx->scratch[slot]);
   if (ctx->d_status != nullptr) cudaFree(ctx->d_status);
+  for (auto &entry : ctx->timing_events) cudaEventDestroy(entry.second);
+  for (cudaEvent_t e : ctx->event_pool) cudaEventDestroy(e);
   delete ctx;
 }
 
@@ -181,4 +203,47 @@ extern "C" int msq_synchronize(msq_ctx *ctx) {
 
 extern "C" uint64_t msq_launch_count(const msq_ctx *ctx) {
   return ctx == nullptr ? 0 : ctx->launches;
+}
+
+extern "C" int msq_timing_begin(msq_ctx *ctx) {
+  if (ctx == nullptr) return MSQ_ERR_INVALID_ARGUMENT;
+  for (auto &entry : ctx->timing_events) ctx->event_pool.push_back(entry.second);
+  ctx->timing_events.clear();
+  cudaEvent_t e = takeEvent(ctx);
+  MSQ_TRY(cudaCheck(ctx, cudaEventRecord(e, ctx->stream), "timing begin"));
+  ctx->timing_events.emplace_back("begin", e);
+  ctx->timing = true;
+  return MSQ_OK;
+}
+
+extern "C" int msq_timing_end(msq_ctx *ctx, char *out, size_t capacity) {
+  if (ctx == nullptr || out == nullptr || capacity == 0) return MSQ_ERR_INVALID_ARGUMENT;
+  ctx->timing = false;
+  MSQ_TRY(cudaCheck(ctx, cudaStreamSynchronize(ctx->stream), "timing end"));
+  struct Acc { double ms = 0.0; long count = 0; };
+  std::vector<std::pair<std::string, Acc>> rows;
+  for (size_t i = 1; i < ctx->timing_events.size(); ++i) {
+    float ms = 0.0f;
+    cudaEventElapsedTime(&ms, ctx->timing_events[i - 1].second, ctx->timing_events[i].second);
+    const std::string name = ctx->timing_events[i].first;
+    Acc *acc = nullptr;
+    for (auto &r : rows)
+      if (r.first == name) acc = &r.second;
+    if (acc == nullptr) {
+      rows.emplace_back(name, Acc{});
+      acc = &rows.back().second;
+    }
+    acc->ms += ms;
+    acc->count += 1;
+  }
+  std::string text;
+  for (auto &r : rows) {
+    text += r.first + "\t" + std::to_string(r.second.count) + "\t" +
+            std::to_string(r.second.ms) + "\n";
+  }
+  std::strncpy(out, text.c_str(), capacity - 1);
+  out[capacity - 1] = '\0';
+  for (auto &entry : ctx->timing_events) ctx->event_pool.push_back(entry.second);
+  ctx->timing_events.clear();
+  return MSQ_OK;
 }

@@ -1,0 +1,49 @@
+// Host-side entry points of the dense (CUDA-core) kernels in msq_dense.cu.
+#pragma once
+
+#include "msq_internal.cuh"
+
+namespace msq {
+
+enum GemmEpilogue : int {
+  kEpilogueStore = 0,
+  kEpilogueInverseH = 1,  // C_ij / (sqrt(lambda_i) + sqrt(lambda_j))
+};
+
+struct GemmArgs {
+  const int4 *work;
+  int items;
+  const float *a, *b;
+  float *c;
+  const int64_t *a_offset, *b_offset, *c_offset;
+  const int32_t *n;
+  const float *eigenvalues;
+  const int64_t *eig_offset;
+  int a_mmajor;  // A(i,k) at i + k*n instead of k + i*n
+  int b_nmajor;  // B(k,j) at j + k*n instead of k + j*n
+};
+
+struct ResidualArgs {
+  const int4 *work;
+  int items;
+  const float *a, *x_hi, *x_lo;
+  float *r;
+  double *norms;
+  const int64_t *offset;
+  const int32_t *n;
+};
+
+// Flat (matrix, tile_i, tile_j) work list for square tiles of size `tile`.
+int gemmWork(msq_ctx *ctx, const DeviceBatch *b, int tile, const int4 **work, int *items);
+// C = A B per matrix, FP32 FMA; by default A(i,k) = a[k + i*n] and
+// B(k,j) = bm[k + j*n] (C = a^T bm).
+int gemmTN(msq_ctx *ctx, const DeviceBatch *b, const float *a, const float *bm, float *c,
+           int epilogue, const float *eigenvalues, bool a_mmajor = false,
+           bool b_nmajor = false);
+int residualFF(msq_ctx *ctx, const DeviceBatch *b, const float *a, const float *x_hi,
+               const float *x_lo, float *r, double *norms);
+int makeFactor(msq_ctx *ctx, const DeviceBatch *b, const float *v, const float *lam, float *f);
+int transpose(msq_ctx *ctx, const DeviceBatch *b, const float *src, float *dst);
+int symmetricAdd(msq_ctx *ctx, const DeviceBatch *b, float *x_hi, float *x_lo, const float *e);
+
+}  // namespace msq

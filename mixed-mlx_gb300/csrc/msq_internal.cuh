@@ -26,6 +26,12 @@ enum DeviceStatus : int {
   kStatusBadOrder = 4,
 };
 
+struct WorkList {
+  int tile;
+  int4 *work;
+  int items;
+};
+
 // Batched layout uploaded to the device once per distinct (n, offset) set.
 struct DeviceBatch {
   int count = 0;
@@ -39,6 +45,7 @@ struct DeviceBatch {
   std::vector<int32_t> host_n;
   std::vector<int64_t> host_offset;
   std::vector<int64_t> host_eig_offset;
+  std::vector<WorkList> work_cache;  // tile work lists (msq_dense.cu)
 };
 
 }  // namespace msq
@@ -49,11 +56,17 @@ struct msq_ctx {
   std::string error;
   uint64_t launches = 0;
   int *d_status = nullptr;  // device status word
-  // Grow-only scratch owned by the context (freed in msq_destroy).
-  void *scratch = nullptr;
-  size_t scratch_bytes = 0;
+  // Grow-only scratch arenas owned by the context (freed in msq_destroy);
+  // one per user so nested stages never share memory.
+  void *scratch[4] = {nullptr, nullptr, nullptr, nullptr};
+  size_t scratch_bytes[4] = {0, 0, 0, 0};
   // Batch layouts cached by content hash (small: a few entries).
   std::vector<msq::DeviceBatch *> batches;
+  // Launch timing (msq_timing_begin/end): one event after every launch; the
+  // gap between consecutive events on the stream is that launch's duration.
+  bool timing = false;
+  std::vector<std::pair<const char *, cudaEvent_t>> timing_events;
+  std::vector<cudaEvent_t> event_pool;
 };
 
 namespace msq {
@@ -67,8 +80,10 @@ int checkDeviceStatus(msq_ctx *ctx);
 // Uploads (or finds cached) the batch layout; null on error (ctx->error set).
 const DeviceBatch *prepareBatch(msq_ctx *ctx, const int32_t *n,
                                 const int64_t *offset, int count);
-// Grow-only context scratch, stream-ordered.
-void *scratch(msq_ctx *ctx, size_t bytes);
+// Grow-only context scratch arena `slot` (0: Jacobi, 1: solver,
+// 2: codec operands, 3: GEMM split operands).
+enum ScratchSlot : int { kScratchJacobi = 0, kScratchSolver = 1, kScratchOperand = 2, kScratchGemm = 3 };
+void *scratch(msq_ctx *ctx, size_t bytes, int slot);
 
 inline unsigned gridFor(size_t work_items, unsigned threads,
                         unsigned ctas_per_sm = 8) {

@@ -482,7 +482,7 @@ int jacobiEnqueue(msq_ctx *ctx, const DeviceBatch *b, float *matrices,
   const size_t state_bytes = (b->count * sizeof(JacobiState) + 255) & ~size_t(255);
   const size_t packed_bytes = (plan->packed_total * sizeof(float) + 255) & ~size_t(255);
   const size_t log_bytes = plan->log_total * sizeof(float2);
-  char *work = static_cast<char *>(scratch(ctx, state_bytes + packed_bytes + log_bytes));
+  char *work = static_cast<char *>(scratch(ctx, state_bytes + packed_bytes + log_bytes, kScratchJacobi));
   if (work == nullptr) return MSQ_ERR_CUDA;
   JacobiArgs args{};
   args.a = matrices;

@@ -1,0 +1,284 @@
+// Pipeline stages behind the C ABI and the batched solve.
+//
+// msq_solve_batched is the batched form of solveGpuResidentSpd
+// (src/metal_solver.cpp:92-336): Jacobi -> factor W = V diag(lambda^(1/4))
+// -> (quantize W) -> reconstruction X0 = W W^T -> float-float residual ->
+// frozen-basis Sylvester sweeps (refineUpdateAndMeasure,
+// src/metal_runtime.cpp:847-966) -> final float-float residual.  Matrices
+// are grouped by plan; a matrix whose final residual misses the tolerance is
+// re-solved by the plain FP32 plan (the reference escalates a rejected
+// low-precision factor to FP32 the same way, src/metal_solver.cpp:225-235).
+// Corrections always use the FP32 stable basis, as the reference does
+// (:304-310).
+#include "msq_dense.cuh"
+#include "msq_internal.cuh"
+#include "msq_stages.cuh"
+
+#include <cmath>
+#include <map>
+#include <vector>
+
+namespace msq {
+namespace {
+
+size_t alignUp(size_t bytes) { return (bytes + 255) & ~static_cast<size_t>(255); }
+
+// One Sylvester sweep on a batch, FP32 GEMMs on the CUDA cores:
+//   G = R V, C = (V^T G) o H, Z = V C, E = Z V^T, X <- X + (E + E^T)/2.
+int sylvesterFp32(msq_ctx *ctx, const DeviceBatch *b, const float *v, const float *lam,
+                  const float *r, float *x_hi, float *x_lo, float *ws0, float *ws1) {
+  MSQ_TRY(gemmTN(ctx, b, r, v, ws0, kEpilogueStore, nullptr));           // G = R V
+  MSQ_TRY(gemmTN(ctx, b, v, ws0, ws1, kEpilogueInverseH, lam));          // C = V^T G o H
+  MSQ_TRY(gemmTN(ctx, b, v, ws1, ws0, kEpilogueStore, nullptr, true));   // Z = V C
+  MSQ_TRY(gemmTN(ctx, b, ws0, v, ws1, kEpilogueStore, nullptr, true, true));  // E = Z V^T
+  return symmetricAdd(ctx, b, x_hi, x_lo, ws1);
+}
+
+}  // namespace
+
+int sylvesterSweep(msq_ctx *ctx, const DeviceBatch *b, int gemm_format, const float *v,
+                   const float *lam, const float *r, float *x_hi, float *x_lo, float *ws0,
+                   float *ws1) {
+  if (gemm_format != MSQ_FMT_FP32) {
+    return setError(ctx, MSQ_ERR_UNSUPPORTED, "Sylvester sweep: only FP32 correction GEMMs");
+  }
+  return sylvesterFp32(ctx, b, v, lam, r, x_hi, x_lo, ws0, ws1);
+}
+
+// X0 = F^T F from the FP32 factor F (K-major W^T) in the plan's format.
+int reconstructFromFactor(msq_ctx *ctx, const DeviceBatch *b, int plan_format, const float *f,
+                          float *x) {
+  switch (plan_format) {
+    case MSQ_PLAN_FP32:
+      return gemmTN(ctx, b, f, f, x, kEpilogueStore, nullptr);
+    case MSQ_PLAN_BF16:
+      return reconstructLowBit(ctx, b, MSQ_FMT_BF16, f, x);
+    case MSQ_PLAN_FP8:
+      return reconstructLowBit(ctx, b, MSQ_FMT_FP8_E4M3FN_ROWSCALE, f, x);
+    case MSQ_PLAN_MXFP4:
+      return reconstructLowBit(ctx, b, MSQ_FMT_MXFP4_E2M1, f, x);
+    default:
+      return setError(ctx, MSQ_ERR_INVALID_ARGUMENT, "unknown plan format");
+  }
+}
+
+}  // namespace msq
+
+using namespace msq;
+
+extern "C" int msq_make_factor(msq_ctx *ctx, const float *vectors, const float *eigenvalues,
+                               const int32_t *n, const int64_t *offset, int count,
+                               float *factor_t) {
+  if (ctx == nullptr) return MSQ_ERR_INVALID_ARGUMENT;
+  if (!vectors || !eigenvalues || !factor_t)
+    return setError(ctx, MSQ_ERR_INVALID_ARGUMENT, "msq_make_factor: null buffer");
+  const DeviceBatch *b = prepareBatch(ctx, n, offset, count);
+  if (b == nullptr) return MSQ_ERR_INVALID_ARGUMENT;
+  return makeFactor(ctx, b, vectors, eigenvalues, factor_t);
+}
+
+extern "C" int msq_reconstruct(msq_ctx *ctx, int format, const void *values, const float *scales,
+                               const int32_t *n, const int64_t *offset, int count, float *root) {
+  if (ctx == nullptr) return MSQ_ERR_INVALID_ARGUMENT;
+  if (!values || !root) return setError(ctx, MSQ_ERR_INVALID_ARGUMENT, "msq_reconstruct: null buffer");
+  const DeviceBatch *b = prepareBatch(ctx, n, offset, count);
+  if (b == nullptr) return MSQ_ERR_INVALID_ARGUMENT;
+  if (format == MSQ_FMT_FP32) {
+    const float *f = static_cast<const float *>(values);
+    return gemmTN(ctx, b, f, f, root, kEpilogueStore, nullptr);
+  }
+  return reconstructEncoded(ctx, b, format, values, scales, root);
+}
+
+extern "C" int msq_residual(msq_ctx *ctx, const float *a, const float *x_hi, const float *x_lo,
+                            const int32_t *n, const int64_t *offset, int count, float *residual,
+                            double *norms) {
+  if (ctx == nullptr) return MSQ_ERR_INVALID_ARGUMENT;
+  if (!a || !x_hi || !norms) return setError(ctx, MSQ_ERR_INVALID_ARGUMENT, "msq_residual: null buffer");
+  const DeviceBatch *b = prepareBatch(ctx, n, offset, count);
+  if (b == nullptr) return MSQ_ERR_INVALID_ARGUMENT;
+  return residualFF(ctx, b, a, x_hi, x_lo, residual, norms);
+}
+
+extern "C" int msq_sylvester_sweep(msq_ctx *ctx, int gemm_format, const float *vectors,
+                                   const float *eigenvalues, const float *residual,
+                                   const int32_t *n, const int64_t *offset, int count,
+                                   float *x_hi, float *x_lo, float *workspace) {
+  if (ctx == nullptr) return MSQ_ERR_INVALID_ARGUMENT;
+  if (!vectors || !eigenvalues || !residual || !x_hi || !x_lo || !workspace)
+    return setError(ctx, MSQ_ERR_INVALID_ARGUMENT, "msq_sylvester_sweep: null buffer");
+  if (gemm_format != MSQ_FMT_FP32 && gemm_format != MSQ_FMT_BF16)
+    return setError(ctx, MSQ_ERR_INVALID_ARGUMENT, "msq_sylvester_sweep: gemm_format must be FP32 or BF16");
+  const DeviceBatch *b = prepareBatch(ctx, n, offset, count);
+  if (b == nullptr) return MSQ_ERR_INVALID_ARGUMENT;
+  float *ws0 = workspace;
+  float *ws1 = workspace + b->host_offset.back() + static_cast<int64_t>(b->host_n.back()) * b->host_n.back();
+  return sylvesterSweep(ctx, b, gemm_format, vectors, eigenvalues, residual, x_hi, x_lo, ws0, ws1);
+}
+
+namespace msq {
+namespace {
+
+struct Group {
+  msq_plan plan;
+  std::vector<int> members;  // indices into the caller's batch
+};
+
+bool samePlan(const msq_plan &a, const msq_plan &b) {
+  return a.format == b.format && a.sweeps == b.sweeps &&
+         a.jacobi_tolerance == b.jacobi_tolerance && a.jacobi_max_sweeps == b.jacobi_max_sweeps;
+}
+
+// Runs one plan over a sub-batch whose matrices are copied into the solver
+// arena (compact layout), writes X into `root` at the caller's offsets and
+// the per-matrix residuals into `final_res` / `initial_res`.
+int runGroup(msq_ctx *ctx, const float *a_user, const int32_t *n_user,
+             const int64_t *off_user, const Group &g, float *root,
+             std::vector<double> &final_res, std::vector<double> &initial_res,
+             std::vector<int> &jsweeps) {
+  const int count = static_cast<int>(g.members.size());
+  std::vector<int32_t> n(count);
+  std::vector<int64_t> off(count);
+  int64_t total = 0, order_total = 0;
+  for (int i = 0; i < count; ++i) {
+    n[i] = n_user[g.members[i]];
+    off[i] = total;
+    total += (static_cast<int64_t>(n[i]) * n[i] + 3) & ~int64_t(3);
+    order_total += n[i];
+  }
+  const DeviceBatch *b = prepareBatch(ctx, n.data(), off.data(), count);
+  if (b == nullptr) return MSQ_ERR_INVALID_ARGUMENT;
+  const size_t mat = alignUp(total * sizeof(float));
+  const size_t vec = alignUp(order_total * sizeof(float));
+  const size_t norms_bytes = alignUp(2 * count * sizeof(double));
+  const size_t sweeps_bytes = alignUp(count * sizeof(int32_t));
+  char *w = static_cast<char *>(scratch(ctx, 8 * mat + vec + norms_bytes + sweeps_bytes,
+                                        kScratchSolver));
+  if (w == nullptr) return MSQ_ERR_CUDA;
+  float *A = reinterpret_cast<float *>(w);
+  float *J = reinterpret_cast<float *>(w + mat);      // Jacobi working copy
+  float *V = reinterpret_cast<float *>(w + 2 * mat);
+  float *F = reinterpret_cast<float *>(w + 3 * mat);
+  float *Xh = reinterpret_cast<float *>(w + 4 * mat);
+  float *Xl = reinterpret_cast<float *>(w + 5 * mat);
+  float *R = reinterpret_cast<float *>(w + 6 * mat);
+  float *W1 = reinterpret_cast<float *>(w + 7 * mat);  // with F: the 2 sweep buffers
+  float *lam = reinterpret_cast<float *>(w + 8 * mat);
+  double *norms = reinterpret_cast<double *>(w + 8 * mat + vec);
+  int32_t *sweeps = reinterpret_cast<int32_t *>(w + 8 * mat + vec + norms_bytes);
+
+  // Gather the group's matrices (contiguous groups copy in one go).
+  for (int i = 0; i < count;) {
+    int j = i + 1;
+    while (j < count && g.members[j] == g.members[j - 1] + 1 &&
+           off_user[g.members[j]] == off_user[g.members[j - 1]] +
+                                         ((static_cast<int64_t>(n[j - 1]) * n[j - 1] + 3) & ~int64_t(3)))
+      ++j;
+    const int64_t last = j - 1;
+    const int64_t bytes = (off[last] - off[i] + static_cast<int64_t>(n[last]) * n[last]) * sizeof(float);
+    MSQ_TRY(cudaCheck(ctx, cudaMemcpyAsync(A + off[i], a_user + off_user[g.members[i]], bytes,
+                                           cudaMemcpyDeviceToDevice, ctx->stream), "gather A"));
+    i = j;
+  }
+  MSQ_TRY(cudaCheck(ctx, cudaMemcpyAsync(J, A, total * sizeof(float), cudaMemcpyDeviceToDevice,
+                                         ctx->stream), "jacobi copy"));
+  const int max_sweeps = g.plan.jacobi_max_sweeps > 0 ? g.plan.jacobi_max_sweeps : 15;
+  MSQ_TRY(jacobiEnqueue(ctx, b, J, V, lam, g.plan.jacobi_tolerance, max_sweeps, sweeps, nullptr));
+  MSQ_TRY(makeFactor(ctx, b, V, lam, F));
+  MSQ_TRY(reconstructFromFactor(ctx, b, g.plan.format, F, Xh));
+  MSQ_TRY(cudaCheck(ctx, cudaMemsetAsync(Xl, 0, total * sizeof(float), ctx->stream), "x_lo reset"));
+  std::vector<double> host_norms(2 * count);
+  MSQ_TRY(residualFF(ctx, b, A, Xh, Xl, R, norms));
+  MSQ_TRY(cudaCheck(ctx, cudaMemcpyAsync(host_norms.data(), norms, 2 * count * sizeof(double),
+                                         cudaMemcpyDeviceToHost, ctx->stream), "norms read"));
+  MSQ_TRY(cudaCheck(ctx, cudaStreamSynchronize(ctx->stream), "norms sync"));
+  for (int i = 0; i < count; ++i)
+    initial_res[g.members[i]] = std::sqrt(host_norms[2 * i] / host_norms[2 * i + 1]);
+  // Corrections use the FP32 stable basis and FP32 GEMMs (the reference's
+  // fp32_frozen correction stage, src/metal_solver.cpp:311-325).
+  const int gemm_format = MSQ_FMT_FP32;
+  for (int s = 0; s < g.plan.sweeps; ++s) {
+    MSQ_TRY(sylvesterSweep(ctx, b, gemm_format, V, lam, R, Xh, Xl, F, W1));
+    MSQ_TRY(residualFF(ctx, b, A, Xh, Xl, R, norms));
+  }
+  if (g.plan.sweeps > 0) {
+    MSQ_TRY(cudaCheck(ctx, cudaMemcpyAsync(host_norms.data(), norms, 2 * count * sizeof(double),
+                                           cudaMemcpyDeviceToHost, ctx->stream), "norms read"));
+  }
+  std::vector<int32_t> host_sweeps(count);
+  MSQ_TRY(cudaCheck(ctx, cudaMemcpyAsync(host_sweeps.data(), sweeps, count * sizeof(int32_t),
+                                         cudaMemcpyDeviceToHost, ctx->stream), "sweeps read"));
+  // Scatter X (hi word; the lo word is below FP32 resolution of the output).
+  for (int i = 0; i < count; ++i) {
+    MSQ_TRY(cudaCheck(ctx, cudaMemcpyAsync(root + off_user[g.members[i]], Xh + off[i],
+                                           static_cast<int64_t>(n[i]) * n[i] * sizeof(float),
+                                           cudaMemcpyDeviceToDevice, ctx->stream), "scatter X"));
+  }
+  MSQ_TRY(cudaCheck(ctx, cudaStreamSynchronize(ctx->stream), "group sync"));
+  MSQ_TRY(checkDeviceStatus(ctx));
+  for (int i = 0; i < count; ++i) {
+    final_res[g.members[i]] = std::sqrt(host_norms[2 * i] / host_norms[2 * i + 1]);
+    jsweeps[g.members[i]] = host_sweeps[i];
+  }
+  return MSQ_OK;
+}
+
+}  // namespace
+}  // namespace msq
+
+extern "C" int msq_solve_batched(msq_ctx *ctx, const float *a, const int32_t *n,
+                                 const int64_t *offset, int count, const msq_plan *plans,
+                                 double tolerance, float *root, msq_solve_result *results) {
+  if (ctx == nullptr) return MSQ_ERR_INVALID_ARGUMENT;
+  if (a == nullptr || root == nullptr || n == nullptr || offset == nullptr || count <= 0)
+    return setError(ctx, MSQ_ERR_INVALID_ARGUMENT, "msq_solve_batched: null or empty input");
+  if (!(tolerance > 0.0)) return setError(ctx, MSQ_ERR_INVALID_ARGUMENT, "tolerance must be > 0");
+  const msq_plan fp32_plan{MSQ_PLAN_FP32, 0, 1e-7, 15, 0};
+  std::vector<Group> groups;
+  for (int i = 0; i < count; ++i) {
+    if (n[i] < 1) return setError(ctx, MSQ_ERR_INVALID_ARGUMENT, "order < 1");
+    const msq_plan p = plans ? plans[i] : fp32_plan;
+    if (p.format < MSQ_PLAN_FP32 || p.format > MSQ_PLAN_MXFP4 || p.sweeps < 0 || p.sweeps > 8)
+      return setError(ctx, MSQ_ERR_INVALID_ARGUMENT, "invalid plan");
+    bool placed = false;
+    for (Group &g : groups) {
+      if (samePlan(g.plan, p)) {
+        g.members.push_back(i);
+        placed = true;
+        break;
+      }
+    }
+    if (!placed) groups.push_back({p, {i}});
+  }
+  std::vector<double> final_res(count, NAN), initial_res(count, NAN);
+  std::vector<int> jsweeps(count, 0), fallback(count, 0), accepted(count, 0), corrections(count, 0);
+  for (const Group &g : groups) {
+    MSQ_TRY(runGroup(ctx, a, n, offset, g, root, final_res, initial_res, jsweeps));
+    for (int m : g.members) corrections[m] = g.plan.sweeps;
+  }
+  Group retry{fp32_plan, {}};
+  for (const Group &g : groups) {
+    if (samePlan(g.plan, fp32_plan)) continue;
+    for (int m : g.members)
+      if (!(final_res[m] <= tolerance)) retry.members.push_back(m);
+  }
+  for (int i = 0; i < count; ++i) accepted[i] = final_res[i] <= tolerance;
+  if (!retry.members.empty()) {
+    MSQ_TRY(runGroup(ctx, a, n, offset, retry, root, final_res, initial_res, jsweeps));
+    for (int m : retry.members) {
+      fallback[m] = 1;
+      corrections[m] = 0;
+    }
+  }
+  if (results != nullptr) {
+    for (int i = 0; i < count; ++i) {
+      results[i].final_residual = final_res[i];
+      results[i].initial_residual = initial_res[i];
+      results[i].jacobi_sweeps = jsweeps[i];
+      results[i].corrections = corrections[i];
+      results[i].accepted = accepted[i];
+      results[i].fallback = fallback[i];
+    }
+  }
+  return MSQ_OK;
+}

@@ -1,0 +1,25 @@
+// Stage entry points shared between translation units.
+#pragma once
+
+#include "msq_internal.cuh"
+
+namespace msq {
+
+// msq_jacobi.cu
+int jacobiEnqueue(msq_ctx *ctx, const DeviceBatch *b, float *matrices, float *vectors,
+                  float *eigenvalues, double tolerance, int max_sweeps,
+                  int32_t *sweeps_done, float *off_ratio);
+
+// msq_tc.cu — tcgen05 reconstruction X = W W^T from the FP32 factor F = W^T
+// (quantized to `format` on the fly) or from already encoded flat codes.
+int reconstructLowBit(msq_ctx *ctx, const DeviceBatch *b, int format, const float *f,
+                      float *x);
+int reconstructEncoded(msq_ctx *ctx, const DeviceBatch *b, int format, const void *values,
+                       const float *scales, float *x);
+
+// msq_solve.cu
+int sylvesterSweep(msq_ctx *ctx, const DeviceBatch *b, int gemm_format, const float *v,
+                   const float *lam, const float *r, float *x_hi, float *x_lo, float *ws0,
+                   float *ws1);
+
+}  // namespace msq

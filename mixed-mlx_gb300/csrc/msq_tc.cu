@@ -1,0 +1,631 @@
+// Low-bit reconstruction X = W W^T on the 5th-generation tensor cores.
+//
+// Replaces reconstructLowFactorTiled / matmul_f32_low_right_* of the
+// reference (src/metal_runtime.cpp:500-534, metal_mixed_sqrt.metal:
+// 1540-1600), which decode the low-bit factor to FP32 in threadgroup memory
+// and run an FP32 FMA tile GEMM.  Here the factor stays low-bit all the way
+// into the MMA:
+//   * packOperand quantizes the K-major factor W^T straight into 128-row x
+//     128-byte tiles laid out in the canonical SWIZZLE_128B K-major shape
+//     (16-byte chunk index XOR row mod 8 inside each 1024-byte atom), so a
+//     tile is one contiguous 16 KB block that a single TMA bulk copy
+//     (cp.async.bulk) lands in shared memory ready for the MMA;
+//   * tcGemmKernel is a persistent, warp-specialized kernel: warp 4 issues
+//     the bulk copies into a 4-stage mbarrier ring, warp 5 owns TMEM (256
+//     columns: two 128x128 FP32 accumulators) and issues tcgen05.mma
+//     (kind::f16 for BF16, kind::f8f6f4 for FP8 E4M3) from one thread, and
+//     warps 0-3 drain the other accumulator with tcgen05.ld while the next
+//     tile accumulates, applying the per-row FP8 scales r_i r_j.
+// MXFP4 factors (E2M1 + E8M0 per 32 along K) are decoded into BF16 tiles,
+// which is exact (E2M1 x 2^e has at most 2 significant bits), and use
+// kind::f16.  Every mbarrier wait is bounded; on expiry the kernel records
+// kStatusMbarrierTimeout in the context's status word and unwinds.
+#include "msq_codec_device.cuh"
+#include "msq_internal.cuh"
+#include "msq_stages.cuh"
+
+#include <algorithm>
+#include <vector>
+
+namespace msq {
+namespace {
+
+constexpr int kTileRows = 128;
+constexpr int kTileBytes = 16384;  // 128 rows x 128 bytes
+constexpr int kStages = 4;
+constexpr int kTcThreads = 192;    // warps 0-3 epilogue, 4 producer, 5 MMA
+constexpr uint32_t kTmemCols = 256;
+constexpr long long kWaitLimit = 1ll << 26;
+
+enum OperandKind : int { kOpBf16 = 0, kOpFp8 = 1 };
+
+__device__ __forceinline__ uint32_t smemAddr(const void *p) {
+  return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+
+__device__ __forceinline__ uint32_t swizzle128(int row, int chunk) {
+  return (row >> 3) * 1024 + (row & 7) * 128 + ((chunk ^ (row & 7)) << 4);
+}
+
+__device__ __forceinline__ void mbarInit(uint32_t bar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(bar), "r"(count));
+}
+
+__device__ __forceinline__ bool mbarTryWait(uint32_t bar, uint32_t parity) {
+  uint32_t done;
+  asm volatile(
+      "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
+      " selp.u32 %0, 1, 0, p;\n}\n"
+      : "=r"(done)
+      : "r"(bar), "r"(parity)
+      : "memory");
+  return done != 0;
+}
+
+// Bounded wait: false (and the status word set) if the phase never completes.
+__device__ __forceinline__ bool mbarWait(uint32_t bar, uint32_t parity, int *status,
+                                         volatile int *abort_flag) {
+  for (long long i = 0; i < kWaitLimit; ++i) {
+    if (mbarTryWait(bar, parity)) return true;
+    if (*abort_flag) return false;
+  }
+  atomicExch(status, kStatusMbarrierTimeout);
+  *abort_flag = 1;
+  return false;
+}
+
+__device__ __forceinline__ void mbarArriveExpectTx(uint32_t bar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes)
+               : "memory");
+}
+
+__device__ __forceinline__ void mbarArrive(uint32_t bar) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(bar) : "memory");
+}
+
+__device__ __forceinline__ void bulkLoad(uint32_t dst, const void *src, uint32_t bytes,
+                                         uint32_t bar) {
+  asm volatile(
+      "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+          dst),
+      "l"(src), "r"(bytes), "r"(bar)
+      : "memory");
+}
+
+// Shared-memory matrix descriptor: K-major, SWIZZLE_128B, 1024-byte atoms.
+__device__ __forceinline__ uint64_t smemDesc(uint32_t addr) {
+  return static_cast<uint64_t>((addr >> 4) & 0x3FFFu) |
+         (static_cast<uint64_t>(1) << 16) |            // LBO (unused for SW128 K-major)
+         (static_cast<uint64_t>(1024 >> 4) << 32) |    // SBO: 8-row atom stride
+         (static_cast<uint64_t>(1) << 46) |            // descriptor version
+         (static_cast<uint64_t>(2) << 61);             // SWIZZLE_128B
+}
+
+// Instruction descriptor: D = F32, K-major A and B, M = 128, N = 128.
+// A/B type field: BF16 = 1 for kind::f16, E4M3 = 0 for kind::f8f6f4.
+__host__ __device__ constexpr uint32_t instrDesc(int kind) {
+  return (1u << 4) | ((kind == kOpBf16 ? 1u : 0u) << 7) | ((kind == kOpBf16 ? 1u : 0u) << 10) |
+         ((128u >> 3) << 17) | ((128u >> 4) << 24);
+}
+
+template <int kKind>
+__device__ __forceinline__ void mmaIssue(uint32_t tmem, uint64_t a, uint64_t b, uint32_t accum) {
+  if constexpr (kKind == kOpBf16) {
+    asm volatile(
+        "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+        " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(tmem),
+        "l"(a), "l"(b), "r"(instrDesc(kOpBf16)), "r"(accum));
+  } else {
+    asm volatile(
+        "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+        " tcgen05.mma.cta_group::1.kind::f8f6f4 [%0], %1, %2, %3, p;\n}\n" ::"r"(tmem),
+        "l"(a), "l"(b), "r"(instrDesc(kOpFp8)), "r"(accum));
+  }
+}
+
+__device__ __forceinline__ void mmaCommit(uint32_t bar) {
+  asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+                   bar)
+               : "memory");
+}
+
+__device__ __forceinline__ void tmemLoad32(uint32_t taddr, float *v) {
+  uint32_t r[32];
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, "
+      "%12, %13, %14, %15, %16, %17, %18, %19, %20, %21, %22, %23, %24, %25, %26, %27, %28, %29, "
+      "%30, %31}, [%32];"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]),
+        "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]),
+        "=r"(r[14]), "=r"(r[15]), "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]),
+        "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]), "=r"(r[24]), "=r"(r[25]),
+        "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
+      : "r"(taddr));
+  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+  for (int i = 0; i < 32; ++i) v[i] = __uint_as_float(r[i]);
+}
+
+struct TcArgs {
+  const int4 *work;        // (matrix, tile_m, tile_n, k_tiles)
+  int items;
+  const uint8_t *tiles;    // packed operand
+  const int64_t *tile_base;// per matrix: first tile index
+  const int32_t *n;
+  const int64_t *x_offset;
+  const int64_t *eig_offset;
+  const float *row_scale;  // FP8 only: per matrix row scales at eig_offset
+  float *x;
+  int *status;
+};
+
+template <int kKind>
+__global__ void __launch_bounds__(kTcThreads, 1) tcGemmKernel(TcArgs args) {
+  extern __shared__ __align__(1024) unsigned char smem_raw[];
+  unsigned char *base = reinterpret_cast<unsigned char *>(
+      (reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~static_cast<uintptr_t>(1023));
+  unsigned char *stage_mem = base;  // kStages x (A 16 KB, B 16 KB)
+  uint64_t *bars = reinterpret_cast<uint64_t *>(base + kStages * 2 * kTileBytes);
+  uint64_t *full = bars, *empty = bars + kStages;
+  uint64_t *acc_full = bars + 2 * kStages, *acc_empty = acc_full + 2;
+  uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(acc_empty + 2);
+  volatile int *abort_flag = reinterpret_cast<volatile int *>(tmem_slot + 1);
+  const int warp = threadIdx.x / 32, lane = threadIdx.x % 32;
+
+  if (threadIdx.x == 0) {
+    for (int s = 0; s < kStages; ++s) {
+      mbarInit(smemAddr(&full[s]), 1);
+      mbarInit(smemAddr(&empty[s]), 1);
+    }
+    for (int a = 0; a < 2; ++a) {
+      mbarInit(smemAddr(&acc_full[a]), 1);
+      mbarInit(smemAddr(&acc_empty[a]), 128);
+    }
+    *abort_flag = 0;
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  if (warp == 5) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
+                     smemAddr(tmem_slot)),
+                 "r"(kTmemCols));
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;");
+  __syncthreads();
+  asm volatile("tcgen05.fence::after_thread_sync;");
+  const uint32_t tmem = *tmem_slot;
+
+  if (warp == 4) {
+    if (lane == 0) {
+      int stage = 0;
+      uint32_t phase = 0;
+      for (int item = blockIdx.x; item < args.items && !*abort_flag; item += gridDim.x) {
+        const int4 w = args.work[item];
+        const uint8_t *tiles = args.tiles + args.tile_base[w.x] * kTileBytes;
+        for (int kt = 0; kt < w.w; ++kt) {
+          if (!mbarWait(smemAddr(&empty[stage]), phase ^ 1, args.status, abort_flag)) break;
+          const uint32_t bar = smemAddr(&full[stage]);
+          mbarArriveExpectTx(bar, 2 * kTileBytes);
+          unsigned char *dst = stage_mem + stage * 2 * kTileBytes;
+          bulkLoad(smemAddr(dst), tiles + (static_cast<int64_t>(w.y) * w.w + kt) * kTileBytes,
+                   kTileBytes, bar);
+          bulkLoad(smemAddr(dst + kTileBytes),
+                   tiles + (static_cast<int64_t>(w.z) * w.w + kt) * kTileBytes, kTileBytes, bar);
+          if (++stage == kStages) {
+            stage = 0;
+            phase ^= 1;
+          }
+        }
+      }
+    }
+  } else if (warp == 5) {
+    if (lane == 0) {
+      int stage = 0;
+      uint32_t phase = 0;
+      int acc = 0;
+      uint32_t acc_phase = 0;
+      for (int item = blockIdx.x; item < args.items && !*abort_flag; item += gridDim.x) {
+        const int4 w = args.work[item];
+        if (!mbarWait(smemAddr(&acc_empty[acc]), acc_phase ^ 1, args.status, abort_flag)) break;
+        asm volatile("tcgen05.fence::after_thread_sync;");
+        const uint32_t d = tmem + acc * 128;
+        for (int kt = 0; kt < w.w; ++kt) {
+          if (!mbarWait(smemAddr(&full[stage]), phase, args.status, abort_flag)) break;
+          asm volatile("tcgen05.fence::after_thread_sync;");
+          const uint32_t a_addr = smemAddr(stage_mem + stage * 2 * kTileBytes);
+          const uint64_t adesc = smemDesc(a_addr);
+          const uint64_t bdesc = smemDesc(a_addr + kTileBytes);
+          // 128 bytes of K per stage: four MMAs of 32 bytes (K = 16 BF16 or
+          // 32 FP8); the start address advances inside the swizzle atom.
+#pragma unroll
+          for (int kk = 0; kk < 4; ++kk) {
+            mmaIssue<kKind>(d, adesc + 2 * kk, bdesc + 2 * kk, (kt | kk) != 0);
+          }
+          mmaCommit(smemAddr(&empty[stage]));
+          if (++stage == kStages) {
+            stage = 0;
+            phase ^= 1;
+          }
+        }
+        mmaCommit(smemAddr(&acc_full[acc]));
+        if (++acc == 2) {
+          acc = 0;
+          acc_phase ^= 1;
+        }
+      }
+    }
+  } else {
+    // Epilogue: thread t owns accumulator row t (TMEM lane t).
+    int acc = 0;
+    uint32_t acc_phase = 0;
+    for (int item = blockIdx.x; item < args.items; item += gridDim.x) {
+      const int4 w = args.work[item];
+      if (!mbarWait(smemAddr(&acc_full[acc]), acc_phase, args.status, abort_flag)) break;
+      asm volatile("tcgen05.fence::after_thread_sync;");
+      const int mi = w.x;
+      const int n = args.n[mi];
+      const int i = w.y * kTileRows + threadIdx.x;
+      const int j0 = w.z * kTileRows;
+      float *X = args.x + args.x_offset[mi];
+      float ri = 1.0f;
+      const float *rs = nullptr;
+      if (kKind == kOpFp8) {
+        rs = args.row_scale + args.eig_offset[mi];
+        ri = i < n ? rs[i] : 0.0f;
+      }
+#pragma unroll 1
+      for (int c = 0; c < 4; ++c) {
+        float v[32];
+        tmemLoad32(tmem + ((32u * warp) << 16) + acc * 128 + c * 32, v);
+        if (i < n) {
+#pragma unroll
+          for (int q = 0; q < 32; ++q) {
+            const int j = j0 + c * 32 + q;
+            if (j < n) {
+              float val = v[q];
+              if (kKind == kOpFp8) val = val * ri * rs[j];
+              X[i + static_cast<int64_t>(j) * n] = val;
+            }
+          }
+        }
+      }
+      asm volatile("tcgen05.fence::before_thread_sync;");
+      mbarArrive(smemAddr(&acc_empty[acc]));
+      if (++acc == 2) {
+        acc = 0;
+        acc_phase ^= 1;
+      }
+    }
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;");
+  __syncthreads();
+  asm volatile("tcgen05.fence::after_thread_sync;");
+  if (warp == 5) {
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem),
+                 "r"(kTmemCols));
+  }
+}
+
+// ------------------------------------------------------------ packing
+
+enum PackSource : int {
+  kPackF32Bf16 = 0,     // FP32 factor -> BF16
+  kPackF32Fp8Row = 1,   // FP32 factor / row scale -> E4M3
+  kPackF32Mxfp4 = 2,    // FP32 factor -> MXFP4 values, decoded into BF16
+  kPackBf16Codes = 3,   // flat BF16 codes
+  kPackFp8Codes = 4,    // flat E4M3 codes (row scales separate)
+  kPackMxfp4Codes = 5,  // flat MXFP4 codes + E8M0 scales, decoded into BF16
+};
+
+struct PackArgs {
+  const int4 *work;       // (matrix, tile_m, tile_k, k_tiles)
+  int items;
+  const float *f;         // FP32 factor, K-major (F[k + i*n] = W_ik)
+  const uint8_t *codes;   // flat codes in the same layout
+  const uint8_t *mx_scales;
+  const float *row_scale;
+  const int64_t *f_offset;
+  const int64_t *eig_offset;
+  const int64_t *tile_base;
+  const int32_t *n;
+  uint8_t *tiles;
+};
+
+// One CTA of 128 threads per tile; thread r packs row r (128 bytes).
+template <int kSource>
+__global__ void __launch_bounds__(128) packKernel(PackArgs args) {
+  for (int item = blockIdx.x; item < args.items; item += gridDim.x) {
+    const int4 w = args.work[item];
+    const int mi = w.x, n = args.n[mi];
+    const int r = threadIdx.x;
+    const int i = w.y * kTileRows + r;
+    constexpr bool kFp8 = kSource == kPackF32Fp8Row || kSource == kPackFp8Codes;
+    constexpr int kElems = kFp8 ? 128 : 64;  // elements per 128-byte row
+    const int k0 = w.z * kElems;
+    const int64_t off = args.f_offset[mi];
+    uint8_t *tile = args.tiles + (args.tile_base[mi] + static_cast<int64_t>(w.y) * w.w + w.z) *
+                                     kTileBytes;
+    const bool row_ok = i < n;
+    float inv_scale_row = 1.0f;
+    if (kSource == kPackF32Fp8Row && row_ok) inv_scale_row = args.row_scale[args.eig_offset[mi] + i];
+    // MX block exponents for the two 32-element blocks of this row segment
+    int mx_e[2] = {0, 0};
+    if (kSource == kPackF32Mxfp4 && row_ok) {
+      for (int blk = 0; blk < 2; ++blk) {
+        float m = 0.0f;
+        for (int e = 0; e < 32; ++e) {
+          const int k = k0 + blk * 32 + e;
+          if (k < n) {
+            const float a = fabsf(args.f[off + k + static_cast<int64_t>(i) * n]);
+            if (a <= 3.402823466e38f) m = fmaxf(m, a);
+          }
+        }
+        mx_e[blk] = mxExponent(m, 2);
+      }
+    }
+#pragma unroll 1
+    for (int c = 0; c < 8; ++c) {
+      uint32_t word[4] = {0, 0, 0, 0};
+      if (row_ok) {
+        if constexpr (kFp8) {
+#pragma unroll
+          for (int e = 0; e < 16; ++e) {
+            const int k = k0 + c * 16 + e;
+            uint32_t code = 0;
+            if (k < n) {
+              const int64_t at = off + k + static_cast<int64_t>(i) * n;
+              code = kSource == kPackFp8Codes ? args.codes[at]
+                                              : encodeE4M3(rowDivide(args.f[at], inv_scale_row));
+            }
+            word[e / 4] |= code << (8 * (e % 4));
+          }
+        } else {
+#pragma unroll
+          for (int e = 0; e < 8; ++e) {
+            const int k = k0 + c * 8 + e;
+            uint32_t h = 0;
+            if (k < n) {
+              const int64_t at = off + k + static_cast<int64_t>(i) * n;
+              if (kSource == kPackF32Bf16) {
+                h = encodeBf16(args.f[at]);
+              } else if (kSource == kPackBf16Codes) {
+                h = reinterpret_cast<const uint16_t *>(args.codes)[at];
+              } else if (kSource == kPackF32Mxfp4) {
+                const int ex = mx_e[(c * 8 + e) / 32];
+                const float q = mxScale(decodeE2M1(encodeE2M1(mxDivide(args.f[at], ex))),
+                                        static_cast<uint32_t>(ex + 127));
+                h = encodeBf16(q);  // exact: at most 2 significant bits
+              } else {  // kPackMxfp4Codes
+                const uint32_t byte = args.codes[at / 2];
+                const float d = decodeE2M1((byte >> ((at & 1) * 4)) & 0xfu);
+                h = encodeBf16(mxScale(d, args.mx_scales[at / 32]));
+              }
+            }
+            word[e / 2] |= h << (16 * (e % 2));
+          }
+        }
+      }
+      *reinterpret_cast<uint4 *>(tile + swizzle128(r, c)) =
+          make_uint4(word[0], word[1], word[2], word[3]);
+    }
+  }
+}
+
+// Row scales of the FP8 factor: r_i = max_k |W_ik| / 448 (1 for a zero
+// row), the MSQ_FMT_FP8_E4M3FN_ROWSCALE definition with rows of W^T's
+// K-major storage.  One warp per row.
+__global__ void rowScaleKernel(const float *__restrict__ f, const int32_t *__restrict__ nn,
+                               const int64_t *__restrict__ off, const int64_t *__restrict__ eoff,
+                               int count, int64_t total_rows, const int32_t *__restrict__ row_matrix,
+                               float *__restrict__ out) {
+  const int lane = threadIdx.x % 32;
+  for (int64_t row = (blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x) / 32;
+       row < total_rows; row += static_cast<int64_t>(gridDim.x) * blockDim.x / 32) {
+    const int mi = row_matrix[row];
+    const int n = nn[mi];
+    const int i = static_cast<int>(row - eoff[mi]);
+    const float *src = f + off[mi] + static_cast<int64_t>(i) * n;
+    float m = 0.0f;
+    for (int k = lane; k < n; k += 32) {
+      const float a = fabsf(src[k]);
+      if (a <= 3.402823466e38f) m = fmaxf(m, a);
+    }
+#pragma unroll
+    for (int s = 16; s > 0; s >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, s));
+    if (lane == 0) out[row] = m == 0.0f ? 1.0f : __fdiv_rn(m, 448.0f);
+  }
+}
+
+// Per-layout tile plan (packing work, GEMM work, tile bases).
+struct TcPlan {
+  uint64_t key;
+  int count;
+  int kind;
+  int device_id;
+  int pack_items, gemm_items;
+  int64_t total_tiles;
+  int4 *pack_work, *gemm_work;
+  int64_t *tile_base;
+  int32_t *row_matrix;
+  void *device;
+};
+std::vector<TcPlan *> g_tc_plans;
+
+TcPlan *tcPlan(msq_ctx *ctx, const DeviceBatch *b, int kind) {
+  for (TcPlan *p : g_tc_plans)
+    if (p->key == b->key && p->count == b->count && p->kind == kind && p->device_id == ctx->device)
+      return p;
+  const int elems = kind == kOpFp8 ? 128 : 64;
+  std::vector<int64_t> base(b->count);
+  std::vector<int4> pack, gemm;
+  std::vector<int32_t> row_matrix;
+  int64_t tiles = 0;
+  std::vector<int> ids(b->count);
+  for (int i = 0; i < b->count; ++i) ids[i] = i;
+  std::stable_sort(ids.begin(), ids.end(),
+                   [&](int x, int y) { return b->host_n[x] > b->host_n[y]; });
+  for (int mi = 0; mi < b->count; ++mi) {
+    const int n = b->host_n[mi];
+    const int mt = (n + kTileRows - 1) / kTileRows, kt = (n + elems - 1) / elems;
+    base[mi] = tiles;
+    tiles += static_cast<int64_t>(mt) * kt;
+    for (int a = 0; a < mt; ++a)
+      for (int k = 0; k < kt; ++k) pack.push_back(make_int4(mi, a, k, kt));
+    for (int r = 0; r < n; ++r) row_matrix.push_back(mi);
+  }
+  for (int mi : ids) {
+    const int n = b->host_n[mi];
+    const int mt = (n + kTileRows - 1) / kTileRows, kt = (n + elems - 1) / elems;
+    for (int a = 0; a < mt; ++a)
+      for (int c = 0; c < mt; ++c) gemm.push_back(make_int4(mi, a, c, kt));
+  }
+  auto *p = new TcPlan{};
+  p->key = b->key;
+  p->count = b->count;
+  p->kind = kind;
+  p->device_id = ctx->device;
+  p->pack_items = static_cast<int>(pack.size());
+  p->gemm_items = static_cast<int>(gemm.size());
+  p->total_tiles = tiles;
+  const size_t bytes = (pack.size() + gemm.size()) * sizeof(int4) + base.size() * sizeof(int64_t) +
+                       row_matrix.size() * sizeof(int32_t) + 64;
+  char *dev = nullptr;
+  if (cudaCheck(ctx, cudaMalloc(&dev, bytes), "tc plan alloc") != MSQ_OK) {
+    delete p;
+    return nullptr;
+  }
+  p->device = dev;
+  p->pack_work = reinterpret_cast<int4 *>(dev);
+  p->gemm_work = p->pack_work + pack.size();
+  p->tile_base = reinterpret_cast<int64_t *>(p->gemm_work + gemm.size());
+  p->row_matrix = reinterpret_cast<int32_t *>(p->tile_base + base.size());
+  cudaMemcpy(p->pack_work, pack.data(), pack.size() * sizeof(int4), cudaMemcpyHostToDevice);
+  cudaMemcpy(p->gemm_work, gemm.data(), gemm.size() * sizeof(int4), cudaMemcpyHostToDevice);
+  cudaMemcpy(p->tile_base, base.data(), base.size() * sizeof(int64_t), cudaMemcpyHostToDevice);
+  cudaMemcpy(p->row_matrix, row_matrix.data(), row_matrix.size() * sizeof(int32_t),
+             cudaMemcpyHostToDevice);
+  if (g_tc_plans.size() >= 16) {
+    cudaFree(g_tc_plans.front()->device);
+    delete g_tc_plans.front();
+    g_tc_plans.erase(g_tc_plans.begin());
+  }
+  g_tc_plans.push_back(p);
+  return p;
+}
+
+size_t tcSmemBytes() { return kStages * 2 * kTileBytes + 1024 + 256; }
+
+int runTcGemm(msq_ctx *ctx, const DeviceBatch *b, TcPlan *p, const uint8_t *tiles,
+              const float *row_scale, float *x) {
+  TcArgs args{};
+  args.work = p->gemm_work;
+  args.items = p->gemm_items;
+  args.tiles = tiles;
+  args.tile_base = p->tile_base;
+  args.n = b->n;
+  args.x_offset = b->offset;
+  args.eig_offset = b->eig_offset;
+  args.row_scale = row_scale;
+  args.x = x;
+  args.status = ctx->d_status;
+  const unsigned grid = std::min(p->gemm_items, kSmCount);
+  static bool attr = false;
+  if (!attr) {
+    MSQ_TRY(cudaCheck(ctx, cudaFuncSetAttribute(tcGemmKernel<kOpBf16>,
+                                                cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                static_cast<int>(tcSmemBytes())), "tc attr"));
+    MSQ_TRY(cudaCheck(ctx, cudaFuncSetAttribute(tcGemmKernel<kOpFp8>,
+                                                cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                static_cast<int>(tcSmemBytes())), "tc attr"));
+    attr = true;
+  }
+  if (p->kind == kOpFp8) {
+    tcGemmKernel<kOpFp8><<<grid, kTcThreads, tcSmemBytes(), ctx->stream>>>(args);
+  } else {
+    tcGemmKernel<kOpBf16><<<grid, kTcThreads, tcSmemBytes(), ctx->stream>>>(args);
+  }
+  return launched(ctx, "tcgen05 reconstruction");
+}
+
+template <int kSource>
+int launchPack(msq_ctx *ctx, const DeviceBatch *b, TcPlan *p, const float *f,
+               const uint8_t *codes, const uint8_t *mx_scales, const float *row_scale,
+               uint8_t *tiles) {
+  PackArgs args{};
+  args.work = p->pack_work;
+  args.items = p->pack_items;
+  args.f = f;
+  args.codes = codes;
+  args.mx_scales = mx_scales;
+  args.row_scale = row_scale;
+  args.f_offset = b->offset;
+  args.eig_offset = b->eig_offset;
+  args.tile_base = p->tile_base;
+  args.n = b->n;
+  args.tiles = tiles;
+  packKernel<kSource><<<std::min(p->pack_items, kSmCount * 16), 128, 0, ctx->stream>>>(args);
+  return launched(ctx, "pack operand");
+}
+
+}  // namespace
+
+int reconstructLowBit(msq_ctx *ctx, const DeviceBatch *b, int format, const float *f, float *x) {
+  const int kind = format == MSQ_FMT_FP8_E4M3FN_ROWSCALE ? kOpFp8 : kOpBf16;
+  TcPlan *p = tcPlan(ctx, b, kind);
+  if (p == nullptr) return MSQ_ERR_CUDA;
+  const size_t tile_bytes = static_cast<size_t>(p->total_tiles) * kTileBytes;
+  const size_t rs_bytes = (b->total_order * sizeof(float) + 255) & ~size_t(255);
+  uint8_t *mem = static_cast<uint8_t *>(scratch(ctx, tile_bytes + rs_bytes, kScratchOperand));
+  if (mem == nullptr) return MSQ_ERR_CUDA;
+  float *row_scale = reinterpret_cast<float *>(mem + tile_bytes);
+  switch (format) {
+    case MSQ_FMT_BF16:
+      MSQ_TRY(launchPack<kPackF32Bf16>(ctx, b, p, f, nullptr, nullptr, nullptr, mem));
+      break;
+    case MSQ_FMT_FP8_E4M3FN_ROWSCALE:
+      rowScaleKernel<<<gridFor(b->total_order * 32, 256), 256, 0, ctx->stream>>>(
+          f, b->n, b->offset, b->eig_offset, b->count, b->total_order, p->row_matrix, row_scale);
+      MSQ_TRY(launched(ctx, "row scales"));
+      MSQ_TRY(launchPack<kPackF32Fp8Row>(ctx, b, p, f, nullptr, nullptr, row_scale, mem));
+      break;
+    case MSQ_FMT_MXFP4_E2M1:
+      MSQ_TRY(launchPack<kPackF32Mxfp4>(ctx, b, p, f, nullptr, nullptr, nullptr, mem));
+      break;
+    default:
+      return setError(ctx, MSQ_ERR_UNSUPPORTED, "reconstruction format not supported");
+  }
+  return runTcGemm(ctx, b, p, mem, row_scale, x);
+}
+
+int reconstructEncoded(msq_ctx *ctx, const DeviceBatch *b, int format, const void *values,
+                       const float *scales, float *x) {
+  const int kind = format == MSQ_FMT_FP8_E4M3FN_ROWSCALE ? kOpFp8 : kOpBf16;
+  if (format != MSQ_FMT_BF16 && format != MSQ_FMT_FP8_E4M3FN_ROWSCALE &&
+      format != MSQ_FMT_MXFP4_E2M1) {
+    return setError(ctx, MSQ_ERR_UNSUPPORTED, "msq_reconstruct: format not supported");
+  }
+  if (format != MSQ_FMT_BF16 && scales == nullptr) {
+    return setError(ctx, MSQ_ERR_INVALID_ARGUMENT, "msq_reconstruct: scales required");
+  }
+  TcPlan *p = tcPlan(ctx, b, kind);
+  if (p == nullptr) return MSQ_ERR_CUDA;
+  uint8_t *mem = static_cast<uint8_t *>(
+      scratch(ctx, static_cast<size_t>(p->total_tiles) * kTileBytes, kScratchOperand));
+  if (mem == nullptr) return MSQ_ERR_CUDA;
+  const uint8_t *codes = static_cast<const uint8_t *>(values);
+  switch (format) {
+    case MSQ_FMT_BF16:
+      MSQ_TRY(launchPack<kPackBf16Codes>(ctx, b, p, nullptr, codes, nullptr, nullptr, mem));
+      break;
+    case MSQ_FMT_FP8_E4M3FN_ROWSCALE:
+      MSQ_TRY(launchPack<kPackFp8Codes>(ctx, b, p, nullptr, codes, nullptr, scales, mem));
+      break;
+    default:
+      MSQ_TRY(launchPack<kPackMxfp4Codes>(ctx, b, p, nullptr, codes,
+                                          reinterpret_cast<const uint8_t *>(scales), nullptr, mem));
+      break;
+  }
+  return runTcGemm(ctx, b, p, mem, scales, x);
+}
+
+}  // namespace msq

@@ -28,7 +28,8 @@ def test_single_matrix_eigenpairs(ctx, msq, n):
     v, w = vs[0], ws[0]
     ref = np.linalg.eigvalsh(a)
     scale = np.abs(ref).max()
-    np.testing.assert_allclose(np.sort(w), ref, rtol=0, atol=5e-6 * scale)
+    # FP32 Jacobi: eigenvalue error grows like n * u * ||A||_2
+    np.testing.assert_allclose(np.sort(w), ref, rtol=0, atol=max(5e-6, 3e-8 * n) * scale)
     np.testing.assert_allclose(v.T @ v, np.eye(n), atol=5e-6 * max(1, np.sqrt(n) / 4))
     # A V = V diag(w)
     resid = np.linalg.norm(a @ v - v * w) / np.linalg.norm(a)
@@ -43,7 +44,7 @@ def test_global_path_orders(ctx, msq, n):
     a = O.wishart(n, seed=n)
     vs, ws, sweeps, off, _ = _run(ctx, msq, [a])
     ref = np.linalg.eigvalsh(a)
-    np.testing.assert_allclose(np.sort(ws[0]), ref, rtol=0, atol=5e-6 * np.abs(ref).max())
+    np.testing.assert_allclose(np.sort(ws[0]), ref, rtol=0, atol=3e-8 * n * np.abs(ref).max())
     assert np.linalg.norm(a @ vs[0] - vs[0] * ws[0]) / np.linalg.norm(a) < 2e-5
 
 
@@ -65,7 +66,7 @@ def test_uneven_batch(ctx, msq):
     vs, ws, sweeps, off, _ = _run(ctx, msq, mats)
     for a, v, w in zip(mats, vs, ws):
         ref = np.linalg.eigvalsh(a)
-        np.testing.assert_allclose(np.sort(w), ref, rtol=0, atol=1e-5 * np.abs(ref).max())
+        np.testing.assert_allclose(np.sort(w), ref, rtol=0, atol=max(1e-5, 3e-8 * len(w)) * np.abs(ref).max())
     assert np.all(off <= 1e-7)
 
 

@@ -1,0 +1,216 @@
+"""GPU parity of the pipeline stages after the eigensolver: factor,
+tcgen05 low-bit reconstruction, float-float residual, Sylvester sweep and the
+batched solve — each against the CPU oracle on the same inputs."""
+import numpy as np
+import pytest
+
+import oracle as O
+
+pytestmark = pytest.mark.gpu
+
+
+def _batch(msq, mats):
+    b = msq.Batch.from_orders([m.shape[0] for m in mats])
+    return b
+
+
+def _dev(x):
+    import torch
+    return torch.from_numpy(np.ascontiguousarray(x, np.float32)).cuda()
+
+
+def _eig_inputs(msq, orders, seed=0):
+    """Random orthonormal V and positive lambda per matrix (FP32)."""
+    rng = np.random.default_rng(seed)
+    vs, ws = [], []
+    for n in orders:
+        q = np.linalg.qr(rng.standard_normal((n, n)))[0].astype(np.float32)
+        vs.append(q)
+        ws.append(np.exp(rng.uniform(np.log(1e-3), 0, n)).astype(np.float32))
+    return vs, ws
+
+
+def _factor_oracle(v, w):
+    """F = W^T with W = V diag(lambda^(1/4)), as float32 (K-major storage of
+    W^T is the column-major storage of W^T)."""
+    return (v.astype(np.float32) * np.sqrt(np.sqrt(w)).astype(np.float32)).T.astype(np.float32)
+
+
+ORDERS = [1, 2, 16, 100, 128, 129, 257, 512]
+
+
+def test_make_factor(ctx, msq):
+    import torch
+    vs, ws = _eig_inputs(msq, ORDERS)
+    b = _batch(msq, vs)
+    f = ctx.make_factor(_dev(b.pack(vs)), _dev(np.concatenate(ws)), b)
+    torch.cuda.synchronize()
+    fs = b.unpack(f.cpu().numpy(), np.float32)
+    for v, w, fg in zip(vs, ws, fs):
+        fo = _factor_oracle(v, w)
+        # fg is stored column-major; column i holds row i of W
+        np.testing.assert_allclose(fg, fo, rtol=2e-6, atol=1e-7)
+
+
+def _quantized_factor(fmt, f):
+    """Oracle quantize/decode of F = W^T, one K-major row (column of F) at a time."""
+    n = f.shape[0]
+    cols = []
+    for i in range(n):
+        col = np.ascontiguousarray(f[:, i], np.float32)
+        if fmt == "bf16":
+            v, s = O.encode(1, col)
+            cols.append(O.decode(1, v, s, n))
+        elif fmt == "fp8row":
+            v, s = O.encode(8, col, row_length=n)
+            cols.append(O.decode(8, v, s, n, row_length=n))
+        elif fmt == "mxfp4":
+            v, s = O.encode(7, col)
+            cols.append(O.decode(7, v, s, n))
+    return np.stack(cols, axis=1).astype(np.float64)
+
+
+@pytest.mark.parametrize("fmt,plan", [("bf16", 1), ("fp8row", 2), ("mxfp4", 3)])
+def test_tcgen05_reconstruction_matches_oracle(ctx, msq, fmt, plan):
+    """X0 = Wq Wq^T from the tensor cores vs the FP64 product of the oracle's
+    quantized factor: only FP32 accumulation error remains."""
+    import torch
+    vs, ws = _eig_inputs(msq, ORDERS, seed=1)
+    b = _batch(msq, vs)
+    f = ctx.make_factor(_dev(b.pack(vs)), _dev(np.concatenate(ws)), b)
+    solver_plan = [msq.plan(plan, 0, 1.0, 0)] * b.count
+    # run only the reconstruction through the solver entry (Jacobi skipped by
+    # a zero sweep budget on an already diagonal input is not possible), so
+    # call the C ABI stage directly with pre-encoded codes where possible
+    fs = b.unpack(f.cpu().numpy(), np.float32)
+    for i, (fg, n) in enumerate(zip(fs, b.n)):
+        fq = _quantized_factor(fmt, fg)
+        x_ref = fq.T @ fq
+        # encode on the GPU with the flat codec (same codes as the oracle)
+        col_major = np.ascontiguousarray(fg.reshape(-1, order="F"))
+        single = msq.Batch.from_orders([int(n)])
+        if fmt == "bf16":
+            vals, scl = ctx.copy_to_storage(msq.BF16, _dev(col_major))
+            x = ctx.reconstruct(msq.BF16, vals, None, single)
+        elif fmt == "fp8row":
+            vals, scl = ctx.copy_to_storage(msq.FP8_E4M3FN_ROWSCALE, _dev(col_major), int(n))
+            x = ctx.reconstruct(msq.FP8_E4M3FN_ROWSCALE, vals, scl, single)
+        else:
+            if n % 32:
+                continue  # flat MX blocks cross K-rows; the factor path covers ragged n
+            vals, scl = ctx.copy_to_storage(msq.MXFP4_E2M1, _dev(col_major))
+            x = ctx.reconstruct(msq.MXFP4_E2M1, vals, scl, single)
+        torch.cuda.synchronize()
+        xg = single.unpack(x.cpu().numpy())[0]
+        err = np.linalg.norm(xg - x_ref) / np.linalg.norm(x_ref)
+        assert err < 2e-6, (fmt, int(n), err)
+
+
+@pytest.mark.parametrize("plan,fmt", [(1, "bf16"), (2, "fp8row"), (3, "mxfp4")])
+def test_solver_reconstruction_path(ctx, msq, plan, fmt):
+    """Through msq_solve_batched with zero sweeps, the reported initial
+    residual equals the oracle's residual of Wq Wq^T built from the solver's
+    own eigenpairs (checked loosely: same quantization, FP32 accumulation)."""
+    import torch
+    orders = [16, 96, 200]
+    mats = [O.spd_loguniform(n, 1e2, seed=n) for n in orders]
+    b = _batch(msq, mats)
+    a = _dev(b.pack(mats))
+    plans = [msq.plan(plan, 0, 1e-7, 15)] * b.count
+    root, res = ctx.solve_batched(a, b, plans, tolerance=1.0)
+    torch.cuda.synchronize()
+    roots = b.unpack(root.cpu().numpy())
+    expect = {"bf16": 2e-2, "fp8row": 2e-1, "mxfp4": 1.0}[fmt]
+    for i, (m, x) in enumerate(zip(mats, roots)):
+        r = O.relative_residual(m, x)
+        assert abs(r - res[i].initial_residual) <= 1e-3 * r + 1e-6
+        assert r < expect
+
+
+def test_float_float_residual_matches_oracle(ctx, msq):
+    import torch
+    orders = [1, 3, 17, 64, 130]
+    mats = [O.spd_loguniform(n, 1e3, seed=n).astype(np.float32) for n in orders]
+    xs = [O.reference_root(m.astype(np.float64)) for m in mats]
+    x_hi = [x.astype(np.float32) for x in xs]
+    x_lo = [(x - xh.astype(np.float64)).astype(np.float32) for x, xh in zip(xs, x_hi)]
+    b = _batch(msq, mats)
+    r, norms = ctx.residual(_dev(b.pack(mats)), _dev(b.pack(x_hi)), _dev(b.pack(x_lo)), b)
+    torch.cuda.synchronize()
+    rs = b.unpack(r.cpu().numpy())
+    norms = norms.cpu().numpy()
+    for i, (m, xh, xl) in enumerate(zip(mats, x_hi, x_lo)):
+        rel_o, r_o = O.ff_residual(m, xh, xl)
+        x64 = xh.astype(np.float64) + xl
+        r64 = m.astype(np.float64) - x64 @ x64
+        np.testing.assert_allclose(rs[i], r64, rtol=0, atol=1e-10 * np.abs(m).max())
+        rel_g = np.sqrt(norms[2 * i] / norms[2 * i + 1])
+        assert abs(rel_g - np.linalg.norm(r64) / np.linalg.norm(m)) < 1e-12
+        assert abs(rel_g - rel_o) < 1e-12
+
+
+def test_sylvester_sweep_matches_fp64_correction(ctx, msq):
+    """One frozen-basis correction on the GPU vs the same correction in FP64
+    (refineUpdateAndMeasure semantics) from the same X0, V, lambda."""
+    import torch
+    orders = [8, 64, 150]
+    mats = [O.spd_loguniform(n, 1e2, seed=3 * n) for n in orders]
+    vs, ws, x0s = [], [], []
+    for m in mats:
+        w, v = np.linalg.eigh(m)
+        v32, w32 = v.astype(np.float32), w.astype(np.float32)
+        vq = O.decode(1, *O.encode(1, v32.reshape(-1)), v32.size).reshape(v32.shape)
+        x0s.append(((vq.astype(np.float64) * np.sqrt(w32)) @ vq.T).astype(np.float32))
+        vs.append(v32)
+        ws.append(w32)
+    b = _batch(msq, mats)
+    a_d = _dev(b.pack(mats))
+    xh = _dev(b.pack(x0s))
+    xl = torch.zeros_like(xh)
+    r, norms = ctx.residual(a_d, xh, xl, b)
+    ctx.sylvester_sweep(msq.FP32, _dev(b.pack(vs)), _dev(np.concatenate(ws)), r, b, xh, xl)
+    r2, norms2 = ctx.residual(a_d, xh, xl, b)
+    torch.cuda.synchronize()
+    x1 = [h.astype(np.float64) + l for h, l in zip(b.unpack(xh.cpu().numpy()), b.unpack(xl.cpu().numpy()))]
+    n0 = norms.cpu().numpy()
+    n1 = norms2.cpu().numpy()
+    for i, (m, v, w, x0) in enumerate(zip(mats, vs, ws, x0s)):
+        v64, s = v.astype(np.float64), np.sqrt(w.astype(np.float64))
+        r64 = m - x0.astype(np.float64) @ x0.astype(np.float64)
+        c = (v64.T @ r64 @ v64) / (s[:, None] + s[None, :])
+        e = v64 @ c @ v64.T
+        x_ref = x0 + 0.5 * (e + e.T)
+        err = np.linalg.norm(x1[i] - x_ref) / np.linalg.norm(x_ref)
+        assert err < 1e-6, err
+        assert np.sqrt(n1[2 * i] / n1[2 * i + 1]) < 0.05 * np.sqrt(n0[2 * i] / n0[2 * i + 1])
+
+
+@pytest.mark.parametrize("plan,sweeps", [(0, 0), (1, 1), (1, 2), (2, 2), (3, 2)])
+def test_solve_batched_meets_tolerance(ctx, msq, plan, sweeps):
+    import torch
+    orders = O.wishart_orders(24, 16, 300, seed=plan * 10 + sweeps)
+    mats = [O.wishart(int(n), seed=i) for i, n in enumerate(orders)]
+    b = _batch(msq, mats)
+    a = _dev(b.pack(mats))
+    plans = [msq.plan(plan, sweeps, 1e-7 if plan == 0 else 1e-4, 15)] * b.count
+    tol = 1e-5
+    root, res = ctx.solve_batched(a, b, plans, tolerance=tol)
+    torch.cuda.synchronize()
+    for i, (m, x) in enumerate(zip(mats, b.unpack(root.cpu().numpy()))):
+        r_oracle = O.relative_residual(m, x)
+        assert res[i].final_residual <= tol
+        assert r_oracle <= max(2 * res[i].final_residual, 1e-6), (i, r_oracle, res[i].final_residual)
+        err = O.relative_error(x, O.reference_root(m))
+        assert err < 1e-4
+    if plan != 0 and sweeps == 2:
+        assert np.mean([r.accepted for r in res]) > 0.9
+
+
+def test_solve_tiny_orders(ctx, msq):
+    import torch
+    mats = [np.array([[4.0]]), np.array([[2.0, 0.5], [0.5, 1.0]]), O.wishart(3, 1)]
+    b = _batch(msq, mats)
+    root, res = ctx.solve_batched(_dev(b.pack(mats)), b, None, tolerance=1e-5)
+    torch.cuda.synchronize()
+    for m, x in zip(mats, b.unpack(root.cpu().numpy())):
+        assert O.relative_residual(m, x) < 1e-6
