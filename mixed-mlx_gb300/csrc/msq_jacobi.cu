@@ -1,26 +1,33 @@
-// Batched parallel-order two-sided Jacobi eigensolver.
+// Batched blocked parallel-order two-sided Jacobi eigensolver.
 //
 // Replaces MetalRuntime::symmetricJacobi (src/metal_runtime.cpp:584-646),
 // its kernels jacobi_rotations_f32 / jacobi_similarity_vectors_f32 /
 // jacobi_root_eigenvalues_f32 (metal_mixed_sqrt.metal:1319-1444) and the
 // host-built schedule makeJacobiSchedule (src/metal_solver.cpp:50-79).
 //
-// Same algorithm, laid out for GB300:
-//  * the round-robin pairing is computed arithmetically (no schedule
-//    arrays: the reference's needs 3 x n(n-1) u32 per order);
-//  * one CTA owns one matrix for a whole sweep; the upper triangle of A is
-//    kept packed in shared memory (n <= 336 fits the 227 KB limit) and the
-//    disjoint 2x2 blocks of a round are rotated in place, so a round costs
-//    one pass over shared memory instead of a global ping-pong;
-//  * rotation angles and the off-norm are computed in FP64 (the reference
-//    uses FP32 angles and a fixed 8 sweeps; here sweeps stop once
-//    off(A) <= tol * ||A||_F);
-//  * every round's (c, s) is logged and a second, row-parallel kernel
-//    replays the sweep onto V: rows of V evolve independently under
-//    right-multiplication by rotations, so V never competes with A for the
-//    CTA's shared memory;
-//  * launches are size-bucketed (threads per CTA grow with n) and the
-//    largest matrices start first.
+// The reference sweeps all n(n-1)/2 index pairs with a round-robin order,
+// one 2x2 rotation per pair, a full matrix pass per round.  Here the same
+// rotation (tau = (a_qq - a_pp) / (2 a_pq), t = sign(tau) / (|tau| +
+// sqrt(1 + tau^2)), c = 1/sqrt(1 + t^2), s = t c; pivot element set to zero)
+// is applied in a blocked order laid out for GB300:
+//  * indices are grouped in blocks of 4; the blocks are paired by the same
+//    round-robin ("chess tournament") rule, computed arithmetically, so a
+//    sweep has m/4 - 1 rounds instead of m - 1;
+//  * each block pair is an 8x8 pivot that one thread holds in registers and
+//    sweeps once over its 28 index pairs (7 inner round-robin rounds),
+//    accumulating the rotations into an 8x8 orthogonal Q_k;
+//  * every other 8x8 super-tile of A is then updated as T' = Q_k^T T Q_l, a
+//    pair of small dense products held in registers (1024 FMA per 64
+//    elements), so a round is FMA-bound instead of latency-bound;
+//  * the upper triangle of A is stored as packed 4x4 tiles, in shared memory
+//    when it fits (n <= 328) and in an L2-resident global workspace beyond;
+//  * each round's Q_k are logged and a row-parallel kernel replays the sweep
+//    onto V (rows of V evolve independently under V <- V Q), so V never
+//    competes with A for shared memory;
+//  * rotation angles are FP32 (as in the reference's kernel); the off-norm
+//    that ends the sweeps is accumulated in FP64 — sweeps stop once
+//    off(A) <= tol * ||A||_F instead of after a fixed 8;
+//  * launches are size-bucketed (threads per CTA grow with n), largest first.
 #include "msq_internal.cuh"
 
 #include <algorithm>
@@ -29,13 +36,16 @@
 namespace msq {
 namespace {
 
-constexpr int kMaxSmemOrder = 336;  // n(n+1)/2 floats + tables <= 227 KB
-constexpr int kVRowsMax = 32;       // rows of V per CTA in the replay kernel
+constexpr int kTileF = 16;      // floats per 4x4 tile
+constexpr int kQF = 64;         // floats per 8x8 rotation
 constexpr size_t kSmemLimit = 227 * 1024;
+constexpr int kMaxOrder = 2048;
+constexpr int kSweepThreadsMax = 256;
+constexpr int kReplayThreads = 256;
 
 struct JacobiState {
   double norm2;       // ||A||_F^2
-  double off_ratio;   // off(A) / ||A||_F at the start of the last sweep
+  double off_ratio;   // off(A) / ||A||_F when the sweeps stopped
   int sweeps;         // sweeps applied
   int done;           // 1 once converged or out of budget
   int logged;         // 1 if the log holds a sweep not yet applied to V
@@ -43,25 +53,26 @@ struct JacobiState {
 };
 
 struct JacobiArgs {
-  float *a;                 // user matrices (full, column-major)
-  float *packed;            // packed upper triangles (global workspace)
-  const int64_t *a_offset;  // element offset of matrix i in a
-  const int64_t *p_offset;  // element offset of matrix i in packed
-  const int64_t *log_offset;// float2 offset of matrix i's rotation log
+  float *a;                  // user matrices (full, column-major)
+  float *tiles;              // packed 4x4 tiles (global workspace)
+  const int64_t *a_offset;   // element offset of matrix i in a
+  const int64_t *t_offset;   // float offset of matrix i's tiles
+  const int64_t *log_offset; // float offset of matrix i's rotation log
   const int64_t *eig_offset;
   const int32_t *n;
-  float2 *log;
+  float *log;
   float *eigenvalues;
   JacobiState *state;
-  const int32_t *order;     // matrix ids of this launch, largest first
-  int count;
+  const int32_t *order;      // matrix ids of this launch, largest first
   double tol;
   int max_sweeps;
-  int first;                // 1 on the first launch (load from a, set norm)
+  int first;                 // 1 on the first launch (load A, set norm)
 };
 
+__host__ __device__ constexpr int padded8(int n) { return (n + 7) & ~7; }
+
 // Slot -> participant of round r (participants 1..m-1 rotate right by one
-// per round, slot 0 fixed), the closed form of std::rotate in
+// per round, slot 0 fixed): the closed form of the std::rotate step in
 // makeJacobiSchedule (src/metal_solver.cpp:75-76).
 __device__ __forceinline__ int rrSlot(int slot, int round, int m) {
   if (slot == 0) return 0;
@@ -77,12 +88,8 @@ __device__ __forceinline__ void rrPair(int pair, int round, int m, int &p, int &
   q = a < b ? b : a;
 }
 
-__device__ __forceinline__ int packedIndex(const int *tri, int r, int c) {
-  return r <= c ? tri[c] + r : tri[r] + c;
-}
-
-// Folded enumeration of the upper triangle {(i, j): i <= j < P} of pair
-// blocks: rows i and P-1-i share one folded row of P+1 items.
+// Folded enumeration of the upper triangle {(i, j): i <= j < P}: rows i and
+// P-1-i share one folded row of P+1 items.
 __device__ __forceinline__ bool foldedBlock(int w, int P, int &i, int &j) {
   const int r = w / (P + 1);
   const int c = w - r * (P + 1);
@@ -91,7 +98,7 @@ __device__ __forceinline__ bool foldedBlock(int w, int P, int &i, int &j) {
     j = r + c;
     return true;
   }
-  if ((P & 1) && r == P / 2) return false;  // middle row of an odd P
+  if ((P & 1) && r == P / 2) return false;
   i = P - 1 - r;
   j = c - 1;
   return true;
@@ -117,17 +124,130 @@ __device__ double blockReduceSum(double v, double *red) {
   return total;
 }
 
+// Packed tile (I, J), I <= J, of a matrix's tile array.
+__device__ __forceinline__ float *tileAt(float *tiles, const int *tri, int I, int J) {
+  return tiles + static_cast<int64_t>(tri[J] + I) * kTileF;
+}
+
+// Loads block (R, C) of A (4x4, row-major in t) from the packed tiles.
+__device__ __forceinline__ void loadBlock(float *tiles, const int *tri, int R, int C, float (&t)[4][4]) {
+  if (R <= C) {
+    const float4 *src = reinterpret_cast<const float4 *>(tileAt(tiles, tri, R, C));
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+      const float4 v = src[i];
+      t[i][0] = v.x; t[i][1] = v.y; t[i][2] = v.z; t[i][3] = v.w;
+    }
+  } else {
+    const float4 *src = reinterpret_cast<const float4 *>(tileAt(tiles, tri, C, R));
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+      const float4 v = src[i];
+      t[0][i] = v.x; t[1][i] = v.y; t[2][i] = v.z; t[3][i] = v.w;
+    }
+  }
+}
+
+__device__ __forceinline__ void storeBlock(float *tiles, const int *tri, int R, int C, const float (&t)[4][4]) {
+  if (R <= C) {
+    float4 *dst = reinterpret_cast<float4 *>(tileAt(tiles, tri, R, C));
+#pragma unroll
+    for (int i = 0; i < 4; ++i) dst[i] = make_float4(t[i][0], t[i][1], t[i][2], t[i][3]);
+  } else {
+    float4 *dst = reinterpret_cast<float4 *>(tileAt(tiles, tri, C, R));
+#pragma unroll
+    for (int i = 0; i < 4; ++i) dst[i] = make_float4(t[0][i], t[1][i], t[2][i], t[3][i]);
+  }
+}
+
+// One Jacobi rotation of the 8x8 pivot p on the index pair (a, b), the
+// reference's angle formula (metal_mixed_sqrt.metal:1347-1357), accumulated
+// into q (q <- q J).  J = [c s; -s c] on (a, b): column a' = c a - s b,
+// column b' = s a + c b; p <- J^T p J with the pivot element set to zero.
+template <int a, int b>
+__device__ __forceinline__ void rotatePivot(float (&p)[8][8], float (&q)[8][8]) {
+  const float apq = p[a][b];
+  if (apq == 0.0f) return;
+  const float tau = (p[b][b] - p[a][a]) / (2.0f * apq);
+  const float t = copysignf(1.0f / (fabsf(tau) + sqrtf(fmaf(tau, tau, 1.0f))), tau);
+  float c = rsqrtf(fmaf(t, t, 1.0f));
+  float s = t * c;
+  // FP32 (c, s) carry a one-signed error in c^2 + s^2 - 1 that compounds
+  // over the thousands of rotations applied to each row of V.  Evaluate
+  // e = c^2 + s^2 - 1 exactly (two-product: each square split by an FMA;
+  // c^2 >= 1/2 so c^2 - 1 is exact) and pull (c, s) back by (1 - e/2): the
+  // rotation is then as orthogonal as one computed in FP64 and rounded.
+  {
+    const float cc = __fmul_rn(c, c), cce = fmaf(c, c, -cc);
+    const float ss = __fmul_rn(s, s), sse = fmaf(s, s, -ss);
+    const float e = __fadd_rn(__fadd_rn(__fsub_rn(cc, 1.0f), ss), __fadd_rn(cce, sse));
+    const float h = -0.5f * e;
+    c = fmaf(h, c, c);
+    s = fmaf(h, s, s);
+  }
+#pragma unroll
+  for (int i = 0; i < 8; ++i) {
+    const float pa = p[i][a], pb = p[i][b];
+    p[i][a] = c * pa - s * pb;
+    p[i][b] = s * pa + c * pb;
+  }
+#pragma unroll
+  for (int j = 0; j < 8; ++j) {
+    const float pa = p[a][j], pb = p[b][j];
+    p[a][j] = c * pa - s * pb;
+    p[b][j] = s * pa + c * pb;
+  }
+  p[a][b] = 0.0f;
+  p[b][a] = 0.0f;
+#pragma unroll
+  for (int i = 0; i < 8; ++i) {
+    const float qa = q[i][a], qb = q[i][b];
+    q[i][a] = c * qa - s * qb;
+    q[i][b] = s * qa + c * qb;
+  }
+}
+
+// One cyclic sweep over the 28 pairs of the pivot in round-robin order
+// (7 rounds of 4 disjoint pairs; disjoint rotations commute).
+__device__ __forceinline__ void sweepPivot(float (&p)[8][8], float (&q)[8][8]) {
+  rotatePivot<0, 7>(p, q); rotatePivot<1, 6>(p, q); rotatePivot<2, 5>(p, q); rotatePivot<3, 4>(p, q);
+  rotatePivot<0, 6>(p, q); rotatePivot<5, 7>(p, q); rotatePivot<1, 4>(p, q); rotatePivot<2, 3>(p, q);
+  rotatePivot<0, 5>(p, q); rotatePivot<4, 6>(p, q); rotatePivot<3, 7>(p, q); rotatePivot<1, 2>(p, q);
+  rotatePivot<0, 4>(p, q); rotatePivot<3, 5>(p, q); rotatePivot<2, 6>(p, q); rotatePivot<1, 7>(p, q);
+  rotatePivot<0, 3>(p, q); rotatePivot<2, 4>(p, q); rotatePivot<1, 5>(p, q); rotatePivot<6, 7>(p, q);
+  rotatePivot<0, 2>(p, q); rotatePivot<1, 3>(p, q); rotatePivot<4, 7>(p, q); rotatePivot<5, 6>(p, q);
+  rotatePivot<0, 1>(p, q); rotatePivot<2, 7>(p, q); rotatePivot<3, 6>(p, q); rotatePivot<4, 5>(p, q);
+}
+
+struct SweepSmem {
+  double *red;
+  int *tri;
+  int *pair_i;
+  int *pair_j;
+  float *q;
+  float *tiles;
+};
+
+__host__ __device__ __forceinline__ size_t sweepSmemLayout(int n, bool with_tiles, size_t *q_off,
+                                                           size_t *tile_off) {
+  const int m = padded8(n), nb = m / 4, P = nb / 2;
+  size_t bytes = 32 * sizeof(double) + (nb + 1 + 2 * P) * sizeof(int);
+  bytes = (bytes + 15) & ~static_cast<size_t>(15);
+  *q_off = bytes;
+  bytes += static_cast<size_t>(P) * kQF * sizeof(float);
+  *tile_off = bytes;
+  if (with_tiles) bytes += static_cast<size_t>(nb) * (nb + 1) / 2 * kTileF * sizeof(float);
+  return bytes;
+}
+
 // One sweep (or the convergence check / write-back) for one matrix per CTA.
-// kSmem: packed A staged in shared memory; otherwise it is rotated in place
-// in the global packed workspace (L2-resident at these orders).
 template <bool kSmem>
-__global__ void __launch_bounds__(1024)
+__global__ void __launch_bounds__(kSweepThreadsMax)
 jacobiSweepKernel(JacobiArgs args) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int mi = args.order[blockIdx.x];
   const int n = args.n[mi];
-  const int m = n + (n & 1);
-  const int P = m / 2;
+  const int m = padded8(n), nb = m / 4, P = nb / 2;
   JacobiState &st = args.state[mi];
   // Snapshot of the state before any thread writes it (the barriers below
   // keep thread 0's final update after every warp's snapshot).
@@ -136,43 +256,51 @@ jacobiSweepKernel(JacobiArgs args) {
     if (threadIdx.x == 0) st.logged = 0;
     return;
   }
-
-  double *red = reinterpret_cast<double *>(smem_raw);               // 32
-  int *tri = reinterpret_cast<int *>(red + 32);                      // m + 1
-  int *pair_p = tri + (m + 1);                                       // P
-  int *pair_q = pair_p + P;                                          // P
-  float *pc = reinterpret_cast<float *>(pair_q + P);                 // P
-  float *ps = pc + P;                                                // P
-  float *packed_s = ps + P;
-  float *A = kSmem ? packed_s : args.packed + args.p_offset[mi];
+  size_t q_off, tile_off;
+  sweepSmemLayout(n, kSmem, &q_off, &tile_off);
+  double *red = reinterpret_cast<double *>(smem_raw);
+  int *tri = reinterpret_cast<int *>(red + 32);
+  int *pair_i = tri + nb + 1;
+  int *pair_j = pair_i + P;
+  float *qs = reinterpret_cast<float *>(smem_raw + q_off);
+  float *gtiles = args.tiles + args.t_offset[mi];
+  float *tiles = kSmem ? reinterpret_cast<float *>(smem_raw + tile_off) : gtiles;
+  const int tile_floats = nb * (nb + 1) / 2 * kTileF;
   const float *full = args.a + args.a_offset[mi];
-  float *packed_g = args.packed + args.p_offset[mi];
-  const int tri_n = n * (n + 1) / 2;
 
-  for (int k = threadIdx.x; k <= m; k += blockDim.x) tri[k] = k * (k + 1) / 2;
+  for (int k = threadIdx.x; k <= nb; k += blockDim.x) tri[k] = k * (k + 1) / 2;
   __syncthreads();
 
-  // Stage the packed upper triangle.
   if (args.first) {
-    // Symmetrised load, as working_from_symmetric_f32 and the averaged
-    // a_pq of jacobi_rotations_f32 do (metal_mixed_sqrt.metal:1349-1350).
-    for (int c = 0; c < n; ++c) {
-      for (int r = threadIdx.x; r <= c; r += blockDim.x) {
-        A[tri[c] + r] = 0.5f * (full[r + static_cast<int64_t>(c) * n] +
-                                full[c + static_cast<int64_t>(r) * n]);
+    // Symmetrised load, as working_from_symmetric_f32 and the averaged a_pq
+    // of jacobi_rotations_f32 do (metal_mixed_sqrt.metal:1349-1350, 1922).
+    for (int J = 0; J < nb; ++J) {
+      for (int idx = threadIdx.x; idx < (J + 1) * kTileF; idx += blockDim.x) {
+        const int I = idx / kTileF, e = idx % kTileF;
+        const int gi = 4 * I + e / 4, gj = 4 * J + e % 4;
+        float v = 0.0f;
+        if (gi < n && gj < n) {
+          v = 0.5f * (full[gi + static_cast<int64_t>(gj) * n] + full[gj + static_cast<int64_t>(gi) * n]);
+        }
+        tiles[static_cast<int64_t>(tri[J] + I) * kTileF + e] = v;
       }
     }
   } else if (kSmem) {
-    for (int k = threadIdx.x; k < tri_n; k += blockDim.x) A[k] = packed_g[k];
+    for (int k = threadIdx.x; k < tile_floats / 4; k += blockDim.x) {
+      reinterpret_cast<float4 *>(tiles)[k] = reinterpret_cast<const float4 *>(gtiles)[k];
+    }
   }
   __syncthreads();
 
   // Off-norm and norm in FP64.
   double off2 = 0.0, diag2 = 0.0;
-  for (int c = 0; c < n; ++c) {
-    for (int r = threadIdx.x; r <= c; r += blockDim.x) {
-      const double v = A[tri[c] + r];
-      if (r == c) diag2 += v * v; else off2 += 2.0 * v * v;
+  for (int J = 0; J < nb; ++J) {
+    for (int idx = threadIdx.x; idx < (J + 1) * kTileF; idx += blockDim.x) {
+      const int I = idx / kTileF, e = idx % kTileF;
+      const double v = tiles[static_cast<int64_t>(tri[J] + I) * kTileF + e];
+      if (I < J) off2 += 2.0 * v * v;
+      else if (e / 4 == e % 4) diag2 += v * v;
+      else off2 += v * v;
     }
   }
   off2 = blockReduceSum(off2, red);
@@ -180,19 +308,21 @@ jacobiSweepKernel(JacobiArgs args) {
   const double norm2 = args.first ? off2 + diag2 : s0.norm2;
   const int sweeps = args.first ? 0 : s0.sweeps;
   const double ratio = norm2 > 0.0 ? sqrt(off2 / norm2) : 0.0;
-  const bool stop = ratio <= args.tol || sweeps >= args.max_sweeps;
 
-  if (stop) {
-    {
-      // Eigenvalues = diagonal (jacobi_root_eigenvalues_f32 takes its sqrt
-      // later, :1436-1444); full symmetric write-back of the matrix.
-      float *eig = args.eigenvalues + args.eig_offset[mi];
-      for (int k = threadIdx.x; k < n; k += blockDim.x) eig[k] = A[tri[k] + k];
-      float *out = args.a + args.a_offset[mi];
-      for (int c = 0; c < n; ++c) {
-        for (int r = threadIdx.x; r < n; r += blockDim.x) {
-          out[r + static_cast<int64_t>(c) * n] = A[packedIndex(tri, r, c)];
-        }
+  if (ratio <= args.tol || sweeps >= args.max_sweeps) {
+    // Eigenvalues = diagonal (jacobi_root_eigenvalues_f32 takes the sqrt
+    // later, :1436-1444); full symmetric write-back of the matrix.
+    float *eig = args.eigenvalues + args.eig_offset[mi];
+    for (int k = threadIdx.x; k < n; k += blockDim.x) {
+      eig[k] = tiles[static_cast<int64_t>(tri[k / 4] + k / 4) * kTileF + (k % 4) * 5];
+    }
+    float *out = args.a + args.a_offset[mi];
+    for (int c = 0; c < n; ++c) {
+      for (int r = threadIdx.x; r < n; r += blockDim.x) {
+        const int I = r / 4, J = c / 4;
+        const float v = I <= J ? tiles[static_cast<int64_t>(tri[J] + I) * kTileF + (r % 4) * 4 + c % 4]
+                               : tiles[static_cast<int64_t>(tri[I] + J) * kTileF + (c % 4) * 4 + r % 4];
+        out[r + static_cast<int64_t>(c) * n] = v;
       }
     }
     if (threadIdx.x == 0) {
@@ -205,72 +335,138 @@ jacobiSweepKernel(JacobiArgs args) {
     return;
   }
 
-  float2 *log = args.log + args.log_offset[mi];
-  for (int round = 0; round < m - 1; ++round) {
-    // Angles of the round's disjoint pairs (FP64).
+  float *log = args.log + args.log_offset[mi];
+  const int items = ((P + 1) / 2) * (P + 1);
+  for (int round = 0; round < nb - 1; ++round) {
+    // Pivots: one thread per block pair sweeps its 8x8 pivot in registers.
     for (int k = threadIdx.x; k < P; k += blockDim.x) {
-      int p, q;
-      rrPair(k, round, m, p, q);
-      double cs = 1.0, sn = 0.0;
-      if (q < n) {
-        const double app = A[tri[p] + p];
-        const double aqq = A[tri[q] + q];
-        const double apq = A[tri[q] + p];
-        if (apq != 0.0) {
-          const double tau = (aqq - app) / (2.0 * apq);
-          const double t = copysign(1.0 / (fabs(tau) + sqrt(1.0 + tau * tau)), tau);
-          cs = 1.0 / sqrt(1.0 + t * t);
-          sn = t * cs;
-        }
+      int I, J;
+      rrPair(k, round, nb, I, J);
+      pair_i[k] = I;
+      pair_j[k] = J;
+      float p[8][8], q[8][8];
+      {
+        float t[4][4];
+        loadBlock(tiles, tri, I, I, t);
+#pragma unroll
+        for (int i = 0; i < 4; ++i)
+#pragma unroll
+          for (int j = 0; j < 4; ++j) p[i][j] = t[i][j];
+        loadBlock(tiles, tri, I, J, t);
+#pragma unroll
+        for (int i = 0; i < 4; ++i)
+#pragma unroll
+          for (int j = 0; j < 4; ++j) {
+            p[i][4 + j] = t[i][j];
+            p[4 + j][i] = t[i][j];
+          }
+        loadBlock(tiles, tri, J, J, t);
+#pragma unroll
+        for (int i = 0; i < 4; ++i)
+#pragma unroll
+          for (int j = 0; j < 4; ++j) p[4 + i][4 + j] = t[i][j];
       }
-      pair_p[k] = p;
-      pair_q[k] = q;
-      pc[k] = static_cast<float>(cs);
-      ps[k] = static_cast<float>(sn);
-      log[static_cast<int64_t>(round) * P + k] = make_float2(pc[k], ps[k]);
+#pragma unroll
+      for (int i = 0; i < 8; ++i)
+#pragma unroll
+        for (int j = 0; j < 8; ++j) q[i][j] = i == j ? 1.0f : 0.0f;
+      sweepPivot(p, q);
+      {
+        float t[4][4];
+#pragma unroll
+        for (int i = 0; i < 4; ++i)
+#pragma unroll
+          for (int j = 0; j < 4; ++j) t[i][j] = p[i][j];
+        storeBlock(tiles, tri, I, I, t);
+#pragma unroll
+        for (int i = 0; i < 4; ++i)
+#pragma unroll
+          for (int j = 0; j < 4; ++j) t[i][j] = p[i][4 + j];
+        storeBlock(tiles, tri, I, J, t);
+#pragma unroll
+        for (int i = 0; i < 4; ++i)
+#pragma unroll
+          for (int j = 0; j < 4; ++j) t[i][j] = p[4 + i][4 + j];
+        storeBlock(tiles, tri, J, J, t);
+      }
+      float4 *qdst = reinterpret_cast<float4 *>(qs + k * kQF);
+      float4 *ldst = reinterpret_cast<float4 *>(log + (static_cast<int64_t>(round) * P + k) * kQF);
+#pragma unroll
+      for (int i = 0; i < 8; ++i) {
+        const float4 lo = make_float4(q[i][0], q[i][1], q[i][2], q[i][3]);
+        const float4 hi = make_float4(q[i][4], q[i][5], q[i][6], q[i][7]);
+        qdst[2 * i] = lo;
+        qdst[2 * i + 1] = hi;
+        ldst[2 * i] = lo;
+        ldst[2 * i + 1] = hi;
+      }
     }
     __syncthreads();
-    // A <- J^T A J on every 2x2 block (i <= j); blocks are disjoint.
-    const int items = ((P + 1) / 2) * (P + 1);
+    // Off-pivot super-tiles: T' = Q_k^T T Q_l for every k < l.
     for (int w = threadIdx.x; w < items; w += blockDim.x) {
-      int i, j;
-      if (!foldedBlock(w, P, i, j)) continue;
-      const int pi = pair_p[i], qi = pair_q[i], pj = pair_p[j], qj = pair_q[j];
-      const float ci = pc[i], si = ps[i], cj = pc[j], sj = ps[j];
-      const bool hi = qi < n, hj = qj < n;
-      if (i == j) {
-        if (!hi) continue;
-        const int kpp = tri[pi] + pi, kqq = tri[qi] + qi, kpq = tri[qi] + pi;
-        const float app = A[kpp], aqq = A[kqq], apq = A[kpq];
-        // [c -s; s c]^T-free form of J^T M J for the pivot block
-        const float t0 = ci * app - si * apq, t1 = ci * apq - si * aqq;
-        const float u0 = si * app + ci * apq, u1 = si * apq + ci * aqq;
-        A[kpp] = ci * t0 - si * t1;
-        A[kqq] = si * u0 + ci * u1;
-        A[kpq] = 0.0f;
-        continue;
+      int k, l;
+      if (!foldedBlock(w, P, k, l) || k == l) continue;
+      const int rb[2] = {pair_i[k], pair_j[k]};
+      const int cb[2] = {pair_i[l], pair_j[l]};
+      float t[8][8];
+#pragma unroll
+      for (int x = 0; x < 2; ++x)
+#pragma unroll
+        for (int y = 0; y < 2; ++y) {
+          float b4[4][4];
+          loadBlock(tiles, tri, rb[x], cb[y], b4);
+#pragma unroll
+          for (int i = 0; i < 4; ++i)
+#pragma unroll
+            for (int j = 0; j < 4; ++j) t[4 * x + i][4 * y + j] = b4[i][j];
+        }
+      float u[8][8];
+#pragma unroll
+      for (int a = 0; a < 8; ++a)
+#pragma unroll
+        for (int c = 0; c < 8; ++c) u[a][c] = 0.0f;
+      const float4 *qk = reinterpret_cast<const float4 *>(qs + k * kQF);
+#pragma unroll
+      for (int i = 0; i < 8; ++i) {
+        const float4 lo = qk[2 * i], hi = qk[2 * i + 1];
+        const float qr[8] = {lo.x, lo.y, lo.z, lo.w, hi.x, hi.y, hi.z, hi.w};
+#pragma unroll
+        for (int a = 0; a < 8; ++a)
+#pragma unroll
+          for (int c = 0; c < 8; ++c) u[a][c] = fmaf(qr[a], t[i][c], u[a][c]);
       }
-      const int k00 = packedIndex(tri, pi, pj);
-      const int k01 = hj ? packedIndex(tri, pi, qj) : 0;
-      const int k10 = hi ? packedIndex(tri, qi, pj) : 0;
-      const int k11 = hi && hj ? packedIndex(tri, qi, qj) : 0;
-      const float m00 = A[k00];
-      const float m01 = hj ? A[k01] : 0.0f;
-      const float m10 = hi ? A[k10] : 0.0f;
-      const float m11 = hi && hj ? A[k11] : 0.0f;
-      // T = M J_j, J = [c s; -s c]
-      const float t00 = cj * m00 - sj * m01, t01 = sj * m00 + cj * m01;
-      const float t10 = cj * m10 - sj * m11, t11 = sj * m10 + cj * m11;
-      // M' = J_i^T T
-      A[k00] = ci * t00 - si * t10;
-      if (hj) A[k01] = ci * t01 - si * t11;
-      if (hi) A[k10] = si * t00 + ci * t10;
-      if (hi && hj) A[k11] = si * t01 + ci * t11;
+      const float4 *ql = reinterpret_cast<const float4 *>(qs + l * kQF);
+#pragma unroll
+      for (int a = 0; a < 8; ++a)
+#pragma unroll
+        for (int c = 0; c < 8; ++c) t[a][c] = 0.0f;
+#pragma unroll
+      for (int j = 0; j < 8; ++j) {
+        const float4 lo = ql[2 * j], hi = ql[2 * j + 1];
+        const float qr[8] = {lo.x, lo.y, lo.z, lo.w, hi.x, hi.y, hi.z, hi.w};
+#pragma unroll
+        for (int a = 0; a < 8; ++a)
+#pragma unroll
+          for (int c = 0; c < 8; ++c) t[a][c] = fmaf(u[a][j], qr[c], t[a][c]);
+      }
+#pragma unroll
+      for (int x = 0; x < 2; ++x)
+#pragma unroll
+        for (int y = 0; y < 2; ++y) {
+          float b4[4][4];
+#pragma unroll
+          for (int i = 0; i < 4; ++i)
+#pragma unroll
+            for (int j = 0; j < 4; ++j) b4[i][j] = t[4 * x + i][4 * y + j];
+          storeBlock(tiles, tri, rb[x], cb[y], b4);
+        }
     }
     __syncthreads();
   }
   if (kSmem) {
-    for (int k = threadIdx.x; k < tri_n; k += blockDim.x) packed_g[k] = A[k];
+    for (int k = threadIdx.x; k < tile_floats / 4; k += blockDim.x) {
+      reinterpret_cast<float4 *>(gtiles)[k] = reinterpret_cast<const float4 *>(tiles)[k];
+    }
   }
   if (threadIdx.x == 0) {
     st.norm2 = norm2;
@@ -286,55 +482,86 @@ struct VArgs {
   const int64_t *a_offset;
   const int64_t *log_offset;
   const int32_t *n;
-  const float2 *log;
+  const float *log;
   const JacobiState *state;
   const int32_t *work_matrix;  // per CTA: matrix id
   const int32_t *work_row;     // per CTA: first row
-  int rows_per_cta;
+  int rows_per_cta;            // multiple of 8
 };
 
-// Replays one logged sweep onto rows [r0, r0 + 32) of V (V <- V J per round,
-// column p: c v_p - s v_q, column q: s v_p + c v_q, the update of
-// jacobi_similarity_vectors_f32 z = 1, metal_mixed_sqrt.metal:1380-1390).
-__global__ void __launch_bounds__(256)
+__host__ __device__ __forceinline__ size_t replaySmemBytes(int max_n, int rows) {
+  const int m = padded8(max_n), P = m / 8;
+  return static_cast<size_t>(rows) * (m + 4) * sizeof(float) + static_cast<size_t>(P) * kQF * sizeof(float);
+}
+
+// Replays one logged sweep onto `rows` rows of V: V <- V Q_k on the column
+// blocks (I_k, J_k) of every pair, round by round (the V update of
+// jacobi_similarity_vectors_f32 z = 1, metal_mixed_sqrt.metal:1380-1390,
+// with 8x8 rotations).  A thread applies one Q_k (held in registers) to 8
+// rows.
+__global__ void __launch_bounds__(kReplayThreads)
 jacobiReplayKernel(VArgs args) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int mi = args.work_matrix[blockIdx.x];
   if (!args.state[mi].logged) return;
   const int r0 = args.work_row[blockIdx.x];
   const int n = args.n[mi];
-  const int m = n + (n & 1);
-  const int P = m / 2;
-  const int kVRows = args.rows_per_cta;
-  float *vs = reinterpret_cast<float *>(smem_raw);  // [m][kVRows]
+  const int m = padded8(n), nb = m / 4, P = nb / 2;
+  const int R = args.rows_per_cta, ld = m + 4;
+  float *vs = reinterpret_cast<float *>(smem_raw);    // [R][ld]
+  float *qs = vs + static_cast<size_t>(R) * ld;       // [P][64]
   float *v = args.v + args.a_offset[mi];
-  const int rows = min(kVRows, n - r0);
-  for (int k = threadIdx.x; k < m * kVRows; k += blockDim.x) {
-    const int c = k / kVRows, r = k % kVRows;
-    vs[k] = (c < n && r < rows) ? v[r0 + r + static_cast<int64_t>(c) * n] : 0.0f;
+  const int rows = min(R, n - r0);
+  for (int k = threadIdx.x; k < m * R; k += blockDim.x) {
+    const int c = k / R, r = k % R;
+    vs[r * ld + c] = (c < n && r < rows) ? v[r0 + r + static_cast<int64_t>(c) * n] : 0.0f;
+  }
+  const float *log = args.log + args.log_offset[mi];
+  const int groups = R / 8;
+  for (int round = 0; round < nb - 1; ++round) {
+    __syncthreads();
+    const float4 *src = reinterpret_cast<const float4 *>(log + static_cast<int64_t>(round) * P * kQF);
+    for (int k = threadIdx.x; k < P * kQF / 4; k += blockDim.x) reinterpret_cast<float4 *>(qs)[k] = src[k];
+    __syncthreads();
+    for (int item = threadIdx.x; item < P * groups; item += blockDim.x) {
+      const int k = item % P, g = item / P;
+      int I, J;
+      rrPair(k, round, nb, I, J);
+      float q[8][8];
+      const float4 *qk = reinterpret_cast<const float4 *>(qs + k * kQF);
+#pragma unroll
+      for (int i = 0; i < 8; ++i) {
+        const float4 lo = qk[2 * i], hi = qk[2 * i + 1];
+        q[i][0] = lo.x; q[i][1] = lo.y; q[i][2] = lo.z; q[i][3] = lo.w;
+        q[i][4] = hi.x; q[i][5] = hi.y; q[i][6] = hi.z; q[i][7] = hi.w;
+      }
+#pragma unroll 2
+      for (int rr = 0; rr < 8; ++rr) {
+        float *row = vs + (g * 8 + rr) * ld;
+        const float4 a = *reinterpret_cast<const float4 *>(row + 4 * I);
+        const float4 b = *reinterpret_cast<const float4 *>(row + 4 * J);
+        const float x[8] = {a.x, a.y, a.z, a.w, b.x, b.y, b.z, b.w};
+        float o[8];
+#pragma unroll
+        for (int c = 0; c < 8; ++c) {
+          float s = 0.0f;
+#pragma unroll
+          for (int j = 0; j < 8; ++j) s = fmaf(x[j], q[j][c], s);
+          o[c] = s;
+        }
+        *reinterpret_cast<float4 *>(row + 4 * I) = make_float4(o[0], o[1], o[2], o[3]);
+        *reinterpret_cast<float4 *>(row + 4 * J) = make_float4(o[4], o[5], o[6], o[7]);
+      }
+    }
   }
   __syncthreads();
-  const float2 *log = args.log + args.log_offset[mi];
-  for (int round = 0; round < m - 1; ++round) {
-    for (int k = threadIdx.x; k < P * kVRows; k += blockDim.x) {
-      const int pair = k / kVRows, r = k % kVRows;
-      int p, q;
-      rrPair(pair, round, m, p, q);
-      const float2 cs = log[static_cast<int64_t>(round) * P + pair];
-      const float vp = vs[p * kVRows + r], vq = vs[q * kVRows + r];
-      vs[p * kVRows + r] = cs.x * vp - cs.y * vq;
-      vs[q * kVRows + r] = cs.y * vp + cs.x * vq;
-    }
-    __syncthreads();
-  }
-  for (int k = threadIdx.x; k < n * kVRows; k += blockDim.x) {
-    const int c = k / kVRows, r = k % kVRows;
-    if (r < rows) v[r0 + r + static_cast<int64_t>(c) * n] = vs[k];
+  for (int k = threadIdx.x; k < n * R; k += blockDim.x) {
+    const int c = k / R, r = k % R;
+    if (r < rows) v[r0 + r + static_cast<int64_t>(c) * n] = vs[r * ld + c];
   }
 }
 
-__global__ void identityKernel(float *v, const int64_t *a_offset,
-                               const int32_t *n, int count) {
+__global__ void identityKernel(float *v, const int64_t *a_offset, const int32_t *n, int count) {
   for (int mi = blockIdx.y; mi < count; mi += gridDim.y) {
     const int64_t nn = static_cast<int64_t>(n[mi]) * n[mi];
     float *out = v + a_offset[mi];
@@ -346,44 +573,46 @@ __global__ void identityKernel(float *v, const int64_t *a_offset,
   }
 }
 
-__global__ void jacobiReportKernel(const JacobiState *state, int count,
-                                   int32_t *sweeps, float *off_ratio) {
-  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < count;
-       i += gridDim.x * blockDim.x) {
+__global__ void jacobiReportKernel(const JacobiState *state, int count, int32_t *sweeps,
+                                   float *off_ratio) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < count; i += gridDim.x * blockDim.x) {
     if (sweeps) sweeps[i] = state[i].sweeps;
     if (off_ratio) off_ratio[i] = static_cast<float>(state[i].off_ratio);
   }
 }
 
-size_t sweepSmemBytes(int n, bool smem) {
-  const int m = n + (n & 1), P = m / 2;
-  size_t bytes = 32 * sizeof(double) + (m + 1 + 2 * P) * sizeof(int) + 2 * P * sizeof(float) + 64;
-  if (smem) bytes += static_cast<size_t>(n) * (n + 1) / 2 * sizeof(float);
-  return bytes;
-}
-
 int threadsFor(int n) {
+  if (n <= 16) return 32;
   if (n <= 32) return 64;
   if (n <= 64) return 128;
-  if (n <= 128) return 256;
-  if (n <= 256) return 512;
-  return 1024;
+  return kSweepThreadsMax;
 }
 
-// Per-layout launch plan, kept with the batch layout.
+bool fitsSmem(int n) {
+  size_t q_off, tile_off;
+  return sweepSmemLayout(n, true, &q_off, &tile_off) <= kSmemLimit;
+}
+
+int replayRows(int max_n) {
+  for (int rows = 32; rows >= 8; rows -= 8)
+    if (replaySmemBytes(max_n, rows) <= kSmemLimit) return rows;
+  return 0;
+}
+
+// Per-layout launch plan, kept per batch layout and device.
 struct JacobiPlan {
   uint64_t key = 0;
   int count = 0;
-  int64_t packed_total = 0, log_total = 0;
-  int64_t *p_offset = nullptr, *log_offset = nullptr;
-  int32_t *order = nullptr;  // all ids grouped by bucket, largest first
+  int device_id = 0;
+  int64_t tile_total = 0, log_total = 0;
+  int64_t *t_offset = nullptr, *log_offset = nullptr;
+  int32_t *order = nullptr;  // ids grouped by bucket, largest first
   struct Bucket { int threads; bool smem; int first; int count; size_t smem_bytes; };
   std::vector<Bucket> buckets;
   int32_t *work_matrix = nullptr, *work_row = nullptr;
   int work_count = 0;
+  int rows_per_cta = 0;
   size_t v_smem = 0;
-  int rows_per_cta = kVRowsMax;
-  int device_id = 0;
   void *device = nullptr;
 };
 
@@ -397,41 +626,38 @@ JacobiPlan *planFor(msq_ctx *ctx, const DeviceBatch *b) {
   plan->key = b->key;
   plan->count = b->count;
   const int count = b->count;
-  std::vector<int64_t> p_off(count), l_off(count);
+  std::vector<int64_t> t_off(count), l_off(count);
   for (int i = 0; i < count; ++i) {
-    const int n = b->host_n[i], m = n + (n & 1);
-    p_off[i] = plan->packed_total;
-    plan->packed_total += static_cast<int64_t>(n) * (n + 1) / 2;
+    const int m = padded8(b->host_n[i]), nb = m / 4, P = nb / 2;
+    t_off[i] = plan->tile_total;
+    plan->tile_total += static_cast<int64_t>(nb) * (nb + 1) / 2 * kTileF;
     l_off[i] = plan->log_total;
-    plan->log_total += static_cast<int64_t>(m - 1) * (m / 2);
+    plan->log_total += static_cast<int64_t>(nb - 1) * P * kQF;
   }
   std::vector<int32_t> ids(count);
   for (int i = 0; i < count; ++i) ids[i] = i;
+  auto key = [&](int i) { return threadsFor(b->host_n[i]) * (fitsSmem(b->host_n[i]) ? 1 : 2); };
   std::stable_sort(ids.begin(), ids.end(), [&](int x, int y) {
-    const int tx = threadsFor(b->host_n[x]) * (b->host_n[x] <= kMaxSmemOrder ? 1 : 2);
-    const int ty = threadsFor(b->host_n[y]) * (b->host_n[y] <= kMaxSmemOrder ? 1 : 2);
-    if (tx != ty) return tx > ty;
+    if (key(x) != key(y)) return key(x) > key(y);
     return b->host_n[x] > b->host_n[y];
   });
   for (int i = 0; i < count;) {
     const int n0 = b->host_n[ids[i]];
     const int t = threadsFor(n0);
-    const bool smem = n0 <= kMaxSmemOrder;
+    const bool smem = fitsSmem(n0);
     int j = i;
     size_t bytes = 0;
-    while (j < count && threadsFor(b->host_n[ids[j]]) == t &&
-           (b->host_n[ids[j]] <= kMaxSmemOrder) == smem) {
-      bytes = std::max(bytes, sweepSmemBytes(b->host_n[ids[j]], smem));
+    while (j < count && threadsFor(b->host_n[ids[j]]) == t && fitsSmem(b->host_n[ids[j]]) == smem) {
+      size_t q_off, tile_off;
+      bytes = std::max(bytes, sweepSmemLayout(b->host_n[ids[j]], smem, &q_off, &tile_off));
       ++j;
     }
     plan->buckets.push_back({t, smem, i, j - i, bytes});
     i = j;
   }
+  plan->rows_per_cta = replayRows(b->max_n);
+  plan->v_smem = replaySmemBytes(b->max_n, plan->rows_per_cta);
   std::vector<int32_t> wm, wr;
-  int max_m = 0;
-  for (int i = 0; i < count; ++i) max_m = std::max(max_m, b->host_n[i] + (b->host_n[i] & 1));
-  plan->rows_per_cta = static_cast<int>(std::max<size_t>(
-      1, std::min<size_t>(kVRowsMax, kSmemLimit / (static_cast<size_t>(max_m) * sizeof(float)))));
   for (int i = 0; i < count; ++i) {
     const int n = b->host_n[ids[i]];
     for (int r = 0; r < n; r += plan->rows_per_cta) {
@@ -440,7 +666,6 @@ JacobiPlan *planFor(msq_ctx *ctx, const DeviceBatch *b) {
     }
   }
   plan->work_count = static_cast<int>(wm.size());
-  plan->v_smem = static_cast<size_t>(max_m) * plan->rows_per_cta * sizeof(float);
   const size_t bytes = 2 * count * sizeof(int64_t) + count * sizeof(int32_t) +
                        2 * wm.size() * sizeof(int32_t) + 64;
   char *dev = nullptr;
@@ -449,12 +674,12 @@ JacobiPlan *planFor(msq_ctx *ctx, const DeviceBatch *b) {
     return nullptr;
   }
   plan->device = dev;
-  plan->p_offset = reinterpret_cast<int64_t *>(dev);
-  plan->log_offset = plan->p_offset + count;
+  plan->t_offset = reinterpret_cast<int64_t *>(dev);
+  plan->log_offset = plan->t_offset + count;
   plan->order = reinterpret_cast<int32_t *>(plan->log_offset + count);
   plan->work_matrix = plan->order + count;
   plan->work_row = plan->work_matrix + wm.size();
-  cudaMemcpy(plan->p_offset, p_off.data(), count * sizeof(int64_t), cudaMemcpyHostToDevice);
+  cudaMemcpy(plan->t_offset, t_off.data(), count * sizeof(int64_t), cudaMemcpyHostToDevice);
   cudaMemcpy(plan->log_offset, l_off.data(), count * sizeof(int64_t), cudaMemcpyHostToDevice);
   cudaMemcpy(plan->order, ids.data(), count * sizeof(int32_t), cudaMemcpyHostToDevice);
   cudaMemcpy(plan->work_matrix, wm.data(), wm.size() * sizeof(int32_t), cudaMemcpyHostToDevice);
@@ -468,47 +693,51 @@ JacobiPlan *planFor(msq_ctx *ctx, const DeviceBatch *b) {
   return plan;
 }
 
+int setKernelAttributes() {
+  static bool done = false;
+  if (done) return MSQ_OK;
+  if (cudaFuncSetAttribute(jacobiSweepKernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                           static_cast<int>(kSmemLimit)) != cudaSuccess ||
+      cudaFuncSetAttribute(jacobiSweepKernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                           static_cast<int>(kSmemLimit)) != cudaSuccess ||
+      cudaFuncSetAttribute(jacobiReplayKernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                           static_cast<int>(kSmemLimit)) != cudaSuccess) {
+    return MSQ_ERR_CUDA;
+  }
+  done = true;
+  return MSQ_OK;
+}
+
 }  // namespace
 
-// Enqueues the whole solve; `work` must hold packed + log + state.
-int jacobiEnqueue(msq_ctx *ctx, const DeviceBatch *b, float *matrices,
-                  float *vectors, float *eigenvalues, double tolerance,
-                  int max_sweeps, int32_t *sweeps_done, float *off_ratio) {
-  if (b->max_n > 8192) {
-    return setError(ctx, MSQ_ERR_UNSUPPORTED, "jacobi: order above 8192");
+// Enqueues the whole solve on ctx->stream (Jacobi scratch arena).
+int jacobiEnqueue(msq_ctx *ctx, const DeviceBatch *b, float *matrices, float *vectors,
+                  float *eigenvalues, double tolerance, int max_sweeps, int32_t *sweeps_done,
+                  float *off_ratio) {
+  if (b->max_n > kMaxOrder) {
+    return setError(ctx, MSQ_ERR_UNSUPPORTED, "jacobi: order above 2048 is not supported");
   }
   JacobiPlan *plan = planFor(ctx, b);
   if (plan == nullptr) return MSQ_ERR_CUDA;
   const size_t state_bytes = (b->count * sizeof(JacobiState) + 255) & ~size_t(255);
-  const size_t packed_bytes = (plan->packed_total * sizeof(float) + 255) & ~size_t(255);
-  const size_t log_bytes = plan->log_total * sizeof(float2);
-  char *work = static_cast<char *>(scratch(ctx, state_bytes + packed_bytes + log_bytes, kScratchJacobi));
+  const size_t tile_bytes = (plan->tile_total * sizeof(float) + 255) & ~size_t(255);
+  const size_t log_bytes = plan->log_total * sizeof(float);
+  char *work = static_cast<char *>(scratch(ctx, state_bytes + tile_bytes + log_bytes, kScratchJacobi));
   if (work == nullptr) return MSQ_ERR_CUDA;
+  if (setKernelAttributes() != MSQ_OK) return cudaCheck(ctx, cudaGetLastError(), "jacobi attributes");
   JacobiArgs args{};
   args.a = matrices;
   args.state = reinterpret_cast<JacobiState *>(work);
-  args.packed = reinterpret_cast<float *>(work + state_bytes);
-  args.log = reinterpret_cast<float2 *>(work + state_bytes + packed_bytes);
+  args.tiles = reinterpret_cast<float *>(work + state_bytes);
+  args.log = reinterpret_cast<float *>(work + state_bytes + tile_bytes);
   args.a_offset = b->offset;
-  args.p_offset = plan->p_offset;
+  args.t_offset = plan->t_offset;
   args.log_offset = plan->log_offset;
   args.eig_offset = b->eig_offset;
   args.n = b->n;
   args.eigenvalues = eigenvalues;
-  args.count = b->count;
   args.tol = tolerance;
   args.max_sweeps = max_sweeps;
-
-  static bool attributes_set = false;
-  if (!attributes_set) {
-    MSQ_TRY(cudaCheck(ctx, cudaFuncSetAttribute(jacobiSweepKernel<true>,
-                                                cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                                227 * 1024), "jacobi smem attr"));
-    MSQ_TRY(cudaCheck(ctx, cudaFuncSetAttribute(jacobiReplayKernel,
-                                                cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                                227 * 1024), "replay smem attr"));
-    attributes_set = true;
-  }
   MSQ_TRY(cudaCheck(ctx, cudaMemsetAsync(args.state, 0, state_bytes, ctx->stream), "state reset"));
   {
     dim3 grid(64, std::min(b->count, 65535));
@@ -529,13 +758,13 @@ int jacobiEnqueue(msq_ctx *ctx, const DeviceBatch *b, float *matrices,
       MSQ_TRY(launched(ctx, "jacobi sweep"));
     }
     if (launch < max_sweeps) {
-      jacobiReplayKernel<<<plan->work_count, 256, plan->v_smem, ctx->stream>>>(vargs);
+      jacobiReplayKernel<<<plan->work_count, kReplayThreads, plan->v_smem, ctx->stream>>>(vargs);
       MSQ_TRY(launched(ctx, "jacobi replay"));
     }
   }
   if (sweeps_done != nullptr || off_ratio != nullptr) {
-    jacobiReportKernel<<<gridFor(b->count, 256), 256, 0, ctx->stream>>>(
-        args.state, b->count, sweeps_done, off_ratio);
+    jacobiReportKernel<<<gridFor(b->count, 256), 256, 0, ctx->stream>>>(args.state, b->count,
+                                                                       sweeps_done, off_ratio);
     MSQ_TRY(launched(ctx, "jacobi report"));
   }
   return MSQ_OK;

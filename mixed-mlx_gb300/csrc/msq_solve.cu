@@ -256,9 +256,13 @@ extern "C" int msq_solve_batched(msq_ctx *ctx, const float *a, const int32_t *n,
     MSQ_TRY(runGroup(ctx, a, n, offset, g, root, final_res, initial_res, jsweeps));
     for (int m : g.members) corrections[m] = g.plan.sweeps;
   }
-  Group retry{fp32_plan, {}};
+  // The fallback is the FP32 path with one FP32 correction sweep: FP32
+  // Jacobi + FP32 reconstruction alone leaves a residual near u * n, which
+  // misses tight tolerances at the larger orders.
+  const msq_plan fallback_plan{MSQ_PLAN_FP32, 1, 1e-7, 15, 0};
+  Group retry{fallback_plan, {}};
   for (const Group &g : groups) {
-    if (samePlan(g.plan, fp32_plan)) continue;
+    if (samePlan(g.plan, fallback_plan)) continue;
     for (int m : g.members)
       if (!(final_res[m] <= tolerance)) retry.members.push_back(m);
   }
@@ -267,7 +271,7 @@ extern "C" int msq_solve_batched(msq_ctx *ctx, const float *a, const int32_t *n,
     MSQ_TRY(runGroup(ctx, a, n, offset, retry, root, final_res, initial_res, jsweeps));
     for (int m : retry.members) {
       fallback[m] = 1;
-      corrections[m] = 0;
+      corrections[m] = fallback_plan.sweeps;
     }
   }
   if (results != nullptr) {

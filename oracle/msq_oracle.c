@@ -314,6 +314,19 @@ int msqo_jacobi(float *a, float *v, float *w, unsigned n, double tol,
           vn[row + col * n] = cc * v[row + col * n] + cs_ * v[row + cp * n];
         }
       }
+      /* The pivot element of every rotated pair is annihilated exactly (the
+       * classic Jacobi step; the CUDA kernel does the same).  The reference's
+       * 4-term update leaves its FP32 rounding residue there instead, which
+       * is harmless for its fixed 8 sweeps but would floor a convergence
+       * test on off(A). */
+      for (unsigned k = 0; k < pairs; ++k) {
+        unsigned p, q;
+        msqo_jacobi_pair(n, round, k, &p, &q);
+        if (q < n) {
+          next[p + q * n] = 0.0f;
+          next[q + p * n] = 0.0f;
+        }
+      }
       memcpy(a, next, sizeof(float) * n * n);
       memcpy(v, vn, sizeof(float) * n * n);
     }
@@ -322,6 +335,140 @@ int msqo_jacobi(float *a, float *v, float *w, unsigned n, double tol,
   for (unsigned i = 0; i < n; ++i) w[i] = a[i + i * n];
   if (off_ratio) *off_ratio = ratio;
   free(next); free(vn); free(c); free(s); free(partner);
+  return sweeps;
+}
+
+/* Blocked ordering of the same rotations, as the CUDA eigensolver applies
+ * them: indices in blocks of 4 (order padded to a multiple of 8 with zero
+ * rows), block pairs by the round-robin rule over m/4 blocks; each 8x8
+ * pivot gets one cyclic sweep of the scalar rotation above in the
+ * round-robin order of 8 indices, accumulated into Q; every off-pivot 8x8
+ * super-tile is replaced by Q_k^T T Q_l; V <- V Q.  FP32 storage and
+ * arithmetic (the pivot angles too), FP64 off-norm.  Returns sweeps. */
+static const int kInner[28][2] = {
+    {0, 7}, {1, 6}, {2, 5}, {3, 4}, {0, 6}, {5, 7}, {1, 4}, {2, 3}, {0, 5}, {4, 6},
+    {3, 7}, {1, 2}, {0, 4}, {3, 5}, {2, 6}, {1, 7}, {0, 3}, {2, 4}, {1, 5}, {6, 7},
+    {0, 2}, {1, 3}, {4, 7}, {5, 6}, {0, 1}, {2, 7}, {3, 6}, {4, 5}};
+
+static void pivot_sweep(float p[8][8], float q[8][8]) {
+  for (int r = 0; r < 8; ++r)
+    for (int c = 0; c < 8; ++c) q[r][c] = r == c ? 1.0f : 0.0f;
+  for (int k = 0; k < 28; ++k) {
+    int a = kInner[k][0], b = kInner[k][1];
+    float apq = p[a][b];
+    if (apq == 0.0f) continue;
+    float tau = (p[b][b] - p[a][a]) / (2.0f * apq);
+    float t = copysignf(1.0f / (fabsf(tau) + sqrtf(tau * tau + 1.0f)), tau);
+    float c = 1.0f / sqrtf(t * t + 1.0f), s = t * c;
+    /* exact e = c^2 + s^2 - 1 (FMA two-products), then (c, s) *= 1 - e/2 */
+    float cc = c * c, cce = fmaf(c, c, -cc), ss = s * s, sse = fmaf(s, s, -ss);
+    float e = ((cc - 1.0f) + ss) + (cce + sse);
+    float h = -0.5f * e;
+    c = fmaf(h, c, c);
+    s = fmaf(h, s, s);
+    for (int i = 0; i < 8; ++i) {
+      float pa = p[i][a], pb = p[i][b];
+      p[i][a] = c * pa - s * pb;
+      p[i][b] = s * pa + c * pb;
+    }
+    for (int j = 0; j < 8; ++j) {
+      float pa = p[a][j], pb = p[b][j];
+      p[a][j] = c * pa - s * pb;
+      p[b][j] = s * pa + c * pb;
+    }
+    p[a][b] = p[b][a] = 0.0f;
+    for (int i = 0; i < 8; ++i) {
+      float qa = q[i][a], qb = q[i][b];
+      q[i][a] = c * qa - s * qb;
+      q[i][b] = s * qa + c * qb;
+    }
+  }
+}
+
+int msqo_jacobi_blocked(const float *a_in, float *v_out, float *w, unsigned n, double tol,
+                        int max_sweeps, double *off_ratio) {
+  unsigned m = (n + 7u) & ~7u, nb = m / 4, P = nb / 2;
+  float *A = (float *)calloc((size_t)m * m, sizeof(float));
+  float *V = (float *)calloc((size_t)m * m, sizeof(float));
+  float (*Q)[8][8] = malloc(sizeof(float) * 64 * (P ? P : 1));
+  unsigned *bi = malloc(sizeof(unsigned) * (P ? P : 1)), *bj = malloc(sizeof(unsigned) * (P ? P : 1));
+  for (unsigned c = 0; c < n; ++c)
+    for (unsigned r = 0; r < n; ++r)
+      A[r + (size_t)c * m] = 0.5f * (a_in[r + (size_t)c * n] + a_in[c + (size_t)r * n]);
+  for (unsigned i = 0; i < m; ++i) V[i + (size_t)i * m] = 1.0f;
+  double norm2 = 0.0;
+  for (size_t i = 0; i < (size_t)m * m; ++i) norm2 += (double)A[i] * A[i];
+  int sweeps = 0;
+  double ratio = 0.0;
+  for (;;) {
+    double off2 = 0.0;
+    for (unsigned c = 0; c < m; ++c)
+      for (unsigned r = 0; r < m; ++r)
+        if (r != c) off2 += (double)A[r + (size_t)c * m] * A[r + (size_t)c * m];
+    ratio = norm2 > 0 ? sqrt(off2 / norm2) : 0.0;
+    if (ratio <= tol || sweeps >= max_sweeps) break;
+    for (unsigned round = 0; round + 1 < nb; ++round) {
+      for (unsigned k = 0; k < P; ++k) {
+        unsigned I, J;
+        msqo_jacobi_pair(nb, round, k, &I, &J);
+        bi[k] = I;
+        bj[k] = J;
+        float p[8][8];
+        unsigned idx[8];
+        for (int x = 0; x < 4; ++x) { idx[x] = 4 * I + x; idx[4 + x] = 4 * J + x; }
+        for (int r = 0; r < 8; ++r)
+          for (int c = 0; c < 8; ++c) p[r][c] = A[idx[r] + (size_t)idx[c] * m];
+        pivot_sweep(p, Q[k]);
+        for (int r = 0; r < 8; ++r)
+          for (int c = 0; c < 8; ++c) A[idx[r] + (size_t)idx[c] * m] = p[r][c];
+      }
+      for (unsigned k = 0; k < P; ++k)
+        for (unsigned l = 0; l < P; ++l) {
+          if (k == l) continue;
+          unsigned ri[8], ci[8];
+          for (int x = 0; x < 4; ++x) {
+            ri[x] = 4 * bi[k] + x; ri[4 + x] = 4 * bj[k] + x;
+            ci[x] = 4 * bi[l] + x; ci[4 + x] = 4 * bj[l] + x;
+          }
+          float t[8][8], u[8][8], o[8][8];
+          for (int r = 0; r < 8; ++r)
+            for (int c = 0; c < 8; ++c) t[r][c] = A[ri[r] + (size_t)ci[c] * m];
+          for (int a = 0; a < 8; ++a)
+            for (int c = 0; c < 8; ++c) {
+              float s = 0.0f;
+              for (int i = 0; i < 8; ++i) s = fmaf(Q[k][i][a], t[i][c], s);
+              u[a][c] = s;
+            }
+          for (int a = 0; a < 8; ++a)
+            for (int c = 0; c < 8; ++c) {
+              float s = 0.0f;
+              for (int j = 0; j < 8; ++j) s = fmaf(u[a][j], Q[l][j][c], s);
+              o[a][c] = s;
+            }
+          for (int r = 0; r < 8; ++r)
+            for (int c = 0; c < 8; ++c) A[ri[r] + (size_t)ci[c] * m] = o[r][c];
+        }
+      for (unsigned row = 0; row < m; ++row)
+        for (unsigned k = 0; k < P; ++k) {
+          unsigned ci[8];
+          for (int x = 0; x < 4; ++x) { ci[x] = 4 * bi[k] + x; ci[4 + x] = 4 * bj[k] + x; }
+          float x8[8], o8[8];
+          for (int j = 0; j < 8; ++j) x8[j] = V[row + (size_t)ci[j] * m];
+          for (int c = 0; c < 8; ++c) {
+            float s = 0.0f;
+            for (int j = 0; j < 8; ++j) s = fmaf(x8[j], Q[k][j][c], s);
+            o8[c] = s;
+          }
+          for (int c = 0; c < 8; ++c) V[row + (size_t)ci[c] * m] = o8[c];
+        }
+    }
+    ++sweeps;
+  }
+  for (unsigned i = 0; i < n; ++i) w[i] = A[i + (size_t)i * m];
+  for (unsigned c = 0; c < n; ++c)
+    for (unsigned r = 0; r < n; ++r) v_out[r + (size_t)c * n] = V[r + (size_t)c * m];
+  if (off_ratio) *off_ratio = ratio;
+  free(A); free(V); free(Q); free(bi); free(bj);
   return sweeps;
 }
 

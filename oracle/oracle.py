@@ -56,6 +56,8 @@ def olib() -> ctypes.CDLL:
         lib.msqo_storage_bytes.restype = ctypes.c_size_t
         lib.msqo_jacobi.argtypes = [_P, _P, _P, ctypes.c_uint, ctypes.c_double, ctypes.c_int,
                                     ctypes.POINTER(ctypes.c_double)]
+        lib.msqo_jacobi_blocked.argtypes = [_P, _P, _P, ctypes.c_uint, ctypes.c_double,
+                                            ctypes.c_int, ctypes.POINTER(ctypes.c_double)]
         lib.msqo_jacobi_pair.argtypes = [ctypes.c_uint, ctypes.c_uint, ctypes.c_uint,
                                          ctypes.POINTER(ctypes.c_uint), ctypes.POINTER(ctypes.c_uint)]
         lib.msqo_ff_residual.argtypes = [_P, _P, _P, ctypes.c_uint, _P]
@@ -113,6 +115,18 @@ def jacobi(a: np.ndarray, tol: float = 1e-7, max_sweeps: int = 15):
     ratio = ctypes.c_double()
     sweeps = olib().msqo_jacobi(A.ctypes.data, V.ctypes.data, w.ctypes.data, n, tol, max_sweeps,
                                 ctypes.byref(ratio))
+    return w, V, sweeps, ratio.value
+
+
+def jacobi_blocked(a: np.ndarray, tol: float = 1e-7, max_sweeps: int = 15):
+    """The same rotations in the blocked order the CUDA eigensolver uses."""
+    n = a.shape[0]
+    A = np.asfortranarray(a, dtype=np.float32)
+    V = np.zeros((n, n), dtype=np.float32, order="F")
+    w = np.zeros(n, dtype=np.float32)
+    ratio = ctypes.c_double()
+    sweeps = olib().msqo_jacobi_blocked(A.ctypes.data, V.ctypes.data, w.ctypes.data, n, tol,
+                                        max_sweeps, ctypes.byref(ratio))
     return w, V, sweeps, ratio.value
 
 

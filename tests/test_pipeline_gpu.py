@@ -202,7 +202,8 @@ def test_solve_batched_meets_tolerance(ctx, msq, plan, sweeps):
         assert r_oracle <= max(2 * res[i].final_residual, 1e-6), (i, r_oracle, res[i].final_residual)
         err = O.relative_error(x, O.reference_root(m))
         assert err < 1e-4
-    if plan != 0 and sweeps == 2:
+    if plan == 1 and sweeps == 2:
+        # BF16 factor: quantization error ~2^-9 contracts fast enough
         assert np.mean([r.accepted for r in res]) > 0.9
 
 
