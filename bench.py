@@ -175,6 +175,75 @@ def run_reference(args):
     print(json.dumps(line), flush=True)
 
 
+def run_codec(args):
+    """Secondary line: MXFP4 (E2M1 + E8M0 per 32) encode + decode of 2^26
+    N(0,1) FP32 values, inputs resident in HBM (256 MB > L2).  Algorithmic
+    bytes per element: encode 4 + 0.5 + 1/32, decode 0.5 + 1/32 + 4."""
+    import torch
+    msq = importlib.import_module("mixed-mlx_gb300")
+    ctx = msq.Context(0)
+    stream = torch.cuda.current_stream()
+    n = 1 << 26
+    g = torch.Generator(device="cuda").manual_seed(5)
+    x = torch.randn(n, device="cuda", generator=g)
+    vals = torch.empty(msq.storage_bytes(msq.MXFP4_E2M1, n), dtype=torch.uint8, device="cuda")
+    scales = torch.empty(msq.scale_bytes(msq.MXFP4_E2M1, n), dtype=torch.uint8, device="cuda")
+    out = torch.empty_like(x)
+    lib = msq.lib()
+
+    def step():
+        ctx.check(lib.msq_encode(ctx.handle, msq.MXFP4_E2M1, x.data_ptr(), n, 0, vals.data_ptr(),
+                                 scales.data_ptr()), "encode")
+        ctx.check(lib.msq_decode(ctx.handle, msq.MXFP4_E2M1, vals.data_ptr(), scales.data_ptr(),
+                                 n, 0, out.data_ptr()), "decode")
+
+    for _ in range(max(3, args.warmup)):
+        step()
+    torch.cuda.synchronize()
+    lib.msq_timing_begin(ctx.handle)
+    s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with ClockSampler(0) as clocks:
+        s.record(stream)
+        for _ in range(args.steps):
+            step()
+        e.record(stream)
+        torch.cuda.synchronize()
+    rows = timing_report(msq, ctx)
+    ms = s.elapsed_time(e) / args.steps
+    enc_bytes = n * (4 + 0.5 + 1 / 32)
+    dec_bytes = n * (0.5 + 1 / 32 + 4)
+    peaks = {}
+    try:
+        peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+    except OSError:
+        pass
+    hbm = peaks.get("hbm_gbs", 6800.0)
+    enc_ms = rows["msq_encode"][1] / rows["msq_encode"][0]
+    dec_ms = rows["msq_decode"][1] / rows["msq_decode"][0]
+    # bit-exact spot check against the oracle on sampled blocks (untimed)
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle as O
+    blocks = np.random.default_rng(0).integers(0, n // 32, 256)
+    sel = torch.from_numpy((blocks[:, None] * 32 + np.arange(32)).reshape(-1)).cuda()
+    ov, os_ = O.encode(msq.MXFP4_E2M1, x[sel].cpu().numpy())
+    exact = bool(np.array_equal(out[sel].cpu().numpy().view(np.uint32),
+                                O.decode(msq.MXFP4_E2M1, ov, os_, sel.numel()).view(np.uint32)))
+    line = {"metric": "MXFP4 codec round trip (encode+decode) throughput", "value": n / (ms / 1e3),
+            "unit": "elements/s", "n_gpus": 1, "steps": args.steps, "warmup": max(3, args.warmup),
+            "ms_per_step": ms, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "u8", "data": "synthetic N(0,1), seeded",
+            "config": {"workload": "MXFP4 E2M1 + E8M0/32 round trip, 2^26 FP32 elements",
+                       "l2": "inputs larger than L2 (268 MB)"},
+            "roofline": {"bound": "hbm", "achieved": enc_bytes / (enc_ms / 1e3) / 1e9, "peak": hbm,
+                         "unit": "GB/s", "frac": enc_bytes / (enc_ms / 1e3) / 1e9 / hbm,
+                         "traffic": None, "kernel": "msq_encode (encodeMxKernel<MXFP4>)",
+                         "decode_achieved": dec_bytes / (dec_ms / 1e3) / 1e9,
+                         "decode_frac": dec_bytes / (dec_ms / 1e3) / 1e9 / hbm},
+            "bit_exact_sampled_blocks": exact, "clocks": clocks.summary(),
+            "gpu_launches": sum(v[0] for v in rows.values())}
+    print(json.dumps(line), flush=True)
+
+
 def timing_report(msq, ctx) -> dict:
     import ctypes
     buf = ctypes.create_string_buffer(1 << 16)
@@ -196,9 +265,15 @@ def main():
     ap.add_argument("--sweeps", type=int, default=1)
     ap.add_argument("--jacobi-tol", type=float, default=1e-4)
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--selector", type=int, default=1,
+                    help="use the trained plan selector when its weights exist")
+    ap.add_argument("--workload", default="batched", choices=["batched", "codec"],
+                    help="codec: MXFP4 round trip of 2^26 N(0,1) values (a secondary line)")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)
+    if args.workload == "codec":
+        return run_codec(args)
 
     import torch
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -217,6 +292,24 @@ def main():
     batch, a = make_batch(msq, torch, orders, 99 + rank, device)
     torch.cuda.synchronize()
     low_plan = [msq.plan(msq.PLAN_BF16, args.sweeps, args.jacobi_tol, 15)] * batch.count
+    plan_source = f"fixed BF16 + {args.sweeps} sweep(s)"
+    weights = os.path.join(ROOT, "mixed-mlx_gb300", "selector_weights.npz")
+    if args.selector and os.path.exists(weights):
+        # learned plan selection: features + MLP forward on the GPU (outside
+        # the timed region, like the plan choice of a serving loop)
+        sel = importlib.import_module("mixed-mlx_gb300.selector")
+        w = np.load(weights)
+        selector = sel.Selector(msq, torch, ctx)
+        selector.params = torch.from_numpy(w["params"]).cuda()
+        selector.mean = torch.from_numpy(w["mean"]).cuda()
+        selector.std = torch.from_numpy(w["std"]).cuda()
+        selector.cost_order = [int(k) for k in w["cost_order"]]
+        choice = selector.choose(sel.features(ctx, torch, batch, a, TOL), float(w["threshold"][0]))
+        low_plan = [msq.plan(msq.PLAN_FP32, 1, 1e-7, 15) if k < 0 else
+                    sel.plan_structs(msq, [int(k)])[0] for k in choice]
+        plan_source = "learned selector (" + ", ".join(
+            f"{('fp32+1' if k < 0 else '%s+%d' % (('bf16', 'fp8', 'mxfp4')[sel.PLANS[k][0] - 1], sel.PLANS[k][1]))}:{int(np.sum(choice == k))}"
+            for k in sorted(set(choice.tolist()))) + ")"
     fp32_plan = [msq.plan(msq.PLAN_FP32, 0, 1e-7, 15)] * batch.count
     root = torch.empty_like(a)
 
@@ -340,8 +433,9 @@ def main():
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "bf16",
         "data": "synthetic (seeded Wishart, generated on device)",
         "config": {"workload": f"{batch.count} Wishart SPD A=X^T X/m+1e-6 I (m=2n), n log-uniform "
-                               f"[{N_LO},{N_HI}], FP32 input, BF16 plan + {args.sweeps} Sylvester "
-                               f"sweep(s), FP32 fallback, tol 1e-5",
+                               f"[{N_LO},{N_HI}], FP32 input, low-bit plan + Sylvester sweeps, "
+                               f"FP32 fallback, tol 1e-5",
+                   "plans": plan_source,
                    "matrices": batch.count, "sum_n3": float(np.sum(n64 ** 3)),
                    "l2": "inputs larger than L2 (%.0f MB)" % (batch.total * 4 / 1e6),
                    "jacobi_tolerance": args.jacobi_tol},

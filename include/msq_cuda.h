@@ -129,14 +129,16 @@ int msq_make_factor(msq_ctx *ctx, const float *vectors,
                     const float *eigenvalues, const int32_t *n,
                     const int64_t *offset, int count, float *factor_t);
 int msq_reconstruct(msq_ctx *ctx, int format, const void *values,
-                    const float *scales, const int32_t *n,
+                    const void *scales, const int32_t *n,
                     const int64_t *offset, int count, float *root);
 
 /* ---- residual and Sylvester correction (the benchmark spec (d)) --------------------
- * msq_residual: R = A - X*X with X = (x_hi + x_lo) in float-float (about 48
- * bits, the reference's WorkingFloat, metal_mixed_sqrt.metal:1268-1317);
- * writes R as FP32 (may be NULL) and per-matrix ||R||_F^2, ||A||_F^2 (FP64,
- * device, 2 per matrix).  x_lo may be NULL (treated as zero).
+ * msq_residual: R = A - X*X with A = (a + a_lo) and X = (x_hi + x_lo) in
+ * float-float (about 48 bits, the reference's WorkingFloat, which also keeps
+ * A as a (high, low) pair: metal_mixed_sqrt.metal:1268-1317,
+ * src/metal_solver.cpp:186-196); writes R as FP32 (may be NULL) and
+ * per-matrix ||R||_F^2, ||A||_F^2 (FP64, device, 2 per matrix).  a_lo and
+ * x_lo may be NULL (treated as zero).
  * msq_sylvester_sweep: one frozen-basis correction of
  * refineUpdateAndMeasure (src/metal_runtime.cpp:847-966):
  *   C = (V^T R V) o H, H_ij = 1/(s_i + s_j) recomputed from s = sqrt(lambda),
@@ -144,9 +146,10 @@ int msq_reconstruct(msq_ctx *ctx, int format, const void *values,
  * `gemm_format` selects the correction GEMMs: MSQ_FMT_FP32 (SIMT FP32) or
  * MSQ_FMT_BF16 (tcgen05 split-BF16, three products, FP32 accumulate).
  * `workspace` must hold 2 * sum(n^2) floats.                               */
-int msq_residual(msq_ctx *ctx, const float *a, const float *x_hi,
-                 const float *x_lo, const int32_t *n, const int64_t *offset,
-                 int count, float *residual, double *norms);
+int msq_residual(msq_ctx *ctx, const float *a, const float *a_lo,
+                 const float *x_hi, const float *x_lo, const int32_t *n,
+                 const int64_t *offset, int count, float *residual,
+                 double *norms);
 int msq_sylvester_sweep(msq_ctx *ctx, int gemm_format, const float *vectors,
                         const float *eigenvalues, const float *residual,
                         const int32_t *n, const int64_t *offset, int count,

@@ -78,7 +78,7 @@ _SIGS = {
     "msq_timing_end": (ctypes.c_int, [_P, ctypes.c_char_p, ctypes.c_size_t]),
     "msq_make_factor": (ctypes.c_int, [_P, _P, _P, _P, _P, ctypes.c_int, _P]),
     "msq_reconstruct": (ctypes.c_int, [_P, ctypes.c_int, _P, _P, _P, _P, ctypes.c_int, _P]),
-    "msq_residual": (ctypes.c_int, [_P, _P, _P, _P, _P, _P, ctypes.c_int, _P, _P]),
+    "msq_residual": (ctypes.c_int, [_P, _P, _P, _P, _P, _P, _P, ctypes.c_int, _P, _P]),
     "msq_sylvester_sweep": (ctypes.c_int, [_P, ctypes.c_int, _P, _P, _P, _P, _P,
                                            ctypes.c_int, _P, _P, _P]),
     "msq_solve_batched": (ctypes.c_int, [_P, _P, _P, _P, ctypes.c_int, _P,
@@ -256,7 +256,7 @@ class Context:
         torch = self.torch
         r = torch.empty_like(a) if want_r else None
         norms = torch.empty(2 * batch.count, dtype=torch.float64, device=a.device)
-        self.check(lib().msq_residual(self.handle, _ptr(a), _ptr(x_hi), _ptr(x_lo),
+        self.check(lib().msq_residual(self.handle, _ptr(a), None, _ptr(x_hi), _ptr(x_lo),
                                       batch.n.ctypes.data, batch.offset.ctypes.data,
                                       batch.count, _ptr(r), _ptr(norms)), "msq_residual")
         return r, norms

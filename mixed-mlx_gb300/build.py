@@ -70,5 +70,28 @@ def build(debug: bool = False, verbose: bool = False) -> str:
     return LIB
 
 
+def build_backend_check() -> str:
+    """Compile the C++ driver of the cuda_backend mirror (tests/cpp), linked
+    against libmsq_cuda.so; the GPU tests run it like the reference's CLI."""
+    root = os.path.dirname(HERE)
+    src = os.path.join(root, "tests", "cpp", "cuda_backend_check.cpp")
+    exe = os.path.join(root, "tests", "cpp", "cuda_backend_check")
+    lib = build()
+    if os.path.exists(exe) and os.path.getmtime(exe) >= max(os.path.getmtime(src),
+                                                           os.path.getmtime(lib)):
+        return exe
+    cuda = os.path.dirname(os.path.dirname(nvcc()))
+    cmd = ["g++", "-std=c++17", "-O2", src, "-o", exe, "-I" + CSRC, "-I" + INCLUDE,
+           "-I" + os.path.join(cuda, "include"), "-L" + HERE, "-lmsq_cuda",
+           "-L" + os.path.join(cuda, "lib64"), "-lcudart", "-Wl,-rpath," + HERE,
+           "-Wl,-rpath," + os.path.join(cuda, "lib64")]
+    res = subprocess.run(cmd, capture_output=True, text=True)
+    if res.returncode != 0:
+        raise RuntimeError(f"driver build failed:\n{res.stderr}")
+    return exe
+
+
 if __name__ == "__main__":
     build(debug="--debug" in sys.argv, verbose=True)
+    if "--driver" in sys.argv:
+        print(build_backend_check())

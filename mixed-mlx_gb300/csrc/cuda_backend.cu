@@ -1,0 +1,406 @@
+// cuda_backend: runCudaCase / runCuda over the C ABI (host code; the CUDA
+// work is enqueued through msq_* entry points).  Follows runMetalCase's
+// GPU-resident branch (src/metal_solver.cpp:477-604) and
+// solveGpuResidentSpd (src/metal_solver.cpp:92-336).
+#include "cuda_backend.hpp"
+
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <cstdio>
+#include <iomanip>
+#include <iostream>
+#include <limits>
+#include <sstream>
+#include <stdexcept>
+
+namespace mixed_sqrt {
+namespace {
+
+using Clock = std::chrono::steady_clock;
+
+[[noreturn]] void failCuda(const std::string &message) { throw std::runtime_error(message); }
+
+double since(Clock::time_point start) {
+  return std::chrono::duration<double>(Clock::now() - start).count();
+}
+
+class DeviceBuffer {
+ public:
+  explicit DeviceBuffer(size_t bytes) : bytes_(bytes) {
+    if (bytes_ != 0 && cudaMalloc(&ptr_, bytes_) != cudaSuccess) {
+      failCuda("cuda_backend: device allocation failed");
+    }
+  }
+  ~DeviceBuffer() {
+    if (ptr_ != nullptr) cudaFree(ptr_);
+  }
+  DeviceBuffer(const DeviceBuffer &) = delete;
+  DeviceBuffer &operator=(const DeviceBuffer &) = delete;
+  template <typename T>
+  T *as() const { return static_cast<T *>(ptr_); }
+
+ private:
+  void *ptr_ = nullptr;
+  size_t bytes_ = 0;
+};
+
+void copyIn(void *dst, const void *src, size_t bytes) {
+  if (cudaMemcpy(dst, src, bytes, cudaMemcpyHostToDevice) != cudaSuccess)
+    failCuda("cuda_backend: host to device copy failed");
+}
+
+void copyOut(void *dst, const void *src, size_t bytes) {
+  if (cudaMemcpy(dst, src, bytes, cudaMemcpyDeviceToHost) != cudaSuccess)
+    failCuda("cuda_backend: device to host copy failed");
+}
+
+// relativeError (src/numerics.cpp:230-240)
+double relativeErrorOf(const std::vector<double> &x, const std::vector<double> &ref) {
+  double num = 0.0, den = 0.0;
+  for (size_t i = 0; i < x.size(); ++i) {
+    const double d = x[i] - ref[i];
+    num += d * d;
+    den += ref[i] * ref[i];
+  }
+  return std::sqrt(num / den);
+}
+
+// relativeSymmetryError (src/numerics.cpp:252-264)
+double symmetryErrorOf(const std::vector<double> &x, size_t n) {
+  double num = 0.0, den = 0.0;
+  for (size_t c = 0; c < n; ++c)
+    for (size_t r = 0; r < n; ++r) {
+      const double v = x[r + c * n];
+      const double d = v - x[c + r * n];
+      num += d * d;
+      den += v * v;
+    }
+  return den > 0.0 ? std::sqrt(num / den) : 0.0;
+}
+
+int codecFor(CudaBasisFormat format) {
+  switch (format) {
+    case CudaBasisFormat::Bf16: return MSQ_FMT_BF16;
+    case CudaBasisFormat::Fp8E4M3FnRowScale: return MSQ_FMT_FP8_E4M3FN_ROWSCALE;
+    case CudaBasisFormat::Mxfp4E2M1: return MSQ_FMT_MXFP4_E2M1;
+    default: return MSQ_FMT_FP32;
+  }
+}
+
+}  // namespace
+
+const char *cudaBasisFormatName(CudaBasisFormat format) {
+  switch (format) {
+    case CudaBasisFormat::Fp32: return "fp32";
+    case CudaBasisFormat::Bf16: return "bf16";
+    case CudaBasisFormat::Fp8E4M3FnRowScale: return "fp8_e4m3fn_rowscale";
+    case CudaBasisFormat::Mxfp4E2M1: return "mxfp4_e2m1";
+  }
+  return "unknown";
+}
+
+CudaBasisFormat cudaBasisFormatForCliName(const std::string &name) {
+  for (CudaBasisFormat f : {CudaBasisFormat::Fp32, CudaBasisFormat::Bf16,
+                            CudaBasisFormat::Fp8E4M3FnRowScale, CudaBasisFormat::Mxfp4E2M1}) {
+    if (name == cudaBasisFormatName(f)) return f;
+  }
+  failCuda("Unsupported precision: " + name);
+}
+
+double cudaBasisOrthogonalityTolerance(CudaBasisFormat format) {
+  switch (format) {
+    case CudaBasisFormat::Fp32: return 1.0e-3;
+    case CudaBasisFormat::Bf16: return 5.0e-3;
+    case CudaBasisFormat::Fp8E4M3FnRowScale: return 1.5e-1;
+    case CudaBasisFormat::Mxfp4E2M1: return 5.0e-1;
+  }
+  return 0.0;
+}
+
+CudaRuntime::CudaRuntime(int device) {
+  if (msq_create(&ctx_, device) != MSQ_OK || ctx_ == nullptr) {
+    failCuda("cuda_backend: could not create the CUDA context");
+  }
+}
+
+CudaRuntime::~CudaRuntime() { msq_destroy(ctx_); }
+
+void CudaRuntime::check(int status, const char *what) const {
+  if (status != MSQ_OK) {
+    failCuda(std::string(what) + ": " + msq_last_error(ctx_));
+  }
+}
+
+CaseResult runCudaCase(CudaRuntime &runtime, const CudaSolverConfiguration &configuration,
+                       const CudaProblem &problem) {
+  if (problem.prepared_matrix == nullptr) failCuda("A prepared matrix is required.");
+  const PreparedMatrix &prepared = *problem.prepared_matrix;
+  const size_t n = problem.order;
+  if (n < 1 || n > 2048 || prepared.values.size() != n * n) {
+    failCuda("The GPU-resident matrix dimensions are invalid.");
+  }
+  if (!std::all_of(prepared.values.begin(), prepared.values.end(),
+                   [](double v) { return std::isfinite(v); })) {
+    failCuda("The prepared matrix is nonfinite.");
+  }
+  if (!std::isfinite(problem.tolerance) || !(problem.tolerance > 0.0)) {
+    failCuda("The residual tolerance must be positive and finite.");
+  }
+  msq_ctx *ctx = runtime.context();
+  const size_t elements = n * n;
+  const int32_t nn = static_cast<int32_t>(n);
+  const int64_t off = 0;
+
+  CaseResult result;
+  result.paper_test_set = prepared.paper_test_set;
+  result.matrix_family = prepared.matrix_family;
+  result.matrix_type = prepared.matrix_type;
+  result.solver_backend = "cuda";
+  result.order = n;
+  result.condition = prepared.condition;
+  result.precision = cudaBasisFormatName(configuration.basis_format);
+  result.basis_precision = result.precision;
+  result.spectrum_precision = "fp32";
+  result.correction_mode = "fp32_reorthogonalized";
+  result.kernel_path = "tiled";
+  result.precision_policy = configuration.basis_format == CudaBasisFormat::Fp32 ||
+                                    configuration.basis_format == CudaBasisFormat::Bf16
+                                ? "required_full_accuracy"
+                                : "measured_controlled";
+  result.execution_model = configuration.basis_format == CudaBasisFormat::Fp32
+                               ? "native_low_correction"
+                               : "quantized_factor_reorthogonalized_fp32_correction";
+  std::ostringstream name;
+  name << "spd_n" << n << "_cuda_" << result.precision;
+  result.name = name.str();
+  result.fp32_basis_bytes = elements * sizeof(float);
+
+  // Host -> device: the FP64 input as an FP32 high word (the eigensolver's
+  // input) plus its low word, so the residual sees the full matrix, as
+  // solveGpuResidentSpd keeps A as a WorkingFloat (src/metal_solver.cpp:186-196).
+  std::vector<float> a32(elements), a32_lo(elements);
+  for (size_t i = 0; i < elements; ++i) {
+    a32[i] = static_cast<float>(prepared.values[i]);
+    a32_lo[i] = static_cast<float>(prepared.values[i] - static_cast<double>(a32[i]));
+  }
+  DeviceBuffer a_lo(elements * sizeof(float));
+  copyIn(a_lo.as<float>(), a32_lo.data(), elements * sizeof(float));
+  DeviceBuffer a(elements * sizeof(float)), work(elements * sizeof(float)),
+      v(elements * sizeof(float)), lam(n * sizeof(float)), f(elements * sizeof(float)),
+      fq(elements * sizeof(float)), x_hi(elements * sizeof(float)), x_lo(elements * sizeof(float)),
+      r(elements * sizeof(float)), ws(2 * elements * sizeof(float)), gram(elements * sizeof(float)),
+      codes(elements * 4 + 64), scales(elements + 4 * n + 64), norms(2 * sizeof(double)),
+      ones(n * sizeof(float));
+  copyIn(a.as<float>(), a32.data(), elements * sizeof(float));
+  copyIn(work.as<float>(), a32.data(), elements * sizeof(float));
+  const std::vector<float> unit(n, 1.0f);
+  copyIn(ones.as<float>(), unit.data(), n * sizeof(float));
+
+  const auto mixed_start = Clock::now();
+  runtime.check(msq_jacobi_batched(ctx, work.as<float>(), v.as<float>(), lam.as<float>(), &nn, &off,
+                                   1, configuration.jacobi_tolerance,
+                                   configuration.jacobi_max_sweeps, nullptr, nullptr),
+                "symmetricJacobi");
+  runtime.check(msq_synchronize(ctx), "symmetricJacobi");
+  result.times.low_eigen_seconds = since(mixed_start);
+  std::vector<float> eig(n);
+  copyOut(eig.data(), lam.as<float>(), n * sizeof(float));
+  for (float value : eig) {
+    if (!(value > 0.0f) || !std::isfinite(value)) {
+      failCuda("The frozen GPU spectrum contains an invalid value.");
+    }
+  }
+
+  // Orthogonality of a basis (quantized or not): ||V V^T - I||_F / sqrt(n)
+  // from the FP32 Gram product, summed on the host as
+  // measureF32Orthogonality does (src/metal_runtime.cpp:742-776).
+  auto orthogonality = [&](const float *basis_t) {
+    runtime.check(msq_reconstruct(ctx, MSQ_FMT_FP32, basis_t, nullptr, &nn, &off, 1,
+                                  gram.as<float>()),
+                  "measureF32Orthogonality");
+    std::vector<float> g(elements);
+    copyOut(g.data(), gram.as<float>(), elements * sizeof(float));
+    double sum = 0.0;
+    for (size_t c = 0; c < n; ++c)
+      for (size_t rr = 0; rr < n; ++rr) {
+        const double d = static_cast<double>(g[rr + c * n]) - (rr == c ? 1.0 : 0.0);
+        sum += d * d;
+      }
+    return std::sqrt(sum / static_cast<double>(n));
+  };
+  // V^T in K-major order: the factor with lambda = 1.
+  runtime.check(msq_make_factor(ctx, v.as<float>(), ones.as<float>(), &nn, &off, 1, f.as<float>()),
+                "transpose basis");
+  result.frozen_basis_orthogonality = orthogonality(f.as<float>());
+
+  CudaBasisFormat format = configuration.basis_format;
+  const int codec = codecFor(format);
+  const size_t row_length = codec == MSQ_FMT_FP8_E4M3FN_ROWSCALE ? n : 0;
+  if (format != CudaBasisFormat::Fp32) {
+    const auto quantize_start = Clock::now();
+    runtime.check(msq_encode(ctx, codec, f.as<float>(), elements, row_length, codes.as<uint8_t>(),
+                             scales.as<uint8_t>()),
+                  "quantizeAndDecode");
+    runtime.check(msq_decode(ctx, codec, codes.as<uint8_t>(), scales.as<uint8_t>(), elements,
+                             row_length, fq.as<float>()),
+                  "quantizeAndDecode");
+    result.quantized_basis_orthogonality = orthogonality(fq.as<float>());
+    result.low_factor_basis_bytes =
+        msq_storage_bytes(codec, elements) + msq_scale_bytes(codec, elements, row_length ? row_length : 1);
+    const bool usable = std::isfinite(result.quantized_basis_orthogonality) &&
+                        result.quantized_basis_orthogonality <=
+                            cudaBasisOrthogonalityTolerance(format);
+    if (usable || !configuration.orthogonality_gate) {
+      result.selected_basis_stage = cudaBasisFormatName(format);
+    } else {
+      // Escalation of a rejected low-precision basis (src/metal_solver.cpp:225-235).
+      result.selected_basis_stage = std::string(cudaBasisFormatName(format)) + "_rejected_to_fp32";
+      ++result.precision_escalations;
+      format = CudaBasisFormat::Fp32;
+    }
+    (void)quantize_start;
+  } else {
+    result.selected_basis_stage = "fp32";
+  }
+  result.selected_spectrum_stage = "fp32";
+
+  // Initial root X0 = W W^T, W = V diag(lambda^(1/4)).
+  const auto initial_start = Clock::now();
+  runtime.check(msq_make_factor(ctx, v.as<float>(), lam.as<float>(), &nn, &off, 1, f.as<float>()),
+                "prepareFrozenSpectralFactor");
+  if (format == CudaBasisFormat::Fp32) {
+    runtime.check(msq_reconstruct(ctx, MSQ_FMT_FP32, f.as<float>(), nullptr, &nn, &off, 1,
+                                  x_hi.as<float>()),
+                  "reconstructTiled");
+  } else {
+    const int fcodec = codecFor(format);
+    const size_t frow = fcodec == MSQ_FMT_FP8_E4M3FN_ROWSCALE ? n : 0;
+    runtime.check(msq_encode(ctx, fcodec, f.as<float>(), elements, frow, codes.as<uint8_t>(),
+                             scales.as<uint8_t>()),
+                  "quantize factor");
+    runtime.check(msq_reconstruct(ctx, fcodec, codes.as<uint8_t>(), scales.as<float>(), &nn, &off,
+                                  1, x_hi.as<float>()),
+                  "reconstructLowFactorTiled");
+  }
+  if (cudaMemset(x_lo.as<float>(), 0, elements * sizeof(float)) != cudaSuccess)
+    failCuda("initializeWorkingRoot failed");
+  runtime.check(msq_synchronize(ctx), "initial root");
+  result.times.initial_gpu_seconds = since(initial_start);
+
+  auto residual = [&]() {
+    const auto t0 = Clock::now();
+    runtime.check(msq_residual(ctx, a.as<float>(), a_lo.as<float>(), x_hi.as<float>(),
+                               x_lo.as<float>(), &nn, &off, 1,
+                               r.as<float>(), norms.as<double>()),
+                  "computeWorkingResidual");
+    double host[2];
+    copyOut(host, norms.as<double>(), sizeof(host));
+    result.times.residual_fp64_seconds += since(t0);
+    if (!(host[1] > 0.0) || !std::isfinite(host[0]) || !std::isfinite(host[1]))
+      return std::numeric_limits<double>::infinity();
+    return std::sqrt(host[0] / host[1]);
+  };
+  auto root_now = [&]() {
+    std::vector<float> hi(elements), lo(elements);
+    copyOut(hi.data(), x_hi.as<float>(), elements * sizeof(float));
+    copyOut(lo.data(), x_lo.as<float>(), elements * sizeof(float));
+    std::vector<double> root(elements);
+    for (size_t i = 0; i < elements; ++i) root[i] = static_cast<double>(hi[i]) + lo[i];
+    return root;
+  };
+  auto forward_error = [&](const std::vector<double> &root) {
+    if (problem.supplied_reference == nullptr ||
+        problem.supplied_reference->size() != elements) {
+      return std::numeric_limits<double>::quiet_NaN();
+    }
+    return relativeErrorOf(root, *problem.supplied_reference);
+  };
+
+  double res = residual();
+  result.history.push_back({0, res, forward_error(root_now())});
+  size_t iteration = 0;
+  while (res > problem.tolerance && iteration < problem.max_iterations && std::isfinite(res)) {
+    const auto t0 = Clock::now();
+    runtime.check(msq_sylvester_sweep(ctx, MSQ_FMT_FP32, v.as<float>(), lam.as<float>(),
+                                      r.as<float>(), &nn, &off, 1, x_hi.as<float>(),
+                                      x_lo.as<float>(), ws.as<float>()),
+                  "refineUpdateAndMeasure");
+    res = residual();
+    result.times.correction_gpu_seconds += since(t0);
+    ++iteration;
+    result.history.push_back({iteration, res, forward_error(root_now())});
+  }
+  result.times.mixed_total_seconds = since(mixed_start);
+  const std::vector<double> root = root_now();
+
+  result.best_residual = result.history.front().residual;
+  result.best_forward_error = result.history.front().forward_error;
+  result.best_iteration = 0;
+  for (const auto &h : result.history) {
+    if (std::isfinite(h.residual) && h.residual < result.best_residual) {
+      result.best_residual = h.residual;
+      result.best_forward_error = h.forward_error;
+      result.best_iteration = h.iteration;
+    }
+  }
+  result.final_residual = result.history.back().residual;
+  result.final_forward_error = result.history.back().forward_error;
+  result.converged = std::isfinite(res) && res <= problem.tolerance;
+  result.finite = std::isfinite(res) &&
+                  std::all_of(root.begin(), root.end(), [](double x) { return std::isfinite(x); });
+  // termination reasons of the reference (src/metal_solver.cpp:550-564)
+  if (!result.finite) {
+    result.termination_reason = "nonfinite";
+  } else if (result.converged) {
+    result.termination_reason = "converged";
+  } else if (result.history.back().residual > result.history.front().residual) {
+    result.termination_reason = "diverged";
+  } else {
+    result.termination_reason = "budget_exhausted";
+  }
+  result.status = result.termination_reason;
+  result.symmetry_error = symmetryErrorOf(root, n);
+  if (problem.enforce_policy) {
+    // Contract enforcement (src/metal_solver.cpp:583-602).
+    if (!result.finite) failCuda("The GPU-resident solver produced a nonfinite result.");
+    if (!result.converged) {
+      std::ostringstream message;
+      message << std::setprecision(17)
+              << "The GPU-resident solver did not reach the residual tolerance. Residual: "
+              << result.final_residual;
+      failCuda(message.str());
+    }
+    if (result.symmetry_error > 1.0e-12) failCuda("The GPU-resident result lost symmetric structure.");
+  }
+  return result;
+}
+
+int runCuda(const CudaRunOptions &options, const PreparedMatrix &matrix) {
+  CudaRuntime runtime(options.device);
+  CudaSolverConfiguration configuration;
+  configuration.basis_format = options.basis_format;
+  CudaProblem problem;
+  problem.order = matrix.order;
+  problem.condition = matrix.condition;
+  problem.max_iterations = options.max_iterations;
+  problem.tolerance = options.tolerance;
+  problem.enforce_policy = false;
+  problem.prepared_matrix = &matrix;
+  const CaseResult result = runCudaCase(runtime, configuration, problem);
+  // key=value report in the style of printResult (src/reporting.cpp:22-122)
+  std::cout << std::setprecision(6) << "case=" << result.name
+            << " solver_backend=" << result.solver_backend << " n=" << result.order
+            << " basis=" << result.selected_basis_stage
+            << " status=" << result.status << " iterations=" << (result.history.size() - 1)
+            << std::scientific << " final_residual=" << result.final_residual
+            << " basis_orthogonality=" << result.frozen_basis_orthogonality
+            << " quantized_basis_orthogonality=" << result.quantized_basis_orthogonality
+            << " symmetry_error=" << result.symmetry_error
+            << " mixed_seconds=" << result.times.mixed_total_seconds << '\n';
+  return options.enforce_policy && !result.converged ? 1 : 0;
+}
+
+}  // namespace mixed_sqrt

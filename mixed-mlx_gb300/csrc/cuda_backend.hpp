@@ -1,0 +1,163 @@
+// cuda_backend — the C++ host side of the CUDA solver, mirroring the
+// reference's backend contract so it drops in beside metal_backend and
+// accelerate_backend:
+//
+//   reference                                     here
+//   MetalRuntime (src/metal_runtime.hpp:69-76)    CudaRuntime (RAII msq_ctx)
+//   MetalSolverConfiguration / MetalProblem       CudaSolverConfiguration /
+//     (src/metal_solver.hpp:12-25)                  CudaProblem
+//   runMetalCase (src/metal_solver.cpp:338-604)   runCudaCase
+//   MetalRunOptions / runMetal                    CudaRunOptions / runCuda
+//     (src/metal_backend.hpp:13-36)
+//
+// Errors follow the reference: fail() -> std::runtime_error for invalid
+// input or a failing CUDA call; numerical outcomes (not converged, rejected
+// low-precision basis, diverged) are reported in CaseResult.status and
+// termination_reason.  Built inside the reference tree (define
+// MSQ_WITH_REFERENCE_CONTRACT and put src/ on the include path) the
+// reference's own experiment.hpp types are used; standalone, the subset of
+// PreparedMatrix / CaseResult fields this backend fills is declared here
+// with the same names and meanings.
+#pragma once
+
+#include <cstddef>
+#include <cstdint>
+#include <string>
+#include <vector>
+
+#include "../../include/msq_cuda.h"
+
+#ifdef MSQ_WITH_REFERENCE_CONTRACT
+#include "experiment.hpp"
+#else
+namespace mixed_sqrt {
+
+struct PreparedMatrix {
+  std::vector<double> values;  // column-major, order x order
+  size_t order = 0;
+  double condition = 0.0;
+  std::string paper_test_set = "controlled";
+  std::string matrix_family = "conditioned_spd";
+  std::string matrix_type = "symmetric";
+  uint64_t rng_seed = 0;
+};
+
+struct IterationMeasurement {
+  size_t iteration;
+  double residual;
+  double forward_error;
+};
+
+struct PhaseTimes {
+  double reference_seconds = 0.0;
+  double low_eigen_seconds = 0.0;
+  double initial_gpu_seconds = 0.0;
+  double residual_fp64_seconds = 0.0;
+  double correction_gpu_seconds = 0.0;
+  double update_fp64_seconds = 0.0;
+  double mixed_total_seconds = 0.0;
+};
+
+struct CaseResult {
+  std::string name;
+  std::string paper_test_set = "controlled";
+  std::string matrix_family = "conditioned_spd";
+  std::string matrix_type = "symmetric";
+  std::string solver_backend = "cuda";
+  std::string precision;
+  std::string basis_precision;
+  std::string correction_mode;
+  std::string spectrum_precision;
+  std::string precision_policy;
+  std::string execution_model;
+  std::string kernel_path;
+  std::string status;
+  std::string termination_reason;
+  std::string selected_basis_stage = "not_applicable";
+  std::string selected_spectrum_stage = "not_applicable";
+  size_t precision_attempts = 1;
+  size_t order = 0;
+  size_t low_factor_basis_bytes = 0;
+  size_t fp32_basis_bytes = 0;
+  size_t best_iteration = 0;
+  size_t precision_escalations = 0;
+  double condition = 0.0;
+  bool converged = false;
+  bool finite = false;
+  double symmetry_error = 0.0;
+  double frozen_basis_orthogonality = 0.0;
+  double quantized_basis_orthogonality = 0.0;
+  double best_residual = 0.0;
+  double best_forward_error = 0.0;
+  double final_residual = 0.0;
+  double final_forward_error = 0.0;
+  std::vector<IterationMeasurement> history;
+  PhaseTimes times;
+};
+
+}  // namespace mixed_sqrt
+#endif
+
+namespace mixed_sqrt {
+
+// Basis storage of the frozen factor (the reference's Precision subset this
+// backend implements; FP8 is the per-row-scaled E4M3 format).
+enum class CudaBasisFormat { Fp32, Bf16, Fp8E4M3FnRowScale, Mxfp4E2M1 };
+
+const char *cudaBasisFormatName(CudaBasisFormat format);
+CudaBasisFormat cudaBasisFormatForCliName(const std::string &name);
+// basisOrthogonalityTolerance (src/configuration.cpp:109-118) per format.
+double cudaBasisOrthogonalityTolerance(CudaBasisFormat format);
+
+class CudaRuntime {
+ public:
+  explicit CudaRuntime(int device = 0);
+  ~CudaRuntime();
+  CudaRuntime(const CudaRuntime &) = delete;
+  CudaRuntime &operator=(const CudaRuntime &) = delete;
+  msq_ctx *context() const { return ctx_; }
+  // Throws (fail) with msq_last_error() when status != MSQ_OK.
+  void check(int status, const char *what) const;
+
+ private:
+  msq_ctx *ctx_ = nullptr;
+};
+
+struct CudaSolverConfiguration {
+  CudaBasisFormat basis_format = CudaBasisFormat::Fp32;
+  double jacobi_tolerance = 1.0e-7;  // off(A) <= tol * ||A||_F
+  int jacobi_max_sweeps = 15;
+  bool orthogonality_gate = true;    // reject a basis that fails the tolerance
+};
+
+struct CudaProblem {
+  size_t order = 0;
+  double condition = 0.0;
+  size_t max_iterations = 8;
+  double tolerance = 1.0e-12;
+  bool enforce_policy = false;
+  const PreparedMatrix *prepared_matrix = nullptr;
+  const std::vector<double> *supplied_reference = nullptr;  // FP64 root
+};
+
+// The GPU-resident solve of one matrix: Jacobi eigensolver, quantized
+// frozen factor with the orthogonality gate (escalation to FP32 on failure),
+// tensor-core reconstruction, float-float residual, frozen-basis Sylvester
+// corrections while residual > tolerance and iterations < max_iterations.
+CaseResult runCudaCase(CudaRuntime &runtime, const CudaSolverConfiguration &configuration,
+                       const CudaProblem &problem);
+
+struct CudaRunOptions {
+  CudaBasisFormat basis_format = CudaBasisFormat::Fp32;
+  size_t max_iterations = 8;
+  double tolerance = 1.0e-12;
+  bool enforce_policy = true;
+  int device = 0;
+};
+
+// runMetal's counterpart for a prepared matrix: solves, prints the result in
+// the reference's key=value style and returns 0, or 1 when enforce_policy
+// is set and the case missed its tolerance.
+int runCuda(const CudaRunOptions &options, const PreparedMatrix &matrix);
+
+}  // namespace mixed_sqrt

@@ -174,6 +174,7 @@ residualFFKernel(ResidualArgs args) {
       __syncthreads();
     }
     const float *A = args.a + off;
+    const float *AL = args.a_lo ? args.a_lo + off : nullptr;
     float *R = args.r ? args.r + off : nullptr;
     double rn = 0.0, an = 0.0;
 #pragma unroll
@@ -185,15 +186,17 @@ residualFFKernel(ResidualArgs args) {
         if (i >= n || j >= n) continue;
         const int64_t idx = i + static_cast<int64_t>(j) * n;
         const float a = A[idx];
-        // A - (s + comp) with a two-sum so the FP32 output rounds once
-        const float hi = -s[r][c], lo = -comp[r][c];
+        const float a_lo = AL ? AL[idx] : 0.0f;  // A = a + a_lo (float-float input)
+        // (a + a_lo) - (s + comp) with a two-sum so the FP32 output rounds once
+        const float hi = -s[r][c], lo = a_lo - comp[r][c];
         const float t = a + hi;
         const float z = t - a;
         const float e = (a - (t - z)) + (hi - z) + lo;
         const double rv = static_cast<double>(t) + static_cast<double>(e);
         if (R) R[idx] = t + e;
         rn += rv * rv;
-        an += static_cast<double>(a) * a;
+        const double av = static_cast<double>(a) + a_lo;
+        an += av * av;
       }
     }
 #pragma unroll
@@ -355,10 +358,11 @@ int gemmTN(msq_ctx *ctx, const DeviceBatch *b, const float *a, const float *bm, 
 }
 
 int residualFF(msq_ctx *ctx, const DeviceBatch *b, const float *a, const float *x_hi,
-               const float *x_lo, float *r, double *norms) {
+               const float *x_lo, float *r, double *norms, const float *a_lo) {
   ResidualArgs args{};
   MSQ_TRY(gemmWork(ctx, b, kTile, &args.work, &args.items));
   args.a = a;
+  args.a_lo = a_lo;
   args.x_hi = x_hi;
   args.x_lo = x_lo;
   args.r = r;

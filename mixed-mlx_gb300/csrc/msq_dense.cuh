@@ -26,7 +26,7 @@ struct GemmArgs {
 struct ResidualArgs {
   const int4 *work;
   int items;
-  const float *a, *x_hi, *x_lo;
+  const float *a, *a_lo, *x_hi, *x_lo;
   float *r;
   double *norms;
   const int64_t *offset;
@@ -40,8 +40,9 @@ int gemmWork(msq_ctx *ctx, const DeviceBatch *b, int tile, const int4 **work, in
 int gemmTN(msq_ctx *ctx, const DeviceBatch *b, const float *a, const float *bm, float *c,
            int epilogue, const float *eigenvalues, bool a_mmajor = false,
            bool b_nmajor = false);
+// R = (a + a_lo) - (x_hi + x_lo)^2 in float-float; a_lo and x_lo may be null.
 int residualFF(msq_ctx *ctx, const DeviceBatch *b, const float *a, const float *x_hi,
-               const float *x_lo, float *r, double *norms);
+               const float *x_lo, float *r, double *norms, const float *a_lo = nullptr);
 int makeFactor(msq_ctx *ctx, const DeviceBatch *b, const float *v, const float *lam, float *f);
 int transpose(msq_ctx *ctx, const DeviceBatch *b, const float *src, float *dst);
 int symmetricAdd(msq_ctx *ctx, const DeviceBatch *b, float *x_hi, float *x_lo, const float *e);

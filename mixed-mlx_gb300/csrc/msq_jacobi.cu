@@ -124,25 +124,33 @@ __device__ double blockReduceSum(double v, double *red) {
   return total;
 }
 
-// Packed tile (I, J), I <= J, of a matrix's tile array.
-__device__ __forceinline__ float *tileAt(float *tiles, const int *tri, int I, int J) {
-  return tiles + static_cast<int64_t>(tri[J] + I) * kTileF;
+// Packed tile (I, J), I <= J, of a matrix's tile array: tile index
+// tri[J] + I, 16 floats.  A 4x4 tile spans half the 32 shared-memory banks,
+// so without care the rows of all tiles would fall on two bank groups; row
+// i of tile t is stored at physical row i ^ (t & 3), which spreads the
+// float4 rows a warp touches over all eight 4-bank groups.
+__device__ __forceinline__ int tileIndex(const int *tri, int I, int J) { return tri[J] + I; }
+
+__device__ __forceinline__ int64_t tileElement(int t, int i, int j) {
+  return static_cast<int64_t>(t) * kTileF + (((i ^ (t & 3)) << 2) | j);
 }
 
 // Loads block (R, C) of A (4x4, row-major in t) from the packed tiles.
 __device__ __forceinline__ void loadBlock(float *tiles, const int *tri, int R, int C, float (&t)[4][4]) {
   if (R <= C) {
-    const float4 *src = reinterpret_cast<const float4 *>(tileAt(tiles, tri, R, C));
+    const int ti = tileIndex(tri, R, C);
+    const float4 *src = reinterpret_cast<const float4 *>(tiles + static_cast<int64_t>(ti) * kTileF);
 #pragma unroll
     for (int i = 0; i < 4; ++i) {
-      const float4 v = src[i];
+      const float4 v = src[i ^ (ti & 3)];
       t[i][0] = v.x; t[i][1] = v.y; t[i][2] = v.z; t[i][3] = v.w;
     }
   } else {
-    const float4 *src = reinterpret_cast<const float4 *>(tileAt(tiles, tri, C, R));
+    const int ti = tileIndex(tri, C, R);
+    const float4 *src = reinterpret_cast<const float4 *>(tiles + static_cast<int64_t>(ti) * kTileF);
 #pragma unroll
     for (int i = 0; i < 4; ++i) {
-      const float4 v = src[i];
+      const float4 v = src[i ^ (ti & 3)];
       t[0][i] = v.x; t[1][i] = v.y; t[2][i] = v.z; t[3][i] = v.w;
     }
   }
@@ -150,13 +158,15 @@ __device__ __forceinline__ void loadBlock(float *tiles, const int *tri, int R, i
 
 __device__ __forceinline__ void storeBlock(float *tiles, const int *tri, int R, int C, const float (&t)[4][4]) {
   if (R <= C) {
-    float4 *dst = reinterpret_cast<float4 *>(tileAt(tiles, tri, R, C));
+    const int ti = tileIndex(tri, R, C);
+    float4 *dst = reinterpret_cast<float4 *>(tiles + static_cast<int64_t>(ti) * kTileF);
 #pragma unroll
-    for (int i = 0; i < 4; ++i) dst[i] = make_float4(t[i][0], t[i][1], t[i][2], t[i][3]);
+    for (int i = 0; i < 4; ++i) dst[i ^ (ti & 3)] = make_float4(t[i][0], t[i][1], t[i][2], t[i][3]);
   } else {
-    float4 *dst = reinterpret_cast<float4 *>(tileAt(tiles, tri, C, R));
+    const int ti = tileIndex(tri, C, R);
+    float4 *dst = reinterpret_cast<float4 *>(tiles + static_cast<int64_t>(ti) * kTileF);
 #pragma unroll
-    for (int i = 0; i < 4; ++i) dst[i] = make_float4(t[0][i], t[1][i], t[2][i], t[3][i]);
+    for (int i = 0; i < 4; ++i) dst[i ^ (ti & 3)] = make_float4(t[0][i], t[1][i], t[2][i], t[3][i]);
   }
 }
 
@@ -282,7 +292,7 @@ jacobiSweepKernel(JacobiArgs args) {
         if (gi < n && gj < n) {
           v = 0.5f * (full[gi + static_cast<int64_t>(gj) * n] + full[gj + static_cast<int64_t>(gi) * n]);
         }
-        tiles[static_cast<int64_t>(tri[J] + I) * kTileF + e] = v;
+        tiles[tileElement(tri[J] + I, e / 4, e % 4)] = v;
       }
     }
   } else if (kSmem) {
@@ -297,7 +307,7 @@ jacobiSweepKernel(JacobiArgs args) {
   for (int J = 0; J < nb; ++J) {
     for (int idx = threadIdx.x; idx < (J + 1) * kTileF; idx += blockDim.x) {
       const int I = idx / kTileF, e = idx % kTileF;
-      const double v = tiles[static_cast<int64_t>(tri[J] + I) * kTileF + e];
+      const double v = tiles[tileElement(tri[J] + I, e / 4, e % 4)];
       if (I < J) off2 += 2.0 * v * v;
       else if (e / 4 == e % 4) diag2 += v * v;
       else off2 += v * v;
@@ -314,14 +324,14 @@ jacobiSweepKernel(JacobiArgs args) {
     // later, :1436-1444); full symmetric write-back of the matrix.
     float *eig = args.eigenvalues + args.eig_offset[mi];
     for (int k = threadIdx.x; k < n; k += blockDim.x) {
-      eig[k] = tiles[static_cast<int64_t>(tri[k / 4] + k / 4) * kTileF + (k % 4) * 5];
+      eig[k] = tiles[tileElement(tri[k / 4] + k / 4, k % 4, k % 4)];
     }
     float *out = args.a + args.a_offset[mi];
     for (int c = 0; c < n; ++c) {
       for (int r = threadIdx.x; r < n; r += blockDim.x) {
         const int I = r / 4, J = c / 4;
-        const float v = I <= J ? tiles[static_cast<int64_t>(tri[J] + I) * kTileF + (r % 4) * 4 + c % 4]
-                               : tiles[static_cast<int64_t>(tri[I] + J) * kTileF + (c % 4) * 4 + r % 4];
+        const float v = I <= J ? tiles[tileElement(tri[J] + I, r % 4, c % 4)]
+                               : tiles[tileElement(tri[I] + J, c % 4, r % 4)];
         out[r + static_cast<int64_t>(c) * n] = v;
       }
     }

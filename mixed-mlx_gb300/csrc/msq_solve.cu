@@ -39,8 +39,10 @@ int sylvesterFp32(msq_ctx *ctx, const DeviceBatch *b, const float *v, const floa
 int sylvesterSweep(msq_ctx *ctx, const DeviceBatch *b, int gemm_format, const float *v,
                    const float *lam, const float *r, float *x_hi, float *x_lo, float *ws0,
                    float *ws1) {
-  if (gemm_format != MSQ_FMT_FP32) {
-    return setError(ctx, MSQ_ERR_UNSUPPORTED, "Sylvester sweep: only FP32 correction GEMMs");
+  if (gemm_format == MSQ_FMT_BF16) {
+    float *e = nullptr;
+    MSQ_TRY(sylvesterTc(ctx, b, v, lam, r, ws0, ws1, &e));
+    return symmetricAdd(ctx, b, x_hi, x_lo, e);
   }
   return sylvesterFp32(ctx, b, v, lam, r, x_hi, x_lo, ws0, ws1);
 }
@@ -77,7 +79,7 @@ extern "C" int msq_make_factor(msq_ctx *ctx, const float *vectors, const float *
   return makeFactor(ctx, b, vectors, eigenvalues, factor_t);
 }
 
-extern "C" int msq_reconstruct(msq_ctx *ctx, int format, const void *values, const float *scales,
+extern "C" int msq_reconstruct(msq_ctx *ctx, int format, const void *values, const void *scales,
                                const int32_t *n, const int64_t *offset, int count, float *root) {
   if (ctx == nullptr) return MSQ_ERR_INVALID_ARGUMENT;
   if (!values || !root) return setError(ctx, MSQ_ERR_INVALID_ARGUMENT, "msq_reconstruct: null buffer");
@@ -90,14 +92,14 @@ extern "C" int msq_reconstruct(msq_ctx *ctx, int format, const void *values, con
   return reconstructEncoded(ctx, b, format, values, scales, root);
 }
 
-extern "C" int msq_residual(msq_ctx *ctx, const float *a, const float *x_hi, const float *x_lo,
-                            const int32_t *n, const int64_t *offset, int count, float *residual,
-                            double *norms) {
+extern "C" int msq_residual(msq_ctx *ctx, const float *a, const float *a_lo, const float *x_hi,
+                            const float *x_lo, const int32_t *n, const int64_t *offset, int count,
+                            float *residual, double *norms) {
   if (ctx == nullptr) return MSQ_ERR_INVALID_ARGUMENT;
   if (!a || !x_hi || !norms) return setError(ctx, MSQ_ERR_INVALID_ARGUMENT, "msq_residual: null buffer");
   const DeviceBatch *b = prepareBatch(ctx, n, offset, count);
   if (b == nullptr) return MSQ_ERR_INVALID_ARGUMENT;
-  return residualFF(ctx, b, a, x_hi, x_lo, residual, norms);
+  return residualFF(ctx, b, a, x_hi, x_lo, residual, norms, a_lo);
 }
 
 extern "C" int msq_sylvester_sweep(msq_ctx *ctx, int gemm_format, const float *vectors,
@@ -188,18 +190,28 @@ int runGroup(msq_ctx *ctx, const float *a_user, const int32_t *n_user,
   MSQ_TRY(reconstructFromFactor(ctx, b, g.plan.format, F, Xh));
   MSQ_TRY(cudaCheck(ctx, cudaMemsetAsync(Xl, 0, total * sizeof(float), ctx->stream), "x_lo reset"));
   std::vector<double> host_norms(2 * count);
-  MSQ_TRY(residualFF(ctx, b, A, Xh, Xl, R, norms));
+  // Corrections use the FP32 stable basis V, as the reference's fp32_frozen
+  // stage does (src/metal_solver.cpp:304-325).  The plain FP32 plan runs its
+  // GEMMs and residuals on the CUDA cores in FP32 / float-float; low-bit
+  // plans run the correction GEMMs and the residuals between sweeps on the
+  // tensor cores (split BF16, FP32 accumulation).  The residual that decides
+  // acceptance is always the float-float one.
+  const bool low_bit = g.plan.format != MSQ_PLAN_FP32;
+  const int gemm_format = low_bit ? MSQ_FMT_BF16 : MSQ_FMT_FP32;
+  auto residual = [&](bool accepting) {
+    return low_bit && !accepting ? residualTc(ctx, b, A, Xh, Xl, R, norms)
+                                 : residualFF(ctx, b, A, Xh, Xl, R, norms);
+  };
+  MSQ_TRY(residual(g.plan.sweeps == 0));
   MSQ_TRY(cudaCheck(ctx, cudaMemcpyAsync(host_norms.data(), norms, 2 * count * sizeof(double),
                                          cudaMemcpyDeviceToHost, ctx->stream), "norms read"));
   MSQ_TRY(cudaCheck(ctx, cudaStreamSynchronize(ctx->stream), "norms sync"));
   for (int i = 0; i < count; ++i)
-    initial_res[g.members[i]] = std::sqrt(host_norms[2 * i] / host_norms[2 * i + 1]);
-  // Corrections use the FP32 stable basis and FP32 GEMMs (the reference's
-  // fp32_frozen correction stage, src/metal_solver.cpp:311-325).
-  const int gemm_format = MSQ_FMT_FP32;
+    if (std::isnan(initial_res[g.members[i]]))  // keep the plan's, not the fallback's
+      initial_res[g.members[i]] = std::sqrt(host_norms[2 * i] / host_norms[2 * i + 1]);
   for (int s = 0; s < g.plan.sweeps; ++s) {
     MSQ_TRY(sylvesterSweep(ctx, b, gemm_format, V, lam, R, Xh, Xl, F, W1));
-    MSQ_TRY(residualFF(ctx, b, A, Xh, Xl, R, norms));
+    MSQ_TRY(residual(s + 1 == g.plan.sweeps));
   }
   if (g.plan.sweeps > 0) {
     MSQ_TRY(cudaCheck(ctx, cudaMemcpyAsync(host_norms.data(), norms, 2 * count * sizeof(double),
@@ -208,11 +220,19 @@ int runGroup(msq_ctx *ctx, const float *a_user, const int32_t *n_user,
   std::vector<int32_t> host_sweeps(count);
   MSQ_TRY(cudaCheck(ctx, cudaMemcpyAsync(host_sweeps.data(), sweeps, count * sizeof(int32_t),
                                          cudaMemcpyDeviceToHost, ctx->stream), "sweeps read"));
-  // Scatter X (hi word; the lo word is below FP32 resolution of the output).
-  for (int i = 0; i < count; ++i) {
-    MSQ_TRY(cudaCheck(ctx, cudaMemcpyAsync(root + off_user[g.members[i]], Xh + off[i],
-                                           static_cast<int64_t>(n[i]) * n[i] * sizeof(float),
+  // Scatter X (hi word; the lo word is below FP32 resolution of the output),
+  // one copy per run of members whose caller offsets are contiguous.
+  for (int i = 0; i < count;) {
+    int j = i + 1;
+    while (j < count && g.members[j] == g.members[j - 1] + 1 &&
+           off_user[g.members[j]] == off_user[g.members[j - 1]] +
+                                         ((static_cast<int64_t>(n[j - 1]) * n[j - 1] + 3) & ~int64_t(3)))
+      ++j;
+    const int64_t last = j - 1;
+    const int64_t bytes = (off[last] - off[i] + static_cast<int64_t>(n[last]) * n[last]) * sizeof(float);
+    MSQ_TRY(cudaCheck(ctx, cudaMemcpyAsync(root + off_user[g.members[i]], Xh + off[i], bytes,
                                            cudaMemcpyDeviceToDevice, ctx->stream), "scatter X"));
+    i = j;
   }
   MSQ_TRY(cudaCheck(ctx, cudaStreamSynchronize(ctx->stream), "group sync"));
   MSQ_TRY(checkDeviceStatus(ctx));

@@ -15,7 +15,14 @@ int jacobiEnqueue(msq_ctx *ctx, const DeviceBatch *b, float *matrices, float *ve
 int reconstructLowBit(msq_ctx *ctx, const DeviceBatch *b, int format, const float *f,
                       float *x);
 int reconstructEncoded(msq_ctx *ctx, const DeviceBatch *b, int format, const void *values,
-                       const float *scales, float *x);
+                       const void *scales, float *x);
+
+// msq_tc.cu — tensor-core Sylvester GEMM chain (the correction is returned in
+// *correction, one of ws0/ws1) and the split-BF16 residual.
+int sylvesterTc(msq_ctx *ctx, const DeviceBatch *b, const float *v, const float *lam,
+                const float *r, float *ws0, float *ws1, float **correction);
+int residualTc(msq_ctx *ctx, const DeviceBatch *b, const float *a, const float *x_hi,
+               const float *x_lo, float *r, double *norms);
 
 // msq_solve.cu
 int sylvesterSweep(msq_ctx *ctx, const DeviceBatch *b, int gemm_format, const float *v,

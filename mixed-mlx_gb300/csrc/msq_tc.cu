@@ -38,6 +38,13 @@ constexpr uint32_t kTmemCols = 256;
 constexpr long long kWaitLimit = 1ll << 26;
 
 enum OperandKind : int { kOpBf16 = 0, kOpFp8 = 1 };
+constexpr int kMaxSegments = 6;
+enum Epilogue : int {
+  kEpiStore = 0,     // X = acc
+  kEpiRowScale = 1,  // X_ij = acc * r_i * r_j (FP8 row-scaled factor)
+  kEpiInverseH = 2,  // X_ij = acc / (s_i + s_j), s = sqrt(lambda)
+  kEpiResidual = 3,  // X = A - acc, FP64 ||X||^2 and ||A||^2 per matrix
+};
 
 __device__ __forceinline__ uint32_t smemAddr(const void *p) {
   return static_cast<uint32_t>(__cvta_generic_to_shared(p));
@@ -149,17 +156,24 @@ __device__ __forceinline__ void tmemLoad32(uint32_t taddr, float *v) {
 struct TcArgs {
   const int4 *work;        // (matrix, tile_m, tile_n, k_tiles)
   int items;
-  const uint8_t *tiles;    // packed operand
+  // The accumulator sums A_s B_s^T over `segments` operand pairs (split-BF16
+  // products); every packed operand shares the plan's tile geometry.
+  int segments;
+  const uint8_t *tiles_a[kMaxSegments];
+  const uint8_t *tiles_b[kMaxSegments];
   const int64_t *tile_base;// per matrix: first tile index
   const int32_t *n;
   const int64_t *x_offset;
   const int64_t *eig_offset;
-  const float *row_scale;  // FP8 only: per matrix row scales at eig_offset
+  const float *row_scale;  // kEpiRowScale: per matrix row scales at eig_offset
+  const float *eigenvalues;// kEpiInverseH: lambda, s = sqrt(max(lambda, 0))
+  const float *a_in;       // kEpiResidual: R = A - acc
+  double *norms;           // kEpiResidual: ||R||^2, ||A||^2 per matrix
   float *x;
   int *status;
 };
 
-template <int kKind>
+template <int kKind, int kEpi>
 __global__ void __launch_bounds__(kTcThreads, 1) tcGemmKernel(TcArgs args) {
   extern __shared__ __align__(1024) unsigned char smem_raw[];
   unsigned char *base = reinterpret_cast<unsigned char *>(
@@ -201,19 +215,23 @@ __global__ void __launch_bounds__(kTcThreads, 1) tcGemmKernel(TcArgs args) {
       uint32_t phase = 0;
       for (int item = blockIdx.x; item < args.items && !*abort_flag; item += gridDim.x) {
         const int4 w = args.work[item];
-        const uint8_t *tiles = args.tiles + args.tile_base[w.x] * kTileBytes;
-        for (int kt = 0; kt < w.w; ++kt) {
-          if (!mbarWait(smemAddr(&empty[stage]), phase ^ 1, args.status, abort_flag)) break;
-          const uint32_t bar = smemAddr(&full[stage]);
-          mbarArriveExpectTx(bar, 2 * kTileBytes);
-          unsigned char *dst = stage_mem + stage * 2 * kTileBytes;
-          bulkLoad(smemAddr(dst), tiles + (static_cast<int64_t>(w.y) * w.w + kt) * kTileBytes,
-                   kTileBytes, bar);
-          bulkLoad(smemAddr(dst + kTileBytes),
-                   tiles + (static_cast<int64_t>(w.z) * w.w + kt) * kTileBytes, kTileBytes, bar);
-          if (++stage == kStages) {
-            stage = 0;
-            phase ^= 1;
+        const int64_t base = args.tile_base[w.x] * kTileBytes;
+        for (int seg = 0; seg < args.segments; ++seg) {
+          const uint8_t *ta = args.tiles_a[seg] + base;
+          const uint8_t *tb = args.tiles_b[seg] + base;
+          for (int kt = 0; kt < w.w; ++kt) {
+            if (!mbarWait(smemAddr(&empty[stage]), phase ^ 1, args.status, abort_flag)) break;
+            const uint32_t bar = smemAddr(&full[stage]);
+            mbarArriveExpectTx(bar, 2 * kTileBytes);
+            unsigned char *dst = stage_mem + stage * 2 * kTileBytes;
+            bulkLoad(smemAddr(dst), ta + (static_cast<int64_t>(w.y) * w.w + kt) * kTileBytes,
+                     kTileBytes, bar);
+            bulkLoad(smemAddr(dst + kTileBytes),
+                     tb + (static_cast<int64_t>(w.z) * w.w + kt) * kTileBytes, kTileBytes, bar);
+            if (++stage == kStages) {
+              stage = 0;
+              phase ^= 1;
+            }
           }
         }
       }
@@ -229,7 +247,8 @@ __global__ void __launch_bounds__(kTcThreads, 1) tcGemmKernel(TcArgs args) {
         if (!mbarWait(smemAddr(&acc_empty[acc]), acc_phase ^ 1, args.status, abort_flag)) break;
         asm volatile("tcgen05.fence::after_thread_sync;");
         const uint32_t d = tmem + acc * 128;
-        for (int kt = 0; kt < w.w; ++kt) {
+        const int steps = args.segments * w.w;
+        for (int step = 0; step < steps; ++step) {
           if (!mbarWait(smemAddr(&full[stage]), phase, args.status, abort_flag)) break;
           asm volatile("tcgen05.fence::after_thread_sync;");
           const uint32_t a_addr = smemAddr(stage_mem + stage * 2 * kTileBytes);
@@ -239,7 +258,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) tcGemmKernel(TcArgs args) {
           // 32 FP8); the start address advances inside the swizzle atom.
 #pragma unroll
           for (int kk = 0; kk < 4; ++kk) {
-            mmaIssue<kKind>(d, adesc + 2 * kk, bdesc + 2 * kk, (kt | kk) != 0);
+            mmaIssue<kKind>(d, adesc + 2 * kk, bdesc + 2 * kk, (step | kk) != 0);
           }
           mmaCommit(smemAddr(&empty[stage]));
           if (++stage == kStages) {
@@ -269,10 +288,14 @@ __global__ void __launch_bounds__(kTcThreads, 1) tcGemmKernel(TcArgs args) {
       float *X = args.x + args.x_offset[mi];
       float ri = 1.0f;
       const float *rs = nullptr;
-      if (kKind == kOpFp8) {
+      if (kEpi == kEpiRowScale) {
         rs = args.row_scale + args.eig_offset[mi];
         ri = i < n ? rs[i] : 0.0f;
       }
+      const float *lam = kEpi == kEpiInverseH ? args.eigenvalues + args.eig_offset[mi] : nullptr;
+      const float si = kEpi == kEpiInverseH && i < n ? sqrtf(fmaxf(lam[i], 0.0f)) : 0.0f;
+      const float *A = kEpi == kEpiResidual ? args.a_in + args.x_offset[mi] : nullptr;
+      double rn = 0.0, an = 0.0;
 #pragma unroll 1
       for (int c = 0; c < 4; ++c) {
         float v[32];
@@ -282,11 +305,31 @@ __global__ void __launch_bounds__(kTcThreads, 1) tcGemmKernel(TcArgs args) {
           for (int q = 0; q < 32; ++q) {
             const int j = j0 + c * 32 + q;
             if (j < n) {
+              const int64_t at = i + static_cast<int64_t>(j) * n;
               float val = v[q];
-              if (kKind == kOpFp8) val = val * ri * rs[j];
-              X[i + static_cast<int64_t>(j) * n] = val;
+              if (kEpi == kEpiRowScale) val = val * ri * rs[j];
+              if (kEpi == kEpiInverseH) val = val / (si + sqrtf(fmaxf(lam[j], 0.0f)));
+              if (kEpi == kEpiResidual) {
+                const float a = A[at];
+                val = a - val;
+                rn += static_cast<double>(val) * val;
+                an += static_cast<double>(a) * a;
+              }
+              X[at] = val;
             }
           }
+        }
+      }
+      if (kEpi == kEpiResidual) {
+        // epilogue warps 0-3 reduce, then one atomic per warp
+#pragma unroll
+        for (int s = 16; s > 0; s >>= 1) {
+          rn += __shfl_xor_sync(0xffffffffu, rn, s);
+          an += __shfl_xor_sync(0xffffffffu, an, s);
+        }
+        if (lane == 0) {
+          atomicAdd(&args.norms[2 * mi], rn);
+          atomicAdd(&args.norms[2 * mi + 1], an);
         }
       }
       asm volatile("tcgen05.fence::before_thread_sync;");
@@ -411,6 +454,63 @@ __global__ void __launch_bounds__(128) packKernel(PackArgs args) {
   }
 }
 
+// Split-BF16 packing of an FP32 (or float-float hi + lo) matrix M, n x n
+// column-major, as the K-major MMA operand: operand row i is column i of M
+// (kTranspose false) or row i of M (kTranspose true).  Piece p is the BF16
+// rounding of what pieces 0..p-1 left over, so three pieces carry the FP32
+// mantissa and the products p_a p_b (exact in FP32) sum to M_a M_b.
+struct SplitArgs {
+  const int4 *work;
+  int items;
+  const float *hi;
+  const float *lo;  // may be null
+  const int64_t *offset;
+  const int64_t *tile_base;
+  const int32_t *n;
+  int pieces;
+  uint8_t *out[3];
+};
+
+template <bool kTranspose>
+__global__ void __launch_bounds__(128) packSplitKernel(SplitArgs args) {
+  for (int item = blockIdx.x; item < args.items; item += gridDim.x) {
+    const int4 w = args.work[item];
+    const int mi = w.x, n = args.n[mi];
+    const int r = threadIdx.x;
+    const int i = w.y * kTileRows + r;
+    const int k0 = w.z * 64;
+    const float *H = args.hi + args.offset[mi];
+    const float *L = args.lo ? args.lo + args.offset[mi] : nullptr;
+    const int64_t tile = (args.tile_base[mi] + static_cast<int64_t>(w.y) * w.w + w.z) * kTileBytes;
+#pragma unroll 1
+    for (int c = 0; c < 8; ++c) {
+      uint32_t word[3][4] = {};
+#pragma unroll
+      for (int e = 0; e < 8; ++e) {
+        const int k = k0 + c * 8 + e;
+        float x = 0.0f, xl = 0.0f;
+        if (i < n && k < n) {
+          const int64_t at = kTranspose ? i + static_cast<int64_t>(k) * n
+                                        : k + static_cast<int64_t>(i) * n;
+          x = H[at];
+          xl = L ? L[at] : 0.0f;
+        }
+        const uint32_t h0 = encodeBf16(x);
+        const float rem = (x - decodeBf16(static_cast<uint16_t>(h0))) + xl;
+        const uint32_t h1 = encodeBf16(rem);
+        const uint32_t h2 = encodeBf16(rem - decodeBf16(static_cast<uint16_t>(h1)));
+        word[0][e / 2] |= h0 << (16 * (e % 2));
+        word[1][e / 2] |= h1 << (16 * (e % 2));
+        word[2][e / 2] |= h2 << (16 * (e % 2));
+      }
+      for (int p = 0; p < args.pieces; ++p) {
+        *reinterpret_cast<uint4 *>(args.out[p] + tile + swizzle128(r, c)) =
+            make_uint4(word[p][0], word[p][1], word[p][2], word[p][3]);
+      }
+    }
+  }
+}
+
 // Row scales of the FP8 factor: r_i = max_k |W_ik| / 448 (1 for a zero
 // row), the MSQ_FMT_FP8_E4M3FN_ROWSCALE definition with rows of W^T's
 // K-major storage.  One warp per row.
@@ -515,36 +615,68 @@ TcPlan *tcPlan(msq_ctx *ctx, const DeviceBatch *b, int kind) {
 
 size_t tcSmemBytes() { return kStages * 2 * kTileBytes + 1024 + 256; }
 
-int runTcGemm(msq_ctx *ctx, const DeviceBatch *b, TcPlan *p, const uint8_t *tiles,
-              const float *row_scale, float *x) {
+int tcAttributes(msq_ctx *ctx) {
+  static bool attr = false;
+  if (attr) return MSQ_OK;
+  const int bytes = static_cast<int>(tcSmemBytes());
+  const cudaFuncAttribute a = cudaFuncAttributeMaxDynamicSharedMemorySize;
+  MSQ_TRY(cudaCheck(ctx, cudaFuncSetAttribute(tcGemmKernel<kOpBf16, kEpiStore>, a, bytes), "tc attr"));
+  MSQ_TRY(cudaCheck(ctx, cudaFuncSetAttribute(tcGemmKernel<kOpFp8, kEpiRowScale>, a, bytes), "tc attr"));
+  MSQ_TRY(cudaCheck(ctx, cudaFuncSetAttribute(tcGemmKernel<kOpBf16, kEpiInverseH>, a, bytes), "tc attr"));
+  MSQ_TRY(cudaCheck(ctx, cudaFuncSetAttribute(tcGemmKernel<kOpBf16, kEpiResidual>, a, bytes), "tc attr"));
+  attr = true;
+  return MSQ_OK;
+}
+
+// Launches the persistent tcgen05 GEMM over the plan's work list:
+// X = sum_s A_s B_s^T per matrix with the given epilogue.
+int launchTcGemm(msq_ctx *ctx, const DeviceBatch *b, TcPlan *p, int epilogue, int segments,
+                 const uint8_t *const *a_tiles, const uint8_t *const *b_tiles,
+                 const float *row_scale, const float *eigenvalues, const float *a_in,
+                 double *norms, float *x, const char *what) {
+  MSQ_TRY(tcAttributes(ctx));
   TcArgs args{};
   args.work = p->gemm_work;
   args.items = p->gemm_items;
-  args.tiles = tiles;
+  args.segments = segments;
+  for (int s = 0; s < segments; ++s) {
+    args.tiles_a[s] = a_tiles[s];
+    args.tiles_b[s] = b_tiles[s];
+  }
   args.tile_base = p->tile_base;
   args.n = b->n;
   args.x_offset = b->offset;
   args.eig_offset = b->eig_offset;
   args.row_scale = row_scale;
+  args.eigenvalues = eigenvalues;
+  args.a_in = a_in;
+  args.norms = norms;
   args.x = x;
   args.status = ctx->d_status;
   const unsigned grid = std::min(p->gemm_items, kSmCount);
-  static bool attr = false;
-  if (!attr) {
-    MSQ_TRY(cudaCheck(ctx, cudaFuncSetAttribute(tcGemmKernel<kOpBf16>,
-                                                cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                                static_cast<int>(tcSmemBytes())), "tc attr"));
-    MSQ_TRY(cudaCheck(ctx, cudaFuncSetAttribute(tcGemmKernel<kOpFp8>,
-                                                cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                                static_cast<int>(tcSmemBytes())), "tc attr"));
-    attr = true;
+  const size_t smem = tcSmemBytes();
+  switch (epilogue) {
+    case kEpiRowScale:
+      tcGemmKernel<kOpFp8, kEpiRowScale><<<grid, kTcThreads, smem, ctx->stream>>>(args);
+      break;
+    case kEpiInverseH:
+      tcGemmKernel<kOpBf16, kEpiInverseH><<<grid, kTcThreads, smem, ctx->stream>>>(args);
+      break;
+    case kEpiResidual:
+      tcGemmKernel<kOpBf16, kEpiResidual><<<grid, kTcThreads, smem, ctx->stream>>>(args);
+      break;
+    default:
+      tcGemmKernel<kOpBf16, kEpiStore><<<grid, kTcThreads, smem, ctx->stream>>>(args);
+      break;
   }
-  if (p->kind == kOpFp8) {
-    tcGemmKernel<kOpFp8><<<grid, kTcThreads, tcSmemBytes(), ctx->stream>>>(args);
-  } else {
-    tcGemmKernel<kOpBf16><<<grid, kTcThreads, tcSmemBytes(), ctx->stream>>>(args);
-  }
-  return launched(ctx, "tcgen05 reconstruction");
+  return launched(ctx, what);
+}
+
+int runTcGemm(msq_ctx *ctx, const DeviceBatch *b, TcPlan *p, const uint8_t *tiles,
+              const float *row_scale, float *x) {
+  const uint8_t *t[1] = {tiles};
+  return launchTcGemm(ctx, b, p, p->kind == kOpFp8 ? kEpiRowScale : kEpiStore, 1, t, t,
+                      row_scale, nullptr, nullptr, nullptr, x, "tcgen05 reconstruction");
 }
 
 template <int kSource>
@@ -568,6 +700,97 @@ int launchPack(msq_ctx *ctx, const DeviceBatch *b, TcPlan *p, const float *f,
 }
 
 }  // namespace
+
+namespace {
+
+int packSplit(msq_ctx *ctx, const DeviceBatch *b, TcPlan *p, const float *hi, const float *lo,
+              bool transpose, int pieces, uint8_t *const *out) {
+  SplitArgs args{};
+  args.work = p->pack_work;
+  args.items = p->pack_items;
+  args.hi = hi;
+  args.lo = lo;
+  args.offset = b->offset;
+  args.tile_base = p->tile_base;
+  args.n = b->n;
+  args.pieces = pieces;
+  for (int q = 0; q < pieces; ++q) args.out[q] = out[q];
+  const unsigned grid = std::min(p->pack_items, kSmCount * 16);
+  if (transpose) {
+    packSplitKernel<true><<<grid, 128, 0, ctx->stream>>>(args);
+  } else {
+    packSplitKernel<false><<<grid, 128, 0, ctx->stream>>>(args);
+  }
+  return launched(ctx, "pack split-BF16");
+}
+
+// Scratch for split operands: kBuffers tile buffers of the BF16 plan.
+constexpr int kBuffers = 6;
+uint8_t *splitBuffers(msq_ctx *ctx, TcPlan *p, uint8_t *bufs[kBuffers]) {
+  const size_t one = static_cast<size_t>(p->total_tiles) * kTileBytes;
+  uint8_t *mem = static_cast<uint8_t *>(scratch(ctx, one * kBuffers, kScratchGemm));
+  if (mem == nullptr) return nullptr;
+  for (int q = 0; q < kBuffers; ++q) bufs[q] = mem + q * one;
+  return mem;
+}
+
+// C = A B^T with A, B each split in two BF16 pieces: a0 b0 + a0 b1 + a1 b0
+// (the dropped a1 b1 term is ~2^-16 relative).
+int gemmSplit2(msq_ctx *ctx, const DeviceBatch *b, TcPlan *p, uint8_t *const *a, uint8_t *const *bb,
+               int epilogue, const float *eigenvalues, float *out, const char *what) {
+  const uint8_t *sa[3] = {a[0], a[0], a[1]};
+  const uint8_t *sb[3] = {bb[0], bb[1], bb[0]};
+  return launchTcGemm(ctx, b, p, epilogue, 3, sa, sb, nullptr, eigenvalues, nullptr, nullptr, out,
+                      what);
+}
+
+}  // namespace
+
+// One frozen-basis Sylvester sweep with every GEMM on the tensor cores
+// (split-BF16 operands, FP32 accumulation in TMEM):
+//   G = R V, C = (V^T G) o H, Z^T = C V^T, E = Z V^T, X <- X + (E + E^T)/2.
+// The correction is residual-sized, so the ~1e-5 relative error of the
+// two-piece products is far below what the next sweep can see.
+int sylvesterTc(msq_ctx *ctx, const DeviceBatch *b, const float *v, const float *lam,
+                const float *r, float *ws0, float *ws1, float **correction) {
+  TcPlan *p = tcPlan(ctx, b, kOpBf16);
+  if (p == nullptr) return MSQ_ERR_CUDA;
+  uint8_t *buf[kBuffers];
+  if (splitBuffers(ctx, p, buf) == nullptr) return MSQ_ERR_CUDA;
+  uint8_t *vn[2] = {buf[0], buf[1]}, *vt[2] = {buf[2], buf[3]}, *op[2] = {buf[4], buf[5]};
+  MSQ_TRY(packSplit(ctx, b, p, v, nullptr, false, 2, vn));  // rows = columns of V
+  MSQ_TRY(packSplit(ctx, b, p, v, nullptr, true, 2, vt));   // rows = rows of V
+  MSQ_TRY(packSplit(ctx, b, p, r, nullptr, false, 2, op));  // R (symmetric)
+  MSQ_TRY(gemmSplit2(ctx, b, p, op, vn, kEpiStore, nullptr, ws0, "tc sylvester G=RV"));
+  MSQ_TRY(packSplit(ctx, b, p, ws0, nullptr, false, 2, op));
+  MSQ_TRY(gemmSplit2(ctx, b, p, vn, op, kEpiInverseH, lam, ws1, "tc sylvester C=V'G/H"));
+  MSQ_TRY(packSplit(ctx, b, p, ws1, nullptr, false, 2, op));
+  MSQ_TRY(gemmSplit2(ctx, b, p, op, vt, kEpiStore, nullptr, ws0, "tc sylvester Zt=CV'"));
+  MSQ_TRY(packSplit(ctx, b, p, ws0, nullptr, false, 2, op));
+  MSQ_TRY(gemmSplit2(ctx, b, p, op, vt, kEpiStore, nullptr, ws1, "tc sylvester E=ZV'"));
+  *correction = ws1;
+  return MSQ_OK;
+}
+
+// R = A - X X on the tensor cores: X = x0 + x1 + x2 (BF16 pieces of the
+// float-float X), X X ~ x0x0 + x0x1 + x1x0 + x0x2 + x2x0 + x1x1 accumulated
+// in FP32 in one TMEM accumulator; the epilogue forms R and the FP64 norms.
+// About FP32 accuracy: used between sweeps; the accepting residual is the
+// float-float one.
+int residualTc(msq_ctx *ctx, const DeviceBatch *b, const float *a, const float *x_hi,
+               const float *x_lo, float *r, double *norms) {
+  TcPlan *p = tcPlan(ctx, b, kOpBf16);
+  if (p == nullptr) return MSQ_ERR_CUDA;
+  uint8_t *buf[kBuffers];
+  if (splitBuffers(ctx, p, buf) == nullptr) return MSQ_ERR_CUDA;
+  MSQ_TRY(packSplit(ctx, b, p, x_hi, x_lo, false, 3, buf));
+  const uint8_t *sa[6] = {buf[0], buf[0], buf[1], buf[0], buf[2], buf[1]};
+  const uint8_t *sb[6] = {buf[0], buf[1], buf[0], buf[2], buf[0], buf[1]};
+  MSQ_TRY(cudaCheck(ctx, cudaMemsetAsync(norms, 0, 2 * b->count * sizeof(double), ctx->stream),
+                    "norm reset"));
+  return launchTcGemm(ctx, b, p, kEpiResidual, 6, sa, sb, nullptr, nullptr, a, norms, r,
+                      "tc residual");
+}
 
 int reconstructLowBit(msq_ctx *ctx, const DeviceBatch *b, int format, const float *f, float *x) {
   const int kind = format == MSQ_FMT_FP8_E4M3FN_ROWSCALE ? kOpFp8 : kOpBf16;
@@ -598,7 +821,7 @@ int reconstructLowBit(msq_ctx *ctx, const DeviceBatch *b, int format, const floa
 }
 
 int reconstructEncoded(msq_ctx *ctx, const DeviceBatch *b, int format, const void *values,
-                       const float *scales, float *x) {
+                       const void *scales, float *x) {
   const int kind = format == MSQ_FMT_FP8_E4M3FN_ROWSCALE ? kOpFp8 : kOpBf16;
   if (format != MSQ_FMT_BF16 && format != MSQ_FMT_FP8_E4M3FN_ROWSCALE &&
       format != MSQ_FMT_MXFP4_E2M1) {
@@ -618,14 +841,16 @@ int reconstructEncoded(msq_ctx *ctx, const DeviceBatch *b, int format, const voi
       MSQ_TRY(launchPack<kPackBf16Codes>(ctx, b, p, nullptr, codes, nullptr, nullptr, mem));
       break;
     case MSQ_FMT_FP8_E4M3FN_ROWSCALE:
-      MSQ_TRY(launchPack<kPackFp8Codes>(ctx, b, p, nullptr, codes, nullptr, scales, mem));
+      MSQ_TRY(launchPack<kPackFp8Codes>(ctx, b, p, nullptr, codes, nullptr,
+                                        static_cast<const float *>(scales), mem));
       break;
     default:
       MSQ_TRY(launchPack<kPackMxfp4Codes>(ctx, b, p, nullptr, codes,
                                           reinterpret_cast<const uint8_t *>(scales), nullptr, mem));
       break;
   }
-  return runTcGemm(ctx, b, p, mem, scales, x);
+  return runTcGemm(ctx, b, p, mem,
+                   kind == kOpFp8 ? static_cast<const float *>(scales) : nullptr, x);
 }
 
 }  // namespace msq

@@ -285,6 +285,51 @@ def plain_method(a: np.ndarray, max_corrections: int = 12, tol: float = 1e-12):
     return root, history
 
 
+# --------------------------------------------------- plan-selector MLP
+
+MLP_SHAPES = ((64, 16), (64, 64), (8, 64))
+
+
+def _mlp_unpack(params: np.ndarray):
+    """FP32 master parameters -> BF16-rounded FP64 (W1, b1, W2, b2, W3, b3),
+    the layout of msq_mlp.cu.  BF16 rounding is the reference codec's RNE."""
+    v, _ = encode(1, np.asarray(params, np.float32))
+    p = decode(1, v, None, params.size).astype(np.float64)
+    out, off = [], 0
+    for rows, cols in MLP_SHAPES:
+        out.append(p[off:off + rows * cols].reshape(rows, cols))
+        off += rows * cols
+        out.append(p[off:off + rows])
+        off += rows
+    return out
+
+
+def mlp_forward(params: np.ndarray, x: np.ndarray):
+    W1, b1, W2, b2, W3, b3 = _mlp_unpack(params)
+    h1 = np.maximum(x @ W1.T + b1, 0.0)
+    h2 = np.maximum(h1 @ W2.T + b2, 0.0)
+    return h2 @ W3.T + b3, (h1, h2)
+
+
+def mlp_loss_and_grad(params: np.ndarray, x: np.ndarray, y: np.ndarray):
+    """Mean sigmoid cross-entropy over rows and outputs and its gradient with
+    respect to the FP32 masters (BF16 rounding as a straight-through
+    identity), in FP64."""
+    W1, b1, W2, b2, W3, b3 = _mlp_unpack(params)
+    x = np.asarray(x, np.float64)
+    z, (h1, h2) = mlp_forward(params, x)
+    scale = 1.0 / z.size
+    loss = np.sum(np.maximum(z, 0) + np.log1p(np.exp(-np.abs(z))) - y * z) * scale
+    dz = (1.0 / (1.0 + np.exp(-z)) - y) * scale
+    gW3, gb3 = dz.T @ h2, dz.sum(0)
+    dh2 = (dz @ W3) * (h2 > 0)
+    gW2, gb2 = dh2.T @ h1, dh2.sum(0)
+    dh1 = (dh2 @ W2) * (h1 > 0)
+    gW1, gb1 = dh1.T @ x, dh1.sum(0)
+    grad = np.concatenate([gW1.ravel(), gb1, gW2.ravel(), gb2, gW3.ravel(), gb3])
+    return loss, grad
+
+
 # ------------------------------------------- the reference's own CPU code
 
 _REF = None

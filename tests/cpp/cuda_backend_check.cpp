@@ -1,0 +1,60 @@
+// Drives the C++ host mirror (runCudaCase) on one matrix, the way the
+// reference's CLI drives runMetalCase.  Input file: int32 n, n*n FP64 A
+// (column-major), optionally n*n FP64 reference root.  Prints key=value.
+// Usage: cuda_backend_check <matrix.bin> <basis: fp32|bf16|fp8_e4m3fn_rowscale|mxfp4_e2m1>
+//                           <tolerance> <max_iterations>
+#include <cstdint>
+#include <cstdio>
+#include <cstdlib>
+#include <exception>
+#include <iomanip>
+#include <iostream>
+#include <vector>
+
+#include "cuda_backend.hpp"
+
+int main(int argc, char **argv) {
+  if (argc < 5) {
+    std::cerr << "usage: cuda_backend_check matrix.bin basis tolerance max_iterations\n";
+    return 2;
+  }
+  try {
+    FILE *f = std::fopen(argv[1], "rb");
+    if (!f) throw std::runtime_error("cannot open input");
+    int32_t n = 0;
+    if (std::fread(&n, sizeof(n), 1, f) != 1) throw std::runtime_error("bad input");
+    mixed_sqrt::PreparedMatrix m;
+    m.order = static_cast<size_t>(n);
+    m.values.resize(m.order * m.order);
+    if (std::fread(m.values.data(), sizeof(double), m.values.size(), f) != m.values.size())
+      throw std::runtime_error("bad input");
+    std::vector<double> ref(m.values.size());
+    const bool have_ref = std::fread(ref.data(), sizeof(double), ref.size(), f) == ref.size();
+    std::fclose(f);
+    mixed_sqrt::CudaRuntime runtime(0);
+    mixed_sqrt::CudaSolverConfiguration config;
+    config.basis_format = mixed_sqrt::cudaBasisFormatForCliName(argv[2]);
+    mixed_sqrt::CudaProblem problem;
+    problem.order = m.order;
+    problem.tolerance = std::atof(argv[3]);
+    problem.max_iterations = static_cast<size_t>(std::atoi(argv[4]));
+    problem.prepared_matrix = &m;
+    problem.supplied_reference = have_ref ? &ref : nullptr;
+    const mixed_sqrt::CaseResult r = mixed_sqrt::runCudaCase(runtime, config, problem);
+    std::cout << std::setprecision(17) << "status=" << r.status
+              << " iterations=" << (r.history.size() - 1)
+              << " final_residual=" << r.final_residual
+              << " final_forward_error=" << r.final_forward_error
+              << " initial_residual=" << r.history.front().residual
+              << " selected_basis_stage=" << r.selected_basis_stage
+              << " precision_escalations=" << r.precision_escalations
+              << " basis_orthogonality=" << r.frozen_basis_orthogonality
+              << " quantized_basis_orthogonality=" << r.quantized_basis_orthogonality
+              << " symmetry_error=" << r.symmetry_error << "\n";
+    return 0;
+  } catch (const std::exception &error) {
+    // the reference's main(): report and exit nonzero (src/main.cpp:12-16)
+    std::cerr << "error: " << error.what() << "\n";
+    return 1;
+  }
+}

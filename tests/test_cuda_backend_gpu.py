@@ -1,0 +1,64 @@
+"""The C++ host mirror of the reference's backend contract (runCudaCase over
+the C ABI), driven like the reference's CLI drives runMetalCase, checked
+against the FP64 oracle."""
+import os
+import subprocess
+
+import numpy as np
+import pytest
+
+import oracle as O
+
+pytestmark = pytest.mark.gpu
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+EXE = os.path.join(ROOT, "tests", "cpp", "cuda_backend_check")
+
+
+def _run(tmp_path, a, basis, tol, iters, with_ref=True):
+    n = a.shape[0]
+    path = tmp_path / f"m{n}_{basis}.bin"
+    with open(path, "wb") as f:
+        f.write(np.int32(n).tobytes())
+        f.write(np.asfortranarray(a, np.float64).tobytes(order="F"))
+        if with_ref:
+            f.write(np.asfortranarray(O.reference_root(a), np.float64).tobytes(order="F"))
+    out = subprocess.run([EXE, str(path), basis, str(tol), str(iters)], capture_output=True,
+                         text=True, timeout=300)
+    fields = dict(kv.split("=", 1) for kv in out.stdout.split()) if out.returncode == 0 else {}
+    return out.returncode, fields, out.stderr
+
+
+@pytest.fixture(scope="module", autouse=True)
+def exe():
+    if not os.path.exists(EXE):
+        pytest.skip("cuda_backend_check was not built")
+
+
+@pytest.mark.parametrize("basis", ["fp32", "bf16", "fp8_e4m3fn_rowscale", "mxfp4_e2m1"])
+def test_run_cuda_case_reaches_tolerance(tmp_path, basis):
+    a = O.controlled(96, 1e2)  # the reference's controlled family (makeSpdMatrix)
+    rc, r, err = _run(tmp_path, a, basis, 1e-12, 12)
+    assert rc == 0, err
+    assert r["status"] == "converged", r
+    assert float(r["final_residual"]) <= 1e-12
+    # FP64-oracle forward error of the returned root (float-float X)
+    assert float(r["final_forward_error"]) < 1e-10
+    assert float(r["symmetry_error"]) < 1e-6
+    if basis == "fp32":
+        assert r["selected_basis_stage"] == "fp32"
+    else:
+        assert r["selected_basis_stage"] in (basis, basis + "_rejected_to_fp32")
+
+
+def test_rejects_invalid_input_like_the_reference(tmp_path):
+    a = O.controlled(16, 10.0)
+    a[3, 3] = np.nan
+    rc, r, err = _run(tmp_path, a, "fp32", 1e-12, 8, with_ref=False)
+    assert rc == 1 and "nonfinite" in err
+
+
+def test_budget_exhausted_status(tmp_path):
+    a = O.spd_loguniform(64, 1e4, seed=2)
+    rc, r, err = _run(tmp_path, a, "bf16", 1e-14, 0)
+    assert rc == 0 and r["status"] in ("budget_exhausted", "converged")
+    assert int(r["iterations"]) == 0

@@ -149,7 +149,8 @@ def test_float_float_residual_matches_oracle(ctx, msq):
         assert abs(rel_g - rel_o) < 1e-12
 
 
-def test_sylvester_sweep_matches_fp64_correction(ctx, msq):
+@pytest.mark.parametrize("gemm", ["fp32", "bf16"])
+def test_sylvester_sweep_matches_fp64_correction(ctx, msq, gemm):
     """One frozen-basis correction on the GPU vs the same correction in FP64
     (refineUpdateAndMeasure semantics) from the same X0, V, lambda."""
     import torch
@@ -168,7 +169,10 @@ def test_sylvester_sweep_matches_fp64_correction(ctx, msq):
     xh = _dev(b.pack(x0s))
     xl = torch.zeros_like(xh)
     r, norms = ctx.residual(a_d, xh, xl, b)
-    ctx.sylvester_sweep(msq.FP32, _dev(b.pack(vs)), _dev(np.concatenate(ws)), r, b, xh, xl)
+    # FP32: SIMT FP32 GEMMs; BF16: tcgen05 split-BF16 GEMMs (the correction is
+    # residual-sized, so its ~1e-5 relative product error stays below 1e-6 of X)
+    fmt = msq.FP32 if gemm == "fp32" else msq.BF16
+    ctx.sylvester_sweep(fmt, _dev(b.pack(vs)), _dev(np.concatenate(ws)), r, b, xh, xl)
     r2, norms2 = ctx.residual(a_d, xh, xl, b)
     torch.cuda.synchronize()
     x1 = [h.astype(np.float64) + l for h, l in zip(b.unpack(xh.cpu().numpy()), b.unpack(xl.cpu().numpy()))]
