@@ -74,7 +74,7 @@ uint64_t msq_launch_count(const msq_ctx *ctx);
 int msq_timing_begin(msq_ctx *ctx);
 int msq_timing_end(msq_ctx *ctx, char *out, size_t capacity);
 
-/* ---- codecs (the benchmark spec (b)) ---------------------------------------------
+/* ---- codecs ---------------------------------------------------------------
  * Byte sizes: storageBytes / scaleBytes (src/configuration.cpp:188-213).
  * For MSQ_FMT_FP8_E4M3FN_ROWSCALE the scale plane is 4 bytes per row.      */
 size_t msq_storage_bytes(int format, size_t elements);
@@ -98,12 +98,14 @@ int msq_decode(msq_ctx *ctx, int format, const uint8_t *values,
  * matrix occupies n[i]*n[i] elements, column-major).  `n` and `offset` are
  * HOST arrays; the library uploads them once per distinct batch layout.   */
 
-/* ---- Jacobi eigensolver (the benchmark spec (a)) -----------------------------------
+/* ---- Jacobi eigensolver ----------------------------------------------------
  * Replaces MetalRuntime::symmetricJacobi (src/metal_runtime.cpp:584-646) and
  * makeJacobiSchedule (src/metal_solver.cpp:50-79).  Parallel-order
- * (round-robin) two-sided cyclic Jacobi, FP32 storage, FP64 rotation angles
- * and FP64 off-norm.  Sweeps stop once off(A) <= tolerance * ||A||_F or
- * after max_sweeps.  In: matrices (FP32).  Out: vectors (FP32, column j =
+ * (round-robin) two-sided cyclic Jacobi over 8x8 block pivots, FP32 storage
+ * and FP32 rotation angles (each (c, s) renormalised so c^2 + s^2 = 1 to
+ * FP32 rounding), FP64 off-norm.  Sweeps stop once
+ * off(A) <= tolerance * ||A||_F or after max_sweeps (tolerance 0: exactly
+ * max_sweeps sweeps).  In: matrices (FP32).  Out: vectors (FP32, column j =
  * eigenvector j), eigenvalues (FP32, n[i] per matrix at value offset
  * eig_offset[i] = sum of previous n), sweeps_done / off_ratio per matrix
  * (device arrays, may be NULL).  `matrices` is overwritten (the converged,
@@ -113,7 +115,7 @@ int msq_jacobi_batched(msq_ctx *ctx, float *matrices, float *vectors,
                        const int64_t *offset, int count, double tolerance,
                        int max_sweeps, int32_t *sweeps_done, float *off_ratio);
 
-/* ---- reconstruction (the benchmark spec (c)) ---------------------------------------
+/* ---- reconstruction ---------------------------------------------------------
  * X = V diag(sqrt(lambda)) V^T per matrix, written as the symmetric product
  * X = W W^T with W = V diag(lambda^(1/4)).  Replaces reconstructTiled /
  * reconstructLowFactorTiled (src/metal_runtime.cpp:429-534).
@@ -132,7 +134,7 @@ int msq_reconstruct(msq_ctx *ctx, int format, const void *values,
                     const void *scales, const int32_t *n,
                     const int64_t *offset, int count, float *root);
 
-/* ---- residual and Sylvester correction (the benchmark spec (d)) --------------------
+/* ---- residual and Sylvester correction -------------------------------------
  * msq_residual: R = A - X*X with A = (a + a_lo) and X = (x_hi + x_lo) in
  * float-float (about 48 bits, the reference's WorkingFloat, which also keeps
  * A as a (high, low) pair: metal_mixed_sqrt.metal:1268-1317,

@@ -252,11 +252,13 @@ class Context:
                                          batch.count, _ptr(out)), "msq_reconstruct")
         return out
 
-    def residual(self, a, x_hi, x_lo, batch: Batch, want_r: bool = True):
+    def residual(self, a, x_hi, x_lo, batch: Batch, want_r: bool = True, a_lo=None):
+        """R = (a + a_lo) - (x_hi + x_lo)^2 in float-float; returns (R, norms)
+        with norms[2i] = ||R_i||^2, norms[2i+1] = ||A_i||^2 (FP64)."""
         torch = self.torch
         r = torch.empty_like(a) if want_r else None
         norms = torch.empty(2 * batch.count, dtype=torch.float64, device=a.device)
-        self.check(lib().msq_residual(self.handle, _ptr(a), None, _ptr(x_hi), _ptr(x_lo),
+        self.check(lib().msq_residual(self.handle, _ptr(a), _ptr(a_lo), _ptr(x_hi), _ptr(x_lo),
                                       batch.n.ctypes.data, batch.offset.ctypes.data,
                                       batch.count, _ptr(r), _ptr(norms)), "msq_residual")
         return r, norms

@@ -28,15 +28,81 @@ static cudaEvent_t takeEvent(msq_ctx *ctx) {
   return e;
 }
 
+static void recycleTiming(msq_ctx *ctx) {
+  for (auto &entry : ctx->timing_events) {
+    ctx->event_pool.push_back(entry.end);
+    if (entry.begin != nullptr) ctx->event_pool.push_back(entry.begin);
+  }
+  ctx->timing_events.clear();
+  if (ctx->pending_begin != nullptr) {
+    ctx->event_pool.push_back(ctx->pending_begin);
+    ctx->pending_begin = nullptr;
+  }
+}
+
 int launched(msq_ctx *ctx, const char *what) {
   ++ctx->launches;
   const int status = cudaCheck(ctx, cudaGetLastError(), what);
   if (status == MSQ_OK && ctx->timing) {
     cudaEvent_t e = takeEvent(ctx);
     cudaEventRecord(e, ctx->stream);
-    ctx->timing_events.emplace_back(what, e);
+    ctx->timing_events.push_back({what, e, nullptr});
   }
   return status;
+}
+
+void launchBegin(msq_ctx *ctx, cudaStream_t stream) {
+  if (!ctx->timing) return;
+  ctx->pending_begin = takeEvent(ctx);
+  cudaEventRecord(ctx->pending_begin, stream);
+}
+
+int launchedOn(msq_ctx *ctx, cudaStream_t stream, const char *what) {
+  ++ctx->launches;
+  const int status = cudaCheck(ctx, cudaGetLastError(), what);
+  if (ctx->timing && ctx->pending_begin != nullptr) {
+    cudaEvent_t e = takeEvent(ctx);
+    cudaEventRecord(e, stream);
+    ctx->timing_events.push_back({what, e, ctx->pending_begin});
+    ctx->pending_begin = nullptr;
+  }
+  return status;
+}
+
+cudaStream_t auxStream(msq_ctx *ctx, int i) {
+  if (ctx->aux[i] == nullptr) {
+    if (cudaStreamCreateWithFlags(&ctx->aux[i], cudaStreamNonBlocking) != cudaSuccess) {
+      ctx->aux[i] = nullptr;
+      return ctx->stream;  // degrade to the context stream (still correct)
+    }
+  }
+  return ctx->aux[i];
+}
+
+void syncReset(msq_ctx *ctx) { ctx->sync_next = 0; }
+
+cudaEvent_t syncEvent(msq_ctx *ctx) {
+  if (ctx->sync_next == ctx->sync_pool.size()) {
+    cudaEvent_t e = nullptr;
+    cudaEventCreateWithFlags(&e, cudaEventDisableTiming);
+    ctx->sync_pool.push_back(e);
+  }
+  return ctx->sync_pool[ctx->sync_next++];
+}
+
+int streamWait(msq_ctx *ctx, cudaStream_t waiter, cudaStream_t source) {
+  if (waiter == source) return MSQ_OK;
+  cudaEvent_t e = syncEvent(ctx);
+  MSQ_TRY(cudaCheck(ctx, cudaEventRecord(e, source), "event record"));
+  MSQ_TRY(cudaCheck(ctx, cudaStreamWaitEvent(waiter, e, 0), "stream wait"));
+  if (ctx->timing && waiter == ctx->stream) {
+    // restart the context-stream chain after a join (the join's wait is not
+    // a launch's duration)
+    cudaEvent_t m = takeEvent(ctx);
+    cudaEventRecord(m, ctx->stream);
+    ctx->timing_events.push_back({nullptr, m, nullptr});
+  }
+  return MSQ_OK;
 }
 
 int checkDeviceStatus(msq_ctx *ctx) {
@@ -180,8 +246,11 @@ extern "C" void msq_destroy(msq_ctx *ctx) {
   for (int slot = 0; slot < 4; ++slot)
     if (ctx->scratch[slot] != nullptr) cudaFree(ctx->scratch[slot]);
   if (ctx->d_status != nullptr) cudaFree(ctx->d_status);
-  for (auto &entry : ctx->timing_events) cudaEventDestroy(entry.second);
+  recycleTiming(ctx);
   for (cudaEvent_t e : ctx->event_pool) cudaEventDestroy(e);
+  for (cudaEvent_t e : ctx->sync_pool) cudaEventDestroy(e);
+  for (cudaStream_t s : ctx->aux)
+    if (s != nullptr) cudaStreamDestroy(s);
   delete ctx;
 }
 
@@ -207,11 +276,10 @@ extern "C" uint64_t msq_launch_count(const msq_ctx *ctx) {
 
 extern "C" int msq_timing_begin(msq_ctx *ctx) {
   if (ctx == nullptr) return MSQ_ERR_INVALID_ARGUMENT;
-  for (auto &entry : ctx->timing_events) ctx->event_pool.push_back(entry.second);
-  ctx->timing_events.clear();
+  recycleTiming(ctx);
   cudaEvent_t e = takeEvent(ctx);
   MSQ_TRY(cudaCheck(ctx, cudaEventRecord(e, ctx->stream), "timing begin"));
-  ctx->timing_events.emplace_back("begin", e);
+  ctx->timing_events.push_back({nullptr, e, nullptr});
   ctx->timing = true;
   return MSQ_OK;
 }
@@ -219,13 +287,21 @@ extern "C" int msq_timing_begin(msq_ctx *ctx) {
 extern "C" int msq_timing_end(msq_ctx *ctx, char *out, size_t capacity) {
   if (ctx == nullptr || out == nullptr || capacity == 0) return MSQ_ERR_INVALID_ARGUMENT;
   ctx->timing = false;
-  MSQ_TRY(cudaCheck(ctx, cudaStreamSynchronize(ctx->stream), "timing end"));
+  MSQ_TRY(cudaCheck(ctx, cudaDeviceSynchronize(), "timing end"));
   struct Acc { double ms = 0.0; long count = 0; };
   std::vector<std::pair<std::string, Acc>> rows;
-  for (size_t i = 1; i < ctx->timing_events.size(); ++i) {
+  cudaEvent_t chain = nullptr;  // last context-stream event
+  for (size_t i = 0; i < ctx->timing_events.size(); ++i) {
+    const auto &entry = ctx->timing_events[i];
     float ms = 0.0f;
-    cudaEventElapsedTime(&ms, ctx->timing_events[i - 1].second, ctx->timing_events[i].second);
-    const std::string name = ctx->timing_events[i].first;
+    if (entry.begin != nullptr) {
+      cudaEventElapsedTime(&ms, entry.begin, entry.end);
+    } else {
+      if (chain != nullptr && entry.name != nullptr) cudaEventElapsedTime(&ms, chain, entry.end);
+      chain = entry.end;
+    }
+    if (entry.name == nullptr) continue;  // marker
+    const std::string name = entry.name;
     Acc *acc = nullptr;
     for (auto &r : rows)
       if (r.first == name) acc = &r.second;
@@ -243,7 +319,6 @@ extern "C" int msq_timing_end(msq_ctx *ctx, char *out, size_t capacity) {
   }
   std::strncpy(out, text.c_str(), capacity - 1);
   out[capacity - 1] = '\0';
-  for (auto &entry : ctx->timing_events) ctx->event_pool.push_back(entry.second);
-  ctx->timing_events.clear();
+  recycleTiming(ctx);
   return MSQ_OK;
 }

@@ -104,7 +104,10 @@ gemmTNKernel(GemmArgs args) {
         float v = acc[r][c];
         if (kEpilogue == kEpilogueInverseH) {
           const float *lam = args.eigenvalues + args.eig_offset[mi];
-          v = v / (rootOf(lam[i]) + rootOf(lam[j]));
+          // an FP32 eigenvalue <= 0 (below FP32 resolution of a nearly
+          // singular input) has root 0; the pair of two such gets no correction
+          const float d = rootOf(lam[i]) + rootOf(lam[j]);
+          v = d > 0.0f ? v / d : 0.0f;
         }
         C[i + static_cast<int64_t>(j) * n] = v;
       }

@@ -62,19 +62,43 @@ struct msq_ctx {
   size_t scratch_bytes[4] = {0, 0, 0, 0};
   // Batch layouts cached by content hash (small: a few entries).
   std::vector<msq::DeviceBatch *> batches;
-  // Launch timing (msq_timing_begin/end): one event after every launch; the
-  // gap between consecutive events on the stream is that launch's duration.
+  // Launch timing (msq_timing_begin/end).  Launches on the context stream
+  // record one event after each launch (duration = gap to the previous
+  // event on that stream); launches on auxiliary streams record a begin and
+  // an end event around the kernel.
+  struct TimingEntry {
+    const char *name;     // nullptr: a marker that only restarts the chain
+    cudaEvent_t end;
+    cudaEvent_t begin;    // nullptr for context-stream launches
+  };
   bool timing = false;
-  std::vector<std::pair<const char *, cudaEvent_t>> timing_events;
+  std::vector<TimingEntry> timing_events;
   std::vector<cudaEvent_t> event_pool;
+  cudaEvent_t pending_begin = nullptr;  // begin recorded for the next aux launch
+  // Auxiliary streams (non-blocking, created on first use) that fork from and
+  // join back into `stream` through events from sync_pool.
+  cudaStream_t aux[4] = {nullptr, nullptr, nullptr, nullptr};
+  std::vector<cudaEvent_t> sync_pool;
+  size_t sync_next = 0;
 };
 
 namespace msq {
 
 int setError(msq_ctx *ctx, int code, const std::string &message);
 int cudaCheck(msq_ctx *ctx, cudaError_t status, const char *what);
-// Checks the last launch error and counts one launch.
+// Checks the last launch error and counts one launch (context stream).
 int launched(msq_ctx *ctx, const char *what);
+// Launches on an auxiliary stream: launchBegin before, launchedOn after.
+void launchBegin(msq_ctx *ctx, cudaStream_t stream);
+int launchedOn(msq_ctx *ctx, cudaStream_t stream, const char *what);
+// Auxiliary stream i (0..3), created non-blocking on first use.
+cudaStream_t auxStream(msq_ctx *ctx, int i);
+// A disable-timing event from the context's pool; syncReset() recycles the
+// pool at the start of a call (events may be re-recorded once waited on).
+cudaEvent_t syncEvent(msq_ctx *ctx);
+void syncReset(msq_ctx *ctx);
+// `waiter` waits for everything enqueued so far on `source`.
+int streamWait(msq_ctx *ctx, cudaStream_t waiter, cudaStream_t source);
 // Returns MSQ_ERR_DEVICE_STATUS (and resets the word) if a kernel set it.
 int checkDeviceStatus(msq_ctx *ctx);
 // Uploads (or finds cached) the batch layout; null on error (ctx->error set).

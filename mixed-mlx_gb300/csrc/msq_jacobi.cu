@@ -48,8 +48,10 @@ struct JacobiState {
   double off_ratio;   // off(A) / ||A||_F when the sweeps stopped
   int sweeps;         // sweeps applied
   int done;           // 1 once converged or out of budget
-  int logged;         // 1 if the log holds a sweep not yet applied to V
-  int pad;
+  // logged[p]: 1 if log buffer p holds a sweep not yet applied to V.  The
+  // log is double-buffered by sweep parity so sweep k+1 can run while the
+  // replay of sweep k reads the other buffer.
+  int logged[2];
 };
 
 struct JacobiArgs {
@@ -67,6 +69,7 @@ struct JacobiArgs {
   double tol;
   int max_sweeps;
   int first;                 // 1 on the first launch (load A, set norm)
+  int parity;                // log buffer of this sweep (log points at it)
 };
 
 __host__ __device__ constexpr int padded8(int n) { return (n + 7) & ~7; }
@@ -174,14 +177,18 @@ __device__ __forceinline__ void storeBlock(float *tiles, const int *tri, int R, 
 // reference's angle formula (metal_mixed_sqrt.metal:1347-1357), accumulated
 // into q (q <- q J).  J = [c s; -s c] on (a, b): column a' = c a - s b,
 // column b' = s a + c b; p <- J^T p J with the pivot element set to zero.
+// Every operation is an explicitly rounded one (no contraction into FMA, no
+// approximate reciprocal square root), so the rotation is the same bit for
+// bit as the C restatement compiled with -ffp-contract=off.
 template <int a, int b>
 __device__ __forceinline__ void rotatePivot(float (&p)[8][8], float (&q)[8][8]) {
   const float apq = p[a][b];
   if (apq == 0.0f) return;
-  const float tau = (p[b][b] - p[a][a]) / (2.0f * apq);
-  const float t = copysignf(1.0f / (fabsf(tau) + sqrtf(fmaf(tau, tau, 1.0f))), tau);
-  float c = rsqrtf(fmaf(t, t, 1.0f));
-  float s = t * c;
+  const float tau = __fdiv_rn(__fsub_rn(p[b][b], p[a][a]), __fmul_rn(2.0f, apq));
+  const float root = __fsqrt_rn(__fadd_rn(__fmul_rn(tau, tau), 1.0f));
+  const float t = copysignf(__fdiv_rn(1.0f, __fadd_rn(fabsf(tau), root)), tau);
+  float c = __fdiv_rn(1.0f, __fsqrt_rn(__fadd_rn(__fmul_rn(t, t), 1.0f)));
+  float s = __fmul_rn(t, c);
   // FP32 (c, s) carry a one-signed error in c^2 + s^2 - 1 that compounds
   // over the thousands of rotations applied to each row of V.  Evaluate
   // e = c^2 + s^2 - 1 exactly (two-product: each square split by an FMA;
@@ -191,29 +198,29 @@ __device__ __forceinline__ void rotatePivot(float (&p)[8][8], float (&q)[8][8]) 
     const float cc = __fmul_rn(c, c), cce = fmaf(c, c, -cc);
     const float ss = __fmul_rn(s, s), sse = fmaf(s, s, -ss);
     const float e = __fadd_rn(__fadd_rn(__fsub_rn(cc, 1.0f), ss), __fadd_rn(cce, sse));
-    const float h = -0.5f * e;
+    const float h = __fmul_rn(-0.5f, e);
     c = fmaf(h, c, c);
     s = fmaf(h, s, s);
   }
 #pragma unroll
   for (int i = 0; i < 8; ++i) {
     const float pa = p[i][a], pb = p[i][b];
-    p[i][a] = c * pa - s * pb;
-    p[i][b] = s * pa + c * pb;
+    p[i][a] = __fsub_rn(__fmul_rn(c, pa), __fmul_rn(s, pb));
+    p[i][b] = __fadd_rn(__fmul_rn(s, pa), __fmul_rn(c, pb));
   }
 #pragma unroll
   for (int j = 0; j < 8; ++j) {
     const float pa = p[a][j], pb = p[b][j];
-    p[a][j] = c * pa - s * pb;
-    p[b][j] = s * pa + c * pb;
+    p[a][j] = __fsub_rn(__fmul_rn(c, pa), __fmul_rn(s, pb));
+    p[b][j] = __fadd_rn(__fmul_rn(s, pa), __fmul_rn(c, pb));
   }
   p[a][b] = 0.0f;
   p[b][a] = 0.0f;
 #pragma unroll
   for (int i = 0; i < 8; ++i) {
     const float qa = q[i][a], qb = q[i][b];
-    q[i][a] = c * qa - s * qb;
-    q[i][b] = s * qa + c * qb;
+    q[i][a] = __fsub_rn(__fmul_rn(c, qa), __fmul_rn(s, qb));
+    q[i][b] = __fadd_rn(__fmul_rn(s, qa), __fmul_rn(c, qb));
   }
 }
 
@@ -263,7 +270,7 @@ jacobiSweepKernel(JacobiArgs args) {
   // keep thread 0's final update after every warp's snapshot).
   const JacobiState s0 = st;
   if (!args.first && s0.done) {
-    if (threadIdx.x == 0) st.logged = 0;
+    if (threadIdx.x == 0) st.logged[args.parity] = 0;
     return;
   }
   size_t q_off, tile_off;
@@ -340,7 +347,7 @@ jacobiSweepKernel(JacobiArgs args) {
       st.sweeps = sweeps;
       st.off_ratio = ratio;
       st.done = 1;
-      st.logged = 0;
+      st.logged[args.parity] = 0;
     }
     return;
   }
@@ -483,7 +490,7 @@ jacobiSweepKernel(JacobiArgs args) {
     st.off_ratio = ratio;
     st.sweeps = sweeps + 1;
     st.done = 0;
-    st.logged = 1;
+    st.logged[args.parity] = 1;
   }
 }
 
@@ -497,6 +504,7 @@ struct VArgs {
   const int32_t *work_matrix;  // per CTA: matrix id
   const int32_t *work_row;     // per CTA: first row
   int rows_per_cta;            // multiple of 8
+  int parity;                  // log buffer to replay (log points at it)
 };
 
 __host__ __device__ __forceinline__ size_t replaySmemBytes(int max_n, int rows) {
@@ -513,7 +521,7 @@ __global__ void __launch_bounds__(kReplayThreads)
 jacobiReplayKernel(VArgs args) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int mi = args.work_matrix[blockIdx.x];
-  if (!args.state[mi].logged) return;
+  if (!args.state[mi].logged[args.parity]) return;
   const int r0 = args.work_row[blockIdx.x];
   const int n = args.n[mi];
   const int m = padded8(n), nb = m / 4, P = nb / 2;
@@ -729,9 +737,11 @@ int jacobiEnqueue(msq_ctx *ctx, const DeviceBatch *b, float *matrices, float *ve
   }
   JacobiPlan *plan = planFor(ctx, b);
   if (plan == nullptr) return MSQ_ERR_CUDA;
+  if (plan->buckets.empty()) return MSQ_OK;
   const size_t state_bytes = (b->count * sizeof(JacobiState) + 255) & ~size_t(255);
   const size_t tile_bytes = (plan->tile_total * sizeof(float) + 255) & ~size_t(255);
-  const size_t log_bytes = plan->log_total * sizeof(float);
+  // Two log buffers (sweep parity) so sweep k+1 overlaps the replay of k.
+  const size_t log_bytes = 2 * plan->log_total * sizeof(float);
   char *work = static_cast<char *>(scratch(ctx, state_bytes + tile_bytes + log_bytes, kScratchJacobi));
   if (work == nullptr) return MSQ_ERR_CUDA;
   if (setKernelAttributes() != MSQ_OK) return cudaCheck(ctx, cudaGetLastError(), "jacobi attributes");
@@ -739,7 +749,7 @@ int jacobiEnqueue(msq_ctx *ctx, const DeviceBatch *b, float *matrices, float *ve
   args.a = matrices;
   args.state = reinterpret_cast<JacobiState *>(work);
   args.tiles = reinterpret_cast<float *>(work + state_bytes);
-  args.log = reinterpret_cast<float *>(work + state_bytes + tile_bytes);
+  float *log_base = reinterpret_cast<float *>(work + state_bytes + tile_bytes);
   args.a_offset = b->offset;
   args.t_offset = plan->t_offset;
   args.log_offset = plan->log_offset;
@@ -754,24 +764,57 @@ int jacobiEnqueue(msq_ctx *ctx, const DeviceBatch *b, float *matrices, float *ve
     identityKernel<<<grid, 256, 0, ctx->stream>>>(vectors, b->offset, b->n, b->count);
     MSQ_TRY(launched(ctx, "jacobi identity"));
   }
-  VArgs vargs{vectors, b->offset, plan->log_offset, b->n, args.log, args.state,
-              plan->work_matrix, plan->work_row, plan->rows_per_cta};
+  VArgs vargs{vectors, b->offset, plan->log_offset, b->n, log_base, args.state,
+              plan->work_matrix, plan->work_row, plan->rows_per_cta, 0};
+  // Streams: size buckets round-robin over three sweep streams, the replay
+  // on a fourth.  Order: sweep k of a bucket follows sweep k-1 (same
+  // stream) and the replay of k-2 (which read the log buffer sweep k
+  // overwrites); the replay of k follows every bucket's sweep k.
+  syncReset(ctx);
+  const int sweep_streams = std::min<int>(3, static_cast<int>(plan->buckets.size()));
+  cudaStream_t ss[3];
+  for (int i = 0; i < sweep_streams; ++i) {
+    ss[i] = auxStream(ctx, 1 + i);
+    MSQ_TRY(streamWait(ctx, ss[i], ctx->stream));
+  }
+  cudaStream_t rs = auxStream(ctx, 0);
+  MSQ_TRY(streamWait(ctx, rs, ctx->stream));
+  cudaEvent_t replay_done[2] = {nullptr, nullptr};  // by parity
   for (int launch = 0; launch <= max_sweeps; ++launch) {
+    const int parity = launch & 1;
     args.first = launch == 0;
-    for (const auto &bucket : plan->buckets) {
-      args.order = plan->order + bucket.first;
-      if (bucket.smem) {
-        jacobiSweepKernel<true><<<bucket.count, bucket.threads, bucket.smem_bytes, ctx->stream>>>(args);
-      } else {
-        jacobiSweepKernel<false><<<bucket.count, bucket.threads, bucket.smem_bytes, ctx->stream>>>(args);
+    args.parity = parity;
+    args.log = log_base + parity * plan->log_total;
+    if (replay_done[parity] != nullptr) {
+      for (int i = 0; i < sweep_streams; ++i) {
+        MSQ_TRY(cudaCheck(ctx, cudaStreamWaitEvent(ss[i], replay_done[parity], 0), "stream wait"));
       }
-      MSQ_TRY(launched(ctx, "jacobi sweep"));
+    }
+    for (size_t k = 0; k < plan->buckets.size(); ++k) {
+      const auto &bucket = plan->buckets[k];
+      cudaStream_t s = ss[k % sweep_streams];
+      args.order = plan->order + bucket.first;
+      launchBegin(ctx, s);
+      if (bucket.smem) {
+        jacobiSweepKernel<true><<<bucket.count, bucket.threads, bucket.smem_bytes, s>>>(args);
+      } else {
+        jacobiSweepKernel<false><<<bucket.count, bucket.threads, bucket.smem_bytes, s>>>(args);
+      }
+      MSQ_TRY(launchedOn(ctx, s, "jacobi sweep"));
     }
     if (launch < max_sweeps) {
-      jacobiReplayKernel<<<plan->work_count, kReplayThreads, plan->v_smem, ctx->stream>>>(vargs);
-      MSQ_TRY(launched(ctx, "jacobi replay"));
+      for (int i = 0; i < sweep_streams; ++i) MSQ_TRY(streamWait(ctx, rs, ss[i]));
+      vargs.parity = parity;
+      vargs.log = args.log;
+      launchBegin(ctx, rs);
+      jacobiReplayKernel<<<plan->work_count, kReplayThreads, plan->v_smem, rs>>>(vargs);
+      MSQ_TRY(launchedOn(ctx, rs, "jacobi replay"));
+      replay_done[parity] = syncEvent(ctx);
+      MSQ_TRY(cudaCheck(ctx, cudaEventRecord(replay_done[parity], rs), "event record"));
     }
   }
+  for (int i = 0; i < sweep_streams; ++i) MSQ_TRY(streamWait(ctx, ctx->stream, ss[i]));
+  MSQ_TRY(streamWait(ctx, ctx->stream, rs));
   if (sweeps_done != nullptr || off_ratio != nullptr) {
     jacobiReportKernel<<<gridFor(b->count, 256), 256, 0, ctx->stream>>>(args.state, b->count,
                                                                        sweeps_done, off_ratio);

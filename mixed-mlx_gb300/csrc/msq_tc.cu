@@ -307,8 +307,13 @@ __global__ void __launch_bounds__(kTcThreads, 1) tcGemmKernel(TcArgs args) {
             if (j < n) {
               const int64_t at = i + static_cast<int64_t>(j) * n;
               float val = v[q];
-              if (kEpi == kEpiRowScale) val = val * ri * rs[j];
-              if (kEpi == kEpiInverseH) val = val / (si + sqrtf(fmaxf(lam[j], 0.0f)));
+              // (r_i r_j) first: the product of the two scales is the same
+              // for (i, j) and (j, i), so X stays exactly symmetric
+              if (kEpi == kEpiRowScale) val = val * (ri * rs[j]);
+              if (kEpi == kEpiInverseH) {
+                const float d = si + sqrtf(fmaxf(lam[j], 0.0f));
+                val = d > 0.0f ? val / d : 0.0f;  // both roots 0: no correction
+              }
               if (kEpi == kEpiResidual) {
                 const float a = A[at];
                 val = a - val;

@@ -343,8 +343,11 @@ int msqo_jacobi(float *a, float *v, float *w, unsigned n, double tol,
  * rows), block pairs by the round-robin rule over m/4 blocks; each 8x8
  * pivot gets one cyclic sweep of the scalar rotation above in the
  * round-robin order of 8 indices, accumulated into Q; every off-pivot 8x8
- * super-tile is replaced by Q_k^T T Q_l; V <- V Q.  FP32 storage and
- * arithmetic (the pivot angles too), FP64 off-norm.  Returns sweeps. */
+ * super-tile (k < l) is replaced by Q_k^T T Q_l and mirrored; V <- V Q.
+ * FP32 storage and arithmetic (the pivot angles too) with the roundings the
+ * CUDA kernels make, FP64 off-norm: after the same number of sweeps the
+ * results agree bit for bit.  Returns sweeps; a_out (nullable) receives the
+ * rotated matrix. */
 static const int kInner[28][2] = {
     {0, 7}, {1, 6}, {2, 5}, {3, 4}, {0, 6}, {5, 7}, {1, 4}, {2, 3}, {0, 5}, {4, 6},
     {3, 7}, {1, 2}, {0, 4}, {3, 5}, {2, 6}, {1, 7}, {0, 3}, {2, 4}, {1, 5}, {6, 7},
@@ -385,8 +388,8 @@ static void pivot_sweep(float p[8][8], float q[8][8]) {
   }
 }
 
-int msqo_jacobi_blocked(const float *a_in, float *v_out, float *w, unsigned n, double tol,
-                        int max_sweeps, double *off_ratio) {
+int msqo_jacobi_blocked(const float *a_in, float *a_out, float *v_out, float *w, unsigned n,
+                        double tol, int max_sweeps, double *off_ratio) {
   unsigned m = (n + 7u) & ~7u, nb = m / 4, P = nb / 2;
   float *A = (float *)calloc((size_t)m * m, sizeof(float));
   float *V = (float *)calloc((size_t)m * m, sizeof(float));
@@ -419,12 +422,18 @@ int msqo_jacobi_blocked(const float *a_in, float *v_out, float *w, unsigned n, d
         for (int r = 0; r < 8; ++r)
           for (int c = 0; c < 8; ++c) p[r][c] = A[idx[r] + (size_t)idx[c] * m];
         pivot_sweep(p, Q[k]);
+        /* the two diagonal 4x4 blocks are kept whole; the off-diagonal
+         * block is kept from the upper half and mirrored (the CUDA solver
+         * stores only upper 4x4 tiles) */
         for (int r = 0; r < 8; ++r)
-          for (int c = 0; c < 8; ++c) A[idx[r] + (size_t)idx[c] * m] = p[r][c];
+          for (int c = 0; c < 8; ++c) {
+            if ((r < 4) == (c < 4)) A[idx[r] + (size_t)idx[c] * m] = p[r][c];
+            else if (r < 4) A[idx[r] + (size_t)idx[c] * m] = A[idx[c] + (size_t)idx[r] * m] = p[r][c];
+          }
       }
+      /* off-pivot super-tiles k < l, mirrored into the lower half */
       for (unsigned k = 0; k < P; ++k)
-        for (unsigned l = 0; l < P; ++l) {
-          if (k == l) continue;
+        for (unsigned l = k + 1; l < P; ++l) {
           unsigned ri[8], ci[8];
           for (int x = 0; x < 4; ++x) {
             ri[x] = 4 * bi[k] + x; ri[4 + x] = 4 * bj[k] + x;
@@ -446,7 +455,8 @@ int msqo_jacobi_blocked(const float *a_in, float *v_out, float *w, unsigned n, d
               o[a][c] = s;
             }
           for (int r = 0; r < 8; ++r)
-            for (int c = 0; c < 8; ++c) A[ri[r] + (size_t)ci[c] * m] = o[r][c];
+            for (int c = 0; c < 8; ++c)
+              A[ri[r] + (size_t)ci[c] * m] = A[ci[c] + (size_t)ri[r] * m] = o[r][c];
         }
       for (unsigned row = 0; row < m; ++row)
         for (unsigned k = 0; k < P; ++k) {
@@ -466,7 +476,10 @@ int msqo_jacobi_blocked(const float *a_in, float *v_out, float *w, unsigned n, d
   }
   for (unsigned i = 0; i < n; ++i) w[i] = A[i + (size_t)i * m];
   for (unsigned c = 0; c < n; ++c)
-    for (unsigned r = 0; r < n; ++r) v_out[r + (size_t)c * n] = V[r + (size_t)c * m];
+    for (unsigned r = 0; r < n; ++r) {
+      v_out[r + (size_t)c * n] = V[r + (size_t)c * m];
+      if (a_out) a_out[r + (size_t)c * n] = A[r + (size_t)c * m];
+    }
   if (off_ratio) *off_ratio = ratio;
   free(A); free(V); free(Q); free(bi); free(bj);
   return sweeps;

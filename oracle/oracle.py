@@ -56,7 +56,7 @@ def olib() -> ctypes.CDLL:
         lib.msqo_storage_bytes.restype = ctypes.c_size_t
         lib.msqo_jacobi.argtypes = [_P, _P, _P, ctypes.c_uint, ctypes.c_double, ctypes.c_int,
                                     ctypes.POINTER(ctypes.c_double)]
-        lib.msqo_jacobi_blocked.argtypes = [_P, _P, _P, ctypes.c_uint, ctypes.c_double,
+        lib.msqo_jacobi_blocked.argtypes = [_P, _P, _P, _P, ctypes.c_uint, ctypes.c_double,
                                             ctypes.c_int, ctypes.POINTER(ctypes.c_double)]
         lib.msqo_jacobi_pair.argtypes = [ctypes.c_uint, ctypes.c_uint, ctypes.c_uint,
                                          ctypes.POINTER(ctypes.c_uint), ctypes.POINTER(ctypes.c_uint)]
@@ -118,15 +118,21 @@ def jacobi(a: np.ndarray, tol: float = 1e-7, max_sweeps: int = 15):
     return w, V, sweeps, ratio.value
 
 
-def jacobi_blocked(a: np.ndarray, tol: float = 1e-7, max_sweeps: int = 15):
-    """The same rotations in the blocked order the CUDA eigensolver uses."""
+def jacobi_blocked(a: np.ndarray, tol: float = 1e-7, max_sweeps: int = 15, with_matrix=False):
+    """The same rotations in the blocked order the CUDA eigensolver uses, with
+    the same FP32 roundings: after the same number of sweeps the CUDA kernels
+    return the same eigenvalues, eigenvectors and rotated matrix bit for bit.
+    Returns (w, V, sweeps, off_ratio[, final matrix])."""
     n = a.shape[0]
     A = np.asfortranarray(a, dtype=np.float32)
+    out = np.zeros((n, n), dtype=np.float32, order="F")
     V = np.zeros((n, n), dtype=np.float32, order="F")
     w = np.zeros(n, dtype=np.float32)
     ratio = ctypes.c_double()
-    sweeps = olib().msqo_jacobi_blocked(A.ctypes.data, V.ctypes.data, w.ctypes.data, n, tol,
-                                        max_sweeps, ctypes.byref(ratio))
+    sweeps = olib().msqo_jacobi_blocked(A.ctypes.data, out.ctypes.data, V.ctypes.data,
+                                        w.ctypes.data, n, tol, max_sweeps, ctypes.byref(ratio))
+    if with_matrix:
+        return w, V, sweeps, ratio.value, out
     return w, V, sweeps, ratio.value
 
 

@@ -42,7 +42,7 @@ def test_run_cuda_case_reaches_tolerance(tmp_path, basis):
     assert r["status"] == "converged", r
     assert float(r["final_residual"]) <= 1e-12
     # FP64-oracle forward error of the returned root (float-float X)
-    assert float(r["final_forward_error"]) < 1e-10
+    assert float(r["final_forward_error"]) < 1e-10, r
     assert float(r["symmetry_error"]) < 1e-6
     if basis == "fp32":
         assert r["selected_basis_stage"] == "fp32"

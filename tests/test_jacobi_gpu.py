@@ -6,6 +6,7 @@ import pytest
 import oracle as O
 
 pytestmark = pytest.mark.gpu
+U32 = 2.0 ** -24  # FP32 unit roundoff
 
 
 def _run(ctx, msq, mats, tol=1e-7, max_sweeps=15):
@@ -29,11 +30,11 @@ def test_single_matrix_eigenpairs(ctx, msq, n):
     ref = np.linalg.eigvalsh(a)
     scale = np.abs(ref).max()
     # FP32 Jacobi: eigenvalue error grows like n * u * ||A||_2
-    np.testing.assert_allclose(np.sort(w), ref, rtol=0, atol=max(5e-6, 6e-8 * n) * scale)
+    np.testing.assert_allclose(np.sort(w), ref, rtol=0, atol=max(5e-6, 3 * n * U32) * scale)
     np.testing.assert_allclose(v.T @ v, np.eye(n), atol=5e-6 * max(1, np.sqrt(n) / 4))
     # A V = V diag(w)
     resid = np.linalg.norm(a @ v - v * w) / np.linalg.norm(a)
-    assert resid < 1e-5
+    assert resid < max(1e-5, n * U32)
     assert off[0] <= 1e-7 or n == 1
     # the converged matrix is written back, nearly diagonal
     assert np.linalg.norm(af[0] - np.diag(np.diag(af[0]))) <= 1e-6 * np.linalg.norm(a)
@@ -44,30 +45,50 @@ def test_global_path_orders(ctx, msq, n):
     a = O.wishart(n, seed=n)
     vs, ws, sweeps, off, _ = _run(ctx, msq, [a])
     ref = np.linalg.eigvalsh(a)
-    np.testing.assert_allclose(np.sort(ws[0]), ref, rtol=0, atol=6e-8 * n * np.abs(ref).max())
-    assert np.linalg.norm(a @ vs[0] - vs[0] * ws[0]) / np.linalg.norm(a) < 2e-5
+    # FP32 Jacobi: eigenvalue error of order n * u * ||A|| (the CPU
+    # restatement of the same rotations measures 1.3-1.5 n u on Wishart input)
+    np.testing.assert_allclose(np.sort(ws[0]), ref, rtol=0, atol=3 * n * U32 * np.abs(ref).max())
+    assert np.linalg.norm(a @ vs[0] - vs[0] * ws[0]) / np.linalg.norm(a) < n * U32
 
 
-def test_matches_cpu_restatement_sweep_for_sweep(ctx, msq):
-    """Same blocked round-robin order, same rotation formula, FP32 storage:
-    the GPU and the CPU restatement take the same number of sweeps and agree
-    to FP32 rounding."""
+@pytest.mark.parametrize("n", [8, 24, 65, 130, 400])
+def test_bit_exact_against_cpu_restatement(ctx, msq, n):
+    """Same blocked round-robin order, same rotations, same FP32 roundings:
+    after the same number of sweeps (tolerance 0, fixed budget) the GPU and
+    the CPU restatement return identical eigenvalues, eigenvectors and
+    rotated matrix, bit for bit (n = 400 runs the global-memory tile path)."""
+    a = O.spd_loguniform(n, 1e2, seed=n) if n < 400 else O.wishart(n, seed=n)
+    sweeps_fixed = 3
+    w_o, v_o, sw_o, _, a_o = O.jacobi_blocked(a, 0.0, sweeps_fixed, with_matrix=True)
+    vs, ws, sweeps, off, af = _run(ctx, msq, [a], tol=0.0, max_sweeps=sweeps_fixed)
+    assert sw_o == sweeps_fixed and int(sweeps[0]) == sweeps_fixed
+    assert np.array_equal(ws[0].astype(np.float32), w_o)
+    assert np.array_equal(vs[0], v_o)
+    assert np.array_equal(af[0], a_o)
+
+
+def test_converged_sweeps_match_cpu_restatement(ctx, msq):
+    """With a tolerance, both stop after the same number of sweeps (the FP64
+    off-norms differ only in summation order) and agree on the spectrum."""
     for n in (8, 24, 65, 130):
         a = O.spd_loguniform(n, 1e2, seed=n)
         w_o, v_o, sw_o, off_o = O.jacobi_blocked(a, 1e-7, 15)
         vs, ws, sweeps, off, _ = _run(ctx, msq, [a])
         assert sw_o < 15 and abs(int(sweeps[0]) - sw_o) <= 1
-        np.testing.assert_allclose(ws[0], w_o, rtol=0, atol=1e-5 * np.abs(w_o).max())
+        if int(sweeps[0]) == sw_o:
+            assert np.array_equal(ws[0].astype(np.float32), w_o)
+        np.testing.assert_allclose(np.sort(ws[0]), np.sort(w_o), rtol=0,
+                                   atol=3 * n * U32 * np.abs(w_o).max())
 
 
 def test_uneven_batch(ctx, msq):
-    rng = np.random.default_rng(9)
     orders = O.wishart_orders(64, 16, 512, seed=4)
     mats = [O.wishart(int(n), seed=i) for i, n in enumerate(orders)]
     vs, ws, sweeps, off, _ = _run(ctx, msq, mats)
     for a, v, w in zip(mats, vs, ws):
         ref = np.linalg.eigvalsh(a)
-        np.testing.assert_allclose(np.sort(w), ref, rtol=0, atol=max(1e-5, 6e-8 * len(w)) * np.abs(ref).max())
+        np.testing.assert_allclose(np.sort(w), ref, rtol=0,
+                                   atol=max(1e-5, 3 * len(w) * U32) * np.abs(ref).max())
     assert np.all(off <= 1e-7)
 
 
