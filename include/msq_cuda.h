@@ -115,6 +115,34 @@ int msq_jacobi_batched(msq_ctx *ctx, float *matrices, float *vectors,
                        const int64_t *offset, int count, double tolerance,
                        int max_sweeps, int32_t *sweeps_done, float *off_ratio);
 
+/* ---- Jacobi without allocation ----------------------------------------------
+ * No counterpart in the reference.  For callers that must not allocate
+ * device memory: latency-critical loops, where cudaMalloc/cudaFree may
+ * synchronise the device and take unbounded time, and host applications that
+ * own all device memory and hand the library only their own buffers.  Solves
+ * ONE matrix of order n <= MSQ_NOALLOC_MAX_ORDER (256) with the same kernels
+ * and results as msq_jacobi_batched; every piece of scratch lives in one
+ * static device array of about 0.65 MB, which every GPU that loads the
+ * library holds until the process exits.  Needs no msq_ctx and calls no
+ * cudaMalloc, cudaFree or other allocating function.  Larger (or
+ * non-positive) n, a null buffer, tolerance < 0 or max_sweeps outside
+ * [0, 64] return MSQ_ERR_INVALID_ARGUMENT before anything is launched.
+ * The first call on a device (the current device) looks up the array's
+ * device address once; make that first call before capturing any stream.
+ * Each call first resets, with a small kernel on `stream`, the part of the
+ * array that must start at zero (the sweep state); everything else is
+ * written before it is read.  All calls on one device share the one array:
+ * calls that overlap on the GPU (on two streams, or from two threads) race
+ * on it and corrupt each other's results, so issue them on one stream.
+ * `stream` is a cudaStream_t (NULL: the default stream); `matrix` is
+ * overwritten as in msq_jacobi_batched; sweeps_done / off_ratio are device
+ * pointers to one element each, or NULL.  The call is asynchronous; a CUDA
+ * launch error returns MSQ_ERR_CUDA.                                        */
+#define MSQ_NOALLOC_MAX_ORDER 256
+int msq_jacobi_noalloc(float *matrix, float *vectors, float *eigenvalues, int n,
+                       double tolerance, int max_sweeps, void *stream,
+                       int32_t *sweeps_done, float *off_ratio);
+
 /* ---- reconstruction ---------------------------------------------------------
  * X = V diag(sqrt(lambda)) V^T per matrix, written as the symmetric product
  * X = W W^T with W = V diag(lambda^(1/4)).  Replaces reconstructTiled /

@@ -74,6 +74,8 @@ _SIGS = {
     "msq_decode": (ctypes.c_int, [_P, ctypes.c_int, _P, _P, ctypes.c_size_t, ctypes.c_size_t, _P]),
     "msq_jacobi_batched": (ctypes.c_int, [_P, _P, _P, _P, _P, _P, ctypes.c_int,
                                           ctypes.c_double, ctypes.c_int, _P, _P]),
+    "msq_jacobi_noalloc": (ctypes.c_int, [_P, _P, _P, ctypes.c_int, ctypes.c_double,
+                                          ctypes.c_int, _P, _P, _P]),
     "msq_timing_begin": (ctypes.c_int, [_P]),
     "msq_timing_end": (ctypes.c_int, [_P, ctypes.c_char_p, ctypes.c_size_t]),
     "msq_make_factor": (ctypes.c_int, [_P, _P, _P, _P, _P, ctypes.c_int, _P]),

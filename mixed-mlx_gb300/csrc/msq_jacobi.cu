@@ -845,3 +845,130 @@ extern "C" int msq_jacobi_batched(msq_ctx *ctx, float *matrices, float *vectors,
   return jacobiEnqueue(ctx, b, matrices, vectors, eigenvalues, tolerance,
                        max_sweeps, sweeps_done, off_ratio);
 }
+
+// ---------------------------------------------------------------------------
+// Jacobi for callers that must not allocate device memory.
+//
+// Latency-critical loops (cudaMalloc/cudaFree may synchronise the device and
+// take unbounded time) and host applications that own all device memory
+// cannot use the context's grow-only scratch.  msq_jacobi_noalloc solves one
+// matrix with the same kernels as msq_jacobi_batched, but every piece of
+// scratch (the packed tiles of A, the per-round rotation log, the sweep state
+// and the small layout tables) lives in the file-scope array below, sized
+// for one matrix of order up to MSQ_NOALLOC_MAX_ORDER: 130 KiB of tiles,
+// 504 KiB of log and a few hundred bytes of tables, about 0.65 MB in all.
+// The array is part of the loaded module, so every GPU that loads this
+// library holds it until the process exits.  It uses one log buffer (parity
+// 0): sweeps and replays alternate on the caller's stream.
+namespace msq {
+namespace {
+
+constexpr int kNoAllocOrder = MSQ_NOALLOC_MAX_ORDER;
+constexpr int kNoAllocBlocks = padded8(kNoAllocOrder) / 4;
+constexpr int kNoAllocPairs = kNoAllocBlocks / 2;
+constexpr int kNoAllocRowsPerCta = 32;
+constexpr int kNoAllocCtas = (kNoAllocOrder + kNoAllocRowsPerCta - 1) / kNoAllocRowsPerCta;
+
+struct NoAllocScratch {
+  JacobiState state[1];
+  int32_t n[1];
+  int32_t order[1];
+  int64_t a_offset[1];  // all offsets are zero: one matrix
+  int64_t t_offset[1];
+  int64_t log_offset[1];
+  int64_t eig_offset[1];
+  int32_t work_matrix[kNoAllocCtas];
+  int32_t work_row[kNoAllocCtas];
+  alignas(16) float tiles[kNoAllocBlocks * (kNoAllocBlocks + 1) / 2 * kTileF];
+  alignas(16) float log[(kNoAllocBlocks - 1) * kNoAllocPairs * kQF];
+};
+
+static __device__ __align__(256) unsigned char g_noalloc_scratch[sizeof(NoAllocScratch)];
+
+// Device address of g_noalloc_scratch per device, looked up once per device
+// (cudaGetSymbolAddress with that device current).  Host code must not use
+// the symbol itself: on the host it names a stand-in, not device memory.
+NoAllocScratch *g_noalloc_address[64] = {};
+
+// Resets what must start at zero (the sweep state) and writes the one-matrix
+// layout tables; the tiles and the log are fully written before being read.
+__global__ void noAllocSetupKernel(NoAllocScratch *s, int n) {
+  const int t = threadIdx.x;
+  if (t == 0) {
+    s->state[0] = JacobiState{};
+    s->n[0] = n;
+    s->order[0] = 0;
+    s->a_offset[0] = 0;
+    s->t_offset[0] = 0;
+    s->log_offset[0] = 0;
+    s->eig_offset[0] = 0;
+  }
+  for (int r = t; r < kNoAllocCtas; r += blockDim.x) {
+    s->work_matrix[r] = 0;
+    s->work_row[r] = r * kNoAllocRowsPerCta;
+  }
+}
+
+}  // namespace
+}  // namespace msq
+
+extern "C" int msq_jacobi_noalloc(float *matrix, float *vectors, float *eigenvalues, int n,
+                                  double tolerance, int max_sweeps, void *stream,
+                                  int32_t *sweeps_done, float *off_ratio) {
+  if (matrix == nullptr || vectors == nullptr || eigenvalues == nullptr) {
+    return MSQ_ERR_INVALID_ARGUMENT;
+  }
+  if (n < 1 || n > kNoAllocOrder) return MSQ_ERR_INVALID_ARGUMENT;  // beyond the static scratch
+  if (!(tolerance >= 0.0) || max_sweeps < 0 || max_sweeps > 64) return MSQ_ERR_INVALID_ARGUMENT;
+  int device = 0;
+  if (cudaGetDevice(&device) != cudaSuccess || device < 0 || device >= 64) return MSQ_ERR_CUDA;
+  NoAllocScratch *s = g_noalloc_address[device];
+  if (s == nullptr) {
+    // One-time set-up for this device (so the first call on a device should
+    // come before any stream capture).
+    void *address = nullptr;
+    if (cudaGetSymbolAddress(&address, g_noalloc_scratch) != cudaSuccess || address == nullptr) {
+      return MSQ_ERR_CUDA;
+    }
+    if (setKernelAttributes() != MSQ_OK) return MSQ_ERR_CUDA;
+    s = static_cast<NoAllocScratch *>(address);
+    g_noalloc_address[device] = s;
+  }
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  noAllocSetupKernel<<<1, 128, 0, st>>>(s, n);
+  JacobiArgs args{};
+  args.a = matrix;
+  args.tiles = s->tiles;
+  args.a_offset = s->a_offset;
+  args.t_offset = s->t_offset;
+  args.log_offset = s->log_offset;
+  args.eig_offset = s->eig_offset;
+  args.n = s->n;
+  args.log = s->log;
+  args.eigenvalues = eigenvalues;
+  args.state = s->state;
+  args.order = s->order;
+  args.tol = tolerance;
+  args.max_sweeps = max_sweeps;
+  const bool smem = fitsSmem(n);
+  size_t q_off, tile_off;
+  const size_t sweep_smem = sweepSmemLayout(n, smem, &q_off, &tile_off);
+  const int rows = (n + kNoAllocRowsPerCta - 1) / kNoAllocRowsPerCta;
+  VArgs vargs{vectors, s->a_offset, s->log_offset, s->n, s->log, s->state,
+              s->work_matrix, s->work_row, kNoAllocRowsPerCta};
+  const size_t v_smem = replaySmemBytes(n, kNoAllocRowsPerCta);
+  identityKernel<<<dim3(64, 1), 256, 0, st>>>(vectors, s->a_offset, s->n, 1);
+  for (int launch = 0; launch <= max_sweeps; ++launch) {
+    args.first = launch == 0;
+    if (smem) {
+      jacobiSweepKernel<true><<<1, threadsFor(n), sweep_smem, st>>>(args);
+    } else {
+      jacobiSweepKernel<false><<<1, threadsFor(n), sweep_smem, st>>>(args);
+    }
+    if (launch < max_sweeps) jacobiReplayKernel<<<rows, kReplayThreads, v_smem, st>>>(vargs);
+  }
+  if (sweeps_done != nullptr || off_ratio != nullptr) {
+    jacobiReportKernel<<<1, 32, 0, st>>>(s->state, 1, sweeps_done, off_ratio);
+  }
+  return cudaGetLastError() == cudaSuccess ? MSQ_OK : MSQ_ERR_CUDA;
+}

@@ -37,7 +37,7 @@ def test_header_declares_the_boundary():
     names = declared_symbols()
     for must in ("msq_create", "msq_encode", "msq_decode", "msq_jacobi_batched",
                  "msq_reconstruct", "msq_residual", "msq_sylvester_sweep", "msq_solve_batched",
-                 "msq_mlp_forward", "msq_mlp_backward", "msq_mlp_step"):
+                 "msq_mlp_forward", "msq_mlp_backward", "msq_mlp_step", "msq_jacobi_noalloc"):
         assert must in names
 
 
