@@ -40,7 +40,7 @@ constexpr int kTileF = 16;      // floats per 4x4 tile
 constexpr int kQF = 64;         // floats per 8x8 rotation
 constexpr size_t kSmemLimit = 227 * 1024;
 constexpr int kMaxOrder = 2048;
-constexpr int kSweepThreadsMax = 256;
+constexpr int kSweepThreadsMax = 512;
 constexpr int kReplayThreads = 256;
 
 struct JacobiState {
@@ -173,77 +173,206 @@ __device__ __forceinline__ void storeBlock(float *tiles, const int *tri, int R, 
   }
 }
 
-// One Jacobi rotation of the 8x8 pivot p on the index pair (a, b), the
-// reference's angle formula (metal_mixed_sqrt.metal:1347-1357), accumulated
-// into q (q <- q J).  J = [c s; -s c] on (a, b): column a' = c a - s b,
-// column b' = s a + c b; p <- J^T p J with the pivot element set to zero.
-// Every operation is an explicitly rounded one (no contraction into FMA, no
-// approximate reciprocal square root), so the rotation is the same bit for
-// bit as the C restatement compiled with -ffp-contract=off.
-template <int a, int b>
-__device__ __forceinline__ void rotatePivot(float (&p)[8][8], float (&q)[8][8]) {
-  const float apq = p[a][b];
-  if (apq == 0.0f) return;
-  const float tau = __fdiv_rn(__fsub_rn(p[b][b], p[a][a]), __fmul_rn(2.0f, apq));
+// ---------------------------------------------------------------------------
+// Pivot sweep: the 28 index pairs of an 8x8 pivot in the round-robin order of
+// 8 indices, 7 groups of 4 disjoint pairs, one rotation per pair with the
+// reference's angle formula (metal_mixed_sqrt.metal:1347-1357):
+// tau = (p_bb - p_aa) / (2 p_ab), t = sign(tau) / (|tau| + sqrt(1 + tau^2)),
+// c = 1 / sqrt(1 + t^2), s = t c; J = [c s; -s c] on (a, b): column
+// a' = c a - s b, column b' = s a + c b; p <- J^T p J, p_ab = p_ba = 0;
+// Q <- Q J.
+//
+// A quad of lanes sweeps one pivot.  In group g lane t owns the two rows
+// (a_t, b_t) of its pair.  The four angles of a group depend only on the
+// pair's own 2x2 block, which no other rotation of the group touches, so
+// they are computed at once and shared with shuffles; each lane then
+// updates its two rows.  Element (x, y) of a row pair t and column pair j is
+// touched by the row rotation of t and the column rotation of j, applied in
+// the order of the pairs in the group (the sequential order); the diagonal
+// block (j = t) takes the column rotation first.  Every operation is an
+// explicitly rounded one (no FMA contraction, no approximate reciprocal
+// square root), so the sweep equals, bit for bit, the sequential sweep of
+// the C restatement compiled with -ffp-contract=off.
+
+// Pairs of group g packed as 4 x (a: 3 bits, b: 3 bits), a < b.
+__host__ __device__ constexpr uint32_t groupWord(int g) {
+  constexpr int pairs[8][8] = {{0, 7, 1, 6, 2, 5, 3, 4}, {0, 6, 5, 7, 1, 4, 2, 3},
+                               {0, 5, 4, 6, 3, 7, 1, 2}, {0, 4, 3, 5, 2, 6, 1, 7},
+                               {0, 3, 2, 4, 1, 5, 6, 7}, {0, 2, 1, 3, 4, 7, 5, 6},
+                               {0, 1, 2, 7, 3, 6, 4, 5},
+                               // layout used to store the pivot: rows (t, 4 + t)
+                               {0, 4, 1, 5, 2, 6, 3, 7}};
+  uint32_t w = 0;
+  for (int t = 0; t < 4; ++t)
+    w |= static_cast<uint32_t>(pairs[g][2 * t] | (pairs[g][2 * t + 1] << 3)) << (6 * t);
+  return w;
+}
+
+// For each row r: owner lane (2 bits) and slot (1 bit, 1 = second row of
+// the pair) in group g, packed 3 bits per row.
+__host__ __device__ constexpr uint32_t ownerWord(int g) {
+  uint32_t w = 0;
+  for (int t = 0; t < 4; ++t) {
+    const uint32_t a = (groupWord(g) >> (6 * t)) & 7, b = (groupWord(g) >> (6 * t + 3)) & 7;
+    w |= static_cast<uint32_t>(t) << (3 * a);
+    w |= static_cast<uint32_t>(t | 4) << (3 * b);
+  }
+  return w;
+}
+
+__device__ __forceinline__ float pick8(const float (&r)[8], int i) {
+  float v = r[0];
+#pragma unroll
+  for (int k = 1; k < 8; ++k) v = i == k ? r[k] : v;
+  return v;
+}
+
+// Rotation angle of one pair (explicitly rounded; renormalised so that
+// c^2 + s^2 - 1, evaluated exactly with FMA two-products, is pulled back by
+// (1 - e/2): FP32 (c, s) otherwise carry a one-signed error in c^2 + s^2
+// that compounds over the thousands of rotations applied to each row of V).
+__device__ __forceinline__ bool jacobiAngle(float paa, float pbb, float pab, float &c, float &s) {
+  c = 1.0f;
+  s = 0.0f;
+  if (pab == 0.0f) return false;
+  const float tau = __fdiv_rn(__fsub_rn(pbb, paa), __fmul_rn(2.0f, pab));
   const float root = __fsqrt_rn(__fadd_rn(__fmul_rn(tau, tau), 1.0f));
   const float t = copysignf(__fdiv_rn(1.0f, __fadd_rn(fabsf(tau), root)), tau);
-  float c = __fdiv_rn(1.0f, __fsqrt_rn(__fadd_rn(__fmul_rn(t, t), 1.0f)));
-  float s = __fmul_rn(t, c);
-  // FP32 (c, s) carry a one-signed error in c^2 + s^2 - 1 that compounds
-  // over the thousands of rotations applied to each row of V.  Evaluate
-  // e = c^2 + s^2 - 1 exactly (two-product: each square split by an FMA;
-  // c^2 >= 1/2 so c^2 - 1 is exact) and pull (c, s) back by (1 - e/2): the
-  // rotation is then as orthogonal as one computed in FP64 and rounded.
-  {
-    const float cc = __fmul_rn(c, c), cce = fmaf(c, c, -cc);
-    const float ss = __fmul_rn(s, s), sse = fmaf(s, s, -ss);
-    const float e = __fadd_rn(__fadd_rn(__fsub_rn(cc, 1.0f), ss), __fadd_rn(cce, sse));
-    const float h = __fmul_rn(-0.5f, e);
-    c = fmaf(h, c, c);
-    s = fmaf(h, s, s);
+  float cc0 = __fdiv_rn(1.0f, __fsqrt_rn(__fadd_rn(__fmul_rn(t, t), 1.0f)));
+  float ss0 = __fmul_rn(t, cc0);
+  const float cc = __fmul_rn(cc0, cc0), cce = fmaf(cc0, cc0, -cc);
+  const float ss = __fmul_rn(ss0, ss0), sse = fmaf(ss0, ss0, -ss);
+  const float e = __fadd_rn(__fadd_rn(__fsub_rn(cc, 1.0f), ss), __fadd_rn(cce, sse));
+  const float h = __fmul_rn(-0.5f, e);
+  c = fmaf(h, cc0, cc0);
+  s = fmaf(h, ss0, ss0);
+  return true;
+}
+
+// x' = c x - s y, y' = s x + c y (explicitly rounded); identity if !on.
+__device__ __forceinline__ void rot2(float &x, float &y, float c, float s, bool on) {
+  const float nx = __fsub_rn(__fmul_rn(c, x), __fmul_rn(s, y));
+  const float ny = __fadd_rn(__fmul_rn(s, x), __fmul_rn(c, y));
+  x = on ? nx : x;
+  y = on ? ny : y;
+}
+
+// One group of 4 rotations on the quad.  ra / rb: this lane's rows a_t / b_t
+// (all 8 columns); qcol: the pivot's Q, column-major (column x at qcol[8x]).
+template <int G>
+__device__ __forceinline__ void pivotGroup(float (&ra)[8], float (&rb)[8], float *qcol, int t,
+                                           bool active) {
+  constexpr uint32_t W = groupWord(G);
+  const int a = (W >> (6 * t)) & 7, b = (W >> (6 * t + 3)) & 7;
+  float c, s;
+  const bool on = jacobiAngle(pick8(ra, a), pick8(rb, b), pick8(ra, b), c, s);
+  float cj[4], sj[4];
+  bool onj[4];
+#pragma unroll
+  for (int j = 0; j < 4; ++j) {
+    cj[j] = __shfl_sync(0xffffffffu, c, j, 4);
+    sj[j] = __shfl_sync(0xffffffffu, s, j, 4);
+    onj[j] = __shfl_sync(0xffffffffu, static_cast<int>(on), j, 4) != 0;
   }
 #pragma unroll
-  for (int i = 0; i < 8; ++i) {
-    const float pa = p[i][a], pb = p[i][b];
-    p[i][a] = __fsub_rn(__fmul_rn(c, pa), __fmul_rn(s, pb));
-    p[i][b] = __fadd_rn(__fmul_rn(s, pa), __fmul_rn(c, pb));
+  for (int j = 0; j < 4; ++j) {
+    const int A = (W >> (6 * j)) & 7, B = (W >> (6 * j + 3)) & 7;
+    // 2x2 block X: rows (a_t, b_t), columns (A, B) of pair j.  If j comes
+    // first in the group (or j = t) the column rotation precedes the row
+    // rotation: Y = (C_t(R_j(X^T)))^T, else Y = C_j(R_t(X)), where R mixes
+    // rows and C mixes columns with the same two-term arithmetic.
+    const bool swap = j <= t;
+    float x00 = ra[A], x01 = swap ? rb[A] : ra[B];
+    float x10 = swap ? ra[B] : rb[A], x11 = rb[B];
+    const float c1 = swap ? cj[j] : c, s1 = swap ? sj[j] : s;
+    const bool on1 = swap ? onj[j] : on;
+    const float c2 = swap ? c : cj[j], s2 = swap ? s : sj[j];
+    const bool on2 = swap ? on : onj[j];
+    rot2(x00, x10, c1, s1, on1);  // rows of X'
+    rot2(x01, x11, c1, s1, on1);
+    rot2(x00, x01, c2, s2, on2);  // columns of X'
+    rot2(x10, x11, c2, s2, on2);
+    const bool diag = j == t && on;
+    ra[A] = x00;
+    rb[B] = x11;
+    const float y01 = swap ? x10 : x01, y10 = swap ? x01 : x10;
+    ra[B] = diag ? 0.0f : y01;
+    rb[A] = diag ? 0.0f : y10;
+  }
+  if (active && on) {
+    float4 *ca = reinterpret_cast<float4 *>(qcol + 8 * a);
+    float4 *cb = reinterpret_cast<float4 *>(qcol + 8 * b);
+    float4 x0 = ca[0], x1 = ca[1], y0 = cb[0], y1 = cb[1];
+    rot2(x0.x, y0.x, c, s, true); rot2(x0.y, y0.y, c, s, true);
+    rot2(x0.z, y0.z, c, s, true); rot2(x0.w, y0.w, c, s, true);
+    rot2(x1.x, y1.x, c, s, true); rot2(x1.y, y1.y, c, s, true);
+    rot2(x1.z, y1.z, c, s, true); rot2(x1.w, y1.w, c, s, true);
+    ca[0] = x0; ca[1] = x1; cb[0] = y0; cb[1] = y1;
+  }
+  __syncwarp();
+}
+
+// Moves the rows from the ownership of group G to that of group G + 1.
+template <int G>
+__device__ __forceinline__ void pivotExchange(float (&ra)[8], float (&rb)[8], int t) {
+  constexpr uint32_t O = ownerWord(G), W1 = groupWord(G + 1);
+  const int a1 = (W1 >> (6 * t)) & 7, b1 = (W1 >> (6 * t + 3)) & 7;
+  const int src_a = (O >> (3 * a1)) & 3, slot_a = (O >> (3 * a1 + 2)) & 1;
+  const int src_b = (O >> (3 * b1)) & 3, slot_b = (O >> (3 * b1 + 2)) & 1;
+  float na[8], nb[8];
+#pragma unroll
+  for (int y = 0; y < 8; ++y) {
+    const float u0 = __shfl_sync(0xffffffffu, ra[y], src_a, 4);
+    const float u1 = __shfl_sync(0xffffffffu, rb[y], src_a, 4);
+    const float v0 = __shfl_sync(0xffffffffu, ra[y], src_b, 4);
+    const float v1 = __shfl_sync(0xffffffffu, rb[y], src_b, 4);
+    na[y] = slot_a ? u1 : u0;
+    nb[y] = slot_b ? v1 : v0;
   }
 #pragma unroll
-  for (int j = 0; j < 8; ++j) {
-    const float pa = p[a][j], pb = p[b][j];
-    p[a][j] = __fsub_rn(__fmul_rn(c, pa), __fmul_rn(s, pb));
-    p[b][j] = __fadd_rn(__fmul_rn(s, pa), __fmul_rn(c, pb));
-  }
-  p[a][b] = 0.0f;
-  p[b][a] = 0.0f;
-#pragma unroll
-  for (int i = 0; i < 8; ++i) {
-    const float qa = q[i][a], qb = q[i][b];
-    q[i][a] = __fsub_rn(__fmul_rn(c, qa), __fmul_rn(s, qb));
-    q[i][b] = __fadd_rn(__fmul_rn(s, qa), __fmul_rn(c, qb));
+  for (int y = 0; y < 8; ++y) {
+    ra[y] = na[y];
+    rb[y] = nb[y];
   }
 }
 
-// One cyclic sweep over the 28 pairs of the pivot in round-robin order
-// (7 rounds of 4 disjoint pairs; disjoint rotations commute).
-__device__ __forceinline__ void sweepPivot(float (&p)[8][8], float (&q)[8][8]) {
-  rotatePivot<0, 7>(p, q); rotatePivot<1, 6>(p, q); rotatePivot<2, 5>(p, q); rotatePivot<3, 4>(p, q);
-  rotatePivot<0, 6>(p, q); rotatePivot<5, 7>(p, q); rotatePivot<1, 4>(p, q); rotatePivot<2, 3>(p, q);
-  rotatePivot<0, 5>(p, q); rotatePivot<4, 6>(p, q); rotatePivot<3, 7>(p, q); rotatePivot<1, 2>(p, q);
-  rotatePivot<0, 4>(p, q); rotatePivot<3, 5>(p, q); rotatePivot<2, 6>(p, q); rotatePivot<1, 7>(p, q);
-  rotatePivot<0, 3>(p, q); rotatePivot<2, 4>(p, q); rotatePivot<1, 5>(p, q); rotatePivot<6, 7>(p, q);
-  rotatePivot<0, 2>(p, q); rotatePivot<1, 3>(p, q); rotatePivot<4, 7>(p, q); rotatePivot<5, 6>(p, q);
-  rotatePivot<0, 1>(p, q); rotatePivot<2, 7>(p, q); rotatePivot<3, 6>(p, q); rotatePivot<4, 5>(p, q);
+// Full pivot sweep on the quad; on return ra / rb hold rows (t, 4 + t) and
+// qcol holds Q row-major.
+__device__ __forceinline__ void pivotSweep(float (&ra)[8], float (&rb)[8], float *qcol, int t,
+                                           bool active) {
+  if (active) {
+    // Q = I, column-major: lane t writes columns 2t and 2t + 1.
+    float4 *q4 = reinterpret_cast<float4 *>(qcol);
+#pragma unroll
+    for (int x = 0; x < 2; ++x) {
+      const int col = 2 * t + x;
+      q4[2 * col] = make_float4(col == 0, col == 1, col == 2, col == 3);
+      q4[2 * col + 1] = make_float4(col == 4, col == 5, col == 6, col == 7);
+    }
+  }
+  __syncwarp();
+  pivotGroup<0>(ra, rb, qcol, t, active); pivotExchange<0>(ra, rb, t);
+  pivotGroup<1>(ra, rb, qcol, t, active); pivotExchange<1>(ra, rb, t);
+  pivotGroup<2>(ra, rb, qcol, t, active); pivotExchange<2>(ra, rb, t);
+  pivotGroup<3>(ra, rb, qcol, t, active); pivotExchange<3>(ra, rb, t);
+  pivotGroup<4>(ra, rb, qcol, t, active); pivotExchange<4>(ra, rb, t);
+  pivotGroup<5>(ra, rb, qcol, t, active); pivotExchange<5>(ra, rb, t);
+  pivotGroup<6>(ra, rb, qcol, t, active); pivotExchange<6>(ra, rb, t);
+  // Q column-major -> row-major in place: lane t gathers rows 2t, 2t + 1.
+  float2 r2[8];
+  if (active) {
+#pragma unroll
+    for (int col = 0; col < 8; ++col) r2[col] = reinterpret_cast<const float2 *>(qcol + 8 * col)[t];
+  }
+  __syncwarp();
+  if (active) {
+    float4 *q4 = reinterpret_cast<float4 *>(qcol);
+    q4[4 * t + 0] = make_float4(r2[0].x, r2[1].x, r2[2].x, r2[3].x);
+    q4[4 * t + 1] = make_float4(r2[4].x, r2[5].x, r2[6].x, r2[7].x);
+    q4[4 * t + 2] = make_float4(r2[0].y, r2[1].y, r2[2].y, r2[3].y);
+    q4[4 * t + 3] = make_float4(r2[4].y, r2[5].y, r2[6].y, r2[7].y);
+  }
 }
-
-struct SweepSmem {
-  double *red;
-  int *tri;
-  int *pair_i;
-  int *pair_j;
-  float *q;
-  float *tiles;
-};
 
 __host__ __device__ __forceinline__ size_t sweepSmemLayout(int n, bool with_tiles, size_t *q_off,
                                                            size_t *tile_off) {
@@ -355,128 +484,141 @@ jacobiSweepKernel(JacobiArgs args) {
   float *log = args.log + args.log_offset[mi];
   const int items = ((P + 1) / 2) * (P + 1);
   for (int round = 0; round < nb - 1; ++round) {
-    // Pivots: one thread per block pair sweeps its 8x8 pivot in registers.
-    for (int k = threadIdx.x; k < P; k += blockDim.x) {
-      int I, J;
-      rrPair(k, round, nb, I, J);
-      pair_i[k] = I;
-      pair_j[k] = J;
-      float p[8][8], q[8][8];
-      {
-        float t[4][4];
-        loadBlock(tiles, tri, I, I, t);
+    // Pivots: a quad of lanes per block pair.  The loop is warp-uniform (all
+    // lanes of a warp take part in the quad shuffles; lanes past P idle).
+    const int quads = blockDim.x >> 2, t4 = threadIdx.x & 3;
+    for (int base = 0; base < P; base += quads) {
+      const int k = base + (threadIdx.x >> 2);
+      const bool active = k < P;
+      float ra[8], rb[8];
+      int tII = 0, tIJ = 0, tJJ = 0;
+      if (active) {
+        int I, J;
+        rrPair(k, round, nb, I, J);
+        if (t4 == 0) {
+          pair_i[k] = I;
+          pair_j[k] = J;
+        }
+        tII = tileIndex(tri, I, I);
+        tIJ = tileIndex(tri, I, J);
+        tJJ = tileIndex(tri, J, J);
+        // lane t starts with rows t (block I) and 7 - t (block J row 3 - t;
+        // its left half is the mirror of tile (I, J))
+        const float4 *sII = reinterpret_cast<const float4 *>(tiles + static_cast<int64_t>(tII) * kTileF);
+        const float4 *sIJ = reinterpret_cast<const float4 *>(tiles + static_cast<int64_t>(tIJ) * kTileF);
+        const float4 *sJJ = reinterpret_cast<const float4 *>(tiles + static_cast<int64_t>(tJJ) * kTileF);
+        const int jr = 3 - t4;
+        const float4 v0 = sII[t4 ^ (tII & 3)], v1 = sIJ[t4 ^ (tIJ & 3)], v2 = sJJ[jr ^ (tJJ & 3)];
+        ra[0] = v0.x; ra[1] = v0.y; ra[2] = v0.z; ra[3] = v0.w;
+        ra[4] = v1.x; ra[5] = v1.y; ra[6] = v1.z; ra[7] = v1.w;
 #pragma unroll
-        for (int i = 0; i < 4; ++i)
+        for (int i = 0; i < 4; ++i) rb[i] = tiles[tileElement(tIJ, i, jr)];
+        rb[4] = v2.x; rb[5] = v2.y; rb[6] = v2.z; rb[7] = v2.w;
+      } else {
 #pragma unroll
-          for (int j = 0; j < 4; ++j) p[i][j] = t[i][j];
-        loadBlock(tiles, tri, I, J, t);
-#pragma unroll
-        for (int i = 0; i < 4; ++i)
-#pragma unroll
-          for (int j = 0; j < 4; ++j) {
-            p[i][4 + j] = t[i][j];
-            p[4 + j][i] = t[i][j];
-          }
-        loadBlock(tiles, tri, J, J, t);
-#pragma unroll
-        for (int i = 0; i < 4; ++i)
-#pragma unroll
-          for (int j = 0; j < 4; ++j) p[4 + i][4 + j] = t[i][j];
+        for (int y = 0; y < 8; ++y) ra[y] = rb[y] = 0.0f;
       }
-#pragma unroll
-      for (int i = 0; i < 8; ++i)
-#pragma unroll
-        for (int j = 0; j < 8; ++j) q[i][j] = i == j ? 1.0f : 0.0f;
-      sweepPivot(p, q);
-      {
-        float t[4][4];
-#pragma unroll
-        for (int i = 0; i < 4; ++i)
-#pragma unroll
-          for (int j = 0; j < 4; ++j) t[i][j] = p[i][j];
-        storeBlock(tiles, tri, I, I, t);
-#pragma unroll
-        for (int i = 0; i < 4; ++i)
-#pragma unroll
-          for (int j = 0; j < 4; ++j) t[i][j] = p[i][4 + j];
-        storeBlock(tiles, tri, I, J, t);
-#pragma unroll
-        for (int i = 0; i < 4; ++i)
-#pragma unroll
-          for (int j = 0; j < 4; ++j) t[i][j] = p[4 + i][4 + j];
-        storeBlock(tiles, tri, J, J, t);
-      }
-      float4 *qdst = reinterpret_cast<float4 *>(qs + k * kQF);
-      float4 *ldst = reinterpret_cast<float4 *>(log + (static_cast<int64_t>(round) * P + k) * kQF);
-#pragma unroll
-      for (int i = 0; i < 8; ++i) {
-        const float4 lo = make_float4(q[i][0], q[i][1], q[i][2], q[i][3]);
-        const float4 hi = make_float4(q[i][4], q[i][5], q[i][6], q[i][7]);
-        qdst[2 * i] = lo;
-        qdst[2 * i + 1] = hi;
-        ldst[2 * i] = lo;
-        ldst[2 * i + 1] = hi;
+      pivotSweep(ra, rb, qs + (active ? k : 0) * kQF, t4, active);
+      if (active) {
+        // rows t (tiles (I, I), (I, J)) and 4 + t (tile (J, J)); the lower
+        // left block is the mirror of tile (I, J) and is not stored
+        float4 *sII = reinterpret_cast<float4 *>(tiles + static_cast<int64_t>(tII) * kTileF);
+        float4 *sIJ = reinterpret_cast<float4 *>(tiles + static_cast<int64_t>(tIJ) * kTileF);
+        float4 *sJJ = reinterpret_cast<float4 *>(tiles + static_cast<int64_t>(tJJ) * kTileF);
+        sII[t4 ^ (tII & 3)] = make_float4(ra[0], ra[1], ra[2], ra[3]);
+        sIJ[t4 ^ (tIJ & 3)] = make_float4(ra[4], ra[5], ra[6], ra[7]);
+        sJJ[t4 ^ (tJJ & 3)] = make_float4(rb[4], rb[5], rb[6], rb[7]);
       }
     }
     __syncthreads();
-    // Off-pivot super-tiles: T' = Q_k^T T Q_l for every k < l.
-    for (int w = threadIdx.x; w < items; w += blockDim.x) {
-      int k, l;
-      if (!foldedBlock(w, P, k, l) || k == l) continue;
-      const int rb[2] = {pair_i[k], pair_j[k]};
-      const int cb[2] = {pair_i[l], pair_j[l]};
-      float t[8][8];
-#pragma unroll
-      for (int x = 0; x < 2; ++x)
-#pragma unroll
-        for (int y = 0; y < 2; ++y) {
-          float b4[4][4];
-          loadBlock(tiles, tri, rb[x], cb[y], b4);
-#pragma unroll
-          for (int i = 0; i < 4; ++i)
-#pragma unroll
-            for (int j = 0; j < 4; ++j) t[4 * x + i][4 * y + j] = b4[i][j];
-        }
-      float u[8][8];
-#pragma unroll
-      for (int a = 0; a < 8; ++a)
-#pragma unroll
-        for (int c = 0; c < 8; ++c) u[a][c] = 0.0f;
+    {
+      // this round's rotations, logged for the V replay (coalesced copy)
+      const float4 *src = reinterpret_cast<const float4 *>(qs);
+      float4 *dst = reinterpret_cast<float4 *>(log + static_cast<int64_t>(round) * P * kQF);
+      for (int x = threadIdx.x; x < P * kQF / 4; x += blockDim.x) dst[x] = src[x];
+    }
+    // Off-pivot super-tiles: T' = Q_k^T T Q_l for every k < l, two lanes per
+    // super-tile.  Lane h forms U[:, 4h:4h+4] = Q_k^T T[:, 4h:4h+4] from the
+    // two 4x4 blocks of column block h, the pair swaps the halves of U each
+    // needs, and lane h forms rows 4h..4h+3 of T' = U Q_l.  Every element is
+    // the same ordered FMA chain as in one-lane form (u over i, t' over j).
+    // The loop is warp-uniform so the pair shuffle has all lanes present.
+    for (int base = threadIdx.x & ~31; base < 2 * items; base += blockDim.x) {
+      const int w2 = base + (threadIdx.x & 31);
+      const int h = w2 & 1;
+      int k = 0, l = 0;
+      const bool valid = w2 < 2 * items && foldedBlock(w2 >> 1, P, k, l) && k != l;
+      if (!valid) k = l = 0;
+      const int rb0 = pair_i[k], rb1 = pair_j[k];
+      const int cbh = h ? pair_j[l] : pair_i[l];
       const float4 *qk = reinterpret_cast<const float4 *>(qs + k * kQF);
-#pragma unroll
-      for (int i = 0; i < 8; ++i) {
-        const float4 lo = qk[2 * i], hi = qk[2 * i + 1];
-        const float qr[8] = {lo.x, lo.y, lo.z, lo.w, hi.x, hi.y, hi.z, hi.w};
-#pragma unroll
-        for (int a = 0; a < 8; ++a)
-#pragma unroll
-          for (int c = 0; c < 8; ++c) u[a][c] = fmaf(qr[a], t[i][c], u[a][c]);
-      }
       const float4 *ql = reinterpret_cast<const float4 *>(qs + l * kQF);
+      float u[8][4];
 #pragma unroll
       for (int a = 0; a < 8; ++a)
 #pragma unroll
-        for (int c = 0; c < 8; ++c) t[a][c] = 0.0f;
+        for (int c = 0; c < 4; ++c) u[a][c] = 0.0f;
 #pragma unroll
-      for (int j = 0; j < 8; ++j) {
-        const float4 lo = ql[2 * j], hi = ql[2 * j + 1];
+      for (int x = 0; x < 2; ++x) {
+        float b4[4][4];
+        if (valid) {
+          loadBlock(tiles, tri, x ? rb1 : rb0, cbh, b4);
+        } else {
+#pragma unroll
+          for (int i = 0; i < 4; ++i)
+#pragma unroll
+            for (int c = 0; c < 4; ++c) b4[i][c] = 0.0f;
+        }
+#pragma unroll
+        for (int i = 0; i < 4; ++i) {
+          const float4 lo = qk[2 * (4 * x + i)], hi = qk[2 * (4 * x + i) + 1];
+          const float qr[8] = {lo.x, lo.y, lo.z, lo.w, hi.x, hi.y, hi.z, hi.w};
+#pragma unroll
+          for (int a = 0; a < 8; ++a)
+#pragma unroll
+            for (int c = 0; c < 4; ++c) u[a][c] = fmaf(qr[a], b4[i][c], u[a][c]);
+        }
+      }
+      // U rows of this lane's half: own columns, and the partner's columns
+      // for these rows (the partner sends the rows of the other half).
+      float ur[4][8];
+#pragma unroll
+      for (int r = 0; r < 4; ++r)
+#pragma unroll
+        for (int c = 0; c < 4; ++c) {
+          const float mine = h ? u[4 + r][c] : u[r][c];
+          const float send = h ? u[r][c] : u[4 + r][c];
+          const float got = __shfl_xor_sync(0xffffffffu, send, 1);
+          ur[r][c] = h ? got : mine;
+          ur[r][4 + c] = h ? mine : got;
+        }
+      float o[4][8];
+#pragma unroll
+      for (int r = 0; r < 4; ++r)
+#pragma unroll
+        for (int c = 0; c < 8; ++c) o[r][c] = 0.0f;
+#pragma unroll
+      for (int jj = 0; jj < 8; ++jj) {
+        const float4 lo = ql[2 * jj], hi = ql[2 * jj + 1];
         const float qr[8] = {lo.x, lo.y, lo.z, lo.w, hi.x, hi.y, hi.z, hi.w};
 #pragma unroll
-        for (int a = 0; a < 8; ++a)
+        for (int r = 0; r < 4; ++r)
 #pragma unroll
-          for (int c = 0; c < 8; ++c) t[a][c] = fmaf(u[a][j], qr[c], t[a][c]);
+          for (int c = 0; c < 8; ++c) o[r][c] = fmaf(ur[r][jj], qr[c], o[r][c]);
       }
-#pragma unroll
-      for (int x = 0; x < 2; ++x)
+      if (valid) {
+        const int rbh = h ? rb1 : rb0;
+        const int cb0 = pair_i[l], cb1 = pair_j[l];
 #pragma unroll
         for (int y = 0; y < 2; ++y) {
           float b4[4][4];
 #pragma unroll
-          for (int i = 0; i < 4; ++i)
+          for (int r = 0; r < 4; ++r)
 #pragma unroll
-            for (int j = 0; j < 4; ++j) b4[i][j] = t[4 * x + i][4 * y + j];
-          storeBlock(tiles, tri, rb[x], cb[y], b4);
+            for (int c = 0; c < 4; ++c) b4[r][c] = o[r][4 * y + c];
+          storeBlock(tiles, tri, rbh, y ? cb1 : cb0, b4);
         }
+      }
     }
     __syncthreads();
   }
@@ -515,8 +657,11 @@ __host__ __device__ __forceinline__ size_t replaySmemBytes(int max_n, int rows) 
 // Replays one logged sweep onto `rows` rows of V: V <- V Q_k on the column
 // blocks (I_k, J_k) of every pair, round by round (the V update of
 // jacobi_similarity_vectors_f32 z = 1, metal_mixed_sqrt.metal:1380-1390,
-// with 8x8 rotations).  A thread applies one Q_k (held in registers) to 8
-// rows.
+// with 8x8 rotations).  Rows are the fast thread index: the 32 lanes of a
+// warp update 32 rows with the same Q_k, so Q_k is read from shared memory
+// as a broadcast, and the row stride (m + 4 floats, 4 mod 8) keeps the
+// lanes' float4 row accesses free of bank conflicts.  Each element is the
+// ordered chain o_c = sum_j x_j q_jc in FP32 FMA, as the CPU restatement.
 __global__ void __launch_bounds__(kReplayThreads)
 jacobiReplayKernel(VArgs args) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -535,41 +680,39 @@ jacobiReplayKernel(VArgs args) {
     vs[r * ld + c] = (c < n && r < rows) ? v[r0 + r + static_cast<int64_t>(c) * n] : 0.0f;
   }
   const float *log = args.log + args.log_offset[mi];
-  const int groups = R / 8;
+  const int lanes_r = R < 32 ? R : 32;  // rows per warp slice
   for (int round = 0; round < nb - 1; ++round) {
     __syncthreads();
     const float4 *src = reinterpret_cast<const float4 *>(log + static_cast<int64_t>(round) * P * kQF);
     for (int k = threadIdx.x; k < P * kQF / 4; k += blockDim.x) reinterpret_cast<float4 *>(qs)[k] = src[k];
     __syncthreads();
-    for (int item = threadIdx.x; item < P * groups; item += blockDim.x) {
-      const int k = item % P, g = item / P;
+    for (int item = threadIdx.x; item < P * R; item += blockDim.x) {
+      // item -> (pair k, row r) with r fastest inside a warp slice
+      const int slice = item / lanes_r, r_in = item % lanes_r;
+      const int slices_per_k = R / lanes_r;
+      const int k = slice / slices_per_k;
+      const int r = (slice % slices_per_k) * lanes_r + r_in;
+      if (r >= rows) continue;
       int I, J;
       rrPair(k, round, nb, I, J);
-      float q[8][8];
       const float4 *qk = reinterpret_cast<const float4 *>(qs + k * kQF);
+      float *row = vs + r * ld;
+      const float4 a = *reinterpret_cast<const float4 *>(row + 4 * I);
+      const float4 b = *reinterpret_cast<const float4 *>(row + 4 * J);
+      const float x[8] = {a.x, a.y, a.z, a.w, b.x, b.y, b.z, b.w};
+      float o[8];
 #pragma unroll
-      for (int i = 0; i < 8; ++i) {
-        const float4 lo = qk[2 * i], hi = qk[2 * i + 1];
-        q[i][0] = lo.x; q[i][1] = lo.y; q[i][2] = lo.z; q[i][3] = lo.w;
-        q[i][4] = hi.x; q[i][5] = hi.y; q[i][6] = hi.z; q[i][7] = hi.w;
+      for (int c = 0; c < 8; ++c) o[c] = 0.0f;
+#pragma unroll
+      for (int j = 0; j < 8; ++j) {
+        const float4 lo = qk[2 * j], hi = qk[2 * j + 1];
+        o[0] = fmaf(x[j], lo.x, o[0]); o[1] = fmaf(x[j], lo.y, o[1]);
+        o[2] = fmaf(x[j], lo.z, o[2]); o[3] = fmaf(x[j], lo.w, o[3]);
+        o[4] = fmaf(x[j], hi.x, o[4]); o[5] = fmaf(x[j], hi.y, o[5]);
+        o[6] = fmaf(x[j], hi.z, o[6]); o[7] = fmaf(x[j], hi.w, o[7]);
       }
-#pragma unroll 2
-      for (int rr = 0; rr < 8; ++rr) {
-        float *row = vs + (g * 8 + rr) * ld;
-        const float4 a = *reinterpret_cast<const float4 *>(row + 4 * I);
-        const float4 b = *reinterpret_cast<const float4 *>(row + 4 * J);
-        const float x[8] = {a.x, a.y, a.z, a.w, b.x, b.y, b.z, b.w};
-        float o[8];
-#pragma unroll
-        for (int c = 0; c < 8; ++c) {
-          float s = 0.0f;
-#pragma unroll
-          for (int j = 0; j < 8; ++j) s = fmaf(x[j], q[j][c], s);
-          o[c] = s;
-        }
-        *reinterpret_cast<float4 *>(row + 4 * I) = make_float4(o[0], o[1], o[2], o[3]);
-        *reinterpret_cast<float4 *>(row + 4 * J) = make_float4(o[4], o[5], o[6], o[7]);
-      }
+      *reinterpret_cast<float4 *>(row + 4 * I) = make_float4(o[0], o[1], o[2], o[3]);
+      *reinterpret_cast<float4 *>(row + 4 * J) = make_float4(o[4], o[5], o[6], o[7]);
     }
   }
   __syncthreads();
@@ -599,10 +742,13 @@ __global__ void jacobiReportKernel(const JacobiState *state, int count, int32_t 
   }
 }
 
+// Threads of a sweep CTA: a quad per pivot and two lanes per super-tile
+// (the kernel fits 128 registers, so 512 threads is one CTA per SM).
 int threadsFor(int n) {
   if (n <= 16) return 32;
   if (n <= 32) return 64;
   if (n <= 64) return 128;
+  if (n <= 256) return 256;
   return kSweepThreadsMax;
 }
 
