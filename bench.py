@@ -37,6 +37,32 @@ COUNT = 4096
 N_LO, N_HI = 16, 512
 
 
+PROFILE_STEPS = 1  # serialized step whose per-kernel times give the roofline
+
+# Size classes of the Jacobi sweep launches (the library's launch names).
+SWEEP_CLASS_NAMES = ["jacobi sweep n<=16", "jacobi sweep n<=32", "jacobi sweep n<=64",
+                     "jacobi sweep n<=128", "jacobi sweep n<=256", "jacobi sweep n<=328",
+                     "jacobi sweep n<=512 (global)", "jacobi sweep n<=1024 (global)",
+                     "jacobi sweep n<=2048 (global)"]
+
+
+def _tiles_fit_shared(n: int) -> bool:
+    """The sweep keeps the packed tiles in shared memory when they fit 227 KB."""
+    m = (n + 7) // 8 * 8
+    nb, p = m // 4, m // 8
+    head = (32 * 8 + (nb + 1 + 2 * p) * 4 + 15) // 16 * 16
+    return head + p * 68 * 4 + nb * (nb + 1) // 2 * 16 * 4 <= 227 * 1024
+
+
+def sweep_class(n: int) -> int:
+    for c, hi in enumerate((16, 32, 64, 128, 256)):
+        if n <= hi:
+            return c
+    if _tiles_fit_shared(n):
+        return 5
+    return 6 if n <= 512 else (7 if n <= 1024 else 8)
+
+
 def workload_orders(count: int, seed: int) -> np.ndarray:
     rng = np.random.default_rng(seed)
     n = np.floor(np.exp(rng.uniform(np.log(N_LO), np.log(N_HI + 1), count))).astype(np.int32)
@@ -341,7 +367,12 @@ def main():
     ms_plain, acc_plain, _, res_plain, _ = timed(fp32_plan, max(1, args.steps // 2), 1)
     # low-bit + Sylvester path (headline), clocks sampled while it runs
     with ClockSampler(local) as clocks:
-        ms, acc, launches, res, rows = timed(low_plan, args.steps, args.warmup, True)
+        ms, acc, launches, res, _ = timed(low_plan, args.steps, args.warmup, False)
+    # per-kernel times from one more step with every launch on one stream
+    # (outside the timed region: concurrent launches would share the GPU)
+    ctx.set_concurrency(False)
+    _, _, _, _, rows = timed(low_plan, PROFILE_STEPS, 0, True)
+    ctx.set_concurrency(True)
     # max over ranks
     t = torch.tensor([ms], device=device)
     if world > 1:
@@ -413,14 +444,16 @@ def main():
     fp32_peak = 152 * 128 * 2 * sm_mhz * 1e6 / 1e12  # TFLOP/s
     if name.startswith("jacobi sweep") or name.startswith("jacobi replay"):
         if name.startswith("jacobi sweep"):
-            fma = (nb64 - 1) * p64 * (p64 - 1) / 2.0 * 1024.0
-            hbm_bytes = 4.0 * 2.0 * m64 * m64 / 2.0  # packed tiles read + written (global path)
+            # the sweep launches are named by size class: count only that class
+            in_class = np.array([SWEEP_CLASS_NAMES[sweep_class(int(n))] == name for n in orders])
+            fma = (nb64 - 1) * p64 * (p64 - 1) / 2.0 * 1024.0 * in_class
+            hbm_bytes = 4.0 * 2.0 * m64 * m64 / 2.0 * in_class  # packed tiles read + written
         else:
             fma = (nb64 - 1) * n64 * p64 * 64.0
             hbm_bytes = 8.0 * n64 * n64  # V read + written once per sweep
-        per_launch = float(np.sum(2.0 * fma * sweeps)) * args.steps / max(cnt, 1)
+        per_launch = float(np.sum(2.0 * fma * sweeps)) * PROFILE_STEPS / max(cnt, 1)
         achieved = per_launch / (avg_ms / 1e3) / 1e12
-        hbm_launch = float(np.sum(hbm_bytes * sweeps)) * args.steps / max(cnt, 1)
+        hbm_launch = float(np.sum(hbm_bytes * sweeps)) * PROFILE_STEPS / max(cnt, 1)
         roof = {"bound": "fp32", "achieved": achieved, "peak": fp32_peak, "unit": "TFLOP/s",
                 "frac": achieved / fp32_peak, "traffic": None, "kernel": name,
                 "peak_source": "nominal FP32 FMA rate: 152 SMs x 128 lanes x 2 flop x %.0f MHz "
@@ -428,7 +461,7 @@ def main():
                 "hbm_view": {"achieved": hbm_launch / (avg_ms / 1e3) / 1e9, "peak": hbm,
                              "unit": "GB/s", "frac": hbm_launch / (avg_ms / 1e3) / 1e9 / hbm}}
     else:
-        flops = float(np.sum(2.0 * n64 ** 3))
+        flops = float(np.sum(2.0 * n64 ** 3)) * PROFILE_STEPS / max(cnt, 1)
         achieved = flops / (avg_ms / 1e3) / 1e12
         roof = {"bound": "tensor", "achieved": achieved, "peak": bf16, "unit": "TFLOP/s",
                 "frac": achieved / bf16, "traffic": None, "kernel": name,
@@ -466,6 +499,8 @@ def main():
                           "residual_p99": float(np.percentile(resid, 99)),
                           "sample": len(idx)},
         "kernels": {k: {"launches": v[0], "ms": v[1], "share": v[1] / total_ms} for k, v in rows.items()},
+        "kernels_source": "launch timer over one extra step with concurrency off (serial)",
+        "autotune": [l for l in ctx.autotune_report().splitlines() if l],
     }
     print(json.dumps(line), flush=True)
     if world > 1:

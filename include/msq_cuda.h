@@ -63,14 +63,22 @@ void msq_destroy(msq_ctx *ctx);
 const char *msq_last_error(const msq_ctx *ctx);
 /* `stream` is a cudaStream_t (NULL = legacy default stream). */
 int msq_set_stream(msq_ctx *ctx, void *stream);
+/* Concurrency inside a call (default on): the Jacobi forks its size buckets
+ * and its V replay onto internal streams that join back into the context's
+ * stream before the call's later work.  enable = 0 keeps every launch on the
+ * context's stream, in serial order (same results, bit for bit).          */
+int msq_set_concurrency(msq_ctx *ctx, int enable);
 int msq_synchronize(msq_ctx *ctx);
 /* Number of this library's kernel launches enqueued so far on `ctx`. */
 uint64_t msq_launch_count(const msq_ctx *ctx);
 /* Launch timing for profiling: between begin and end, an event is recorded
- * on the context's stream after every launch; end synchronises and writes one
- * line per kernel name, "name<TAB>launches<TAB>total_ms", into `out`.  The
- * duration of a launch is the gap to the previous event, so stream-ordered
- * copies issued between launches count toward the next launch. */
+ * on the context's stream after every launch (launches on internal streams
+ * get a begin and an end event); end synchronises and writes one line per
+ * kernel name, "name<TAB>launches<TAB>total_ms", into `out`.  The duration
+ * of a launch on the context's stream is the gap to the previous event, so
+ * stream-ordered copies issued between launches count toward the next
+ * launch; concurrent launches share the GPU, so for per-kernel costs time
+ * with concurrency off. */
 int msq_timing_begin(msq_ctx *ctx);
 int msq_timing_end(msq_ctx *ctx, char *out, size_t capacity);
 
@@ -114,6 +122,18 @@ int msq_jacobi_batched(msq_ctx *ctx, float *matrices, float *vectors,
                        float *eigenvalues, const int32_t *n,
                        const int64_t *offset, int count, double tolerance,
                        int max_sweeps, int32_t *sweeps_done, float *off_ratio);
+
+/* ---- launch-shape autotuner -------------------------------------------------
+ * The Jacobi sweep buckets matrices by size class and picks each class's CTA
+ * size online: while a class is untuned, its first sweeps of a call try each
+ * candidate (all candidates compute identical bits) under timing events, and
+ * a later call keeps the fastest for that device.  Decisions are
+ * process-wide.  msq_autotune_report writes one line per class (candidates,
+ * measured ms per matrix-sweep, choice) for `device`; msq_autotune_reset
+ * forgets all decisions and, with enable = 0, turns tuning off (classes then
+ * use their default shapes).                                               */
+int msq_autotune_report(int device, char *out, size_t capacity);
+int msq_autotune_reset(int enable);
 
 /* ---- Jacobi without allocation ----------------------------------------------
  * No counterpart in the reference.  For callers that must not allocate

@@ -76,6 +76,9 @@ _SIGS = {
                                           ctypes.c_double, ctypes.c_int, _P, _P]),
     "msq_jacobi_noalloc": (ctypes.c_int, [_P, _P, _P, ctypes.c_int, ctypes.c_double,
                                           ctypes.c_int, _P, _P, _P]),
+    "msq_set_concurrency": (ctypes.c_int, [_P, ctypes.c_int]),
+    "msq_autotune_report": (ctypes.c_int, [ctypes.c_int, ctypes.c_char_p, ctypes.c_size_t]),
+    "msq_autotune_reset": (ctypes.c_int, [ctypes.c_int]),
     "msq_timing_begin": (ctypes.c_int, [_P]),
     "msq_timing_end": (ctypes.c_int, [_P, ctypes.c_char_p, ctypes.c_size_t]),
     "msq_make_factor": (ctypes.c_int, [_P, _P, _P, _P, _P, ctypes.c_int, _P]),
@@ -200,12 +203,21 @@ class Context:
         self.check(lib().msq_set_stream(self.handle, ctypes.c_void_p(stream.cuda_stream)),
                    "msq_set_stream")
 
+    def set_concurrency(self, enable: bool) -> None:
+        self.check(lib().msq_set_concurrency(self.handle, int(bool(enable))), "msq_set_concurrency")
+
     def synchronize(self) -> None:
         self.check(lib().msq_synchronize(self.handle), "msq_synchronize")
 
     @property
     def launches(self) -> int:
         return int(lib().msq_launch_count(self.handle))
+
+    def autotune_report(self) -> str:
+        """The launch-shape autotuner's decisions for this context's device."""
+        buf = ctypes.create_string_buffer(4096)
+        self.check(lib().msq_autotune_report(self.device, buf, len(buf)), "msq_autotune_report")
+        return buf.value.decode()
 
     # ---- codecs -------------------------------------------------------
     def copy_to_storage(self, fmt: int, source, row_length: int = 0):

@@ -52,12 +52,14 @@ int launched(msq_ctx *ctx, const char *what) {
 }
 
 void launchBegin(msq_ctx *ctx, cudaStream_t stream) {
-  if (!ctx->timing) return;
+  // a launch on the context's stream is timed by the event chain instead
+  if (!ctx->timing || stream == ctx->stream) return;
   ctx->pending_begin = takeEvent(ctx);
   cudaEventRecord(ctx->pending_begin, stream);
 }
 
 int launchedOn(msq_ctx *ctx, cudaStream_t stream, const char *what) {
+  if (stream == ctx->stream) return launched(ctx, what);
   ++ctx->launches;
   const int status = cudaCheck(ctx, cudaGetLastError(), what);
   if (ctx->timing && ctx->pending_begin != nullptr) {
@@ -261,6 +263,12 @@ extern "C" const char *msq_last_error(const msq_ctx *ctx) {
 extern "C" int msq_set_stream(msq_ctx *ctx, void *stream) {
   if (ctx == nullptr) return MSQ_ERR_INVALID_ARGUMENT;
   ctx->stream = static_cast<cudaStream_t>(stream);
+  return MSQ_OK;
+}
+
+extern "C" int msq_set_concurrency(msq_ctx *ctx, int enable) {
+  if (ctx == nullptr) return MSQ_ERR_INVALID_ARGUMENT;
+  ctx->concurrent = enable != 0;
   return MSQ_OK;
 }
 

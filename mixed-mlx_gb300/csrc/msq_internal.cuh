@@ -78,6 +78,9 @@ struct msq_ctx {
   // Auxiliary streams (non-blocking, created on first use) that fork from and
   // join back into `stream` through events from sync_pool.
   cudaStream_t aux[4] = {nullptr, nullptr, nullptr, nullptr};
+  // false: every launch on `stream` (serial order; per-kernel timings are
+  // then each kernel's own duration, not shared with concurrent work)
+  bool concurrent = true;
   std::vector<cudaEvent_t> sync_pool;
   size_t sync_next = 0;
 };

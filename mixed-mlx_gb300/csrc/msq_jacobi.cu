@@ -31,6 +31,12 @@
 #include "msq_internal.cuh"
 
 #include <algorithm>
+#include <array>
+#include <cstdio>
+#include <cstring>
+#include <map>
+#include <mutex>
+#include <string>
 #include <vector>
 
 namespace msq {
@@ -38,6 +44,10 @@ namespace {
 
 constexpr int kTileF = 16;      // floats per 4x4 tile
 constexpr int kQF = 64;         // floats per 8x8 rotation
+// Shared-memory stride of the rotations in the sweep kernel: 68 floats puts
+// Q_l of different pivots on different banks (a 64-float stride would map
+// every Q_l row to the same four banks).
+constexpr int kQS = 68;
 constexpr size_t kSmemLimit = 227 * 1024;
 constexpr int kMaxOrder = 2048;
 constexpr int kSweepThreadsMax = 512;
@@ -380,7 +390,7 @@ __host__ __device__ __forceinline__ size_t sweepSmemLayout(int n, bool with_tile
   size_t bytes = 32 * sizeof(double) + (nb + 1 + 2 * P) * sizeof(int);
   bytes = (bytes + 15) & ~static_cast<size_t>(15);
   *q_off = bytes;
-  bytes += static_cast<size_t>(P) * kQF * sizeof(float);
+  bytes += static_cast<size_t>(P) * kQS * sizeof(float);
   *tile_off = bytes;
   if (with_tiles) bytes += static_cast<size_t>(nb) * (nb + 1) / 2 * kTileF * sizeof(float);
   return bytes;
@@ -518,7 +528,7 @@ jacobiSweepKernel(JacobiArgs args) {
 #pragma unroll
         for (int y = 0; y < 8; ++y) ra[y] = rb[y] = 0.0f;
       }
-      pivotSweep(ra, rb, qs + (active ? k : 0) * kQF, t4, active);
+      pivotSweep(ra, rb, qs + (active ? k : 0) * kQS, t4, active);
       if (active) {
         // rows t (tiles (I, I), (I, J)) and 4 + t (tile (J, J)); the lower
         // left block is the mirror of tile (I, J) and is not stored
@@ -535,7 +545,9 @@ jacobiSweepKernel(JacobiArgs args) {
       // this round's rotations, logged for the V replay (coalesced copy)
       const float4 *src = reinterpret_cast<const float4 *>(qs);
       float4 *dst = reinterpret_cast<float4 *>(log + static_cast<int64_t>(round) * P * kQF);
-      for (int x = threadIdx.x; x < P * kQF / 4; x += blockDim.x) dst[x] = src[x];
+      for (int x = threadIdx.x; x < P * kQF / 4; x += blockDim.x) {
+        dst[x] = src[(x >> 4) * (kQS / 4) + (x & 15)];
+      }
     }
     // Off-pivot super-tiles: T' = Q_k^T T Q_l for every k < l, two lanes per
     // super-tile.  Lane h forms U[:, 4h:4h+4] = Q_k^T T[:, 4h:4h+4] from the
@@ -551,8 +563,8 @@ jacobiSweepKernel(JacobiArgs args) {
       if (!valid) k = l = 0;
       const int rb0 = pair_i[k], rb1 = pair_j[k];
       const int cbh = h ? pair_j[l] : pair_i[l];
-      const float4 *qk = reinterpret_cast<const float4 *>(qs + k * kQF);
-      const float4 *ql = reinterpret_cast<const float4 *>(qs + l * kQF);
+      const float4 *qk = reinterpret_cast<const float4 *>(qs + k * kQS);
+      const float4 *ql = reinterpret_cast<const float4 *>(qs + l * kQS);
       float u[8][4];
 #pragma unroll
       for (int a = 0; a < 8; ++a)
@@ -649,10 +661,21 @@ struct VArgs {
   int parity;                  // log buffer to replay (log points at it)
 };
 
+// Replay shared memory: `rows` rows of V (stride m + 4) and two rounds of
+// rotations (the next round's are copied in while the current one runs).
 __host__ __device__ __forceinline__ size_t replaySmemBytes(int max_n, int rows) {
   const int m = padded8(max_n), P = m / 8;
-  return static_cast<size_t>(rows) * (m + 4) * sizeof(float) + static_cast<size_t>(P) * kQF * sizeof(float);
+  return static_cast<size_t>(rows) * (m + 4) * sizeof(float) +
+         2 * static_cast<size_t>(P) * kQF * sizeof(float);
 }
+
+// 16-byte asynchronous global -> shared copies (cp.async, L2 only).
+__device__ __forceinline__ void copyAsync16(void *smem, const void *gmem) {
+  const unsigned dst = static_cast<unsigned>(__cvta_generic_to_shared(smem));
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(dst), "l"(gmem) : "memory");
+}
+__device__ __forceinline__ void copyAsyncCommit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+__device__ __forceinline__ void copyAsyncWaitAll() { asm volatile("cp.async.wait_group 0;\n" ::: "memory"); }
 
 // Replays one logged sweep onto `rows` rows of V: V <- V Q_k on the column
 // blocks (I_k, J_k) of every pair, round by round (the V update of
@@ -660,8 +683,10 @@ __host__ __device__ __forceinline__ size_t replaySmemBytes(int max_n, int rows) 
 // with 8x8 rotations).  Rows are the fast thread index: the 32 lanes of a
 // warp update 32 rows with the same Q_k, so Q_k is read from shared memory
 // as a broadcast, and the row stride (m + 4 floats, 4 mod 8) keeps the
-// lanes' float4 row accesses free of bank conflicts.  Each element is the
-// ordered chain o_c = sum_j x_j q_jc in FP32 FMA, as the CPU restatement.
+// lanes' float4 row accesses free of bank conflicts.  The next round's
+// rotations are copied from the log with cp.async while the current round
+// runs, so a round costs one barrier.  Each element is the ordered chain
+// o_c = sum_j x_j q_jc in FP32 FMA, as the CPU restatement.
 __global__ void __launch_bounds__(kReplayThreads)
 jacobiReplayKernel(VArgs args) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -672,49 +697,64 @@ jacobiReplayKernel(VArgs args) {
   const int m = padded8(n), nb = m / 4, P = nb / 2;
   const int R = args.rows_per_cta, ld = m + 4;
   float *vs = reinterpret_cast<float *>(smem_raw);    // [R][ld]
-  float *qs = vs + static_cast<size_t>(R) * ld;       // [P][64]
+  float *qbuf = vs + static_cast<size_t>(R) * ld;     // [2][P][64]
   float *v = args.v + args.a_offset[mi];
   const int rows = min(R, n - r0);
+  const float *log = args.log + args.log_offset[mi];
+  const int chunks = P * kQF / 4;  // 16-byte pieces of one round's rotations
+  for (int x = threadIdx.x; x < chunks; x += blockDim.x) copyAsync16(qbuf + 4 * x, log + 4 * x);
+  copyAsyncCommit();
   for (int k = threadIdx.x; k < m * R; k += blockDim.x) {
     const int c = k / R, r = k % R;
     vs[r * ld + c] = (c < n && r < rows) ? v[r0 + r + static_cast<int64_t>(c) * n] : 0.0f;
   }
-  const float *log = args.log + args.log_offset[mi];
-  const int lanes_r = R < 32 ? R : 32;  // rows per warp slice
+  // item -> (pair k, slice of up to 32 rows); a lane takes row r_in of the
+  // slice and, when R > 32, rows r_in + 32, r_in + 64, ... with the same Q_k
+  const int lanes_r = R < 32 ? R : 32;
+  const int per_lane = R < 32 ? 1 : R / 32;
   for (int round = 0; round < nb - 1; ++round) {
-    __syncthreads();
-    const float4 *src = reinterpret_cast<const float4 *>(log + static_cast<int64_t>(round) * P * kQF);
-    for (int k = threadIdx.x; k < P * kQF / 4; k += blockDim.x) reinterpret_cast<float4 *>(qs)[k] = src[k];
-    __syncthreads();
-    for (int item = threadIdx.x; item < P * R; item += blockDim.x) {
-      // item -> (pair k, row r) with r fastest inside a warp slice
-      const int slice = item / lanes_r, r_in = item % lanes_r;
-      const int slices_per_k = R / lanes_r;
-      const int k = slice / slices_per_k;
-      const int r = (slice % slices_per_k) * lanes_r + r_in;
-      if (r >= rows) continue;
+    copyAsyncWaitAll();
+    __syncthreads();  // this round's rotations landed; last round's rows written
+    if (round + 1 < nb - 1) {
+      float *next = qbuf + ((round + 1) & 1) * P * kQF;
+      const float *src = log + static_cast<int64_t>(round + 1) * P * kQF;
+      for (int x = threadIdx.x; x < chunks; x += blockDim.x) copyAsync16(next + 4 * x, src + 4 * x);
+      copyAsyncCommit();
+    }
+    const float *qs = qbuf + (round & 1) * P * kQF;
+    for (int item = threadIdx.x; item < P * lanes_r; item += blockDim.x) {
+      const int k = item / lanes_r, r_in = item % lanes_r;
       int I, J;
       rrPair(k, round, nb, I, J);
       const float4 *qk = reinterpret_cast<const float4 *>(qs + k * kQF);
-      float *row = vs + r * ld;
-      const float4 a = *reinterpret_cast<const float4 *>(row + 4 * I);
-      const float4 b = *reinterpret_cast<const float4 *>(row + 4 * J);
-      const float x[8] = {a.x, a.y, a.z, a.w, b.x, b.y, b.z, b.w};
-      float o[8];
-#pragma unroll
-      for (int c = 0; c < 8; ++c) o[c] = 0.0f;
+      float q[8][8];
 #pragma unroll
       for (int j = 0; j < 8; ++j) {
         const float4 lo = qk[2 * j], hi = qk[2 * j + 1];
-        o[0] = fmaf(x[j], lo.x, o[0]); o[1] = fmaf(x[j], lo.y, o[1]);
-        o[2] = fmaf(x[j], lo.z, o[2]); o[3] = fmaf(x[j], lo.w, o[3]);
-        o[4] = fmaf(x[j], hi.x, o[4]); o[5] = fmaf(x[j], hi.y, o[5]);
-        o[6] = fmaf(x[j], hi.z, o[6]); o[7] = fmaf(x[j], hi.w, o[7]);
+        q[j][0] = lo.x; q[j][1] = lo.y; q[j][2] = lo.z; q[j][3] = lo.w;
+        q[j][4] = hi.x; q[j][5] = hi.y; q[j][6] = hi.z; q[j][7] = hi.w;
       }
-      *reinterpret_cast<float4 *>(row + 4 * I) = make_float4(o[0], o[1], o[2], o[3]);
-      *reinterpret_cast<float4 *>(row + 4 * J) = make_float4(o[4], o[5], o[6], o[7]);
+      for (int e = 0; e < per_lane; ++e) {
+        const int r = r_in + 32 * e;
+        if (r >= rows) break;
+        float *row = vs + r * ld;
+        const float4 a = *reinterpret_cast<const float4 *>(row + 4 * I);
+        const float4 b = *reinterpret_cast<const float4 *>(row + 4 * J);
+        const float x[8] = {a.x, a.y, a.z, a.w, b.x, b.y, b.z, b.w};
+        float o[8];
+#pragma unroll
+        for (int c = 0; c < 8; ++c) {
+          float acc = 0.0f;
+#pragma unroll
+          for (int j = 0; j < 8; ++j) acc = fmaf(x[j], q[j][c], acc);
+          o[c] = acc;
+        }
+        *reinterpret_cast<float4 *>(row + 4 * I) = make_float4(o[0], o[1], o[2], o[3]);
+        *reinterpret_cast<float4 *>(row + 4 * J) = make_float4(o[4], o[5], o[6], o[7]);
+      }
     }
   }
+  copyAsyncWaitAll();
   __syncthreads();
   for (int k = threadIdx.x; k < n * R; k += blockDim.x) {
     const int c = k / R, r = k % R;
@@ -757,10 +797,132 @@ bool fitsSmem(int n) {
   return sweepSmemLayout(n, true, &q_off, &tile_off) <= kSmemLimit;
 }
 
+// Rows of V per replay CTA for matrices up to order max_n: the whole matrix
+// when it is small, else the most rows (a multiple of 32) that keep two CTAs
+// per SM (<= 112 KB of shared memory each), at least 8.
 int replayRows(int max_n) {
+  if (max_n <= 32) return padded8(max_n);
+  int best = 0;
+  const int cap = (max_n + 31) / 32 * 32;
+  for (int rows = 32; rows <= cap; rows += 32)
+    if (replaySmemBytes(max_n, rows) <= 112 * 1024) best = rows;
+  if (best > 0) return best;
   for (int rows = 32; rows >= 8; rows -= 8)
     if (replaySmemBytes(max_n, rows) <= kSmemLimit) return rows;
   return 0;
+}
+
+// ---------------------------------------------------------------------------
+// Size classes and the online autotuner of the sweep launch shape.
+//
+// Matrices are bucketed by size class; every class has a default CTA size
+// and a short list of candidates.  All candidates compute the same bits (the
+// CTA size only changes which thread runs which pivot quad and super-tile),
+// so the tuner times them on live work: while a class is untuned, sweep
+// launches 1..C of a call (full sweeps: every class needs more) each use the
+// next candidate, bracketed by timing events; a later call reads the events
+// and, once every candidate has a time, keeps the fastest for that device.
+// The decisions are process-wide, like a benchmark cache, and
+// msq_autotune_report prints them.
+constexpr int kClasses = 9;
+
+int sizeClass(int n) {
+  if (n <= 16) return 0;
+  if (n <= 32) return 1;
+  if (n <= 64) return 2;
+  if (n <= 128) return 3;
+  if (n <= 256) return 4;
+  if (fitsSmem(n)) return 5;
+  if (n <= 512) return 6;
+  if (n <= 1024) return 7;
+  return 8;
+}
+
+const char *className(int c) {
+  static const char *names[kClasses] = {"n<=16", "16<n<=32", "32<n<=64", "64<n<=128",
+                                        "128<n<=256", "256<n<=328 (shared tiles)",
+                                        "328<n<=512 (global tiles)", "512<n<=1024", "1024<n<=2048"};
+  return names[c];
+}
+
+std::vector<int> classCandidates(int c) {
+  switch (c) {
+    case 0: return {32};
+    case 1: return {64, 32};
+    case 2: return {128, 64};
+    case 3: return {256, 128};
+    case 4: return {256, 512};
+    default: return {512, 256};
+  }
+}
+
+// Launch names per class (static strings for the launch timer).
+const char *sweepName(int c) {
+  static const char *names[kClasses] = {
+      "jacobi sweep n<=16", "jacobi sweep n<=32", "jacobi sweep n<=64", "jacobi sweep n<=128",
+      "jacobi sweep n<=256", "jacobi sweep n<=328", "jacobi sweep n<=512 (global)",
+      "jacobi sweep n<=1024 (global)", "jacobi sweep n<=2048 (global)"};
+  return names[c];
+}
+
+struct ClassTune {
+  std::vector<int> cands;
+  std::vector<double> ms;   // per candidate, < 0 until measured
+  int best = -1;            // index into cands once tuned
+  bool requested = false;   // a call is measuring this class
+};
+
+struct PendingTiming {
+  int device, cls, cand;
+  cudaEvent_t begin, end;
+  int matrices;             // CTAs of the timed launch (for normalisation)
+};
+
+std::mutex g_tune_mutex;
+std::map<int, std::array<ClassTune, kClasses>> g_tune;  // by device
+std::vector<PendingTiming> g_pending;
+bool g_tune_enabled = true;
+
+std::array<ClassTune, kClasses> &tuneFor(int device) {
+  auto it = g_tune.find(device);
+  if (it == g_tune.end()) {
+    std::array<ClassTune, kClasses> t;
+    for (int c = 0; c < kClasses; ++c) {
+      t[c].cands = classCandidates(c);
+      t[c].ms.assign(t[c].cands.size(), -1.0);
+      if (t[c].cands.size() == 1) t[c].best = 0;
+    }
+    it = g_tune.emplace(device, t).first;
+  }
+  return it->second;
+}
+
+// Reads finished measurements (no waiting); caller holds g_tune_mutex.
+void harvestTimings() {
+  for (size_t i = 0; i < g_pending.size();) {
+    PendingTiming &p = g_pending[i];
+    const cudaError_t q = cudaEventQuery(p.end);
+    if (q == cudaErrorNotReady) {
+      ++i;
+      continue;
+    }
+    float ms = -1.0f;
+    if (q == cudaSuccess) cudaEventElapsedTime(&ms, p.begin, p.end);
+    cudaEventDestroy(p.begin);
+    cudaEventDestroy(p.end);
+    ClassTune &t = tuneFor(p.device)[p.cls];
+    if (ms > 0.0f && t.best < 0) {
+      const double per = ms / std::max(p.matrices, 1);
+      if (t.ms[p.cand] < 0.0 || per < t.ms[p.cand]) t.ms[p.cand] = per;
+      bool all = true;
+      for (double v : t.ms) all = all && v > 0.0;
+      if (all) {
+        t.best = static_cast<int>(std::min_element(t.ms.begin(), t.ms.end()) - t.ms.begin());
+      }
+    }
+    t.requested = false;
+    g_pending.erase(g_pending.begin() + i);
+  }
 }
 
 // Per-layout launch plan, kept per batch layout and device.
@@ -771,12 +933,14 @@ struct JacobiPlan {
   int64_t tile_total = 0, log_total = 0;
   int64_t *t_offset = nullptr, *log_offset = nullptr;
   int32_t *order = nullptr;  // ids grouped by bucket, largest first
-  struct Bucket { int threads; bool smem; int first; int count; size_t smem_bytes; };
+  struct Bucket { int cls; bool smem; int first; int count; size_t smem_bytes; };
   std::vector<Bucket> buckets;
   int32_t *work_matrix = nullptr, *work_row = nullptr;
   int work_count = 0;
-  int rows_per_cta = 0;
-  size_t v_smem = 0;
+  // V replay launches, one per size class: CTAs [first, first + count) of
+  // the work lists, `rows` rows each, `smem` bytes of shared memory.
+  struct ReplayGroup { int first; int count; int rows; size_t smem; };
+  std::vector<ReplayGroup> replays;
   void *device = nullptr;
 };
 
@@ -800,34 +964,40 @@ JacobiPlan *planFor(msq_ctx *ctx, const DeviceBatch *b) {
   }
   std::vector<int32_t> ids(count);
   for (int i = 0; i < count; ++i) ids[i] = i;
-  auto key = [&](int i) { return threadsFor(b->host_n[i]) * (fitsSmem(b->host_n[i]) ? 1 : 2); };
+  // buckets by size class, largest class first
   std::stable_sort(ids.begin(), ids.end(), [&](int x, int y) {
-    if (key(x) != key(y)) return key(x) > key(y);
+    const int cx = sizeClass(b->host_n[x]), cy = sizeClass(b->host_n[y]);
+    if (cx != cy) return cx > cy;
     return b->host_n[x] > b->host_n[y];
   });
   for (int i = 0; i < count;) {
-    const int n0 = b->host_n[ids[i]];
-    const int t = threadsFor(n0);
-    const bool smem = fitsSmem(n0);
+    const int c = sizeClass(b->host_n[ids[i]]);
+    const bool smem = fitsSmem(b->host_n[ids[i]]);
     int j = i;
     size_t bytes = 0;
-    while (j < count && threadsFor(b->host_n[ids[j]]) == t && fitsSmem(b->host_n[ids[j]]) == smem) {
+    while (j < count && sizeClass(b->host_n[ids[j]]) == c) {
       size_t q_off, tile_off;
       bytes = std::max(bytes, sweepSmemLayout(b->host_n[ids[j]], smem, &q_off, &tile_off));
       ++j;
     }
-    plan->buckets.push_back({t, smem, i, j - i, bytes});
+    plan->buckets.push_back({c, smem, i, j - i, bytes});
     i = j;
   }
-  plan->rows_per_cta = replayRows(b->max_n);
-  plan->v_smem = replaySmemBytes(b->max_n, plan->rows_per_cta);
   std::vector<int32_t> wm, wr;
-  for (int i = 0; i < count; ++i) {
-    const int n = b->host_n[ids[i]];
-    for (int r = 0; r < n; r += plan->rows_per_cta) {
-      wm.push_back(ids[i]);
-      wr.push_back(r);
+  for (const auto &bucket : plan->buckets) {
+    int max_n = 0;
+    for (int i = bucket.first; i < bucket.first + bucket.count; ++i) max_n = std::max(max_n, b->host_n[ids[i]]);
+    const int rows = replayRows(max_n);
+    const int first = static_cast<int>(wm.size());
+    for (int i = bucket.first; i < bucket.first + bucket.count; ++i) {
+      const int n = b->host_n[ids[i]];
+      for (int r = 0; r < n; r += rows) {
+        wm.push_back(ids[i]);
+        wr.push_back(r);
+      }
     }
+    plan->replays.push_back({first, static_cast<int>(wm.size()) - first, rows,
+                             replaySmemBytes(max_n, rows)});
   }
   plan->work_count = static_cast<int>(wm.size());
   const size_t bytes = 2 * count * sizeof(int64_t) + count * sizeof(int32_t) +
@@ -911,19 +1081,46 @@ int jacobiEnqueue(msq_ctx *ctx, const DeviceBatch *b, float *matrices, float *ve
     MSQ_TRY(launched(ctx, "jacobi identity"));
   }
   VArgs vargs{vectors, b->offset, plan->log_offset, b->n, log_base, args.state,
-              plan->work_matrix, plan->work_row, plan->rows_per_cta, 0};
+              plan->work_matrix, plan->work_row, 0, 0};
+  // Launch shape per bucket: the tuned CTA size, or (while its class is
+  // being tuned) candidate c on sweep launch 1 + c with timing events.
+  struct BucketLaunch { int threads; int measure; };  // measure: candidate or -1
+  std::vector<std::vector<BucketLaunch>> shape(plan->buckets.size());
+  bool measuring = false;
+  {
+    std::lock_guard<std::mutex> lock(g_tune_mutex);
+    harvestTimings();
+    auto &tune = tuneFor(ctx->device);
+    for (size_t k = 0; k < plan->buckets.size(); ++k) {
+      ClassTune &t = tune[plan->buckets[k].cls];
+      const bool measure = g_tune_enabled && t.best < 0 && !t.requested && max_sweeps >= 1;
+      if (measure) t.requested = true;
+      measuring = measuring || measure;
+      for (int launch = 0; launch <= max_sweeps; ++launch) {
+        const int c = launch - 1;
+        if (measure && c >= 0 && c < static_cast<int>(t.cands.size())) {
+          shape[k].push_back({t.cands[c], c});
+        } else {
+          shape[k].push_back({t.cands[t.best >= 0 ? t.best : 0], -1});
+        }
+      }
+    }
+  }
   // Streams: size buckets round-robin over three sweep streams, the replay
   // on a fourth.  Order: sweep k of a bucket follows sweep k-1 (same
   // stream) and the replay of k-2 (which read the log buffer sweep k
-  // overwrites); the replay of k follows every bucket's sweep k.
+  // overwrites); the replay of k follows every bucket's sweep k.  A call
+  // that measures candidate shapes runs serially so that each timed launch
+  // has the GPU to itself.
   syncReset(ctx);
+  const bool serial = !ctx->concurrent || measuring;
   const int sweep_streams = std::min<int>(3, static_cast<int>(plan->buckets.size()));
   cudaStream_t ss[3];
   for (int i = 0; i < sweep_streams; ++i) {
-    ss[i] = auxStream(ctx, 1 + i);
+    ss[i] = serial ? ctx->stream : auxStream(ctx, 1 + i);
     MSQ_TRY(streamWait(ctx, ss[i], ctx->stream));
   }
-  cudaStream_t rs = auxStream(ctx, 0);
+  cudaStream_t rs = serial ? ctx->stream : auxStream(ctx, 0);
   MSQ_TRY(streamWait(ctx, rs, ctx->stream));
   cudaEvent_t replay_done[2] = {nullptr, nullptr};  // by parity
   for (int launch = 0; launch <= max_sweeps; ++launch) {
@@ -938,23 +1135,40 @@ int jacobiEnqueue(msq_ctx *ctx, const DeviceBatch *b, float *matrices, float *ve
     }
     for (size_t k = 0; k < plan->buckets.size(); ++k) {
       const auto &bucket = plan->buckets[k];
+      const BucketLaunch how = shape[k][launch];
       cudaStream_t s = ss[k % sweep_streams];
       args.order = plan->order + bucket.first;
+      cudaEvent_t t0 = nullptr, t1 = nullptr;
+      if (how.measure >= 0) {
+        cudaEventCreate(&t0);
+        cudaEventCreate(&t1);
+        cudaEventRecord(t0, s);
+      }
       launchBegin(ctx, s);
       if (bucket.smem) {
-        jacobiSweepKernel<true><<<bucket.count, bucket.threads, bucket.smem_bytes, s>>>(args);
+        jacobiSweepKernel<true><<<bucket.count, how.threads, bucket.smem_bytes, s>>>(args);
       } else {
-        jacobiSweepKernel<false><<<bucket.count, bucket.threads, bucket.smem_bytes, s>>>(args);
+        jacobiSweepKernel<false><<<bucket.count, how.threads, bucket.smem_bytes, s>>>(args);
       }
-      MSQ_TRY(launchedOn(ctx, s, "jacobi sweep"));
+      MSQ_TRY(launchedOn(ctx, s, sweepName(bucket.cls)));
+      if (how.measure >= 0) {
+        cudaEventRecord(t1, s);
+        std::lock_guard<std::mutex> lock(g_tune_mutex);
+        g_pending.push_back({ctx->device, bucket.cls, how.measure, t0, t1, bucket.count});
+      }
     }
     if (launch < max_sweeps) {
       for (int i = 0; i < sweep_streams; ++i) MSQ_TRY(streamWait(ctx, rs, ss[i]));
       vargs.parity = parity;
       vargs.log = args.log;
-      launchBegin(ctx, rs);
-      jacobiReplayKernel<<<plan->work_count, kReplayThreads, plan->v_smem, rs>>>(vargs);
-      MSQ_TRY(launchedOn(ctx, rs, "jacobi replay"));
+      for (const auto &g : plan->replays) {
+        vargs.work_matrix = plan->work_matrix + g.first;
+        vargs.work_row = plan->work_row + g.first;
+        vargs.rows_per_cta = g.rows;
+        launchBegin(ctx, rs);
+        jacobiReplayKernel<<<g.count, kReplayThreads, g.smem, rs>>>(vargs);
+        MSQ_TRY(launchedOn(ctx, rs, "jacobi replay"));
+      }
       replay_done[parity] = syncEvent(ctx);
       MSQ_TRY(cudaCheck(ctx, cudaEventRecord(replay_done[parity], rs), "event record"));
     }
@@ -972,6 +1186,41 @@ int jacobiEnqueue(msq_ctx *ctx, const DeviceBatch *b, float *matrices, float *ve
 }  // namespace msq
 
 using namespace msq;
+
+extern "C" int msq_autotune_report(int device, char *out, size_t capacity) {
+  if (out == nullptr || capacity == 0) return MSQ_ERR_INVALID_ARGUMENT;
+  std::string text;
+  {
+    std::lock_guard<std::mutex> lock(g_tune_mutex);
+    harvestTimings();
+    auto &tune = tuneFor(device);
+    for (int c = 0; c < kClasses; ++c) {
+      const ClassTune &t = tune[c];
+      text += std::string("jacobi sweep ") + className(c) + ": threads";
+      for (size_t i = 0; i < t.cands.size(); ++i) {
+        char buf[64];
+        if (t.ms[i] > 0.0) {
+          std::snprintf(buf, sizeof(buf), " %d=%.4fms", t.cands[i], t.ms[i]);
+        } else {
+          std::snprintf(buf, sizeof(buf), " %d=?", t.cands[i]);
+        }
+        text += buf;
+      }
+      text += t.best >= 0 ? " -> " + std::to_string(t.cands[t.best]) + "\n" : " -> untuned\n";
+    }
+  }
+  std::strncpy(out, text.c_str(), capacity - 1);
+  out[capacity - 1] = '\0';
+  return MSQ_OK;
+}
+
+extern "C" int msq_autotune_reset(int enable) {
+  std::lock_guard<std::mutex> lock(g_tune_mutex);
+  harvestTimings();
+  g_tune.clear();
+  g_tune_enabled = enable != 0;
+  return MSQ_OK;
+}
 
 extern "C" int msq_jacobi_batched(msq_ctx *ctx, float *matrices, float *vectors,
                                   float *eigenvalues, const int32_t *n,

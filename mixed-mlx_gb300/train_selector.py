@@ -4,8 +4,8 @@
       --out mixed-mlx_gb300/selector_weights.npz
 
 Training data: SPD matrices of three spectrum families (log-uniform,
-clustered, power law), n log-uniform in [32, 512], condition log-uniform in
-[1e1, 1e8]; every plan is run on every matrix by msq_solve_batched and
+clustered, power law), n log-uniform in [--n-lo, --n-hi] (default [32, 512]),
+condition log-uniform in [1e1, 1e8]; every plan is run on every matrix by msq_solve_batched and
 scored by its own float-float residual at the tolerance.  The network is
 trained by the library's CUDA kernels (msq_mlp_backward / msq_mlp_step).
 Prints accept rate, fallback rate and solves/s on held-out seeds for the
@@ -32,6 +32,8 @@ def main():
     ap.add_argument("--tol", type=float, default=1e-5)
     ap.add_argument("--epochs", type=int, default=150)
     ap.add_argument("--threshold", type=float, default=0.9)
+    ap.add_argument("--n-lo", type=int, default=32)
+    ap.add_argument("--n-hi", type=int, default=512)
     ap.add_argument("--out", default=os.path.join(HERE, "selector_weights.npz"))
     args = ap.parse_args()
     import torch
@@ -42,7 +44,7 @@ def main():
     chunks_f, chunks_y, secs = [], [], np.zeros(len(sel.PLANS))
     for c, start in enumerate(range(0, args.train, 1024)):
         count = min(1024, args.train - start)
-        orders, mats = sel.generate(torch, count, seed=1000 + c)
+        orders, mats = sel.generate(torch, count, seed=1000 + c, n_lo=args.n_lo, n_hi=args.n_hi)
         batch, flat = sel.pack(msq, torch, orders, mats)
         chunks_f.append(sel.features(ctx, torch, batch, flat, args.tol))
         out = sel.score_plans(ctx, msq, torch, batch, flat, args.tol)
@@ -55,7 +57,7 @@ def main():
     selector.cost_order = [int(k) for k in np.argsort(secs)]
     losses = selector.fit(feats, targets, epochs=args.epochs)
 
-    orders, mats = sel.generate(torch, args.test, seed=999_999)
+    orders, mats = sel.generate(torch, args.test, seed=999_999, n_lo=args.n_lo, n_hi=args.n_hi)
     batch, flat = sel.pack(msq, torch, orders, mats)
     feats_t = sel.features(ctx, torch, batch, flat, args.tol)
     choice = selector.choose(feats_t, args.threshold)
