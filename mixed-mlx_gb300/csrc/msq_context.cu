@@ -245,8 +245,10 @@ extern "C" void msq_destroy(msq_ctx *ctx) {
     cudaFree(b->offset);
     delete b;
   }
-  for (int slot = 0; slot < 4; ++slot)
+  for (int slot = 0; slot < 5; ++slot)
     if (ctx->scratch[slot] != nullptr) cudaFree(ctx->scratch[slot]);
+  if (ctx->grid_exec != nullptr) cudaGraphExecDestroy(ctx->grid_exec);
+  if (ctx->grid_host != nullptr) cudaFreeHost(ctx->grid_host);
   if (ctx->d_status != nullptr) cudaFree(ctx->d_status);
   recycleTiming(ctx);
   for (cudaEvent_t e : ctx->event_pool) cudaEventDestroy(e);

@@ -58,8 +58,8 @@ struct msq_ctx {
   int *d_status = nullptr;  // device status word
   // Grow-only scratch arenas owned by the context (freed in msq_destroy);
   // one per user so nested stages never share memory.
-  void *scratch[4] = {nullptr, nullptr, nullptr, nullptr};
-  size_t scratch_bytes[4] = {0, 0, 0, 0};
+  void *scratch[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};
+  size_t scratch_bytes[5] = {0, 0, 0, 0, 0};
   // Batch layouts cached by content hash (small: a few entries).
   std::vector<msq::DeviceBatch *> batches;
   // Launch timing (msq_timing_begin/end).  Launches on the context stream
@@ -77,10 +77,17 @@ struct msq_ctx {
   cudaEvent_t pending_begin = nullptr;  // begin recorded for the next aux launch
   // Auxiliary streams (non-blocking, created on first use) that fork from and
   // join back into `stream` through events from sync_pool.
-  cudaStream_t aux[4] = {nullptr, nullptr, nullptr, nullptr};
+  cudaStream_t aux[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};
   // false: every launch on `stream` (serial order; per-kernel timings are
   // then each kernel's own duration, not shared with concurrent work)
   bool concurrent = true;
+  // Grid Jacobi (one large matrix on all SMs): pinned off-norm readback and
+  // the captured graph of one sweep, valid for order grid_n and workspace
+  // grid_work.
+  double *grid_host = nullptr;
+  cudaGraphExec_t grid_exec = nullptr;
+  int grid_n = 0;
+  void *grid_work = nullptr;
   std::vector<cudaEvent_t> sync_pool;
   size_t sync_next = 0;
 };
@@ -94,7 +101,8 @@ int launched(msq_ctx *ctx, const char *what);
 // Launches on an auxiliary stream: launchBegin before, launchedOn after.
 void launchBegin(msq_ctx *ctx, cudaStream_t stream);
 int launchedOn(msq_ctx *ctx, cudaStream_t stream, const char *what);
-// Auxiliary stream i (0..3), created non-blocking on first use.
+// Auxiliary stream i (0..4), created non-blocking on first use: 0 replay,
+// 1..3 sweep buckets, 4 graph capture.
 cudaStream_t auxStream(msq_ctx *ctx, int i);
 // A disable-timing event from the context's pool; syncReset() recycles the
 // pool at the start of a call (events may be re-recorded once waited on).
@@ -108,8 +116,10 @@ int checkDeviceStatus(msq_ctx *ctx);
 const DeviceBatch *prepareBatch(msq_ctx *ctx, const int32_t *n,
                                 const int64_t *offset, int count);
 // Grow-only context scratch arena `slot` (0: Jacobi, 1: solver,
-// 2: codec operands, 3: GEMM split operands).
-enum ScratchSlot : int { kScratchJacobi = 0, kScratchSolver = 1, kScratchOperand = 2, kScratchGemm = 3 };
+// 2: codec operands, 3: GEMM split operands, 4: grid Jacobi).
+enum ScratchSlot : int {
+  kScratchJacobi = 0, kScratchSolver = 1, kScratchOperand = 2, kScratchGemm = 3, kScratchGrid = 4
+};
 void *scratch(msq_ctx *ctx, size_t bytes, int slot);
 
 inline unsigned gridFor(size_t work_items, unsigned threads,

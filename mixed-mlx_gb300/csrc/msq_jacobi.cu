@@ -29,6 +29,8 @@
 //    off(A) <= tol * ||A||_F instead of after a fixed 8;
 //  * launches are size-bucketed (threads per CTA grow with n), largest first.
 #include "msq_internal.cuh"
+#include "msq_jacobi_device.cuh"
+#include "msq_jacobi_grid.cuh"
 
 #include <algorithm>
 #include <array>
@@ -42,27 +44,12 @@
 namespace msq {
 namespace {
 
-constexpr int kTileF = 16;      // floats per 4x4 tile
-constexpr int kQF = 64;         // floats per 8x8 rotation
-// Shared-memory stride of the rotations in the sweep kernel: 68 floats puts
-// Q_l of different pivots on different banks (a 64-float stride would map
-// every Q_l row to the same four banks).
-constexpr int kQS = 68;
 constexpr size_t kSmemLimit = 227 * 1024;
-constexpr int kMaxOrder = 2048;
+constexpr int kMaxOrder = 16384;    // grid kernels; the batched ones see n <= 1024
+constexpr int kGridMinOrder = 1024;
+constexpr int kGridFewLarge = 8;
 constexpr int kSweepThreadsMax = 512;
 constexpr int kReplayThreads = 256;
-
-struct JacobiState {
-  double norm2;       // ||A||_F^2
-  double off_ratio;   // off(A) / ||A||_F when the sweeps stopped
-  int sweeps;         // sweeps applied
-  int done;           // 1 once converged or out of budget
-  // logged[p]: 1 if log buffer p holds a sweep not yet applied to V.  The
-  // log is double-buffered by sweep parity so sweep k+1 can run while the
-  // replay of sweep k reads the other buffer.
-  int logged[2];
-};
 
 struct JacobiArgs {
   float *a;                  // user matrices (full, column-major)
@@ -81,308 +68,6 @@ struct JacobiArgs {
   int first;                 // 1 on the first launch (load A, set norm)
   int parity;                // log buffer of this sweep (log points at it)
 };
-
-__host__ __device__ constexpr int padded8(int n) { return (n + 7) & ~7; }
-
-// Slot -> participant of round r (participants 1..m-1 rotate right by one
-// per round, slot 0 fixed): the closed form of the std::rotate step in
-// makeJacobiSchedule (src/metal_solver.cpp:75-76).
-__device__ __forceinline__ int rrSlot(int slot, int round, int m) {
-  if (slot == 0) return 0;
-  int k = slot - 1 - round % (m - 1);
-  if (k < 0) k += m - 1;
-  return 1 + k;
-}
-
-__device__ __forceinline__ void rrPair(int pair, int round, int m, int &p, int &q) {
-  const int a = rrSlot(pair, round, m);
-  const int b = rrSlot(m - 1 - pair, round, m);
-  p = a < b ? a : b;
-  q = a < b ? b : a;
-}
-
-// Folded enumeration of the upper triangle {(i, j): i <= j < P}: rows i and
-// P-1-i share one folded row of P+1 items.
-__device__ __forceinline__ bool foldedBlock(int w, int P, int &i, int &j) {
-  const int r = w / (P + 1);
-  const int c = w - r * (P + 1);
-  if (c < P - r) {
-    i = r;
-    j = r + c;
-    return true;
-  }
-  if ((P & 1) && r == P / 2) return false;
-  i = P - 1 - r;
-  j = c - 1;
-  return true;
-}
-
-__device__ double blockReduceSum(double v, double *red) {
-#pragma unroll
-  for (int s = 16; s > 0; s >>= 1) v += __shfl_xor_sync(0xffffffffu, v, s);
-  const int warp = threadIdx.x / 32, lane = threadIdx.x % 32;
-  __syncthreads();
-  if (lane == 0) red[warp] = v;
-  __syncthreads();
-  const int warps = blockDim.x / 32;
-  v = threadIdx.x < warps ? red[threadIdx.x] : 0.0;
-  if (warp == 0) {
-#pragma unroll
-    for (int s = 16; s > 0; s >>= 1) v += __shfl_xor_sync(0xffffffffu, v, s);
-    if (lane == 0) red[0] = v;
-  }
-  __syncthreads();
-  const double total = red[0];
-  __syncthreads();
-  return total;
-}
-
-// Packed tile (I, J), I <= J, of a matrix's tile array: tile index
-// tri[J] + I, 16 floats.  A 4x4 tile spans half the 32 shared-memory banks,
-// so without care the rows of all tiles would fall on two bank groups; row
-// i of tile t is stored at physical row i ^ (t & 3), which spreads the
-// float4 rows a warp touches over all eight 4-bank groups.
-__device__ __forceinline__ int tileIndex(const int *tri, int I, int J) { return tri[J] + I; }
-
-__device__ __forceinline__ int64_t tileElement(int t, int i, int j) {
-  return static_cast<int64_t>(t) * kTileF + (((i ^ (t & 3)) << 2) | j);
-}
-
-// Loads block (R, C) of A (4x4, row-major in t) from the packed tiles.
-__device__ __forceinline__ void loadBlock(float *tiles, const int *tri, int R, int C, float (&t)[4][4]) {
-  if (R <= C) {
-    const int ti = tileIndex(tri, R, C);
-    const float4 *src = reinterpret_cast<const float4 *>(tiles + static_cast<int64_t>(ti) * kTileF);
-#pragma unroll
-    for (int i = 0; i < 4; ++i) {
-      const float4 v = src[i ^ (ti & 3)];
-      t[i][0] = v.x; t[i][1] = v.y; t[i][2] = v.z; t[i][3] = v.w;
-    }
-  } else {
-    const int ti = tileIndex(tri, C, R);
-    const float4 *src = reinterpret_cast<const float4 *>(tiles + static_cast<int64_t>(ti) * kTileF);
-#pragma unroll
-    for (int i = 0; i < 4; ++i) {
-      const float4 v = src[i ^ (ti & 3)];
-      t[0][i] = v.x; t[1][i] = v.y; t[2][i] = v.z; t[3][i] = v.w;
-    }
-  }
-}
-
-__device__ __forceinline__ void storeBlock(float *tiles, const int *tri, int R, int C, const float (&t)[4][4]) {
-  if (R <= C) {
-    const int ti = tileIndex(tri, R, C);
-    float4 *dst = reinterpret_cast<float4 *>(tiles + static_cast<int64_t>(ti) * kTileF);
-#pragma unroll
-    for (int i = 0; i < 4; ++i) dst[i ^ (ti & 3)] = make_float4(t[i][0], t[i][1], t[i][2], t[i][3]);
-  } else {
-    const int ti = tileIndex(tri, C, R);
-    float4 *dst = reinterpret_cast<float4 *>(tiles + static_cast<int64_t>(ti) * kTileF);
-#pragma unroll
-    for (int i = 0; i < 4; ++i) dst[i ^ (ti & 3)] = make_float4(t[0][i], t[1][i], t[2][i], t[3][i]);
-  }
-}
-
-// ---------------------------------------------------------------------------
-// Pivot sweep: the 28 index pairs of an 8x8 pivot in the round-robin order of
-// 8 indices, 7 groups of 4 disjoint pairs, one rotation per pair with the
-// reference's angle formula (metal_mixed_sqrt.metal:1347-1357):
-// tau = (p_bb - p_aa) / (2 p_ab), t = sign(tau) / (|tau| + sqrt(1 + tau^2)),
-// c = 1 / sqrt(1 + t^2), s = t c; J = [c s; -s c] on (a, b): column
-// a' = c a - s b, column b' = s a + c b; p <- J^T p J, p_ab = p_ba = 0;
-// Q <- Q J.
-//
-// A quad of lanes sweeps one pivot.  In group g lane t owns the two rows
-// (a_t, b_t) of its pair.  The four angles of a group depend only on the
-// pair's own 2x2 block, which no other rotation of the group touches, so
-// they are computed at once and shared with shuffles; each lane then
-// updates its two rows.  Element (x, y) of a row pair t and column pair j is
-// touched by the row rotation of t and the column rotation of j, applied in
-// the order of the pairs in the group (the sequential order); the diagonal
-// block (j = t) takes the column rotation first.  Every operation is an
-// explicitly rounded one (no FMA contraction, no approximate reciprocal
-// square root), so the sweep equals, bit for bit, the sequential sweep of
-// the C restatement compiled with -ffp-contract=off.
-
-// Pairs of group g packed as 4 x (a: 3 bits, b: 3 bits), a < b.
-__host__ __device__ constexpr uint32_t groupWord(int g) {
-  constexpr int pairs[8][8] = {{0, 7, 1, 6, 2, 5, 3, 4}, {0, 6, 5, 7, 1, 4, 2, 3},
-                               {0, 5, 4, 6, 3, 7, 1, 2}, {0, 4, 3, 5, 2, 6, 1, 7},
-                               {0, 3, 2, 4, 1, 5, 6, 7}, {0, 2, 1, 3, 4, 7, 5, 6},
-                               {0, 1, 2, 7, 3, 6, 4, 5},
-                               // layout used to store the pivot: rows (t, 4 + t)
-                               {0, 4, 1, 5, 2, 6, 3, 7}};
-  uint32_t w = 0;
-  for (int t = 0; t < 4; ++t)
-    w |= static_cast<uint32_t>(pairs[g][2 * t] | (pairs[g][2 * t + 1] << 3)) << (6 * t);
-  return w;
-}
-
-// For each row r: owner lane (2 bits) and slot (1 bit, 1 = second row of
-// the pair) in group g, packed 3 bits per row.
-__host__ __device__ constexpr uint32_t ownerWord(int g) {
-  uint32_t w = 0;
-  for (int t = 0; t < 4; ++t) {
-    const uint32_t a = (groupWord(g) >> (6 * t)) & 7, b = (groupWord(g) >> (6 * t + 3)) & 7;
-    w |= static_cast<uint32_t>(t) << (3 * a);
-    w |= static_cast<uint32_t>(t | 4) << (3 * b);
-  }
-  return w;
-}
-
-__device__ __forceinline__ float pick8(const float (&r)[8], int i) {
-  float v = r[0];
-#pragma unroll
-  for (int k = 1; k < 8; ++k) v = i == k ? r[k] : v;
-  return v;
-}
-
-// Rotation angle of one pair (explicitly rounded; renormalised so that
-// c^2 + s^2 - 1, evaluated exactly with FMA two-products, is pulled back by
-// (1 - e/2): FP32 (c, s) otherwise carry a one-signed error in c^2 + s^2
-// that compounds over the thousands of rotations applied to each row of V).
-__device__ __forceinline__ bool jacobiAngle(float paa, float pbb, float pab, float &c, float &s) {
-  c = 1.0f;
-  s = 0.0f;
-  if (pab == 0.0f) return false;
-  const float tau = __fdiv_rn(__fsub_rn(pbb, paa), __fmul_rn(2.0f, pab));
-  const float root = __fsqrt_rn(__fadd_rn(__fmul_rn(tau, tau), 1.0f));
-  const float t = copysignf(__fdiv_rn(1.0f, __fadd_rn(fabsf(tau), root)), tau);
-  float cc0 = __fdiv_rn(1.0f, __fsqrt_rn(__fadd_rn(__fmul_rn(t, t), 1.0f)));
-  float ss0 = __fmul_rn(t, cc0);
-  const float cc = __fmul_rn(cc0, cc0), cce = fmaf(cc0, cc0, -cc);
-  const float ss = __fmul_rn(ss0, ss0), sse = fmaf(ss0, ss0, -ss);
-  const float e = __fadd_rn(__fadd_rn(__fsub_rn(cc, 1.0f), ss), __fadd_rn(cce, sse));
-  const float h = __fmul_rn(-0.5f, e);
-  c = fmaf(h, cc0, cc0);
-  s = fmaf(h, ss0, ss0);
-  return true;
-}
-
-// x' = c x - s y, y' = s x + c y (explicitly rounded); identity if !on.
-__device__ __forceinline__ void rot2(float &x, float &y, float c, float s, bool on) {
-  const float nx = __fsub_rn(__fmul_rn(c, x), __fmul_rn(s, y));
-  const float ny = __fadd_rn(__fmul_rn(s, x), __fmul_rn(c, y));
-  x = on ? nx : x;
-  y = on ? ny : y;
-}
-
-// One group of 4 rotations on the quad.  ra / rb: this lane's rows a_t / b_t
-// (all 8 columns); qcol: the pivot's Q, column-major (column x at qcol[8x]).
-template <int G>
-__device__ __forceinline__ void pivotGroup(float (&ra)[8], float (&rb)[8], float *qcol, int t,
-                                           bool active) {
-  constexpr uint32_t W = groupWord(G);
-  const int a = (W >> (6 * t)) & 7, b = (W >> (6 * t + 3)) & 7;
-  float c, s;
-  const bool on = jacobiAngle(pick8(ra, a), pick8(rb, b), pick8(ra, b), c, s);
-  float cj[4], sj[4];
-  bool onj[4];
-#pragma unroll
-  for (int j = 0; j < 4; ++j) {
-    cj[j] = __shfl_sync(0xffffffffu, c, j, 4);
-    sj[j] = __shfl_sync(0xffffffffu, s, j, 4);
-    onj[j] = __shfl_sync(0xffffffffu, static_cast<int>(on), j, 4) != 0;
-  }
-#pragma unroll
-  for (int j = 0; j < 4; ++j) {
-    const int A = (W >> (6 * j)) & 7, B = (W >> (6 * j + 3)) & 7;
-    // 2x2 block X: rows (a_t, b_t), columns (A, B) of pair j.  If j comes
-    // first in the group (or j = t) the column rotation precedes the row
-    // rotation: Y = (C_t(R_j(X^T)))^T, else Y = C_j(R_t(X)), where R mixes
-    // rows and C mixes columns with the same two-term arithmetic.
-    const bool swap = j <= t;
-    float x00 = ra[A], x01 = swap ? rb[A] : ra[B];
-    float x10 = swap ? ra[B] : rb[A], x11 = rb[B];
-    const float c1 = swap ? cj[j] : c, s1 = swap ? sj[j] : s;
-    const bool on1 = swap ? onj[j] : on;
-    const float c2 = swap ? c : cj[j], s2 = swap ? s : sj[j];
-    const bool on2 = swap ? on : onj[j];
-    rot2(x00, x10, c1, s1, on1);  // rows of X'
-    rot2(x01, x11, c1, s1, on1);
-    rot2(x00, x01, c2, s2, on2);  // columns of X'
-    rot2(x10, x11, c2, s2, on2);
-    const bool diag = j == t && on;
-    ra[A] = x00;
-    rb[B] = x11;
-    const float y01 = swap ? x10 : x01, y10 = swap ? x01 : x10;
-    ra[B] = diag ? 0.0f : y01;
-    rb[A] = diag ? 0.0f : y10;
-  }
-  if (active && on) {
-    float4 *ca = reinterpret_cast<float4 *>(qcol + 8 * a);
-    float4 *cb = reinterpret_cast<float4 *>(qcol + 8 * b);
-    float4 x0 = ca[0], x1 = ca[1], y0 = cb[0], y1 = cb[1];
-    rot2(x0.x, y0.x, c, s, true); rot2(x0.y, y0.y, c, s, true);
-    rot2(x0.z, y0.z, c, s, true); rot2(x0.w, y0.w, c, s, true);
-    rot2(x1.x, y1.x, c, s, true); rot2(x1.y, y1.y, c, s, true);
-    rot2(x1.z, y1.z, c, s, true); rot2(x1.w, y1.w, c, s, true);
-    ca[0] = x0; ca[1] = x1; cb[0] = y0; cb[1] = y1;
-  }
-  __syncwarp();
-}
-
-// Moves the rows from the ownership of group G to that of group G + 1.
-template <int G>
-__device__ __forceinline__ void pivotExchange(float (&ra)[8], float (&rb)[8], int t) {
-  constexpr uint32_t O = ownerWord(G), W1 = groupWord(G + 1);
-  const int a1 = (W1 >> (6 * t)) & 7, b1 = (W1 >> (6 * t + 3)) & 7;
-  const int src_a = (O >> (3 * a1)) & 3, slot_a = (O >> (3 * a1 + 2)) & 1;
-  const int src_b = (O >> (3 * b1)) & 3, slot_b = (O >> (3 * b1 + 2)) & 1;
-  float na[8], nb[8];
-#pragma unroll
-  for (int y = 0; y < 8; ++y) {
-    const float u0 = __shfl_sync(0xffffffffu, ra[y], src_a, 4);
-    const float u1 = __shfl_sync(0xffffffffu, rb[y], src_a, 4);
-    const float v0 = __shfl_sync(0xffffffffu, ra[y], src_b, 4);
-    const float v1 = __shfl_sync(0xffffffffu, rb[y], src_b, 4);
-    na[y] = slot_a ? u1 : u0;
-    nb[y] = slot_b ? v1 : v0;
-  }
-#pragma unroll
-  for (int y = 0; y < 8; ++y) {
-    ra[y] = na[y];
-    rb[y] = nb[y];
-  }
-}
-
-// Full pivot sweep on the quad; on return ra / rb hold rows (t, 4 + t) and
-// qcol holds Q row-major.
-__device__ __forceinline__ void pivotSweep(float (&ra)[8], float (&rb)[8], float *qcol, int t,
-                                           bool active) {
-  if (active) {
-    // Q = I, column-major: lane t writes columns 2t and 2t + 1.
-    float4 *q4 = reinterpret_cast<float4 *>(qcol);
-#pragma unroll
-    for (int x = 0; x < 2; ++x) {
-      const int col = 2 * t + x;
-      q4[2 * col] = make_float4(col == 0, col == 1, col == 2, col == 3);
-      q4[2 * col + 1] = make_float4(col == 4, col == 5, col == 6, col == 7);
-    }
-  }
-  __syncwarp();
-  pivotGroup<0>(ra, rb, qcol, t, active); pivotExchange<0>(ra, rb, t);
-  pivotGroup<1>(ra, rb, qcol, t, active); pivotExchange<1>(ra, rb, t);
-  pivotGroup<2>(ra, rb, qcol, t, active); pivotExchange<2>(ra, rb, t);
-  pivotGroup<3>(ra, rb, qcol, t, active); pivotExchange<3>(ra, rb, t);
-  pivotGroup<4>(ra, rb, qcol, t, active); pivotExchange<4>(ra, rb, t);
-  pivotGroup<5>(ra, rb, qcol, t, active); pivotExchange<5>(ra, rb, t);
-  pivotGroup<6>(ra, rb, qcol, t, active); pivotExchange<6>(ra, rb, t);
-  // Q column-major -> row-major in place: lane t gathers rows 2t, 2t + 1.
-  float2 r2[8];
-  if (active) {
-#pragma unroll
-    for (int col = 0; col < 8; ++col) r2[col] = reinterpret_cast<const float2 *>(qcol + 8 * col)[t];
-  }
-  __syncwarp();
-  if (active) {
-    float4 *q4 = reinterpret_cast<float4 *>(qcol);
-    q4[4 * t + 0] = make_float4(r2[0].x, r2[1].x, r2[2].x, r2[3].x);
-    q4[4 * t + 1] = make_float4(r2[4].x, r2[5].x, r2[6].x, r2[7].x);
-    q4[4 * t + 2] = make_float4(r2[0].y, r2[1].y, r2[2].y, r2[3].y);
-    q4[4 * t + 3] = make_float4(r2[4].y, r2[5].y, r2[6].y, r2[7].y);
-  }
-}
 
 __host__ __device__ __forceinline__ size_t sweepSmemLayout(int n, bool with_tiles, size_t *q_off,
                                                            size_t *tile_off) {
@@ -562,75 +247,9 @@ jacobiSweepKernel(JacobiArgs args) {
       const bool valid = w2 < 2 * items && foldedBlock(w2 >> 1, P, k, l) && k != l;
       if (!valid) k = l = 0;
       const int rb0 = pair_i[k], rb1 = pair_j[k];
-      const int cbh = h ? pair_j[l] : pair_i[l];
       const float4 *qk = reinterpret_cast<const float4 *>(qs + k * kQS);
       const float4 *ql = reinterpret_cast<const float4 *>(qs + l * kQS);
-      float u[8][4];
-#pragma unroll
-      for (int a = 0; a < 8; ++a)
-#pragma unroll
-        for (int c = 0; c < 4; ++c) u[a][c] = 0.0f;
-#pragma unroll
-      for (int x = 0; x < 2; ++x) {
-        float b4[4][4];
-        if (valid) {
-          loadBlock(tiles, tri, x ? rb1 : rb0, cbh, b4);
-        } else {
-#pragma unroll
-          for (int i = 0; i < 4; ++i)
-#pragma unroll
-            for (int c = 0; c < 4; ++c) b4[i][c] = 0.0f;
-        }
-#pragma unroll
-        for (int i = 0; i < 4; ++i) {
-          const float4 lo = qk[2 * (4 * x + i)], hi = qk[2 * (4 * x + i) + 1];
-          const float qr[8] = {lo.x, lo.y, lo.z, lo.w, hi.x, hi.y, hi.z, hi.w};
-#pragma unroll
-          for (int a = 0; a < 8; ++a)
-#pragma unroll
-            for (int c = 0; c < 4; ++c) u[a][c] = fmaf(qr[a], b4[i][c], u[a][c]);
-        }
-      }
-      // U rows of this lane's half: own columns, and the partner's columns
-      // for these rows (the partner sends the rows of the other half).
-      float ur[4][8];
-#pragma unroll
-      for (int r = 0; r < 4; ++r)
-#pragma unroll
-        for (int c = 0; c < 4; ++c) {
-          const float mine = h ? u[4 + r][c] : u[r][c];
-          const float send = h ? u[r][c] : u[4 + r][c];
-          const float got = __shfl_xor_sync(0xffffffffu, send, 1);
-          ur[r][c] = h ? got : mine;
-          ur[r][4 + c] = h ? mine : got;
-        }
-      float o[4][8];
-#pragma unroll
-      for (int r = 0; r < 4; ++r)
-#pragma unroll
-        for (int c = 0; c < 8; ++c) o[r][c] = 0.0f;
-#pragma unroll
-      for (int jj = 0; jj < 8; ++jj) {
-        const float4 lo = ql[2 * jj], hi = ql[2 * jj + 1];
-        const float qr[8] = {lo.x, lo.y, lo.z, lo.w, hi.x, hi.y, hi.z, hi.w};
-#pragma unroll
-        for (int r = 0; r < 4; ++r)
-#pragma unroll
-          for (int c = 0; c < 8; ++c) o[r][c] = fmaf(ur[r][jj], qr[c], o[r][c]);
-      }
-      if (valid) {
-        const int rbh = h ? rb1 : rb0;
-        const int cb0 = pair_i[l], cb1 = pair_j[l];
-#pragma unroll
-        for (int y = 0; y < 2; ++y) {
-          float b4[4][4];
-#pragma unroll
-          for (int r = 0; r < 4; ++r)
-#pragma unroll
-            for (int c = 0; c < 4; ++c) b4[r][c] = o[r][4 * y + c];
-          storeBlock(tiles, tri, rbh, y ? cb1 : cb0, b4);
-        }
-      }
+      superTileHalf(tiles, SharedTri{tri}, qk, ql, rb0, rb1, pair_i[l], pair_j[l], h, valid);
     }
     __syncthreads();
   }
@@ -669,13 +288,6 @@ __host__ __device__ __forceinline__ size_t replaySmemBytes(int max_n, int rows) 
          2 * static_cast<size_t>(P) * kQF * sizeof(float);
 }
 
-// 16-byte asynchronous global -> shared copies (cp.async, L2 only).
-__device__ __forceinline__ void copyAsync16(void *smem, const void *gmem) {
-  const unsigned dst = static_cast<unsigned>(__cvta_generic_to_shared(smem));
-  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(dst), "l"(gmem) : "memory");
-}
-__device__ __forceinline__ void copyAsyncCommit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
-__device__ __forceinline__ void copyAsyncWaitAll() { asm volatile("cp.async.wait_group 0;\n" ::: "memory"); }
 
 // Replays one logged sweep onto `rows` rows of V: V <- V Q_k on the column
 // blocks (I_k, J_k) of every pair, round by round (the V update of
@@ -772,6 +384,16 @@ __global__ void identityKernel(float *v, const int64_t *a_offset, const int32_t 
       out[k] = r == c ? 1.0f : 0.0f;
     }
   }
+}
+
+// Final state of a matrix solved by the grid kernels.
+__global__ void gridStateKernel(JacobiState *st, int sweeps, double ratio, double norm2) {
+  st->norm2 = norm2;
+  st->off_ratio = ratio;
+  st->sweeps = sweeps;
+  st->done = 1;
+  st->logged[0] = 0;
+  st->logged[1] = 0;
 }
 
 __global__ void jacobiReportKernel(const JacobiState *state, int count, int32_t *sweeps,
@@ -941,6 +563,7 @@ struct JacobiPlan {
   // the work lists, `rows` rows each, `smem` bytes of shared memory.
   struct ReplayGroup { int first; int count; int rows; size_t smem; };
   std::vector<ReplayGroup> replays;
+  std::vector<int> grid_ids;  // matrices solved by the grid kernels
   void *device = nullptr;
 };
 
@@ -953,17 +576,29 @@ JacobiPlan *planFor(msq_ctx *ctx, const DeviceBatch *b) {
   plan->device_id = ctx->device;
   plan->key = b->key;
   plan->count = b->count;
-  const int count = b->count;
-  std::vector<int64_t> t_off(count), l_off(count);
-  for (int i = 0; i < count; ++i) {
-    const int m = padded8(b->host_n[i]), nb = m / 4, P = nb / 2;
+  const int total = b->count;
+  // Routing: a matrix above kGridMinOrder, or above 256 when at most
+  // kGridFewLarge such matrices are in the batch (too few to fill the SMs one
+  // CTA each), is solved by the grid kernels with every SM; the rest by the
+  // batched kernels.
+  int large = 0;
+  for (int i = 0; i < total; ++i) large += b->host_n[i] > 256;
+  std::vector<int32_t> ids;
+  std::vector<int64_t> t_off(total, 0), l_off(total, 0);
+  for (int i = 0; i < total; ++i) {
+    const int n = b->host_n[i];
+    if (n > kGridMinOrder || (n > 256 && large <= kGridFewLarge)) {
+      plan->grid_ids.push_back(i);
+      continue;
+    }
+    ids.push_back(i);
+    const int m = padded8(n), nb = m / 4, P = nb / 2;
     t_off[i] = plan->tile_total;
     plan->tile_total += static_cast<int64_t>(nb) * (nb + 1) / 2 * kTileF;
     l_off[i] = plan->log_total;
     plan->log_total += static_cast<int64_t>(nb - 1) * P * kQF;
   }
-  std::vector<int32_t> ids(count);
-  for (int i = 0; i < count; ++i) ids[i] = i;
+  const int count = static_cast<int>(ids.size());
   // buckets by size class, largest class first
   std::stable_sort(ids.begin(), ids.end(), [&](int x, int y) {
     const int cx = sizeClass(b->host_n[x]), cy = sizeClass(b->host_n[y]);
@@ -1000,7 +635,7 @@ JacobiPlan *planFor(msq_ctx *ctx, const DeviceBatch *b) {
                              replaySmemBytes(max_n, rows)});
   }
   plan->work_count = static_cast<int>(wm.size());
-  const size_t bytes = 2 * count * sizeof(int64_t) + count * sizeof(int32_t) +
+  const size_t bytes = 2 * total * sizeof(int64_t) + total * sizeof(int32_t) +
                        2 * wm.size() * sizeof(int32_t) + 64;
   char *dev = nullptr;
   if (cudaCheck(ctx, cudaMalloc(&dev, bytes), "jacobi plan alloc") != MSQ_OK) {
@@ -1009,13 +644,13 @@ JacobiPlan *planFor(msq_ctx *ctx, const DeviceBatch *b) {
   }
   plan->device = dev;
   plan->t_offset = reinterpret_cast<int64_t *>(dev);
-  plan->log_offset = plan->t_offset + count;
-  plan->order = reinterpret_cast<int32_t *>(plan->log_offset + count);
-  plan->work_matrix = plan->order + count;
+  plan->log_offset = plan->t_offset + total;
+  plan->order = reinterpret_cast<int32_t *>(plan->log_offset + total);
+  plan->work_matrix = plan->order + total;
   plan->work_row = plan->work_matrix + wm.size();
-  cudaMemcpy(plan->t_offset, t_off.data(), count * sizeof(int64_t), cudaMemcpyHostToDevice);
-  cudaMemcpy(plan->log_offset, l_off.data(), count * sizeof(int64_t), cudaMemcpyHostToDevice);
-  cudaMemcpy(plan->order, ids.data(), count * sizeof(int32_t), cudaMemcpyHostToDevice);
+  cudaMemcpy(plan->t_offset, t_off.data(), total * sizeof(int64_t), cudaMemcpyHostToDevice);
+  cudaMemcpy(plan->log_offset, l_off.data(), total * sizeof(int64_t), cudaMemcpyHostToDevice);
+  if (count > 0) cudaMemcpy(plan->order, ids.data(), count * sizeof(int32_t), cudaMemcpyHostToDevice);
   cudaMemcpy(plan->work_matrix, wm.data(), wm.size() * sizeof(int32_t), cudaMemcpyHostToDevice);
   cudaMemcpy(plan->work_row, wr.data(), wr.size() * sizeof(int32_t), cudaMemcpyHostToDevice);
   if (g_plans.size() >= 8) {
@@ -1049,11 +684,10 @@ int jacobiEnqueue(msq_ctx *ctx, const DeviceBatch *b, float *matrices, float *ve
                   float *eigenvalues, double tolerance, int max_sweeps, int32_t *sweeps_done,
                   float *off_ratio) {
   if (b->max_n > kMaxOrder) {
-    return setError(ctx, MSQ_ERR_UNSUPPORTED, "jacobi: order above 2048 is not supported");
+    return setError(ctx, MSQ_ERR_UNSUPPORTED, "jacobi: order above 16384 is not supported");
   }
   JacobiPlan *plan = planFor(ctx, b);
   if (plan == nullptr) return MSQ_ERR_CUDA;
-  if (plan->buckets.empty()) return MSQ_OK;
   const size_t state_bytes = (b->count * sizeof(JacobiState) + 255) & ~size_t(255);
   const size_t tile_bytes = (plan->tile_total * sizeof(float) + 255) & ~size_t(255);
   // Two log buffers (sweep parity) so sweep k+1 overlaps the replay of k.
@@ -1172,6 +806,17 @@ int jacobiEnqueue(msq_ctx *ctx, const DeviceBatch *b, float *matrices, float *ve
       replay_done[parity] = syncEvent(ctx);
       MSQ_TRY(cudaCheck(ctx, cudaEventRecord(replay_done[parity], rs), "event record"));
     }
+  }
+  // Large matrices: the grid kernels on the context's stream, overlapping the
+  // batched sweeps still running on the internal streams.
+  for (const int gi : plan->grid_ids) {
+    int sweeps = 0;
+    double ratio = 0.0, norm2 = 0.0;
+    MSQ_TRY(gridJacobiSolve(ctx, matrices + b->host_offset[gi], vectors + b->host_offset[gi],
+                            eigenvalues + b->host_eig_offset[gi], b->host_n[gi], tolerance, max_sweeps,
+                            &sweeps, &ratio, &norm2));
+    gridStateKernel<<<1, 1, 0, ctx->stream>>>(args.state + gi, sweeps, ratio, norm2);
+    MSQ_TRY(launched(ctx, "jacobi grid state"));
   }
   for (int i = 0; i < sweep_streams; ++i) MSQ_TRY(streamWait(ctx, ctx->stream, ss[i]));
   MSQ_TRY(streamWait(ctx, ctx->stream, rs));

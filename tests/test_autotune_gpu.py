@@ -18,8 +18,10 @@ def _solve(ctx, msq, b, a_host):
 
 
 def test_tuning_keeps_results_bit_identical(ctx, msq):
-    orders = [12, 30, 60, 100, 200, 300, 400]  # one matrix per size class
-    mats = [O.spd_loguniform(n, 1e2, seed=n) for n in orders]
+    # one matrix in each small size class and nine of order 300 (with more
+    # than eight matrices above 256 these stay on the batched kernels)
+    orders = [12, 30, 60, 100, 200] + [300] * 9
+    mats = [O.spd_loguniform(n, 1e2, seed=i) for i, n in enumerate(orders)]
     b = msq.Batch.from_orders(orders)
     packed = b.pack(mats)
     msq.lib().msq_autotune_reset(1)
@@ -32,8 +34,8 @@ def test_tuning_keeps_results_bit_identical(ctx, msq):
     lines = [l for l in report.splitlines() if l]
     assert len(lines) == 9
     tuned = [l for l in lines if "untuned" not in l]
-    # every class present in the batch (and the single-candidate class) is tuned
-    assert len(tuned) >= 7, report
+    # every class present in the batch (classes n <= 16 .. n <= 328) is tuned
+    assert len(tuned) >= 6, report
 
 
 def test_tuning_disabled_uses_defaults(ctx, msq):

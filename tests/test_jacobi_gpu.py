@@ -98,3 +98,53 @@ def test_sweep_budget_and_tolerance(ctx, msq):
     assert sweeps[0] == 2 and off[0] > 1e-7
     _, _, sweeps, off, _ = _run(ctx, msq, [a], tol=1e-2, max_sweeps=15)
     assert off[0] <= 1e-2 and sweeps[0] < 8
+
+
+# ---- grid kernels (every SM on one matrix) --------------------------------
+
+@pytest.mark.parametrize("n", [300, 400, 1040])
+def test_grid_path_bit_exact_against_cpu_restatement(ctx, msq, n):
+    """A lone matrix above 256 (or any above 1024) is solved by the grid
+    kernels: same rotations, same roundings as the CPU restatement."""
+    a = O.wishart(n, seed=n)
+    sweeps_fixed = 2 if n < 1000 else 1
+    w_o, v_o, sw_o, _, a_o = O.jacobi_blocked(a, 0.0, sweeps_fixed, with_matrix=True)
+    vs, ws, sweeps, off, af = _run(ctx, msq, [a], tol=0.0, max_sweeps=sweeps_fixed)
+    assert int(sweeps[0]) == sweeps_fixed
+    assert np.array_equal(ws[0].astype(np.float32), w_o)
+    assert np.array_equal(vs[0], v_o)
+    assert np.array_equal(af[0], a_o)
+
+
+def test_grid_path_equals_batched_path(ctx, msq):
+    """Nine matrices above 256 go to the batched kernels, one alone to the
+    grid kernels: identical bits for the same matrix."""
+    mats = [O.spd_loguniform(300, 1e3, seed=s) for s in range(9)]
+    vs_b, ws_b, sw_b, _, af_b = _run(ctx, msq, mats, tol=0.0, max_sweeps=3)
+    vs_g, ws_g, sw_g, _, af_g = _run(ctx, msq, mats[:1], tol=0.0, max_sweeps=3)
+    assert np.array_equal(ws_b[0], ws_g[0])
+    assert np.array_equal(vs_b[0], vs_g[0])
+    assert np.array_equal(af_b[0], af_g[0])
+
+
+@pytest.mark.parametrize("n", [2048, 4096])
+def test_grid_path_large_orders(ctx, msq, n):
+    a = O.spd_loguniform(n, 1e4, seed=n)
+    vs, ws, sweeps, off, _ = _run(ctx, msq, [a], tol=1e-7, max_sweeps=20)
+    ref = np.linalg.eigvalsh(a)
+    assert off[0] <= 1e-7 and int(sweeps[0]) < 20
+    np.testing.assert_allclose(np.sort(ws[0]), ref, rtol=0, atol=3 * n * U32 * np.abs(ref).max())
+    v = vs[0].astype(np.float64)
+    assert np.linalg.norm(a @ v - v * ws[0]) / np.linalg.norm(a) < n * U32
+    assert np.abs(v.T @ v - np.eye(n)).max() < 1e-4
+
+
+def test_batched_global_tiles_bit_exact(ctx, msq):
+    """Nine matrices of order 400 stay on the batched kernels (tiles in the
+    global workspace): bit-identical to the CPU restatement."""
+    mats = [O.wishart(400, seed=s) for s in range(9)]
+    w_o, v_o, _, _, a_o = O.jacobi_blocked(mats[0], 0.0, 2, with_matrix=True)
+    vs, ws, sweeps, off, af = _run(ctx, msq, mats, tol=0.0, max_sweeps=2)
+    assert np.array_equal(ws[0].astype(np.float32), w_o)
+    assert np.array_equal(vs[0], v_o)
+    assert np.array_equal(af[0], a_o)
