@@ -51,7 +51,7 @@ def _tiles_fit_shared(n: int) -> bool:
     m = (n + 7) // 8 * 8
     nb, p = m // 4, m // 8
     head = (32 * 8 + (nb + 1 + 2 * p) * 4 + 15) // 16 * 16
-    return head + p * 68 * 4 + nb * (nb + 1) // 2 * 16 * 4 <= 227 * 1024
+    return head + p * 68 * 4 + nb * (nb + 1) // 2 * 16 * 4 <= 227 * 1024 - 256
 
 
 def sweep_class(n: int) -> int:
@@ -336,7 +336,11 @@ def main():
         plan_source = "learned selector (" + ", ".join(
             f"{('fp32+1' if k < 0 else '%s+%d' % (('bf16', 'fp8', 'mxfp4')[sel.PLANS[k][0] - 1], sel.PLANS[k][1]))}:{int(np.sum(choice == k))}"
             for k in sorted(set(choice.tolist()))) + ")"
-    fp32_plan = [msq.plan(msq.PLAN_FP32, 0, 1e-7, 15)] * batch.count
+    # the plain FP32 path: Jacobi to 1e-7, FP32 reconstruction and one FP32
+    # Sylvester correction (the reference's plain method corrects until the
+    # tolerance is met, src/accelerate_backend.cpp:803-1091; FP32 Jacobi +
+    # reconstruction alone misses 1e-5 on a quarter of this batch)
+    fp32_plan = [msq.plan(msq.PLAN_FP32, 1, 1e-7, 15)] * batch.count
     root = torch.empty_like(a)
 
     def barrier():
@@ -364,7 +368,7 @@ def main():
         return ms, statistics.mean(accepted), ctx.launches - l0, res, rows
 
     # plain FP32 path (denominator)
-    ms_plain, acc_plain, _, res_plain, _ = timed(fp32_plan, max(1, args.steps // 2), 1)
+    ms_plain, acc_plain, _, res_plain, _ = timed(fp32_plan, max(1, args.steps // 2), 2)
     # low-bit + Sylvester path (headline), clocks sampled while it runs
     with ClockSampler(local) as clocks:
         ms, acc, launches, res, _ = timed(low_plan, args.steps, args.warmup, False)
@@ -491,7 +495,8 @@ def main():
         "clocks": clocks.summary(),
         "gpu_launches": launches,
         "plain_fp32": {"value": acc_plain * world / (ms_plain / 1e3), "ms_per_step": ms_plain,
-                       "accepted": acc_plain},
+                       "accepted": acc_plain, "fallback": int(sum(r.fallback for r in res_plain)),
+                       "plan": "FP32: Jacobi to 1e-7, FP32 reconstruction, one FP32 Sylvester sweep"},
         "speedup_vs_plain_fp32": (value / (acc_plain * world / (ms_plain / 1e3))) if acc_plain else None,
         "accepted": acc, "fallback": int(fallback),
         "error_vs_fp64": {"p50": float(np.percentile(errs, 50)), "p99": float(np.percentile(errs, 99)),

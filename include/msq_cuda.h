@@ -149,9 +149,9 @@ int msq_autotune_reset(int enable);
  * [0, 64] return MSQ_ERR_INVALID_ARGUMENT before anything is launched.
  * The first call on a device (the current device) looks up the array's
  * device address once; make that first call before capturing any stream.
- * Each call first resets, with a small kernel on `stream`, the part of the
- * array that must start at zero (the sweep state); everything else is
- * written before it is read.  All calls on one device share the one array:
+ * Each call first resets, with a small kernel on `stream`, the parts of the
+ * array that must start at zero (the sweep state and a status word);
+ * everything else is written before it is read.  All calls on one device share the one array:
  * calls that overlap on the GPU (on two streams, or from two threads) race
  * on it and corrupt each other's results, so issue them on one stream.
  * `stream` is a cudaStream_t (NULL: the default stream); `matrix` is

@@ -34,6 +34,7 @@
 
 #include <algorithm>
 #include <array>
+#include <atomic>
 #include <cstdio>
 #include <cstring>
 #include <map>
@@ -45,6 +46,8 @@ namespace msq {
 namespace {
 
 constexpr size_t kSmemLimit = 227 * 1024;
+// the sweep kernel also holds a small static shared block (its mbarrier)
+constexpr size_t kSweepSmemLimit = kSmemLimit - 256;
 constexpr int kMaxOrder = 16384;    // grid kernels; the batched ones see n <= 1024
 constexpr int kGridMinOrder = 1024;
 constexpr int kGridFewLarge = 8;
@@ -67,6 +70,7 @@ struct JacobiArgs {
   int max_sweeps;
   int first;                 // 1 on the first launch (load A, set norm)
   int parity;                // log buffer of this sweep (log points at it)
+  int *status;               // device status word (bounded waits)
 };
 
 __host__ __device__ __forceinline__ size_t sweepSmemLayout(int n, bool with_tiles, size_t *q_off,
@@ -86,6 +90,7 @@ template <bool kSmem>
 __global__ void __launch_bounds__(kSweepThreadsMax)
 jacobiSweepKernel(JacobiArgs args) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
+  __shared__ __align__(8) uint64_t tile_bar;
   const int mi = args.order[blockIdx.x];
   const int n = args.n[mi];
   const int m = padded8(n), nb = m / 4, P = nb / 2;
@@ -127,8 +132,13 @@ jacobiSweepKernel(JacobiArgs args) {
       }
     }
   } else if (kSmem) {
-    for (int k = threadIdx.x; k < tile_floats / 4; k += blockDim.x) {
-      reinterpret_cast<float4 *>(tiles)[k] = reinterpret_cast<const float4 *>(gtiles)[k];
+    // the packed tiles kept between sweeps: one TMA bulk copy into shared
+    // memory (bounded wait; on expiry the launch reports and does nothing)
+    if (threadIdx.x == 0) bulkLoadTiles(tiles, gtiles, tile_floats * sizeof(float), &tile_bar);
+    __syncthreads();
+    if (!bulkWaitTiles(&tile_bar)) {
+      if (threadIdx.x == 0) atomicExch(args.status, kStatusMbarrierTimeout);
+      return;
     }
   }
   __syncthreads();
@@ -254,9 +264,10 @@ jacobiSweepKernel(JacobiArgs args) {
     __syncthreads();
   }
   if (kSmem) {
-    for (int k = threadIdx.x; k < tile_floats / 4; k += blockDim.x) {
-      reinterpret_cast<float4 *>(gtiles)[k] = reinterpret_cast<const float4 *>(tiles)[k];
-    }
+    // tiles back to the workspace: one TMA bulk copy
+    fenceSharedToAsync();
+    __syncthreads();
+    if (threadIdx.x == 0) bulkStoreTiles(gtiles, tiles, tile_floats * sizeof(float));
   }
   if (threadIdx.x == 0) {
     st.norm2 = norm2;
@@ -416,7 +427,7 @@ int threadsFor(int n) {
 
 bool fitsSmem(int n) {
   size_t q_off, tile_off;
-  return sweepSmemLayout(n, true, &q_off, &tile_off) <= kSmemLimit;
+  return sweepSmemLayout(n, true, &q_off, &tile_off) <= kSweepSmemLimit;
 }
 
 // Rows of V per replay CTA for matrices up to order max_n: the whole matrix
@@ -662,18 +673,22 @@ JacobiPlan *planFor(msq_ctx *ctx, const DeviceBatch *b) {
   return plan;
 }
 
+// Opt-in shared memory sizes, set once per device (a bit per device).
 int setKernelAttributes() {
-  static bool done = false;
-  if (done) return MSQ_OK;
+  static std::atomic<uint64_t> done_mask{0};
+  int device = 0;
+  if (cudaGetDevice(&device) != cudaSuccess || device < 0 || device >= 64) return MSQ_ERR_CUDA;
+  const uint64_t bit = uint64_t{1} << device;
+  if (done_mask.load() & bit) return MSQ_OK;
   if (cudaFuncSetAttribute(jacobiSweepKernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                           static_cast<int>(kSmemLimit)) != cudaSuccess ||
+                           static_cast<int>(kSweepSmemLimit)) != cudaSuccess ||
       cudaFuncSetAttribute(jacobiSweepKernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                           static_cast<int>(kSmemLimit)) != cudaSuccess ||
+                           static_cast<int>(kSweepSmemLimit)) != cudaSuccess ||
       cudaFuncSetAttribute(jacobiReplayKernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                            static_cast<int>(kSmemLimit)) != cudaSuccess) {
     return MSQ_ERR_CUDA;
   }
-  done = true;
+  done_mask.fetch_or(bit);
   return MSQ_OK;
 }
 
@@ -708,6 +723,7 @@ int jacobiEnqueue(msq_ctx *ctx, const DeviceBatch *b, float *matrices, float *ve
   args.eigenvalues = eigenvalues;
   args.tol = tolerance;
   args.max_sweeps = max_sweeps;
+  args.status = ctx->d_status;
   MSQ_TRY(cudaCheck(ctx, cudaMemsetAsync(args.state, 0, state_bytes, ctx->stream), "state reset"));
   {
     dim3 grid(64, std::min(b->count, 65535));
@@ -911,6 +927,7 @@ constexpr int kNoAllocCtas = (kNoAllocOrder + kNoAllocRowsPerCta - 1) / kNoAlloc
 
 struct NoAllocScratch {
   JacobiState state[1];
+  int status[1];  // bounded-wait status word of the sweep kernel
   int32_t n[1];
   int32_t order[1];
   int64_t a_offset[1];  // all offsets are zero: one matrix
@@ -930,12 +947,14 @@ static __device__ __align__(256) unsigned char g_noalloc_scratch[sizeof(NoAllocS
 // the symbol itself: on the host it names a stand-in, not device memory.
 NoAllocScratch *g_noalloc_address[64] = {};
 
-// Resets what must start at zero (the sweep state) and writes the one-matrix
-// layout tables; the tiles and the log are fully written before being read.
+// Resets what must start at zero (the sweep state and the kernels' status
+// word) and writes the one-matrix layout tables; the tiles and the log are
+// fully written before being read.
 __global__ void noAllocSetupKernel(NoAllocScratch *s, int n) {
   const int t = threadIdx.x;
   if (t == 0) {
     s->state[0] = JacobiState{};
+    s->status[0] = 0;
     s->n[0] = n;
     s->order[0] = 0;
     s->a_offset[0] = 0;
@@ -990,6 +1009,7 @@ extern "C" int msq_jacobi_noalloc(float *matrix, float *vectors, float *eigenval
   args.order = s->order;
   args.tol = tolerance;
   args.max_sweeps = max_sweeps;
+  args.status = s->status;
   const bool smem = fitsSmem(n);
   size_t q_off, tile_off;
   const size_t sweep_smem = sweepSmemLayout(n, smem, &q_off, &tile_off);

@@ -437,6 +437,58 @@ __device__ __forceinline__ void superTileHalf(float *tiles, TileOf tileOf, const
   }
 }
 
+// TMA bulk copies (cp.async.bulk) of a contiguous block between global and
+// shared memory; both addresses 16-byte aligned, size a multiple of 16.  The
+// load completes on an mbarrier (expect_tx); the wait is bounded.
+constexpr long long kTileWaitLimit = 1ll << 26;
+
+__device__ __forceinline__ uint32_t smemAddr(const void *p) {
+  return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+
+__device__ __forceinline__ void bulkLoadTiles(void *smem, const void *gmem, uint32_t bytes,
+                                              uint64_t *bar) {
+  const uint32_t b = smemAddr(bar);
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(b) : "memory");
+  asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(b), "r"(bytes) : "memory");
+  asm volatile(
+      "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+          smemAddr(smem)),
+      "l"(gmem), "r"(bytes), "r"(b)
+      : "memory");
+}
+
+// True once phase 0 of the barrier completed; false after kTileWaitLimit polls.
+__device__ __forceinline__ bool bulkWaitTiles(uint64_t *bar) {
+  const uint32_t b = smemAddr(bar);
+  for (long long i = 0; i < kTileWaitLimit; ++i) {
+    uint32_t done;
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], 0;\n"
+        " selp.u32 %0, 1, 0, p;\n}\n"
+        : "=r"(done)
+        : "r"(b)
+        : "memory");
+    if (done) return true;
+  }
+  return false;
+}
+
+// Store: every writer thread fences its shared writes to the async proxy and
+// the CTA synchronises before one thread issues the copy and waits for it.
+__device__ __forceinline__ void fenceSharedToAsync() {
+  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+}
+
+__device__ __forceinline__ void bulkStoreTiles(void *gmem, const void *smem, uint32_t bytes) {
+  asm volatile("cp.async.bulk.global.shared::cta.bulk_group [%0], [%1], %2;" ::"l"(gmem),
+               "r"(smemAddr(smem)), "r"(bytes)
+               : "memory");
+  asm volatile("cp.async.bulk.commit_group;" ::: "memory");
+  asm volatile("cp.async.bulk.wait_group 0;" ::: "memory");
+}
+
 // 16-byte asynchronous global -> shared copies (cp.async, L2 only).
 __device__ __forceinline__ void copyAsync16(void *smem, const void *gmem) {
   const unsigned dst = static_cast<unsigned>(__cvta_generic_to_shared(smem));

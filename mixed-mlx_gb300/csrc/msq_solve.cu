@@ -193,14 +193,18 @@ int runGroup(msq_ctx *ctx, const float *a_user, const int32_t *n_user,
   // Corrections use the FP32 stable basis V, as the reference's fp32_frozen
   // stage does (src/metal_solver.cpp:304-325).  The plain FP32 plan runs its
   // GEMMs and residuals on the CUDA cores in FP32 / float-float; low-bit
-  // plans run the correction GEMMs and the residuals between sweeps on the
-  // tensor cores (split BF16, FP32 accumulation).  The residual that decides
-  // acceptance is always the float-float one.
+  // plans run the correction GEMMs on the tensor cores (split BF16, FP32
+  // accumulation) and the residual of the low-bit X0 too.  A tensor-core
+  // residual carries the FP32 accumulation error of an n-long sum (about
+  // sqrt(n) 2^-24 of ||A||): negligible against the quantization residual of
+  // X0, not against the residual after a correction, which a further
+  // correction could not push below it.  So every residual after the first
+  // correction, and the one that decides acceptance, are float-float.
   const bool low_bit = g.plan.format != MSQ_PLAN_FP32;
   const int gemm_format = low_bit ? MSQ_FMT_BF16 : MSQ_FMT_FP32;
-  auto residual = [&](bool accepting) {
-    return low_bit && !accepting ? residualTc(ctx, b, A, Xh, Xl, R, norms)
-                                 : residualFF(ctx, b, A, Xh, Xl, R, norms);
+  auto residual = [&](bool accurate) {
+    return low_bit && !accurate ? residualTc(ctx, b, A, Xh, Xl, R, norms)
+                                : residualFF(ctx, b, A, Xh, Xl, R, norms);
   };
   MSQ_TRY(residual(g.plan.sweeps == 0));
   MSQ_TRY(cudaCheck(ctx, cudaMemcpyAsync(host_norms.data(), norms, 2 * count * sizeof(double),
@@ -211,7 +215,7 @@ int runGroup(msq_ctx *ctx, const float *a_user, const int32_t *n_user,
       initial_res[g.members[i]] = std::sqrt(host_norms[2 * i] / host_norms[2 * i + 1]);
   for (int s = 0; s < g.plan.sweeps; ++s) {
     MSQ_TRY(sylvesterSweep(ctx, b, gemm_format, V, lam, R, Xh, Xl, F, W1));
-    MSQ_TRY(residual(s + 1 == g.plan.sweeps));
+    MSQ_TRY(residual(true));
   }
   if (g.plan.sweeps > 0) {
     MSQ_TRY(cudaCheck(ctx, cudaMemcpyAsync(host_norms.data(), norms, 2 * count * sizeof(double),
