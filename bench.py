@@ -69,6 +69,25 @@ def workload_orders(count: int, seed: int) -> np.ndarray:
     return np.clip(n, N_LO, N_HI)
 
 
+def rank_shard(count: int, rank: int):
+    """Weak scaling: rank r solves its own seeded batch of `count` matrices
+    (orders seed 1234 + r, matrix seed 99 + r); no data crosses ranks."""
+    return workload_orders(count, 1234 + rank), 99 + rank
+
+
+def whole_job(accepted: float, ms: float, world: int, device) -> tuple:
+    """Sum of accepted solves over the ranks and the slowest rank's time."""
+    if world == 1:
+        return float(accepted), float(ms)
+    import torch
+    import torch.distributed as dist
+    acc = torch.tensor([float(accepted)], dtype=torch.float64, device=device)
+    t = torch.tensor([float(ms)], dtype=torch.float64, device=device)
+    dist.all_reduce(acc, op=dist.ReduceOp.SUM)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(acc.item()), float(t.item())
+
+
 def make_batch(msq, torch, orders, seed, device):
     """Wishart matrices generated on the GPU (FP64), stored FP32, packed."""
     batch = msq.Batch.from_orders(orders)
@@ -134,60 +153,61 @@ class ClockSampler:
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
-def cpu_baseline(oracle, mats, budget_s: float) -> dict:
-    """The reference's CPU plain method (runAccelerateCase restated in the
-    oracle) on a stratified sample of the batch, bounded to ~budget_s."""
-    order = np.argsort([m.shape[0] for m in mats])
-    stride = max(1, len(order) // 64)
-    sample = order[::stride]
-    rng = np.random.default_rng(0)
-    rng.shuffle(sample)
-    done, t_used, ok = 0, 0.0, 0
+def stratified(orders, k: int = 64) -> np.ndarray:
+    """k matrices of the batch spread evenly over the sorted orders."""
+    order = np.argsort(orders, kind="stable")
+    return order[:: max(1, len(order) // k)][:k]
+
+
+def time_plain(oracle, mats: dict, sample, budget_s: float):
+    """Times the reference's CPU plain method (runAccelerateCase restated in
+    the oracle) on `sample`, stopping once budget_s is used.  Returns
+    (seconds per solve, fraction meeting the tolerance, solves timed)."""
+    done, ok, t_used = 0, 0, 0.0
     for idx in sample:
         t0 = time.perf_counter()
-        root, hist = oracle.plain_method(mats[idx], 12, TOL)
+        root, hist = oracle.plain_method(mats[int(idx)], 12, TOL)
         t_used += time.perf_counter() - t0
         done += 1
         ok += hist[-1] <= TOL
         if t_used > budget_s:
             break
-    # scale the stratified sample's mean time to the whole batch
-    per_solve = t_used / done
+    return t_used / done, ok / done, done
+
+
+def cpu_baseline(oracle, mats, budget_s: float) -> dict:
+    """The reference's CPU plain method on a stratified sample of the batch
+    (every order range in proportion), bounded to ~budget_s."""
+    sample = stratified([m.shape[0] for m in mats])
+    per_solve, ok, done = time_plain(oracle, dict(enumerate(mats)), sample, budget_s)
     cores = os.cpu_count() or 1
-    return {"value": (ok / done) / per_solve, "unit": "solves/s", "cores": cores,
-            "kind": "port",
+    return {"value": ok / per_solve, "unit": "solves/s", "cores": cores, "kind": "port",
             "sample": f"{done} of {len(mats)} matrices (stratified by n), "
-                      f"{t_used:.1f}s, OpenBLAS threads={os.environ.get('OPENBLAS_NUM_THREADS', cores)}"}
+                      f"{per_solve * done:.1f}s, OpenBLAS threads={os.environ.get('OPENBLAS_NUM_THREADS', cores)}"}
 
 
 def run_reference(args):
     """--impl reference: the reference's CPU path (oracle port of
     runAccelerateCase; the reference's own build is x86-only here) on the
-    host cores, same metric and workload, bounded samples per step."""
+    host cores, same metric and workload: each step times a stratified
+    sample of 64 of the 4096 matrices (bounded to ~20 s)."""
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
         return
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import oracle as O
     orders = workload_orders(COUNT, 1234)
-    rng = np.random.default_rng(7)
-    pick = rng.choice(COUNT, 48, replace=False)
-    mats = {int(i): O.wishart(int(orders[i]), seed=int(i)) for i in pick}
+    sample = stratified(orders)
+    mats = {int(i): O.wishart(int(orders[i]), seed=int(i)) for i in sample}
     for _ in range(args.warmup):
-        O.plain_method(mats[int(pick[0])], 12, TOL)
-    times, oks = [], 0
-    for step in range(args.steps):
-        t0 = time.perf_counter()
-        done = 0
-        for i in pick:
-            root, hist = O.plain_method(mats[int(i)], 12, TOL)
-            oks += hist[-1] <= TOL
-            done += 1
-            if time.perf_counter() - t0 > 20:
-                break
-        times.append((time.perf_counter() - t0) / done)
-    per_solve = statistics.mean(times)
-    value = 1.0 / per_solve
+        O.plain_method(mats[int(sample[0])], 12, TOL)
+    per, oks = [], []
+    for _ in range(args.steps):
+        p, ok, _ = time_plain(O, mats, sample, 20.0)
+        per.append(p)
+        oks.append(ok)
+    per_solve = statistics.mean(per)
+    value = statistics.mean(oks) / per_solve
     cores = os.cpu_count() or 1
     line = {"metric": METRIC, "value": value, "unit": "solves/s", "n_gpus": args.gpus,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": per_solve * COUNT * 1e3,
@@ -195,7 +215,8 @@ def run_reference(args):
             "data": "synthetic", "impl": "reference",
             "config": {"workload": f"{COUNT} Wishart SPD (m=2n), n log-uniform [{N_LO},{N_HI}], tol 1e-5"},
             "cpu_baseline": {"value": value, "unit": "solves/s", "cores": cores, "kind": "port",
-                             "sample": f"48 random matrices of the batch per step, <=20 s per step"},
+                             "sample": f"{len(sample)} of {COUNT} matrices per step (stratified by n), "
+                                       f"<=20 s per step"},
             "e2e": {"value": value, "unit": "solves/s", "h2d_bytes_per_step": 0,
                     "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
@@ -270,6 +291,71 @@ def run_codec(args):
     print(json.dumps(line), flush=True)
 
 
+def run_selector(args):
+    """Learned plan selection on held-out seeds: SPD matrices of the three
+    spectrum families, n log-uniform in [64, 1024], condition log-uniform in
+    [1e1, 1e8]; each matrix gets the cheapest plan the MLP predicts to meet
+    1e-5 (FP32 fallback on a miss); compared with every matrix on the plain
+    FP32 path."""
+    import torch
+    msq = importlib.import_module("mixed-mlx_gb300")
+    sel = importlib.import_module("mixed-mlx_gb300.selector")
+    weights = os.path.join(ROOT, "mixed-mlx_gb300", "selector_weights.npz")
+    if not os.path.exists(weights):
+        print(json.dumps({"metric": "selector", "unavailable": "no trained selector weights"}))
+        return
+    ctx = msq.Context(0)
+    w = np.load(weights)
+    selector = sel.Selector(msq, torch, ctx)
+    selector.params = torch.from_numpy(w["params"]).cuda()
+    selector.mean = torch.from_numpy(w["mean"]).cuda()
+    selector.std = torch.from_numpy(w["std"]).cuda()
+    selector.cost_order = [int(k) for k in w["cost_order"]]
+    count = args.count if args.count != COUNT else 2048
+    orders, mats = sel.generate(torch, count, seed=777_777, n_lo=64, n_hi=1024)
+    batch, flat = sel.pack(msq, torch, orders, mats)
+    del mats
+    choice = selector.choose(sel.features(ctx, torch, batch, flat, TOL), float(w["threshold"][0]))
+    plans = [msq.plan(msq.PLAN_FP32, 1, 1e-7, 15) if k < 0 else sel.plan_structs(msq, [int(k)])[0]
+             for k in choice]
+    fp32 = [msq.plan(msq.PLAN_FP32, 1, 1e-7, 15)] * batch.count
+    out = torch.empty_like(flat)
+
+    def timed(p):
+        for _ in range(max(1, args.warmup)):
+            ctx.solve_batched(flat, batch, p, TOL, out=out)
+        torch.cuda.synchronize()
+        s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        steps = max(1, args.steps // 2)
+        s.record()
+        for _ in range(steps):
+            _, res = ctx.solve_batched(flat, batch, p, TOL, out=out)
+        e.record()
+        torch.cuda.synchronize()
+        return s.elapsed_time(e) / steps, res
+
+    ms_sel, res_sel = timed(plans)
+    ms_fp32, res_fp32 = timed(fp32)
+    met = lambda res: sum(r.final_residual <= TOL for r in res)
+    hist = {("fp32+1" if k < 0 else "%s+%d" % (("bf16", "fp8", "mxfp4")[sel.PLANS[k][0] - 1], sel.PLANS[k][1])):
+            int(np.sum(choice == k)) for k in sorted(set(choice.tolist()))}
+    print(json.dumps({
+        "metric": "SPD sqrt solves/s at rel. residual <=1e-5 with learned plan selection (held-out seeds)",
+        "value": met(res_sel) / (ms_sel / 1e3), "unit": "solves/s", "n_gpus": 1,
+        "steps": max(1, args.steps // 2), "warmup": max(1, args.warmup), "ms_per_step": ms_sel,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "bf16",
+        "data": "synthetic (seeded Gaussian-QR spectra: log-uniform, clustered, power law)",
+        "config": {"workload": f"{batch.count} held-out SPD, n log-uniform [64,1024], cond [1e1,1e8], tol 1e-5",
+                   "selector": "MLP 16-64-64-8, trained by the library's CUDA kernels"},
+        "fp32_path": {"value": met(res_fp32) / (ms_fp32 / 1e3), "ms_per_step": ms_fp32},
+        "speedup_vs_fp32_path": (met(res_sel) / ms_sel) / max(met(res_fp32) / ms_fp32, 1e-30),
+        "accept_rate": float(np.mean([r.accepted for r in res_sel])),
+        "fallback_rate": float(np.mean([r.fallback for r in res_sel])),
+        "met_tolerance": float(met(res_sel)) / batch.count,
+        "plan_histogram": hist,
+    }), flush=True)
+
+
 def timing_report(msq, ctx) -> dict:
     import ctypes
     buf = ctypes.create_string_buffer(1 << 16)
@@ -291,15 +377,18 @@ def main():
     ap.add_argument("--sweeps", type=int, default=1)
     ap.add_argument("--jacobi-tol", type=float, default=1e-4)
     ap.add_argument("--no-cpu", action="store_true")
-    ap.add_argument("--selector", type=int, default=1,
-                    help="use the trained plan selector when its weights exist")
-    ap.add_argument("--workload", default="batched", choices=["batched", "codec"],
-                    help="codec: MXFP4 round trip of 2^26 N(0,1) values (a secondary line)")
+    ap.add_argument("--selector", type=int, default=0,
+                    help="batched workload: plans from the trained selector instead of BF16 + sweeps")
+    ap.add_argument("--workload", default="batched", choices=["batched", "codec", "selector"],
+                    help="codec: MXFP4 round trip of 2^26 N(0,1) values; selector: learned plan "
+                         "selection on held-out matrices (secondary lines)")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)
     if args.workload == "codec":
         return run_codec(args)
+    if args.workload == "selector":
+        return run_selector(args)
 
     import torch
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -314,8 +403,8 @@ def main():
     ctx = msq.Context(local)
     stream = torch.cuda.current_stream(device)
 
-    orders = workload_orders(args.count, 1234 + rank)
-    batch, a = make_batch(msq, torch, orders, 99 + rank, device)
+    orders, matrix_seed = rank_shard(args.count, rank)
+    batch, a = make_batch(msq, torch, orders, matrix_seed, device)
     torch.cuda.synchronize()
     low_plan = [msq.plan(msq.PLAN_BF16, args.sweeps, args.jacobi_tol, 15)] * batch.count
     plan_source = f"fixed BF16 + {args.sweeps} sweep(s)"
@@ -369,6 +458,8 @@ def main():
 
     # plain FP32 path (denominator)
     ms_plain, acc_plain, _, res_plain, _ = timed(fp32_plan, max(1, args.steps // 2), 2)
+    plain_all, ms_plain_max = whole_job(acc_plain, ms_plain, world, device)
+    plain_value = plain_all / (ms_plain_max / 1e3)
     # low-bit + Sylvester path (headline), clocks sampled while it runs
     with ClockSampler(local) as clocks:
         ms, acc, launches, res, _ = timed(low_plan, args.steps, args.warmup, False)
@@ -377,12 +468,9 @@ def main():
     ctx.set_concurrency(False)
     _, _, _, _, rows = timed(low_plan, PROFILE_STEPS, 0, True)
     ctx.set_concurrency(True)
-    # max over ranks
-    t = torch.tensor([ms], device=device)
-    if world > 1:
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-    ms_max = float(t.item())
-    value = acc * world / (ms_max / 1e3)
+    # whole job: solves of all ranks over the slowest rank's time
+    acc_all, ms_max = whole_job(acc, ms, world, device)
+    value = acc_all / (ms_max / 1e3)
 
     # end to end: pinned host input, H2D + solve + D2H of the roots per step
     host_in = torch.empty(batch.total, dtype=torch.float32, pin_memory=True)
@@ -392,7 +480,7 @@ def main():
     ctx.solve_batched(a, batch, low_plan, TOL, out=root)
     barrier()
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    e2e_steps = max(1, args.steps // 2)
+    e2e_steps = args.steps
     e2e_acc = []
     e0.record(stream)
     for _ in range(e2e_steps):
@@ -402,8 +490,9 @@ def main():
         e2e_acc.append(sum(r.final_residual <= TOL for r in r_e))
     e1.record(stream)
     barrier()
-    e2e_ms = e0.elapsed_time(e1) / e2e_steps
-    e2e_value = statistics.mean(e2e_acc) * world / (e2e_ms / 1e3)
+    e2e_acc_all, e2e_ms = whole_job(statistics.mean(e2e_acc), e0.elapsed_time(e1) / e2e_steps,
+                                    world, device)
+    e2e_value = e2e_acc_all / (e2e_ms / 1e3)
 
     if rank != 0:
         if world > 1:
@@ -494,10 +583,10 @@ def main():
         "cpu_baseline": cpu,
         "clocks": clocks.summary(),
         "gpu_launches": launches,
-        "plain_fp32": {"value": acc_plain * world / (ms_plain / 1e3), "ms_per_step": ms_plain,
+        "plain_fp32": {"value": plain_value, "ms_per_step": ms_plain_max,
                        "accepted": acc_plain, "fallback": int(sum(r.fallback for r in res_plain)),
                        "plan": "FP32: Jacobi to 1e-7, FP32 reconstruction, one FP32 Sylvester sweep"},
-        "speedup_vs_plain_fp32": (value / (acc_plain * world / (ms_plain / 1e3))) if acc_plain else None,
+        "speedup_vs_plain_fp32": (value / plain_value) if plain_value > 0 else None,
         "accepted": acc, "fallback": int(fallback),
         "error_vs_fp64": {"p50": float(np.percentile(errs, 50)), "p99": float(np.percentile(errs, 99)),
                           "residual_p50": float(np.percentile(resid, 50)),

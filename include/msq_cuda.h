@@ -68,6 +68,10 @@ int msq_set_stream(msq_ctx *ctx, void *stream);
  * stream before the call's later work.  enable = 0 keeps every launch on the
  * context's stream, in serial order (same results, bit for bit).          */
 int msq_set_concurrency(msq_ctx *ctx, int enable);
+/* CUDA graphs (default on): the batched Jacobi's launch sequence is captured
+ * once per plan, buffers, tolerance and launch shapes, then replayed.
+ * enable = 0 launches every kernel directly (same results, bit for bit).   */
+int msq_set_graphs(msq_ctx *ctx, int enable);
 int msq_synchronize(msq_ctx *ctx);
 /* Number of this library's kernel launches enqueued so far on `ctx`. */
 uint64_t msq_launch_count(const msq_ctx *ctx);
@@ -117,7 +121,11 @@ int msq_decode(msq_ctx *ctx, int format, const uint8_t *values,
  * eigenvector j), eigenvalues (FP32, n[i] per matrix at value offset
  * eig_offset[i] = sum of previous n), sweeps_done / off_ratio per matrix
  * (device arrays, may be NULL).  `matrices` is overwritten (the converged,
- * nearly diagonal matrix).                                                 */
+ * nearly diagonal matrix).  Orders up to 16384: a matrix above 1024, or one
+ * of at most 8 above 256 in the batch, is solved with every SM (the grid
+ * kernels; the call then synchronises the context's stream once per sweep
+ * to read the off-norm), the others one CTA each.  Results are the same
+ * bits either way.                                                        */
 int msq_jacobi_batched(msq_ctx *ctx, float *matrices, float *vectors,
                        float *eigenvalues, const int32_t *n,
                        const int64_t *offset, int count, double tolerance,

@@ -77,6 +77,7 @@ _SIGS = {
     "msq_jacobi_noalloc": (ctypes.c_int, [_P, _P, _P, ctypes.c_int, ctypes.c_double,
                                           ctypes.c_int, _P, _P, _P]),
     "msq_set_concurrency": (ctypes.c_int, [_P, ctypes.c_int]),
+    "msq_set_graphs": (ctypes.c_int, [_P, ctypes.c_int]),
     "msq_autotune_report": (ctypes.c_int, [ctypes.c_int, ctypes.c_char_p, ctypes.c_size_t]),
     "msq_autotune_reset": (ctypes.c_int, [ctypes.c_int]),
     "msq_timing_begin": (ctypes.c_int, [_P]),
@@ -205,6 +206,9 @@ class Context:
 
     def set_concurrency(self, enable: bool) -> None:
         self.check(lib().msq_set_concurrency(self.handle, int(bool(enable))), "msq_set_concurrency")
+
+    def set_graphs(self, enable: bool) -> None:
+        self.check(lib().msq_set_graphs(self.handle, int(bool(enable))), "msq_set_graphs")
 
     def synchronize(self) -> None:
         self.check(lib().msq_synchronize(self.handle), "msq_synchronize")

@@ -248,6 +248,7 @@ extern "C" void msq_destroy(msq_ctx *ctx) {
   for (int slot = 0; slot < 5; ++slot)
     if (ctx->scratch[slot] != nullptr) cudaFree(ctx->scratch[slot]);
   if (ctx->grid_exec != nullptr) cudaGraphExecDestroy(ctx->grid_exec);
+  for (auto &g : ctx->jacobi_graphs) cudaGraphExecDestroy(g.exec);
   if (ctx->grid_host != nullptr) cudaFreeHost(ctx->grid_host);
   if (ctx->d_status != nullptr) cudaFree(ctx->d_status);
   recycleTiming(ctx);
@@ -271,6 +272,12 @@ extern "C" int msq_set_stream(msq_ctx *ctx, void *stream) {
 extern "C" int msq_set_concurrency(msq_ctx *ctx, int enable) {
   if (ctx == nullptr) return MSQ_ERR_INVALID_ARGUMENT;
   ctx->concurrent = enable != 0;
+  return MSQ_OK;
+}
+
+extern "C" int msq_set_graphs(msq_ctx *ctx, int enable) {
+  if (ctx == nullptr) return MSQ_ERR_INVALID_ARGUMENT;
+  ctx->graphs = enable != 0;
   return MSQ_OK;
 }
 

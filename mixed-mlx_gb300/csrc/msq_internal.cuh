@@ -48,6 +48,28 @@ struct DeviceBatch {
   std::vector<WorkList> work_cache;  // tile work lists (msq_dense.cu)
 };
 
+// A captured batched-Jacobi launch sequence and what it was captured for.
+struct JacobiGraphKey {
+  uint64_t plan_serial, batch_key;
+  const void *batch, *a, *v, *w, *sweeps, *off, *work;
+  double tol;
+  int max_sweeps;
+  bool concurrent;
+  uint64_t shapes;
+  bool operator==(const JacobiGraphKey &o) const {
+    return plan_serial == o.plan_serial && batch_key == o.batch_key && batch == o.batch && a == o.a &&
+           v == o.v && w == o.w && sweeps == o.sweeps && off == o.off && work == o.work &&
+           tol == o.tol && max_sweeps == o.max_sweeps && concurrent == o.concurrent &&
+           shapes == o.shapes;
+  }
+};
+
+struct JacobiGraph {
+  JacobiGraphKey key;
+  cudaGraphExec_t exec;
+  uint64_t launches;  // kernel launches the graph holds
+};
+
 }  // namespace msq
 
 struct msq_ctx {
@@ -84,6 +106,9 @@ struct msq_ctx {
   // Grid Jacobi (one large matrix on all SMs): pinned off-norm readback and
   // the captured graph of one sweep, valid for order grid_n and workspace
   // grid_work.
+  // Batched Jacobi launch sequences captured as CUDA graphs (at most 8).
+  bool graphs = true;
+  std::vector<msq::JacobiGraph> jacobi_graphs;
   double *grid_host = nullptr;
   cudaGraphExec_t grid_exec = nullptr;
   int grid_n = 0;

@@ -561,6 +561,7 @@ void harvestTimings() {
 // Per-layout launch plan, kept per batch layout and device.
 struct JacobiPlan {
   uint64_t key = 0;
+  uint64_t serial = 0;  // unique per plan ever built (keys captured graphs)
   int count = 0;
   int device_id = 0;
   int64_t tile_total = 0, log_total = 0;
@@ -583,7 +584,9 @@ std::vector<JacobiPlan *> g_plans;
 JacobiPlan *planFor(msq_ctx *ctx, const DeviceBatch *b) {
   for (JacobiPlan *p : g_plans)
     if (p->key == b->key && p->count == b->count && p->device_id == ctx->device) return p;
+  static std::atomic<uint64_t> next_serial{1};
   auto *plan = new JacobiPlan;
+  plan->serial = next_serial.fetch_add(1);
   plan->device_id = ctx->device;
   plan->key = b->key;
   plan->count = b->count;
@@ -724,12 +727,6 @@ int jacobiEnqueue(msq_ctx *ctx, const DeviceBatch *b, float *matrices, float *ve
   args.tol = tolerance;
   args.max_sweeps = max_sweeps;
   args.status = ctx->d_status;
-  MSQ_TRY(cudaCheck(ctx, cudaMemsetAsync(args.state, 0, state_bytes, ctx->stream), "state reset"));
-  {
-    dim3 grid(64, std::min(b->count, 65535));
-    identityKernel<<<grid, 256, 0, ctx->stream>>>(vectors, b->offset, b->n, b->count);
-    MSQ_TRY(launched(ctx, "jacobi identity"));
-  }
   VArgs vargs{vectors, b->offset, plan->log_offset, b->n, log_base, args.state,
               plan->work_matrix, plan->work_row, 0, 0};
   // Launch shape per bucket: the tuned CTA size, or (while its class is
@@ -755,6 +752,44 @@ int jacobiEnqueue(msq_ctx *ctx, const DeviceBatch *b, float *matrices, float *ve
         }
       }
     }
+  }
+  // The batched launch sequence (no host synchronisation, no allocation) is
+  // captured once into a CUDA graph per (plan, buffers, tolerance, budget,
+  // launch shapes, concurrency) and replayed on later calls.  Calls that
+  // measure launch shapes, run the launch timer or solve a matrix on the grid
+  // kernels (host-synchronised per sweep) are enqueued directly.
+  uint64_t shape_hash = 1469598103934665603ull;
+  for (const auto &per : shape)
+    for (const auto &h : per) shape_hash = (shape_hash ^ static_cast<uint64_t>(h.threads)) * 1099511628211ull;
+  const bool graphable = !measuring && !ctx->timing && plan->grid_ids.empty() && ctx->graphs;
+  const JacobiGraphKey key{plan->serial, b->key, b->offset, matrices, vectors, eigenvalues,
+                           sweeps_done, off_ratio, work, tolerance, max_sweeps, ctx->concurrent,
+                           shape_hash};
+  if (graphable) {
+    for (auto &e : ctx->jacobi_graphs) {
+      if (e.key == key) {
+        MSQ_TRY(cudaCheck(ctx, cudaGraphLaunch(e.exec, ctx->stream), "jacobi graph launch"));
+        ctx->launches += e.launches;
+        return MSQ_OK;
+      }
+    }
+  }
+  cudaStream_t caller = ctx->stream;
+  cudaStream_t capture = nullptr;
+  const uint64_t launches0 = ctx->launches;
+  if (graphable) {
+    capture = auxStream(ctx, 4);
+    if (capture == caller) return setError(ctx, MSQ_ERR_CUDA, "jacobi: no capture stream");
+    MSQ_TRY(cudaCheck(ctx, cudaStreamBeginCapture(capture, cudaStreamCaptureModeThreadLocal),
+                      "jacobi capture"));
+    ctx->stream = capture;
+  }
+  auto body = [&]() -> int {
+  MSQ_TRY(cudaCheck(ctx, cudaMemsetAsync(args.state, 0, state_bytes, ctx->stream), "state reset"));
+  {
+    dim3 grid(64, std::min(b->count, 65535));
+    identityKernel<<<grid, 256, 0, ctx->stream>>>(vectors, b->offset, b->n, b->count);
+    MSQ_TRY(launched(ctx, "jacobi identity"));
   }
   // Streams: size buckets round-robin over three sweep streams, the replay
   // on a fourth.  Order: sweep k of a bucket follows sweep k-1 (same
@@ -841,6 +876,31 @@ int jacobiEnqueue(msq_ctx *ctx, const DeviceBatch *b, float *matrices, float *ve
                                                                        sweeps_done, off_ratio);
     MSQ_TRY(launched(ctx, "jacobi report"));
   }
+  return MSQ_OK;
+  };
+  const int status = body();
+  if (!graphable) return status;
+  ctx->stream = caller;
+  cudaGraph_t graph = nullptr;
+  const cudaError_t end = cudaStreamEndCapture(capture, &graph);
+  if (status != MSQ_OK) {
+    if (graph != nullptr) cudaGraphDestroy(graph);
+    return status;
+  }
+  MSQ_TRY(cudaCheck(ctx, end, "jacobi capture end"));
+  cudaGraphExec_t exec = nullptr;
+  const cudaError_t inst = cudaGraphInstantiate(&exec, graph, 0);
+  cudaGraphDestroy(graph);
+  MSQ_TRY(cudaCheck(ctx, inst, "jacobi graph instantiate"));
+  const uint64_t captured = ctx->launches - launches0;
+  ctx->launches = launches0;
+  if (ctx->jacobi_graphs.size() >= 8) {
+    cudaGraphExecDestroy(ctx->jacobi_graphs.front().exec);
+    ctx->jacobi_graphs.erase(ctx->jacobi_graphs.begin());
+  }
+  ctx->jacobi_graphs.push_back({key, exec, captured});
+  MSQ_TRY(cudaCheck(ctx, cudaGraphLaunch(exec, ctx->stream), "jacobi graph launch"));
+  ctx->launches += captured;
   return MSQ_OK;
 }
 
