@@ -296,7 +296,7 @@ struct VArgs {
 __host__ __device__ __forceinline__ size_t replaySmemBytes(int max_n, int rows) {
   const int m = padded8(max_n), P = m / 8;
   return static_cast<size_t>(rows) * (m + 4) * sizeof(float) +
-         2 * static_cast<size_t>(P) * kQF * sizeof(float);
+         2 * static_cast<size_t>(P) * kQF * sizeof(float) + 2 * static_cast<size_t>(P) * sizeof(int2);
 }
 
 
@@ -321,6 +321,7 @@ jacobiReplayKernel(VArgs args) {
   const int R = args.rows_per_cta, ld = m + 4;
   float *vs = reinterpret_cast<float *>(smem_raw);    // [R][ld]
   float *qbuf = vs + static_cast<size_t>(R) * ld;     // [2][P][64]
+  int2 *pairs = reinterpret_cast<int2 *>(qbuf + 2 * P * kQF);  // [2][P] (I, J) by round parity
   float *v = args.v + args.a_offset[mi];
   const int rows = min(R, n - r0);
   const float *log = args.log + args.log_offset[mi];
@@ -331,24 +332,37 @@ jacobiReplayKernel(VArgs args) {
     const int c = k / R, r = k % R;
     vs[r * ld + c] = (c < n && r < rows) ? v[r0 + r + static_cast<int64_t>(c) * n] : 0.0f;
   }
+  for (int k = threadIdx.x; k < P; k += blockDim.x) {
+    int I, J;
+    rrPair(k, 0, nb, I, J);
+    pairs[k] = make_int2(I, J);
+  }
   // item -> (pair k, slice of up to 32 rows); a lane takes row r_in of the
   // slice and, when R > 32, rows r_in + 32, r_in + 64, ... with the same Q_k
   const int lanes_r = R < 32 ? R : 32;
+  const int lanes_shift = R < 32 ? -1 : 5;
   const int per_lane = R < 32 ? 1 : R / 32;
   for (int round = 0; round < nb - 1; ++round) {
     copyAsyncWaitAll();
-    __syncthreads();  // this round's rotations landed; last round's rows written
+    __syncthreads();  // this round's rotations and pairs ready; last round's rows written
     if (round + 1 < nb - 1) {
       float *next = qbuf + ((round + 1) & 1) * P * kQF;
       const float *src = log + static_cast<int64_t>(round + 1) * P * kQF;
       for (int x = threadIdx.x; x < chunks; x += blockDim.x) copyAsync16(next + 4 * x, src + 4 * x);
       copyAsyncCommit();
+      for (int k = threadIdx.x; k < P; k += blockDim.x) {
+        int I, J;
+        rrPair(k, round + 1, nb, I, J);
+        pairs[((round + 1) & 1) * P + k] = make_int2(I, J);
+      }
     }
     const float *qs = qbuf + (round & 1) * P * kQF;
+    const int2 *pr = pairs + (round & 1) * P;
     for (int item = threadIdx.x; item < P * lanes_r; item += blockDim.x) {
-      const int k = item / lanes_r, r_in = item % lanes_r;
-      int I, J;
-      rrPair(k, round, nb, I, J);
+      const int k = lanes_shift > 0 ? item >> lanes_shift : item / lanes_r;
+      const int r_in = lanes_shift > 0 ? item & 31 : item % lanes_r;
+      const int2 ij = pr[k];
+      const int I = ij.x, J = ij.y;
       const float4 *qk = reinterpret_cast<const float4 *>(qs + k * kQF);
       float q[8][8];
 #pragma unroll

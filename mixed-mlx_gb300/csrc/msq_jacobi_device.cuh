@@ -52,9 +52,14 @@ __device__ __forceinline__ void rrPair(int pair, int round, int m, int &p, int &
 
 // Folded enumeration of the upper triangle {(i, j): i <= j < P}: rows i and
 // P-1-i share one folded row of P+1 items.
+// The row w / (P + 1) is taken from a float reciprocal and corrected by one
+// step either way (exact for every w < 2^22), instead of an integer divide.
 __device__ __forceinline__ bool foldedBlock(int w, int P, int &i, int &j) {
-  const int r = w / (P + 1);
-  const int c = w - r * (P + 1);
+  const int q = P + 1;
+  int r = __float2int_rz(static_cast<float>(w) * __frcp_rn(static_cast<float>(q)));
+  if ((r + 1) * q <= w) ++r;
+  if (r * q > w) --r;
+  const int c = w - r * q;
   if (c < P - r) {
     i = r;
     j = r + c;
