@@ -331,6 +331,7 @@ extern "C" int msq_encode(msq_ctx *ctx, int format, const float *source,
                           size_t elements, size_t row_length, uint8_t *values,
                           uint8_t *scales) {
   if (ctx == nullptr) return MSQ_ERR_INVALID_ARGUMENT;
+  msq::DeviceGuard device_guard(ctx);
   if (elements == 0) return MSQ_OK;
   if (source == nullptr || values == nullptr) {
     return setError(ctx, MSQ_ERR_INVALID_ARGUMENT, "msq_encode: null buffer");
@@ -390,6 +391,7 @@ extern "C" int msq_decode(msq_ctx *ctx, int format, const uint8_t *values,
                           const uint8_t *scales, size_t elements,
                           size_t row_length, float *output) {
   if (ctx == nullptr) return MSQ_ERR_INVALID_ARGUMENT;
+  msq::DeviceGuard device_guard(ctx);
   if (elements == 0) return MSQ_OK;
   if (values == nullptr || output == nullptr) {
     return setError(ctx, MSQ_ERR_INVALID_ARGUMENT, "msq_decode: null buffer");

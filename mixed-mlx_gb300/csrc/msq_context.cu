@@ -249,6 +249,8 @@ extern "C" void msq_destroy(msq_ctx *ctx) {
     if (ctx->scratch[slot] != nullptr) cudaFree(ctx->scratch[slot]);
   if (ctx->grid_exec != nullptr) cudaGraphExecDestroy(ctx->grid_exec);
   for (auto &g : ctx->jacobi_graphs) cudaGraphExecDestroy(g.exec);
+  destroyJacobiPlans(ctx->jacobi_plans);
+  destroyTcPlans(ctx->tc_plans);
   if (ctx->grid_host != nullptr) cudaFreeHost(ctx->grid_host);
   if (ctx->d_status != nullptr) cudaFree(ctx->d_status);
   recycleTiming(ctx);
@@ -283,6 +285,7 @@ extern "C" int msq_set_graphs(msq_ctx *ctx, int enable) {
 
 extern "C" int msq_synchronize(msq_ctx *ctx) {
   if (ctx == nullptr) return MSQ_ERR_INVALID_ARGUMENT;
+  msq::DeviceGuard device_guard(ctx);
   MSQ_TRY(cudaCheck(ctx, cudaStreamSynchronize(ctx->stream), "msq_synchronize"));
   return checkDeviceStatus(ctx);
 }
@@ -293,6 +296,7 @@ extern "C" uint64_t msq_launch_count(const msq_ctx *ctx) {
 
 extern "C" int msq_timing_begin(msq_ctx *ctx) {
   if (ctx == nullptr) return MSQ_ERR_INVALID_ARGUMENT;
+  msq::DeviceGuard device_guard(ctx);
   recycleTiming(ctx);
   cudaEvent_t e = takeEvent(ctx);
   MSQ_TRY(cudaCheck(ctx, cudaEventRecord(e, ctx->stream), "timing begin"));
@@ -303,6 +307,7 @@ extern "C" int msq_timing_begin(msq_ctx *ctx) {
 
 extern "C" int msq_timing_end(msq_ctx *ctx, char *out, size_t capacity) {
   if (ctx == nullptr || out == nullptr || capacity == 0) return MSQ_ERR_INVALID_ARGUMENT;
+  msq::DeviceGuard device_guard(ctx);
   ctx->timing = false;
   MSQ_TRY(cudaCheck(ctx, cudaDeviceSynchronize(), "timing end"));
   struct Acc { double ms = 0.0; long count = 0; };

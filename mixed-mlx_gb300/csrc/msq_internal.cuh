@@ -48,6 +48,13 @@ struct DeviceBatch {
   std::vector<WorkList> work_cache;  // tile work lists (msq_dense.cu)
 };
 
+// The context's cached Jacobi launch plans (msq_jacobi.cu) and tcgen05 tile
+// plans (msq_tc.cu).
+struct JacobiPlanCache;
+void destroyJacobiPlans(JacobiPlanCache *cache);
+struct TcPlanCache;
+void destroyTcPlans(TcPlanCache *cache);
+
 // A captured batched-Jacobi launch sequence and what it was captured for.
 struct JacobiGraphKey {
   uint64_t plan_serial, batch_key;
@@ -106,6 +113,8 @@ struct msq_ctx {
   // Grid Jacobi (one large matrix on all SMs): pinned off-norm readback and
   // the captured graph of one sweep, valid for order grid_n and workspace
   // grid_work.
+  msq::JacobiPlanCache *jacobi_plans = nullptr;
+  msq::TcPlanCache *tc_plans = nullptr;
   // Batched Jacobi launch sequences captured as CUDA graphs (at most 8).
   bool graphs = true;
   std::vector<msq::JacobiGraph> jacobi_graphs;
@@ -146,6 +155,24 @@ enum ScratchSlot : int {
   kScratchJacobi = 0, kScratchSolver = 1, kScratchOperand = 2, kScratchGemm = 3, kScratchGrid = 4
 };
 void *scratch(msq_ctx *ctx, size_t bytes, int slot);
+
+// Makes the context's device current for one entry point and restores the
+// caller's device on return (a process may drive several GPUs).
+struct DeviceGuard {
+  int previous = -1;
+  explicit DeviceGuard(const msq_ctx *ctx) {
+    int current = 0;
+    if (cudaGetDevice(&current) == cudaSuccess && current != ctx->device &&
+        cudaSetDevice(ctx->device) == cudaSuccess) {
+      previous = current;
+    }
+  }
+  ~DeviceGuard() {
+    if (previous >= 0) cudaSetDevice(previous);
+  }
+  DeviceGuard(const DeviceGuard &) = delete;
+  DeviceGuard &operator=(const DeviceGuard &) = delete;
+};
 
 inline unsigned gridFor(size_t work_items, unsigned threads,
                         unsigned ctas_per_sm = 8) {

@@ -572,7 +572,7 @@ void harvestTimings() {
   }
 }
 
-// Per-layout launch plan, kept per batch layout and device.
+// Per-layout launch plan, kept per batch layout and device in the context.
 struct JacobiPlan {
   uint64_t key = 0;
   uint64_t serial = 0;  // unique per plan ever built (keys captured graphs)
@@ -593,10 +593,29 @@ struct JacobiPlan {
   void *device = nullptr;
 };
 
-std::vector<JacobiPlan *> g_plans;
+}  // namespace
+
+// The context's Jacobi plans (at most 8 layouts, oldest evicted first).
+struct JacobiPlanCache {
+  std::vector<JacobiPlan *> plans;
+};
+
+void destroyJacobiPlans(JacobiPlanCache *cache) {
+  if (cache == nullptr) return;
+  for (JacobiPlan *p : cache->plans) {
+    cudaFree(p->device);
+    delete p;
+  }
+  delete cache;
+}
+
+namespace {
+
 
 JacobiPlan *planFor(msq_ctx *ctx, const DeviceBatch *b) {
-  for (JacobiPlan *p : g_plans)
+  if (ctx->jacobi_plans == nullptr) ctx->jacobi_plans = new JacobiPlanCache;
+  auto &plans = ctx->jacobi_plans->plans;
+  for (JacobiPlan *p : plans)
     if (p->key == b->key && p->count == b->count && p->device_id == ctx->device) return p;
   static std::atomic<uint64_t> next_serial{1};
   auto *plan = new JacobiPlan;
@@ -681,12 +700,12 @@ JacobiPlan *planFor(msq_ctx *ctx, const DeviceBatch *b) {
   if (count > 0) cudaMemcpy(plan->order, ids.data(), count * sizeof(int32_t), cudaMemcpyHostToDevice);
   cudaMemcpy(plan->work_matrix, wm.data(), wm.size() * sizeof(int32_t), cudaMemcpyHostToDevice);
   cudaMemcpy(plan->work_row, wr.data(), wr.size() * sizeof(int32_t), cudaMemcpyHostToDevice);
-  if (g_plans.size() >= 8) {
-    cudaFree(g_plans.front()->device);
-    delete g_plans.front();
-    g_plans.erase(g_plans.begin());
+  if (plans.size() >= 8) {
+    cudaFree(plans.front()->device);
+    delete plans.front();
+    plans.erase(plans.begin());
   }
-  g_plans.push_back(plan);
+  plans.push_back(plan);
   return plan;
 }
 
@@ -963,6 +982,7 @@ extern "C" int msq_jacobi_batched(msq_ctx *ctx, float *matrices, float *vectors,
                                   double tolerance, int max_sweeps,
                                   int32_t *sweeps_done, float *off_ratio) {
   if (ctx == nullptr) return MSQ_ERR_INVALID_ARGUMENT;
+  msq::DeviceGuard device_guard(ctx);
   if (matrices == nullptr || vectors == nullptr || eigenvalues == nullptr) {
     return setError(ctx, MSQ_ERR_INVALID_ARGUMENT, "msq_jacobi_batched: null buffer");
   }

@@ -241,6 +241,7 @@ using namespace msq;
 extern "C" int msq_features(msq_ctx *ctx, const float *a, const int32_t *n, const int64_t *offset,
                             int count, float *features) {
   if (ctx == nullptr) return MSQ_ERR_INVALID_ARGUMENT;
+  msq::DeviceGuard device_guard(ctx);
   if (!a || !features) return setError(ctx, MSQ_ERR_INVALID_ARGUMENT, "msq_features: null buffer");
   const DeviceBatch *b = prepareBatch(ctx, n, offset, count);
   if (b == nullptr) return MSQ_ERR_INVALID_ARGUMENT;
@@ -251,6 +252,7 @@ extern "C" int msq_features(msq_ctx *ctx, const float *a, const int32_t *n, cons
 extern "C" int msq_mlp_forward(msq_ctx *ctx, const float *params, const float *features, int rows,
                                float *logits) {
   if (ctx == nullptr) return MSQ_ERR_INVALID_ARGUMENT;
+  msq::DeviceGuard device_guard(ctx);
   if (!params || !features || !logits || rows < 0)
     return setError(ctx, MSQ_ERR_INVALID_ARGUMENT, "msq_mlp_forward: bad argument");
   if (rows == 0) return MSQ_OK;
@@ -262,6 +264,7 @@ extern "C" int msq_mlp_forward(msq_ctx *ctx, const float *params, const float *f
 extern "C" int msq_mlp_backward(msq_ctx *ctx, const float *params, const float *features,
                                 const float *targets, int rows, float *grad_params, float *loss) {
   if (ctx == nullptr) return MSQ_ERR_INVALID_ARGUMENT;
+  msq::DeviceGuard device_guard(ctx);
   if (!params || !features || !targets || !grad_params || !loss || rows <= 0)
     return setError(ctx, MSQ_ERR_INVALID_ARGUMENT, "msq_mlp_backward: bad argument");
   mlpBackwardKernel<<<std::min(rows, kSmCount * 4), 64, 0, ctx->stream>>>(
@@ -272,6 +275,7 @@ extern "C" int msq_mlp_backward(msq_ctx *ctx, const float *params, const float *
 extern "C" int msq_mlp_step(msq_ctx *ctx, float *params, const float *grad_params, float *adam_m,
                             float *adam_v, int step, float learning_rate) {
   if (ctx == nullptr) return MSQ_ERR_INVALID_ARGUMENT;
+  msq::DeviceGuard device_guard(ctx);
   if (!params || !grad_params || !adam_m || !adam_v || step < 1)
     return setError(ctx, MSQ_ERR_INVALID_ARGUMENT, "msq_mlp_step: bad argument");
   adamKernel<<<(kParams + 255) / 256, 256, 0, ctx->stream>>>(params, grad_params, adam_m, adam_v,

@@ -72,6 +72,7 @@ extern "C" int msq_make_factor(msq_ctx *ctx, const float *vectors, const float *
                                const int32_t *n, const int64_t *offset, int count,
                                float *factor_t) {
   if (ctx == nullptr) return MSQ_ERR_INVALID_ARGUMENT;
+  msq::DeviceGuard device_guard(ctx);
   if (!vectors || !eigenvalues || !factor_t)
     return setError(ctx, MSQ_ERR_INVALID_ARGUMENT, "msq_make_factor: null buffer");
   const DeviceBatch *b = prepareBatch(ctx, n, offset, count);
@@ -82,6 +83,7 @@ extern "C" int msq_make_factor(msq_ctx *ctx, const float *vectors, const float *
 extern "C" int msq_reconstruct(msq_ctx *ctx, int format, const void *values, const void *scales,
                                const int32_t *n, const int64_t *offset, int count, float *root) {
   if (ctx == nullptr) return MSQ_ERR_INVALID_ARGUMENT;
+  msq::DeviceGuard device_guard(ctx);
   if (!values || !root) return setError(ctx, MSQ_ERR_INVALID_ARGUMENT, "msq_reconstruct: null buffer");
   const DeviceBatch *b = prepareBatch(ctx, n, offset, count);
   if (b == nullptr) return MSQ_ERR_INVALID_ARGUMENT;
@@ -96,6 +98,7 @@ extern "C" int msq_residual(msq_ctx *ctx, const float *a, const float *a_lo, con
                             const float *x_lo, const int32_t *n, const int64_t *offset, int count,
                             float *residual, double *norms) {
   if (ctx == nullptr) return MSQ_ERR_INVALID_ARGUMENT;
+  msq::DeviceGuard device_guard(ctx);
   if (!a || !x_hi || !norms) return setError(ctx, MSQ_ERR_INVALID_ARGUMENT, "msq_residual: null buffer");
   const DeviceBatch *b = prepareBatch(ctx, n, offset, count);
   if (b == nullptr) return MSQ_ERR_INVALID_ARGUMENT;
@@ -107,6 +110,7 @@ extern "C" int msq_sylvester_sweep(msq_ctx *ctx, int gemm_format, const float *v
                                    const int32_t *n, const int64_t *offset, int count,
                                    float *x_hi, float *x_lo, float *workspace) {
   if (ctx == nullptr) return MSQ_ERR_INVALID_ARGUMENT;
+  msq::DeviceGuard device_guard(ctx);
   if (!vectors || !eigenvalues || !residual || !x_hi || !x_lo || !workspace)
     return setError(ctx, MSQ_ERR_INVALID_ARGUMENT, "msq_sylvester_sweep: null buffer");
   if (gemm_format != MSQ_FMT_FP32 && gemm_format != MSQ_FMT_BF16)
@@ -254,6 +258,7 @@ extern "C" int msq_solve_batched(msq_ctx *ctx, const float *a, const int32_t *n,
                                  const int64_t *offset, int count, const msq_plan *plans,
                                  double tolerance, float *root, msq_solve_result *results) {
   if (ctx == nullptr) return MSQ_ERR_INVALID_ARGUMENT;
+  msq::DeviceGuard device_guard(ctx);
   if (a == nullptr || root == nullptr || n == nullptr || offset == nullptr || count <= 0)
     return setError(ctx, MSQ_ERR_INVALID_ARGUMENT, "msq_solve_batched: null or empty input");
   if (!(tolerance > 0.0)) return setError(ctx, MSQ_ERR_INVALID_ARGUMENT, "tolerance must be > 0");

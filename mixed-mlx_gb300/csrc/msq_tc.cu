@@ -25,6 +25,7 @@
 #include "msq_stages.cuh"
 
 #include <algorithm>
+#include <atomic>
 #include <vector>
 
 namespace msq {
@@ -554,10 +555,29 @@ struct TcPlan {
   int32_t *row_matrix;
   void *device;
 };
-std::vector<TcPlan *> g_tc_plans;
+
+}  // namespace
+
+// The context's tile plans (at most 16 layouts and kinds, oldest evicted).
+struct TcPlanCache {
+  std::vector<TcPlan *> plans;
+};
+
+void destroyTcPlans(TcPlanCache *cache) {
+  if (cache == nullptr) return;
+  for (TcPlan *p : cache->plans) {
+    cudaFree(p->device);
+    delete p;
+  }
+  delete cache;
+}
+
+namespace {
 
 TcPlan *tcPlan(msq_ctx *ctx, const DeviceBatch *b, int kind) {
-  for (TcPlan *p : g_tc_plans)
+  if (ctx->tc_plans == nullptr) ctx->tc_plans = new TcPlanCache;
+  auto &plans = ctx->tc_plans->plans;
+  for (TcPlan *p : plans)
     if (p->key == b->key && p->count == b->count && p->kind == kind && p->device_id == ctx->device)
       return p;
   const int elems = kind == kOpFp8 ? 128 : 64;
@@ -609,27 +629,29 @@ TcPlan *tcPlan(msq_ctx *ctx, const DeviceBatch *b, int kind) {
   cudaMemcpy(p->tile_base, base.data(), base.size() * sizeof(int64_t), cudaMemcpyHostToDevice);
   cudaMemcpy(p->row_matrix, row_matrix.data(), row_matrix.size() * sizeof(int32_t),
              cudaMemcpyHostToDevice);
-  if (g_tc_plans.size() >= 16) {
-    cudaFree(g_tc_plans.front()->device);
-    delete g_tc_plans.front();
-    g_tc_plans.erase(g_tc_plans.begin());
+  if (plans.size() >= 16) {
+    cudaFree(plans.front()->device);
+    delete plans.front();
+    plans.erase(plans.begin());
   }
-  g_tc_plans.push_back(p);
+  plans.push_back(p);
   return p;
 }
 
 size_t tcSmemBytes() { return kStages * 2 * kTileBytes + 1024 + 256; }
 
+// Opt-in shared memory of the GEMM kernels, once per device.
 int tcAttributes(msq_ctx *ctx) {
-  static bool attr = false;
-  if (attr) return MSQ_OK;
+  static std::atomic<uint64_t> done_mask{0};
+  const uint64_t bit = ctx->device >= 0 && ctx->device < 64 ? uint64_t{1} << ctx->device : 0;
+  if (bit != 0 && (done_mask.load() & bit)) return MSQ_OK;
   const int bytes = static_cast<int>(tcSmemBytes());
   const cudaFuncAttribute a = cudaFuncAttributeMaxDynamicSharedMemorySize;
   MSQ_TRY(cudaCheck(ctx, cudaFuncSetAttribute(tcGemmKernel<kOpBf16, kEpiStore>, a, bytes), "tc attr"));
   MSQ_TRY(cudaCheck(ctx, cudaFuncSetAttribute(tcGemmKernel<kOpFp8, kEpiRowScale>, a, bytes), "tc attr"));
   MSQ_TRY(cudaCheck(ctx, cudaFuncSetAttribute(tcGemmKernel<kOpBf16, kEpiInverseH>, a, bytes), "tc attr"));
   MSQ_TRY(cudaCheck(ctx, cudaFuncSetAttribute(tcGemmKernel<kOpBf16, kEpiResidual>, a, bytes), "tc attr"));
-  attr = true;
+  done_mask.fetch_or(bit);
   return MSQ_OK;
 }
 
