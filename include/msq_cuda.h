@@ -131,6 +131,39 @@ int msq_jacobi_batched(msq_ctx *ctx, float *matrices, float *vectors,
                        const int64_t *offset, int count, double tolerance,
                        int max_sweeps, int32_t *sweeps_done, float *off_ratio);
 
+/* ---- eigenvector accumulation (orders 257..512) ----------------------------
+ * No counterpart in the reference, whose V <- V J runs after every round on
+ * the CUDA-core equivalent of its GPU (metal_mixed_sqrt.metal:1380-1390).
+ * For 256 < n <= 512 on the one-CTA-per-matrix kernels the solver can pair
+ * blocks in two levels: super-blocks of 8 blocks (32 indices), rounds 0..6
+ * inside each super-block, then per outer round-robin round over
+ * super-blocks 8 rounds of cross pairs.  The rotations of rounds 0..14 and
+ * of each later group of 8 stay inside 64-index super-pairs, so their
+ * product is block diagonal (64x64 blocks) and V <- V Z is a GEMM.
+ *   MSQ_VECTORS_AUTO    (-1, default) msq_jacobi_batched: REPLAY;
+ *                       msq_solve_batched: TENSOR for BF16 / FP8 / MXFP4
+ *                       plans, REPLAY for FP32 plans;
+ *   MSQ_VECTORS_REPLAY  (0) round-robin pairing, FP32 replay of every round;
+ *   MSQ_VECTORS_BLOCKED (1) two-level pairing, FP32 replay (bit-exact with
+ *                       the oracle's blocked Jacobi in the same order);
+ *   MSQ_VECTORS_TENSOR  (2) two-level pairing; each stage's 64x64 rotations
+ *                       applied to V held in TMEM by tcgen05.mma in split
+ *                       BF16 (hi*hi + lo*hi + hi*lo, FP32 accumulation): V
+ *                       orthonormal to about 1e-4, eigenvalues unchanged.
+ * The mode applies to later calls on the context.                          */
+enum {
+  MSQ_VECTORS_AUTO = -1,
+  MSQ_VECTORS_REPLAY = 0,
+  MSQ_VECTORS_BLOCKED = 1,
+  MSQ_VECTORS_TENSOR = 2
+};
+int msq_set_jacobi_vectors(msq_ctx *ctx, int mode);
+/* The two-level pair table for `blocks` 4-index blocks (even, 2..4096),
+ * host-only (no GPU, no context): writes *rounds and, when `pairs` is not
+ * NULL and capacity >= rounds * blocks, rounds x blocks/2 pairs (I, J) with
+ * I < J, J stored as -1 - J for a pair that keeps the identity rotation.   */
+int msq_jacobi_schedule(int blocks, int32_t *pairs, size_t capacity, int *rounds);
+
 /* ---- launch-shape autotuner -------------------------------------------------
  * The Jacobi sweep buckets matrices by size class and picks each class's CTA
  * size online: while a class is untuned, its first sweeps of a call try each

@@ -35,6 +35,8 @@ FORMAT_NAMES = {
 
 # Plans (msq_plan_format)
 PLAN_FP32, PLAN_BF16, PLAN_FP8, PLAN_MXFP4 = range(4)
+# msq_set_jacobi_vectors modes
+VECTORS_AUTO, VECTORS_REPLAY, VECTORS_BLOCKED, VECTORS_TENSOR = -1, 0, 1, 2
 
 MLP_IN, MLP_HIDDEN, MLP_OUT = 16, 64, 8
 MLP_PARAMS = (MLP_IN * MLP_HIDDEN + MLP_HIDDEN + MLP_HIDDEN * MLP_HIDDEN +
@@ -78,6 +80,9 @@ _SIGS = {
                                           ctypes.c_int, _P, _P, _P]),
     "msq_set_concurrency": (ctypes.c_int, [_P, ctypes.c_int]),
     "msq_set_graphs": (ctypes.c_int, [_P, ctypes.c_int]),
+    "msq_set_jacobi_vectors": (ctypes.c_int, [_P, ctypes.c_int]),
+    "msq_jacobi_schedule": (ctypes.c_int, [ctypes.c_int, _P, ctypes.c_size_t,
+                                           ctypes.POINTER(ctypes.c_int)]),
     "msq_autotune_report": (ctypes.c_int, [ctypes.c_int, ctypes.c_char_p, ctypes.c_size_t]),
     "msq_autotune_reset": (ctypes.c_int, [ctypes.c_int]),
     "msq_timing_begin": (ctypes.c_int, [_P]),
@@ -166,6 +171,21 @@ class Batch:
         return out
 
 
+def jacobi_schedule(blocks: int) -> np.ndarray:
+    """The library's two-level pair table for `blocks` 4-index blocks
+    (host-side, no GPU): (rounds, blocks/2, 2) int32 pairs (I, J), with
+    J = -1 - J for an identity pair."""
+    rounds = ctypes.c_int()
+    status = lib().msq_jacobi_schedule(blocks, None, 0, ctypes.byref(rounds))
+    if status != 0:
+        raise MsqError(f"msq_jacobi_schedule({blocks}): status {status}")
+    out = np.zeros(rounds.value * blocks, dtype=np.int32)
+    status = lib().msq_jacobi_schedule(blocks, out.ctypes.data, out.size, ctypes.byref(rounds))
+    if status != 0:
+        raise MsqError(f"msq_jacobi_schedule({blocks}): status {status}")
+    return out.reshape(rounds.value, blocks // 2, 2)
+
+
 class Context:
     """Owns one msq_ctx bound to a CUDA device and torch's current stream."""
 
@@ -209,6 +229,11 @@ class Context:
 
     def set_graphs(self, enable: bool) -> None:
         self.check(lib().msq_set_graphs(self.handle, int(bool(enable))), "msq_set_graphs")
+
+    def set_jacobi_vectors(self, mode: int) -> None:
+        """Eigenvector mode of the batched Jacobi for 256 < n <= 512:
+        VECTORS_AUTO, VECTORS_REPLAY, VECTORS_BLOCKED or VECTORS_TENSOR."""
+        self.check(lib().msq_set_jacobi_vectors(self.handle, int(mode)), "msq_set_jacobi_vectors")
 
     def synchronize(self) -> None:
         self.check(lib().msq_synchronize(self.handle), "msq_synchronize")

@@ -110,14 +110,19 @@ struct msq_ctx {
   // false: every launch on `stream` (serial order; per-kernel timings are
   // then each kernel's own duration, not shared with concurrent work)
   bool concurrent = true;
-  // Grid Jacobi (one large matrix on all SMs): pinned off-norm readback and
-  // the captured graph of one sweep, valid for order grid_n and workspace
-  // grid_work.
+  // Eigenvector accumulation of the batched Jacobi for 256 < n <= 512
+  // (msq_set_jacobi_vectors): -1 automatic, 0 round-robin + FP32 replay,
+  // 1 two-level pairing + FP32 replay, 2 two-level pairing + tensor cores.
+  int jacobi_vectors = -1;
+  // Per-layout work plans of the Jacobi and of the tensor-core GEMMs.
   msq::JacobiPlanCache *jacobi_plans = nullptr;
   msq::TcPlanCache *tc_plans = nullptr;
   // Batched Jacobi launch sequences captured as CUDA graphs (at most 8).
   bool graphs = true;
   std::vector<msq::JacobiGraph> jacobi_graphs;
+  // Grid Jacobi (one large matrix on all SMs): pinned off-norm readback and
+  // the captured graph of one sweep, valid for order grid_n and workspace
+  // grid_work.
   double *grid_host = nullptr;
   cudaGraphExec_t grid_exec = nullptr;
   int grid_n = 0;

@@ -31,6 +31,7 @@
 #include "msq_internal.cuh"
 #include "msq_jacobi_device.cuh"
 #include "msq_jacobi_grid.cuh"
+#include "msq_jacobi_tc.cuh"
 
 #include <algorithm>
 #include <array>
@@ -71,6 +72,8 @@ struct JacobiArgs {
   int first;                 // 1 on the first launch (load A, set norm)
   int parity;                // log buffer of this sweep (log points at it)
   int *status;               // device status word (bounded waits)
+  const int2 *sched;         // two-level pair tables (null: round-robin for all)
+  const int32_t *sched_off;  // per matrix: its table in sched (int2 units), -1 = round-robin
 };
 
 __host__ __device__ __forceinline__ size_t sweepSmemLayout(int n, bool with_tiles, size_t *q_off,
@@ -113,6 +116,9 @@ jacobiSweepKernel(JacobiArgs args) {
   float *tiles = kSmem ? reinterpret_cast<float *>(smem_raw + tile_off) : gtiles;
   const int tile_floats = nb * (nb + 1) / 2 * kTileF;
   const float *full = args.a + args.a_offset[mi];
+  const int sched_at = args.sched_off != nullptr ? args.sched_off[mi] : -1;
+  const int2 *sched = sched_at >= 0 ? args.sched + sched_at : nullptr;
+  const int rounds = sched != nullptr ? twoLevelRounds(nb) : nb - 1;
 
   for (int k = threadIdx.x; k <= nb; k += blockDim.x) tri[k] = k * (k + 1) / 2;
   __syncthreads();
@@ -188,22 +194,25 @@ jacobiSweepKernel(JacobiArgs args) {
 
   float *log = args.log + args.log_offset[mi];
   const int items = ((P + 1) / 2) * (P + 1);
-  for (int round = 0; round < nb - 1; ++round) {
+  for (int round = 0; round < rounds; ++round) {
     // Pivots: a quad of lanes per block pair.  The loop is warp-uniform (all
     // lanes of a warp take part in the quad shuffles; lanes past P idle).
+    // An identity pair of the two-level table keeps its blocks and logs Q = I.
     const int quads = blockDim.x >> 2, t4 = threadIdx.x & 3;
     for (int base = 0; base < P; base += quads) {
       const int k = base + (threadIdx.x >> 2);
-      const bool active = k < P;
+      const bool present = k < P;
+      bool active = present;
       float ra[8], rb[8];
-      int tII = 0, tIJ = 0, tJJ = 0;
-      if (active) {
-        int I, J;
-        rrPair(k, round, nb, I, J);
+      int tII = 0, tIJ = 0, tJJ = 0, I = 0, J = 0;
+      if (present) {
+        roundPair(sched, k, round, nb, I, J, active);
         if (t4 == 0) {
           pair_i[k] = I;
           pair_j[k] = J;
         }
+      }
+      if (active) {
         tII = tileIndex(tri, I, I);
         tIJ = tileIndex(tri, I, J);
         tJJ = tileIndex(tri, J, J);
@@ -233,6 +242,15 @@ jacobiSweepKernel(JacobiArgs args) {
         sII[t4 ^ (tII & 3)] = make_float4(ra[0], ra[1], ra[2], ra[3]);
         sIJ[t4 ^ (tIJ & 3)] = make_float4(ra[4], ra[5], ra[6], ra[7]);
         sJJ[t4 ^ (tJJ & 3)] = make_float4(rb[4], rb[5], rb[6], rb[7]);
+      } else if (present) {
+        // identity pair: Q = I (lane t writes rows 2t and 2t + 1)
+        float4 *q4 = reinterpret_cast<float4 *>(qs + k * kQS);
+#pragma unroll
+        for (int x = 0; x < 2; ++x) {
+          const int row = 2 * t4 + x;
+          q4[2 * row] = make_float4(row == 0, row == 1, row == 2, row == 3);
+          q4[2 * row + 1] = make_float4(row == 4, row == 5, row == 6, row == 7);
+        }
       }
     }
     __syncthreads();
@@ -289,6 +307,8 @@ struct VArgs {
   const int32_t *work_row;     // per CTA: first row
   int rows_per_cta;            // multiple of 8
   int parity;                  // log buffer to replay (log points at it)
+  const int2 *sched;           // two-level pair tables, as JacobiArgs
+  const int32_t *sched_off;
 };
 
 // Replay shared memory: `rows` rows of V (stride m + 4) and two rounds of
@@ -325,6 +345,9 @@ jacobiReplayKernel(VArgs args) {
   float *v = args.v + args.a_offset[mi];
   const int rows = min(R, n - r0);
   const float *log = args.log + args.log_offset[mi];
+  const int sched_at = args.sched_off != nullptr ? args.sched_off[mi] : -1;
+  const int2 *sched = sched_at >= 0 ? args.sched + sched_at : nullptr;
+  const int rounds = sched != nullptr ? twoLevelRounds(nb) : nb - 1;
   const int chunks = P * kQF / 4;  // 16-byte pieces of one round's rotations
   for (int x = threadIdx.x; x < chunks; x += blockDim.x) copyAsync16(qbuf + 4 * x, log + 4 * x);
   copyAsyncCommit();
@@ -334,7 +357,8 @@ jacobiReplayKernel(VArgs args) {
   }
   for (int k = threadIdx.x; k < P; k += blockDim.x) {
     int I, J;
-    rrPair(k, 0, nb, I, J);
+    bool rotate;
+    roundPair(sched, k, 0, nb, I, J, rotate);
     pairs[k] = make_int2(I, J);
   }
   // item -> (pair k, slice of up to 32 rows); a lane takes row r_in of the
@@ -342,17 +366,18 @@ jacobiReplayKernel(VArgs args) {
   const int lanes_r = R < 32 ? R : 32;
   const int lanes_shift = R < 32 ? -1 : 5;
   const int per_lane = R < 32 ? 1 : R / 32;
-  for (int round = 0; round < nb - 1; ++round) {
+  for (int round = 0; round < rounds; ++round) {
     copyAsyncWaitAll();
     __syncthreads();  // this round's rotations and pairs ready; last round's rows written
-    if (round + 1 < nb - 1) {
+    if (round + 1 < rounds) {
       float *next = qbuf + ((round + 1) & 1) * P * kQF;
       const float *src = log + static_cast<int64_t>(round + 1) * P * kQF;
       for (int x = threadIdx.x; x < chunks; x += blockDim.x) copyAsync16(next + 4 * x, src + 4 * x);
       copyAsyncCommit();
       for (int k = threadIdx.x; k < P; k += blockDim.x) {
         int I, J;
-        rrPair(k, round + 1, nb, I, J);
+        bool rotate;
+        roundPair(sched, k, round + 1, nb, I, J, rotate);
         pairs[((round + 1) & 1) * P + k] = make_int2(I, J);
       }
     }
@@ -590,6 +615,14 @@ struct JacobiPlan {
   struct ReplayGroup { int first; int count; int rows; size_t smem; };
   std::vector<ReplayGroup> replays;
   std::vector<int> grid_ids;  // matrices solved by the grid kernels
+  // Eigenvector mode (msq_set_jacobi_vectors, resolved): two-level pair
+  // tables for 256 < n <= 512 in modes 1 and 2; in mode 2 those matrices'
+  // V update runs on the tensor cores (tcv) instead of the FP32 replay.
+  int mode = 0;
+  const int2 *sched = nullptr;
+  const int32_t *sched_off = nullptr;
+  TcVectorsDevice tcv;
+  int64_t tcv_images = 0;
   void *device = nullptr;
 };
 
@@ -612,17 +645,31 @@ void destroyJacobiPlans(JacobiPlanCache *cache) {
 namespace {
 
 
-JacobiPlan *planFor(msq_ctx *ctx, const DeviceBatch *b) {
+// Carves aligned arrays out of one device allocation.
+struct Carve {
+  size_t bytes = 0;
+  template <typename T>
+  size_t take(size_t count) {
+    bytes = (bytes + 15) & ~static_cast<size_t>(15);
+    const size_t at = bytes;
+    bytes += count * sizeof(T);
+    return at;
+  }
+};
+
+JacobiPlan *planFor(msq_ctx *ctx, const DeviceBatch *b, int mode) {
   if (ctx->jacobi_plans == nullptr) ctx->jacobi_plans = new JacobiPlanCache;
   auto &plans = ctx->jacobi_plans->plans;
   for (JacobiPlan *p : plans)
-    if (p->key == b->key && p->count == b->count && p->device_id == ctx->device) return p;
+    if (p->key == b->key && p->count == b->count && p->device_id == ctx->device && p->mode == mode)
+      return p;
   static std::atomic<uint64_t> next_serial{1};
   auto *plan = new JacobiPlan;
   plan->serial = next_serial.fetch_add(1);
   plan->device_id = ctx->device;
   plan->key = b->key;
   plan->count = b->count;
+  plan->mode = mode;
   const int total = b->count;
   // Routing: a matrix above kGridMinOrder, or above 256 when at most
   // kGridFewLarge such matrices are in the batch (too few to fill the SMs one
@@ -632,6 +679,10 @@ JacobiPlan *planFor(msq_ctx *ctx, const DeviceBatch *b) {
   for (int i = 0; i < total; ++i) large += b->host_n[i] > 256;
   std::vector<int32_t> ids;
   std::vector<int64_t> t_off(total, 0), l_off(total, 0);
+  std::vector<int32_t> sched_off(total, -1), sched_host, table;
+  std::map<int, int32_t> sched_at;  // block count -> table offset (int2 units)
+  std::vector<int> tc_ids;
+  std::vector<char> on_tc(total, 0);
   for (int i = 0; i < total; ++i) {
     const int n = b->host_n[i];
     if (n > kGridMinOrder || (n > 256 && large <= kGridFewLarge)) {
@@ -640,11 +691,27 @@ JacobiPlan *planFor(msq_ctx *ctx, const DeviceBatch *b) {
     }
     ids.push_back(i);
     const int m = padded8(n), nb = m / 4, P = nb / 2;
+    const bool two_level = mode != 0 && n >= kTwoLevelMinOrder && n <= kTwoLevelMaxOrder;
     t_off[i] = plan->tile_total;
     plan->tile_total += static_cast<int64_t>(nb) * (nb + 1) / 2 * kTileF;
     l_off[i] = plan->log_total;
-    plan->log_total += static_cast<int64_t>(nb - 1) * P * kQF;
+    plan->log_total += static_cast<int64_t>(two_level ? twoLevelRounds(nb) : nb - 1) * P * kQF;
+    if (two_level) {
+      auto at = sched_at.find(nb);
+      if (at == sched_at.end()) {
+        twoLevelSchedule(nb, table);
+        at = sched_at.emplace(nb, static_cast<int32_t>(sched_host.size() / 2)).first;
+        sched_host.insert(sched_host.end(), table.begin(), table.end());
+      }
+      sched_off[i] = at->second;
+      if (mode == 2) {
+        tc_ids.push_back(i);
+        on_tc[i] = 1;
+      }
+    }
   }
+  TcVectorsTables tcv;
+  tcVectorsTables(b->host_n.data(), total, tc_ids, tcv);
   const int count = static_cast<int>(ids.size());
   // buckets by size class, largest class first
   std::stable_sort(ids.begin(), ids.end(), [&](int x, int y) {
@@ -672,34 +739,69 @@ JacobiPlan *planFor(msq_ctx *ctx, const DeviceBatch *b) {
     const int rows = replayRows(max_n);
     const int first = static_cast<int>(wm.size());
     for (int i = bucket.first; i < bucket.first + bucket.count; ++i) {
+      if (on_tc[ids[i]]) continue;  // V on the tensor cores
       const int n = b->host_n[ids[i]];
       for (int r = 0; r < n; r += rows) {
         wm.push_back(ids[i]);
         wr.push_back(r);
       }
     }
-    plan->replays.push_back({first, static_cast<int>(wm.size()) - first, rows,
-                             replaySmemBytes(max_n, rows)});
+    if (static_cast<int>(wm.size()) > first) {
+      plan->replays.push_back({first, static_cast<int>(wm.size()) - first, rows,
+                               replaySmemBytes(max_n, rows)});
+    }
   }
   plan->work_count = static_cast<int>(wm.size());
-  const size_t bytes = 2 * total * sizeof(int64_t) + total * sizeof(int32_t) +
-                       2 * wm.size() * sizeof(int32_t) + 64;
+  Carve carve;
+  const size_t at_t = carve.take<int64_t>(total), at_l = carve.take<int64_t>(total);
+  const size_t at_img = carve.take<int64_t>(total);
+  const size_t at_order = carve.take<int32_t>(total), at_wm = carve.take<int32_t>(wm.size());
+  const size_t at_wr = carve.take<int32_t>(wr.size()), at_so = carve.take<int32_t>(total);
+  const size_t at_sched = carve.take<int32_t>(sched_host.size());
+  const size_t at_prog = carve.take<int32_t>(tcv.prog.size());
+  const size_t at_po = carve.take<int32_t>(total);
+  const size_t at_fw = carve.take<int32_t>(tcv.form_work.size());
+  const size_t at_aw = carve.take<int32_t>(tcv.apply_work.size());
   char *dev = nullptr;
-  if (cudaCheck(ctx, cudaMalloc(&dev, bytes), "jacobi plan alloc") != MSQ_OK) {
+  if (cudaCheck(ctx, cudaMalloc(&dev, carve.bytes + 16), "jacobi plan alloc") != MSQ_OK) {
     delete plan;
     return nullptr;
   }
+  auto put = [&](size_t at, const void *src, size_t bytes) {
+    if (bytes > 0) cudaMemcpy(dev + at, src, bytes, cudaMemcpyHostToDevice);
+  };
   plan->device = dev;
-  plan->t_offset = reinterpret_cast<int64_t *>(dev);
-  plan->log_offset = plan->t_offset + total;
-  plan->order = reinterpret_cast<int32_t *>(plan->log_offset + total);
-  plan->work_matrix = plan->order + total;
-  plan->work_row = plan->work_matrix + wm.size();
-  cudaMemcpy(plan->t_offset, t_off.data(), total * sizeof(int64_t), cudaMemcpyHostToDevice);
-  cudaMemcpy(plan->log_offset, l_off.data(), total * sizeof(int64_t), cudaMemcpyHostToDevice);
-  if (count > 0) cudaMemcpy(plan->order, ids.data(), count * sizeof(int32_t), cudaMemcpyHostToDevice);
-  cudaMemcpy(plan->work_matrix, wm.data(), wm.size() * sizeof(int32_t), cudaMemcpyHostToDevice);
-  cudaMemcpy(plan->work_row, wr.data(), wr.size() * sizeof(int32_t), cudaMemcpyHostToDevice);
+  plan->t_offset = reinterpret_cast<int64_t *>(dev + at_t);
+  plan->log_offset = reinterpret_cast<int64_t *>(dev + at_l);
+  plan->order = reinterpret_cast<int32_t *>(dev + at_order);
+  plan->work_matrix = reinterpret_cast<int32_t *>(dev + at_wm);
+  plan->work_row = reinterpret_cast<int32_t *>(dev + at_wr);
+  put(at_t, t_off.data(), total * sizeof(int64_t));
+  put(at_l, l_off.data(), total * sizeof(int64_t));
+  put(at_order, ids.data(), count * sizeof(int32_t));
+  put(at_wm, wm.data(), wm.size() * sizeof(int32_t));
+  put(at_wr, wr.data(), wr.size() * sizeof(int32_t));
+  if (!sched_host.empty()) {
+    plan->sched = reinterpret_cast<const int2 *>(dev + at_sched);
+    plan->sched_off = reinterpret_cast<const int32_t *>(dev + at_so);
+    put(at_sched, sched_host.data(), sched_host.size() * sizeof(int32_t));
+    put(at_so, sched_off.data(), total * sizeof(int32_t));
+  }
+  if (!tc_ids.empty()) {
+    plan->tcv.form_work = reinterpret_cast<const int2 *>(dev + at_fw);
+    plan->tcv.form_items = static_cast<int>(tcv.form_work.size() / 2);
+    plan->tcv.apply_work = reinterpret_cast<const int2 *>(dev + at_aw);
+    plan->tcv.apply_items = static_cast<int>(tcv.apply_work.size() / 2);
+    plan->tcv.prog = reinterpret_cast<const int32_t *>(dev + at_prog);
+    plan->tcv.prog_off = reinterpret_cast<const int32_t *>(dev + at_po);
+    plan->tcv.image_off = reinterpret_cast<const int64_t *>(dev + at_img);
+    plan->tcv_images = tcv.images;
+    put(at_fw, tcv.form_work.data(), tcv.form_work.size() * sizeof(int32_t));
+    put(at_aw, tcv.apply_work.data(), tcv.apply_work.size() * sizeof(int32_t));
+    put(at_prog, tcv.prog.data(), tcv.prog.size() * sizeof(int32_t));
+    put(at_po, tcv.prog_off.data(), total * sizeof(int32_t));
+    put(at_img, tcv.image_off.data(), total * sizeof(int64_t));
+  }
   if (plans.size() >= 8) {
     cudaFree(plans.front()->device);
     delete plans.front();
@@ -733,18 +835,22 @@ int setKernelAttributes() {
 // Enqueues the whole solve on ctx->stream (Jacobi scratch arena).
 int jacobiEnqueue(msq_ctx *ctx, const DeviceBatch *b, float *matrices, float *vectors,
                   float *eigenvalues, double tolerance, int max_sweeps, int32_t *sweeps_done,
-                  float *off_ratio) {
+                  float *off_ratio, bool low_bit_basis) {
   if (b->max_n > kMaxOrder) {
     return setError(ctx, MSQ_ERR_UNSUPPORTED, "jacobi: order above 16384 is not supported");
   }
-  JacobiPlan *plan = planFor(ctx, b);
+  const int mode = ctx->jacobi_vectors >= 0 ? ctx->jacobi_vectors : (low_bit_basis ? 2 : 0);
+  JacobiPlan *plan = planFor(ctx, b, mode);
   if (plan == nullptr) return MSQ_ERR_CUDA;
   const size_t state_bytes = (b->count * sizeof(JacobiState) + 255) & ~size_t(255);
   const size_t tile_bytes = (plan->tile_total * sizeof(float) + 255) & ~size_t(255);
   // Two log buffers (sweep parity) so sweep k+1 overlaps the replay of k.
-  const size_t log_bytes = 2 * plan->log_total * sizeof(float);
-  char *work = static_cast<char *>(scratch(ctx, state_bytes + tile_bytes + log_bytes, kScratchJacobi));
+  const size_t log_bytes = (2 * plan->log_total * sizeof(float) + 1023) & ~size_t(1023);
+  const size_t image_bytes = static_cast<size_t>(plan->tcv_images) * kRotationImageBytes;
+  char *work = static_cast<char *>(
+      scratch(ctx, state_bytes + tile_bytes + log_bytes + image_bytes, kScratchJacobi));
   if (work == nullptr) return MSQ_ERR_CUDA;
+  uint8_t *images = reinterpret_cast<uint8_t *>(work + state_bytes + tile_bytes + log_bytes);
   if (setKernelAttributes() != MSQ_OK) return cudaCheck(ctx, cudaGetLastError(), "jacobi attributes");
   JacobiArgs args{};
   args.a = matrices;
@@ -760,8 +866,10 @@ int jacobiEnqueue(msq_ctx *ctx, const DeviceBatch *b, float *matrices, float *ve
   args.tol = tolerance;
   args.max_sweeps = max_sweeps;
   args.status = ctx->d_status;
+  args.sched = plan->sched;
+  args.sched_off = plan->sched_off;
   VArgs vargs{vectors, b->offset, plan->log_offset, b->n, log_base, args.state,
-              plan->work_matrix, plan->work_row, 0, 0};
+              plan->work_matrix, plan->work_row, 0, 0, plan->sched, plan->sched_off};
   // Launch shape per bucket: the tuned CTA size, or (while its class is
   // being tuned) candidate c on sweep launch 1 + c with timing events.
   struct BucketLaunch { int threads; int measure; };  // measure: candidate or -1
@@ -887,6 +995,8 @@ int jacobiEnqueue(msq_ctx *ctx, const DeviceBatch *b, float *matrices, float *ve
         jacobiReplayKernel<<<g.count, kReplayThreads, g.smem, rs>>>(vargs);
         MSQ_TRY(launchedOn(ctx, rs, "jacobi replay"));
       }
+      MSQ_TRY(tcVectorsEnqueue(ctx, rs, plan->tcv, vectors, b->offset, b->n, args.state, args.log,
+                               plan->log_offset, images, parity));
       replay_done[parity] = syncEvent(ctx);
       MSQ_TRY(cudaCheck(ctx, cudaEventRecord(replay_done[parity], rs), "event record"));
     }
@@ -993,7 +1103,7 @@ extern "C" int msq_jacobi_batched(msq_ctx *ctx, float *matrices, float *vectors,
   const DeviceBatch *b = prepareBatch(ctx, n, offset, count);
   if (b == nullptr) return MSQ_ERR_INVALID_ARGUMENT;
   return jacobiEnqueue(ctx, b, matrices, vectors, eigenvalues, tolerance,
-                       max_sweeps, sweeps_done, off_ratio);
+                       max_sweeps, sweeps_done, off_ratio, false);
 }
 
 // ---------------------------------------------------------------------------

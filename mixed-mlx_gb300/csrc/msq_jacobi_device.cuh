@@ -9,6 +9,8 @@
 
 #include <cstdint>
 
+#include "msq_tcgen05.cuh"
+
 namespace msq {
 namespace {
 
@@ -36,18 +38,59 @@ __host__ __device__ constexpr int padded8(int n) { return (n + 7) & ~7; }
 // Slot -> participant of round r (participants 1..m-1 rotate right by one
 // per round, slot 0 fixed): the closed form of the std::rotate step in
 // makeJacobiSchedule (src/metal_solver.cpp:75-76).
-__device__ __forceinline__ int rrSlot(int slot, int round, int m) {
+__host__ __device__ __forceinline__ int rrSlot(int slot, int round, int m) {
   if (slot == 0) return 0;
   int k = slot - 1 - round % (m - 1);
   if (k < 0) k += m - 1;
   return 1 + k;
 }
 
-__device__ __forceinline__ void rrPair(int pair, int round, int m, int &p, int &q) {
+__host__ __device__ __forceinline__ void rrPair(int pair, int round, int m, int &p, int &q) {
   const int a = rrSlot(pair, round, m);
   const int b = rrSlot(m - 1 - pair, round, m);
   p = a < b ? a : b;
   q = a < b ? b : a;
+}
+
+// Two-level pairing of nb blocks (the tensor-core eigenvector path): blocks
+// form super-blocks of 8 (32 indices; the last may hold fewer, and a dummy
+// empty one makes their count even).  Rounds 0..6 pair the blocks inside
+// each super-block (round-robin over 8 slots); then an outer round-robin
+// over super-blocks pairs them, and each outer round spends 8 rounds on the
+// cross pairs (i of P with (i + t) mod 8 of Q in round t).  Every block pair
+// meets once per sweep, and the rotations of rounds [0, 15) and of each
+// later group of 8 stay inside the outer round's super-pairs, so their
+// product is block diagonal with 64x64 blocks.  Blocks without a partner in
+// a round are paired among themselves with the identity rotation (J stored
+// as -1 - J in the schedule table).
+constexpr int kSuperBlock = 8;
+__host__ __device__ constexpr int twoLevelSupers(int nb) {
+  return (nb + kSuperBlock - 1) / kSuperBlock + (((nb + kSuperBlock - 1) / kSuperBlock) & 1);
+}
+__host__ __device__ constexpr int twoLevelRounds(int nb) {
+  return (kSuperBlock - 1) + kSuperBlock * (twoLevelSupers(nb) - 1);
+}
+// Stage s of the eigenvector update: rounds [first, first + count).
+__host__ __device__ constexpr int twoLevelStageFirst(int s) {
+  return s == 0 ? 0 : (kSuperBlock - 1) + kSuperBlock * s;
+}
+__host__ __device__ constexpr int twoLevelStageRounds(int s) {
+  return s == 0 ? 2 * kSuperBlock - 1 : kSuperBlock;
+}
+
+// Pair k of a round from the two-level table (sched != nullptr) or the
+// round-robin rule; *rotate is false for an identity pair.
+__device__ __forceinline__ void roundPair(const int2 *sched, int k, int round, int nb, int &I,
+                                          int &J, bool &rotate) {
+  if (sched != nullptr) {
+    const int2 ij = sched[round * (nb / 2) + k];
+    I = ij.x;
+    rotate = ij.y >= 0;
+    J = rotate ? ij.y : -1 - ij.y;
+  } else {
+    rrPair(k, round, nb, I, J);
+    rotate = true;
+  }
 }
 
 // Folded enumeration of the upper triangle {(i, j): i <= j < P}: rows i and
@@ -446,10 +489,6 @@ __device__ __forceinline__ void superTileHalf(float *tiles, TileOf tileOf, const
 // shared memory; both addresses 16-byte aligned, size a multiple of 16.  The
 // load completes on an mbarrier (expect_tx); the wait is bounded.
 constexpr long long kTileWaitLimit = 1ll << 26;
-
-__device__ __forceinline__ uint32_t smemAddr(const void *p) {
-  return static_cast<uint32_t>(__cvta_generic_to_shared(p));
-}
 
 __device__ __forceinline__ void bulkLoadTiles(void *smem, const void *gmem, uint32_t bytes,
                                               uint64_t *bar) {

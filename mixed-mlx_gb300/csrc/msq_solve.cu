@@ -189,7 +189,8 @@ int runGroup(msq_ctx *ctx, const float *a_user, const int32_t *n_user,
   MSQ_TRY(cudaCheck(ctx, cudaMemcpyAsync(J, A, total * sizeof(float), cudaMemcpyDeviceToDevice,
                                          ctx->stream), "jacobi copy"));
   const int max_sweeps = g.plan.jacobi_max_sweeps > 0 ? g.plan.jacobi_max_sweeps : 15;
-  MSQ_TRY(jacobiEnqueue(ctx, b, J, V, lam, g.plan.jacobi_tolerance, max_sweeps, sweeps, nullptr));
+  MSQ_TRY(jacobiEnqueue(ctx, b, J, V, lam, g.plan.jacobi_tolerance, max_sweeps, sweeps, nullptr,
+                        g.plan.format != MSQ_PLAN_FP32));
   MSQ_TRY(makeFactor(ctx, b, V, lam, F));
   MSQ_TRY(reconstructFromFactor(ctx, b, g.plan.format, F, Xh));
   MSQ_TRY(cudaCheck(ctx, cudaMemsetAsync(Xl, 0, total * sizeof(float), ctx->stream), "x_lo reset"));

@@ -6,9 +6,11 @@
 namespace msq {
 
 // msq_jacobi.cu
+// low_bit_basis: the caller quantizes the basis to BF16 or fewer bits, so the
+// automatic eigenvector mode may accumulate V on the tensor cores.
 int jacobiEnqueue(msq_ctx *ctx, const DeviceBatch *b, float *matrices, float *vectors,
                   float *eigenvalues, double tolerance, int max_sweeps,
-                  int32_t *sweeps_done, float *off_ratio);
+                  int32_t *sweeps_done, float *off_ratio, bool low_bit_basis);
 
 // msq_tc.cu — tcgen05 reconstruction X = W W^T from the FP32 factor F = W^T
 // (quantized to `format` on the fly) or from already encoded flat codes.

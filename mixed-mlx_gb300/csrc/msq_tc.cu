@@ -23,6 +23,7 @@
 #include "msq_codec_device.cuh"
 #include "msq_internal.cuh"
 #include "msq_stages.cuh"
+#include "msq_tcgen05.cuh"
 
 #include <algorithm>
 #include <atomic>
@@ -47,29 +48,6 @@ enum Epilogue : int {
   kEpiResidual = 3,  // X = A - acc, FP64 ||X||^2 and ||A||^2 per matrix
 };
 
-__device__ __forceinline__ uint32_t smemAddr(const void *p) {
-  return static_cast<uint32_t>(__cvta_generic_to_shared(p));
-}
-
-__device__ __forceinline__ uint32_t swizzle128(int row, int chunk) {
-  return (row >> 3) * 1024 + (row & 7) * 128 + ((chunk ^ (row & 7)) << 4);
-}
-
-__device__ __forceinline__ void mbarInit(uint32_t bar, uint32_t count) {
-  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(bar), "r"(count));
-}
-
-__device__ __forceinline__ bool mbarTryWait(uint32_t bar, uint32_t parity) {
-  uint32_t done;
-  asm volatile(
-      "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
-      " selp.u32 %0, 1, 0, p;\n}\n"
-      : "=r"(done)
-      : "r"(bar), "r"(parity)
-      : "memory");
-  return done != 0;
-}
-
 // Bounded wait: false (and the status word set) if the phase never completes.
 __device__ __forceinline__ bool mbarWait(uint32_t bar, uint32_t parity, int *status,
                                          volatile int *abort_flag) {
@@ -80,33 +58,6 @@ __device__ __forceinline__ bool mbarWait(uint32_t bar, uint32_t parity, int *sta
   atomicExch(status, kStatusMbarrierTimeout);
   *abort_flag = 1;
   return false;
-}
-
-__device__ __forceinline__ void mbarArriveExpectTx(uint32_t bar, uint32_t bytes) {
-  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes)
-               : "memory");
-}
-
-__device__ __forceinline__ void mbarArrive(uint32_t bar) {
-  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(bar) : "memory");
-}
-
-__device__ __forceinline__ void bulkLoad(uint32_t dst, const void *src, uint32_t bytes,
-                                         uint32_t bar) {
-  asm volatile(
-      "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
-          dst),
-      "l"(src), "r"(bytes), "r"(bar)
-      : "memory");
-}
-
-// Shared-memory matrix descriptor: K-major, SWIZZLE_128B, 1024-byte atoms.
-__device__ __forceinline__ uint64_t smemDesc(uint32_t addr) {
-  return static_cast<uint64_t>((addr >> 4) & 0x3FFFu) |
-         (static_cast<uint64_t>(1) << 16) |            // LBO (unused for SW128 K-major)
-         (static_cast<uint64_t>(1024 >> 4) << 32) |    // SBO: 8-row atom stride
-         (static_cast<uint64_t>(1) << 46) |            // descriptor version
-         (static_cast<uint64_t>(2) << 61);             // SWIZZLE_128B
 }
 
 // Instruction descriptor: D = F32, K-major A and B, M = 128, N = 128.
@@ -129,29 +80,6 @@ __device__ __forceinline__ void mmaIssue(uint32_t tmem, uint64_t a, uint64_t b, 
         " tcgen05.mma.cta_group::1.kind::f8f6f4 [%0], %1, %2, %3, p;\n}\n" ::"r"(tmem),
         "l"(a), "l"(b), "r"(instrDesc(kOpFp8)), "r"(accum));
   }
-}
-
-__device__ __forceinline__ void mmaCommit(uint32_t bar) {
-  asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
-                   bar)
-               : "memory");
-}
-
-__device__ __forceinline__ void tmemLoad32(uint32_t taddr, float *v) {
-  uint32_t r[32];
-  asm volatile(
-      "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, "
-      "%12, %13, %14, %15, %16, %17, %18, %19, %20, %21, %22, %23, %24, %25, %26, %27, %28, %29, "
-      "%30, %31}, [%32];"
-      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]),
-        "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]),
-        "=r"(r[14]), "=r"(r[15]), "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]),
-        "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]), "=r"(r[24]), "=r"(r[25]),
-        "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
-      : "r"(taddr));
-  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
-#pragma unroll
-  for (int i = 0; i < 32; ++i) v[i] = __uint_as_float(r[i]);
 }
 
 struct TcArgs {

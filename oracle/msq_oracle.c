@@ -251,6 +251,75 @@ void msqo_jacobi_pair(unsigned order, unsigned round, unsigned pair,
   *q = a < b ? b : a;
 }
 
+/* Two-level pairing of nb blocks (nb even), the order the CUDA solver uses
+ * for orders 257..512 when it accumulates eigenvectors on the tensor cores:
+ * super-blocks of 8 blocks (the last holds nb mod 8 when that is nonzero; an
+ * empty one is added when their count is odd).  Rounds 0..6: inside every
+ * super-block, round r of the round-robin over its 8 slots (pairs whose
+ * slots both exist).  Then for each outer round o of the round-robin over
+ * super-blocks and t = 0..7: block i of P with block (i + t) mod 8 of Q for
+ * every super-pair (P, Q), P < Q.  Blocks left without a partner are paired
+ * in increasing order, as identity rotations (J stored as -1 - J).  out:
+ * rounds x nb ints, pair k of round r at out[r * nb + 2k]. */
+static unsigned tl_supers(unsigned nb) {
+  unsigned s = (nb + 7u) / 8u;
+  return s + (s & 1u);
+}
+
+int msqo_two_level_rounds(unsigned nb) { return (int)(7u + 8u * (tl_supers(nb) - 1u)); }
+
+void msqo_two_level_schedule(unsigned nb, int *out) {
+  unsigned supers = tl_supers(nb), rounds = (unsigned)msqo_two_level_rounds(nb);
+  unsigned char *used = (unsigned char *)malloc(nb);
+  for (unsigned r = 0; r < rounds; ++r) {
+    int *row = out + (size_t)r * nb;
+    unsigned k = 0;
+    memset(used, 0, nb);
+    if (r < 7) {
+      for (unsigned S = 0; 8 * S < nb; ++S) {
+        unsigned size = nb - 8 * S < 8 ? nb - 8 * S : 8;
+        for (unsigned x = 0; x < 4; ++x) {
+          unsigned a, b;
+          msqo_jacobi_pair(8, r, x, &a, &b);
+          if (b < size) {
+            row[2 * k] = (int)(8 * S + a);
+            row[2 * k + 1] = (int)(8 * S + b);
+            used[8 * S + a] = used[8 * S + b] = 1;
+            ++k;
+          }
+        }
+      }
+    } else {
+      unsigned o = (r - 7) / 8, t = (r - 7) % 8;
+      for (unsigned x = 0; x < supers / 2; ++x) {
+        unsigned P, Q;
+        msqo_jacobi_pair(supers, o, x, &P, &Q);
+        unsigned sp = 8 * P >= nb ? 0 : (nb - 8 * P < 8 ? nb - 8 * P : 8);
+        unsigned sq = 8 * Q >= nb ? 0 : (nb - 8 * Q < 8 ? nb - 8 * Q : 8);
+        for (unsigned i = 0; i < 8; ++i) {
+          unsigned j = (i + t) % 8;
+          if (i < sp && j < sq) {
+            row[2 * k] = (int)(8 * P + i);
+            row[2 * k + 1] = (int)(8 * Q + j);
+            used[8 * P + i] = used[8 * Q + j] = 1;
+            ++k;
+          }
+        }
+      }
+    }
+    int idle = -1;
+    for (unsigned blk = 0; blk < nb; ++blk) {
+      if (used[blk]) continue;
+      if (idle < 0) { idle = (int)blk; continue; }
+      row[2 * k] = idle;
+      row[2 * k + 1] = -1 - (int)blk;
+      ++k;
+      idle = -1;
+    }
+  }
+  free(used);
+}
+
 /* One parallel-order cyclic Jacobi solve of the symmetric FP32 matrix a
  * (n x n, column-major, overwritten), vectors v (n x n), eigenvalues w.
  * Per round: angles of all disjoint pairs from the round's start matrix in
@@ -388,9 +457,27 @@ static void pivot_sweep(float p[8][8], float q[8][8]) {
   }
 }
 
+int msqo_jacobi_blocked_order(const float *a_in, float *a_out, float *v_out, float *w,
+                              unsigned n, double tol, int max_sweeps, double *off_ratio,
+                              int two_level);
+
 int msqo_jacobi_blocked(const float *a_in, float *a_out, float *v_out, float *w, unsigned n,
                         double tol, int max_sweeps, double *off_ratio) {
+  return msqo_jacobi_blocked_order(a_in, a_out, v_out, w, n, tol, max_sweeps, off_ratio, 0);
+}
+
+/* two_level != 0: the two-level pairing above instead of the round-robin
+ * rule (identity pairs keep their pivot blocks and use Q = I). */
+int msqo_jacobi_blocked_order(const float *a_in, float *a_out, float *v_out, float *w,
+                              unsigned n, double tol, int max_sweeps, double *off_ratio,
+                              int two_level) {
   unsigned m = (n + 7u) & ~7u, nb = m / 4, P = nb / 2;
+  unsigned rounds = two_level ? (unsigned)msqo_two_level_rounds(nb) : nb - 1;
+  int *sched = NULL;
+  if (two_level) {
+    sched = (int *)malloc(sizeof(int) * (size_t)rounds * nb);
+    msqo_two_level_schedule(nb, sched);
+  }
   float *A = (float *)calloc((size_t)m * m, sizeof(float));
   float *V = (float *)calloc((size_t)m * m, sizeof(float));
   float (*Q)[8][8] = malloc(sizeof(float) * 64 * (P ? P : 1));
@@ -410,12 +497,25 @@ int msqo_jacobi_blocked(const float *a_in, float *a_out, float *v_out, float *w,
         if (r != c) off2 += (double)A[r + (size_t)c * m] * A[r + (size_t)c * m];
     ratio = norm2 > 0 ? sqrt(off2 / norm2) : 0.0;
     if (ratio <= tol || sweeps >= max_sweeps) break;
-    for (unsigned round = 0; round + 1 < nb; ++round) {
+    for (unsigned round = 0; round < rounds; ++round) {
       for (unsigned k = 0; k < P; ++k) {
         unsigned I, J;
-        msqo_jacobi_pair(nb, round, k, &I, &J);
+        int rotate = 1;
+        if (sched) {
+          int sj = sched[(size_t)round * nb + 2 * k + 1];
+          I = (unsigned)sched[(size_t)round * nb + 2 * k];
+          rotate = sj >= 0;
+          J = (unsigned)(rotate ? sj : -1 - sj);
+        } else {
+          msqo_jacobi_pair(nb, round, k, &I, &J);
+        }
         bi[k] = I;
         bj[k] = J;
+        if (!rotate) {
+          for (int r = 0; r < 8; ++r)
+            for (int c = 0; c < 8; ++c) Q[k][r][c] = r == c ? 1.0f : 0.0f;
+          continue;
+        }
         float p[8][8];
         unsigned idx[8];
         for (int x = 0; x < 4; ++x) { idx[x] = 4 * I + x; idx[4 + x] = 4 * J + x; }
@@ -481,7 +581,7 @@ int msqo_jacobi_blocked(const float *a_in, float *a_out, float *v_out, float *w,
       if (a_out) a_out[r + (size_t)c * n] = A[r + (size_t)c * m];
     }
   if (off_ratio) *off_ratio = ratio;
-  free(A); free(V); free(Q); free(bi); free(bj);
+  free(A); free(V); free(Q); free(bi); free(bj); free(sched);
   return sweeps;
 }
 

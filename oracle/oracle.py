@@ -58,6 +58,11 @@ def olib() -> ctypes.CDLL:
                                     ctypes.POINTER(ctypes.c_double)]
         lib.msqo_jacobi_blocked.argtypes = [_P, _P, _P, _P, ctypes.c_uint, ctypes.c_double,
                                             ctypes.c_int, ctypes.POINTER(ctypes.c_double)]
+        lib.msqo_jacobi_blocked_order.argtypes = [_P, _P, _P, _P, ctypes.c_uint, ctypes.c_double,
+                                                  ctypes.c_int, ctypes.POINTER(ctypes.c_double),
+                                                  ctypes.c_int]
+        lib.msqo_two_level_rounds.argtypes = [ctypes.c_uint]
+        lib.msqo_two_level_schedule.argtypes = [ctypes.c_uint, _P]
         lib.msqo_jacobi_pair.argtypes = [ctypes.c_uint, ctypes.c_uint, ctypes.c_uint,
                                          ctypes.POINTER(ctypes.c_uint), ctypes.POINTER(ctypes.c_uint)]
         lib.msqo_ff_residual.argtypes = [_P, _P, _P, ctypes.c_uint, _P]
@@ -118,10 +123,22 @@ def jacobi(a: np.ndarray, tol: float = 1e-7, max_sweeps: int = 15):
     return w, V, sweeps, ratio.value
 
 
-def jacobi_blocked(a: np.ndarray, tol: float = 1e-7, max_sweeps: int = 15, with_matrix=False):
+def two_level_schedule(blocks: int) -> np.ndarray:
+    """The two-level pair table for `blocks` 4-index blocks: (rounds, blocks/2,
+    2) int32 pairs (I, J), J = -1 - J for an identity pair."""
+    rounds = olib().msqo_two_level_rounds(blocks)
+    out = np.zeros(rounds * blocks, dtype=np.int32)
+    olib().msqo_two_level_schedule(blocks, out.ctypes.data)
+    return out.reshape(rounds, blocks // 2, 2)
+
+
+def jacobi_blocked(a: np.ndarray, tol: float = 1e-7, max_sweeps: int = 15, with_matrix=False,
+                   two_level=False):
     """The same rotations in the blocked order the CUDA eigensolver uses, with
     the same FP32 roundings: after the same number of sweeps the CUDA kernels
     return the same eigenvalues, eigenvectors and rotated matrix bit for bit.
+    two_level: the two-level pairing the solver uses for orders 257..512 in
+    its blocked and tensor-core eigenvector modes.
     Returns (w, V, sweeps, off_ratio[, final matrix])."""
     n = a.shape[0]
     A = np.asfortranarray(a, dtype=np.float32)
@@ -129,8 +146,9 @@ def jacobi_blocked(a: np.ndarray, tol: float = 1e-7, max_sweeps: int = 15, with_
     V = np.zeros((n, n), dtype=np.float32, order="F")
     w = np.zeros(n, dtype=np.float32)
     ratio = ctypes.c_double()
-    sweeps = olib().msqo_jacobi_blocked(A.ctypes.data, out.ctypes.data, V.ctypes.data,
-                                        w.ctypes.data, n, tol, max_sweeps, ctypes.byref(ratio))
+    sweeps = olib().msqo_jacobi_blocked_order(A.ctypes.data, out.ctypes.data, V.ctypes.data,
+                                              w.ctypes.data, n, tol, max_sweeps,
+                                              ctypes.byref(ratio), int(bool(two_level)))
     if with_matrix:
         return w, V, sweeps, ratio.value, out
     return w, V, sweeps, ratio.value
