@@ -375,7 +375,7 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--count", type=int, default=COUNT)
     ap.add_argument("--sweeps", type=int, default=1)
-    ap.add_argument("--jacobi-tol", type=float, default=1e-4)
+    ap.add_argument("--jacobi-tol", type=float, default=1e-3)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--selector", type=int, default=0,
                     help="batched workload: plans from the trained selector instead of BF16 + sweeps")

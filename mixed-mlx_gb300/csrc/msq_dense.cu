@@ -120,6 +120,9 @@ gemmTNKernel(GemmArgs args) {
 // each product is split exactly with an FMA, sums are two-sums, and the
 // low-order terms accumulate in a separate FP32 compensation (Ogita-Rump-
 // Oishi Dot2).  Per-matrix ||R||_F^2 and ||A||_F^2 reduce into FP64.
+// X is symmetric, so X X is too: only tiles on or above the diagonal are
+// computed, and an off-diagonal tile also writes R_ji = A_ji - (X X)_ij
+// (the same products in the same order as a direct (j, i) tile).
 __global__ void __launch_bounds__(kThreads)
 residualFFKernel(ResidualArgs args) {
   __shared__ __align__(16) float Hs[kBK][kTile + 4];
@@ -179,6 +182,7 @@ residualFFKernel(ResidualArgs args) {
     const float *A = args.a + off;
     const float *AL = args.a_lo ? args.a_lo + off : nullptr;
     float *R = args.r ? args.r + off : nullptr;
+    const bool mirror = w.z > w.y;
     double rn = 0.0, an = 0.0;
 #pragma unroll
     for (int c = 0; c < 4; ++c) {
@@ -200,6 +204,19 @@ residualFFKernel(ResidualArgs args) {
         rn += rv * rv;
         const double av = static_cast<double>(a) + a_lo;
         an += av * av;
+        if (mirror) {
+          const int64_t idt = j + static_cast<int64_t>(i) * n;
+          const float a2 = A[idt];
+          const float lo2 = (AL ? AL[idt] : 0.0f) - comp[r][c];
+          const float t2 = a2 + hi;
+          const float z2 = t2 - a2;
+          const float e2 = (a2 - (t2 - z2)) + (hi - z2) + lo2;
+          const double rv2 = static_cast<double>(t2) + static_cast<double>(e2);
+          if (R) R[idt] = t2 + e2;
+          rn += rv2 * rv2;
+          const double av2 = static_cast<double>(a2) + (AL ? AL[idt] : 0.0f);
+          an += av2 * av2;
+        }
       }
     }
 #pragma unroll
@@ -306,7 +323,8 @@ __global__ void symmetricAddKernel(float *__restrict__ x_hi, float *__restrict__
 }  // namespace
 
 int gemmWork(msq_ctx *ctx, const DeviceBatch *b, int tile, const int4 **work, int *items) {
-  // One list per (layout, tile size); cached on the batch.
+  // One list per (layout, tile size); cached on the batch.  A negative tile
+  // size asks for the upper triangle of tiles only (tj >= ti).
   auto &cache = const_cast<DeviceBatch *>(b)->work_cache;
   for (auto &e : cache) {
     if (e.tile == tile) {
@@ -321,10 +339,12 @@ int gemmWork(msq_ctx *ctx, const DeviceBatch *b, int tile, const int4 **work, in
   for (int i = 0; i < b->count; ++i) ids[i] = i;
   std::stable_sort(ids.begin(), ids.end(),
                    [&](int x, int y) { return b->host_n[x] > b->host_n[y]; });
+  const bool upper = tile < 0;
+  const int size = upper ? -tile : tile;
   for (int mi : ids) {
-    const int t = (b->host_n[mi] + tile - 1) / tile;
+    const int t = (b->host_n[mi] + size - 1) / size;
     for (int ti = 0; ti < t; ++ti)
-      for (int tj = 0; tj < t; ++tj) list.push_back(make_int4(mi, ti, tj, 0));
+      for (int tj = upper ? ti : 0; tj < t; ++tj) list.push_back(make_int4(mi, ti, tj, 0));
   }
   int4 *dev = nullptr;
   MSQ_TRY(cudaCheck(ctx, cudaMalloc(&dev, list.size() * sizeof(int4)), "work list alloc"));
@@ -363,7 +383,7 @@ int gemmTN(msq_ctx *ctx, const DeviceBatch *b, const float *a, const float *bm, 
 int residualFF(msq_ctx *ctx, const DeviceBatch *b, const float *a, const float *x_hi,
                const float *x_lo, float *r, double *norms, const float *a_lo) {
   ResidualArgs args{};
-  MSQ_TRY(gemmWork(ctx, b, kTile, &args.work, &args.items));
+  MSQ_TRY(gemmWork(ctx, b, -kTile, &args.work, &args.items));  // upper tiles
   args.a = a;
   args.a_lo = a_lo;
   args.x_hi = x_hi;

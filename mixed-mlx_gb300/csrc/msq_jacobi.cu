@@ -76,6 +76,8 @@ struct JacobiArgs {
   const int32_t *sched_off;  // per matrix: its table in sched (int2 units), -1 = round-robin
 };
 
+// Shared memory of the sweep kernel: reduction scratch, pair tables, the
+// round's rotations, then the packed tiles (with_tiles).
 __host__ __device__ __forceinline__ size_t sweepSmemLayout(int n, bool with_tiles, size_t *q_off,
                                                            size_t *tile_off) {
   const int m = padded8(n), nb = m / 4, P = nb / 2;
@@ -194,11 +196,16 @@ jacobiSweepKernel(JacobiArgs args) {
 
   float *log = args.log + args.log_offset[mi];
   const int items = ((P + 1) / 2) * (P + 1);
+  // With one pivot per quad, a quad reads its pair of the next round from
+  // the two-level table while the current round runs.
+  const int quads = blockDim.x >> 2, t4 = threadIdx.x & 3;
+  const bool prefetch = sched != nullptr && P <= quads;
+  int2 next_pair = make_int2(0, 0);
+  if (prefetch && (threadIdx.x >> 2) < P) next_pair = sched[threadIdx.x >> 2];
   for (int round = 0; round < rounds; ++round) {
     // Pivots: a quad of lanes per block pair.  The loop is warp-uniform (all
     // lanes of a warp take part in the quad shuffles; lanes past P idle).
     // An identity pair of the two-level table keeps its blocks and logs Q = I.
-    const int quads = blockDim.x >> 2, t4 = threadIdx.x & 3;
     for (int base = 0; base < P; base += quads) {
       const int k = base + (threadIdx.x >> 2);
       const bool present = k < P;
@@ -206,7 +213,14 @@ jacobiSweepKernel(JacobiArgs args) {
       float ra[8], rb[8];
       int tII = 0, tIJ = 0, tJJ = 0, I = 0, J = 0;
       if (present) {
-        roundPair(sched, k, round, nb, I, J, active);
+        if (prefetch) {
+          I = next_pair.x;
+          active = next_pair.y >= 0;
+          J = active ? next_pair.y : -1 - next_pair.y;
+          if (round + 1 < rounds) next_pair = sched[(round + 1) * P + k];
+        } else {
+          roundPair(sched, k, round, nb, I, J, active);
+        }
         if (t4 == 0) {
           pair_i[k] = I;
           pair_j[k] = J;
@@ -268,16 +282,21 @@ jacobiSweepKernel(JacobiArgs args) {
     // needs, and lane h forms rows 4h..4h+3 of T' = U Q_l.  Every element is
     // the same ordered FMA chain as in one-lane form (u over i, t' over j).
     // The loop is warp-uniform so the pair shuffle has all lanes present.
-    for (int base = threadIdx.x & ~31; base < 2 * items; base += blockDim.x) {
+    auto itemAt = [&](int base, int &k, int &l, int &h) {
       const int w2 = base + (threadIdx.x & 31);
-      const int h = w2 & 1;
-      int k = 0, l = 0;
+      h = w2 & 1;
+      k = l = 0;
       const bool valid = w2 < 2 * items && foldedBlock(w2 >> 1, P, k, l) && k != l;
       if (!valid) k = l = 0;
-      const int rb0 = pair_i[k], rb1 = pair_j[k];
+      return valid;
+    };
+    for (int base = threadIdx.x & ~31; base < 2 * items; base += blockDim.x) {
+      int k, l, h;
+      const bool valid = itemAt(base, k, l, h);
       const float4 *qk = reinterpret_cast<const float4 *>(qs + k * kQS);
       const float4 *ql = reinterpret_cast<const float4 *>(qs + l * kQS);
-      superTileHalf(tiles, SharedTri{tri}, qk, ql, rb0, rb1, pair_i[l], pair_j[l], h, valid);
+      superTileHalf(tiles, SharedTri{tri}, qk, ql, pair_i[k], pair_j[k], pair_i[l], pair_j[l], h,
+                    valid);
     }
     __syncthreads();
   }

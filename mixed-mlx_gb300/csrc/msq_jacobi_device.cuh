@@ -147,6 +147,14 @@ __device__ __forceinline__ int64_t tileElement(int t, int i, int j) {
 
 // Loads block (R, C) of A (4x4, row-major in t) from packed tile ti, which
 // holds (min, max) of the two block indices (transposed when R > C).
+// 16-byte asynchronous global -> shared copies (cp.async, L2 only).
+__device__ __forceinline__ void copyAsync16(void *smem, const void *gmem) {
+  const unsigned dst = static_cast<unsigned>(__cvta_generic_to_shared(smem));
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(dst), "l"(gmem) : "memory");
+}
+__device__ __forceinline__ void copyAsyncCommit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+__device__ __forceinline__ void copyAsyncWaitAll() { asm volatile("cp.async.wait_group 0;\n" ::: "memory"); }
+
 __device__ __forceinline__ void loadTile(const float *tiles, int ti, bool transposed, float (&t)[4][4]) {
   const float4 *src = reinterpret_cast<const float4 *>(tiles + static_cast<int64_t>(ti) * kTileF);
 #pragma unroll
@@ -400,6 +408,11 @@ struct ComputedTri {
   }
 };
 
+template <class TileOf>
+__device__ __forceinline__ void superTileHalf(float *tiles, TileOf tileOf, const float4 *qk,
+                                              const float4 *ql, int rb0, int rb1, int cb0, int cb1,
+                                              int h, bool valid);
+
 // Super-tile update T' = Q_k^T T Q_l on two lanes (h = 0, 1 of an adjacent
 // pair; the warp's lanes must all call it).  T is the 8x8 block of A on row
 // blocks (rb0, rb1) of pair k and column blocks (cb0, cb1) of pair l; qk, ql
@@ -409,10 +422,21 @@ struct ComputedTri {
 // 4h..4h+3 of T' = U Q_l.  Every element is the ordered FMA chain of the
 // one-lane form (u over i, t' over j), as the CPU restatement.  Invalid
 // lanes compute on zeros and store nothing.
+// Source of the two input blocks: the tile store itself ...
 template <class TileOf>
-__device__ __forceinline__ void superTileHalf(float *tiles, TileOf tileOf, const float4 *qk,
-                                              const float4 *ql, int rb0, int rb1, int cb0, int cb1,
-                                              int h, bool valid) {
+struct TileSource {
+  const float *tiles;
+  TileOf tileOf;
+  __device__ __forceinline__ void operator()(int R, int C, int, float (&t)[4][4]) const {
+    bool tr;
+    const int ti = tileOf(R, C, tr);
+    loadTile(tiles, ti, tr, t);
+  }
+};
+template <class TileOf, class Source>
+__device__ __forceinline__ void superTileHalf(float *tiles, TileOf tileOf, const Source &source,
+                                              const float4 *qk, const float4 *ql, int rb0, int rb1,
+                                              int cb0, int cb1, int h, bool valid) {
   const int cbh = h ? cb1 : cb0;
   float u[8][4];
 #pragma unroll
@@ -423,9 +447,7 @@ __device__ __forceinline__ void superTileHalf(float *tiles, TileOf tileOf, const
   for (int x = 0; x < 2; ++x) {
     float b4[4][4];
     if (valid) {
-      bool tr;
-      const int ti = tileOf(x ? rb1 : rb0, cbh, tr);
-      loadTile(tiles, ti, tr, b4);
+      source(x ? rb1 : rb0, cbh, x, b4);
     } else {
 #pragma unroll
       for (int i = 0; i < 4; ++i)
@@ -485,6 +507,15 @@ __device__ __forceinline__ void superTileHalf(float *tiles, TileOf tileOf, const
   }
 }
 
+template <class TileOf>
+__device__ __forceinline__ void superTileHalf(float *tiles, TileOf tileOf, const float4 *qk,
+                                              const float4 *ql, int rb0, int rb1, int cb0, int cb1,
+                                              int h, bool valid) {
+  superTileHalf(tiles, tileOf, TileSource<TileOf>{tiles, tileOf}, qk, ql, rb0, rb1, cb0, cb1, h,
+                valid);
+}
+
+
 // TMA bulk copies (cp.async.bulk) of a contiguous block between global and
 // shared memory; both addresses 16-byte aligned, size a multiple of 16.  The
 // load completes on an mbarrier (expect_tx); the wait is bounded.
@@ -533,13 +564,6 @@ __device__ __forceinline__ void bulkStoreTiles(void *gmem, const void *smem, uin
   asm volatile("cp.async.bulk.wait_group 0;" ::: "memory");
 }
 
-// 16-byte asynchronous global -> shared copies (cp.async, L2 only).
-__device__ __forceinline__ void copyAsync16(void *smem, const void *gmem) {
-  const unsigned dst = static_cast<unsigned>(__cvta_generic_to_shared(smem));
-  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(dst), "l"(gmem) : "memory");
-}
-__device__ __forceinline__ void copyAsyncCommit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
-__device__ __forceinline__ void copyAsyncWaitAll() { asm volatile("cp.async.wait_group 0;\n" ::: "memory"); }
 
 }  // namespace
 }  // namespace msq

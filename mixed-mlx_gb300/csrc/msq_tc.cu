@@ -405,8 +405,18 @@ struct SplitArgs {
   uint8_t *out[3];
 };
 
-template <bool kTranspose>
+template <bool kTranspose, bool kLo>
 __global__ void __launch_bounds__(128) packSplitKernel(SplitArgs args) {
+  // kTranspose false reads operand row i from column i of M: the tile's 128
+  // columns x 64 rows are staged in shared memory with coalesced loads (a
+  // warp reads 32 consecutive elements of one column, eight columns in
+  // flight), then each thread reads its row there (stride 65: no bank
+  // conflicts).  kLo: M is float-float (hi + lo).
+  constexpr int kLd = 65;
+  constexpr int kStage = kTranspose ? 1 : kTileRows * kLd;
+  __shared__ float stage_hi[kStage];
+  __shared__ float stage_lo[kLo ? kStage : 1];
+  const int warp = threadIdx.x / 32, lane = threadIdx.x % 32;
   for (int item = blockIdx.x; item < args.items; item += gridDim.x) {
     const int4 w = args.work[item];
     const int mi = w.x, n = args.n[mi];
@@ -414,8 +424,35 @@ __global__ void __launch_bounds__(128) packSplitKernel(SplitArgs args) {
     const int i = w.y * kTileRows + r;
     const int k0 = w.z * 64;
     const float *H = args.hi + args.offset[mi];
-    const float *L = args.lo ? args.lo + args.offset[mi] : nullptr;
+    const float *L = kLo ? args.lo + args.offset[mi] : nullptr;
     const int64_t tile = (args.tile_base[mi] + static_cast<int64_t>(w.y) * w.w + w.z) * kTileBytes;
+    if (!kTranspose) {
+      __syncthreads();  // the previous item's rows have been read
+#pragma unroll 1
+      for (int c0 = 8 * warp; c0 < kTileRows; c0 += 32) {
+        float xh[8][2], xl[8][2];
+#pragma unroll
+        for (int q = 0; q < 8; ++q) {
+          const int col = w.y * kTileRows + c0 + q;
+#pragma unroll
+          for (int h = 0; h < 2; ++h) {
+            const int k = k0 + lane + 32 * h;
+            const bool in = col < n && k < n;
+            const int64_t at = k + static_cast<int64_t>(col) * n;
+            xh[q][h] = in ? H[at] : 0.0f;
+            xl[q][h] = kLo && in ? L[at] : 0.0f;
+          }
+        }
+#pragma unroll
+        for (int q = 0; q < 8; ++q)
+#pragma unroll
+          for (int h = 0; h < 2; ++h) {
+            stage_hi[(c0 + q) * kLd + lane + 32 * h] = xh[q][h];
+            if (kLo) stage_lo[(c0 + q) * kLd + lane + 32 * h] = xl[q][h];
+          }
+      }
+      __syncthreads();
+    }
 #pragma unroll 1
     for (int c = 0; c < 8; ++c) {
       uint32_t word[3][4] = {};
@@ -423,11 +460,15 @@ __global__ void __launch_bounds__(128) packSplitKernel(SplitArgs args) {
       for (int e = 0; e < 8; ++e) {
         const int k = k0 + c * 8 + e;
         float x = 0.0f, xl = 0.0f;
-        if (i < n && k < n) {
-          const int64_t at = kTranspose ? i + static_cast<int64_t>(k) * n
-                                        : k + static_cast<int64_t>(i) * n;
-          x = H[at];
-          xl = L ? L[at] : 0.0f;
+        if (kTranspose) {
+          if (i < n && k < n) {
+            const int64_t at = i + static_cast<int64_t>(k) * n;
+            x = H[at];
+            xl = kLo ? L[at] : 0.0f;
+          }
+        } else {
+          x = stage_hi[r * kLd + c * 8 + e];
+          xl = kLo ? stage_lo[r * kLd + c * 8 + e] : 0.0f;
         }
         const uint32_t h0 = encodeBf16(x);
         const float rem = (x - decodeBf16(static_cast<uint16_t>(h0))) + xl;
@@ -672,9 +713,11 @@ int packSplit(msq_ctx *ctx, const DeviceBatch *b, TcPlan *p, const float *hi, co
   for (int q = 0; q < pieces; ++q) args.out[q] = out[q];
   const unsigned grid = std::min(p->pack_items, kSmCount * 16);
   if (transpose) {
-    packSplitKernel<true><<<grid, 128, 0, ctx->stream>>>(args);
+    if (lo) packSplitKernel<true, true><<<grid, 128, 0, ctx->stream>>>(args);
+    else packSplitKernel<true, false><<<grid, 128, 0, ctx->stream>>>(args);
   } else {
-    packSplitKernel<false><<<grid, 128, 0, ctx->stream>>>(args);
+    if (lo) packSplitKernel<false, true><<<grid, 128, 0, ctx->stream>>>(args);
+    else packSplitKernel<false, false><<<grid, 128, 0, ctx->stream>>>(args);
   }
   return launched(ctx, "pack split-BF16");
 }
