@@ -149,13 +149,21 @@ int msq_jacobi_batched(msq_ctx *ctx, float *matrices, float *vectors,
  *   MSQ_VECTORS_TENSOR  (2) two-level pairing; each stage's 64x64 rotations
  *                       applied to V held in TMEM by tcgen05.mma in split
  *                       BF16 (hi*hi + lo*hi + hi*lo, FP32 accumulation): V
- *                       orthonormal to about 1e-4, eigenvalues unchanged.
+ *                       orthonormal to about 1e-4, eigenvalues unchanged;
+ *   MSQ_VECTORS_TENSOR_A (3) two-level pairing; a stage's rounds rotate only
+ *                       the 64x64 diagonal blocks (CUDA cores) and the rest
+ *                       of A is brought up to date once per stage on the
+ *                       tensor cores (B = A Z, A = B^T Z, split BF16), V as
+ *                       in mode 2.  Eigenvalues to about 1e-4 ||A||; slower
+ *                       than mode 2 on GB300 (the per-stage passes stream
+ *                       A through HBM twice).
  * The mode applies to later calls on the context.                          */
 enum {
   MSQ_VECTORS_AUTO = -1,
   MSQ_VECTORS_REPLAY = 0,
   MSQ_VECTORS_BLOCKED = 1,
-  MSQ_VECTORS_TENSOR = 2
+  MSQ_VECTORS_TENSOR = 2,
+  MSQ_VECTORS_TENSOR_A = 3
 };
 int msq_set_jacobi_vectors(msq_ctx *ctx, int mode);
 /* The two-level pair table for `blocks` 4-index blocks (even, 2..4096),

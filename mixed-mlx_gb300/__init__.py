@@ -36,7 +36,7 @@ FORMAT_NAMES = {
 # Plans (msq_plan_format)
 PLAN_FP32, PLAN_BF16, PLAN_FP8, PLAN_MXFP4 = range(4)
 # msq_set_jacobi_vectors modes
-VECTORS_AUTO, VECTORS_REPLAY, VECTORS_BLOCKED, VECTORS_TENSOR = -1, 0, 1, 2
+VECTORS_AUTO, VECTORS_REPLAY, VECTORS_BLOCKED, VECTORS_TENSOR, VECTORS_TENSOR_A = -1, 0, 1, 2, 3
 
 MLP_IN, MLP_HIDDEN, MLP_OUT = 16, 64, 8
 MLP_PARAMS = (MLP_IN * MLP_HIDDEN + MLP_HIDDEN + MLP_HIDDEN * MLP_HIDDEN +
@@ -232,7 +232,8 @@ class Context:
 
     def set_jacobi_vectors(self, mode: int) -> None:
         """Eigenvector mode of the batched Jacobi for 256 < n <= 512:
-        VECTORS_AUTO, VECTORS_REPLAY, VECTORS_BLOCKED or VECTORS_TENSOR."""
+        VECTORS_AUTO, VECTORS_REPLAY, VECTORS_BLOCKED, VECTORS_TENSOR or
+        VECTORS_TENSOR_A."""
         self.check(lib().msq_set_jacobi_vectors(self.handle, int(mode)), "msq_set_jacobi_vectors")
 
     def synchronize(self) -> None:

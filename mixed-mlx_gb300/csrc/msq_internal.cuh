@@ -112,7 +112,8 @@ struct msq_ctx {
   bool concurrent = true;
   // Eigenvector accumulation of the batched Jacobi for 256 < n <= 512
   // (msq_set_jacobi_vectors): -1 automatic, 0 round-robin + FP32 replay,
-  // 1 two-level pairing + FP32 replay, 2 two-level pairing + tensor cores.
+  // 1 two-level pairing + FP32 replay, 2 two-level pairing + V on the
+  // tensor cores, 3 two-level pairing + A and V on the tensor cores.
   int jacobi_vectors = -1;
   // Per-layout work plans of the Jacobi and of the tensor-core GEMMs.
   msq::JacobiPlanCache *jacobi_plans = nullptr;

@@ -642,6 +642,10 @@ struct JacobiPlan {
   const int32_t *sched_off = nullptr;
   TcVectorsDevice tcv;
   int64_t tcv_images = 0;
+  // mode 2: the two-level tensor-core Jacobi for 256 < n <= 512 (tl),
+  // its B scratch (elements of the batch) and diagonal blocks
+  TwoLevelDevice tl;
+  int64_t batch_elements = 0, diag_blocks = 0;
   void *device = nullptr;
 };
 
@@ -700,7 +704,7 @@ JacobiPlan *planFor(msq_ctx *ctx, const DeviceBatch *b, int mode) {
   std::vector<int64_t> t_off(total, 0), l_off(total, 0);
   std::vector<int32_t> sched_off(total, -1), sched_host, table;
   std::map<int, int32_t> sched_at;  // block count -> table offset (int2 units)
-  std::vector<int> tc_ids;
+  std::vector<int> tc_ids, tl_ids;  // V on the tensor cores; A too (mode 3)
   std::vector<char> on_tc(total, 0);
   for (int i = 0; i < total; ++i) {
     const int n = b->host_n[i];
@@ -708,9 +712,17 @@ JacobiPlan *planFor(msq_ctx *ctx, const DeviceBatch *b, int mode) {
       plan->grid_ids.push_back(i);
       continue;
     }
-    ids.push_back(i);
     const int m = padded8(n), nb = m / 4, P = nb / 2;
     const bool two_level = mode != 0 && n >= kTwoLevelMinOrder && n <= kTwoLevelMaxOrder;
+    if (two_level && mode == 3) {
+      // the two-level Jacobi with tensor-core updates of A: no packed
+      // tiles, no rotation log
+      tc_ids.push_back(i);
+      tl_ids.push_back(i);
+      on_tc[i] = 1;
+      continue;
+    }
+    ids.push_back(i);
     t_off[i] = plan->tile_total;
     plan->tile_total += static_cast<int64_t>(nb) * (nb + 1) / 2 * kTileF;
     l_off[i] = plan->log_total;
@@ -731,6 +743,11 @@ JacobiPlan *planFor(msq_ctx *ctx, const DeviceBatch *b, int mode) {
   }
   TcVectorsTables tcv;
   tcVectorsTables(b->host_n.data(), total, tc_ids, tcv);
+  TwoLevelTables tlt;
+  twoLevelTables(b->host_n.data(), total, tl_ids, tlt);
+  for (int i = 0; i < total; ++i)
+    plan->batch_elements = std::max<int64_t>(
+        plan->batch_elements, b->host_offset[i] + static_cast<int64_t>(b->host_n[i]) * b->host_n[i]);
   const int count = static_cast<int>(ids.size());
   // buckets by size class, largest class first
   std::stable_sort(ids.begin(), ids.end(), [&](int x, int y) {
@@ -781,6 +798,9 @@ JacobiPlan *planFor(msq_ctx *ctx, const DeviceBatch *b, int mode) {
   const size_t at_po = carve.take<int32_t>(total);
   const size_t at_fw = carve.take<int32_t>(tcv.form_work.size());
   const size_t at_aw = carve.take<int32_t>(tcv.apply_work.size());
+  const size_t at_tl_ids = carve.take<int32_t>(tlt.ids.size());
+  const size_t at_tl_inner = carve.take<int32_t>(tlt.inner.size());
+  const size_t at_tl_diag = carve.take<int64_t>(total);
   char *dev = nullptr;
   if (cudaCheck(ctx, cudaMalloc(&dev, carve.bytes + 16), "jacobi plan alloc") != MSQ_OK) {
     delete plan;
@@ -820,6 +840,18 @@ JacobiPlan *planFor(msq_ctx *ctx, const DeviceBatch *b, int mode) {
     put(at_prog, tcv.prog.data(), tcv.prog.size() * sizeof(int32_t));
     put(at_po, tcv.prog_off.data(), total * sizeof(int32_t));
     put(at_img, tcv.image_off.data(), total * sizeof(int64_t));
+  }
+  if (!tl_ids.empty()) {
+    plan->tl.ids = reinterpret_cast<const int32_t *>(dev + at_tl_ids);
+    plan->tl.count = static_cast<int>(tlt.ids.size());
+    plan->tl.inner = reinterpret_cast<const int2 *>(dev + at_tl_inner);
+    plan->tl.stage_first = tlt.stage_first;
+    plan->tl.stage_count = tlt.stage_count;
+    plan->tl.diag_off = reinterpret_cast<const int64_t *>(dev + at_tl_diag);
+    plan->diag_blocks = tlt.diag_blocks;
+    put(at_tl_ids, tlt.ids.data(), tlt.ids.size() * sizeof(int32_t));
+    put(at_tl_inner, tlt.inner.data(), tlt.inner.size() * sizeof(int32_t));
+    put(at_tl_diag, tlt.diag_off.data(), total * sizeof(int64_t));
   }
   if (plans.size() >= 8) {
     cudaFree(plans.front()->device);
@@ -865,11 +897,20 @@ int jacobiEnqueue(msq_ctx *ctx, const DeviceBatch *b, float *matrices, float *ve
   const size_t tile_bytes = (plan->tile_total * sizeof(float) + 255) & ~size_t(255);
   // Two log buffers (sweep parity) so sweep k+1 overlaps the replay of k.
   const size_t log_bytes = (2 * plan->log_total * sizeof(float) + 1023) & ~size_t(1023);
-  const size_t image_bytes = static_cast<size_t>(plan->tcv_images) * kRotationImageBytes;
-  char *work = static_cast<char *>(
-      scratch(ctx, state_bytes + tile_bytes + log_bytes + image_bytes, kScratchJacobi));
+  // rotation images double-buffered by sweep parity (the V update of sweep
+  // k reads them while sweep k + 1 writes the other set); two-level B
+  // scratch and diagonal blocks
+  const size_t image_set = static_cast<size_t>(plan->tcv_images) * kRotationImageBytes;
+  const size_t b_bytes = plan->tl.count > 0
+                             ? (static_cast<size_t>(plan->batch_elements) * sizeof(float) + 255) & ~size_t(255)
+                             : 0;
+  const size_t diag_bytes = static_cast<size_t>(plan->diag_blocks) * 4096 * sizeof(float);
+  char *work = static_cast<char *>(scratch(
+      ctx, state_bytes + tile_bytes + log_bytes + 2 * image_set + b_bytes + diag_bytes, kScratchJacobi));
   if (work == nullptr) return MSQ_ERR_CUDA;
   uint8_t *images = reinterpret_cast<uint8_t *>(work + state_bytes + tile_bytes + log_bytes);
+  float *b_scratch = reinterpret_cast<float *>(work + state_bytes + tile_bytes + log_bytes + 2 * image_set);
+  float *diag = reinterpret_cast<float *>(work + state_bytes + tile_bytes + log_bytes + 2 * image_set + b_bytes);
   if (setKernelAttributes() != MSQ_OK) return cudaCheck(ctx, cudaGetLastError(), "jacobi attributes");
   JacobiArgs args{};
   args.a = matrices;
@@ -959,7 +1000,9 @@ int jacobiEnqueue(msq_ctx *ctx, const DeviceBatch *b, float *matrices, float *ve
   // has the GPU to itself.
   syncReset(ctx);
   const bool serial = !ctx->concurrent || measuring;
-  const int sweep_streams = std::min<int>(3, static_cast<int>(plan->buckets.size()));
+  // the two-level group takes the stream after the buckets'
+  const int groups = static_cast<int>(plan->buckets.size()) + (plan->tl.count > 0 ? 1 : 0);
+  const int sweep_streams = std::min<int>(3, groups);
   cudaStream_t ss[3];
   for (int i = 0; i < sweep_streams; ++i) {
     ss[i] = serial ? ctx->stream : auxStream(ctx, 1 + i);
@@ -1002,6 +1045,13 @@ int jacobiEnqueue(msq_ctx *ctx, const DeviceBatch *b, float *matrices, float *ve
         g_pending.push_back({ctx->device, bucket.cls, how.measure, t0, t1, bucket.count});
       }
     }
+    if (plan->tl.count > 0) {
+      cudaStream_t s = ss[plan->buckets.size() % sweep_streams];
+      MSQ_TRY(twoLevelEnqueue(ctx, s, plan->tl, plan->tcv, matrices, b_scratch, diag,
+                              images + parity * image_set, b->offset, b->n, b->eig_offset,
+                              eigenvalues, args.state, tolerance, max_sweeps, launch == 0,
+                              launch < max_sweeps, parity));
+    }
     if (launch < max_sweeps) {
       for (int i = 0; i < sweep_streams; ++i) MSQ_TRY(streamWait(ctx, rs, ss[i]));
       vargs.parity = parity;
@@ -1015,7 +1065,8 @@ int jacobiEnqueue(msq_ctx *ctx, const DeviceBatch *b, float *matrices, float *ve
         MSQ_TRY(launchedOn(ctx, rs, "jacobi replay"));
       }
       MSQ_TRY(tcVectorsEnqueue(ctx, rs, plan->tcv, vectors, b->offset, b->n, args.state, args.log,
-                               plan->log_offset, images, parity));
+                               plan->log_offset, images + parity * image_set, parity,
+                               plan->tl.count == 0));
       replay_done[parity] = syncEvent(ctx);
       MSQ_TRY(cudaCheck(ctx, cudaEventRecord(replay_done[parity], rs), "event record"));
     }

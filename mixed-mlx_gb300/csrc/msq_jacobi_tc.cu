@@ -209,8 +209,9 @@ __global__ void __launch_bounds__(kFormThreads) tcvFormKernel(FormArgs args) {
   copyAsyncWaitAll();
   __syncwarp();
   if (!owner) return;
-  // B operand rows j (output columns), K = the 64 local indices: Z^T,
-  // halves j < 32 (super-block P) and j >= 32 (super-block Q), hi and lo.
+  // B operand rows j (output columns), K = the 64 local indices: Z^T, as
+  // hi rows 0..63 then lo rows 0..63 (rows 32..63, super-block Q, start
+  // 4 KB into each term).
   uint8_t *img = args.images +
                  (args.image_off[mi] + static_cast<int64_t>(stage) * pairs + warp) * kRotationImageBytes;
 #pragma unroll 1
@@ -222,9 +223,9 @@ __global__ void __launch_bounds__(kFormThreads) tcvFormKernel(FormArgs args) {
 #pragma unroll
       for (int p = 0; p < 4; ++p)
         splitPair(z[(8 * c + 2 * p) * kFormLd + j], z[(8 * c + 2 * p + 1) * kFormLd + j], hi[p], lo[p]);
-      const uint32_t at = swizzle128(lane, c);
-      *reinterpret_cast<uint4 *>(img + (2 * h) * 4096 + at) = make_uint4(hi[0], hi[1], hi[2], hi[3]);
-      *reinterpret_cast<uint4 *>(img + (2 * h + 1) * 4096 + at) = make_uint4(lo[0], lo[1], lo[2], lo[3]);
+      const uint32_t at = swizzle128(j, c);
+      *reinterpret_cast<uint4 *>(img + at) = make_uint4(hi[0], hi[1], hi[2], hi[3]);
+      *reinterpret_cast<uint4 *>(img + kImageTermBytes + at) = make_uint4(lo[0], lo[1], lo[2], lo[3]);
     }
   }
 }
@@ -346,7 +347,8 @@ __global__ void __launch_bounds__(kApplyThreads, 1) tcvApplyKernel(ApplyArgs arg
             if (S >= real) continue;
             const uint32_t d = tmem + 32 * S;
             const uint64_t ah = smemDesc(a_hi), al = smemDesc(a_lo);
-            const uint64_t zh = smemDesc(zimg + h * 8192), zl = smemDesc(zimg + h * 8192 + 4096);
+            const uint64_t zh = smemDesc(zimg + h * 4096);
+            const uint64_t zl = smemDesc(zimg + kImageTermBytes + h * 4096);
 #pragma unroll
             for (int kk = 0; kk < 4; ++kk) {
               mmaBf16(d, ah + 2 * kk, zh + 2 * kk, idesc, kk > 0);
@@ -456,6 +458,446 @@ __global__ void __launch_bounds__(kApplyThreads, 1) tcvApplyKernel(ApplyArgs arg
   }
 }
 
+// ---------------------------------------------------------------------------
+// Two-level Jacobi with the off-diagonal work on the tensor cores.
+//
+// With the two-level pairing, the rounds of a stage rotate only inside the
+// stage's 64-index super-pairs.  So each stage can run its rounds on the
+// 64x64 diagonal blocks alone (tlInnerKernel: the quad-pivot sweep and
+// super-tile updates of the batched kernel on 16 local blocks, with the
+// stage rotation Z of the block accumulated in shared memory as it goes),
+// and bring the rest of A up to date once per stage: A' = Z^T A Z with
+// block-diagonal Z, as two tcgen05 passes B = A Z and A' = B^T Z (A' is
+// symmetric; tlPassKernel, split-BF16 operands, FP32 accumulation).  The
+// second pass takes the diagonal blocks from the inner kernel.  The stage
+// rotations are the operand images the V update applies after the sweep.
+
+constexpr int kInnerThreads = 128;
+constexpr int kLocalBlocks = 16;
+constexpr int kLocalTiles = kLocalBlocks * (kLocalBlocks + 1) / 2;
+constexpr int kPassRows = 128;
+constexpr int kPassThreads = 160;        // warps 0-3 rows, warp 4 TMEM + MMA + copies
+constexpr uint32_t kPassTmemCols = 64;
+constexpr int kStageLd = 65;
+constexpr size_t kPassSmem = 2 * kOperandBytes + kRotationImageBytes +
+                             static_cast<size_t>(kPassRows) * kStageLd * sizeof(float) + 1024 + 256;
+
+struct CheckArgs {
+  float *a;
+  const int64_t *a_offset;
+  const int32_t *n;
+  const int64_t *eig_offset;
+  float *eigenvalues;
+  JacobiState *state;
+  const int32_t *ids;
+  double tol;
+  int max_sweeps;
+  int first;
+  int parity;
+};
+
+// Convergence check before a sweep (and, on the first launch, the symmetrised
+// input and ||A||_F^2): the state and the eigenvalues of a converged matrix.
+__global__ void __launch_bounds__(256) tlCheckKernel(CheckArgs args) {
+  __shared__ double red[32];
+  const int mi = args.ids[blockIdx.x];
+  JacobiState &st = args.state[mi];
+  const JacobiState s0 = st;
+  if (!args.first && s0.done) {
+    if (threadIdx.x == 0) st.logged[args.parity] = 0;
+    return;
+  }
+  const int n = args.n[mi];
+  float *A = args.a + args.a_offset[mi];
+  if (args.first) {
+    // A <- (A + A^T) / 2 (working_from_symmetric_f32, metal_mixed_sqrt.metal:1349-1350)
+    const int64_t pairs = static_cast<int64_t>(n) * (n - 1) / 2;
+    for (int64_t q = threadIdx.x; q < pairs; q += blockDim.x) {
+      int j = static_cast<int>((1.0 + sqrt(1.0 + 8.0 * static_cast<double>(q))) / 2.0);
+      while (static_cast<int64_t>(j) * (j - 1) / 2 > q) --j;
+      while (static_cast<int64_t>(j + 1) * j / 2 <= q) ++j;
+      const int i = static_cast<int>(q - static_cast<int64_t>(j) * (j - 1) / 2);
+      const int64_t ij = i + static_cast<int64_t>(j) * n, ji = j + static_cast<int64_t>(i) * n;
+      const float v = 0.5f * (A[ij] + A[ji]);
+      A[ij] = v;
+      A[ji] = v;
+    }
+    __syncthreads();
+  }
+  double off2 = 0.0, diag2 = 0.0;
+  const int64_t nn = static_cast<int64_t>(n) * n;
+  for (int64_t q = threadIdx.x; q < nn; q += blockDim.x) {
+    const double v = A[q];
+    if (q % (n + 1) == 0) diag2 += v * v;
+    else off2 += v * v;
+  }
+  off2 = blockReduceSum(off2, red);
+  diag2 = blockReduceSum(diag2, red);
+  const double norm2 = args.first ? off2 + diag2 : s0.norm2;
+  const int sweeps = args.first ? 0 : s0.sweeps;
+  const double ratio = norm2 > 0.0 ? sqrt(off2 / norm2) : 0.0;
+  const bool stop = ratio <= args.tol || sweeps >= args.max_sweeps;
+  if (stop) {
+    float *eig = args.eigenvalues + args.eig_offset[mi];
+    for (int k = threadIdx.x; k < n; k += blockDim.x) eig[k] = A[k + static_cast<int64_t>(k) * n];
+  }
+  if (threadIdx.x == 0) {
+    st.norm2 = norm2;
+    st.off_ratio = ratio;
+    st.sweeps = stop ? sweeps : sweeps + 1;
+    st.done = stop ? 1 : 0;
+    st.logged[args.parity] = stop ? 0 : 1;
+  }
+}
+
+struct InnerArgs {
+  const float *a;
+  const int64_t *a_offset;
+  const int32_t *n;
+  const JacobiState *state;
+  const int2 *work;          // (matrix, super-pair) of this stage
+  const int32_t *prog;
+  const int32_t *prog_off;
+  const int64_t *image_off;
+  uint8_t *images;
+  float *diag;               // rotated 64x64 diagonal blocks (row-major, local order)
+  const int64_t *diag_off;   // per matrix: first block (one per super-pair)
+  int stage;
+};
+
+// Local index li (0..63) of super-pair (P, Q) -> global index, -1 outside A.
+__device__ __forceinline__ int localToGlobal(int li, int Ps, int Qs, int n) {
+  const int g = li < 32 ? 32 * Ps + li : 32 * Qs + li - 32;
+  return g < n ? g : -1;
+}
+
+__global__ void __launch_bounds__(kInnerThreads) tlInnerKernel(InnerArgs args) {
+  __shared__ __align__(16) float tiles[kLocalTiles * kTileF];
+  __shared__ __align__(16) float z[64 * kFormLd];
+  __shared__ __align__(16) float qs[8 * kQS];
+  __shared__ int tri[kLocalBlocks + 1];
+  __shared__ int pair_i[8], pair_j[8], pair_on[8];
+  const int2 w = args.work[blockIdx.x];
+  const int mi = w.x, x = w.y;
+  if (args.state[mi].done) return;
+  const int n = args.n[mi], m = padded8(n), nb = m / 4;
+  const int supers = twoLevelSupers(nb), pairs = supers / 2;
+  int Ps, Qs;
+  rrPair(x, args.stage, supers, Ps, Qs);
+  const float *A = args.a + args.a_offset[mi];
+  const int tid = threadIdx.x, warp = tid >> 5;
+  for (int k = tid; k <= kLocalBlocks; k += blockDim.x) tri[k] = k * (k + 1) / 2;
+  for (int i = tid; i < 64; i += blockDim.x)
+    for (int c = 0; c < 64; c += 4)
+      *reinterpret_cast<float4 *>(z + i * kFormLd + c) =
+          make_float4(i == c, i == c + 1, i == c + 2, i == c + 3);
+  __syncthreads();
+  for (int J = 0; J < kLocalBlocks; ++J) {
+    for (int idx = tid; idx < (J + 1) * kTileF; idx += blockDim.x) {
+      const int I = idx / kTileF, e = idx % kTileF;
+      const int gi = localToGlobal(4 * I + e / 4, Ps, Qs, n);
+      const int gj = localToGlobal(4 * J + e % 4, Ps, Qs, n);
+      tiles[tileElement(tri[J] + I, e / 4, e % 4)] =
+          gi >= 0 && gj >= 0 ? A[gi + static_cast<int64_t>(gj) * n] : 0.0f;
+    }
+  }
+  const int32_t *prog = args.prog + args.prog_off[mi];
+  const int r0 = twoLevelStageFirst(args.stage), rounds = twoLevelStageRounds(args.stage);
+  for (int t = 0; t < rounds; ++t) {
+    const int r = r0 + t;
+    if (tid == 0) {
+      // the round's rotating pairs, then the other local blocks paired in
+      // order with the identity
+      unsigned used = 0;
+      int cnt = 0;
+      for (int e = 0; e < 8; ++e) {
+        const int code = prog[(r * pairs + x) * 8 + e];
+        if (code < 0) break;
+        const int la = (code >> 8) & 255, lb = code >> 16;
+        pair_i[cnt] = la;
+        pair_j[cnt] = lb;
+        pair_on[cnt] = 1;
+        used |= (1u << la) | (1u << lb);
+        ++cnt;
+      }
+      int idle = -1;
+      for (int L = 0; L < kLocalBlocks; ++L) {
+        if (used & (1u << L)) continue;
+        if (idle < 0) {
+          idle = L;
+          continue;
+        }
+        pair_i[cnt] = idle;
+        pair_j[cnt] = L;
+        pair_on[cnt] = 0;
+        ++cnt;
+        idle = -1;
+      }
+    }
+    __syncthreads();
+    if (warp == 0) {
+      // pivots: quad k of warp 0 sweeps local pair k
+      const int k = tid >> 2, t4 = tid & 3;
+      const bool active = pair_on[k] != 0;
+      const int I = pair_i[k], J = pair_j[k];
+      float ra[8], rb[8];
+      int tII = 0, tIJ = 0, tJJ = 0;
+      if (active) {
+        tII = tileIndex(tri, I, I);
+        tIJ = tileIndex(tri, I, J);
+        tJJ = tileIndex(tri, J, J);
+        const float4 *sII = reinterpret_cast<const float4 *>(tiles + tII * kTileF);
+        const float4 *sIJ = reinterpret_cast<const float4 *>(tiles + tIJ * kTileF);
+        const float4 *sJJ = reinterpret_cast<const float4 *>(tiles + tJJ * kTileF);
+        const int jr = 3 - t4;
+        const float4 v0 = sII[t4 ^ (tII & 3)], v1 = sIJ[t4 ^ (tIJ & 3)], v2 = sJJ[jr ^ (tJJ & 3)];
+        ra[0] = v0.x; ra[1] = v0.y; ra[2] = v0.z; ra[3] = v0.w;
+        ra[4] = v1.x; ra[5] = v1.y; ra[6] = v1.z; ra[7] = v1.w;
+#pragma unroll
+        for (int i = 0; i < 4; ++i) rb[i] = tiles[tileElement(tIJ, i, jr)];
+        rb[4] = v2.x; rb[5] = v2.y; rb[6] = v2.z; rb[7] = v2.w;
+      } else {
+#pragma unroll
+        for (int y = 0; y < 8; ++y) ra[y] = rb[y] = 0.0f;
+      }
+      pivotSweep(ra, rb, qs + (active ? k : 0) * kQS, t4, active);
+      if (active) {
+        float4 *sII = reinterpret_cast<float4 *>(tiles + tII * kTileF);
+        float4 *sIJ = reinterpret_cast<float4 *>(tiles + tIJ * kTileF);
+        float4 *sJJ = reinterpret_cast<float4 *>(tiles + tJJ * kTileF);
+        sII[t4 ^ (tII & 3)] = make_float4(ra[0], ra[1], ra[2], ra[3]);
+        sIJ[t4 ^ (tIJ & 3)] = make_float4(ra[4], ra[5], ra[6], ra[7]);
+        sJJ[t4 ^ (tJJ & 3)] = make_float4(rb[4], rb[5], rb[6], rb[7]);
+      } else {
+        float4 *q4 = reinterpret_cast<float4 *>(qs + k * kQS);
+#pragma unroll
+        for (int y = 0; y < 2; ++y) {
+          const int row = 2 * t4 + y;
+          q4[2 * row] = make_float4(row == 0, row == 1, row == 2, row == 3);
+          q4[2 * row + 1] = make_float4(row == 4, row == 5, row == 6, row == 7);
+        }
+      }
+    }
+    __syncthreads();
+    if (warp < 3) {
+      // off-pivot super-tiles of the local pairs, two lanes each (warp-uniform)
+      constexpr int kItems = ((8 + 1) / 2) * (8 + 1);
+      const int h = tid & 1;
+      int k = 0, l = 0;
+      const bool valid = tid < 2 * kItems && foldedBlock(tid >> 1, 8, k, l) && k != l;
+      if (!valid) k = l = 0;
+      superTileHalf(tiles, SharedTri{tri}, reinterpret_cast<const float4 *>(qs + k * kQS),
+                    reinterpret_cast<const float4 *>(qs + l * kQS), pair_i[k], pair_j[k],
+                    pair_i[l], pair_j[l], h, valid);
+    }
+    {
+      // Z <- Z Q of the rotating pairs (row = tid mod 64, pairs of one parity)
+      const int row = tid & 63;
+      float *zr = z + row * kFormLd;
+      for (int pp = tid >> 6; pp < 8; pp += 2) {
+        if (!pair_on[pp]) continue;
+        const int I = pair_i[pp], J = pair_j[pp];
+        const float4 *q4 = reinterpret_cast<const float4 *>(qs + pp * kQS);
+        const float4 a = *reinterpret_cast<const float4 *>(zr + 4 * I);
+        const float4 b = *reinterpret_cast<const float4 *>(zr + 4 * J);
+        const float xv[8] = {a.x, a.y, a.z, a.w, b.x, b.y, b.z, b.w};
+        float o[8] = {0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f};
+#pragma unroll
+        for (int j = 0; j < 8; ++j) {
+          const float4 lo = q4[2 * j], hi = q4[2 * j + 1];
+          o[0] = fmaf(xv[j], lo.x, o[0]); o[1] = fmaf(xv[j], lo.y, o[1]);
+          o[2] = fmaf(xv[j], lo.z, o[2]); o[3] = fmaf(xv[j], lo.w, o[3]);
+          o[4] = fmaf(xv[j], hi.x, o[4]); o[5] = fmaf(xv[j], hi.y, o[5]);
+          o[6] = fmaf(xv[j], hi.z, o[6]); o[7] = fmaf(xv[j], hi.w, o[7]);
+        }
+        *reinterpret_cast<float4 *>(zr + 4 * I) = make_float4(o[0], o[1], o[2], o[3]);
+        *reinterpret_cast<float4 *>(zr + 4 * J) = make_float4(o[4], o[5], o[6], o[7]);
+      }
+    }
+    __syncthreads();
+  }
+  // the rotated diagonal block, row-major in local order
+  float *D = args.diag + (args.diag_off[mi] + x) * 4096;
+  for (int idx = tid; idx < 4096; idx += blockDim.x) {
+    const int li = idx >> 6, lj = idx & 63, I = li >> 2, J = lj >> 2;
+    D[idx] = I <= J ? tiles[tileElement(tri[J] + I, li & 3, lj & 3)]
+                    : tiles[tileElement(tri[I] + J, lj & 3, li & 3)];
+  }
+  // Z^T split into the tcgen05 operand image (rows j, K = local index k)
+  uint8_t *img = args.images +
+                 (args.image_off[mi] + static_cast<int64_t>(args.stage) * pairs + x) * kRotationImageBytes;
+  const int j = tid & 63;
+  for (int c = tid >> 6; c < 8; c += 2) {
+    uint32_t hv[4], lv[4];
+#pragma unroll
+    for (int p = 0; p < 4; ++p)
+      splitPair(z[(8 * c + 2 * p) * kFormLd + j], z[(8 * c + 2 * p + 1) * kFormLd + j], hv[p], lv[p]);
+    const uint32_t at = swizzle128(j, c);
+    *reinterpret_cast<uint4 *>(img + at) = make_uint4(hv[0], hv[1], hv[2], hv[3]);
+    *reinterpret_cast<uint4 *>(img + kImageTermBytes + at) = make_uint4(lv[0], lv[1], lv[2], lv[3]);
+  }
+}
+
+struct PassArgs {
+  const float *src;
+  float *dst;
+  const int64_t *a_offset;
+  const int32_t *n;
+  const JacobiState *state;
+  const int2 *work;          // (matrix, first row)
+  const int64_t *image_off;
+  const uint8_t *images;
+  const float *diag;
+  const int64_t *diag_off;
+  int stage;
+  int *status;
+};
+
+// One 128-row chunk times the stage's block-diagonal Z.  Pass 1 (kSecond
+// false): rows of A, B = A Z.  Pass 2: rows of B^T (columns of B, staged
+// through shared memory for coalesced reads), A' = B^T Z, with the diagonal
+// blocks taken from the inner kernel.  Per super-pair: the 128 x 64 operand
+// split into BF16 hi + lo, 12 tcgen05.mma (M = 128, N = 64, K = 16; three
+// products) into a 64-column TMEM accumulator, then the epilogue.
+template <bool kSecond>
+__global__ void __launch_bounds__(kPassThreads, 1) tlPassKernel(PassArgs args) {
+  extern __shared__ __align__(1024) unsigned char smem_raw[];
+  const int2 w = args.work[blockIdx.x];
+  const int mi = w.x, r0 = w.y;
+  if (args.state[mi].done) return;  // uniform: before any barrier
+  const int n = args.n[mi], m = padded8(n), nb = m / 4;
+  const int supers = twoLevelSupers(nb), pairs = supers / 2;
+  if (args.stage >= supers - 1) return;
+  unsigned char *base = reinterpret_cast<unsigned char *>(
+      (reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~static_cast<uintptr_t>(1023));
+  unsigned char *op_hi = base, *op_lo = base + kOperandBytes;
+  unsigned char *zimg = base + 2 * kOperandBytes;
+  float *stage = reinterpret_cast<float *>(zimg + kRotationImageBytes);
+  uint64_t *bars = reinterpret_cast<uint64_t *>(stage + kPassRows * kStageLd);
+  uint64_t *img_full = bars, *mma_done = bars + 1;
+  uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(bars + 2);
+  volatile int *abort_flag = reinterpret_cast<volatile int *>(tmem_slot + 1);
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  if (tid == 0) {
+    mbarInit(smemAddr(img_full), 1);
+    mbarInit(smemAddr(mma_done), 1);
+    *abort_flag = 0;
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  if (warp == 4) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
+                     smemAddr(tmem_slot)),
+                 "r"(kPassTmemCols));
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;");
+  __syncthreads();
+  asm volatile("tcgen05.fence::after_thread_sync;");
+  const uint32_t tmem = *tmem_slot;
+  const float *S = args.src + args.a_offset[mi];
+  float *Dst = args.dst + args.a_offset[mi];
+  const uint8_t *images = args.images +
+                          (args.image_off[mi] + static_cast<int64_t>(args.stage) * pairs) * kRotationImageBytes;
+  const float *diag = kSecond ? args.diag + args.diag_off[mi] * 4096 : nullptr;
+  const int row = r0 + tid;  // warps 0-3: operand row / output row (TMEM lane tid)
+  bool ok = true;
+  for (int x = 0; x < pairs && ok; ++x) {
+    int Ps, Qs;
+    rrPair(x, args.stage, supers, Ps, Qs);
+    if (tid == 128) {
+      mbarArriveExpectTx(smemAddr(img_full), static_cast<uint32_t>(kRotationImageBytes));
+      bulkLoad(smemAddr(zimg), images + static_cast<int64_t>(x) * kRotationImageBytes,
+               static_cast<uint32_t>(kRotationImageBytes), smemAddr(img_full));
+    }
+    if (kSecond) {
+      // columns r0 .. r0 + 127 of B, rows of the super-pair: a warp reads 32
+      // consecutive rows of one column
+      for (int c = warp; c < kPassRows && warp < 4; c += 4) {
+        const int col = r0 + c;
+#pragma unroll
+        for (int h = 0; h < 2; ++h) {
+          const int g = localToGlobal(32 * h + lane, Ps, Qs, n);
+          stage[c * kStageLd + 32 * h + lane] =
+              col < n && g >= 0 ? S[g + static_cast<int64_t>(col) * n] : 0.0f;
+        }
+      }
+      __syncthreads();
+    }
+    if (warp < 4) {
+#pragma unroll
+      for (int c = 0; c < 8; ++c) {
+        uint32_t hv[4], lv[4];
+#pragma unroll
+        for (int p = 0; p < 4; ++p) {
+          float e[2];
+#pragma unroll
+          for (int q = 0; q < 2; ++q) {
+            const int k = 8 * c + 2 * p + q;
+            if (kSecond) {
+              e[q] = stage[tid * kStageLd + k];
+            } else {
+              const int g = localToGlobal(k, Ps, Qs, n);
+              e[q] = row < n && g >= 0 ? S[row + static_cast<int64_t>(g) * n] : 0.0f;
+            }
+          }
+          splitPair(e[0], e[1], hv[p], lv[p]);
+        }
+        const uint32_t at = swizzle128(tid, c);
+        *reinterpret_cast<uint4 *>(op_hi + at) = make_uint4(hv[0], hv[1], hv[2], hv[3]);
+        *reinterpret_cast<uint4 *>(op_lo + at) = make_uint4(lv[0], lv[1], lv[2], lv[3]);
+      }
+      asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;");
+    __syncthreads();
+    if (tid == 128) {
+      if (applyWait(smemAddr(img_full), x & 1, args.status, abort_flag)) {
+        asm volatile("tcgen05.fence::after_thread_sync;");
+        constexpr uint32_t idesc = instrDescBf16(128, 64);
+        const uint64_t ah = smemDesc(smemAddr(op_hi)), al = smemDesc(smemAddr(op_lo));
+        const uint64_t zh = smemDesc(smemAddr(zimg)), zl = smemDesc(smemAddr(zimg) + kImageTermBytes);
+#pragma unroll
+        for (int kk = 0; kk < 4; ++kk) {
+          mmaBf16(tmem, ah + 2 * kk, zh + 2 * kk, idesc, kk > 0);
+          mmaBf16(tmem, al + 2 * kk, zh + 2 * kk, idesc, 1);
+          mmaBf16(tmem, ah + 2 * kk, zl + 2 * kk, idesc, 1);
+        }
+        mmaCommit(smemAddr(mma_done));
+      }
+    }
+    if (warp < 4) {
+      ok = applyWait(smemAddr(mma_done), x & 1, args.status, abort_flag);
+      if (ok) {
+        asm volatile("tcgen05.fence::after_thread_sync;");
+        float d[64];
+        tmemLoad32(tmem + ((32u * warp) << 16), d);
+        tmemLoad32(tmem + ((32u * warp) << 16) + 32, d + 32);
+        if (row < n) {
+          // pass 2: a row inside the super-pair keeps the inner kernel's block
+          const int sb = row >> 5;
+          const int local = sb == Ps ? row - 32 * Ps : (sb == Qs ? 32 + row - 32 * Qs : -1);
+#pragma unroll 8
+          for (int j = 0; j < 64; ++j) {
+            const int g = localToGlobal(j, Ps, Qs, n);
+            if (g < 0) continue;
+            float v = d[j];
+            if (kSecond && local >= 0) v = diag[(static_cast<int64_t>(x) * 64 + local) * 64 + j];
+            Dst[row + static_cast<int64_t>(g) * n] = v;
+          }
+        }
+      }
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;");
+    __syncthreads();
+    ok = ok && !*abort_flag;
+  }
+  asm volatile("tcgen05.fence::after_thread_sync;");
+  if (warp == 4) {
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem),
+                 "r"(kPassTmemCols));
+  }
+}
+
 int setAttributes() {
   static std::atomic<uint64_t> done_mask{0};
   int device = 0;
@@ -465,7 +907,11 @@ int setAttributes() {
   if (cudaFuncSetAttribute(tcvFormKernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                            static_cast<int>(kFormSmem)) != cudaSuccess ||
       cudaFuncSetAttribute(tcvApplyKernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                           static_cast<int>(kApplySmem)) != cudaSuccess) {
+                           static_cast<int>(kApplySmem)) != cudaSuccess ||
+      cudaFuncSetAttribute(tlPassKernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                           static_cast<int>(kPassSmem)) != cudaSuccess ||
+      cudaFuncSetAttribute(tlPassKernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                           static_cast<int>(kPassSmem)) != cudaSuccess) {
     return MSQ_ERR_CUDA;
   }
   done_mask.fetch_or(bit);
@@ -529,18 +975,84 @@ void tcVectorsTables(const int *host_n, int count, const std::vector<int> &ids,
 
 int tcVectorsEnqueue(msq_ctx *ctx, cudaStream_t stream, const TcVectorsDevice &d, float *vectors,
                      const int64_t *a_offset, const int32_t *n, const void *state,
-                     const float *log, const int64_t *log_offset, uint8_t *images, int parity) {
-  if (d.form_items == 0) return MSQ_OK;
+                     const float *log, const int64_t *log_offset, uint8_t *images, int parity,
+                     bool form) {
+  if (d.apply_items == 0) return MSQ_OK;
   if (setAttributes() != MSQ_OK) return cudaCheck(ctx, cudaGetLastError(), "tensor-core vectors attributes");
   const auto *st = static_cast<const JacobiState *>(state);
-  FormArgs fa{log, log_offset, n, st, d.form_work, d.prog, d.prog_off, d.image_off, images, parity};
-  launchBegin(ctx, stream);
-  tcvFormKernel<<<d.form_items, kFormThreads, kFormSmem, stream>>>(fa);
-  MSQ_TRY(launchedOn(ctx, stream, "jacobi stage rotations"));
+  if (form) {
+    FormArgs fa{log, log_offset, n, st, d.form_work, d.prog, d.prog_off, d.image_off, images, parity};
+    launchBegin(ctx, stream);
+    tcvFormKernel<<<d.form_items, kFormThreads, kFormSmem, stream>>>(fa);
+    MSQ_TRY(launchedOn(ctx, stream, "jacobi stage rotations"));
+  }
   ApplyArgs aa{vectors, a_offset, n, st, d.apply_work, d.image_off, images, parity, ctx->d_status};
   launchBegin(ctx, stream);
   tcvApplyKernel<<<d.apply_items, kApplyThreads, kApplySmem, stream>>>(aa);
   return launchedOn(ctx, stream, "jacobi vectors tcgen05");
+}
+
+void twoLevelTables(const int *host_n, int count, const std::vector<int> &ids, TwoLevelTables &out) {
+  out = TwoLevelTables{};
+  out.diag_off.assign(count, 0);
+  int max_stages = 0;
+  for (const int i : ids) {
+    const int nb = padded8(host_n[i]) / 4;
+    max_stages = std::max(max_stages, twoLevelSupers(nb) - 1);
+  }
+  out.stage_first.assign(max_stages, 0);
+  out.stage_count.assign(max_stages, 0);
+  for (int s = 0; s < max_stages; ++s) {
+    out.stage_first[s] = static_cast<int>(out.inner.size() / 2);
+    for (const int i : ids) {
+      const int supers = twoLevelSupers(padded8(host_n[i]) / 4);
+      if (s >= supers - 1) continue;
+      for (int x = 0; x < supers / 2; ++x) {
+        out.inner.push_back(i);
+        out.inner.push_back(x);
+      }
+    }
+    out.stage_count[s] = static_cast<int>(out.inner.size() / 2) - out.stage_first[s];
+  }
+  for (const int i : ids) {
+    out.ids.push_back(i);
+    out.diag_off[i] = out.diag_blocks;
+    out.diag_blocks += twoLevelSupers(padded8(host_n[i]) / 4) / 2;
+  }
+}
+
+int twoLevelEnqueue(msq_ctx *ctx, cudaStream_t stream, const TwoLevelDevice &t,
+                    const TcVectorsDevice &v, float *matrices, float *b_scratch, float *diag,
+                    uint8_t *images, const int64_t *a_offset, const int32_t *n,
+                    const int64_t *eig_offset, float *eigenvalues, void *state, double tol,
+                    int max_sweeps, bool first, bool sweep, int parity) {
+  if (t.count == 0) return MSQ_OK;
+  if (setAttributes() != MSQ_OK) return cudaCheck(ctx, cudaGetLastError(), "two-level attributes");
+  auto *st = static_cast<JacobiState *>(state);
+  CheckArgs ca{matrices, a_offset, n, eig_offset, eigenvalues, st, t.ids, tol, max_sweeps,
+               first ? 1 : 0, parity};
+  launchBegin(ctx, stream);
+  tlCheckKernel<<<t.count, 256, 0, stream>>>(ca);
+  MSQ_TRY(launchedOn(ctx, stream, "jacobi two-level check"));
+  if (!sweep) return MSQ_OK;
+  for (size_t s = 0; s < t.stage_first.size(); ++s) {
+    InnerArgs ia{matrices, a_offset, n, st, t.inner + t.stage_first[s], v.prog, v.prog_off,
+                 v.image_off, images, diag, t.diag_off, static_cast<int>(s)};
+    launchBegin(ctx, stream);
+    tlInnerKernel<<<t.stage_count[s], kInnerThreads, 0, stream>>>(ia);
+    MSQ_TRY(launchedOn(ctx, stream, "jacobi two-level blocks"));
+    PassArgs pa{matrices, b_scratch, a_offset, n, st, v.apply_work, v.image_off, images,
+                diag, t.diag_off, static_cast<int>(s), ctx->d_status};
+    launchBegin(ctx, stream);
+    tlPassKernel<false><<<v.apply_items, kPassThreads, kPassSmem, stream>>>(pa);
+    MSQ_TRY(launchedOn(ctx, stream, "jacobi two-level A Z tcgen05"));
+    pa.src = b_scratch;
+    pa.dst = matrices;
+    launchBegin(ctx, stream);
+    tlPassKernel<true><<<v.apply_items, kPassThreads, kPassSmem, stream>>>(pa);
+    MSQ_TRY(launchedOn(ctx, stream, "jacobi two-level Z^T A Z tcgen05"));
+  }
+  return MSQ_OK;
 }
 
 }  // namespace msq
@@ -560,7 +1072,7 @@ extern "C" int msq_jacobi_schedule(int blocks, int32_t *pairs, size_t capacity, 
 }
 
 extern "C" int msq_set_jacobi_vectors(msq_ctx *ctx, int mode) {
-  if (ctx == nullptr || mode < -1 || mode > 2) return MSQ_ERR_INVALID_ARGUMENT;
+  if (ctx == nullptr || mode < -1 || mode > 3) return MSQ_ERR_INVALID_ARGUMENT;
   ctx->jacobi_vectors = mode;
   return MSQ_OK;
 }

@@ -1,11 +1,13 @@
 """Batched Jacobi for 256 < n <= 512 in the two-level pairing.
 
 VECTORS_BLOCKED (FP32 replay) must agree bit for bit with the oracle's
-blocked Jacobi in the same order.  VECTORS_TENSOR leaves the rotations of A
-unchanged (eigenvalues and rotated matrix still bit-exact) and accumulates V
-with split-BF16 tcgen05 GEMMs: V is compared with the oracle's FP32 V within
-the split's error (relative 2^-16 per stage product), and checked for
-orthonormality and A V = V diag(w)."""
+blocked Jacobi in the same order.  VECTORS_TENSOR keeps those rotations of A
+(bit-exact) and accumulates V with split-BF16 tcgen05 GEMMs.
+VECTORS_TENSOR_A rotates only the 64x64 diagonal blocks on the CUDA cores
+and brings the rest of A up to date once per stage on the tensor cores too.
+The tensor-core results are checked within the split-BF16 error (about
+2^-16 relative per product): against FP64 (orthonormal V, A V = V diag(w),
+eigenvalues) and against the oracle."""
 import numpy as np
 import pytest
 
@@ -51,27 +53,48 @@ def test_blocked_mode_bit_exact(ctx, msq):
         assert np.array_equal(af[i], a_o), ORDERS[i]
 
 
-def test_tensor_mode_against_oracle(ctx, msq):
+def test_tensor_vectors_against_oracle(ctx, msq):
+    """VECTORS_TENSOR: the rotations of A are the FP32 two-level ones
+    (eigenvalues and rotated matrix bit-exact with the oracle); V is
+    accumulated with split-BF16 tcgen05 GEMMs, within the split's error of
+    the oracle's FP32 V (about 2^-16 relative per stage product; the entries
+    of V are O(n^-1/2))."""
     mats = _mats()
     vs, ws, sweeps, _, af = _run(ctx, msq, mats, msq.VECTORS_TENSOR, 0.0, 3)
     for i, a in enumerate(mats):
         n = ORDERS[i]
         w_o, v_o, _, _, a_o = O.jacobi_blocked(a, 0.0, 3, with_matrix=True, two_level=True)
         assert int(sweeps[i]) == 3
-        # the rotations of A do not depend on V: still bit for bit
         assert np.array_equal(ws[i], w_o), n
         assert np.array_equal(af[i], a_o), n
-        # V: about 2^-16 relative per stage product, 3 sweeps of up to 15
-        # stages; the entries of V are O(n^-1/2)
         err = np.abs(vs[i].astype(np.float64) - v_o).max()
-        assert err <= 2e-4 / np.sqrt(n) * 10, (n, err)
+        assert err <= 2e-3 / np.sqrt(n), (n, err)
         v = vs[i].astype(np.float64)
         assert np.abs(v.T @ v - np.eye(n)).max() <= 1e-4, n
 
 
-def test_tensor_mode_converged_eigenpairs(ctx, msq):
+def test_tensor_blocks_fixed_sweeps(ctx, msq):
+    """VECTORS_TENSOR_A, three sweeps: the diagonal blocks rotate on the CUDA
+    cores, the rest of A and V on the tensor cores.  The returned matrix is
+    V^T A V (to the split-BF16 accuracy), V is orthonormal, and the off-norm
+    falls like the oracle's two-level FP32 sweeps."""
     mats = _mats()
-    vs, ws, sweeps, off, _ = _run(ctx, msq, mats, msq.VECTORS_TENSOR, 1e-4, 15)
+    vs, ws, sweeps, off, af = _run(ctx, msq, mats, msq.VECTORS_TENSOR_A, 0.0, 3)
+    for i, a in enumerate(mats):
+        n = ORDERS[i]
+        _, _, _, off_o, _ = O.jacobi_blocked(a, 0.0, 3, with_matrix=True, two_level=True)
+        assert int(sweeps[i]) == 3
+        v = vs[i].astype(np.float64)
+        assert np.abs(v.T @ v - np.eye(n)).max() <= 1e-4, (n, np.abs(v.T @ v - np.eye(n)).max())
+        dev = np.linalg.norm(af[i] - v.T @ a @ v) / np.linalg.norm(a)
+        assert dev <= 1e-4, (n, dev)
+        assert off[i] <= 2 * off_o + 1e-4, (n, off[i], off_o)
+
+
+@pytest.mark.parametrize("mode", ["VECTORS_TENSOR", "VECTORS_TENSOR_A"])
+def test_tensor_modes_converged_eigenpairs(ctx, msq, mode):
+    mats = _mats()
+    vs, ws, sweeps, off, _ = _run(ctx, msq, mats, getattr(msq, mode), 1e-4, 15)
     for i, a in enumerate(mats):
         n = ORDERS[i]
         assert off[i] <= 1e-4 and sweeps[i] < 15
