@@ -477,10 +477,8 @@ constexpr int kLocalBlocks = 16;
 constexpr int kLocalTiles = kLocalBlocks * (kLocalBlocks + 1) / 2;
 constexpr int kPassRows = 128;
 constexpr int kPassThreads = 160;        // warps 0-3 rows, warp 4 TMEM + MMA + copies
-constexpr uint32_t kPassTmemCols = 64;
+constexpr uint32_t kPassTmemCols = 128;  // two 64-column accumulators
 constexpr int kStageLd = 65;
-constexpr size_t kPassSmem = 2 * kOperandBytes + kRotationImageBytes +
-                             static_cast<size_t>(kPassRows) * kStageLd * sizeof(float) + 1024 + 256;
 
 struct CheckArgs {
   float *a;
@@ -577,6 +575,7 @@ __global__ void __launch_bounds__(kInnerThreads) tlInnerKernel(InnerArgs args) {
   __shared__ __align__(16) float qs[8 * kQS];
   __shared__ int tri[kLocalBlocks + 1];
   __shared__ int pair_i[8], pair_j[8], pair_on[8];
+  __shared__ int entries[2 * kSuperBlock - 1][8];  // the stage's rotating pairs, round by round
   const int2 w = args.work[blockIdx.x];
   const int mi = w.x, x = w.y;
   if (args.state[mi].done) return;
@@ -592,26 +591,28 @@ __global__ void __launch_bounds__(kInnerThreads) tlInnerKernel(InnerArgs args) {
       *reinterpret_cast<float4 *>(z + i * kFormLd + c) =
           make_float4(i == c, i == c + 1, i == c + 2, i == c + 3);
   __syncthreads();
-  for (int J = 0; J < kLocalBlocks; ++J) {
-    for (int idx = tid; idx < (J + 1) * kTileF; idx += blockDim.x) {
-      const int I = idx / kTileF, e = idx % kTileF;
-      const int gi = localToGlobal(4 * I + e / 4, Ps, Qs, n);
-      const int gj = localToGlobal(4 * J + e % 4, Ps, Qs, n);
-      tiles[tileElement(tri[J] + I, e / 4, e % 4)] =
-          gi >= 0 && gj >= 0 ? A[gi + static_cast<int64_t>(gj) * n] : 0.0f;
-    }
+  // upper triangle of the 64x64 block: column lj, rows li <= (lj | 3);
+  // consecutive threads read consecutive rows of a column
+  for (int q = tid; q < 64 * 64; q += blockDim.x) {
+    const int lj = q >> 6, li = q & 63, I = li >> 2, J = lj >> 2;
+    if (I > J) continue;
+    const int gi = localToGlobal(li, Ps, Qs, n), gj = localToGlobal(lj, Ps, Qs, n);
+    tiles[tileElement(tri[J] + I, li & 3, lj & 3)] =
+        gi >= 0 && gj >= 0 ? A[gi + static_cast<int64_t>(gj) * n] : 0.0f;
   }
   const int32_t *prog = args.prog + args.prog_off[mi];
   const int r0 = twoLevelStageFirst(args.stage), rounds = twoLevelStageRounds(args.stage);
+  for (int q = tid; q < rounds * 8; q += blockDim.x)
+    entries[q / 8][q % 8] = prog[((r0 + q / 8) * pairs + x) * 8 + q % 8];
+  __syncthreads();
   for (int t = 0; t < rounds; ++t) {
-    const int r = r0 + t;
     if (tid == 0) {
       // the round's rotating pairs, then the other local blocks paired in
       // order with the identity
       unsigned used = 0;
       int cnt = 0;
       for (int e = 0; e < 8; ++e) {
-        const int code = prog[(r * pairs + x) * 8 + e];
+        const int code = entries[t][e];
         if (code < 0) break;
         const int la = (code >> 8) & 255, lb = code >> 16;
         pair_i[cnt] = la;
@@ -753,12 +754,21 @@ struct PassArgs {
   int *status;
 };
 
-// One 128-row chunk times the stage's block-diagonal Z.  Pass 1 (kSecond
-// false): rows of A, B = A Z.  Pass 2: rows of B^T (columns of B, staged
-// through shared memory for coalesced reads), A' = B^T Z, with the diagonal
-// blocks taken from the inner kernel.  Per super-pair: the 128 x 64 operand
-// split into BF16 hi + lo, 12 tcgen05.mma (M = 128, N = 64, K = 16; three
-// products) into a 64-column TMEM accumulator, then the epilogue.
+// One 128-row chunk times the stage's block-diagonal Z, super-pair by
+// super-pair, software-pipelined: the row warps split the operand of
+// super-pair x into BF16 hi + lo (buffer x mod 2) while the MMA of x - 1
+// runs, then drain the accumulator of x - 1 (TMEM, two 64-column buffers);
+// a thread of warp 4 issues 12 tcgen05.mma per super-pair (M = 128, N = 64,
+// three split products) and another bulk-copies the rotation images.
+// Pass 1 (kSecond false): operand rows are rows of A, B = A Z is stored
+// row-major through a shared-memory transpose (coalesced), so pass 2 reads
+// its operand rows, the columns of B, with coalesced loads: A' = B^T Z,
+// with the diagonal blocks taken from the inner kernel.
+constexpr int kPassBuffers = 2;
+constexpr size_t kPassSmemFirst = kPassBuffers * (2 * kOperandBytes + kRotationImageBytes) +
+                                  static_cast<size_t>(kPassRows) * kStageLd * sizeof(float) + 1024 + 256;
+constexpr size_t kPassSmemSecond = kPassBuffers * (2 * kOperandBytes + kRotationImageBytes) + 1024 + 256;
+
 template <bool kSecond>
 __global__ void __launch_bounds__(kPassThreads, 1) tlPassKernel(PassArgs args) {
   extern __shared__ __align__(1024) unsigned char smem_raw[];
@@ -770,17 +780,23 @@ __global__ void __launch_bounds__(kPassThreads, 1) tlPassKernel(PassArgs args) {
   if (args.stage >= supers - 1) return;
   unsigned char *base = reinterpret_cast<unsigned char *>(
       (reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~static_cast<uintptr_t>(1023));
-  unsigned char *op_hi = base, *op_lo = base + kOperandBytes;
-  unsigned char *zimg = base + 2 * kOperandBytes;
-  float *stage = reinterpret_cast<float *>(zimg + kRotationImageBytes);
-  uint64_t *bars = reinterpret_cast<uint64_t *>(stage + kPassRows * kStageLd);
-  uint64_t *img_full = bars, *mma_done = bars + 1;
-  uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(bars + 2);
+  unsigned char *ops = base;                                            // [2][hi, lo]
+  unsigned char *ring = base + kPassBuffers * 2 * kOperandBytes;        // [2] images
+  unsigned char *after = ring + kPassBuffers * kRotationImageBytes;
+  float *stage = reinterpret_cast<float *>(after);                      // pass 1 only
+  uint64_t *bars = reinterpret_cast<uint64_t *>(
+      after + (kSecond ? 0 : static_cast<size_t>(kPassRows) * kStageLd * sizeof(float)));
+  uint64_t *img_full = bars, *op_full = bars + 2, *d_full = bars + 4, *d_empty = bars + 6;
+  uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(bars + 8);
   volatile int *abort_flag = reinterpret_cast<volatile int *>(tmem_slot + 1);
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   if (tid == 0) {
-    mbarInit(smemAddr(img_full), 1);
-    mbarInit(smemAddr(mma_done), 1);
+    for (int b = 0; b < kPassBuffers; ++b) {
+      mbarInit(smemAddr(&img_full[b]), 1);
+      mbarInit(smemAddr(&op_full[b]), kPassRows);
+      mbarInit(smemAddr(&d_full[b]), 1);
+      mbarInit(smemAddr(&d_empty[b]), kPassRows);
+    }
     *abort_flag = 0;
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
@@ -798,99 +814,124 @@ __global__ void __launch_bounds__(kPassThreads, 1) tlPassKernel(PassArgs args) {
   float *Dst = args.dst + args.a_offset[mi];
   const uint8_t *images = args.images +
                           (args.image_off[mi] + static_cast<int64_t>(args.stage) * pairs) * kRotationImageBytes;
-  const float *diag = kSecond ? args.diag + args.diag_off[mi] * 4096 : nullptr;
-  const int row = r0 + tid;  // warps 0-3: operand row / output row (TMEM lane tid)
-  bool ok = true;
-  for (int x = 0; x < pairs && ok; ++x) {
-    int Ps, Qs;
-    rrPair(x, args.stage, supers, Ps, Qs);
-    if (tid == 128) {
-      mbarArriveExpectTx(smemAddr(img_full), static_cast<uint32_t>(kRotationImageBytes));
-      bulkLoad(smemAddr(zimg), images + static_cast<int64_t>(x) * kRotationImageBytes,
-               static_cast<uint32_t>(kRotationImageBytes), smemAddr(img_full));
-    }
-    if (kSecond) {
-      // columns r0 .. r0 + 127 of B, rows of the super-pair: a warp reads 32
-      // consecutive rows of one column
-      for (int c = warp; c < kPassRows && warp < 4; c += 4) {
-        const int col = r0 + c;
-#pragma unroll
-        for (int h = 0; h < 2; ++h) {
-          const int g = localToGlobal(32 * h + lane, Ps, Qs, n);
-          stage[c * kStageLd + 32 * h + lane] =
-              col < n && g >= 0 ? S[g + static_cast<int64_t>(col) * n] : 0.0f;
-        }
+
+  if (warp == 4) {
+    if (lane == 0) {
+      // rotation images, two ahead
+      for (int x = 0; x < pairs && !*abort_flag; ++x) {
+        const int b = x & 1, u = x >> 1;
+        if (u >= 1 && !applyWait(smemAddr(&d_full[b]), (u - 1) & 1, args.status, abort_flag)) break;
+        mbarArriveExpectTx(smemAddr(&img_full[b]), static_cast<uint32_t>(kRotationImageBytes));
+        bulkLoad(smemAddr(ring + b * kRotationImageBytes),
+                 images + static_cast<int64_t>(x) * kRotationImageBytes,
+                 static_cast<uint32_t>(kRotationImageBytes), smemAddr(&img_full[b]));
       }
-      __syncthreads();
-    }
-    if (warp < 4) {
-#pragma unroll
-      for (int c = 0; c < 8; ++c) {
-        uint32_t hv[4], lv[4];
-#pragma unroll
-        for (int p = 0; p < 4; ++p) {
-          float e[2];
-#pragma unroll
-          for (int q = 0; q < 2; ++q) {
-            const int k = 8 * c + 2 * p + q;
-            if (kSecond) {
-              e[q] = stage[tid * kStageLd + k];
-            } else {
-              const int g = localToGlobal(k, Ps, Qs, n);
-              e[q] = row < n && g >= 0 ? S[row + static_cast<int64_t>(g) * n] : 0.0f;
-            }
-          }
-          splitPair(e[0], e[1], hv[p], lv[p]);
-        }
-        const uint32_t at = swizzle128(tid, c);
-        *reinterpret_cast<uint4 *>(op_hi + at) = make_uint4(hv[0], hv[1], hv[2], hv[3]);
-        *reinterpret_cast<uint4 *>(op_lo + at) = make_uint4(lv[0], lv[1], lv[2], lv[3]);
-      }
-      asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-    }
-    asm volatile("tcgen05.fence::before_thread_sync;");
-    __syncthreads();
-    if (tid == 128) {
-      if (applyWait(smemAddr(img_full), x & 1, args.status, abort_flag)) {
+    } else if (lane == 1) {
+      constexpr uint32_t idesc = instrDescBf16(128, 64);
+      for (int x = 0; x < pairs && !*abort_flag; ++x) {
+        const int b = x & 1, u = x >> 1;
+        if (!applyWait(smemAddr(&img_full[b]), u & 1, args.status, abort_flag) ||
+            !applyWait(smemAddr(&op_full[b]), u & 1, args.status, abort_flag) ||
+            (u >= 1 && !applyWait(smemAddr(&d_empty[b]), (u - 1) & 1, args.status, abort_flag)))
+          break;
         asm volatile("tcgen05.fence::after_thread_sync;");
-        constexpr uint32_t idesc = instrDescBf16(128, 64);
-        const uint64_t ah = smemDesc(smemAddr(op_hi)), al = smemDesc(smemAddr(op_lo));
-        const uint64_t zh = smemDesc(smemAddr(zimg)), zl = smemDesc(smemAddr(zimg) + kImageTermBytes);
+        const uint32_t hi = smemAddr(ops + b * 2 * kOperandBytes);
+        const uint64_t ah = smemDesc(hi), al = smemDesc(hi + kOperandBytes);
+        const uint32_t img = smemAddr(ring + b * kRotationImageBytes);
+        const uint64_t zh = smemDesc(img), zl = smemDesc(img + kImageTermBytes);
+        const uint32_t d = tmem + 64 * b;
 #pragma unroll
         for (int kk = 0; kk < 4; ++kk) {
-          mmaBf16(tmem, ah + 2 * kk, zh + 2 * kk, idesc, kk > 0);
-          mmaBf16(tmem, al + 2 * kk, zh + 2 * kk, idesc, 1);
-          mmaBf16(tmem, ah + 2 * kk, zl + 2 * kk, idesc, 1);
+          mmaBf16(d, ah + 2 * kk, zh + 2 * kk, idesc, kk > 0);
+          mmaBf16(d, al + 2 * kk, zh + 2 * kk, idesc, 1);
+          mmaBf16(d, ah + 2 * kk, zl + 2 * kk, idesc, 1);
         }
-        mmaCommit(smemAddr(mma_done));
+        mmaCommit(smemAddr(&d_full[b]));
       }
     }
-    if (warp < 4) {
-      ok = applyWait(smemAddr(mma_done), x & 1, args.status, abort_flag);
-      if (ok) {
+  } else {
+    const int row = r0 + tid;  // operand row: a row of A (pass 1) or a column of B (pass 2)
+    const float *diag = kSecond ? args.diag + args.diag_off[mi] * 4096 : nullptr;
+    bool ok = true;
+    for (int x = 0; x <= pairs && ok; ++x) {
+      if (x < pairs) {
+        // operand of super-pair x (its buffer was freed by the MMA of x - 2,
+        // whose completion the drain of x - 2 waited for)
+        int Ps, Qs;
+        rrPair(x, args.stage, supers, Ps, Qs);
+        const int b = x & 1;
+        unsigned char *op_hi = ops + b * 2 * kOperandBytes, *op_lo = op_hi + kOperandBytes;
+#pragma unroll
+        for (int c = 0; c < 8; ++c) {
+          uint32_t hv[4], lv[4];
+#pragma unroll
+          for (int p = 0; p < 4; ++p) {
+            float e[2];
+#pragma unroll
+            for (int q = 0; q < 2; ++q) {
+              const int g = localToGlobal(8 * c + 2 * p + q, Ps, Qs, n);
+              // pass 1: A[row, g] (A symmetric: read as A[g, row]... column-major
+              // A[row + g n]); pass 2: B[g, row], B row-major: B[row + g n]
+              e[q] = row < n && g >= 0 ? S[row + static_cast<int64_t>(g) * n] : 0.0f;
+            }
+            splitPair(e[0], e[1], hv[p], lv[p]);
+          }
+          const uint32_t at = swizzle128(tid, c);
+          *reinterpret_cast<uint4 *>(op_hi + at) = make_uint4(hv[0], hv[1], hv[2], hv[3]);
+          *reinterpret_cast<uint4 *>(op_lo + at) = make_uint4(lv[0], lv[1], lv[2], lv[3]);
+        }
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+        mbarArrive(smemAddr(&op_full[b]));
+      }
+      if (x >= 1) {
+        // drain the accumulator of super-pair x - 1
+        const int y = x - 1, b = y & 1, u = y >> 1;
+        int Ps, Qs;
+        rrPair(y, args.stage, supers, Ps, Qs);
+        if (!applyWait(smemAddr(&d_full[b]), u & 1, args.status, abort_flag)) {
+          ok = false;
+          break;
+        }
         asm volatile("tcgen05.fence::after_thread_sync;");
         float d[64];
-        tmemLoad32(tmem + ((32u * warp) << 16), d);
-        tmemLoad32(tmem + ((32u * warp) << 16) + 32, d + 32);
-        if (row < n) {
-          // pass 2: a row inside the super-pair keeps the inner kernel's block
-          const int sb = row >> 5;
-          const int local = sb == Ps ? row - 32 * Ps : (sb == Qs ? 32 + row - 32 * Qs : -1);
+        tmemLoad32(tmem + ((32u * warp) << 16) + 64 * b, d);
+        tmemLoad32(tmem + ((32u * warp) << 16) + 64 * b + 32, d + 32);
+        asm volatile("tcgen05.fence::before_thread_sync;");
+        mbarArrive(smemAddr(&d_empty[b]));
+        if (kSecond) {
+          if (row < n) {
+            const int sb = row >> 5;
+            const int local = sb == Ps ? row - 32 * Ps : (sb == Qs ? 32 + row - 32 * Qs : -1);
 #pragma unroll 8
-          for (int j = 0; j < 64; ++j) {
-            const int g = localToGlobal(j, Ps, Qs, n);
-            if (g < 0) continue;
-            float v = d[j];
-            if (kSecond && local >= 0) v = diag[(static_cast<int64_t>(x) * 64 + local) * 64 + j];
-            Dst[row + static_cast<int64_t>(g) * n] = v;
+            for (int j = 0; j < 64; ++j) {
+              const int g = localToGlobal(j, Ps, Qs, n);
+              if (g < 0) continue;
+              const float v = local >= 0 ? diag[(static_cast<int64_t>(y) * 64 + local) * 64 + j] : d[j];
+              Dst[row + static_cast<int64_t>(g) * n] = v;
+            }
           }
+        } else {
+          // B row-major through a transpose in shared memory: a warp writes
+          // 32 consecutive columns of one row of B
+#pragma unroll
+          for (int j = 0; j < 64; ++j) stage[tid * kStageLd + j] = d[j];
+          asm volatile("bar.sync 1, 128;" ::: "memory");
+          for (int rr = warp; rr < kPassRows; rr += 4) {
+            const int R = r0 + rr;
+            if (R >= n) continue;
+#pragma unroll
+            for (int h = 0; h < 2; ++h) {
+              const int g = localToGlobal(32 * h + lane, Ps, Qs, n);
+              if (g >= 0) Dst[g + static_cast<int64_t>(R) * n] = stage[rr * kStageLd + 32 * h + lane];
+            }
+          }
+          asm volatile("bar.sync 1, 128;" ::: "memory");
         }
       }
     }
-    asm volatile("tcgen05.fence::before_thread_sync;");
-    __syncthreads();
-    ok = ok && !*abort_flag;
   }
+  asm volatile("tcgen05.fence::before_thread_sync;");
+  __syncthreads();
   asm volatile("tcgen05.fence::after_thread_sync;");
   if (warp == 4) {
     asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem),
@@ -909,9 +950,9 @@ int setAttributes() {
       cudaFuncSetAttribute(tcvApplyKernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                            static_cast<int>(kApplySmem)) != cudaSuccess ||
       cudaFuncSetAttribute(tlPassKernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                           static_cast<int>(kPassSmem)) != cudaSuccess ||
+                           static_cast<int>(kPassSmemFirst)) != cudaSuccess ||
       cudaFuncSetAttribute(tlPassKernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                           static_cast<int>(kPassSmem)) != cudaSuccess) {
+                           static_cast<int>(kPassSmemSecond)) != cudaSuccess) {
     return MSQ_ERR_CUDA;
   }
   done_mask.fetch_or(bit);
@@ -1044,12 +1085,12 @@ int twoLevelEnqueue(msq_ctx *ctx, cudaStream_t stream, const TwoLevelDevice &t,
     PassArgs pa{matrices, b_scratch, a_offset, n, st, v.apply_work, v.image_off, images,
                 diag, t.diag_off, static_cast<int>(s), ctx->d_status};
     launchBegin(ctx, stream);
-    tlPassKernel<false><<<v.apply_items, kPassThreads, kPassSmem, stream>>>(pa);
+    tlPassKernel<false><<<v.apply_items, kPassThreads, kPassSmemFirst, stream>>>(pa);
     MSQ_TRY(launchedOn(ctx, stream, "jacobi two-level A Z tcgen05"));
     pa.src = b_scratch;
     pa.dst = matrices;
     launchBegin(ctx, stream);
-    tlPassKernel<true><<<v.apply_items, kPassThreads, kPassSmem, stream>>>(pa);
+    tlPassKernel<true><<<v.apply_items, kPassThreads, kPassSmemSecond, stream>>>(pa);
     MSQ_TRY(launchedOn(ctx, stream, "jacobi two-level Z^T A Z tcgen05"));
   }
   return MSQ_OK;
