@@ -41,6 +41,7 @@
 #include <map>
 #include <mutex>
 #include <string>
+#include <type_traits>
 #include <vector>
 
 namespace msq {
@@ -49,6 +50,8 @@ namespace {
 constexpr size_t kSmemLimit = 227 * 1024;
 // the sweep kernel also holds a small static shared block (its mbarrier)
 constexpr size_t kSweepSmemLimit = kSmemLimit - 256;
+// per CTA when two share an SM (228 KB per SM, 1 KB reserved per CTA)
+constexpr size_t kSweepSmemHalf = 110 * 1024;
 constexpr int kMaxOrder = 16384;    // grid kernels; the batched ones see n <= 1024
 constexpr int kGridMinOrder = 1024;
 constexpr int kGridFewLarge = 8;
@@ -74,7 +77,15 @@ struct JacobiArgs {
   int *status;               // device status word (bounded waits)
   const int2 *sched;         // two-level pair tables (null: round-robin for all)
   const int32_t *sched_off;  // per matrix: its table in sched (int2 units), -1 = round-robin
+  int smem_tiles;            // global-tile variant: tiles kept in shared memory
 };
+
+__device__ __forceinline__ FlatTiles tileMem(std::true_type, float *s, float *, int) {
+  return FlatTiles{s};
+}
+__device__ __forceinline__ SplitTiles tileMem(std::false_type, float *s, float *g, int split) {
+  return SplitTiles{s, g, split};
+}
 
 // Shared memory of the sweep kernel: reduction scratch, pair tables, the
 // round's rotations, then the packed tiles (with_tiles).
@@ -115,8 +126,12 @@ jacobiSweepKernel(JacobiArgs args) {
   int *pair_j = pair_i + P;
   float *qs = reinterpret_cast<float *>(smem_raw + q_off);
   float *gtiles = args.tiles + args.t_offset[mi];
-  float *tiles = kSmem ? reinterpret_cast<float *>(smem_raw + tile_off) : gtiles;
-  const int tile_floats = nb * (nb + 1) / 2 * kTileF;
+  float *stiles = reinterpret_cast<float *>(smem_raw + tile_off);
+  const int tile_count = nb * (nb + 1) / 2;
+  // the shared-tile variant holds every tile on chip; the global-tile one the
+  // first smem_tiles (the rest stay in the L2-resident workspace)
+  const int split = kSmem ? tile_count : min(args.smem_tiles, tile_count);
+  const auto tiles = tileMem(std::integral_constant<bool, kSmem>{}, stiles, gtiles, split);
   const float *full = args.a + args.a_offset[mi];
   const int sched_at = args.sched_off != nullptr ? args.sched_off[mi] : -1;
   const int2 *sched = sched_at >= 0 ? args.sched + sched_at : nullptr;
@@ -136,13 +151,13 @@ jacobiSweepKernel(JacobiArgs args) {
         if (gi < n && gj < n) {
           v = 0.5f * (full[gi + static_cast<int64_t>(gj) * n] + full[gj + static_cast<int64_t>(gi) * n]);
         }
-        tiles[tileElement(tri[J] + I, e / 4, e % 4)] = v;
+        tileAt(tiles, tileElement(tri[J] + I, e / 4, e % 4)) = v;
       }
     }
-  } else if (kSmem) {
+  } else if (split > 0) {
     // the packed tiles kept between sweeps: one TMA bulk copy into shared
     // memory (bounded wait; on expiry the launch reports and does nothing)
-    if (threadIdx.x == 0) bulkLoadTiles(tiles, gtiles, tile_floats * sizeof(float), &tile_bar);
+    if (threadIdx.x == 0) bulkLoadTiles(stiles, gtiles, split * kTileF * sizeof(float), &tile_bar);
     __syncthreads();
     if (!bulkWaitTiles(&tile_bar)) {
       if (threadIdx.x == 0) atomicExch(args.status, kStatusMbarrierTimeout);
@@ -156,7 +171,7 @@ jacobiSweepKernel(JacobiArgs args) {
   for (int J = 0; J < nb; ++J) {
     for (int idx = threadIdx.x; idx < (J + 1) * kTileF; idx += blockDim.x) {
       const int I = idx / kTileF, e = idx % kTileF;
-      const double v = tiles[tileElement(tri[J] + I, e / 4, e % 4)];
+      const double v = tileAt(tiles, tileElement(tri[J] + I, e / 4, e % 4));
       if (I < J) off2 += 2.0 * v * v;
       else if (e / 4 == e % 4) diag2 += v * v;
       else off2 += v * v;
@@ -173,14 +188,14 @@ jacobiSweepKernel(JacobiArgs args) {
     // later, :1436-1444); full symmetric write-back of the matrix.
     float *eig = args.eigenvalues + args.eig_offset[mi];
     for (int k = threadIdx.x; k < n; k += blockDim.x) {
-      eig[k] = tiles[tileElement(tri[k / 4] + k / 4, k % 4, k % 4)];
+      eig[k] = tileAt(tiles, tileElement(tri[k / 4] + k / 4, k % 4, k % 4));
     }
     float *out = args.a + args.a_offset[mi];
     for (int c = 0; c < n; ++c) {
       for (int r = threadIdx.x; r < n; r += blockDim.x) {
         const int I = r / 4, J = c / 4;
-        const float v = I <= J ? tiles[tileElement(tri[J] + I, r % 4, c % 4)]
-                               : tiles[tileElement(tri[I] + J, c % 4, r % 4)];
+        const float v = I <= J ? tileAt(tiles, tileElement(tri[J] + I, r % 4, c % 4))
+                               : tileAt(tiles, tileElement(tri[I] + J, c % 4, r % 4));
         out[r + static_cast<int64_t>(c) * n] = v;
       }
     }
@@ -232,15 +247,15 @@ jacobiSweepKernel(JacobiArgs args) {
         tJJ = tileIndex(tri, J, J);
         // lane t starts with rows t (block I) and 7 - t (block J row 3 - t;
         // its left half is the mirror of tile (I, J))
-        const float4 *sII = reinterpret_cast<const float4 *>(tiles + static_cast<int64_t>(tII) * kTileF);
-        const float4 *sIJ = reinterpret_cast<const float4 *>(tiles + static_cast<int64_t>(tIJ) * kTileF);
-        const float4 *sJJ = reinterpret_cast<const float4 *>(tiles + static_cast<int64_t>(tJJ) * kTileF);
+        const float4 *sII = reinterpret_cast<const float4 *>(tiles.base(tII));
+        const float4 *sIJ = reinterpret_cast<const float4 *>(tiles.base(tIJ));
+        const float4 *sJJ = reinterpret_cast<const float4 *>(tiles.base(tJJ));
         const int jr = 3 - t4;
         const float4 v0 = sII[t4 ^ (tII & 3)], v1 = sIJ[t4 ^ (tIJ & 3)], v2 = sJJ[jr ^ (tJJ & 3)];
         ra[0] = v0.x; ra[1] = v0.y; ra[2] = v0.z; ra[3] = v0.w;
         ra[4] = v1.x; ra[5] = v1.y; ra[6] = v1.z; ra[7] = v1.w;
 #pragma unroll
-        for (int i = 0; i < 4; ++i) rb[i] = tiles[tileElement(tIJ, i, jr)];
+        for (int i = 0; i < 4; ++i) rb[i] = tileAt(tiles, tileElement(tIJ, i, jr));
         rb[4] = v2.x; rb[5] = v2.y; rb[6] = v2.z; rb[7] = v2.w;
       } else {
 #pragma unroll
@@ -250,9 +265,9 @@ jacobiSweepKernel(JacobiArgs args) {
       if (active) {
         // rows t (tiles (I, I), (I, J)) and 4 + t (tile (J, J)); the lower
         // left block is the mirror of tile (I, J) and is not stored
-        float4 *sII = reinterpret_cast<float4 *>(tiles + static_cast<int64_t>(tII) * kTileF);
-        float4 *sIJ = reinterpret_cast<float4 *>(tiles + static_cast<int64_t>(tIJ) * kTileF);
-        float4 *sJJ = reinterpret_cast<float4 *>(tiles + static_cast<int64_t>(tJJ) * kTileF);
+        float4 *sII = reinterpret_cast<float4 *>(tiles.base(tII));
+        float4 *sIJ = reinterpret_cast<float4 *>(tiles.base(tIJ));
+        float4 *sJJ = reinterpret_cast<float4 *>(tiles.base(tJJ));
         sII[t4 ^ (tII & 3)] = make_float4(ra[0], ra[1], ra[2], ra[3]);
         sIJ[t4 ^ (tIJ & 3)] = make_float4(ra[4], ra[5], ra[6], ra[7]);
         sJJ[t4 ^ (tJJ & 3)] = make_float4(rb[4], rb[5], rb[6], rb[7]);
@@ -295,16 +310,16 @@ jacobiSweepKernel(JacobiArgs args) {
       const bool valid = itemAt(base, k, l, h);
       const float4 *qk = reinterpret_cast<const float4 *>(qs + k * kQS);
       const float4 *ql = reinterpret_cast<const float4 *>(qs + l * kQS);
-      superTileHalf(tiles, SharedTri{tri}, qk, ql, pair_i[k], pair_j[k], pair_i[l], pair_j[l], h,
-                    valid);
+      superTileHalfMem(tiles, SharedTri{tri}, qk, ql, pair_i[k], pair_j[k], pair_i[l], pair_j[l], h,
+                       valid);
     }
     __syncthreads();
   }
-  if (kSmem) {
-    // tiles back to the workspace: one TMA bulk copy
+  if (split > 0) {
+    // the shared tiles back to the workspace: one TMA bulk copy
     fenceSharedToAsync();
     __syncthreads();
-    if (threadIdx.x == 0) bulkStoreTiles(gtiles, tiles, tile_floats * sizeof(float));
+    if (threadIdx.x == 0) bulkStoreTiles(gtiles, stiles, split * kTileF * sizeof(float));
   }
   if (threadIdx.x == 0) {
     st.norm2 = norm2;
@@ -1036,7 +1051,15 @@ int jacobiEnqueue(msq_ctx *ctx, const DeviceBatch *b, float *matrices, float *ve
       if (bucket.smem) {
         jacobiSweepKernel<true><<<bucket.count, how.threads, bucket.smem_bytes, s>>>(args);
       } else {
-        jacobiSweepKernel<false><<<bucket.count, how.threads, bucket.smem_bytes, s>>>(args);
+        // the global-tile class keeps what fits of its tiles in shared
+        // memory: one CTA per SM at 512 threads, two at 256 (the register
+        // budget allows two)
+        const size_t limit = how.threads >= 512 ? kSweepSmemLimit : kSweepSmemHalf;
+        const size_t room = limit > bucket.smem_bytes ? limit - bucket.smem_bytes : 0;
+        args.smem_tiles = static_cast<int>(room / (kTileF * sizeof(float)));
+        jacobiSweepKernel<false><<<bucket.count, how.threads,
+                                   bucket.smem_bytes + args.smem_tiles * kTileF * sizeof(float), s>>>(args);
+        args.smem_tiles = 0;
       }
       MSQ_TRY(launchedOn(ctx, s, sweepName(bucket.cls)));
       if (how.measure >= 0) {

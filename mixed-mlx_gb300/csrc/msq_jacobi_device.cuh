@@ -408,10 +408,48 @@ struct ComputedTri {
   }
 };
 
-template <class TileOf>
-__device__ __forceinline__ void superTileHalf(float *tiles, TileOf tileOf, const float4 *qk,
-                                              const float4 *ql, int rb0, int rb1, int cb0, int cb1,
-                                              int h, bool valid);
+// Where tile t lives: one flat array ...
+struct FlatTiles {
+  float *t;
+  __device__ __forceinline__ float *base(int ti) const { return t + static_cast<int64_t>(ti) * kTileF; }
+};
+// ... or tiles [0, split) in shared memory and the rest in the global
+// workspace (the global-tile sweep keeps what fits on chip).
+struct SplitTiles {
+  float *s;
+  float *g;
+  int split;
+  __device__ __forceinline__ float *base(int ti) const {
+    return ti < split ? s + ti * kTileF : g + static_cast<int64_t>(ti) * kTileF;
+  }
+};
+// Element e = tileElement(t, i, j) of a tile store.
+template <class Mem>
+__device__ __forceinline__ float &tileAt(const Mem &mem, int64_t e) {
+  return mem.base(static_cast<int>(e >> 4))[e & 15];
+}
+
+__device__ __forceinline__ void loadTileAt(const float *p, int ti, bool transposed, float (&t)[4][4]) {
+  const float4 *src = reinterpret_cast<const float4 *>(p);
+#pragma unroll
+  for (int i = 0; i < 4; ++i) {
+    const float4 v = src[i ^ (ti & 3)];
+    if (!transposed) {
+      t[i][0] = v.x; t[i][1] = v.y; t[i][2] = v.z; t[i][3] = v.w;
+    } else {
+      t[0][i] = v.x; t[1][i] = v.y; t[2][i] = v.z; t[3][i] = v.w;
+    }
+  }
+}
+
+__device__ __forceinline__ void storeTileAt(float *p, int ti, bool transposed, const float (&t)[4][4]) {
+  float4 *dst = reinterpret_cast<float4 *>(p);
+#pragma unroll
+  for (int i = 0; i < 4; ++i) {
+    dst[i ^ (ti & 3)] = transposed ? make_float4(t[0][i], t[1][i], t[2][i], t[3][i])
+                                   : make_float4(t[i][0], t[i][1], t[i][2], t[i][3]);
+  }
+}
 
 // Super-tile update T' = Q_k^T T Q_l on two lanes (h = 0, 1 of an adjacent
 // pair; the warp's lanes must all call it).  T is the 8x8 block of A on row
@@ -422,21 +460,10 @@ __device__ __forceinline__ void superTileHalf(float *tiles, TileOf tileOf, const
 // 4h..4h+3 of T' = U Q_l.  Every element is the ordered FMA chain of the
 // one-lane form (u over i, t' over j), as the CPU restatement.  Invalid
 // lanes compute on zeros and store nothing.
-// Source of the two input blocks: the tile store itself ...
-template <class TileOf>
-struct TileSource {
-  const float *tiles;
-  TileOf tileOf;
-  __device__ __forceinline__ void operator()(int R, int C, int, float (&t)[4][4]) const {
-    bool tr;
-    const int ti = tileOf(R, C, tr);
-    loadTile(tiles, ti, tr, t);
-  }
-};
-template <class TileOf, class Source>
-__device__ __forceinline__ void superTileHalf(float *tiles, TileOf tileOf, const Source &source,
-                                              const float4 *qk, const float4 *ql, int rb0, int rb1,
-                                              int cb0, int cb1, int h, bool valid) {
+template <class Mem, class TileOf>
+__device__ __forceinline__ void superTileHalfMem(const Mem &mem, TileOf tileOf, const float4 *qk,
+                                                 const float4 *ql, int rb0, int rb1, int cb0,
+                                                 int cb1, int h, bool valid) {
   const int cbh = h ? cb1 : cb0;
   float u[8][4];
 #pragma unroll
@@ -447,7 +474,9 @@ __device__ __forceinline__ void superTileHalf(float *tiles, TileOf tileOf, const
   for (int x = 0; x < 2; ++x) {
     float b4[4][4];
     if (valid) {
-      source(x ? rb1 : rb0, cbh, x, b4);
+      bool tr;
+      const int ti = tileOf(x ? rb1 : rb0, cbh, tr);
+      loadTileAt(mem.base(ti), ti, tr, b4);
     } else {
 #pragma unroll
       for (int i = 0; i < 4; ++i)
@@ -502,7 +531,7 @@ __device__ __forceinline__ void superTileHalf(float *tiles, TileOf tileOf, const
         for (int c = 0; c < 4; ++c) b4[r][c] = o[r][4 * y + c];
       bool tr;
       const int ti = tileOf(rbh, y ? cb1 : cb0, tr);
-      storeTile(tiles, ti, tr, b4);
+      storeTileAt(mem.base(ti), ti, tr, b4);
     }
   }
 }
@@ -511,8 +540,7 @@ template <class TileOf>
 __device__ __forceinline__ void superTileHalf(float *tiles, TileOf tileOf, const float4 *qk,
                                               const float4 *ql, int rb0, int rb1, int cb0, int cb1,
                                               int h, bool valid) {
-  superTileHalf(tiles, tileOf, TileSource<TileOf>{tiles, tileOf}, qk, ql, rb0, rb1, cb0, cb1, h,
-                valid);
+  superTileHalfMem(FlatTiles{tiles}, tileOf, qk, ql, rb0, rb1, cb0, cb1, h, valid);
 }
 
 
