@@ -551,13 +551,18 @@ const char *className(int c) {
   return names[c];
 }
 
+// A candidate is a CTA size; a negative one runs a shared-tile class with
+// the global-tile variant (as many tiles in shared memory as fit two CTAs
+// per SM, the rest in the workspace), trading on-chip tiles for a second
+// CTA that overlaps the other's pivot phase.
 std::vector<int> classCandidates(int c) {
   switch (c) {
     case 0: return {32};
     case 1: return {64, 32};
     case 2: return {128, 64};
     case 3: return {256, 128};
-    case 4: return {256, 512};
+    case 4: return {256, 512, -256};
+    case 5: return {512, 256, -256};
     default: return {512, 256};
   }
 }
@@ -640,7 +645,9 @@ struct JacobiPlan {
   int64_t tile_total = 0, log_total = 0;
   int64_t *t_offset = nullptr, *log_offset = nullptr;
   int32_t *order = nullptr;  // ids grouped by bucket, largest first
-  struct Bucket { int cls; bool smem; int first; int count; size_t smem_bytes; };
+  // smem_bytes: the class's kernel layout; base_bytes: the layout without
+  // tiles (the global-tile variant adds what it keeps on chip)
+  struct Bucket { int cls; bool smem; int first; int count; size_t smem_bytes; size_t base_bytes; };
   std::vector<Bucket> buckets;
   int32_t *work_matrix = nullptr, *work_row = nullptr;
   int work_count = 0;
@@ -774,13 +781,14 @@ JacobiPlan *planFor(msq_ctx *ctx, const DeviceBatch *b, int mode) {
     const int c = sizeClass(b->host_n[ids[i]]);
     const bool smem = fitsSmem(b->host_n[ids[i]]);
     int j = i;
-    size_t bytes = 0;
+    size_t bytes = 0, base = 0;
     while (j < count && sizeClass(b->host_n[ids[j]]) == c) {
       size_t q_off, tile_off;
       bytes = std::max(bytes, sweepSmemLayout(b->host_n[ids[j]], smem, &q_off, &tile_off));
+      base = std::max(base, sweepSmemLayout(b->host_n[ids[j]], false, &q_off, &tile_off));
       ++j;
     }
-    plan->buckets.push_back({c, smem, i, j - i, bytes});
+    plan->buckets.push_back({c, smem, i, j - i, bytes, base});
     i = j;
   }
   std::vector<int32_t> wm, wr;
@@ -1048,17 +1056,18 @@ int jacobiEnqueue(msq_ctx *ctx, const DeviceBatch *b, float *matrices, float *ve
         cudaEventRecord(t0, s);
       }
       launchBegin(ctx, s);
-      if (bucket.smem) {
-        jacobiSweepKernel<true><<<bucket.count, how.threads, bucket.smem_bytes, s>>>(args);
+      const int threads = how.threads < 0 ? -how.threads : how.threads;
+      if (bucket.smem && how.threads > 0) {
+        jacobiSweepKernel<true><<<bucket.count, threads, bucket.smem_bytes, s>>>(args);
       } else {
-        // the global-tile class keeps what fits of its tiles in shared
-        // memory: one CTA per SM at 512 threads, two at 256 (the register
-        // budget allows two)
-        const size_t limit = how.threads >= 512 ? kSweepSmemLimit : kSweepSmemHalf;
-        const size_t room = limit > bucket.smem_bytes ? limit - bucket.smem_bytes : 0;
+        // global-tile variant: what fits of the tiles in shared memory, one
+        // CTA per SM at 512 threads, two at 256 (the register budget allows
+        // two)
+        const size_t limit = threads >= 512 ? kSweepSmemLimit : kSweepSmemHalf;
+        const size_t room = limit > bucket.base_bytes ? limit - bucket.base_bytes : 0;
         args.smem_tiles = static_cast<int>(room / (kTileF * sizeof(float)));
-        jacobiSweepKernel<false><<<bucket.count, how.threads,
-                                   bucket.smem_bytes + args.smem_tiles * kTileF * sizeof(float), s>>>(args);
+        jacobiSweepKernel<false><<<bucket.count, threads,
+                                   bucket.base_bytes + args.smem_tiles * kTileF * sizeof(float), s>>>(args);
         args.smem_tiles = 0;
       }
       MSQ_TRY(launchedOn(ctx, s, sweepName(bucket.cls)));
@@ -1156,14 +1165,20 @@ extern "C" int msq_autotune_report(int device, char *out, size_t capacity) {
       text += std::string("jacobi sweep ") + className(c) + ": threads";
       for (size_t i = 0; i < t.cands.size(); ++i) {
         char buf[64];
+        const int c = t.cands[i];
         if (t.ms[i] > 0.0) {
-          std::snprintf(buf, sizeof(buf), " %d=%.4fms", t.cands[i], t.ms[i]);
+          std::snprintf(buf, sizeof(buf), " %d%s=%.4fms", c < 0 ? -c : c, c < 0 ? "(split)" : "", t.ms[i]);
         } else {
-          std::snprintf(buf, sizeof(buf), " %d=?", t.cands[i]);
+          std::snprintf(buf, sizeof(buf), " %d%s=?", c < 0 ? -c : c, c < 0 ? "(split)" : "");
         }
         text += buf;
       }
-      text += t.best >= 0 ? " -> " + std::to_string(t.cands[t.best]) + "\n" : " -> untuned\n";
+      if (t.best >= 0) {
+        const int c = t.cands[t.best];
+        text += " -> " + std::to_string(c < 0 ? -c : c) + (c < 0 ? "(split)\n" : "\n");
+      } else {
+        text += " -> untuned\n";
+      }
     }
   }
   std::strncpy(out, text.c_str(), capacity - 1);
