@@ -238,11 +238,29 @@ def run_codec(args):
     out = torch.empty_like(x)
     lib = msq.lib()
 
-    def step():
+    def encode():
         ctx.check(lib.msq_encode(ctx.handle, msq.MXFP4_E2M1, x.data_ptr(), n, 0, vals.data_ptr(),
                                  scales.data_ptr()), "encode")
+
+    def decode():
         ctx.check(lib.msq_decode(ctx.handle, msq.MXFP4_E2M1, vals.data_ptr(), scales.data_ptr(),
                                  n, 0, out.data_ptr()), "decode")
+
+    def step():
+        encode()
+        decode()
+
+    def kernel_ms(fn, reps):
+        # back-to-back launches of one kernel between two events on the
+        # launching stream: its average duration
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        a.record(stream)
+        for _ in range(reps):
+            fn()
+        b.record(stream)
+        torch.cuda.synchronize()
+        return a.elapsed_time(b) / reps
 
     for _ in range(max(3, args.warmup)):
         step()
@@ -265,8 +283,8 @@ def run_codec(args):
     except OSError:
         pass
     hbm = peaks.get("hbm_gbs", 6800.0)
-    enc_ms = rows["msq_encode"][1] / rows["msq_encode"][0]
-    dec_ms = rows["msq_decode"][1] / rows["msq_decode"][0]
+    enc_ms = kernel_ms(encode, 4 * args.steps)
+    dec_ms = kernel_ms(decode, 4 * args.steps)
     # bit-exact spot check against the oracle on sampled blocks (untimed)
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import oracle as O

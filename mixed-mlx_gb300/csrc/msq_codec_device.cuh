@@ -101,6 +101,22 @@ __device__ __forceinline__ uint32_t encodeE2M1(float value) {
   return sign | roundMagnitude<1, 1>(magnitude);
 }
 
+// Two values to E2M1 with the hardware conversion (round to nearest even,
+// saturating to +-6 for a larger magnitude or an infinity), packed with the
+// even element in the low nibble.  The conversion has no NaN code; a NaN
+// becomes +-0 with its sign, as floatToFp4E2M1 maps it
+// (src/storage_codecs.cpp:457-466).  Same codes as encodeE2M1.
+__device__ __forceinline__ uint32_t encodeE2M1Pair(float even, float odd) {
+  uint16_t r;
+  asm("{\n .reg .b8 t;\n cvt.rn.satfinite.e2m1x2.f32 t, %1, %2;\n cvt.u16.u8 %0, t;\n}"
+      : "=h"(r)
+      : "f"(odd), "f"(even));
+  uint32_t code = r;
+  if (even != even) code = (code & 0xf0u) | ((__float_as_uint(even) >> 28) & 0x8u);
+  if (odd != odd) code = (code & 0x0fu) | ((__float_as_uint(odd) >> 24) & 0x80u);
+  return code;
+}
+
 __device__ __forceinline__ float signedNan(uint32_t negative) {
   return __uint_as_float(0x7fc00000u | (negative ? 0x80000000u : 0u));
 }

@@ -169,8 +169,9 @@ encodeMxKernel(const float *__restrict__ source, size_t elements,
     if constexpr (kFormat == MSQ_FMT_MXFP4_E2M1) {
       uint64_t packed = 0;
 #pragma unroll
-      for (int i = 0; i < kGroup; ++i) {
-        packed |= static_cast<uint64_t>(encodeE2M1(mxDivide(g.v[i], e))) << (4 * i);
+      for (int i = 0; i < kGroup; i += 2) {
+        packed |= static_cast<uint64_t>(encodeE2M1Pair(mxDivide(g.v[i], e), mxDivide(g.v[i + 1], e)))
+                  << (4 * i);
       }
       storeBytes(values, base / 2, packed, static_cast<int>((valid + 1) / 2),
                  vector_ok);
