@@ -485,24 +485,25 @@ __device__ __forceinline__ void superTileHalfMem(const Mem &mem, TileOf tileOf, 
     }
 #pragma unroll
     for (int i = 0; i < 4; ++i) {
-      const float4 lo = qk[2 * (4 * x + i)], hi = qk[2 * (4 * x + i) + 1];
-      const float qr[8] = {lo.x, lo.y, lo.z, lo.w, hi.x, hi.y, hi.z, hi.w};
+      // u[a] holds U row (a + 4h) mod 8: lane h reads the two halves of the
+      // rotation row in its own order (same FMA chains, no selects)
+      const float4 first = qk[2 * (4 * x + i) + h], second = qk[2 * (4 * x + i) + 1 - h];
+      const float qr[8] = {first.x, first.y, first.z, first.w, second.x, second.y, second.z, second.w};
 #pragma unroll
       for (int a = 0; a < 8; ++a)
 #pragma unroll
         for (int c = 0; c < 4; ++c) u[a][c] = fmaf(qr[a], b4[i][c], u[a][c]);
     }
   }
-  // U rows of this lane's half: own columns, and the partner's columns
-  // for these rows (the partner sends the rows of the other half).
+  // U rows 4h..4h+3 of this lane's half: own columns (u[0..3]) and the
+  // partner's columns for these rows (the partner sends its u[4..7]).
   float ur[4][8];
 #pragma unroll
   for (int r = 0; r < 4; ++r)
 #pragma unroll
     for (int c = 0; c < 4; ++c) {
-      const float mine = h ? u[4 + r][c] : u[r][c];
-      const float send = h ? u[r][c] : u[4 + r][c];
-      const float got = __shfl_xor_sync(0xffffffffu, send, 1);
+      const float mine = u[r][c];
+      const float got = __shfl_xor_sync(0xffffffffu, u[4 + r][c], 1);
       ur[r][c] = h ? got : mine;
       ur[r][4 + c] = h ? mine : got;
     }
