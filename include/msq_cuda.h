@@ -154,9 +154,9 @@ int msq_jacobi_batched(msq_ctx *ctx, float *matrices, float *vectors,
  *                       the 64x64 diagonal blocks (CUDA cores) and the rest
  *                       of A is brought up to date once per stage on the
  *                       tensor cores (B = A Z, A = B^T Z, split BF16), V as
- *                       in mode 2.  Eigenvalues to about 1e-4 ||A||; slower
- *                       than mode 2 on GB300 (the per-stage passes stream
- *                       A through HBM twice).
+ *                       in mode 2.  Eigenvalues to about 1e-4 ||A||; about
+ *                       2x slower than mode 2 on GB300 (the per-stage
+ *                       passes stream A through HBM twice).
  * The mode applies to later calls on the context.                          */
 enum {
   MSQ_VECTORS_AUTO = -1,

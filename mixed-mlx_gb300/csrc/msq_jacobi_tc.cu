@@ -569,13 +569,15 @@ __device__ __forceinline__ int localToGlobal(int li, int Ps, int Qs, int n) {
   return g < n ? g : -1;
 }
 
-__global__ void __launch_bounds__(kInnerThreads) tlInnerKernel(InnerArgs args) {
+__global__ void __launch_bounds__(kInnerThreads, 4) tlInnerKernel(InnerArgs args) {
   __shared__ __align__(16) float tiles[kLocalTiles * kTileF];
   __shared__ __align__(16) float z[64 * kFormLd];
   __shared__ __align__(16) float qs[8 * kQS];
   __shared__ int tri[kLocalBlocks + 1];
-  __shared__ int pair_i[8], pair_j[8], pair_on[8];
-  __shared__ int entries[2 * kSuperBlock - 1][8];  // the stage's rotating pairs, round by round
+  // local pairs of every round of the stage: the rotating ones, then the
+  // other local blocks paired in order with the identity
+  __shared__ int pairs_i[2 * kSuperBlock - 1][8], pairs_j[2 * kSuperBlock - 1][8];
+  __shared__ int pairs_on[2 * kSuperBlock - 1][8];
   const int2 w = args.work[blockIdx.x];
   const int mi = w.x, x = w.y;
   if (args.state[mi].done) return;
@@ -602,40 +604,38 @@ __global__ void __launch_bounds__(kInnerThreads) tlInnerKernel(InnerArgs args) {
   }
   const int32_t *prog = args.prog + args.prog_off[mi];
   const int r0 = twoLevelStageFirst(args.stage), rounds = twoLevelStageRounds(args.stage);
-  for (int q = tid; q < rounds * 8; q += blockDim.x)
-    entries[q / 8][q % 8] = prog[((r0 + q / 8) * pairs + x) * 8 + q % 8];
+  if (tid < rounds) {
+    const int t = tid;
+    const int32_t *entry = prog + ((r0 + t) * pairs + x) * 8;
+    unsigned used = 0;
+    int cnt = 0;
+    for (int e = 0; e < 8; ++e) {
+      const int code = entry[e];
+      if (code < 0) break;
+      const int la = (code >> 8) & 255, lb = code >> 16;
+      pairs_i[t][cnt] = la;
+      pairs_j[t][cnt] = lb;
+      pairs_on[t][cnt] = 1;
+      used |= (1u << la) | (1u << lb);
+      ++cnt;
+    }
+    int idle = -1;
+    for (int L = 0; L < kLocalBlocks; ++L) {
+      if (used & (1u << L)) continue;
+      if (idle < 0) {
+        idle = L;
+        continue;
+      }
+      pairs_i[t][cnt] = idle;
+      pairs_j[t][cnt] = L;
+      pairs_on[t][cnt] = 0;
+      ++cnt;
+      idle = -1;
+    }
+  }
   __syncthreads();
   for (int t = 0; t < rounds; ++t) {
-    if (tid == 0) {
-      // the round's rotating pairs, then the other local blocks paired in
-      // order with the identity
-      unsigned used = 0;
-      int cnt = 0;
-      for (int e = 0; e < 8; ++e) {
-        const int code = entries[t][e];
-        if (code < 0) break;
-        const int la = (code >> 8) & 255, lb = code >> 16;
-        pair_i[cnt] = la;
-        pair_j[cnt] = lb;
-        pair_on[cnt] = 1;
-        used |= (1u << la) | (1u << lb);
-        ++cnt;
-      }
-      int idle = -1;
-      for (int L = 0; L < kLocalBlocks; ++L) {
-        if (used & (1u << L)) continue;
-        if (idle < 0) {
-          idle = L;
-          continue;
-        }
-        pair_i[cnt] = idle;
-        pair_j[cnt] = L;
-        pair_on[cnt] = 0;
-        ++cnt;
-        idle = -1;
-      }
-    }
-    __syncthreads();
+    const int *pair_i = pairs_i[t], *pair_j = pairs_j[t], *pair_on = pairs_on[t];
     if (warp == 0) {
       // pivots: quad k of warp 0 sweeps local pair k
       const int k = tid >> 2, t4 = tid & 3;
@@ -902,12 +902,12 @@ __global__ void __launch_bounds__(kPassThreads, 1) tlPassKernel(PassArgs args) {
           if (row < n) {
             const int sb = row >> 5;
             const int local = sb == Ps ? row - 32 * Ps : (sb == Qs ? 32 + row - 32 * Qs : -1);
-#pragma unroll 8
+            const float *drow = local >= 0 ? diag + (static_cast<int64_t>(y) * 64 + local) * 64 : nullptr;
+#pragma unroll
             for (int j = 0; j < 64; ++j) {
               const int g = localToGlobal(j, Ps, Qs, n);
               if (g < 0) continue;
-              const float v = local >= 0 ? diag[(static_cast<int64_t>(y) * 64 + local) * 64 + j] : d[j];
-              Dst[row + static_cast<int64_t>(g) * n] = v;
+              Dst[row + static_cast<int64_t>(g) * n] = drow != nullptr ? drow[j] : d[j];
             }
           }
         } else {
