@@ -105,15 +105,18 @@ __device__ __forceinline__ uint32_t encodeE2M1(float value) {
 // saturating to +-6 for a larger magnitude or an infinity), packed with the
 // even element in the low nibble.  The conversion has no NaN code; a NaN
 // becomes +-0 with its sign, as floatToFp4E2M1 maps it
-// (src/storage_codecs.cpp:457-466).  Same codes as encodeE2M1.
-__device__ __forceinline__ uint32_t encodeE2M1Pair(float even, float odd) {
+// (src/storage_codecs.cpp:457-466): nan_even / nan_odd are the values whose
+// NaN-ness and sign decide that (the unscaled inputs, since a product may
+// not keep a NaN's sign).  Same codes as encodeE2M1.
+__device__ __forceinline__ uint32_t encodeE2M1Pair(float even, float odd, float nan_even,
+                                                   float nan_odd) {
   uint16_t r;
   asm("{\n .reg .b8 t;\n cvt.rn.satfinite.e2m1x2.f32 t, %1, %2;\n cvt.u16.u8 %0, t;\n}"
       : "=h"(r)
       : "f"(odd), "f"(even));
   uint32_t code = r;
-  if (even != even) code = (code & 0xf0u) | ((__float_as_uint(even) >> 28) & 0x8u);
-  if (odd != odd) code = (code & 0x0fu) | ((__float_as_uint(odd) >> 24) & 0x80u);
+  if (nan_even != nan_even) code = (code & 0xf0u) | ((__float_as_uint(nan_even) >> 28) & 0x8u);
+  if (nan_odd != nan_odd) code = (code & 0x0fu) | ((__float_as_uint(nan_odd) >> 24) & 0x80u);
   return code;
 }
 

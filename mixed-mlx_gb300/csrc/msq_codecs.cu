@@ -168,10 +168,20 @@ encodeMxKernel(const float *__restrict__ source, size_t elements,
     if (group % 4 == 0) scales[group / 4] = static_cast<uint8_t>(e + 127);
     if constexpr (kFormat == MSQ_FMT_MXFP4_E2M1) {
       uint64_t packed = 0;
+      if (e >= -126 && e <= 126) {
+        // x / 2^e is the exact product x * 2^-e; a NaN keeps the sign of x
+        const float s = exp2Int(-e);
 #pragma unroll
-      for (int i = 0; i < kGroup; i += 2) {
-        packed |= static_cast<uint64_t>(encodeE2M1Pair(mxDivide(g.v[i], e), mxDivide(g.v[i + 1], e)))
-                  << (4 * i);
+        for (int i = 0; i < kGroup; i += 2) {
+          packed |= static_cast<uint64_t>(encodeE2M1Pair(g.v[i] * s, g.v[i + 1] * s, g.v[i], g.v[i + 1]))
+                    << (4 * i);
+        }
+      } else {
+#pragma unroll
+        for (int i = 0; i < kGroup; i += 2) {
+          const float a = mxDivide(g.v[i], e), b = mxDivide(g.v[i + 1], e);
+          packed |= static_cast<uint64_t>(encodeE2M1Pair(a, b, a, b)) << (4 * i);
+        }
       }
       storeBytes(values, base / 2, packed, static_cast<int>((valid + 1) / 2),
                  vector_ok);
