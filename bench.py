@@ -301,7 +301,7 @@ def run_codec(args):
                        "l2": "inputs larger than L2 (268 MB)"},
             "roofline": {"bound": "hbm", "achieved": enc_bytes / (enc_ms / 1e3) / 1e9, "peak": hbm,
                          "unit": "GB/s", "frac": enc_bytes / (enc_ms / 1e3) / 1e9 / hbm,
-                         "traffic": None, "kernel": "msq_encode (encodeMxKernel<MXFP4>)",
+                         "traffic": None, "kernel": "msq_encode (encodeMxfp4Kernel)",
                          "decode_achieved": dec_bytes / (dec_ms / 1e3) / 1e9,
                          "decode_frac": dec_bytes / (dec_ms / 1e3) / 1e9 / hbm},
             "bit_exact_sampled_blocks": exact, "clocks": clocks.summary(),

@@ -20,6 +20,8 @@
 //    an exact ldexp (all products are representable).
 #pragma once
 
+#include <cuda_fp16.h>
+
 #include <cstdint>
 
 namespace msq {
@@ -162,6 +164,15 @@ __device__ __forceinline__ float decodeE2M1(uint32_t code) {
     return __uint_as_float(sign | (fraction ? 0x3f000000u : 0u));
   }
   return __uint_as_float(sign | ((exponent + 126u) << 23) | (fraction << 22));
+}
+
+// Two E2M1 codes (one byte, even element in the low nibble) to FP32 through
+// the hardware E2M1 -> FP16 conversion, which is exact (E2M1 values have at
+// most two significant bits).  Same values as decodeE2M1.
+__device__ __forceinline__ float2 decodeE2M1Pair(uint32_t byte) {
+  uint32_t h2;
+  asm("{\n .reg .b8 t;\n cvt.u8.u32 t, %1;\n cvt.rn.f16x2.e2m1x2 %0, t;\n}" : "=r"(h2) : "r"(byte));
+  return __half22float2(*reinterpret_cast<const __half2 *>(&h2));
 }
 
 // ilogb of a finite, nonzero magnitude (normal or subnormal FP32).

@@ -199,6 +199,65 @@ encodeMxKernel(const float *__restrict__ source, size_t elements,
   }
 }
 
+constexpr int kDecodeStride = 9;  // float4 per staged block row (8 + 1 pad)
+
+// MXFP4 encode, one 32-element block per lane: a warp loads its 32
+// consecutive blocks as 512 contiguous bytes per instruction into shared
+// memory (the decode kernel's padded layout), then each lane takes its
+// block's maximum without shuffles, converts its 32 values with the
+// hardware E2M1 conversion and stores 16 bytes of codes and its scale byte.
+// Whole blocks only: the generic kernel encodes a ragged tail.
+__global__ void __launch_bounds__(kThreads)
+encodeMxfp4Kernel(const float *__restrict__ source, size_t blocks, uint8_t *__restrict__ values,
+                  uint8_t *__restrict__ scales) {
+  __shared__ float4 stage[kThreads / 32][32 * kDecodeStride];
+  const int warp = threadIdx.x / 32, lane = threadIdx.x % 32;
+  float4 *my = stage[warp];
+  const size_t warps = static_cast<size_t>(gridDim.x) * (blockDim.x / 32);
+  for (size_t first = (blockIdx.x * static_cast<size_t>(blockDim.x / 32) + warp) * 32; first < blocks;
+       first += warps * 32) {
+    const float4 *in = reinterpret_cast<const float4 *>(source + first * 32);
+#pragma unroll
+    for (int q = 0; q < 8; ++q) {
+      const int f = 32 * q + lane;
+      if (first + f / 8 < blocks) my[(f / 8) * kDecodeStride + f % 8] = __ldcs(in + f);
+    }
+    __syncwarp();
+    const size_t blk = first + lane;
+    if (blk < blocks) {
+      float v[32];
+#pragma unroll
+      for (int j = 0; j < 8; ++j) {
+        const float4 t = my[lane * kDecodeStride + j];
+        v[4 * j] = t.x; v[4 * j + 1] = t.y; v[4 * j + 2] = t.z; v[4 * j + 3] = t.w;
+      }
+      float m = 0.0f;
+#pragma unroll
+      for (int i = 0; i < 32; ++i) {
+        const float a = fabsf(v[i]);
+        if (a <= 3.402823466e38f) m = fmaxf(m, a);  // finite only (NaN fails)
+      }
+      const int e = mxExponent(m, 2);
+      scales[blk] = static_cast<uint8_t>(e + 127);
+      uint32_t w[4] = {0u, 0u, 0u, 0u};
+      if (e >= -126 && e <= 126) {
+        const float s = exp2Int(-e);
+#pragma unroll
+        for (int i = 0; i < 32; i += 2)
+          w[i / 8] |= encodeE2M1Pair(v[i] * s, v[i + 1] * s, v[i], v[i + 1]) << (4 * (i % 8));
+      } else {
+#pragma unroll
+        for (int i = 0; i < 32; i += 2) {
+          const float a = mxDivide(v[i], e), b = mxDivide(v[i + 1], e);
+          w[i / 8] |= encodeE2M1Pair(a, b, a, b) << (4 * (i % 8));
+        }
+      }
+      __stcs(reinterpret_cast<uint4 *>(values + blk * 16), make_uint4(w[0], w[1], w[2], w[3]));
+    }
+    __syncwarp();
+  }
+}
+
 // FP8 E4M3FN with one FP32 scale per contiguous row: s = max|row| / 448
 // (1 when the row has no nonzero finite value), code = E4M3(x / s).  One warp
 // per row: a max pass, then an encode pass (the row is re-read from L1/L2).
@@ -228,6 +287,61 @@ encodeRowScaleKernel(const float *__restrict__ source, size_t rows,
 }
 
 // ---------------------------------------------------------------- decoders
+
+// MXFP4 decode, one 32-element block per lane: one 16-byte load of its
+// codes and its scale byte (four times the bytes in flight per thread of
+// the generic kernel), the hardware E2M1 -> FP16 conversion, and one
+// multiplication by 2^(scale - 127) — exact for the exponents of normal
+// powers of two; the two-step product of mxScale otherwise.  A warp decodes
+// 32 consecutive blocks into shared memory (row stride 9 float4: no bank
+// conflicts) and stores them back as 512 contiguous bytes per instruction.
+// Whole blocks only: the generic kernel decodes a ragged tail.
+__global__ void __launch_bounds__(kThreads)
+decodeMxfp4Kernel(const uint8_t *__restrict__ values, const uint8_t *__restrict__ scales,
+                  size_t blocks, float *__restrict__ output) {
+  __shared__ float4 stage[kThreads / 32][32 * kDecodeStride];
+  const int warp = threadIdx.x / 32, lane = threadIdx.x % 32;
+  float4 *my = stage[warp];
+  const size_t warps = static_cast<size_t>(gridDim.x) * (blockDim.x / 32);
+  for (size_t first = (blockIdx.x * static_cast<size_t>(blockDim.x / 32) + warp) * 32; first < blocks;
+       first += warps * 32) {
+    const size_t blk = first + lane;
+    if (blk < blocks) {
+      const uint4 p = __ldcs(reinterpret_cast<const uint4 *>(values + blk * 16));
+      const uint32_t scale = scales[blk];
+      const int k = static_cast<int>(scale) - 127;
+      const uint32_t w[4] = {p.x, p.y, p.z, p.w};
+      float4 *row = my + lane * kDecodeStride;
+      if (k >= -126 && k <= 127) {
+        const float s = exp2Int(k);
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+          const float2 a = decodeE2M1Pair(w[q] & 0xffu), b = decodeE2M1Pair((w[q] >> 8) & 0xffu);
+          const float2 c = decodeE2M1Pair((w[q] >> 16) & 0xffu), d = decodeE2M1Pair(w[q] >> 24);
+          row[2 * q] = make_float4(a.x * s, a.y * s, b.x * s, b.y * s);
+          row[2 * q + 1] = make_float4(c.x * s, c.y * s, d.x * s, d.y * s);
+        }
+      } else {
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+          float v[8];
+#pragma unroll
+          for (int i = 0; i < 8; ++i) v[i] = mxScale(decodeE2M1((w[q] >> (4 * i)) & 0xfu), scale);
+          row[2 * q] = make_float4(v[0], v[1], v[2], v[3]);
+          row[2 * q + 1] = make_float4(v[4], v[5], v[6], v[7]);
+        }
+      }
+    }
+    __syncwarp();
+    float4 *out = reinterpret_cast<float4 *>(output + first * 32);
+#pragma unroll
+    for (int q = 0; q < 8; ++q) {
+      const int f = 32 * q + lane;  // float4 index in the warp's 32 blocks
+      if (first + f / 8 < blocks) __stcs(out + f, my[(f / 8) * kDecodeStride + f % 8]);
+    }
+    __syncwarp();
+  }
+}
 
 template <int kFormat>
 __global__ void __launch_bounds__(kThreads)
@@ -380,7 +494,18 @@ extern "C" int msq_encode(msq_ctx *ctx, int format, const float *source,
       encodeMxKernel<MSQ_FMT_MXFP8_E5M2><<<gridFor((elements + 31) / 32 * 4, kThreads), kThreads, 0, s>>>(source, elements, values, scales, vec);
       break;
     case MSQ_FMT_MXFP4_E2M1:
-      encodeMxKernel<MSQ_FMT_MXFP4_E2M1><<<gridFor((elements + 31) / 32 * 4, kThreads), kThreads, 0, s>>>(source, elements, values, scales, vec);
+      if (vec && elements >= 32) {
+        const size_t whole = elements / 32;
+        encodeMxfp4Kernel<<<gridFor(whole, kThreads), kThreads, 0, s>>>(source, whole, values, scales);
+        if (whole * 32 < elements) {
+          MSQ_TRY(launched(ctx, "msq_encode"));
+          const size_t rest = elements - whole * 32;
+          encodeMxKernel<MSQ_FMT_MXFP4_E2M1><<<1, kThreads, 0, s>>>(
+              source + whole * 32, rest, values + whole * 16, scales + whole, vec);
+        }
+      } else {
+        encodeMxKernel<MSQ_FMT_MXFP4_E2M1><<<gridFor((elements + 31) / 32 * 4, kThreads), kThreads, 0, s>>>(source, elements, values, scales, vec);
+      }
       break;
     case MSQ_FMT_FP8_E4M3FN_ROWSCALE: {
       if (row_length == 0 || elements % row_length != 0) {
@@ -421,6 +546,19 @@ extern "C" int msq_decode(msq_ctx *ctx, int format, const uint8_t *values,
       return cudaCheck(ctx, cudaMemcpyAsync(output, values, elements * 4,
                                             cudaMemcpyDeviceToDevice, s),
                        "msq_decode fp32 copy");
+    case MSQ_FMT_MXFP4_E2M1:
+      if (vec && elements >= 32) {
+        const size_t whole = elements / 32;
+        decodeMxfp4Kernel<<<gridFor(whole, kThreads), kThreads, 0, s>>>(values, scales, whole, output);
+        if (whole * 32 < elements) {
+          MSQ_TRY(launched(ctx, "msq_decode"));
+          decodeKernel<MSQ_FMT_MXFP4_E2M1><<<1, kThreads, 0, s>>>(
+              values + whole * 16, scales + whole, elements - whole * 32, output + whole * 32, vec);
+        }
+      } else {
+        decodeKernel<MSQ_FMT_MXFP4_E2M1><<<grid, kThreads, 0, s>>>(values, scales, elements, output, vec);
+      }
+      break;
 #define MSQ_DECODE_CASE(F) \
     case F: decodeKernel<F><<<grid, kThreads, 0, s>>>(values, scales, elements, output, vec); break;
     MSQ_DECODE_CASE(MSQ_FMT_BF16)
@@ -429,7 +567,6 @@ extern "C" int msq_decode(msq_ctx *ctx, int format, const uint8_t *values,
     MSQ_DECODE_CASE(MSQ_FMT_MXFP8_E4M3FN)
     MSQ_DECODE_CASE(MSQ_FMT_MXFP8_E5M2)
     MSQ_DECODE_CASE(MSQ_FMT_FP4_E2M1)
-    MSQ_DECODE_CASE(MSQ_FMT_MXFP4_E2M1)
 #undef MSQ_DECODE_CASE
     case MSQ_FMT_FP8_E4M3FN_ROWSCALE:
       if (row_length == 0 || elements % row_length != 0) {
