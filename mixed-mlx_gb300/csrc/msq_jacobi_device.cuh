@@ -255,8 +255,9 @@ __device__ __forceinline__ bool jacobiAngle(float paa, float pbb, float pab, flo
   if (pab == 0.0f) return false;
   const float tau = __fdiv_rn(__fsub_rn(pbb, paa), __fmul_rn(2.0f, pab));
   const float root = __fsqrt_rn(__fadd_rn(__fmul_rn(tau, tau), 1.0f));
-  const float t = copysignf(__fdiv_rn(1.0f, __fadd_rn(fabsf(tau), root)), tau);
-  float cc0 = __fdiv_rn(1.0f, __fsqrt_rn(__fadd_rn(__fmul_rn(t, t), 1.0f)));
+  // 1 / x correctly rounded (__frcp_rn) is the IEEE quotient 1.0f / x
+  const float t = copysignf(__frcp_rn(__fadd_rn(fabsf(tau), root)), tau);
+  float cc0 = __frcp_rn(__fsqrt_rn(__fadd_rn(__fmul_rn(t, t), 1.0f)));
   float ss0 = __fmul_rn(t, cc0);
   const float cc = __fmul_rn(cc0, cc0), cce = fmaf(cc0, cc0, -cc);
   const float ss = __fmul_rn(ss0, ss0), sse = fmaf(ss0, ss0, -ss);
