@@ -452,6 +452,25 @@ __device__ __forceinline__ void storeTileAt(float *p, int ti, bool transposed, c
   }
 }
 
+// Two FP32 values in one 64-bit register (low half first, as in memory).
+// fma.rn.f32x2 performs two IEEE fused multiply-adds: the bits of two fmaf
+// calls, issued as one instruction.
+typedef unsigned long long f32x2;
+__device__ __forceinline__ f32x2 f2zero() { return 0ull; }
+__device__ __forceinline__ f32x2 f2make(float lo, float hi) {
+  f32x2 r;
+  asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(lo), "f"(hi));
+  return r;
+}
+__device__ __forceinline__ void f2split(f32x2 v, float &lo, float &hi) {
+  asm("mov.b64 {%0, %1}, %2;" : "=f"(lo), "=f"(hi) : "l"(v));
+}
+__device__ __forceinline__ f32x2 f2fma(f32x2 a, f32x2 b, f32x2 c) {
+  f32x2 d;
+  asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(d) : "l"(a), "l"(b), "l"(c));
+  return d;
+}
+
 // Super-tile update T' = Q_k^T T Q_l on two lanes (h = 0, 1 of an adjacent
 // pair; the warp's lanes must all call it).  T is the 8x8 block of A on row
 // blocks (rb0, rb1) of pair k and column blocks (cb0, cb1) of pair l; qk, ql
@@ -466,11 +485,15 @@ __device__ __forceinline__ void superTileHalfMem(const Mem &mem, TileOf tileOf, 
                                                  const float4 *ql, int rb0, int rb1, int cb0,
                                                  int cb1, int h, bool valid) {
   const int cbh = h ? cb1 : cb0;
-  float u[8][4];
+  // u2[p][c] holds U rows 2p, 2p + 1 (lane-relative) of column c: the two
+  // FMAs of a row pair are one fma.rn.f32x2 with the rotation row's
+  // adjacent entries as one operand and the tile element broadcast
+  f32x2 u2[4][4];
 #pragma unroll
-  for (int a = 0; a < 8; ++a)
+  for (int p = 0; p < 4; ++p)
 #pragma unroll
-    for (int c = 0; c < 4; ++c) u[a][c] = 0.0f;
+    for (int c = 0; c < 4; ++c) u2[p][c] = f2zero();
+  const ulonglong2 *qk2 = reinterpret_cast<const ulonglong2 *>(qk);
 #pragma unroll
   for (int x = 0; x < 2; ++x) {
     float b4[4][4];
@@ -486,41 +509,59 @@ __device__ __forceinline__ void superTileHalfMem(const Mem &mem, TileOf tileOf, 
     }
 #pragma unroll
     for (int i = 0; i < 4; ++i) {
-      // u[a] holds U row (a + 4h) mod 8: lane h reads the two halves of the
+      // U row a holds row (a + 4h) mod 8: lane h reads the two halves of the
       // rotation row in its own order (same FMA chains, no selects)
-      const float4 first = qk[2 * (4 * x + i) + h], second = qk[2 * (4 * x + i) + 1 - h];
-      const float qr[8] = {first.x, first.y, first.z, first.w, second.x, second.y, second.z, second.w};
+      const ulonglong2 first = qk2[2 * (4 * x + i) + h], second = qk2[2 * (4 * x + i) + 1 - h];
+      const f32x2 qp[4] = {first.x, first.y, second.x, second.y};
 #pragma unroll
-      for (int a = 0; a < 8; ++a)
+      for (int c = 0; c < 4; ++c) {
+        const f32x2 bc = f2make(b4[i][c], b4[i][c]);
 #pragma unroll
-        for (int c = 0; c < 4; ++c) u[a][c] = fmaf(qr[a], b4[i][c], u[a][c]);
+        for (int p = 0; p < 4; ++p) u2[p][c] = f2fma(qp[p], bc, u2[p][c]);
+      }
     }
   }
-  // U rows 4h..4h+3 of this lane's half: own columns (u[0..3]) and the
-  // partner's columns for these rows (the partner sends its u[4..7]).
-  float ur[4][8];
+  // T' = U Q_l for U rows 4h..4h+3: columns 0..3 of those rows come from
+  // lane 0 of the pair and columns 4..7 from lane 1 (each lane keeps its own
+  // rows 0..3 of u2 and sends rows 4..7).  o2[r][q] holds T' row r of this
+  // lane's four, columns 2q, 2q + 1; the chain over U's columns runs 0..7
+  // as in the one-lane form, the second half kept until the first is done.
+  f32x2 o2[4][4];
 #pragma unroll
   for (int r = 0; r < 4; ++r)
 #pragma unroll
-    for (int c = 0; c < 4; ++c) {
-      const float mine = u[r][c];
-      const float got = __shfl_xor_sync(0xffffffffu, u[4 + r][c], 1);
-      ur[r][c] = h ? got : mine;
-      ur[r][4 + c] = h ? mine : got;
+    for (int q = 0; q < 4; ++q) o2[r][q] = f2zero();
+  const ulonglong2 *ql2 = reinterpret_cast<const ulonglong2 *>(ql);
+  float later[4][4];
+#pragma unroll
+  for (int c = 0; c < 4; ++c) {
+    float mine[4], send[4];
+    f2split(u2[0][c], mine[0], mine[1]);
+    f2split(u2[1][c], mine[2], mine[3]);
+    f2split(u2[2][c], send[0], send[1]);
+    f2split(u2[3][c], send[2], send[3]);
+    const ulonglong2 lo = ql2[2 * c], hi = ql2[2 * c + 1];
+    const f32x2 qp[4] = {lo.x, lo.y, hi.x, hi.y};
+#pragma unroll
+    for (int r = 0; r < 4; ++r) {
+      const float got = __shfl_xor_sync(0xffffffffu, send[r], 1);
+      const float now = h ? got : mine[r];
+      later[r][c] = h ? mine[r] : got;
+      const f32x2 ub = f2make(now, now);
+#pragma unroll
+      for (int q = 0; q < 4; ++q) o2[r][q] = f2fma(ub, qp[q], o2[r][q]);
     }
-  float o[4][8];
+  }
 #pragma unroll
-  for (int r = 0; r < 4; ++r)
+  for (int c = 0; c < 4; ++c) {
+    const ulonglong2 lo = ql2[2 * (4 + c)], hi = ql2[2 * (4 + c) + 1];
+    const f32x2 qp[4] = {lo.x, lo.y, hi.x, hi.y};
 #pragma unroll
-    for (int c = 0; c < 8; ++c) o[r][c] = 0.0f;
+    for (int r = 0; r < 4; ++r) {
+      const f32x2 ub = f2make(later[r][c], later[r][c]);
 #pragma unroll
-  for (int jj = 0; jj < 8; ++jj) {
-    const float4 lo = ql[2 * jj], hi = ql[2 * jj + 1];
-    const float qr[8] = {lo.x, lo.y, lo.z, lo.w, hi.x, hi.y, hi.z, hi.w};
-#pragma unroll
-    for (int r = 0; r < 4; ++r)
-#pragma unroll
-      for (int c = 0; c < 8; ++c) o[r][c] = fmaf(ur[r][jj], qr[c], o[r][c]);
+      for (int q = 0; q < 4; ++q) o2[r][q] = f2fma(ub, qp[q], o2[r][q]);
+    }
   }
   if (valid) {
     const int rbh = h ? rb1 : rb0;
@@ -528,9 +569,10 @@ __device__ __forceinline__ void superTileHalfMem(const Mem &mem, TileOf tileOf, 
     for (int y = 0; y < 2; ++y) {
       float b4[4][4];
 #pragma unroll
-      for (int r = 0; r < 4; ++r)
-#pragma unroll
-        for (int c = 0; c < 4; ++c) b4[r][c] = o[r][4 * y + c];
+      for (int r = 0; r < 4; ++r) {
+        f2split(o2[r][2 * y], b4[r][0], b4[r][1]);
+        f2split(o2[r][2 * y + 1], b4[r][2], b4[r][3]);
+      }
       bool tr;
       const int ti = tileOf(rbh, y ? cb1 : cb0, tr);
       storeTileAt(mem.base(ti), ti, tr, b4);
