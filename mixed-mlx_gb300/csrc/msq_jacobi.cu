@@ -209,6 +209,16 @@ jacobiSweepKernel(JacobiArgs args) {
     return;
   }
 
+  // The state after this sweep, written now (every thread took its snapshot
+  // before the reductions' barriers; nothing below reads the state), so the
+  // norms are not held in registers through the rounds.
+  if (threadIdx.x == 0) {
+    st.norm2 = norm2;
+    st.off_ratio = ratio;
+    st.sweeps = sweeps + 1;
+    st.done = 0;
+    st.logged[args.parity] = 1;
+  }
   float *log = args.log + args.log_offset[mi];
   const int items = ((P + 1) / 2) * (P + 1);
   // With one pivot per quad, a quad reads its pair of the next round from
@@ -320,13 +330,6 @@ jacobiSweepKernel(JacobiArgs args) {
     fenceSharedToAsync();
     __syncthreads();
     if (threadIdx.x == 0) bulkStoreTiles(gtiles, stiles, split * kTileF * sizeof(float));
-  }
-  if (threadIdx.x == 0) {
-    st.norm2 = norm2;
-    st.off_ratio = ratio;
-    st.sweeps = sweeps + 1;
-    st.done = 0;
-    st.logged[args.parity] = 1;
   }
 }
 

@@ -255,9 +255,10 @@ __device__ __forceinline__ bool jacobiAngle(float paa, float pbb, float pab, flo
   if (pab == 0.0f) return false;
   const float tau = __fdiv_rn(__fsub_rn(pbb, paa), __fmul_rn(2.0f, pab));
   const float root = __fsqrt_rn(__fadd_rn(__fmul_rn(tau, tau), 1.0f));
-  // 1 / x correctly rounded (__frcp_rn) is the IEEE quotient 1.0f / x
-  const float t = copysignf(__frcp_rn(__fadd_rn(fabsf(tau), root)), tau);
-  float cc0 = __frcp_rn(__fsqrt_rn(__fadd_rn(__fmul_rn(t, t), 1.0f)));
+  // the IEEE quotients 1 / x (the shorter of the two correctly rounded
+  // forms on this GPU: __fdiv_rn(1, x) ~51 cycles, __frcp_rn ~70)
+  const float t = copysignf(__fdiv_rn(1.0f, __fadd_rn(fabsf(tau), root)), tau);
+  float cc0 = __fdiv_rn(1.0f, __fsqrt_rn(__fadd_rn(__fmul_rn(t, t), 1.0f)));
   float ss0 = __fmul_rn(t, cc0);
   const float cc = __fmul_rn(cc0, cc0), cce = fmaf(cc0, cc0, -cc);
   const float ss = __fmul_rn(ss0, ss0), sse = fmaf(ss0, ss0, -ss);
@@ -277,10 +278,11 @@ __device__ __forceinline__ void rot2(float &x, float &y, float c, float s, bool 
 }
 
 // One group of 4 rotations on the quad.  ra / rb: this lane's rows a_t / b_t
-// (all 8 columns); qcol: the pivot's Q, column-major (column x at qcol[8x]).
+// (all 8 columns); q: rows 2t and 2t + 1 of the pivot's Q, which every lane
+// updates for all four rotations of the group (Q <- Q J touches columns a, b
+// of each row; the group's pairs are disjoint, so their order is free).
 template <int G>
-__device__ __forceinline__ void pivotGroup(float (&ra)[8], float (&rb)[8], float *qcol, int t,
-                                           bool active) {
+__device__ __forceinline__ void pivotGroup(float (&ra)[8], float (&rb)[8], float (&q)[2][8], int t) {
   constexpr uint32_t W = groupWord(G);
   const int a = (W >> (6 * t)) & 7, b = (W >> (6 * t + 3)) & 7;
   float c, s;
@@ -317,18 +319,9 @@ __device__ __forceinline__ void pivotGroup(float (&ra)[8], float (&rb)[8], float
     const float y01 = swap ? x10 : x01, y10 = swap ? x01 : x10;
     ra[B] = diag ? 0.0f : y01;
     rb[A] = diag ? 0.0f : y10;
+    rot2(q[0][A], q[0][B], cj[j], sj[j], onj[j]);
+    rot2(q[1][A], q[1][B], cj[j], sj[j], onj[j]);
   }
-  if (active && on) {
-    float4 *ca = reinterpret_cast<float4 *>(qcol + 8 * a);
-    float4 *cb = reinterpret_cast<float4 *>(qcol + 8 * b);
-    float4 x0 = ca[0], x1 = ca[1], y0 = cb[0], y1 = cb[1];
-    rot2(x0.x, y0.x, c, s, true); rot2(x0.y, y0.y, c, s, true);
-    rot2(x0.z, y0.z, c, s, true); rot2(x0.w, y0.w, c, s, true);
-    rot2(x1.x, y1.x, c, s, true); rot2(x1.y, y1.y, c, s, true);
-    rot2(x1.z, y1.z, c, s, true); rot2(x1.w, y1.w, c, s, true);
-    ca[0] = x0; ca[1] = x1; cb[0] = y0; cb[1] = y1;
-  }
-  __syncwarp();
 }
 
 // Moves the rows from the ownership of group G to that of group G + 1.
@@ -355,41 +348,28 @@ __device__ __forceinline__ void pivotExchange(float (&ra)[8], float (&rb)[8], in
   }
 }
 
-// Full pivot sweep on the quad; on return ra / rb hold rows (t, 4 + t) and
-// qcol holds Q row-major.
-__device__ __forceinline__ void pivotSweep(float (&ra)[8], float (&rb)[8], float *qcol, int t,
+// Full pivot sweep on the quad; on return ra / rb hold rows (t, 4 + t) and,
+// if active, qrow holds Q row-major (lane t writes rows 2t and 2t + 1).
+__device__ __forceinline__ void pivotSweep(float (&ra)[8], float (&rb)[8], float *qrow, int t,
                                            bool active) {
-  if (active) {
-    // Q = I, column-major: lane t writes columns 2t and 2t + 1.
-    float4 *q4 = reinterpret_cast<float4 *>(qcol);
+  float q[2][8];
 #pragma unroll
-    for (int x = 0; x < 2; ++x) {
-      const int col = 2 * t + x;
-      q4[2 * col] = make_float4(col == 0, col == 1, col == 2, col == 3);
-      q4[2 * col + 1] = make_float4(col == 4, col == 5, col == 6, col == 7);
-    }
-  }
-  __syncwarp();
-  pivotGroup<0>(ra, rb, qcol, t, active); pivotExchange<0>(ra, rb, t);
-  pivotGroup<1>(ra, rb, qcol, t, active); pivotExchange<1>(ra, rb, t);
-  pivotGroup<2>(ra, rb, qcol, t, active); pivotExchange<2>(ra, rb, t);
-  pivotGroup<3>(ra, rb, qcol, t, active); pivotExchange<3>(ra, rb, t);
-  pivotGroup<4>(ra, rb, qcol, t, active); pivotExchange<4>(ra, rb, t);
-  pivotGroup<5>(ra, rb, qcol, t, active); pivotExchange<5>(ra, rb, t);
-  pivotGroup<6>(ra, rb, qcol, t, active); pivotExchange<6>(ra, rb, t);
-  // Q column-major -> row-major in place: lane t gathers rows 2t, 2t + 1.
-  float2 r2[8];
-  if (active) {
+  for (int x = 0; x < 2; ++x)
 #pragma unroll
-    for (int col = 0; col < 8; ++col) r2[col] = reinterpret_cast<const float2 *>(qcol + 8 * col)[t];
-  }
-  __syncwarp();
+    for (int y = 0; y < 8; ++y) q[x][y] = y == 2 * t + x ? 1.0f : 0.0f;
+  pivotGroup<0>(ra, rb, q, t); pivotExchange<0>(ra, rb, t);
+  pivotGroup<1>(ra, rb, q, t); pivotExchange<1>(ra, rb, t);
+  pivotGroup<2>(ra, rb, q, t); pivotExchange<2>(ra, rb, t);
+  pivotGroup<3>(ra, rb, q, t); pivotExchange<3>(ra, rb, t);
+  pivotGroup<4>(ra, rb, q, t); pivotExchange<4>(ra, rb, t);
+  pivotGroup<5>(ra, rb, q, t); pivotExchange<5>(ra, rb, t);
+  pivotGroup<6>(ra, rb, q, t); pivotExchange<6>(ra, rb, t);
   if (active) {
-    float4 *q4 = reinterpret_cast<float4 *>(qcol);
-    q4[4 * t + 0] = make_float4(r2[0].x, r2[1].x, r2[2].x, r2[3].x);
-    q4[4 * t + 1] = make_float4(r2[4].x, r2[5].x, r2[6].x, r2[7].x);
-    q4[4 * t + 2] = make_float4(r2[0].y, r2[1].y, r2[2].y, r2[3].y);
-    q4[4 * t + 3] = make_float4(r2[4].y, r2[5].y, r2[6].y, r2[7].y);
+    float4 *q4 = reinterpret_cast<float4 *>(qrow);
+    q4[4 * t + 0] = make_float4(q[0][0], q[0][1], q[0][2], q[0][3]);
+    q4[4 * t + 1] = make_float4(q[0][4], q[0][5], q[0][6], q[0][7]);
+    q4[4 * t + 2] = make_float4(q[1][0], q[1][1], q[1][2], q[1][3]);
+    q4[4 * t + 3] = make_float4(q[1][4], q[1][5], q[1][6], q[1][7]);
   }
 }
 
