@@ -120,6 +120,7 @@ int checkDeviceStatus(msq_ctx *ctx) {
     const char *why = status == kStatusMbarrierTimeout   ? "bounded mbarrier wait expired"
                       : status == kStatusTmemAllocFailed ? "TMEM allocation failed"
                       : status == kStatusBadOrder        ? "matrix order outside kernel limits"
+                      : status == kStatusFlagTimeout     ? "bounded shared-memory flag wait expired"
                                                          : "kernel reported an error";
     return setError(ctx, MSQ_ERR_DEVICE_STATUS,
                     std::string("device status ") + std::to_string(status) + ": " + why);

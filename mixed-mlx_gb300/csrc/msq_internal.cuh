@@ -24,6 +24,7 @@ enum DeviceStatus : int {
   kStatusMbarrierTimeout = 2,
   kStatusTmemAllocFailed = 3,
   kStatusBadOrder = 4,
+  kStatusFlagTimeout = 5,
 };
 
 struct WorkList {

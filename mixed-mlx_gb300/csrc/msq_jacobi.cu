@@ -20,7 +20,7 @@
 //    pair of small dense products held in registers (1024 FMA per 64
 //    elements), so a round is FMA-bound instead of latency-bound;
 //  * the upper triangle of A is stored as packed 4x4 tiles, in shared memory
-//    when it fits (n <= 328) and in an L2-resident global workspace beyond;
+//    when it fits (n <= 320) and in an L2-resident global workspace beyond;
 //  * each round's Q_k are logged and a row-parallel kernel replays the sweep
 //    onto V (rows of V evolve independently under V <- V Q), so V never
 //    competes with A for shared memory;
@@ -87,15 +87,37 @@ __device__ __forceinline__ SplitTiles tileMem(std::false_type, float *s, float *
   return SplitTiles{s, g, split};
 }
 
-// Shared memory of the sweep kernel: reduction scratch, pair tables, the
-// round's rotations, then the packed tiles (with_tiles).
+// Entries (16-bit) of one round table of the sweep kernel: pairs (I, J),
+// rotate flags, per block its pair and its partner (-1: not rotated).
+__host__ __device__ __forceinline__ int roundTableShorts(int nb) { return 3 * (nb / 2) + 2 * nb; }
+
+// One round's table in shared memory and its P 8x8 rotations (kQS floats
+// apart).
+struct RoundTable {
+  short *t;
+  float *q;
+  int P;
+  __device__ short &pi(int k) const { return t[k]; }
+  __device__ short &pj(int k) const { return t[P + k]; }
+  __device__ short &on(int k) const { return t[2 * P + k]; }
+  __device__ short &slot(int b) const { return t[3 * P + b]; }
+  __device__ short &partner(int b) const { return t[5 * P + b]; }
+};
+
+// Polls of a done flag before the sweep kernel reports kStatusFlagTimeout.
+constexpr int kFlagWaitLimit = 1 << 22;
+
+// Shared memory of the sweep kernel: reduction scratch; the tile table, two
+// work counters, P done flags and three round tables; the rotations of two
+// rounds; then the packed tiles (with_tiles).
 __host__ __device__ __forceinline__ size_t sweepSmemLayout(int n, bool with_tiles, size_t *q_off,
                                                            size_t *tile_off) {
   const int m = padded8(n), nb = m / 4, P = nb / 2;
-  size_t bytes = 32 * sizeof(double) + (nb + 1 + 2 * P) * sizeof(int);
+  size_t bytes = 32 * sizeof(double) + (nb + 1 + 2 + P) * sizeof(int) +
+                 3 * roundTableShorts(nb) * sizeof(short);
   bytes = (bytes + 15) & ~static_cast<size_t>(15);
   *q_off = bytes;
-  bytes += static_cast<size_t>(P) * kQS * sizeof(float);
+  bytes += 2 * static_cast<size_t>(P) * kQS * sizeof(float);
   *tile_off = bytes;
   if (with_tiles) bytes += static_cast<size_t>(nb) * (nb + 1) / 2 * kTileF * sizeof(float);
   return bytes;
@@ -122,8 +144,9 @@ jacobiSweepKernel(JacobiArgs args) {
   sweepSmemLayout(n, kSmem, &q_off, &tile_off);
   double *red = reinterpret_cast<double *>(smem_raw);
   int *tri = reinterpret_cast<int *>(red + 32);
-  int *pair_i = tri + nb + 1;
-  int *pair_j = pair_i + P;
+  int *counters = tri + nb + 1;
+  int *flags = counters + 2;
+  short *tables = reinterpret_cast<short *>(flags + P);
   float *qs = reinterpret_cast<float *>(smem_raw + q_off);
   float *gtiles = args.tiles + args.t_offset[mi];
   float *stiles = reinterpret_cast<float *>(smem_raw + tile_off);
@@ -221,108 +244,198 @@ jacobiSweepKernel(JacobiArgs args) {
   }
   float *log = args.log + args.log_offset[mi];
   const int items = ((P + 1) / 2) * (P + 1);
-  // With one pivot per quad, a quad reads its pair of the next round from
-  // the two-level table while the current round runs.
-  const int quads = blockDim.x >> 2, t4 = threadIdx.x & 3;
-  const bool prefetch = sched != nullptr && P <= quads;
-  int2 next_pair = make_int2(0, 0);
-  if (prefetch && (threadIdx.x >> 2) < P) next_pair = sched[threadIdx.x >> 2];
-  for (int round = 0; round < rounds; ++round) {
-    // Pivots: a quad of lanes per block pair.  The loop is warp-uniform (all
-    // lanes of a warp take part in the quad shuffles; lanes past P idle).
-    // An identity pair of the two-level table keeps its blocks and logs Q = I.
-    for (int base = 0; base < P; base += quads) {
-      const int k = base + (threadIdx.x >> 2);
-      const bool present = k < P;
-      bool active = present;
-      float ra[8], rb[8];
-      int tII = 0, tIJ = 0, tJJ = 0, I = 0, J = 0;
-      if (present) {
-        if (prefetch) {
-          I = next_pair.x;
-          active = next_pair.y >= 0;
-          J = active ? next_pair.y : -1 - next_pair.y;
-          if (round + 1 < rounds) next_pair = sched[(round + 1) * P + k];
-        } else {
-          roundPair(sched, k, round, nb, I, J, active);
-        }
-        if (t4 == 0) {
-          pair_i[k] = I;
-          pair_j[k] = J;
-        }
-      }
-      if (active) {
-        tII = tileIndex(tri, I, I);
-        tIJ = tileIndex(tri, I, J);
-        tJJ = tileIndex(tri, J, J);
-        // lane t starts with rows t (block I) and 7 - t (block J row 3 - t;
-        // its left half is the mirror of tile (I, J))
-        const float4 *sII = reinterpret_cast<const float4 *>(tiles.base(tII));
-        const float4 *sIJ = reinterpret_cast<const float4 *>(tiles.base(tIJ));
-        const float4 *sJJ = reinterpret_cast<const float4 *>(tiles.base(tJJ));
-        const int jr = 3 - t4;
-        const float4 v0 = sII[t4 ^ (tII & 3)], v1 = sIJ[t4 ^ (tIJ & 3)], v2 = sJJ[jr ^ (tJJ & 3)];
-        ra[0] = v0.x; ra[1] = v0.y; ra[2] = v0.z; ra[3] = v0.w;
-        ra[4] = v1.x; ra[5] = v1.y; ra[6] = v1.z; ra[7] = v1.w;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, warps = blockDim.x >> 5;
+  // round r's table is buffer r % 3, its rotations buffer r & 1
+  auto table = [&](int r) {
+    return RoundTable{tables + (r % 3) * roundTableShorts(nb), qs + (r & 1) * P * kQS, P};
+  };
+
+  // Pairs of round r into its table (threads [first, blockDim) take part).
+  auto stagePairs = [&](int r, int first) {
+    const RoundTable t = table(r);
+    for (int k = threadIdx.x - first; k < P; k += blockDim.x - first) {
+      int I, J;
+      bool on;
+      roundPair(sched, k, r, nb, I, J, on);
+      t.pi(k) = static_cast<short>(I);
+      t.pj(k) = static_cast<short>(J);
+      t.on(k) = static_cast<short>(on);
+      t.slot(I) = static_cast<short>(k);
+      t.slot(J) = static_cast<short>(k);
+      t.partner(I) = static_cast<short>(on ? J : -1);
+      t.partner(J) = static_cast<short>(on ? I : -1);
+    }
+  };
+
+  // Pivots of a round: a quad of lanes per block pair, eight pairs per warp,
+  // warps [0, pw) of the CTA.  The loop is warp-uniform (all lanes of a warp
+  // take part in the quad shuffles; lanes past P idle).  An identity pair
+  // keeps its blocks and logs Q = I.
+  auto pivot = [&](const RoundTable &t, int k) {
+    const int t4 = lane & 3;
+    const bool present = k < P;
+    const bool active = present && t.on(k);
+    float ra[8], rb[8];
+    int tII = 0, tIJ = 0, tJJ = 0;
+    if (active) {
+      const int I = t.pi(k), J = t.pj(k);
+      tII = tileIndex(tri, I, I);
+      tIJ = tileIndex(tri, I, J);
+      tJJ = tileIndex(tri, J, J);
+      // lane t starts with rows t (block I) and 7 - t (block J row 3 - t;
+      // its left half is the mirror of tile (I, J))
+      const float4 *sII = reinterpret_cast<const float4 *>(tiles.base(tII));
+      const float4 *sIJ = reinterpret_cast<const float4 *>(tiles.base(tIJ));
+      const float4 *sJJ = reinterpret_cast<const float4 *>(tiles.base(tJJ));
+      const int jr = 3 - t4;
+      const float4 v0 = sII[t4 ^ (tII & 3)], v1 = sIJ[t4 ^ (tIJ & 3)], v2 = sJJ[jr ^ (tJJ & 3)];
+      ra[0] = v0.x; ra[1] = v0.y; ra[2] = v0.z; ra[3] = v0.w;
+      ra[4] = v1.x; ra[5] = v1.y; ra[6] = v1.z; ra[7] = v1.w;
 #pragma unroll
-        for (int i = 0; i < 4; ++i) rb[i] = tileAt(tiles, tileElement(tIJ, i, jr));
-        rb[4] = v2.x; rb[5] = v2.y; rb[6] = v2.z; rb[7] = v2.w;
-      } else {
+      for (int i = 0; i < 4; ++i) rb[i] = tileAt(tiles, tileElement(tIJ, i, jr));
+      rb[4] = v2.x; rb[5] = v2.y; rb[6] = v2.z; rb[7] = v2.w;
+    } else {
 #pragma unroll
-        for (int y = 0; y < 8; ++y) ra[y] = rb[y] = 0.0f;
-      }
-      pivotSweep(ra, rb, qs + (active ? k : 0) * kQS, t4, active);
-      if (active) {
-        // rows t (tiles (I, I), (I, J)) and 4 + t (tile (J, J)); the lower
-        // left block is the mirror of tile (I, J) and is not stored
-        float4 *sII = reinterpret_cast<float4 *>(tiles.base(tII));
-        float4 *sIJ = reinterpret_cast<float4 *>(tiles.base(tIJ));
-        float4 *sJJ = reinterpret_cast<float4 *>(tiles.base(tJJ));
-        sII[t4 ^ (tII & 3)] = make_float4(ra[0], ra[1], ra[2], ra[3]);
-        sIJ[t4 ^ (tIJ & 3)] = make_float4(ra[4], ra[5], ra[6], ra[7]);
-        sJJ[t4 ^ (tJJ & 3)] = make_float4(rb[4], rb[5], rb[6], rb[7]);
-      } else if (present) {
-        // identity pair: Q = I (lane t writes rows 2t and 2t + 1)
-        float4 *q4 = reinterpret_cast<float4 *>(qs + k * kQS);
+      for (int y = 0; y < 8; ++y) ra[y] = rb[y] = 0.0f;
+    }
+    pivotSweep(ra, rb, t.q + (active ? k : 0) * kQS, t4, active);
+    if (active) {
+      // rows t (tiles (I, I), (I, J)) and 4 + t (tile (J, J)); the lower
+      // left block is the mirror of tile (I, J) and is not stored
+      float4 *sII = reinterpret_cast<float4 *>(tiles.base(tII));
+      float4 *sIJ = reinterpret_cast<float4 *>(tiles.base(tIJ));
+      float4 *sJJ = reinterpret_cast<float4 *>(tiles.base(tJJ));
+      sII[t4 ^ (tII & 3)] = make_float4(ra[0], ra[1], ra[2], ra[3]);
+      sIJ[t4 ^ (tIJ & 3)] = make_float4(ra[4], ra[5], ra[6], ra[7]);
+      sJJ[t4 ^ (tJJ & 3)] = make_float4(rb[4], rb[5], rb[6], rb[7]);
+    } else if (present) {
+      // identity pair: Q = I (lane t writes rows 2t and 2t + 1)
+      float4 *q4 = reinterpret_cast<float4 *>(t.q + k * kQS);
 #pragma unroll
-        for (int x = 0; x < 2; ++x) {
-          const int row = 2 * t4 + x;
-          q4[2 * row] = make_float4(row == 0, row == 1, row == 2, row == 3);
-          q4[2 * row + 1] = make_float4(row == 4, row == 5, row == 6, row == 7);
-        }
+      for (int x = 0; x < 2; ++x) {
+        const int row = 2 * t4 + x;
+        q4[2 * row] = make_float4(row == 0, row == 1, row == 2, row == 3);
+        q4[2 * row + 1] = make_float4(row == 4, row == 5, row == 6, row == 7);
       }
     }
-    __syncthreads();
-    {
+  };
+
+  // Off-pivot super-tiles: T' = Q_k^T T Q_l for pairs k < l of a round, two
+  // lanes per super-tile (warp-uniform: the pair shuffle has all lanes).
+  auto superTile = [&](const RoundTable &t, int k, int l, int h, bool valid) {
+    superTileHalfMem(tiles, SharedTri{tri}, reinterpret_cast<const float4 *>(t.q + k * kQS),
+                     reinterpret_cast<const float4 *>(t.q + l * kQS), t.pi(k), t.pj(k), t.pi(l),
+                     t.pj(l), h, valid);
+  };
+  // The super-tile (k, l) of round `cur` holding the tile (x, y) that pivot
+  // kk of round `nxt` reads (none when cur paired x and y: its pivot wrote
+  // that tile).  Two pairs of nxt can meet the same super-tile; the one
+  // holding the smaller block computes it (*owner = kk) and the other waits
+  // for it (*owner = that pair).  Returns whether kk needs a super-tile.
+  auto criticalItem = [&](const RoundTable &cur, const RoundTable &nxt, int kk, int &k, int &l,
+                          int &owner) {
+    owner = kk;
+    if (kk >= P || !nxt.on(kk)) return false;
+    const int x = nxt.pi(kk), y = nxt.pj(kk);
+    k = cur.slot(x);
+    l = cur.slot(y);
+    if (k == l) return false;
+    const int ox = cur.pi(k) + cur.pj(k) - x, oy = cur.pi(l) + cur.pj(l) - y;
+    if (nxt.partner(ox) == oy && min(ox, oy) < min(x, y)) owner = nxt.slot(ox);
+    if (k > l) {
+      const int s = k;
+      k = l;
+      l = s;
+    }
+    return true;
+  };
+  // Whether super-tile (k, l) of cur is one of those.
+  auto isCritical = [&](const RoundTable &cur, const RoundTable &nxt, int k, int l) {
+    const int p1 = nxt.partner(cur.pi(k)), p2 = nxt.partner(cur.pj(k));
+    return (p1 >= 0 && cur.slot(p1) == l) || (p2 >= 0 && cur.slot(p2) == l);
+  };
+  // The other super-tiles of cur (all of them without a next round), taken
+  // by warps 32 lanes (16 super-tiles) at a time from a shared counter.
+  auto otherItems = [&](const RoundTable &cur, const RoundTable &nxt, bool more, int *counter) {
+    for (;;) {
+      int base = 0;
+      if (lane == 0) base = atomicAdd(counter, 32);
+      base = __shfl_sync(0xffffffffu, base, 0);
+      if (base >= 2 * items) break;
+      const int w2 = base + lane;
+      int k = 0, l = 0;
+      bool valid = w2 < 2 * items && foldedBlock(w2 >> 1, P, k, l) && k != l;
+      if (valid && more && isCritical(cur, nxt, k, l)) valid = false;
+      if (!valid) k = l = 0;
+      superTile(cur, k, l, w2 & 1, valid);
+    }
+  };
+
+  // Round r+1's pivots need only round r's pivots and, of r's super-tiles,
+  // the one holding each pivot's cross tile.  So while the CTA updates
+  // round r's other super-tiles, warps [0, pw) compute those super-tiles
+  // (two lanes of each pivot's quad) and run round r+1's pivots: one barrier
+  // per round.  Every tile sees the same operations in the same order as in
+  // the plain round order (pivots, then all super-tiles, round by round).
+  const int pw = min(warps, (P + 7) / 8);
+  const int stage_first = pw < warps ? 32 * pw : 0;  // threads that stage tables and log
+  stagePairs(0, 0);
+  if (rounds > 1) stagePairs(1, 0);
+  if (threadIdx.x == 0) counters[0] = counters[1] = 0;
+  for (int k = threadIdx.x; k < P; k += blockDim.x) flags[k] = 0;
+  __syncthreads();
+  for (int base = 8 * warp; base < P; base += 8 * warps) pivot(table(0), base + (lane >> 2));
+  __syncthreads();
+  for (int round = 0; round < rounds; ++round) {
+    const RoundTable cur = table(round), nxt = table(round + 1);
+    const bool more = round + 1 < rounds;
+    const bool pivot_warp = more && warp < pw;
+    if (pivot_warp) {
+      // round r's super-tiles under round r+1's pivots (all of this warp's
+      // first, then their done flags, so no warp waits before it has set its own)
+      for (int base = 8 * warp; base < P; base += 8 * pw) {
+        const int kk = base + (lane >> 2);
+        int k = 0, l = 0, owner = kk;
+        const bool own = (lane & 2) == 0 && criticalItem(cur, nxt, kk, k, l, owner) && owner == kk;
+        if (!own) k = l = 0;
+        superTile(cur, k, l, lane & 1, own);
+        __syncwarp();
+        if (own && (lane & 3) == 0) {
+          __threadfence_block();
+          atomicExch(&flags[kk], round + 1);
+        }
+      }
+      for (int base = 8 * warp; base < P; base += 8 * pw) {
+        const int kk = base + (lane >> 2);
+        int k = 0, l = 0, owner = kk;
+        const bool wait = criticalItem(cur, nxt, kk, k, l, owner) && owner != kk;
+        if (wait && (lane & 3) == 0) {
+          // bounded: on expiry the launch reports and goes on
+          int spins = 0;
+          while (atomicAdd(&flags[owner], 0) != round + 1) {
+            if (++spins > kFlagWaitLimit) {
+              atomicExch(args.status, kStatusFlagTimeout);
+              break;
+            }
+            __nanosleep(32);
+          }
+          __threadfence_block();
+        }
+        __syncwarp();
+        pivot(nxt, kk);
+      }
+    }
+    if (static_cast<int>(threadIdx.x) >= stage_first) {
+      if (round + 2 < rounds) stagePairs(round + 2, stage_first);
+      if (threadIdx.x == stage_first) counters[(round + 1) & 1] = 0;
       // this round's rotations, logged for the V replay (coalesced copy)
-      const float4 *src = reinterpret_cast<const float4 *>(qs);
+      const float4 *src = reinterpret_cast<const float4 *>(cur.q);
       float4 *dst = reinterpret_cast<float4 *>(log + static_cast<int64_t>(round) * P * kQF);
-      for (int x = threadIdx.x; x < P * kQF / 4; x += blockDim.x) {
+      for (int x = threadIdx.x - stage_first; x < P * kQF / 4; x += blockDim.x - stage_first) {
         dst[x] = src[(x >> 4) * (kQS / 4) + (x & 15)];
       }
     }
-    // Off-pivot super-tiles: T' = Q_k^T T Q_l for every k < l, two lanes per
-    // super-tile.  Lane h forms U[:, 4h:4h+4] = Q_k^T T[:, 4h:4h+4] from the
-    // two 4x4 blocks of column block h, the pair swaps the halves of U each
-    // needs, and lane h forms rows 4h..4h+3 of T' = U Q_l.  Every element is
-    // the same ordered FMA chain as in one-lane form (u over i, t' over j).
-    // The loop is warp-uniform so the pair shuffle has all lanes present.
-    auto itemAt = [&](int base, int &k, int &l, int &h) {
-      const int w2 = base + (threadIdx.x & 31);
-      h = w2 & 1;
-      k = l = 0;
-      const bool valid = w2 < 2 * items && foldedBlock(w2 >> 1, P, k, l) && k != l;
-      if (!valid) k = l = 0;
-      return valid;
-    };
-    for (int base = threadIdx.x & ~31; base < 2 * items; base += blockDim.x) {
-      int k, l, h;
-      const bool valid = itemAt(base, k, l, h);
-      const float4 *qk = reinterpret_cast<const float4 *>(qs + k * kQS);
-      const float4 *ql = reinterpret_cast<const float4 *>(qs + l * kQS);
-      superTileHalfMem(tiles, SharedTri{tri}, qk, ql, pair_i[k], pair_j[k], pair_i[l], pair_j[l], h,
-                       valid);
-    }
+    otherItems(cur, nxt, more, counters + (round & 1));
     __syncthreads();
   }
   if (split > 0) {
@@ -530,7 +643,8 @@ int replayRows(int max_n) {
 // so the tuner times them on live work: while a class is untuned, sweep
 // launches 1..C of a call (full sweeps: every class needs more) each use the
 // next candidate, bracketed by timing events; a later call reads the events
-// and, once every candidate has a time, keeps the fastest for that device.
+// and, once every candidate has kTuneSamples times (from as many calls),
+// keeps the fastest for that device.
 // The decisions are process-wide, like a benchmark cache, and
 // msq_autotune_report prints them.
 constexpr int kClasses = 9;
@@ -549,8 +663,8 @@ int sizeClass(int n) {
 
 const char *className(int c) {
   static const char *names[kClasses] = {"n<=16", "16<n<=32", "32<n<=64", "64<n<=128",
-                                        "128<n<=256", "256<n<=328 (shared tiles)",
-                                        "328<n<=512 (global tiles)", "512<n<=1024", "1024<n<=2048"};
+                                        "128<n<=256", "256<n<=320 (shared tiles)",
+                                        "320<n<=512 (global tiles)", "512<n<=1024", "1024<n<=2048"};
   return names[c];
 }
 
@@ -574,14 +688,20 @@ std::vector<int> classCandidates(int c) {
 const char *sweepName(int c) {
   static const char *names[kClasses] = {
       "jacobi sweep n<=16", "jacobi sweep n<=32", "jacobi sweep n<=64", "jacobi sweep n<=128",
-      "jacobi sweep n<=256", "jacobi sweep n<=328", "jacobi sweep n<=512 (global)",
+      "jacobi sweep n<=256", "jacobi sweep n<=320", "jacobi sweep n<=512 (global)",
       "jacobi sweep n<=1024 (global)", "jacobi sweep n<=2048 (global)"};
   return names[c];
 }
 
+// Timed launches per candidate before a class is decided (the fastest of
+// them counts: a single launch shares the GPU with the other buckets'
+// streams, and one sample can misorder candidates a few percent apart).
+constexpr int kTuneSamples = 2;
+
 struct ClassTune {
   std::vector<int> cands;
-  std::vector<double> ms;   // per candidate, < 0 until measured
+  std::vector<double> ms;   // per candidate: fastest sample, < 0 until measured
+  std::vector<int> samples; // per candidate: timed launches so far
   int best = -1;            // index into cands once tuned
   bool requested = false;   // a call is measuring this class
 };
@@ -604,6 +724,7 @@ std::array<ClassTune, kClasses> &tuneFor(int device) {
     for (int c = 0; c < kClasses; ++c) {
       t[c].cands = classCandidates(c);
       t[c].ms.assign(t[c].cands.size(), -1.0);
+      t[c].samples.assign(t[c].cands.size(), 0);
       if (t[c].cands.size() == 1) t[c].best = 0;
     }
     it = g_tune.emplace(device, t).first;
@@ -628,8 +749,9 @@ void harvestTimings() {
     if (ms > 0.0f && t.best < 0) {
       const double per = ms / std::max(p.matrices, 1);
       if (t.ms[p.cand] < 0.0 || per < t.ms[p.cand]) t.ms[p.cand] = per;
+      ++t.samples[p.cand];
       bool all = true;
-      for (double v : t.ms) all = all && v > 0.0;
+      for (int v : t.samples) all = all && v >= kTuneSamples;
       if (all) {
         t.best = static_cast<int>(std::min_element(t.ms.begin(), t.ms.end()) - t.ms.begin());
       }

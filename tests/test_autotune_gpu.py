@@ -34,7 +34,7 @@ def test_tuning_keeps_results_bit_identical(ctx, msq):
     lines = [l for l in report.splitlines() if l]
     assert len(lines) == 9
     tuned = [l for l in lines if "untuned" not in l]
-    # every class present in the batch (classes n <= 16 .. n <= 328) is tuned
+    # every class present in the batch (classes n <= 16 .. n <= 320) is tuned
     assert len(tuned) >= 6, report
 
 
