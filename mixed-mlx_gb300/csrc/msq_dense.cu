@@ -16,6 +16,7 @@
 // covers an uneven batch.
 #include "msq_dense.cuh"
 #include "msq_internal.cuh"
+#include "msq_f32x2.cuh"
 
 #include <algorithm>
 #include <vector>
@@ -139,7 +140,13 @@ residualFFKernel(ResidualArgs args) {
     const int64_t off = args.offset[mi];
     const float *Xh = args.x_hi + off;
     const float *Xl = args.x_lo ? args.x_lo + off : nullptr;
-    float s[4][4] = {}, comp[4][4] = {};
+    // accumulators in pairs of adjacent columns: s (leading part) and comp
+    // (low-order terms), two outputs per packed FP32 instruction
+    f32x2 s2[4][2], comp2[4][2];
+#pragma unroll
+    for (int r = 0; r < 4; ++r)
+#pragma unroll
+      for (int q = 0; q < 2; ++q) s2[r][q] = comp2[r][q] = f2zero();
     for (int k0 = 0; k0 < n; k0 += kBK) {
 #pragma unroll
       for (int e = 0; e < 4; ++e) {
@@ -156,29 +163,41 @@ residualFFKernel(ResidualArgs args) {
       __syncthreads();
 #pragma unroll 4
       for (int kk = 0; kk < kBK; ++kk) {
-        float ah[4], al[4], bh[4], bl[4];
+        const float4 ah4 = *reinterpret_cast<const float4 *>(&Hs[kk][ty * 4]);
+        const float4 al4 = *reinterpret_cast<const float4 *>(&Ls[kk][ty * 4]);
+        const ulonglong2 bh2 = *reinterpret_cast<const ulonglong2 *>(&Hb[kk][tx * 4]);
+        const ulonglong2 bl2 = *reinterpret_cast<const ulonglong2 *>(&Lb[kk][tx * 4]);
+        const float ah[4] = {ah4.x, ah4.y, ah4.z, ah4.w}, al[4] = {al4.x, al4.y, al4.z, al4.w};
+        const f32x2 bh[2] = {bh2.x, bh2.y}, bl[2] = {bl2.x, bl2.y};
 #pragma unroll
-        for (int q = 0; q < 4; ++q) {
-          ah[q] = Hs[kk][ty * 4 + q];
-          al[q] = Ls[kk][ty * 4 + q];
-          bh[q] = Hb[kk][tx * 4 + q];
-          bl[q] = Lb[kk][tx * 4 + q];
-        }
+        for (int r = 0; r < 4; ++r) {
+          const f32x2 a2 = f2make(ah[r], ah[r]), na2 = f2make(-ah[r], -ah[r]);
+          const f32x2 l2 = f2make(al[r], al[r]);
 #pragma unroll
-        for (int r = 0; r < 4; ++r)
-#pragma unroll
-          for (int c = 0; c < 4; ++c) {
-            const float p = ah[r] * bh[c];
-            const float pe = fmaf(ah[r], bh[c], -p);
-            const float t = s[r][c] + p;
-            const float z = t - s[r][c];
-            const float se = (s[r][c] - (t - z)) + (p - z);
-            s[r][c] = t;
-            comp[r][c] += se + pe + fmaf(ah[r], bl[c], al[r] * bh[c]);
+          for (int q = 0; q < 2; ++q) {
+            // p = a b (carried negated: m = -p, exact), its error e = a b - p,
+            // the two-sum t + se = s + p, and the low-order terms into comp
+            const f32x2 m = f2mul(na2, bh[q]);
+            const f32x2 pe = f2fma(a2, bh[q], m);
+            const f32x2 t = f2sub(s2[r][q], m);
+            const f32x2 z = f2sub(t, s2[r][q]);
+            const f32x2 se = f2sub(f2sub(s2[r][q], f2sub(t, z)), f2add(m, z));
+            s2[r][q] = t;
+            const f32x2 cross = f2fma(a2, bl[q], f2mul(l2, bh[q]));
+            comp2[r][q] = f2add(comp2[r][q], f2add(f2add(se, pe), cross));
           }
+        }
       }
       __syncthreads();
     }
+    float s[4][4], comp[4][4];
+#pragma unroll
+    for (int r = 0; r < 4; ++r)
+#pragma unroll
+      for (int q = 0; q < 2; ++q) {
+        f2split(s2[r][q], s[r][2 * q], s[r][2 * q + 1]);
+        f2split(comp2[r][q], comp[r][2 * q], comp[r][2 * q + 1]);
+      }
     const float *A = args.a + off;
     const float *AL = args.a_lo ? args.a_lo + off : nullptr;
     float *R = args.r ? args.r + off : nullptr;

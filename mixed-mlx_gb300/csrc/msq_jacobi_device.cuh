@@ -9,6 +9,7 @@
 
 #include <cstdint>
 
+#include "msq_f32x2.cuh"
 #include "msq_tcgen05.cuh"
 
 namespace msq {
@@ -430,25 +431,6 @@ __device__ __forceinline__ void storeTileAt(float *p, int ti, bool transposed, c
     dst[i ^ (ti & 3)] = transposed ? make_float4(t[0][i], t[1][i], t[2][i], t[3][i])
                                    : make_float4(t[i][0], t[i][1], t[i][2], t[i][3]);
   }
-}
-
-// Two FP32 values in one 64-bit register (low half first, as in memory).
-// fma.rn.f32x2 performs two IEEE fused multiply-adds: the bits of two fmaf
-// calls, issued as one instruction.
-typedef unsigned long long f32x2;
-__device__ __forceinline__ f32x2 f2zero() { return 0ull; }
-__device__ __forceinline__ f32x2 f2make(float lo, float hi) {
-  f32x2 r;
-  asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(lo), "f"(hi));
-  return r;
-}
-__device__ __forceinline__ void f2split(f32x2 v, float &lo, float &hi) {
-  asm("mov.b64 {%0, %1}, %2;" : "=f"(lo), "=f"(hi) : "l"(v));
-}
-__device__ __forceinline__ f32x2 f2fma(f32x2 a, f32x2 b, f32x2 c) {
-  f32x2 d;
-  asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(d) : "l"(a), "l"(b), "l"(c));
-  return d;
 }
 
 // Super-tile update T' = Q_k^T T Q_l on two lanes (h = 0, 1 of an adjacent
