@@ -44,14 +44,20 @@ SWEEP_CLASS_NAMES = ["jacobi sweep n<=16", "jacobi sweep n<=32", "jacobi sweep n
                      "jacobi sweep n<=128", "jacobi sweep n<=256", "jacobi sweep n<=320",
                      "jacobi sweep n<=512 (global)", "jacobi sweep n<=1024 (global)",
                      "jacobi sweep n<=2048 (global)"]
+# DRAM bytes (read + write) per matrix-sweep of the global-tile sweep kernel,
+# 320 < n <= 512: ncu dram__bytes_read.sum + dram__bytes_write.sum of one
+# 67-matrix launch of `bench.py --count 512` (the roofline's `traffic`)
+GLOBAL_SWEEP_DRAM_PER_MATRIX_SWEEP = 80.5e6 / 67
 
 
 def _tiles_fit_shared(n: int) -> bool:
     """The sweep keeps the packed tiles in shared memory when they fit 227 KB."""
     m = (n + 7) // 8 * 8
     nb, p = m // 4, m // 8
-    head = (32 * 8 + (nb + 1 + 2 * p) * 4 + 15) // 16 * 16
-    return head + p * 68 * 4 + nb * (nb + 1) // 2 * 16 * 4 <= 227 * 1024 - 256
+    # reduction scratch, tile table, counters, done flags, three 16-bit round
+    # tables; two rotation buffers (68-float stride); the packed tiles
+    head = (32 * 8 + (nb + 1 + 2 + p) * 4 + 3 * (3 * p + 2 * nb) * 2 + 15) // 16 * 16
+    return head + 2 * p * 68 * 4 + nb * (nb + 1) // 2 * 16 * 4 <= 227 * 1024 - 256
 
 
 def sweep_class(n: int) -> int:
@@ -595,8 +601,15 @@ def main():
         per_launch = float(np.sum(2.0 * fma * sweeps)) * PROFILE_STEPS / max(cnt, 1)
         achieved = per_launch / (avg_ms / 1e3) / 1e12
         hbm_launch = float(np.sum(hbm_bytes * sweeps)) * PROFILE_STEPS / max(cnt, 1)
+        traffic = None
+        if name == SWEEP_CLASS_NAMES[6]:
+            # DRAM read + write per matrix-sweep of the global-tile class from
+            # one ncu capture (80.5 MB over a 67-matrix launch of the
+            # 512-matrix workload), times this launch's matrix-sweeps
+            msweeps = float(np.sum(sweeps * in_class)) * PROFILE_STEPS / max(cnt, 1)
+            traffic = GLOBAL_SWEEP_DRAM_PER_MATRIX_SWEEP * msweeps
         roof = {"bound": "fp32", "achieved": achieved, "peak": fp32_peak, "unit": "TFLOP/s",
-                "frac": achieved / fp32_peak, "traffic": None, "kernel": name,
+                "frac": achieved / fp32_peak, "traffic": traffic, "kernel": name,
                 "peak_source": "nominal FP32 FMA rate: 152 SMs x 128 lanes x 2 flop x %.0f MHz "
                                "(no FP32 figure among the measured peaks)" % sm_mhz,
                 "hbm_view": {"achieved": hbm_launch / (avg_ms / 1e3) / 1e9, "peak": hbm,
