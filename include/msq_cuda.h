@@ -104,6 +104,43 @@ int msq_decode(msq_ctx *ctx, int format, const uint8_t *values,
                const uint8_t *scales, size_t elements, size_t row_length,
                float *output);
 
+/* ---- stochastic rounding (--rounding stochastic) ---------------------------
+ * The reference's device quantizers for stochastic rounding
+ * (metal_mixed_sqrt.metal:394-405 hash; :462-484, :545-568, :740-763 FP8 /
+ * FP4 element rules; :1888-1907 BF16; MX :971-1000, :1113-1140, :1232-1260),
+ * which replace the host copyToStorage (src/storage_codecs.cpp:315-321)
+ * when the reference runs with --rounding stochastic --rounding-seed S:
+ * element i (flat index) between codes lo < |x| < hi rounds up with
+ * probability (|x| - lo) / (hi - lo) against a 24-bit sample of
+ * hash(i, seed, stream); BF16 adds one ulp when the hash's low 16 bits are
+ * below the 16 dropped bits; zero, NaN and magnitudes at or above the
+ * largest finite code keep the nearest code; MX scales as msq_encode.
+ * Same buffers and sizes as msq_encode; every format of msq_encode.      */
+int msq_encode_stochastic(msq_ctx *ctx, int format, const float *source, size_t elements,
+                          size_t row_length, uint32_t seed, uint32_t stream,
+                          uint8_t *values, uint8_t *scales);
+
+/* ---- log-spectrum storage (fp8_e4m3fn_log_s, fp4_e2m1_log_s) ---------------
+ * Replaces copySpectrumToStorage / spectrumValueAt
+ * (src/storage_codecs.cpp:387-460) and the device kernels
+ * log_spectrum_metadata / quantize_*_log_s / decode_*_log_s_to_f32
+ * (metal_mixed_sqrt.metal:1689-1804): root eigenvalues in blocks of
+ * MSQ_LOG_SPECTRUM_BLOCK with metadata (min, span) of log2 s per block (two
+ * floats, 8-byte aligned), codes of max * (log2 s - min) / span (max = 448
+ * for MSQ_FMT_FP8_E4M3FN, 6 for MSQ_FMT_FP4_E2M1), decoded as
+ * exp2(min + span * code / max).  Device semantics: the span is lowered by
+ * one ulp when min + span rounds above the block's maximum log.  Inputs
+ * must be finite and positive; otherwise the device status is set and the
+ * next msq_synchronize returns MSQ_ERR_DEVICE_STATUS.                     */
+#define MSQ_LOG_SPECTRUM_BLOCK 8
+enum { MSQ_ROUND_NEAREST = 0, MSQ_ROUND_STOCHASTIC = 1 };
+size_t msq_spectrum_metadata_bytes(size_t elements);
+int msq_spectrum_encode(msq_ctx *ctx, int format, const float *spectrum, size_t elements,
+                        int rounding, uint32_t seed, uint32_t stream, uint8_t *values,
+                        float *metadata);
+int msq_spectrum_decode(msq_ctx *ctx, int format, const uint8_t *values, const float *metadata,
+                        size_t elements, float *spectrum);
+
 /* ---- batched layout -------------------------------------------------------
  * A batch is `count` square matrices of orders n[i], packed back to back:
  * matrix i starts at element offset[i] (offsets are in elements; each

@@ -32,6 +32,9 @@ FORMAT_NAMES = {
     MXFP8_E4M3FN: "mxfp8_e4m3fn", MXFP8_E5M2: "mxfp8_e5m2", FP4_E2M1: "fp4_e2m1",
     MXFP4_E2M1: "mxfp4_e2m1", FP8_E4M3FN_ROWSCALE: "fp8_e4m3fn_rowscale",
 }
+# Rounding modes of msq_spectrum_encode (the reference's --rounding).
+ROUND_NEAREST = 0
+ROUND_STOCHASTIC = 1
 
 # Plans (msq_plan_format)
 PLAN_FP32, PLAN_BF16, PLAN_FP8, PLAN_MXFP4 = range(4)
@@ -74,6 +77,12 @@ _SIGS = {
     "msq_scale_bytes": (ctypes.c_size_t, [ctypes.c_int, ctypes.c_size_t, ctypes.c_size_t]),
     "msq_encode": (ctypes.c_int, [_P, ctypes.c_int, _P, ctypes.c_size_t, ctypes.c_size_t, _P, _P]),
     "msq_decode": (ctypes.c_int, [_P, ctypes.c_int, _P, _P, ctypes.c_size_t, ctypes.c_size_t, _P]),
+    "msq_encode_stochastic": (ctypes.c_int, [_P, ctypes.c_int, _P, ctypes.c_size_t, ctypes.c_size_t,
+                                             ctypes.c_uint32, ctypes.c_uint32, _P, _P]),
+    "msq_spectrum_metadata_bytes": (ctypes.c_size_t, [ctypes.c_size_t]),
+    "msq_spectrum_encode": (ctypes.c_int, [_P, ctypes.c_int, _P, ctypes.c_size_t, ctypes.c_int,
+                                           ctypes.c_uint32, ctypes.c_uint32, _P, _P]),
+    "msq_spectrum_decode": (ctypes.c_int, [_P, ctypes.c_int, _P, _P, ctypes.c_size_t, _P]),
     "msq_jacobi_batched": (ctypes.c_int, [_P, _P, _P, _P, _P, _P, ctypes.c_int,
                                           ctypes.c_double, ctypes.c_int, _P, _P]),
     "msq_jacobi_noalloc": (ctypes.c_int, [_P, _P, _P, ctypes.c_int, ctypes.c_double,
@@ -266,6 +275,43 @@ class Context:
         out = self.torch.empty(elements, dtype=self.torch.float32, device=values.device)
         self.check(lib().msq_decode(self.handle, fmt, _ptr(values), _ptr(scales), elements,
                                     row_length, _ptr(out)), "msq_decode")
+        return out
+
+    def copy_to_storage_stochastic(self, fmt: int, source, seed: int, stream: int,
+                                   row_length: int = 0):
+        """The device quantizers' stochastic rounding (--rounding stochastic):
+        returns (values uint8, scales uint8 or None) as copy_to_storage."""
+        torch = self.torch
+        n = source.numel()
+        values = torch.empty(max(storage_bytes(fmt, n), 1), dtype=torch.uint8, device=source.device)
+        sb = scale_bytes(fmt, n, row_length)
+        scales = torch.empty(sb, dtype=torch.uint8, device=source.device) if sb else None
+        self.check(lib().msq_encode_stochastic(self.handle, fmt, _ptr(source), n, row_length,
+                                               seed & 0xffffffff, stream & 0xffffffff,
+                                               _ptr(values), _ptr(scales)),
+                   "msq_encode_stochastic")
+        return values, scales
+
+    def copy_spectrum_to_storage(self, fmt: int, spectrum, rounding: int = ROUND_NEAREST,
+                                 seed: int = 0, stream: int = 0):
+        """Log-spectrum storage (copySpectrumToStorage, device form) of finite
+        positive root eigenvalues: returns (codes uint8, metadata float32 of
+        (min, span) per block of 8)."""
+        torch = self.torch
+        n = spectrum.numel()
+        values = torch.empty(max(storage_bytes(fmt, n), 1), dtype=torch.uint8, device=spectrum.device)
+        meta = torch.empty(max(lib().msq_spectrum_metadata_bytes(n) // 4, 2), dtype=torch.float32,
+                           device=spectrum.device)
+        self.check(lib().msq_spectrum_encode(self.handle, fmt, _ptr(spectrum), n, rounding,
+                                             seed & 0xffffffff, stream & 0xffffffff,
+                                             _ptr(values), _ptr(meta)), "msq_spectrum_encode")
+        return values, meta
+
+    def spectrum_values(self, fmt: int, values, meta, elements: int):
+        """spectrumValueAt for every index (device form): FP32 tensor."""
+        out = self.torch.empty(elements, dtype=self.torch.float32, device=values.device)
+        self.check(lib().msq_spectrum_decode(self.handle, fmt, _ptr(values), _ptr(meta), elements,
+                                             _ptr(out)), "msq_spectrum_decode")
         return out
 
     # ---- pipeline stages -----------------------------------------------

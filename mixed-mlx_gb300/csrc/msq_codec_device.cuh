@@ -228,4 +228,83 @@ __device__ __forceinline__ float mxScale(float decoded, uint32_t scale_byte) {
   return (decoded * exp2Int(half)) * exp2Int(k - half);
 }
 
+// ---- stochastic rounding ---------------------------------------------------
+// The reference's device quantizers for --rounding stochastic
+// (metal_mixed_sqrt.metal): stochastic_hash / stochastic_round_up :394-405,
+// encode_fp8_e4m3fn_stochastic :462-484, encode_fp8_e5m2_stochastic
+// :545-568, encode_fp4_e2m1_stochastic :740-763, quantize_bf16_stochastic
+// :1888-1907.  A finite magnitude strictly between two codes rounds up with
+// probability (|x| - lo) / (hi - lo) against a 24-bit sample of the hash of
+// (element index, seed, stream); zero, NaN and magnitudes at or above the
+// largest finite code take the nearest code.  Adjacent codes differ by a
+// power of two, so the probability is an exact quotient.
+
+__device__ __forceinline__ uint32_t stochasticHash(uint32_t index, uint32_t seed, uint32_t stream) {
+  const uint32_t state = index * 747796405u + seed + stream * 2891336453u;
+  const uint32_t word = ((state >> ((state >> 28u) + 4u)) ^ state) * 277803737u;
+  return (word >> 22u) ^ word;
+}
+
+__device__ __forceinline__ bool stochasticUp(float probability, uint32_t index, uint32_t seed,
+                                             uint32_t stream) {
+  // 24-bit sample times 2^-24 (exact)
+  const float sample = static_cast<float>(stochasticHash(index, seed, stream) >> 8u) *
+                       5.9604644775390625e-08f;
+  return sample < probability;
+}
+
+// The code below or above a finite magnitude that lies between codes, from
+// its nearest code (codes of one sign are ordered like their values).
+template <class Decode>
+__device__ __forceinline__ uint32_t stochasticCode(uint32_t nearest, float magnitude, Decode dec,
+                                                   uint32_t index, uint32_t seed, uint32_t stream) {
+  const float nearest_value = dec(nearest);
+  if (nearest_value == magnitude) return nearest;
+  const uint32_t lower = nearest_value < magnitude ? nearest : nearest - 1u;
+  const float lo = dec(lower), hi = dec(lower + 1u);
+  const float probability = __fdiv_rn(magnitude - lo, hi - lo);
+  return stochasticUp(probability, index, seed, stream) ? lower + 1u : lower;
+}
+
+__device__ __forceinline__ uint8_t encodeE4M3Stochastic(float value, uint32_t index, uint32_t seed,
+                                                        uint32_t stream) {
+  const float magnitude = fabsf(value);
+  if (value != value || magnitude == 0.0f || magnitude >= 448.0f) return encodeE4M3(value);
+  const uint32_t sign = (__float_as_uint(value) >> 24) & 0x80u;
+  return static_cast<uint8_t>(
+      sign | stochasticCode(encodeE4M3(magnitude), magnitude,
+                            [](uint32_t c) { return decodeE4M3(c); }, index, seed, stream));
+}
+
+__device__ __forceinline__ uint8_t encodeE5M2Stochastic(float value, uint32_t index, uint32_t seed,
+                                                        uint32_t stream) {
+  const float magnitude = fabsf(value);
+  if (value != value || isinf(magnitude) || magnitude == 0.0f || magnitude >= 57344.0f) {
+    return encodeE5M2(value);
+  }
+  const uint32_t sign = (__float_as_uint(value) >> 24) & 0x80u;
+  return static_cast<uint8_t>(
+      sign | stochasticCode(encodeE5M2(magnitude), magnitude,
+                            [](uint32_t c) { return decodeE5M2(c); }, index, seed, stream));
+}
+
+// 4-bit code in the low nibble
+__device__ __forceinline__ uint32_t encodeE2M1Stochastic(float value, uint32_t index, uint32_t seed,
+                                                         uint32_t stream) {
+  const float magnitude = fabsf(value);
+  if (value != value || magnitude == 0.0f || magnitude >= 6.0f) return encodeE2M1(value);
+  const uint32_t sign = (__float_as_uint(value) >> 28) & 0x8u;
+  return sign | stochasticCode(encodeE2M1(magnitude), magnitude,
+                               [](uint32_t c) { return decodeE2M1(c); }, index, seed, stream);
+}
+
+__device__ __forceinline__ uint16_t encodeBf16Stochastic(float value, uint32_t index, uint32_t seed,
+                                                         uint32_t stream) {
+  if (!isfinite(value) || value == 0.0f) return encodeBf16(value);
+  const uint32_t bits = __float_as_uint(value);
+  uint32_t rounded = bits & 0xffff0000u;
+  if ((stochasticHash(index, seed, stream) & 0xffffu) < (bits & 0xffffu)) rounded += 0x00010000u;
+  return static_cast<uint16_t>(rounded >> 16);
+}
+
 }  // namespace msq

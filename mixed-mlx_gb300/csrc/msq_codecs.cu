@@ -421,6 +421,172 @@ bool aligned16(const void *p) {
   return (reinterpret_cast<uintptr_t>(p) & 15u) == 0;
 }
 
+// ------------------------------------------------- stochastic rounding
+
+// Stochastic encoders (msq_encode_stochastic): one thread per element, the
+// element's flat index feeding the hash; FP4 lanes pair up by shuffle (the
+// even lane writes the byte); MX formats take one warp per 32-element block
+// (the block's finite maximum by a warp reduction, then x / 2^e per lane as
+// the nearest encoders compute it).  The loop is warp-uniform.
+template <int kFormat>
+__global__ void __launch_bounds__(kThreads)
+encodeStochasticKernel(const float *__restrict__ source, size_t elements, uint32_t seed,
+                       uint32_t stream, uint8_t *__restrict__ values,
+                       uint8_t *__restrict__ scales) {
+  constexpr bool kMx = kFormat == MSQ_FMT_MXFP8_E4M3FN || kFormat == MSQ_FMT_MXFP8_E5M2 ||
+                       kFormat == MSQ_FMT_MXFP4_E2M1;
+  constexpr bool kFp4 = kFormat == MSQ_FMT_FP4_E2M1 || kFormat == MSQ_FMT_MXFP4_E2M1;
+  const int lane = threadIdx.x & 31;
+  const size_t stride = static_cast<size_t>(gridDim.x) * blockDim.x;
+  for (size_t base = blockIdx.x * static_cast<size_t>(blockDim.x) + (threadIdx.x & ~31u);
+       base < elements; base += stride) {
+    const size_t i = base + lane;
+    const bool valid = i < elements;
+    float x = valid ? source[i] : 0.0f;
+    if constexpr (kMx) {
+      constexpr int kEmax = kFormat == MSQ_FMT_MXFP8_E4M3FN ? 8 : (kFormat == MSQ_FMT_MXFP8_E5M2 ? 15 : 2);
+      const float a = fabsf(x);
+      // finite magnitudes order like their bits
+      uint32_t m = valid && a <= 3.402823466e38f ? __float_as_uint(a) : 0u;
+      m = __reduce_max_sync(0xffffffffu, m);
+      const int e = mxExponent(__uint_as_float(m), kEmax);
+      if (lane == 0) scales[base / 32] = static_cast<uint8_t>(e + 127);
+      x = mxDivide(x, e);
+    }
+    const uint32_t index = static_cast<uint32_t>(i);
+    if constexpr (kFormat == MSQ_FMT_BF16) {
+      if (valid) reinterpret_cast<uint16_t *>(values)[i] = encodeBf16Stochastic(x, index, seed, stream);
+    } else if constexpr (kFormat == MSQ_FMT_FP8_E4M3FN || kFormat == MSQ_FMT_MXFP8_E4M3FN) {
+      if (valid) values[i] = encodeE4M3Stochastic(x, index, seed, stream);
+    } else if constexpr (kFormat == MSQ_FMT_FP8_E5M2 || kFormat == MSQ_FMT_MXFP8_E5M2) {
+      if (valid) values[i] = encodeE5M2Stochastic(x, index, seed, stream);
+    } else {
+      static_assert(kFp4, "format");
+      const uint32_t code = valid ? encodeE2M1Stochastic(x, index, seed, stream) : 0u;
+      const uint32_t next = __shfl_down_sync(0xffffffffu, code, 1);
+      if (valid && (i & 1) == 0) {
+        values[i / 2] = static_cast<uint8_t>(code | (i + 1 < elements ? next << 4 : 0u));
+      }
+    }
+  }
+}
+
+// Row-scaled FP8 with stochastic rounding: one warp per row as the nearest
+// row-scale encoder, each element rounded with its flat index.
+__global__ void __launch_bounds__(kThreads)
+encodeRowScaleStochasticKernel(const float *__restrict__ source, size_t rows, size_t row_length,
+                               uint32_t seed, uint32_t stream, uint8_t *__restrict__ values,
+                               float *__restrict__ scales) {
+  const int lane = threadIdx.x % 32;
+  const size_t warps = static_cast<size_t>(gridDim.x) * (blockDim.x / 32);
+  for (size_t row = blockIdx.x * static_cast<size_t>(blockDim.x / 32) + threadIdx.x / 32;
+       row < rows; row += warps) {
+    const float *in = source + row * row_length;
+    float m = 0.0f;
+    for (size_t i = lane; i < row_length; i += 32) {
+      const float a = fabsf(in[i]);
+      if (a <= 3.402823466e38f) m = fmaxf(m, a);
+    }
+#pragma unroll
+    for (int s = 16; s > 0; s >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, s));
+    const float scale = m == 0.0f ? 1.0f : __fdiv_rn(m, 448.0f);
+    if (lane == 0) scales[row] = scale;
+    uint8_t *out = values + row * row_length;
+    for (size_t i = lane; i < row_length; i += 32) {
+      out[i] = encodeE4M3Stochastic(rowDivide(in[i], scale),
+                                    static_cast<uint32_t>(row * row_length + i), seed, stream);
+    }
+  }
+}
+
+// ------------------------------------------------- log-spectrum storage
+
+// fp8_e4m3fn_log_s / fp4_e2m1_log_s (src/precision.hpp:87-92) in the
+// device form of metal_mixed_sqrt.metal:1689-1804: per block of 8 root
+// eigenvalues (min, span) of log2 s, the span lowered by one ulp when
+// min + span rounds above the block's maximum log (so the top code decodes
+// at or below the largest input); codes of maximum * (log2 s - min) / span
+// (maximum 448 or 6), nearest or stochastic; decode exp2(min + span *
+// dec(code) / maximum).  A value that is not finite and positive sets
+// kStatusBadSpectrum (the reference host codec fails on it).
+constexpr int kSpectrumBlock = 8;
+
+__global__ void __launch_bounds__(kThreads)
+spectrumMetadataKernel(const float *__restrict__ spectrum, size_t elements,
+                       float2 *__restrict__ metadata, int *status) {
+  const size_t blocks = (elements + kSpectrumBlock - 1) / kSpectrumBlock;
+  for (size_t b = blockIdx.x * static_cast<size_t>(blockDim.x) + threadIdx.x; b < blocks;
+       b += static_cast<size_t>(gridDim.x) * blockDim.x) {
+    const size_t begin = b * kSpectrumBlock;
+    const size_t end = begin + kSpectrumBlock < elements ? begin + kSpectrumBlock : elements;
+    float lo = __uint_as_float(0x7f800000u), hi = -lo;
+    bool bad = false;
+    for (size_t i = begin; i < end; ++i) {
+      const float v = spectrum[i];
+      bad = bad || !(v > 0.0f) || !(v <= 3.402823466e38f);
+      const float l = log2f(v);
+      lo = fminf(lo, l);
+      hi = fmaxf(hi, l);
+    }
+    if (bad) {
+      atomicExch(status, kStatusBadSpectrum);
+      lo = hi = 0.0f;
+    }
+    float span = hi - lo;
+    if (lo + span > hi) span = nextafterf(span, 0.0f);
+    metadata[b] = make_float2(lo, span);
+  }
+}
+
+template <int kFormat>
+__device__ __forceinline__ float spectrumScaled(const float *spectrum, const float2 *metadata,
+                                                size_t i) {
+  constexpr float kMax = kFormat == MSQ_FMT_FP8_E4M3FN ? 448.0f : 6.0f;
+  const float2 block = metadata[i / kSpectrumBlock];
+  return block.y == 0.0f ? 0.0f : __fdiv_rn(kMax * (log2f(spectrum[i]) - block.x), block.y);
+}
+
+// One thread per element; FP4 lanes pair up by shuffle (warp-uniform loop).
+template <int kFormat>
+__global__ void __launch_bounds__(kThreads)
+spectrumEncodeKernel(const float *__restrict__ spectrum, size_t elements,
+                     const float2 *__restrict__ metadata, int stochastic, uint32_t seed,
+                     uint32_t stream, uint8_t *__restrict__ values) {
+  const int lane = threadIdx.x & 31;
+  const size_t stride = static_cast<size_t>(gridDim.x) * blockDim.x;
+  for (size_t base = blockIdx.x * static_cast<size_t>(blockDim.x) + (threadIdx.x & ~31u);
+       base < elements; base += stride) {
+    const size_t i = base + lane;
+    const bool valid = i < elements;
+    const float x = valid ? spectrumScaled<kFormat>(spectrum, metadata, i) : 0.0f;
+    const uint32_t index = static_cast<uint32_t>(i);
+    if constexpr (kFormat == MSQ_FMT_FP8_E4M3FN) {
+      if (valid) values[i] = stochastic ? encodeE4M3Stochastic(x, index, seed, stream) : encodeE4M3(x);
+    } else {
+      const uint32_t code =
+          valid ? (stochastic ? encodeE2M1Stochastic(x, index, seed, stream) : encodeE2M1(x)) : 0u;
+      const uint32_t next = __shfl_down_sync(0xffffffffu, code, 1);
+      if (valid && (i & 1) == 0) {
+        values[i / 2] = static_cast<uint8_t>(code | (i + 1 < elements ? next << 4 : 0u));
+      }
+    }
+  }
+}
+
+template <int kFormat>
+__global__ void __launch_bounds__(kThreads)
+spectrumDecodeKernel(const uint8_t *__restrict__ values, const float2 *__restrict__ metadata,
+                     size_t elements, float *__restrict__ spectrum) {
+  constexpr float kMax = kFormat == MSQ_FMT_FP8_E4M3FN ? 448.0f : 6.0f;
+  for (size_t i = blockIdx.x * static_cast<size_t>(blockDim.x) + threadIdx.x; i < elements;
+       i += static_cast<size_t>(gridDim.x) * blockDim.x) {
+    const float2 block = metadata[i / kSpectrumBlock];
+    const float d = kFormat == MSQ_FMT_FP8_E4M3FN ? decodeE4M3(values[i])
+                                                 : decodeE2M1((values[i / 2] >> ((i & 1) * 4)) & 0xfu);
+    spectrum[i] = exp2f(block.x + __fdiv_rn(block.y * d, kMax));
+  }
+}
+
 }  // namespace
 }  // namespace msq
 
@@ -580,4 +746,130 @@ extern "C" int msq_decode(msq_ctx *ctx, int format, const uint8_t *values,
       return setError(ctx, MSQ_ERR_INVALID_ARGUMENT, "msq_decode: unknown format");
   }
   return launched(ctx, "msq_decode");
+}
+
+extern "C" int msq_encode_stochastic(msq_ctx *ctx, int format, const float *source,
+                                     size_t elements, size_t row_length, uint32_t seed,
+                                     uint32_t stream, uint8_t *values, uint8_t *scales) {
+  if (ctx == nullptr) return MSQ_ERR_INVALID_ARGUMENT;
+  msq::DeviceGuard device_guard(ctx);
+  if (elements == 0) return MSQ_OK;
+  if (source == nullptr || values == nullptr) {
+    return setError(ctx, MSQ_ERR_INVALID_ARGUMENT, "msq_encode_stochastic: null buffer");
+  }
+  const bool needs_scales = msq_scale_bytes(format, elements, row_length ? row_length : 1) != 0;
+  if (needs_scales && scales == nullptr) {
+    return setError(ctx, MSQ_ERR_INVALID_ARGUMENT,
+                    "msq_encode_stochastic: this format requires a scale plane");
+  }
+  cudaStream_t s = ctx->stream;
+  const unsigned grid = gridFor((elements + 31) / 32 * 32, kThreads);
+  switch (format) {
+    case MSQ_FMT_FP32:
+      return cudaCheck(ctx, cudaMemcpyAsync(values, source, elements * 4,
+                                            cudaMemcpyDeviceToDevice, s),
+                       "msq_encode_stochastic fp32 copy");
+    case MSQ_FMT_BF16:
+      encodeStochasticKernel<MSQ_FMT_BF16><<<grid, kThreads, 0, s>>>(source, elements, seed, stream, values, scales);
+      break;
+    case MSQ_FMT_FP8_E4M3FN:
+      encodeStochasticKernel<MSQ_FMT_FP8_E4M3FN><<<grid, kThreads, 0, s>>>(source, elements, seed, stream, values, scales);
+      break;
+    case MSQ_FMT_FP8_E5M2:
+      encodeStochasticKernel<MSQ_FMT_FP8_E5M2><<<grid, kThreads, 0, s>>>(source, elements, seed, stream, values, scales);
+      break;
+    case MSQ_FMT_FP4_E2M1:
+      encodeStochasticKernel<MSQ_FMT_FP4_E2M1><<<grid, kThreads, 0, s>>>(source, elements, seed, stream, values, scales);
+      break;
+    case MSQ_FMT_MXFP8_E4M3FN:
+      encodeStochasticKernel<MSQ_FMT_MXFP8_E4M3FN><<<grid, kThreads, 0, s>>>(source, elements, seed, stream, values, scales);
+      break;
+    case MSQ_FMT_MXFP8_E5M2:
+      encodeStochasticKernel<MSQ_FMT_MXFP8_E5M2><<<grid, kThreads, 0, s>>>(source, elements, seed, stream, values, scales);
+      break;
+    case MSQ_FMT_MXFP4_E2M1:
+      encodeStochasticKernel<MSQ_FMT_MXFP4_E2M1><<<grid, kThreads, 0, s>>>(source, elements, seed, stream, values, scales);
+      break;
+    case MSQ_FMT_FP8_E4M3FN_ROWSCALE: {
+      if (row_length == 0 || elements % row_length != 0) {
+        return setError(ctx, MSQ_ERR_INVALID_ARGUMENT,
+                        "msq_encode_stochastic: elements must be a multiple of row_length");
+      }
+      const size_t rows = elements / row_length;
+      encodeRowScaleStochasticKernel<<<gridFor(rows * 32, kThreads), kThreads, 0, s>>>(
+          source, rows, row_length, seed, stream, values, reinterpret_cast<float *>(scales));
+      break;
+    }
+    default:
+      return setError(ctx, MSQ_ERR_INVALID_ARGUMENT, "msq_encode_stochastic: unknown format");
+  }
+  return launched(ctx, "msq_encode_stochastic");
+}
+
+extern "C" size_t msq_spectrum_metadata_bytes(size_t elements) {
+  return 2 * sizeof(float) * ((elements + kSpectrumBlock - 1) / kSpectrumBlock);
+}
+
+extern "C" int msq_spectrum_encode(msq_ctx *ctx, int format, const float *spectrum,
+                                   size_t elements, int rounding, uint32_t seed, uint32_t stream,
+                                   uint8_t *values, float *metadata) {
+  if (ctx == nullptr) return MSQ_ERR_INVALID_ARGUMENT;
+  msq::DeviceGuard device_guard(ctx);
+  if (elements == 0) return MSQ_OK;
+  if (spectrum == nullptr || values == nullptr || metadata == nullptr) {
+    return setError(ctx, MSQ_ERR_INVALID_ARGUMENT, "msq_spectrum_encode: null buffer");
+  }
+  if (format != MSQ_FMT_FP8_E4M3FN && format != MSQ_FMT_FP4_E2M1) {
+    return setError(ctx, MSQ_ERR_INVALID_ARGUMENT,
+                    "msq_spectrum_encode: log-spectrum storage uses FP8-E4M3FN or FP4-E2M1 codes");
+  }
+  if (rounding != MSQ_ROUND_NEAREST && rounding != MSQ_ROUND_STOCHASTIC) {
+    return setError(ctx, MSQ_ERR_INVALID_ARGUMENT, "msq_spectrum_encode: unknown rounding mode");
+  }
+  if (reinterpret_cast<uintptr_t>(metadata) % 8 != 0) {
+    return setError(ctx, MSQ_ERR_INVALID_ARGUMENT, "msq_spectrum_encode: metadata not 8-byte aligned");
+  }
+  cudaStream_t s = ctx->stream;
+  float2 *meta = reinterpret_cast<float2 *>(metadata);
+  const size_t blocks = (elements + kSpectrumBlock - 1) / kSpectrumBlock;
+  spectrumMetadataKernel<<<gridFor(blocks, kThreads), kThreads, 0, s>>>(spectrum, elements, meta,
+                                                                       ctx->d_status);
+  MSQ_TRY(launched(ctx, "msq_spectrum_encode"));
+  const unsigned grid = gridFor((elements + 31) / 32 * 32, kThreads);
+  const int stochastic = rounding == MSQ_ROUND_STOCHASTIC;
+  if (format == MSQ_FMT_FP8_E4M3FN) {
+    spectrumEncodeKernel<MSQ_FMT_FP8_E4M3FN><<<grid, kThreads, 0, s>>>(spectrum, elements, meta,
+                                                                        stochastic, seed, stream, values);
+  } else {
+    spectrumEncodeKernel<MSQ_FMT_FP4_E2M1><<<grid, kThreads, 0, s>>>(spectrum, elements, meta,
+                                                                      stochastic, seed, stream, values);
+  }
+  return launched(ctx, "msq_spectrum_encode");
+}
+
+extern "C" int msq_spectrum_decode(msq_ctx *ctx, int format, const uint8_t *values,
+                                   const float *metadata, size_t elements, float *spectrum) {
+  if (ctx == nullptr) return MSQ_ERR_INVALID_ARGUMENT;
+  msq::DeviceGuard device_guard(ctx);
+  if (elements == 0) return MSQ_OK;
+  if (spectrum == nullptr || values == nullptr || metadata == nullptr) {
+    return setError(ctx, MSQ_ERR_INVALID_ARGUMENT, "msq_spectrum_decode: null buffer");
+  }
+  if (format != MSQ_FMT_FP8_E4M3FN && format != MSQ_FMT_FP4_E2M1) {
+    return setError(ctx, MSQ_ERR_INVALID_ARGUMENT,
+                    "msq_spectrum_decode: log-spectrum storage uses FP8-E4M3FN or FP4-E2M1 codes");
+  }
+  if (reinterpret_cast<uintptr_t>(metadata) % 8 != 0) {
+    return setError(ctx, MSQ_ERR_INVALID_ARGUMENT, "msq_spectrum_decode: metadata not 8-byte aligned");
+  }
+  cudaStream_t s = ctx->stream;
+  const float2 *meta = reinterpret_cast<const float2 *>(metadata);
+  if (format == MSQ_FMT_FP8_E4M3FN) {
+    spectrumDecodeKernel<MSQ_FMT_FP8_E4M3FN><<<gridFor(elements, kThreads), kThreads, 0, s>>>(
+        values, meta, elements, spectrum);
+  } else {
+    spectrumDecodeKernel<MSQ_FMT_FP4_E2M1><<<gridFor(elements, kThreads), kThreads, 0, s>>>(
+        values, meta, elements, spectrum);
+  }
+  return launched(ctx, "msq_spectrum_decode");
 }

@@ -121,6 +121,7 @@ int checkDeviceStatus(msq_ctx *ctx) {
                       : status == kStatusTmemAllocFailed ? "TMEM allocation failed"
                       : status == kStatusBadOrder        ? "matrix order outside kernel limits"
                       : status == kStatusFlagTimeout     ? "bounded shared-memory flag wait expired"
+                      : status == kStatusBadSpectrum     ? "log-spectrum input not finite and positive"
                                                          : "kernel reported an error";
     return setError(ctx, MSQ_ERR_DEVICE_STATUS,
                     std::string("device status ") + std::to_string(status) + ": " + why);

@@ -17,7 +17,8 @@ namespace msq {
 constexpr int kSmCount = 152;
 
 // Device-side status words (one int each) written by kernels that bound a
-// wait or check an index; read back by msq_check_device_status().
+// wait or check an index or an input; read back by msq_synchronize and the
+// solve calls (checkDeviceStatus).
 enum DeviceStatus : int {
   kStatusOk = 0,
   kStatusJacobiOrderTooLarge = 1,
@@ -25,6 +26,7 @@ enum DeviceStatus : int {
   kStatusTmemAllocFailed = 3,
   kStatusBadOrder = 4,
   kStatusFlagTimeout = 5,
+  kStatusBadSpectrum = 6,
 };
 
 struct WorkList {

@@ -13,6 +13,8 @@
  *    its linear nearest-code scan, so it is independent of the integer
  *    rounding the CUDA kernels use;
  *  - the FP8-E4M3 per-row-scale format (no reference counterpart);
+ *  - the device quantizers' stochastic rounding and the log-spectrum
+ *    storage of the root eigenvalues (restated from the shader source);
  *  - the parallel-order two-sided Jacobi of metal_mixed_sqrt.metal:1319-1444
  *    with the round-robin schedule of src/metal_solver.cpp:50-79, angles in
  *    FP64, FP32 storage, convergence-tested;
@@ -226,6 +228,212 @@ int msqo_decode(int format, const uint8_t *values, const uint8_t *scales,
         break;
       default: return 1;
     }
+  }
+  return 0;
+}
+
+/* ------------------------------------------------- stochastic rounding */
+
+/* The reference's device quantizers for --rounding stochastic
+ * (metal_mixed_sqrt.metal): stochastic_hash / stochastic_round_up :394-405;
+ * encode_fp8_e4m3fn_stochastic :462-484, encode_fp8_e5m2_stochastic
+ * :545-568, encode_fp4_e2m1_stochastic :740-763 (bracketing codes lo < |x|
+ * < hi; round up with probability (|x| - lo) / (hi - lo) against a 24-bit
+ * sample of the hash of (element index, seed, stream); zero, NaN, and
+ * magnitudes at or above the largest finite code take the nearest code);
+ * quantize_bf16_stochastic :1888-1907 (add one BF16 ulp when the hash's low
+ * 16 bits are below the 16 dropped bits).  The MX quantizers
+ * (:971-1000, :1113-1140, :1232-1260) scale a block of 32 as the nearest
+ * ones do and apply the element rule to x / 2^e with the global index.  No
+ * host counterpart exists: these are restated from the shader source.
+ * Adjacent codes differ by a power of two, so the probability is an exact
+ * quotient whatever the division. */
+uint32_t msqo_stochastic_hash(uint32_t index, uint32_t seed, uint32_t stream) {
+  uint32_t state = index * 747796405u + seed + stream * 2891336453u;
+  uint32_t word = ((state >> ((state >> 28u) + 4u)) ^ state) * 277803737u;
+  return (word >> 22u) ^ word;
+}
+
+static int round_up(float probability, uint32_t index, uint32_t seed, uint32_t stream) {
+  float sample = (float)(msqo_stochastic_hash(index, seed, stream) >> 8u) * 0x1.0p-24f;
+  return sample < probability;
+}
+
+/* the bracketing codes of a finite magnitude below the largest code */
+static uint8_t sr_code(uint8_t nearest, float magnitude, float (*dec)(uint8_t), uint32_t index,
+                       uint32_t seed, uint32_t stream) {
+  float nearest_value = dec(nearest);
+  if (nearest_value == magnitude) return nearest;
+  uint8_t lower = nearest_value < magnitude ? nearest : (uint8_t)(nearest - 1u);
+  uint8_t upper = (uint8_t)(lower + 1u);
+  float lo = dec(lower), hi = dec(upper);
+  float p = (magnitude - lo) / (hi - lo);
+  return round_up(p, index, seed, stream) ? upper : lower;
+}
+
+uint8_t msqo_encode_e4m3_sr(float value, uint32_t index, uint32_t seed, uint32_t stream) {
+  float magnitude = fabsf(value);
+  if (isnan(value) || magnitude == 0.0f || magnitude >= 448.0f) return msqo_encode_e4m3(value);
+  uint8_t sign = signbit(value) ? 0x80u : 0u;
+  return (uint8_t)(sign | sr_code(msqo_encode_e4m3(magnitude), magnitude, msqo_decode_e4m3,
+                                  index, seed, stream));
+}
+
+uint8_t msqo_encode_e5m2_sr(float value, uint32_t index, uint32_t seed, uint32_t stream) {
+  float magnitude = fabsf(value);
+  if (isnan(value) || isinf(value) || magnitude == 0.0f || magnitude >= 57344.0f)
+    return msqo_encode_e5m2(value);
+  uint8_t sign = signbit(value) ? 0x80u : 0u;
+  return (uint8_t)(sign | sr_code(msqo_encode_e5m2(magnitude), magnitude, msqo_decode_e5m2,
+                                  index, seed, stream));
+}
+
+uint8_t msqo_encode_e2m1_sr(float value, uint32_t index, uint32_t seed, uint32_t stream) {
+  float magnitude = fabsf(value);
+  if (isnan(value) || magnitude == 0.0f || magnitude >= 6.0f) return msqo_encode_e2m1(value);
+  uint8_t sign = signbit(value) ? 0x08u : 0u;
+  /* the shader scans for the largest code not above the magnitude */
+  uint8_t lower = 0;
+  while (lower < 7u && msqo_decode_e2m1((uint8_t)(lower + 1u)) <= magnitude) ++lower;
+  float lo = msqo_decode_e2m1(lower);
+  if (lo == magnitude || lower == 7u) return (uint8_t)(sign | lower);
+  uint8_t upper = (uint8_t)(lower + 1u);
+  float p = (magnitude - lo) / (msqo_decode_e2m1(upper) - lo);
+  return (uint8_t)(sign | (round_up(p, index, seed, stream) ? upper : lower));
+}
+
+uint16_t msqo_encode_bf16_sr(float value, uint32_t index, uint32_t seed, uint32_t stream) {
+  if (!isfinite(value) || value == 0.0f) return msqo_encode_bf16(value);
+  uint32_t bits;
+  memcpy(&bits, &value, 4);
+  uint32_t rounded = bits & 0xffff0000u;
+  if ((msqo_stochastic_hash(index, seed, stream) & 0xffffu) < (bits & 0xffffu)) rounded += 0x00010000u;
+  return (uint16_t)(rounded >> 16);
+}
+
+/* Stochastic counterpart of msqo_encode for every format (8: E4M3 of
+ * x / s_row, s_row = max|row| / 448, with the element's flat index). */
+int msqo_encode_stochastic(int format, const float *src, size_t elements, size_t row_length,
+                           uint32_t seed, uint32_t stream, uint8_t *values, uint8_t *scales) {
+  switch (format) {
+    case 0: memcpy(values, src, elements * 4); return 0;
+    case 1:
+      for (size_t i = 0; i < elements; ++i)
+        ((uint16_t *)values)[i] = msqo_encode_bf16_sr(src[i], (uint32_t)i, seed, stream);
+      return 0;
+    case 2:
+      for (size_t i = 0; i < elements; ++i) values[i] = msqo_encode_e4m3_sr(src[i], (uint32_t)i, seed, stream);
+      return 0;
+    case 3:
+      for (size_t i = 0; i < elements; ++i) values[i] = msqo_encode_e5m2_sr(src[i], (uint32_t)i, seed, stream);
+      return 0;
+    case 4: case 5: {
+      int emax = format == 4 ? 8 : 15;
+      for (size_t b = 0, blk = 0; b < elements; b += 32, ++blk) {
+        size_t end = b + 32 < elements ? b + 32 : elements;
+        int e = mx_exponent(src, b, end, emax);
+        scales[blk] = (uint8_t)(e + 127);
+        float scale = ldexpf(1.0f, e);
+        for (size_t i = b; i < end; ++i)
+          values[i] = format == 4 ? msqo_encode_e4m3_sr(src[i] / scale, (uint32_t)i, seed, stream)
+                                  : msqo_encode_e5m2_sr(src[i] / scale, (uint32_t)i, seed, stream);
+      }
+      return 0;
+    }
+    case 6:
+      for (size_t i = 0; i < elements; i += 2) {
+        uint8_t lo = msqo_encode_e2m1_sr(src[i], (uint32_t)i, seed, stream);
+        uint8_t hi = i + 1 < elements ? msqo_encode_e2m1_sr(src[i + 1], (uint32_t)(i + 1), seed, stream) : 0u;
+        values[i / 2] = (uint8_t)(lo | (hi << 4));
+      }
+      return 0;
+    case 7:
+      for (size_t b = 0, blk = 0; b < elements; b += 32, ++blk) {
+        size_t end = b + 32 < elements ? b + 32 : elements;
+        int e = mx_exponent(src, b, end, 2);
+        scales[blk] = (uint8_t)(e + 127);
+        float scale = ldexpf(1.0f, e);
+        for (size_t i = b; i < end; i += 2) {
+          uint8_t lo = msqo_encode_e2m1_sr(src[i] / scale, (uint32_t)i, seed, stream);
+          uint8_t hi = i + 1 < end ? msqo_encode_e2m1_sr(src[i + 1] / scale, (uint32_t)(i + 1), seed, stream) : 0u;
+          values[i / 2] = (uint8_t)(lo | (hi << 4));
+        }
+      }
+      return 0;
+    case 8: {
+      if (row_length == 0 || elements % row_length) return 1;
+      float *row_scales = (float *)scales;
+      for (size_t r = 0; r < elements / row_length; ++r) {
+        const float *row = src + r * row_length;
+        float m = 0.0f;
+        for (size_t i = 0; i < row_length; ++i)
+          if (isfinite(row[i]) && fabsf(row[i]) > m) m = fabsf(row[i]);
+        float s = m == 0.0f ? 1.0f : m / 448.0f;
+        row_scales[r] = s;
+        for (size_t i = 0; i < row_length; ++i) {
+          size_t k = r * row_length + i;
+          values[k] = msqo_encode_e4m3_sr(row[i] / s, (uint32_t)k, seed, stream);
+        }
+      }
+      return 0;
+    }
+    default: return 1;
+  }
+}
+
+/* ------------------------------------------------- log-spectrum storage */
+
+/* fp8_e4m3fn_log_s / fp4_e2m1_log_s (src/precision.hpp:87-92): root
+ * eigenvalues in blocks of 8 stored as codes of maximum * (log2 s - min) /
+ * span, metadata (min, span) of log2 s per block; decode exp2(min + span *
+ * dec(code) / maximum), maximum = 448 (E4M3) or 6 (E2M1).  The device form
+ * (metal_mixed_sqrt.metal:1689-1804): the span is lowered by one ulp when
+ * min + span rounds above the block's maximum log, so the top code decodes
+ * at or below the largest input.  The host form (copySpectrumToStorage,
+ * src/storage_codecs.cpp:400-440) keeps the span; with that difference the
+ * two agree (tests).  Inputs must be finite and positive.  Returns 0, or 1
+ * for an unsupported format or an invalid input. */
+int msqo_spectrum_encode(int format, const float *s, size_t elements, int stochastic,
+                         uint32_t seed, uint32_t stream, uint8_t *values, float *metadata) {
+  if (format != 2 && format != 6) return 1;
+  const float maximum = format == 2 ? 448.0f : 6.0f;
+  for (size_t b = 0, blk = 0; b < elements; b += 8, ++blk) {
+    size_t end = b + 8 < elements ? b + 8 : elements;
+    float lo = INFINITY, hi = -INFINITY;
+    for (size_t i = b; i < end; ++i) {
+      if (!(s[i] > 0.0f) || !isfinite(s[i])) return 1;
+      float l = log2f(s[i]);
+      lo = fminf(lo, l);
+      hi = fmaxf(hi, l);
+    }
+    float span = hi - lo;
+    if (lo + span > hi) span = nextafterf(span, 0.0f);
+    metadata[2 * blk] = lo;
+    metadata[2 * blk + 1] = span;
+  }
+  if (format == 6) memset(values, 0, (elements + 1) / 2);
+  for (size_t i = 0; i < elements; ++i) {
+    const float lo = metadata[2 * (i / 8)], span = metadata[2 * (i / 8) + 1];
+    const float x = span == 0.0f ? 0.0f : maximum * (log2f(s[i]) - lo) / span;
+    if (format == 2) {
+      values[i] = stochastic ? msqo_encode_e4m3_sr(x, (uint32_t)i, seed, stream) : msqo_encode_e4m3(x);
+    } else {
+      uint8_t c = stochastic ? msqo_encode_e2m1_sr(x, (uint32_t)i, seed, stream) : msqo_encode_e2m1(x);
+      values[i / 2] |= (uint8_t)(c << ((i & 1u) * 4));
+    }
+  }
+  return 0;
+}
+
+int msqo_spectrum_decode(int format, const uint8_t *values, const float *metadata,
+                         size_t elements, float *out) {
+  if (format != 2 && format != 6) return 1;
+  const float maximum = format == 2 ? 448.0f : 6.0f;
+  for (size_t i = 0; i < elements; ++i) {
+    const float lo = metadata[2 * (i / 8)], span = metadata[2 * (i / 8) + 1];
+    const float d = format == 2 ? msqo_decode_e4m3(values[i])
+                                : msqo_decode_e2m1((values[i / 2] >> ((i & 1u) * 4)) & 0x0fu);
+    out[i] = exp2f(lo + span * d / maximum);
   }
   return 0;
 }

@@ -67,6 +67,13 @@ def olib() -> ctypes.CDLL:
                                          ctypes.POINTER(ctypes.c_uint), ctypes.POINTER(ctypes.c_uint)]
         lib.msqo_ff_residual.argtypes = [_P, _P, _P, ctypes.c_uint, _P]
         lib.msqo_ff_residual.restype = ctypes.c_double
+        lib.msqo_stochastic_hash.argtypes = [ctypes.c_uint32] * 3
+        lib.msqo_stochastic_hash.restype = ctypes.c_uint32
+        lib.msqo_encode_stochastic.argtypes = [ctypes.c_int, _P, ctypes.c_size_t, ctypes.c_size_t,
+                                               ctypes.c_uint32, ctypes.c_uint32, _P, _P]
+        lib.msqo_spectrum_encode.argtypes = [ctypes.c_int, _P, ctypes.c_size_t, ctypes.c_int,
+                                             ctypes.c_uint32, ctypes.c_uint32, _P, _P]
+        lib.msqo_spectrum_decode.argtypes = [ctypes.c_int, _P, _P, ctypes.c_size_t, _P]
         _ORACLE = lib
     return _ORACLE
 
@@ -102,6 +109,49 @@ def decode(fmt: int, values: np.ndarray, scales, elements: int, row_length: int 
                             out.ctypes.data)
     if rc:
         raise ValueError("oracle decode failed")
+    return out
+
+
+def encode_stochastic(fmt: int, x: np.ndarray, seed: int, stream: int, row_length: int = 0):
+    """The device quantizers' stochastic rounding restated: (values, scales | None)."""
+    x = np.ascontiguousarray(x, dtype=np.float32)
+    n = x.size
+    values = np.zeros(max(olib().msqo_storage_bytes(fmt, n), 1), dtype=np.uint8)
+    sb = scale_bytes(fmt, n, row_length)
+    scales = np.zeros(max(sb, 1), dtype=np.uint8)
+    rc = olib().msqo_encode_stochastic(fmt, x.ctypes.data, n, row_length, seed & 0xffffffff,
+                                       stream & 0xffffffff, values.ctypes.data, scales.ctypes.data)
+    if rc:
+        raise ValueError("oracle stochastic encode failed")
+    return values[:olib().msqo_storage_bytes(fmt, n)], (scales[:sb] if sb else None)
+
+
+def spectrum_metadata_floats(elements: int) -> int:
+    """Two floats (min, span of log2 s) per block of 8 root eigenvalues."""
+    return 2 * ((elements + 7) // 8)
+
+
+def spectrum_encode(fmt: int, s: np.ndarray, stochastic: bool = False, seed: int = 0,
+                    stream: int = 0):
+    """Log-spectrum storage (device form): returns (codes, metadata)."""
+    s = np.ascontiguousarray(s, dtype=np.float32)
+    n = s.size
+    values = np.zeros(max(olib().msqo_storage_bytes(fmt, n), 1), dtype=np.uint8)
+    meta = np.zeros(max(spectrum_metadata_floats(n), 1), dtype=np.float32)
+    rc = olib().msqo_spectrum_encode(fmt, s.ctypes.data, n, int(stochastic), seed & 0xffffffff,
+                                     stream & 0xffffffff, values.ctypes.data, meta.ctypes.data)
+    if rc:
+        raise ValueError("oracle spectrum encode failed (format or non-positive input)")
+    return values[:olib().msqo_storage_bytes(fmt, n)], meta[:spectrum_metadata_floats(n)]
+
+
+def spectrum_decode(fmt: int, values: np.ndarray, meta: np.ndarray, elements: int):
+    out = np.zeros(elements, dtype=np.float32)
+    values = np.ascontiguousarray(values, dtype=np.uint8)
+    meta = np.ascontiguousarray(meta, dtype=np.float32)
+    if olib().msqo_spectrum_decode(fmt, values.ctypes.data, meta.ctypes.data, elements,
+                                   out.ctypes.data):
+        raise ValueError("oracle spectrum decode failed")
     return out
 
 
@@ -384,6 +434,8 @@ def ref() -> ctypes.CDLL:
         lib.ref_relative_error.restype = ctypes.c_double
         lib.ref_run_accelerate.argtypes = [_P, ctypes.c_size_t, ctypes.c_double, ctypes.c_size_t,
                                            ctypes.c_double, _P, _P, ctypes.c_size_t]
+        lib.ref_spectrum_encode.argtypes = [ctypes.c_int, _P, ctypes.c_size_t, _P, _P]
+        lib.ref_spectrum_decode.argtypes = [ctypes.c_int, _P, _P, ctypes.c_size_t, _P]
         _REF = lib
     return _REF
 
@@ -407,5 +459,28 @@ def ref_decode(fmt: int, values: np.ndarray, scales, elements: int):
     sc = np.ascontiguousarray(scales, dtype=np.uint8) if scales is not None else None
     if lib.ref_decode(fmt, values.ctypes.data, sc.ctypes.data if sc is not None else None,
                       elements, out.ctypes.data):
+        raise ValueError(lib.ref_last_error().decode())
+    return out
+
+
+def ref_spectrum_encode(fmt: int, s: np.ndarray):
+    """copySpectrumToStorage of the reference (host form): (codes, metadata)."""
+    lib = ref()
+    s = np.ascontiguousarray(s, dtype=np.float32)
+    n = s.size
+    values = np.zeros(max(lib.ref_storage_bytes(fmt, n), 1), dtype=np.uint8)
+    meta = np.zeros(max(spectrum_metadata_floats(n), 1), dtype=np.float32)
+    if lib.ref_spectrum_encode(fmt, s.ctypes.data, n, values.ctypes.data, meta.ctypes.data):
+        raise ValueError(lib.ref_last_error().decode())
+    return values[:lib.ref_storage_bytes(fmt, n)], meta[:spectrum_metadata_floats(n)]
+
+
+def ref_spectrum_decode(fmt: int, values: np.ndarray, meta: np.ndarray, elements: int):
+    lib = ref()
+    out = np.zeros(elements, dtype=np.float32)
+    values = np.ascontiguousarray(values, dtype=np.uint8)
+    meta = np.ascontiguousarray(meta, dtype=np.float32)
+    if lib.ref_spectrum_decode(fmt, values.ctypes.data, meta.ctypes.data, elements,
+                               out.ctypes.data):
         raise ValueError(lib.ref_last_error().decode())
     return out

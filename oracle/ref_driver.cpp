@@ -98,6 +98,46 @@ int ref_decode(int codec, const uint8_t *values, const uint8_t *scales,
   });
 }
 
+// The log-spectrum precision whose scalar codec is `codec` (2 = FP8-E4M3FN,
+// 6 = FP4-E2M1: fp8_e4m3fn_log_s / fp4_e2m1_log_s of kPrecisionSpecs).
+const PrecisionSpec *logSpecForCodec(int codec) {
+  for (const PrecisionSpec &spec : kPrecisionSpecs) {
+    if (static_cast<int>(spec.host_storage) == codec && spec.usesLogSpectrum()) {
+      return &spec;
+    }
+  }
+  return nullptr;
+}
+
+// copySpectrumToStorage (src/storage_codecs.cpp:400-440): codes and two
+// floats (min, span) per block of spectral_block_elements.
+int ref_spectrum_encode(int codec, const float *source, size_t elements,
+                        uint8_t *values, float *metadata) {
+  return guarded([&] {
+    const PrecisionSpec *spec = logSpecForCodec(codec);
+    if (spec == nullptr) throw std::runtime_error("no log-spectrum precision for codec");
+    std::vector<float> input(source, source + elements);
+    MTL::Buffer value_buffer(values, storageBytes(*spec, elements));
+    MTL::Buffer metadata_buffer(metadata, spectrumMetadataBytes(*spec, elements));
+    copySpectrumToStorage(*spec, input, &value_buffer, &metadata_buffer);
+  });
+}
+
+// spectrumValueAt (src/storage_codecs.cpp:442-460) for every index.
+int ref_spectrum_decode(int codec, const uint8_t *values, const float *metadata,
+                        size_t elements, float *output) {
+  return guarded([&] {
+    const PrecisionSpec *spec = logSpecForCodec(codec);
+    if (spec == nullptr) throw std::runtime_error("no log-spectrum precision for codec");
+    MTL::Buffer value_buffer(const_cast<uint8_t *>(values), storageBytes(*spec, elements));
+    MTL::Buffer metadata_buffer(const_cast<float *>(metadata),
+                                spectrumMetadataBytes(*spec, elements));
+    for (size_t index = 0; index < elements; ++index) {
+      output[index] = spectrumValueAt(*spec, &value_buffer, &metadata_buffer, index);
+    }
+  });
+}
+
 // makeSpdMatrix (src/numerics.cpp:175-195).
 int ref_make_spd(size_t order, double condition, double *output) {
   return guarded([&] {

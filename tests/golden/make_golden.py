@@ -12,8 +12,15 @@ them (src/storage_codecs.cpp, src/numerics.cpp, src/accelerate_backend.cpp,
   numerics.npz   makeSpdMatrix(n, cond) outputs, symmetricReferenceRoot of
                  them, and runAccelerateCase (src/accelerate_backend.cpp:
                  803-1091) residual/forward-error histories.
+  spectrum.npz   copySpectrumToStorage / spectrumValueAt (src/storage_codecs.
+                 cpp:387-460) codes, (min, span) metadata and decoded values
+                 of the log-spectrum precisions (FP8-E4M3FN and FP4-E2M1
+                 codes) for the roots of checkLogSpectrumStorage, the
+                 spectrum of checkStochasticQuantization and log-uniform
+                 spectra with equal-valued blocks and a ragged tail.
 
-Usage: make -C oracle && python tests/golden/make_golden.py
+Usage: make -C oracle && python tests/golden/make_golden.py [spectrum]
+(with `spectrum`, only spectrum.npz is written)
 """
 from __future__ import annotations
 
@@ -74,9 +81,41 @@ def codec_inputs() -> np.ndarray:
     return np.concatenate([x, rng.standard_normal(pad).astype(F32)])
 
 
+def spectrum_inputs() -> dict:
+    """Finite positive spectra: the roots checkLogSpectrumStorage uses
+    (src/metal_checks.cpp:507-509), 1024 values of the spectrum
+    checkStochasticQuantization builds (:425-431), and 2^U(-20, 20) values
+    with two equal-valued blocks (span 0) and a ragged tail (1001 values)."""
+    check = np.array([1.0, 1.5, 2.0, 3.0, 10.0, 31.622776, 100.0, 1000.0], dtype=F32)
+    idx = np.arange(1024)
+    pos = np.power((idx % 8) / F32(7.0), F32(1.3)).astype(F32)
+    pattern = np.exp2(F32(-2.0) + F32(4.0) * pos).astype(F32)
+    rng = np.random.default_rng(2024)
+    wide = np.exp2(rng.uniform(-20.0, 20.0, 1001)).astype(F32)
+    wide[8:16] = F32(3.0)
+    wide[16:24] = F32(1e-3)
+    return {"check": check, "pattern": pattern, "wide": wide}
+
+
+def write_spectrum() -> None:
+    out = {}
+    for name, s in spectrum_inputs().items():
+        out[f"{name}_input"] = s
+        for fmt in (2, 6):
+            v, m = O.ref_spectrum_encode(fmt, s)
+            out[f"{name}_values_{fmt}"] = v
+            out[f"{name}_meta_{fmt}"] = m
+            out[f"{name}_decoded_{fmt}"] = O.ref_spectrum_decode(fmt, v, m, s.size)
+    np.savez_compressed(os.path.join(HERE, "spectrum.npz"), **out)
+    print("wrote", os.path.join(HERE, "spectrum.npz"))
+
+
 def main() -> None:
     if not O.ref_available():
         raise SystemExit("oracle/_ref/libmsq_ref.so missing: run `make -C oracle` first")
+    write_spectrum()
+    if sys.argv[1:] == ["spectrum"]:
+        return
     lib = O.ref()
     assert lib.ref_check_codecs() == 0, lib.ref_last_error()
     x = codec_inputs()

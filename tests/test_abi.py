@@ -37,7 +37,9 @@ def test_header_declares_the_boundary():
     names = declared_symbols()
     for must in ("msq_create", "msq_encode", "msq_decode", "msq_jacobi_batched",
                  "msq_reconstruct", "msq_residual", "msq_sylvester_sweep", "msq_solve_batched",
-                 "msq_mlp_forward", "msq_mlp_backward", "msq_mlp_step", "msq_jacobi_noalloc"):
+                 "msq_mlp_forward", "msq_mlp_backward", "msq_mlp_step", "msq_jacobi_noalloc",
+                 "msq_encode_stochastic", "msq_spectrum_encode", "msq_spectrum_decode",
+                 "msq_spectrum_metadata_bytes"):
         assert must in names
 
 
@@ -58,6 +60,10 @@ def test_library_loads_without_gpu(lib_path):
     lib.msq_scale_bytes.argtypes = [ctypes.c_int, ctypes.c_size_t, ctypes.c_size_t]
     # storageBytes / scaleBytes (src/configuration.cpp:188-213), host-only
     assert lib.msq_storage_bytes(7, 33) == 17 and lib.msq_scale_bytes(7, 33, 0) == 2
+    lib.msq_spectrum_metadata_bytes.restype = ctypes.c_size_t
+    lib.msq_spectrum_metadata_bytes.argtypes = [ctypes.c_size_t]
+    # two floats (min, span of log2 s) per block of 8 root eigenvalues
+    assert lib.msq_spectrum_metadata_bytes(17) == 24
     assert lib.msq_storage_bytes(1, 10) == 20 and lib.msq_scale_bytes(1, 10, 0) == 0
     assert lib.msq_scale_bytes(8, 64, 16) == 16
 
