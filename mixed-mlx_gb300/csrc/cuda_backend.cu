@@ -110,6 +110,33 @@ CudaBasisFormat cudaBasisFormatForCliName(const std::string &name) {
   failCuda("Unsupported precision: " + name);
 }
 
+const char *cudaSpectrumFormatName(CudaSpectrumFormat format) {
+  switch (format) {
+    case CudaSpectrumFormat::Fp32: return "fp32";
+    case CudaSpectrumFormat::Fp8E4M3FnLogS: return "fp8_e4m3fn_log_s";
+    case CudaSpectrumFormat::Fp4E2M1LogS: return "fp4_e2m1_log_s";
+  }
+  return "unknown";
+}
+
+CudaSpectrumFormat cudaSpectrumFormatForCliName(const std::string &name) {
+  for (CudaSpectrumFormat f : {CudaSpectrumFormat::Fp32, CudaSpectrumFormat::Fp8E4M3FnLogS,
+                               CudaSpectrumFormat::Fp4E2M1LogS}) {
+    if (name == cudaSpectrumFormatName(f)) return f;
+  }
+  failCuda("Unsupported spectrum precision: " + name);
+}
+
+const char *cudaRoundingModeName(CudaRoundingMode mode) {
+  return mode == CudaRoundingMode::Stochastic ? "stochastic" : "nearest";
+}
+
+CudaRoundingMode cudaRoundingModeForCliName(const std::string &name) {
+  if (name == "nearest") return CudaRoundingMode::Nearest;
+  if (name == "stochastic") return CudaRoundingMode::Stochastic;
+  failCuda("--rounding requires nearest or stochastic.");
+}
+
 double cudaBasisOrthogonalityTolerance(CudaBasisFormat format) {
   switch (format) {
     case CudaBasisFormat::Fp32: return 1.0e-3;
@@ -236,14 +263,22 @@ CaseResult runCudaCase(CudaRuntime &runtime, const CudaSolverConfiguration &conf
                 "transpose basis");
   result.frozen_basis_orthogonality = orthogonality(f.as<float>());
 
+  // Quantization of the basis (and of the factor built on it): nearest, or
+  // the device quantizers' stochastic rounding with the run's seed on
+  // stream 0, as the reference quantizes its basis (src/metal_solver.cpp:219).
+  const bool stochastic = configuration.rounding_mode == CudaRoundingMode::Stochastic;
+  auto encode_basis = [&](int c, const float *src, size_t rl) {
+    return stochastic ? msq_encode_stochastic(ctx, c, src, elements, rl, configuration.rounding_seed,
+                                              0u, codes.as<uint8_t>(), scales.as<uint8_t>())
+                      : msq_encode(ctx, c, src, elements, rl, codes.as<uint8_t>(),
+                                   scales.as<uint8_t>());
+  };
   CudaBasisFormat format = configuration.basis_format;
   const int codec = codecFor(format);
   const size_t row_length = codec == MSQ_FMT_FP8_E4M3FN_ROWSCALE ? n : 0;
   if (format != CudaBasisFormat::Fp32) {
     const auto quantize_start = Clock::now();
-    runtime.check(msq_encode(ctx, codec, f.as<float>(), elements, row_length, codes.as<uint8_t>(),
-                             scales.as<uint8_t>()),
-                  "quantizeAndDecode");
+    runtime.check(encode_basis(codec, f.as<float>(), row_length), "quantizeAndDecode");
     runtime.check(msq_decode(ctx, codec, codes.as<uint8_t>(), scales.as<uint8_t>(), elements,
                              row_length, fq.as<float>()),
                   "quantizeAndDecode");
@@ -265,11 +300,54 @@ CaseResult runCudaCase(CudaRuntime &runtime, const CudaSolverConfiguration &conf
   } else {
     result.selected_basis_stage = "fp32";
   }
-  result.selected_spectrum_stage = "fp32";
+  // The root eigenvalues s = sqrt(lambda) of the initial root, optionally in
+  // log-affine storage: quantizeAndDecode of the spectrum on stream 1 and the
+  // reference's validity check (src/metal_solver.cpp:241-263).  The
+  // corrections below use the FP32 spectrum, as the reference returns to
+  // the stable roots for them (:304-310).
+  result.spectrum_precision = cudaSpectrumFormatName(configuration.spectrum_format);
+  DeviceBuffer lam0(n * sizeof(float));
+  bool quantized_spectrum = false;
+  if (configuration.spectrum_format != CudaSpectrumFormat::Fp32) {
+    const int sfmt = configuration.spectrum_format == CudaSpectrumFormat::Fp8E4M3FnLogS
+                         ? MSQ_FMT_FP8_E4M3FN
+                         : MSQ_FMT_FP4_E2M1;
+    std::vector<float> roots(n);
+    for (size_t i = 0; i < n; ++i) roots[i] = std::sqrt(eig[i]);
+    DeviceBuffer s_in(n * sizeof(float)), s_out(n * sizeof(float)), s_codes(n + 16),
+        s_meta(msq_spectrum_metadata_bytes(n) + 16);
+    copyIn(s_in.as<float>(), roots.data(), n * sizeof(float));
+    runtime.check(msq_spectrum_encode(ctx, sfmt, s_in.as<float>(), n,
+                                      stochastic ? MSQ_ROUND_STOCHASTIC : MSQ_ROUND_NEAREST,
+                                      configuration.rounding_seed, 1u, s_codes.as<uint8_t>(),
+                                      s_meta.as<float>()),
+                  "quantizeAndDecode spectrum");
+    runtime.check(msq_spectrum_decode(ctx, sfmt, s_codes.as<uint8_t>(), s_meta.as<float>(), n,
+                                      s_out.as<float>()),
+                  "quantizeAndDecode spectrum");
+    runtime.check(msq_synchronize(ctx), "quantizeAndDecode spectrum");
+    std::vector<float> quantized(n);
+    copyOut(quantized.data(), s_out.as<float>(), n * sizeof(float));
+    bool usable = true;
+    for (float value : quantized) usable = usable && value > 0.0f && std::isfinite(value);
+    if (usable) {
+      for (size_t i = 0; i < n; ++i) quantized[i] *= quantized[i];  // lambda = s^2
+      copyIn(lam0.as<float>(), quantized.data(), n * sizeof(float));
+      quantized_spectrum = true;
+      result.selected_spectrum_stage = cudaSpectrumFormatName(configuration.spectrum_format);
+    } else {
+      result.selected_spectrum_stage =
+          std::string(cudaSpectrumFormatName(configuration.spectrum_format)) + "_rejected_to_fp32";
+      ++result.precision_escalations;
+    }
+  } else {
+    result.selected_spectrum_stage = "fp32";
+  }
 
   // Initial root X0 = W W^T, W = V diag(lambda^(1/4)).
   const auto initial_start = Clock::now();
-  runtime.check(msq_make_factor(ctx, v.as<float>(), lam.as<float>(), &nn, &off, 1, f.as<float>()),
+  runtime.check(msq_make_factor(ctx, v.as<float>(), quantized_spectrum ? lam0.as<float>() : lam.as<float>(),
+                                &nn, &off, 1, f.as<float>()),
                 "prepareFrozenSpectralFactor");
   if (format == CudaBasisFormat::Fp32) {
     runtime.check(msq_reconstruct(ctx, MSQ_FMT_FP32, f.as<float>(), nullptr, &nn, &off, 1,
@@ -278,9 +356,7 @@ CaseResult runCudaCase(CudaRuntime &runtime, const CudaSolverConfiguration &conf
   } else {
     const int fcodec = codecFor(format);
     const size_t frow = fcodec == MSQ_FMT_FP8_E4M3FN_ROWSCALE ? n : 0;
-    runtime.check(msq_encode(ctx, fcodec, f.as<float>(), elements, frow, codes.as<uint8_t>(),
-                             scales.as<uint8_t>()),
-                  "quantize factor");
+    runtime.check(encode_basis(fcodec, f.as<float>(), frow), "quantize factor");
     runtime.check(msq_reconstruct(ctx, fcodec, codes.as<uint8_t>(), scales.as<float>(), &nn, &off,
                                   1, x_hi.as<float>()),
                   "reconstructLowFactorTiled");
@@ -382,6 +458,9 @@ int runCuda(const CudaRunOptions &options, const PreparedMatrix &matrix) {
   CudaRuntime runtime(options.device);
   CudaSolverConfiguration configuration;
   configuration.basis_format = options.basis_format;
+  configuration.spectrum_format = options.spectrum_format;
+  configuration.rounding_mode = options.rounding_mode;
+  configuration.rounding_seed = options.rounding_seed;
   CudaProblem problem;
   problem.order = matrix.order;
   problem.condition = matrix.condition;
@@ -394,6 +473,7 @@ int runCuda(const CudaRunOptions &options, const PreparedMatrix &matrix) {
   std::cout << std::setprecision(6) << "case=" << result.name
             << " solver_backend=" << result.solver_backend << " n=" << result.order
             << " basis=" << result.selected_basis_stage
+            << " spectrum=" << result.selected_spectrum_stage
             << " status=" << result.status << " iterations=" << (result.history.size() - 1)
             << std::scientific << " final_residual=" << result.final_residual
             << " basis_orthogonality=" << result.frozen_basis_orthogonality

@@ -109,6 +109,21 @@ CudaBasisFormat cudaBasisFormatForCliName(const std::string &name);
 // basisOrthogonalityTolerance (src/configuration.cpp:109-118) per format.
 double cudaBasisOrthogonalityTolerance(CudaBasisFormat format);
 
+// Storage of the root eigenvalues used by the initial root: FP32, or the
+// log-affine formats of the reference's fp8_e4m3fn_log_s / fp4_e2m1_log_s
+// spectrum precisions (src/precision.hpp:87-92).
+enum class CudaSpectrumFormat { Fp32, Fp8E4M3FnLogS, Fp4E2M1LogS };
+
+const char *cudaSpectrumFormatName(CudaSpectrumFormat format);
+CudaSpectrumFormat cudaSpectrumFormatForCliName(const std::string &name);
+
+// --rounding nearest|stochastic (RoundingMode, src/precision.hpp:22): how the
+// basis and the spectrum are quantized.
+enum class CudaRoundingMode { Nearest, Stochastic };
+
+const char *cudaRoundingModeName(CudaRoundingMode mode);
+CudaRoundingMode cudaRoundingModeForCliName(const std::string &name);
+
 class CudaRuntime {
  public:
   explicit CudaRuntime(int device = 0);
@@ -125,6 +140,9 @@ class CudaRuntime {
 
 struct CudaSolverConfiguration {
   CudaBasisFormat basis_format = CudaBasisFormat::Fp32;
+  CudaSpectrumFormat spectrum_format = CudaSpectrumFormat::Fp32;
+  CudaRoundingMode rounding_mode = CudaRoundingMode::Nearest;
+  uint32_t rounding_seed = 0;        // --rounding-seed (stochastic rounding)
   double jacobi_tolerance = 1.0e-7;  // off(A) <= tol * ||A||_F
   int jacobi_max_sweeps = 15;
   bool orthogonality_gate = true;    // reject a basis that fails the tolerance
@@ -149,6 +167,9 @@ CaseResult runCudaCase(CudaRuntime &runtime, const CudaSolverConfiguration &conf
 
 struct CudaRunOptions {
   CudaBasisFormat basis_format = CudaBasisFormat::Fp32;
+  CudaSpectrumFormat spectrum_format = CudaSpectrumFormat::Fp32;
+  CudaRoundingMode rounding_mode = CudaRoundingMode::Nearest;
+  uint32_t rounding_seed = 0;
   size_t max_iterations = 8;
   double tolerance = 1.0e-12;
   bool enforce_policy = true;

@@ -3,6 +3,8 @@
 // (column-major), optionally n*n FP64 reference root.  Prints key=value.
 // Usage: cuda_backend_check <matrix.bin> <basis: fp32|bf16|fp8_e4m3fn_rowscale|mxfp4_e2m1>
 //                           <tolerance> <max_iterations>
+//                           [spectrum: fp32|fp8_e4m3fn_log_s|fp4_e2m1_log_s]
+//                           [rounding: nearest|stochastic] [rounding seed]
 #include <cstdint>
 #include <cstdio>
 #include <cstdlib>
@@ -34,6 +36,10 @@ int main(int argc, char **argv) {
     mixed_sqrt::CudaRuntime runtime(0);
     mixed_sqrt::CudaSolverConfiguration config;
     config.basis_format = mixed_sqrt::cudaBasisFormatForCliName(argv[2]);
+    // optional: spectrum precision, rounding mode, rounding seed
+    if (argc > 5) config.spectrum_format = mixed_sqrt::cudaSpectrumFormatForCliName(argv[5]);
+    if (argc > 6) config.rounding_mode = mixed_sqrt::cudaRoundingModeForCliName(argv[6]);
+    if (argc > 7) config.rounding_seed = static_cast<uint32_t>(std::strtoul(argv[7], nullptr, 0));
     mixed_sqrt::CudaProblem problem;
     problem.order = m.order;
     problem.tolerance = std::atof(argv[3]);
@@ -47,6 +53,7 @@ int main(int argc, char **argv) {
               << " final_forward_error=" << r.final_forward_error
               << " initial_residual=" << r.history.front().residual
               << " selected_basis_stage=" << r.selected_basis_stage
+              << " selected_spectrum_stage=" << r.selected_spectrum_stage
               << " precision_escalations=" << r.precision_escalations
               << " basis_orthogonality=" << r.frozen_basis_orthogonality
               << " quantized_basis_orthogonality=" << r.quantized_basis_orthogonality

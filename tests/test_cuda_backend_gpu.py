@@ -14,7 +14,7 @@ ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 EXE = os.path.join(ROOT, "tests", "cpp", "cuda_backend_check")
 
 
-def _run(tmp_path, a, basis, tol, iters, with_ref=True):
+def _run(tmp_path, a, basis, tol, iters, with_ref=True, extra=()):
     n = a.shape[0]
     path = tmp_path / f"m{n}_{basis}.bin"
     with open(path, "wb") as f:
@@ -22,8 +22,8 @@ def _run(tmp_path, a, basis, tol, iters, with_ref=True):
         f.write(np.asfortranarray(a, np.float64).tobytes(order="F"))
         if with_ref:
             f.write(np.asfortranarray(O.reference_root(a), np.float64).tobytes(order="F"))
-    out = subprocess.run([EXE, str(path), basis, str(tol), str(iters)], capture_output=True,
-                         text=True, timeout=300)
+    out = subprocess.run([EXE, str(path), basis, str(tol), str(iters), *map(str, extra)],
+                         capture_output=True, text=True, timeout=300)
     fields = dict(kv.split("=", 1) for kv in out.stdout.split()) if out.returncode == 0 else {}
     return out.returncode, fields, out.stderr
 
@@ -62,3 +62,32 @@ def test_budget_exhausted_status(tmp_path):
     rc, r, err = _run(tmp_path, a, "bf16", 1e-14, 0)
     assert rc == 0 and r["status"] in ("budget_exhausted", "converged")
     assert int(r["iterations"]) == 0
+
+
+@pytest.mark.parametrize("basis,spectrum,rounding", [
+    ("bf16", "fp8_e4m3fn_log_s", "stochastic"),
+    ("fp8_e4m3fn_rowscale", "fp4_e2m1_log_s", "nearest"),
+    ("mxfp4_e2m1", "fp8_e4m3fn_log_s", "stochastic"),
+    ("fp32", "fp4_e2m1_log_s", "stochastic"),
+])
+def test_log_spectrum_and_stochastic_rounding_reach_tolerance(tmp_path, basis, spectrum, rounding):
+    """A log-affine spectrum and stochastic rounding change only the initial
+    root (the corrections use the FP32 basis and spectrum, as the reference's
+    do), so the case still converges to the FP64-oracle root."""
+    a = O.controlled(96, 1e2)
+    rc, r, err = _run(tmp_path, a, basis, 1e-12, 16, extra=(spectrum, rounding, 0x1234))
+    assert rc == 0, err
+    assert r["status"] == "converged", r
+    assert float(r["final_residual"]) <= 1e-12
+    assert float(r["final_forward_error"]) < 1e-10, r
+    assert r["selected_spectrum_stage"] in (spectrum, spectrum + "_rejected_to_fp32")
+
+
+def test_stochastic_rounding_is_reproducible_per_seed(tmp_path):
+    a = O.controlled(64, 1e3)
+    runs = [_run(tmp_path, a, "bf16", 1e-12, 0, extra=("fp8_e4m3fn_log_s", "stochastic", seed))
+            for seed in (7, 7, 8)]
+    assert all(rc == 0 for rc, _, _ in runs), [e for _, _, e in runs]
+    first, again, other = (r["initial_residual"] for _, r, _ in runs)
+    assert first == again                 # same seed, same bits
+    assert first != other                 # another seed, other codes
