@@ -291,6 +291,30 @@ int msq_sylvester_sweep(msq_ctx *ctx, int gemm_format, const float *vectors,
                         const int32_t *n, const int64_t *offset, int count,
                         float *x_hi, float *x_lo, float *workspace);
 
+/* msq_native_sylvester_sweep: one correction of the reference's
+ * native-quantized mode (--correction native_quantized, refineNativeStaged /
+ * refineNativePerStage, src/metal_runtime.cpp:292-411, driven at
+ * src/metal_solver.cpp:829-848): every operand and intermediate is stored in
+ * `format` (any msq_encode format; MSQ_FMT_FP32 keeps FP32):
+ *   R_q = Q(R), W1 = Q(Vt R_q), W2 = Q(W1 V), C = Q(W2_ij / (s_i + s_j)),
+ *   W1 = Q(V C), E = Q(W1 Vt),   X <- X + (E + E^T)/2 (float-float),
+ * where Q quantizes an FP32 matrix to `format` with nearest rounding (per
+ * matrix; row length n for the row-scaled format) and decodes it, and the
+ * products are FP32 with each element an FMA chain over the inner index in
+ * order (the reference's matmul kernels on decoded operands,
+ * metal_mixed_sqrt.metal:39-56).  vectors / vectors_t: the decoded stored
+ * basis V and transposed basis V^T (stored separately, as the reference
+ * stores them); spectrum: the decoded root eigenvalues s (sum(n) floats,
+ * matrix i at the prefix sum of n).  workspace: 3 * E floats, E = max over
+ * matrices of offset + n^2; codes / scales: msq_storage_bytes(format, n^2)
+ * and msq_scale_bytes(format, n^2, n) bytes for the largest n (16-byte
+ * aligned; unused for MSQ_FMT_FP32).                                      */
+int msq_native_sylvester_sweep(msq_ctx *ctx, int format, const float *vectors,
+                               const float *vectors_t, const float *spectrum,
+                               const float *residual, const int32_t *n,
+                               const int64_t *offset, int count, float *x_hi, float *x_lo,
+                               float *workspace, uint8_t *codes, uint8_t *scales);
+
 /* ---- whole-pipeline batched solve ------------------------------------------
  * The GPU-resident solve of solveGpuResidentSpd (src/metal_solver.cpp:92-336)
  * over a batch: Jacobi -> (quantize W) -> reconstruct -> Sylvester sweeps ->

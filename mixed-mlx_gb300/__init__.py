@@ -83,6 +83,8 @@ _SIGS = {
     "msq_spectrum_encode": (ctypes.c_int, [_P, ctypes.c_int, _P, ctypes.c_size_t, ctypes.c_int,
                                            ctypes.c_uint32, ctypes.c_uint32, _P, _P]),
     "msq_spectrum_decode": (ctypes.c_int, [_P, ctypes.c_int, _P, _P, ctypes.c_size_t, _P]),
+    "msq_native_sylvester_sweep": (ctypes.c_int, [_P, ctypes.c_int, _P, _P, _P, _P, _P, _P,
+                                                  ctypes.c_int, _P, _P, _P, _P, _P]),
     "msq_jacobi_batched": (ctypes.c_int, [_P, _P, _P, _P, _P, _P, ctypes.c_int,
                                           ctypes.c_double, ctypes.c_int, _P, _P]),
     "msq_jacobi_noalloc": (ctypes.c_int, [_P, _P, _P, ctypes.c_int, ctypes.c_double,
@@ -352,6 +354,21 @@ class Context:
                                       batch.n.ctypes.data, batch.offset.ctypes.data,
                                       batch.count, _ptr(r), _ptr(norms)), "msq_residual")
         return r, norms
+
+    def native_sylvester_sweep(self, fmt: int, v, vt, s, r, batch: Batch, x_hi, x_lo):
+        """One native-quantized correction (every operand and intermediate
+        in `fmt`); v / vt: decoded stored V and V^T, s: decoded root
+        eigenvalues (sum of n floats); updates x_hi / x_lo."""
+        torch = self.torch
+        big = int(max(batch.n)) ** 2
+        workspace = torch.empty(3 * batch.total, dtype=torch.float32, device=v.device)
+        codes = torch.empty(max(storage_bytes(fmt, big), 16) + 16, dtype=torch.uint8, device=v.device)
+        scales = torch.empty(max(scale_bytes(fmt, big, int(max(batch.n))), 16) + 16,
+                             dtype=torch.uint8, device=v.device)
+        self.check(lib().msq_native_sylvester_sweep(
+            self.handle, fmt, _ptr(v), _ptr(vt), _ptr(s), _ptr(r), batch.n.ctypes.data,
+            batch.offset.ctypes.data, batch.count, _ptr(x_hi), _ptr(x_lo), _ptr(workspace),
+            _ptr(codes), _ptr(scales)), "msq_native_sylvester_sweep")
 
     def sylvester_sweep(self, gemm_fmt: int, v, w, r, batch: Batch, x_hi, x_lo, workspace=None):
         if workspace is None:

@@ -191,7 +191,8 @@ CaseResult runCudaCase(CudaRuntime &runtime, const CudaSolverConfiguration &conf
   result.precision = cudaBasisFormatName(configuration.basis_format);
   result.basis_precision = result.precision;
   result.spectrum_precision = "fp32";
-  result.correction_mode = "fp32_reorthogonalized";
+  result.correction_mode =
+      configuration.native_correction ? "native_quantized" : "fp32_reorthogonalized";
   result.kernel_path = "tiled";
   result.precision_policy = configuration.basis_format == CudaBasisFormat::Fp32 ||
                                     configuration.basis_format == CudaBasisFormat::Bf16
@@ -395,19 +396,99 @@ CaseResult runCudaCase(CudaRuntime &runtime, const CudaSolverConfiguration &conf
     return relativeErrorOf(root, *problem.supplied_reference);
   };
 
+  // Native-quantized corrections (refineNativeStaged, the frozen-factor loop
+  // of src/metal_solver.cpp:829-915): the stored basis V and V^T and the
+  // stored spectrum in the selected formats (nearest, as copyToStorage /
+  // copySpectrumToStorage store them), every stage of the correction in the
+  // basis format.
+  const bool native = configuration.native_correction;
+  const int ncodec = codecFor(format);
+  DeviceBuffer nv(native ? elements * sizeof(float) : 0), nvt(native ? elements * sizeof(float) : 0),
+      ns(native ? n * sizeof(float) : 0), nws(native ? 3 * elements * sizeof(float) : 0),
+      best_hi(native ? elements * sizeof(float) : 0), best_lo(native ? elements * sizeof(float) : 0);
+  if (native) {
+    runtime.check(msq_make_factor(ctx, v.as<float>(), ones.as<float>(), &nn, &off, 1, nvt.as<float>()),
+                  "transpose basis");
+    const size_t nrow = ncodec == MSQ_FMT_FP8_E4M3FN_ROWSCALE ? n : 0;
+    auto store = [&](const float *src, float *dst) {
+      if (ncodec == MSQ_FMT_FP32) {
+        // the context's stream is idle here (synchronised above)
+        if (src != dst &&
+            cudaMemcpy(dst, src, elements * sizeof(float), cudaMemcpyDeviceToDevice) != cudaSuccess)
+          failCuda("copyToStorage failed");
+        return;
+      }
+      runtime.check(msq_encode(ctx, ncodec, src, elements, nrow, codes.as<uint8_t>(), scales.as<uint8_t>()),
+                    "copyToStorage");
+      runtime.check(msq_decode(ctx, ncodec, codes.as<uint8_t>(), scales.as<uint8_t>(), elements, nrow, dst),
+                    "unpackFromStorage");
+    };
+    runtime.check(msq_synchronize(ctx), "transpose basis");
+    store(v.as<float>(), nv.as<float>());
+    store(nvt.as<float>(), nvt.as<float>());
+    std::vector<float> roots(n);
+    if (quantized_spectrum) {
+      copyOut(roots.data(), lam0.as<float>(), n * sizeof(float));
+      for (float &x : roots) x = std::sqrt(x);  // lambda0 = s_q^2 holds the stored roots squared
+    } else {
+      for (size_t i = 0; i < n; ++i) roots[i] = std::sqrt(eig[i]);
+    }
+    copyIn(ns.as<float>(), roots.data(), n * sizeof(float));
+    runtime.check(msq_synchronize(ctx), "native correction operands");
+  }
+
   double res = residual();
   result.history.push_back({0, res, forward_error(root_now())});
-  size_t iteration = 0;
+  double best = res;
+  bool best_saved = false;
+  size_t iteration = 0, flat_steps = 0;
   while (res > problem.tolerance && iteration < problem.max_iterations && std::isfinite(res)) {
     const auto t0 = Clock::now();
-    runtime.check(msq_sylvester_sweep(ctx, MSQ_FMT_FP32, v.as<float>(), lam.as<float>(),
-                                      r.as<float>(), &nn, &off, 1, x_hi.as<float>(),
-                                      x_lo.as<float>(), ws.as<float>()),
-                  "refineUpdateAndMeasure");
+    if (native) {
+      runtime.check(msq_native_sylvester_sweep(ctx, ncodec, nv.as<float>(), nvt.as<float>(),
+                                               ns.as<float>(), r.as<float>(), &nn, &off, 1,
+                                               x_hi.as<float>(), x_lo.as<float>(), nws.as<float>(),
+                                               codes.as<uint8_t>(), scales.as<uint8_t>()),
+                    "refineNativeStaged");
+    } else {
+      runtime.check(msq_sylvester_sweep(ctx, MSQ_FMT_FP32, v.as<float>(), lam.as<float>(),
+                                        r.as<float>(), &nn, &off, 1, x_hi.as<float>(),
+                                        x_lo.as<float>(), ws.as<float>()),
+                    "refineUpdateAndMeasure");
+    }
+    const double previous_best = best;
     res = residual();
     result.times.correction_gpu_seconds += since(t0);
     ++iteration;
     result.history.push_back({iteration, res, forward_error(root_now())});
+    if (!std::isfinite(res)) break;
+    if (native && res < best) {
+      best = res;
+      // keep the best root (the stagnation policy returns it)
+      if (cudaMemcpy(best_hi.as<float>(), x_hi.as<float>(), elements * sizeof(float),
+                     cudaMemcpyDeviceToDevice) != cudaSuccess ||
+          cudaMemcpy(best_lo.as<float>(), x_lo.as<float>(), elements * sizeof(float),
+                     cudaMemcpyDeviceToDevice) != cudaSuccess)
+        failCuda("best root copy failed");
+      best_saved = true;
+    }
+    if (native && configuration.stop_on_stagnation && res > problem.tolerance) {
+      const double improvement = previous_best > 0.0 ? (previous_best - res) / previous_best : 0.0;
+      flat_steps = improvement > configuration.min_relative_improvement ? 0 : flat_steps + 1;
+      result.stagnation_steps = flat_steps;
+      if (flat_steps >= configuration.stagnation_window) break;
+    }
+  }
+  if (native && configuration.stop_on_stagnation && best_saved &&
+      best < result.history.back().residual) {
+    // the stagnation policy reports the best root (src/metal_solver.cpp:905-915)
+    if (cudaMemcpy(x_hi.as<float>(), best_hi.as<float>(), elements * sizeof(float),
+                   cudaMemcpyDeviceToDevice) != cudaSuccess ||
+        cudaMemcpy(x_lo.as<float>(), best_lo.as<float>(), elements * sizeof(float),
+                   cudaMemcpyDeviceToDevice) != cudaSuccess)
+      failCuda("best root copy failed");
+    res = best;
+    result.history.push_back({iteration, best, forward_error(root_now())});
   }
   result.times.mixed_total_seconds = since(mixed_start);
   const std::vector<double> root = root_now();
@@ -461,6 +542,10 @@ int runCuda(const CudaRunOptions &options, const PreparedMatrix &matrix) {
   configuration.spectrum_format = options.spectrum_format;
   configuration.rounding_mode = options.rounding_mode;
   configuration.rounding_seed = options.rounding_seed;
+  configuration.native_correction = options.native_correction;
+  configuration.stop_on_stagnation = options.stop_on_stagnation;
+  configuration.stagnation_window = options.stagnation_window;
+  configuration.min_relative_improvement = options.min_relative_improvement;
   CudaProblem problem;
   problem.order = matrix.order;
   problem.condition = matrix.condition;

@@ -91,6 +91,7 @@ struct CaseResult {
   double best_forward_error = 0.0;
   double final_residual = 0.0;
   double final_forward_error = 0.0;
+  size_t stagnation_steps = 0;
   std::vector<IterationMeasurement> history;
   PhaseTimes times;
 };
@@ -143,6 +144,15 @@ struct CudaSolverConfiguration {
   CudaSpectrumFormat spectrum_format = CudaSpectrumFormat::Fp32;
   CudaRoundingMode rounding_mode = CudaRoundingMode::Nearest;
   uint32_t rounding_seed = 0;        // --rounding-seed (stochastic rounding)
+  // --correction native_quantized (CorrectionMode): corrections with every
+  // operand and intermediate stored in the basis format (refineNativeStaged),
+  // and its stopping policy: a fixed budget, or --native-stopping stagnation
+  // (stop after `stagnation_window` corrections in a row that improve the best
+  // residual by no more than `min_relative_improvement`, keep the best root).
+  bool native_correction = false;
+  bool stop_on_stagnation = false;
+  size_t stagnation_window = 4;              // the reference's defaults
+  double min_relative_improvement = 1.0e-3;
   double jacobi_tolerance = 1.0e-7;  // off(A) <= tol * ||A||_F
   int jacobi_max_sweeps = 15;
   bool orthogonality_gate = true;    // reject a basis that fails the tolerance
@@ -170,6 +180,10 @@ struct CudaRunOptions {
   CudaSpectrumFormat spectrum_format = CudaSpectrumFormat::Fp32;
   CudaRoundingMode rounding_mode = CudaRoundingMode::Nearest;
   uint32_t rounding_seed = 0;
+  bool native_correction = false;
+  bool stop_on_stagnation = false;
+  size_t stagnation_window = 4;
+  double min_relative_improvement = 1.0e-3;
   size_t max_iterations = 8;
   double tolerance = 1.0e-12;
   bool enforce_policy = true;

@@ -436,6 +436,59 @@ int transpose(msq_ctx *ctx, const DeviceBatch *b, const float *src, float *dst) 
   return launched(ctx, "transpose");
 }
 
+// C = A B for one n x n column-major matrix, each element the FMA chain
+// sum = fma(A[r, k], B[k, c], sum) over k = 0..n-1 in order, as the
+// reference's matmul kernels accumulate (metal_mixed_sqrt.metal:39-56,
+// matmul_tiled_*: decoded operands, FP32).  16 x 16 outputs per CTA, K
+// staged through shared memory 16 at a time (the chain order is kept).
+namespace {
+constexpr int kMmTile = 16;
+
+__global__ void __launch_bounds__(kMmTile * kMmTile)
+matmulFmaKernel(const float *__restrict__ a, const float *__restrict__ b, float *__restrict__ c,
+                int n) {
+  __shared__ float as[kMmTile][kMmTile + 1];
+  __shared__ float bs[kMmTile][kMmTile + 1];
+  const int tr = threadIdx.x, tc = threadIdx.y;  // row fastest: coalesced column reads
+  const int row = blockIdx.x * kMmTile + tr, col = blockIdx.y * kMmTile + tc;
+  float sum = 0.0f;
+  for (int k0 = 0; k0 < n; k0 += kMmTile) {
+    // A[row, k0 + tc] and B[k0 + tr, col]
+    as[tr][tc] = row < n && k0 + tc < n ? a[row + static_cast<int64_t>(k0 + tc) * n] : 0.0f;
+    bs[tr][tc] = k0 + tr < n && col < n ? b[(k0 + tr) + static_cast<int64_t>(col) * n] : 0.0f;
+    __syncthreads();
+    const int kend = min(kMmTile, n - k0);
+    for (int k = 0; k < kend; ++k) sum = fmaf(as[tr][k], bs[k][tc], sum);
+    __syncthreads();
+  }
+  if (row < n && col < n) c[row + static_cast<int64_t>(col) * n] = sum;
+}
+
+// C_ij = W_ij / (s_i + s_j) (diagonal_sylvester_*, metal_mixed_sqrt.metal:58-74).
+__global__ void diagonalSylvesterKernel(const float *__restrict__ w, const float *__restrict__ s,
+                                        float *__restrict__ c, int n) {
+  const int64_t total = static_cast<int64_t>(n) * n;
+  for (int64_t idx = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; idx < total;
+       idx += static_cast<int64_t>(gridDim.x) * blockDim.x) {
+    const int i = static_cast<int>(idx % n), j = static_cast<int>(idx / n);
+    c[idx] = __fdiv_rn(w[idx], s[i] + s[j]);
+  }
+}
+}  // namespace
+
+int matmulFma(msq_ctx *ctx, const float *a, const float *b, float *c, int n) {
+  const dim3 grid((n + kMmTile - 1) / kMmTile, (n + kMmTile - 1) / kMmTile);
+  matmulFmaKernel<<<grid, dim3(kMmTile, kMmTile), 0, ctx->stream>>>(a, b, c, n);
+  return launched(ctx, "native matmul");
+}
+
+int diagonalSylvester(msq_ctx *ctx, const float *w, const float *s, float *c, int n) {
+  const int64_t total = static_cast<int64_t>(n) * n;
+  const int grid = static_cast<int>(std::min<int64_t>((total + 255) / 256, kSmCount * 8));
+  diagonalSylvesterKernel<<<grid, 256, 0, ctx->stream>>>(w, s, c, n);
+  return launched(ctx, "native diagonal sylvester");
+}
+
 int symmetricAdd(msq_ctx *ctx, const DeviceBatch *b, float *x_hi, float *x_lo, const float *e) {
   const int4 *work;
   int items;

@@ -15,6 +15,7 @@
  *  - the FP8-E4M3 per-row-scale format (no reference counterpart);
  *  - the device quantizers' stochastic rounding and the log-spectrum
  *    storage of the root eigenvalues (restated from the shader source);
+ *  - one correction of the native-quantized mode;
  *  - the parallel-order two-sided Jacobi of metal_mixed_sqrt.metal:1319-1444
  *    with the round-robin schedule of src/metal_solver.cpp:50-79, angles in
  *    FP64, FP32 storage, convergence-tested;
@@ -436,6 +437,59 @@ int msqo_spectrum_decode(int format, const uint8_t *values, const float *metadat
     out[i] = exp2f(lo + span * d / maximum);
   }
   return 0;
+}
+
+/* ----------------------------------------- native-quantized correction */
+
+/* C = A B (n x n, column-major), each element the FMA chain over the inner
+ * index in order (matmul_f32 and the low-precision matmuls on decoded
+ * operands, metal_mixed_sqrt.metal:39-56). */
+static void matmul_fma(const float *a, const float *b, float *c, unsigned n) {
+  for (unsigned col = 0; col < n; ++col)
+    for (unsigned row = 0; row < n; ++row) {
+      float sum = 0.0f;
+      for (unsigned k = 0; k < n; ++k) sum = fmaf(a[row + (size_t)k * n], b[k + (size_t)col * n], sum);
+      c[row + (size_t)col * n] = sum;
+    }
+}
+
+/* x quantized to `format` (nearest; row length n for format 8) and decoded */
+static int quantize_decode(int format, float *x, unsigned n, uint8_t *codes, uint8_t *scales) {
+  if (format == 0) return 0;
+  size_t e = (size_t)n * n, rl = format == 8 ? n : 0;
+  if (msqo_encode(format, x, e, rl, codes, scales)) return 1;
+  return msqo_decode(format, codes, scales, e, rl, x);
+}
+
+/* One correction of the native-quantized mode (refineNativeStaged,
+ * src/metal_runtime.cpp:313-411; driven at src/metal_solver.cpp:829-848):
+ * R_q = Q(R), W1 = Q(Vt R_q), W2 = Q(W1 V), C = Q(W2_ij / (s_i + s_j)),
+ * W1 = Q(V C), E = Q(W1 Vt); e_out receives E.  v / vt are the decoded
+ * stored basis and transposed basis, s the decoded root eigenvalues. */
+int msqo_native_correction(int format, const float *v, const float *vt, const float *s,
+                           const float *r, unsigned n, float *e_out) {
+  size_t e = (size_t)n * n;
+  float *rq = malloc(e * 4), *w1 = malloc(e * 4), *w2 = malloc(e * 4);
+  uint8_t *codes = malloc(e * 4 + 16), *scales = malloc(e + 4 * (size_t)n + 16);
+  int rc = 1;
+  if (!rq || !w1 || !w2 || !codes || !scales) goto done;
+  memcpy(rq, r, e * 4);
+  if (quantize_decode(format, rq, n, codes, scales)) goto done;
+  matmul_fma(vt, rq, w1, n);
+  if (quantize_decode(format, w1, n, codes, scales)) goto done;
+  matmul_fma(w1, v, w2, n);
+  if (quantize_decode(format, w2, n, codes, scales)) goto done;
+  for (unsigned j = 0; j < n; ++j)
+    for (unsigned i = 0; i < n; ++i) w1[i + (size_t)j * n] = w2[i + (size_t)j * n] / (s[i] + s[j]);
+  if (quantize_decode(format, w1, n, codes, scales)) goto done;
+  matmul_fma(v, w1, w2, n);
+  if (quantize_decode(format, w2, n, codes, scales)) goto done;
+  matmul_fma(w2, vt, e_out, n);
+  if (quantize_decode(format, e_out, n, codes, scales)) goto done;
+  rc = 0;
+done:
+  free(rq); free(w1); free(w2); free(codes); free(scales);
+  return rc;
 }
 
 /* ---------------------------------------------------------------- Jacobi */

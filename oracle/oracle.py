@@ -74,6 +74,7 @@ def olib() -> ctypes.CDLL:
         lib.msqo_spectrum_encode.argtypes = [ctypes.c_int, _P, ctypes.c_size_t, ctypes.c_int,
                                              ctypes.c_uint32, ctypes.c_uint32, _P, _P]
         lib.msqo_spectrum_decode.argtypes = [ctypes.c_int, _P, _P, ctypes.c_size_t, _P]
+        lib.msqo_native_correction.argtypes = [ctypes.c_int, _P, _P, _P, _P, ctypes.c_uint, _P]
         _ORACLE = lib
     return _ORACLE
 
@@ -153,6 +154,20 @@ def spectrum_decode(fmt: int, values: np.ndarray, meta: np.ndarray, elements: in
                                    out.ctypes.data):
         raise ValueError("oracle spectrum decode failed")
     return out
+
+
+def native_correction(fmt: int, v: np.ndarray, vt: np.ndarray, s: np.ndarray, r: np.ndarray):
+    """One native-quantized correction E (refineNativeStaged restated); all
+    matrices n x n FP32 column-major, s the n root eigenvalues."""
+    n = v.shape[0]
+    f = lambda m: np.asfortranarray(m, dtype=np.float32)
+    V, VT, R = f(v), f(vt), f(r)
+    S = np.ascontiguousarray(s, dtype=np.float32)
+    E = np.zeros((n, n), dtype=np.float32, order="F")
+    if olib().msqo_native_correction(fmt, V.ctypes.data, VT.ctypes.data, S.ctypes.data,
+                                     R.ctypes.data, n, E.ctypes.data):
+        raise ValueError("oracle native correction failed")
+    return E
 
 
 def jacobi_pair(order: int, rnd: int, pair: int) -> tuple[int, int]:

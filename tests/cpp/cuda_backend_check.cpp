@@ -5,12 +5,15 @@
 //                           <tolerance> <max_iterations>
 //                           [spectrum: fp32|fp8_e4m3fn_log_s|fp4_e2m1_log_s]
 //                           [rounding: nearest|stochastic] [rounding seed]
+//                           [correction: fp32_reorthogonalized|native_quantized]
+//                           [native stopping: fixed_budget|stagnation]
 #include <cstdint>
 #include <cstdio>
 #include <cstdlib>
 #include <exception>
 #include <iomanip>
 #include <iostream>
+#include <string>
 #include <vector>
 
 #include "cuda_backend.hpp"
@@ -40,6 +43,10 @@ int main(int argc, char **argv) {
     if (argc > 5) config.spectrum_format = mixed_sqrt::cudaSpectrumFormatForCliName(argv[5]);
     if (argc > 6) config.rounding_mode = mixed_sqrt::cudaRoundingModeForCliName(argv[6]);
     if (argc > 7) config.rounding_seed = static_cast<uint32_t>(std::strtoul(argv[7], nullptr, 0));
+    // optional: correction mode (fp32_reorthogonalized | native_quantized) and
+    // native stopping policy (fixed_budget | stagnation)
+    if (argc > 8) config.native_correction = std::string(argv[8]) == "native_quantized";
+    if (argc > 9) config.stop_on_stagnation = std::string(argv[9]) == "stagnation";
     mixed_sqrt::CudaProblem problem;
     problem.order = m.order;
     problem.tolerance = std::atof(argv[3]);
@@ -54,6 +61,9 @@ int main(int argc, char **argv) {
               << " initial_residual=" << r.history.front().residual
               << " selected_basis_stage=" << r.selected_basis_stage
               << " selected_spectrum_stage=" << r.selected_spectrum_stage
+              << " correction_mode=" << r.correction_mode
+              << " stagnation_steps=" << r.stagnation_steps
+              << " best_residual=" << r.best_residual
               << " precision_escalations=" << r.precision_escalations
               << " basis_orthogonality=" << r.frozen_basis_orthogonality
               << " quantized_basis_orthogonality=" << r.quantized_basis_orthogonality

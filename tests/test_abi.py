@@ -39,7 +39,7 @@ def test_header_declares_the_boundary():
                  "msq_reconstruct", "msq_residual", "msq_sylvester_sweep", "msq_solve_batched",
                  "msq_mlp_forward", "msq_mlp_backward", "msq_mlp_step", "msq_jacobi_noalloc",
                  "msq_encode_stochastic", "msq_spectrum_encode", "msq_spectrum_decode",
-                 "msq_spectrum_metadata_bytes"):
+                 "msq_spectrum_metadata_bytes", "msq_native_sylvester_sweep"):
         assert must in names
 
 

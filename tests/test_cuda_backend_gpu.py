@@ -91,3 +91,32 @@ def test_stochastic_rounding_is_reproducible_per_seed(tmp_path):
     first, again, other = (r["initial_residual"] for _, r, _ in runs)
     assert first == again                 # same seed, same bits
     assert first != other                 # another seed, other codes
+
+
+@pytest.mark.parametrize("basis", ["fp32", "bf16"])
+def test_native_quantized_correction_fixed_budget(tmp_path, basis):
+    """--correction native_quantized: every stage of the correction in the
+    basis format.  In FP32 it converges like the FP32 correction; in BF16 it
+    lowers the residual until BF16 storage stops it."""
+    a = O.controlled(64, 1e2)
+    rc, r, err = _run(tmp_path, a, basis, 1e-12, 6,
+                      extra=("fp32", "nearest", 0, "native_quantized", "fixed_budget"))
+    assert rc == 0, err
+    assert r["correction_mode"] == "native_quantized"
+    init, final = float(r["initial_residual"]), float(r["final_residual"])
+    if basis == "fp32":
+        assert r["status"] == "converged" and final <= 1e-12, r
+    else:
+        assert final < 0.1 * init, r
+
+
+def test_native_quantized_correction_stops_on_stagnation(tmp_path):
+    """The stagnation policy stops after four corrections without a 1e-3
+    relative improvement and reports the best root."""
+    a = O.controlled(64, 1e2)
+    rc, r, err = _run(tmp_path, a, "bf16", 1e-14, 40,
+                      extra=("fp32", "nearest", 0, "native_quantized", "stagnation"))
+    assert rc == 0, err
+    assert int(r["iterations"]) < 40, r
+    assert int(r["stagnation_steps"]) >= 4, r
+    assert float(r["final_residual"]) == float(r["best_residual"]), r

@@ -126,3 +126,38 @@ def test_log_spectrum_rejects_non_positive_input(ctx, msq):
         ctx.synchronize()
     v, m = ctx.copy_spectrum_to_storage(2, torch.tensor([1.0, 2.0], device="cuda"))
     ctx.synchronize()
+
+
+@pytest.mark.parametrize("fmt", [0, 1, 2, 3, 4, 5, 6, 7, 8])
+@pytest.mark.parametrize("n", [1, 7, 33, 64])
+def test_native_correction_equals_the_oracle(ctx, msq, fmt, n):
+    """msq_native_sylvester_sweep from X = 0 leaves (E + E^T) / 2 with E the
+    oracle's native correction, bit for bit (same quantizer, same FMA
+    chains, same divisions)."""
+    import torch
+    rng = np.random.default_rng(100 * fmt + n)
+    q, _ = np.linalg.qr(rng.standard_normal((n, n)))
+    v = q.astype(np.float32)
+    rl = n if fmt == 8 else 0
+    def stored(m):
+        if fmt == 0:
+            return np.asfortranarray(m, np.float32)
+        flat = np.asfortranarray(m, np.float32).reshape(-1, order="F")
+        return O.decode(fmt, *O.encode(fmt, flat, rl), flat.size, rl).reshape(n, n, order="F")
+    vq, vtq = stored(v), stored(v.T)
+    s = np.exp(rng.uniform(-1, 1, n)).astype(np.float32)
+    r = (1e-3 * rng.standard_normal((n, n))).astype(np.float32)
+    r = np.asfortranarray(0.5 * (r + r.T))
+    e = O.native_correction(fmt, vq, vtq, s, r)
+    b = msq.Batch.from_orders([n])
+    col = lambda m: torch.from_numpy(b.pack([np.asfortranarray(m, np.float32)])).cuda()
+    x_hi = torch.zeros(b.total, dtype=torch.float32, device="cuda")
+    x_lo = torch.zeros_like(x_hi)
+    ctx.native_sylvester_sweep(fmt, col(vq), col(vtq), torch.from_numpy(s).cuda(), col(r), b,
+                               x_hi, x_lo)
+    ctx.synchronize()
+    got = b.unpack(x_hi.cpu().numpy(), dtype=np.float32)[0]
+    # the float-float add starts from x = +0: +0 + corr turns a -0 into +0
+    want = (np.float32(0.5) * (e + e.T) + np.float32(0.0)).astype(np.float32)
+    assert np.array_equal(np.ascontiguousarray(got).view(np.uint32),
+                          np.ascontiguousarray(want).view(np.uint32))

@@ -171,3 +171,38 @@ def test_log_spectrum_rejects_non_positive_input():
     for bad in ([1.0, 0.0], [1.0, -2.0], [np.inf, 1.0], [np.nan]):
         with pytest.raises(ValueError):
             O.spectrum_encode(2, np.array(bad, dtype=np.float32))
+
+
+def _near_root_case(n: int, seed: int):
+    rng = np.random.default_rng(seed)
+    q, _ = np.linalg.qr(rng.standard_normal((n, n)))
+    s = np.exp(rng.uniform(-1.0, 1.0, n))
+    a = (q * s ** 2) @ q.T
+    x0 = (q * s) @ q.T + 1e-3 * rng.standard_normal((n, n))
+    x0 = 0.5 * (x0 + x0.T)
+    return q, s, a, x0, a - x0 @ x0
+
+
+def test_native_correction_in_fp32_is_the_sylvester_correction():
+    """With FP32 storage the native correction is E = V ((V^T R V) o H) V^T
+    (refineNativeStaged with no quantizer)."""
+    q, s, a, x0, r = _near_root_case(24, 1)
+    f = lambda m: m.astype(np.float32)
+    e = O.native_correction(0, f(q), f(q.T), f(s), f(r))
+    e64 = q @ ((q.T @ r @ q) / (s[:, None] + s[None, :])) @ q.T
+    assert np.abs(e - e64).max() <= 1e-5 * np.abs(e64).max()
+
+
+@pytest.mark.parametrize("fmt,gain", [(0, 1e-2), (1, 1e-1), (8, 0.5), (7, 0.5)])
+def test_native_correction_reduces_the_residual(fmt, gain):
+    q, s, a, x0, r = _near_root_case(24, 2)
+    f = lambda m: m.astype(np.float32)
+    vq = O.decode(fmt, *O.encode(fmt, f(q).reshape(-1, order="F"), 24 if fmt == 8 else 0),
+                  24 * 24, 24 if fmt == 8 else 0).reshape(24, 24, order="F") if fmt else f(q)
+    vtq = O.decode(fmt, *O.encode(fmt, f(q.T).reshape(-1, order="F"), 24 if fmt == 8 else 0),
+                   24 * 24, 24 if fmt == 8 else 0).reshape(24, 24, order="F") if fmt else f(q.T)
+    e = O.native_correction(fmt, vq, vtq, f(s), f(r))
+    x1 = x0 + 0.5 * (e + e.T)
+    before = np.linalg.norm(a - x0 @ x0) / np.linalg.norm(a)
+    after = np.linalg.norm(a - x1 @ x1) / np.linalg.norm(a)
+    assert after < gain * before, (before, after)
