@@ -315,6 +315,14 @@ int msq_native_sylvester_sweep(msq_ctx *ctx, int format, const float *vectors,
                                const int64_t *offset, int count, float *x_hi, float *x_lo,
                                float *workspace, uint8_t *codes, uint8_t *scales);
 
+/* The reference's CSV schema (writeSummaryHeader / writeIterationsHeader,
+ * src/reporting.cpp:124-166, 305-327): the header lines of the summary and
+ * per-iteration files that the C++ mirror's writers (cuda_backend.hpp) fill
+ * row by row.  Host only (no GPU needed).  Returns MSQ_ERR_INVALID_ARGUMENT
+ * when a buffer is too small.                                             */
+int msq_csv_headers(char *summary, size_t summary_capacity, char *iterations,
+                    size_t iterations_capacity);
+
 /* ---- whole-pipeline batched solve ------------------------------------------
  * The GPU-resident solve of solveGpuResidentSpd (src/metal_solver.cpp:92-336)
  * over a batch: Jacobi -> (quantize W) -> reconstruct -> Sylvester sweeps ->

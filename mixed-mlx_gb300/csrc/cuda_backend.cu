@@ -14,6 +14,8 @@
 #include <iostream>
 #include <limits>
 #include <sstream>
+#include <utility>
+#include <vector>
 #include <stdexcept>
 
 namespace mixed_sqrt {
@@ -194,6 +196,11 @@ CaseResult runCudaCase(CudaRuntime &runtime, const CudaSolverConfiguration &conf
   result.correction_mode =
       configuration.native_correction ? "native_quantized" : "fp32_reorthogonalized";
   result.kernel_path = "tiled";
+  result.rounding_mode = cudaRoundingModeName(configuration.rounding_mode);
+  result.rounding_seed = configuration.rounding_seed;
+  result.stopping_policy =
+      configuration.native_correction && configuration.stop_on_stagnation ? "stagnation" : "fixed_budget";
+  result.dispatch_policy = configuration.native_correction ? "fused" : "not_applicable";
   result.precision_policy = configuration.basis_format == CudaBasisFormat::Fp32 ||
                                     configuration.basis_format == CudaBasisFormat::Bf16
                                 ? "required_full_accuracy"
@@ -297,7 +304,7 @@ CaseResult runCudaCase(CudaRuntime &runtime, const CudaSolverConfiguration &conf
       ++result.precision_escalations;
       format = CudaBasisFormat::Fp32;
     }
-    (void)quantize_start;
+    result.factor_quantization_seconds += since(quantize_start);
   } else {
     result.selected_basis_stage = "fp32";
   }
@@ -310,6 +317,7 @@ CaseResult runCudaCase(CudaRuntime &runtime, const CudaSolverConfiguration &conf
   DeviceBuffer lam0(n * sizeof(float));
   bool quantized_spectrum = false;
   if (configuration.spectrum_format != CudaSpectrumFormat::Fp32) {
+    const auto spectrum_start = Clock::now();
     const int sfmt = configuration.spectrum_format == CudaSpectrumFormat::Fp8E4M3FnLogS
                          ? MSQ_FMT_FP8_E4M3FN
                          : MSQ_FMT_FP4_E2M1;
@@ -329,6 +337,7 @@ CaseResult runCudaCase(CudaRuntime &runtime, const CudaSolverConfiguration &conf
     runtime.check(msq_synchronize(ctx), "quantizeAndDecode spectrum");
     std::vector<float> quantized(n);
     copyOut(quantized.data(), s_out.as<float>(), n * sizeof(float));
+    result.factor_quantization_seconds += since(spectrum_start);
     bool usable = true;
     for (float value : quantized) usable = usable && value > 0.0f && std::isfinite(value);
     if (usable) {
@@ -442,8 +451,11 @@ CaseResult runCudaCase(CudaRuntime &runtime, const CudaSolverConfiguration &conf
   double best = res;
   bool best_saved = false;
   size_t iteration = 0, flat_steps = 0;
+  std::string stages;
+  uint64_t correction_launches = 0;
   while (res > problem.tolerance && iteration < problem.max_iterations && std::isfinite(res)) {
     const auto t0 = Clock::now();
+    const uint64_t launches_before = msq_launch_count(ctx);
     if (native) {
       runtime.check(msq_native_sylvester_sweep(ctx, ncodec, nv.as<float>(), nvt.as<float>(),
                                                ns.as<float>(), r.as<float>(), &nn, &off, 1,
@@ -456,6 +468,9 @@ CaseResult runCudaCase(CudaRuntime &runtime, const CudaSolverConfiguration &conf
                                         x_lo.as<float>(), ws.as<float>()),
                     "refineUpdateAndMeasure");
     }
+    correction_launches += msq_launch_count(ctx) - launches_before;
+    stages += (stages.empty() ? "" : ";") +
+              std::string(native ? "native_quantized" : "fp32_frozen");
     const double previous_best = best;
     res = residual();
     result.times.correction_gpu_seconds += since(t0);
@@ -491,7 +506,30 @@ CaseResult runCudaCase(CudaRuntime &runtime, const CudaSolverConfiguration &conf
     result.history.push_back({iteration, best, forward_error(root_now())});
   }
   result.times.mixed_total_seconds = since(mixed_start);
+  if (!stages.empty()) result.correction_stage_history = stages;
+  if (iteration > 0) result.kernel_dispatches_per_correction = correction_launches / iteration;
+  result.low_factor_corrections = native && ncodec != MSQ_FMT_FP32 ? iteration : 0;
   const std::vector<double> root = root_now();
+  if (problem.supplied_reference != nullptr && problem.supplied_reference->size() == elements &&
+      n <= 1024) {
+    // the FP64 residual of the supplied reference root (runMetalCase reports it)
+    const std::vector<double> &ref = *problem.supplied_reference;
+    double num = 0.0, den = 0.0;
+    std::vector<double> column(n);
+    for (size_t c = 0; c < n; ++c) {
+      std::fill(column.begin(), column.end(), 0.0);
+      for (size_t k = 0; k < n; ++k) {
+        const double b = ref[k + c * n];
+        for (size_t r2 = 0; r2 < n; ++r2) column[r2] += ref[r2 + k * n] * b;
+      }
+      for (size_t r2 = 0; r2 < n; ++r2) {
+        const double a = prepared.values[r2 + c * n];
+        num += (a - column[r2]) * (a - column[r2]);
+        den += a * a;
+      }
+    }
+    result.reference_residual = den > 0.0 ? std::sqrt(num / den) : 0.0;
+  }
 
   result.best_residual = result.history.front().residual;
   result.best_forward_error = result.history.front().forward_error;
@@ -569,3 +607,211 @@ int runCuda(const CudaRunOptions &options, const PreparedMatrix &matrix) {
 }
 
 }  // namespace mixed_sqrt
+
+namespace mixed_sqrt {
+namespace {
+
+// One row of a schema: (column, formatted value) in column order.
+using Row = std::vector<std::pair<const char *, std::string>>;
+
+template <typename T>
+std::string text(const T &value) {
+  std::ostringstream out;
+  out << std::setprecision(17) << value;
+  return out.str();
+}
+
+double basisStorageRatio(const CaseResult &r) {
+  return r.fp32_basis_bytes > 0 ? static_cast<double>(r.low_factor_basis_bytes) /
+                                      static_cast<double>(r.fp32_basis_bytes)
+                                : 0.0;
+}
+
+double otherSeconds(const CaseResult &r) {
+  const double accounted = r.times.low_eigen_seconds + r.times.initial_gpu_seconds +
+                           r.times.residual_fp64_seconds + r.times.correction_gpu_seconds;
+  return std::max(0.0, r.times.mixed_total_seconds - accounted);
+}
+
+// The columns both files begin with (through kernel_path).
+void leadingColumns(const CaseResult &r, Row &row) {
+  row.insert(row.end(), {
+      {"paper_test_set", r.paper_test_set}, {"matrix_family", r.matrix_family},
+      {"matrix_type", r.matrix_type}, {"solver_backend", r.solver_backend},
+      {"rng_seed", text(r.rng_seed)}, {"rounding_mode", r.rounding_mode},
+      {"rounding_seed", text(r.rounding_seed)}, {"diagonal_shift", text(r.diagonal_shift)},
+      {"shift_rule", r.shift_rule}, {"case", r.name}, {"precision", r.precision},
+      {"basis_precision", r.basis_precision}, {"spectrum_precision", r.spectrum_precision},
+      {"correction_mode", r.correction_mode}, {"precision_policy", r.precision_policy},
+      {"stopping_policy", r.stopping_policy}, {"dispatch_policy", r.dispatch_policy},
+      {"termination_reason", r.termination_reason}, {"selection_policy", r.selection_policy},
+      {"precision_attempts", text(r.precision_attempts)}, {"execution_model", r.execution_model},
+      {"kernel_path", r.kernel_path}});
+}
+
+// Basis stages through basis_reorthogonalization_seconds.
+void stageColumns(const CaseResult &r, Row &row) {
+  row.insert(row.end(), {
+      {"selected_basis_stage", r.selected_basis_stage},
+      {"selected_spectrum_stage", r.selected_spectrum_stage},
+      {"correction_stage_history", r.correction_stage_history},
+      {"precision_escalations", text(r.precision_escalations)},
+      {"low_factor_corrections", text(r.low_factor_corrections)},
+      {"low_factor_basis_bytes", text(r.low_factor_basis_bytes)},
+      {"fp32_basis_bytes", text(r.fp32_basis_bytes)},
+      {"basis_storage_ratio", text(basisStorageRatio(r))},
+      {"quantized_basis_orthogonality", text(r.quantized_basis_orthogonality)},
+      {"factor_quantization_seconds", text(r.factor_quantization_seconds)},
+      {"basis_reorthogonalization_seconds", text(r.basis_reorthogonalization_seconds)}});
+}
+
+void referenceTimingColumns(const CaseResult &r, Row &row) {
+  row.insert(row.end(), {
+      {"reference_timing_min_seconds", text(r.reference_timing.minimum_seconds)},
+      {"reference_timing_max_seconds", text(r.reference_timing.maximum_seconds)},
+      {"reference_timing_median_seconds", text(r.reference_timing.median_seconds)},
+      {"reference_timing_mean_seconds", text(r.reference_timing.mean_seconds)},
+      {"reference_timing_variance_seconds2", text(r.reference_timing.variance_seconds2)}});
+}
+
+void pairedRatioColumns(const CaseResult &r, Row &row) {
+  row.insert(row.end(), {
+      {"paired_ratio_mean", text(r.paired_ratio_summary.mean)},
+      {"paired_ratio_variance", text(r.paired_ratio_summary.variance)},
+      {"paired_ratio_min", text(r.paired_ratio_summary.minimum)},
+      {"paired_ratio_max", text(r.paired_ratio_summary.maximum)},
+      {"paired_ratio_median", text(r.paired_ratio_summary.median)}});
+}
+
+// The phase columns factorization_seconds .. mixed_total_seconds.
+void phaseColumns(const CaseResult &r, Row &row) {
+  const PhaseTimes &t = r.times;
+  row.insert(row.end(), {
+      {"factorization_seconds", text(t.low_eigen_seconds)},
+      {"initial_root_seconds", text(t.initial_gpu_seconds)},
+      {"single_seconds", text(t.low_eigen_seconds + t.initial_gpu_seconds)},
+      {"residual_seconds", text(t.residual_fp64_seconds)},
+      {"correction_system_seconds", text(t.correction_gpu_seconds)},
+      {"updates_and_others_seconds", text(otherSeconds(r))},
+      {"mixed_total_seconds", text(t.mixed_total_seconds)}});
+}
+
+Row summaryRow(const CaseResult &r) {
+  static const IterationMeasurement kEmpty{0, std::numeric_limits<double>::quiet_NaN(),
+                                           std::numeric_limits<double>::quiet_NaN()};
+  const IterationMeasurement &first = r.history.empty() ? kEmpty : r.history.front();
+  const IterationMeasurement &last = r.history.empty() ? kEmpty : r.history.back();
+  const double total = r.times.mixed_total_seconds;
+  auto fraction = [total](double seconds) { return text(total > 0.0 ? seconds / total : 0.0); };
+  Row row;
+  leadingColumns(r, row);
+  row.insert(row.end(), {
+      {"command_buffers_per_correction", text(r.command_buffers_per_correction)},
+      {"kernel_dispatches_per_correction", text(r.kernel_dispatches_per_correction)}});
+  stageColumns(r, row);
+  row.insert(row.end(), {
+      {"warmups", text(r.timing.warmups)}, {"evaluations", text(r.timing.evaluations)},
+      {"timing_evaluations", text(r.timing.evaluations)},
+      {"timing_min_seconds", text(r.timing.minimum_seconds)},
+      {"timing_max_seconds", text(r.timing.maximum_seconds)},
+      {"timing_median_seconds", text(r.timing.median_seconds)},
+      {"timing_mean_seconds", text(r.timing.mean_seconds)},
+      {"timing_variance_seconds2", text(r.timing.variance_seconds2)}});
+  referenceTimingColumns(r, row);
+  row.insert(row.end(), {
+      {"order", text(r.order)}, {"condition", text(r.condition)},
+      {"iterations", text(last.iteration)}, {"best_iteration", text(r.best_iteration)},
+      {"best_residual", text(r.best_residual)}, {"best_forward_error", text(r.best_forward_error)},
+      {"stagnation_steps", text(r.stagnation_steps)}, {"converged", text(r.converged)},
+      {"finite", text(r.finite)}, {"status", r.status},
+      {"initial_residual", text(first.residual)}, {"final_residual", text(r.final_residual)},
+      {"initial_forward_error", text(first.forward_error)},
+      {"final_forward_error", text(r.final_forward_error)},
+      {"symmetry_error", text(r.symmetry_error)}, {"reference_residual", text(r.reference_residual)},
+      {"frozen_factor_error", text(r.frozen_factor_error)},
+      {"frozen_factor_relative_error", text(r.frozen_factor_relative_error)},
+      {"frozen_basis_orthogonality", text(r.frozen_basis_orthogonality)},
+      {"frozen_sylvester_inverse_norm", text(r.frozen_sylvester_inverse_norm)},
+      {"frozen_contraction_bound", text(r.frozen_contraction_bound)},
+      {"certificate_usable", text(r.certificate_usable)},
+      {"reference_seconds", text(r.times.reference_seconds)},
+      {"low_eigen_seconds", text(r.times.low_eigen_seconds)},
+      {"initial_gpu_seconds", text(r.times.initial_gpu_seconds)},
+      {"residual_fp64_seconds", text(r.times.residual_fp64_seconds)},
+      {"correction_gpu_seconds", text(r.times.correction_gpu_seconds)},
+      {"update_fp64_seconds", text(r.times.update_fp64_seconds)}});
+  phaseColumns(r, row);
+  row.insert(row.end(), {
+      {"low_eigen_fraction", fraction(r.times.low_eigen_seconds)},
+      {"initial_gpu_fraction", fraction(r.times.initial_gpu_seconds)},
+      {"residual_fraction", fraction(r.times.residual_fp64_seconds)},
+      {"correction_gpu_fraction", fraction(r.times.correction_gpu_seconds)},
+      {"update_fraction", fraction(r.times.update_fp64_seconds)}});
+  pairedRatioColumns(r, row);
+  row.push_back({"mixed_to_reference",
+                 text(r.reference_timing.mean_seconds > 0.0
+                          ? r.timing.mean_seconds / r.reference_timing.mean_seconds
+                          : 0.0)});
+  return row;
+}
+
+Row iterationRow(const CaseResult &r, const IterationMeasurement &record) {
+  Row row;
+  leadingColumns(r, row);
+  stageColumns(r, row);
+  row.insert(row.end(), {
+      {"order", text(r.order)}, {"condition", text(r.condition)},
+      {"warmups", text(r.timing.warmups)}, {"evaluations", text(r.timing.evaluations)},
+      {"timing_evaluations", text(r.timing.evaluations)}});
+  referenceTimingColumns(r, row);
+  pairedRatioColumns(r, row);
+  phaseColumns(r, row);
+  row.insert(row.end(), {{"iteration", text(record.iteration)},
+                         {"residual", text(record.residual)},
+                         {"forward_error", text(record.forward_error)}});
+  return row;
+}
+
+void writeNames(std::ostream &out, const Row &row) {
+  for (size_t i = 0; i < row.size(); ++i) out << (i ? "," : "") << row[i].first;
+  out << '\n';
+}
+
+void writeValues(std::ostream &out, const Row &row) {
+  for (size_t i = 0; i < row.size(); ++i) out << (i ? "," : "") << row[i].second;
+  out << '\n';
+}
+
+}  // namespace
+
+void writeCudaSummaryHeader(std::ostream &output) { writeNames(output, summaryRow(CaseResult{})); }
+
+void writeCudaIterationsHeader(std::ostream &output) {
+  writeNames(output, iterationRow(CaseResult{}, IterationMeasurement{0, 0.0, 0.0}));
+}
+
+void writeCudaCaseCsv(const CaseResult &result, std::ostream &summary, std::ostream &iterations) {
+  writeValues(summary, summaryRow(result));
+  for (const IterationMeasurement &record : result.history) {
+    writeValues(iterations, iterationRow(result, record));
+  }
+}
+
+}  // namespace mixed_sqrt
+
+extern "C" int msq_csv_headers(char *summary, size_t summary_capacity, char *iterations,
+                               size_t iterations_capacity) {
+  std::ostringstream s, i;
+  mixed_sqrt::writeCudaSummaryHeader(s);
+  mixed_sqrt::writeCudaIterationsHeader(i);
+  const std::string a = s.str(), b = i.str();
+  if (summary == nullptr || iterations == nullptr || a.size() + 1 > summary_capacity ||
+      b.size() + 1 > iterations_capacity) {
+    return MSQ_ERR_INVALID_ARGUMENT;
+  }
+  std::copy(a.begin(), a.end(), summary);
+  summary[a.size()] = '\0';
+  std::copy(b.begin(), b.end(), iterations);
+  iterations[b.size()] = '\0';
+  return MSQ_OK;
+}

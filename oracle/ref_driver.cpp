@@ -9,6 +9,7 @@
 #include "accelerate_backend.hpp"
 #include "numerics.hpp"
 #include "precision.hpp"
+#include "reporting.hpp"
 #include "storage_codecs.hpp"
 
 #include <Metal/Metal.hpp>
@@ -16,6 +17,7 @@
 #include <cstdint>
 #include <cstring>
 #include <exception>
+#include <fstream>
 #include <stdexcept>
 #include <string>
 #include <vector>
@@ -135,6 +137,16 @@ int ref_spectrum_decode(int codec, const uint8_t *values, const float *metadata,
     for (size_t index = 0; index < elements; ++index) {
       output[index] = spectrumValueAt(*spec, &value_buffer, &metadata_buffer, index);
     }
+  });
+}
+
+// writeSummaryHeader / writeIterationsHeader (src/reporting.cpp:124-166,
+// 305-327) into the files `summary_path` and `iterations_path`.
+int ref_csv_headers(const char *summary_path, const char *iterations_path) {
+  return guarded([&] {
+    std::ofstream summary(summary_path), iterations(iterations_path);
+    writeSummaryHeader(summary);
+    writeIterationsHeader(iterations);
   });
 }
 

@@ -6,11 +6,12 @@
 //                           [spectrum: fp32|fp8_e4m3fn_log_s|fp4_e2m1_log_s]
 //                           [rounding: nearest|stochastic] [rounding seed]
 //                           [correction: fp32_reorthogonalized|native_quantized]
-//                           [native stopping: fixed_budget|stagnation]
+//                           [native stopping: fixed_budget|stagnation] [csv prefix]
 #include <cstdint>
 #include <cstdio>
 #include <cstdlib>
 #include <exception>
+#include <fstream>
 #include <iomanip>
 #include <iostream>
 #include <string>
@@ -47,6 +48,9 @@ int main(int argc, char **argv) {
     // native stopping policy (fixed_budget | stagnation)
     if (argc > 8) config.native_correction = std::string(argv[8]) == "native_quantized";
     if (argc > 9) config.stop_on_stagnation = std::string(argv[9]) == "stagnation";
+    // optional: write the reference's CSV schema to <prefix>_summary.csv and
+    // <prefix>_iterations.csv
+    const std::string csv_prefix = argc > 10 ? argv[10] : "";
     mixed_sqrt::CudaProblem problem;
     problem.order = m.order;
     problem.tolerance = std::atof(argv[3]);
@@ -54,6 +58,12 @@ int main(int argc, char **argv) {
     problem.prepared_matrix = &m;
     problem.supplied_reference = have_ref ? &ref : nullptr;
     const mixed_sqrt::CaseResult r = mixed_sqrt::runCudaCase(runtime, config, problem);
+    if (!csv_prefix.empty()) {
+      std::ofstream summary(csv_prefix + "_summary.csv"), iterations(csv_prefix + "_iterations.csv");
+      mixed_sqrt::writeCudaSummaryHeader(summary);
+      mixed_sqrt::writeCudaIterationsHeader(iterations);
+      mixed_sqrt::writeCudaCaseCsv(r, summary, iterations);
+    }
     std::cout << std::setprecision(17) << "status=" << r.status
               << " iterations=" << (r.history.size() - 1)
               << " final_residual=" << r.final_residual

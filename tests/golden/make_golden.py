@@ -12,6 +12,9 @@ them (src/storage_codecs.cpp, src/numerics.cpp, src/accelerate_backend.cpp,
   numerics.npz   makeSpdMatrix(n, cond) outputs, symmetricReferenceRoot of
                  them, and runAccelerateCase (src/accelerate_backend.cpp:
                  803-1091) residual/forward-error histories.
+  csv_headers.txt  writeSummaryHeader and writeIterationsHeader
+                 (src/reporting.cpp:124-166, 305-327): the reference's CSV
+                 schema, one header line each.
   spectrum.npz   copySpectrumToStorage / spectrumValueAt (src/storage_codecs.
                  cpp:387-460) codes, (min, span) metadata and decoded values
                  of the log-spectrum precisions (FP8-E4M3FN and FP4-E2M1
@@ -19,8 +22,9 @@ them (src/storage_codecs.cpp, src/numerics.cpp, src/accelerate_backend.cpp,
                  spectrum of checkStochasticQuantization and log-uniform
                  spectra with equal-valued blocks and a ragged tail.
 
-Usage: make -C oracle && python tests/golden/make_golden.py [spectrum]
-(with `spectrum`, only spectrum.npz is written)
+Usage: make -C oracle && python tests/golden/make_golden.py [csv | spectrum]
+(with `csv`, only csv_headers.txt is written; with `spectrum`, csv_headers.txt
+and spectrum.npz)
 """
 from __future__ import annotations
 
@@ -110,9 +114,25 @@ def write_spectrum() -> None:
     print("wrote", os.path.join(HERE, "spectrum.npz"))
 
 
+def write_csv_headers() -> None:
+    import tempfile
+    lib = O.ref()
+    lib.ref_csv_headers.argtypes = [ctypes.c_char_p, ctypes.c_char_p]
+    with tempfile.TemporaryDirectory() as tmp:
+        a, b = os.path.join(tmp, "s.csv"), os.path.join(tmp, "i.csv")
+        assert lib.ref_csv_headers(a.encode(), b.encode()) == 0, lib.ref_last_error()
+        lines = [open(a).read().strip(), open(b).read().strip()]
+    with open(os.path.join(HERE, "csv_headers.txt"), "w") as f:
+        f.write("\n".join(lines) + "\n")
+    print("wrote", os.path.join(HERE, "csv_headers.txt"))
+
+
 def main() -> None:
     if not O.ref_available():
         raise SystemExit("oracle/_ref/libmsq_ref.so missing: run `make -C oracle` first")
+    write_csv_headers()
+    if sys.argv[1:] == ["csv"]:
+        return
     write_spectrum()
     if sys.argv[1:] == ["spectrum"]:
         return

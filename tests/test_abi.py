@@ -76,3 +76,17 @@ def test_python_host_layer_refuses_without_gpu():
         pytest.skip("GPU present")
     with pytest.raises(msq.MsqError):
         msq.Context(0)
+
+
+def test_csv_schema_is_the_references(lib_path):
+    """msq_csv_headers (the C++ mirror's writers) against the header lines
+    the reference's own writeSummaryHeader / writeIterationsHeader wrote
+    (tests/golden/csv_headers.txt)."""
+    import ctypes
+    lib = ctypes.CDLL(lib_path)
+    a, b = ctypes.create_string_buffer(8192), ctypes.create_string_buffer(8192)
+    assert lib.msq_csv_headers(a, 8192, b, 8192) == 0
+    golden = open(os.path.join(ROOT, "tests", "golden", "csv_headers.txt")).read().split("\n")
+    assert a.value.decode().rstrip("\n") == golden[0]
+    assert b.value.decode().rstrip("\n") == golden[1]
+    assert lib.msq_csv_headers(a, 16, b, 8192) != 0   # too small a buffer

@@ -120,3 +120,32 @@ def test_native_quantized_correction_stops_on_stagnation(tmp_path):
     assert int(r["iterations"]) < 40, r
     assert int(r["stagnation_steps"]) >= 4, r
     assert float(r["final_residual"]) == float(r["best_residual"]), r
+
+
+def test_results_write_the_references_csv_schema(tmp_path):
+    """The mirror's CSV writers: the reference's columns (checked against the
+    reference's own header lines), one summary row, one iteration row per
+    history entry, values consistent with the key=value report."""
+    import csv
+    a = O.controlled(48, 1e2)
+    prefix = tmp_path / "case"
+    rc, r, err = _run(tmp_path, a, "bf16", 1e-12, 8,
+                      extra=("fp8_e4m3fn_log_s", "stochastic", 99, "fp32_reorthogonalized",
+                             "fixed_budget", prefix))
+    assert rc == 0, err
+    golden = open(os.path.join(ROOT, "tests", "golden", "csv_headers.txt")).read().split("\n")
+    with open(f"{prefix}_summary.csv") as f:
+        rows = list(csv.reader(f))
+    assert ",".join(rows[0]) == golden[0] and len(rows) == 2 and len(rows[1]) == len(rows[0])
+    summary = dict(zip(rows[0], rows[1]))
+    assert summary["solver_backend"] == "cuda" and summary["status"] == r["status"]
+    assert summary["rounding_mode"] == "stochastic" and summary["rounding_seed"] == "99"
+    assert summary["selected_spectrum_stage"] == r["selected_spectrum_stage"]
+    assert float(summary["final_residual"]) == float(r["final_residual"])
+    assert summary["correction_stage_history"].split(";") == ["fp32_frozen"] * int(r["iterations"])
+    assert int(summary["kernel_dispatches_per_correction"]) > 0
+    assert float(summary["reference_residual"]) < 1e-12
+    with open(f"{prefix}_iterations.csv") as f:
+        it = list(csv.reader(f))
+    assert ",".join(it[0]) == golden[1]
+    assert len(it) - 1 == int(r["iterations"]) + 1 and all(len(x) == len(it[0]) for x in it)
