@@ -16,6 +16,7 @@
  *  - the device quantizers' stochastic rounding and the log-spectrum
  *    storage of the root eigenvalues (restated from the shader source);
  *  - one correction of the native-quantized mode;
+ *  - the symmetric paper test sets V-VII (generator and Hilbert matrix);
  *  - the parallel-order two-sided Jacobi of metal_mixed_sqrt.metal:1319-1444
  *    with the round-robin schedule of src/metal_solver.cpp:50-79, angles in
  *    FP64, FP32 storage, convergence-tested;
@@ -490,6 +491,63 @@ int msqo_native_correction(int format, const float *v, const float *vt, const fl
 done:
   free(rq); free(w1); free(w2); free(codes); free(scales);
   return rc;
+}
+
+/* -------------------------------------------------- paper test sets */
+
+/* DeterministicGenerator (src/accelerate_backend.cpp:626-664): xorshift
+ * state update, 53-bit uniform from a multiplied state, Box-Muller normals
+ * (cosine first, sine kept as the spare). */
+typedef struct { uint64_t state; double spare; int has_spare; } paper_rng;
+
+static double rng_uniform(paper_rng *g) {
+  uint64_t v = g->state;
+  v ^= v >> 12;
+  v ^= v << 25;
+  v ^= v >> 27;
+  g->state = v;
+  return (double)((v * UINT64_C(2685821657736338717)) >> 11) * 0x1.0p-53;
+}
+
+static double rng_normal(paper_rng *g) {
+  if (g->has_spare) { g->has_spare = 0; return g->spare; }
+  double first = rng_uniform(g);
+  if (first < 2.2250738585072014e-308) first = 2.2250738585072014e-308;
+  double second = rng_uniform(g);
+  double radius = sqrt(-2.0 * log(first)), angle = 6.283185307179586476925286766559 * second;
+  g->spare = radius * sin(angle);
+  g->has_spare = 1;
+  return radius * cos(angle);
+}
+
+/* preparePaperMatrix (src/accelerate_backend.cpp:690-801) for the symmetric
+ * sets V (uniform), VI (normal) and VII (Hilbert + 1e-6 I), before the
+ * spectral shift of V and VI (which needs the FP64 extreme eigenvalues and
+ * is applied by the caller).  *seed receives the generator seed (0 for VII).
+ * Returns 0, or 1 for another set. */
+int msqo_paper_matrix(int set, unsigned n, double *out, uint64_t *seed) {
+  if (set == 7) {
+    for (unsigned c = 0; c < n; ++c) {
+      for (unsigned r = 0; r < n; ++r) out[r + (size_t)c * n] = 1.0 / (double)(r + c + 1);
+      out[c + (size_t)c * n] += 1.0e-6;
+    }
+    *seed = 0;
+    return 0;
+  }
+  if (set != 5 && set != 6) return 1;
+  paper_rng g;
+  g.state = UINT64_C(0x243f6a8885a308d3) ^ (UINT64_C(0x9e3779b97f4a7c15) * (uint64_t)set);
+  *seed = g.state;
+  if (g.state == 0) g.state = UINT64_C(0x9e3779b97f4a7c15);
+  g.has_spare = 0;
+  g.spare = 0.0;
+  for (unsigned c = 0; c < n; ++c)
+    for (unsigned r = c; r < n; ++r) {
+      double v = set == 5 ? rng_uniform(&g) : rng_normal(&g);
+      out[r + (size_t)c * n] = v;
+      out[c + (size_t)r * n] = v;
+    }
+  return 0;
 }
 
 /* ---------------------------------------------------------------- Jacobi */

@@ -75,6 +75,8 @@ def olib() -> ctypes.CDLL:
                                              ctypes.c_uint32, ctypes.c_uint32, _P, _P]
         lib.msqo_spectrum_decode.argtypes = [ctypes.c_int, _P, _P, ctypes.c_size_t, _P]
         lib.msqo_native_correction.argtypes = [ctypes.c_int, _P, _P, _P, _P, ctypes.c_uint, _P]
+        lib.msqo_paper_matrix.argtypes = [ctypes.c_int, ctypes.c_uint, _P,
+                                          ctypes.POINTER(ctypes.c_uint64)]
         _ORACLE = lib
     return _ORACLE
 
@@ -168,6 +170,27 @@ def native_correction(fmt: int, v: np.ndarray, vt: np.ndarray, s: np.ndarray, r:
                                      R.ctypes.data, n, E.ctypes.data):
         raise ValueError("oracle native correction failed")
     return E
+
+
+PAPER_ORDERS = {5: 4096, 6: 4096, 7: 1024}  # paperTestSetOrder (src/configuration.cpp:255-271)
+
+
+def paper_matrix(test_set: int, n: int):
+    """preparePaperMatrix (src/accelerate_backend.cpp:690-801) for the
+    symmetric sets V, VI, VII: (matrix, diagonal_shift, condition, rng_seed).
+    Sets V and VI are shifted so that the smallest eigenvalue is
+    max(1, 0.01 ||A||_inf) (FP64 eigenvalues, numpy's LAPACK)."""
+    a = np.zeros((n, n), dtype=np.float64, order="F")
+    seed = ctypes.c_uint64(0)
+    if olib().msqo_paper_matrix(test_set, n, a.ctypes.data, ctypes.byref(seed)):
+        raise ValueError("paper sets V, VI and VII only")
+    lam = np.linalg.eigvalsh(a)
+    if test_set == 7:
+        return a, 1e-6, float(lam[-1] / lam[0]), 0
+    separation = max(1.0, 0.01 * np.abs(a).sum(axis=1).max())
+    shift = max(0.0, separation - lam[0])
+    a[np.diag_indices(n)] += shift
+    return a, shift, float((lam[-1] + shift) / (lam[0] + shift)), int(seed.value)
 
 
 def jacobi_pair(order: int, rnd: int, pair: int) -> tuple[int, int]:

@@ -14,6 +14,7 @@
 
 #include <Metal/Metal.hpp>
 
+#include <algorithm>
 #include <cstdint>
 #include <cstring>
 #include <exception>
@@ -147,6 +148,18 @@ int ref_csv_headers(const char *summary_path, const char *iterations_path) {
     std::ofstream summary(summary_path), iterations(iterations_path);
     writeSummaryHeader(summary);
     writeIterationsHeader(iterations);
+  });
+}
+
+// preparePaperMatrix (src/accelerate_backend.cpp:690-801) for set
+// I..VII = 1..7: values and (diagonal_shift, condition, rng_seed).
+int ref_paper_matrix(int set, size_t order, double *output, double *meta) {
+  return guarded([&] {
+    const PreparedMatrix m = preparePaperMatrix(static_cast<PaperTestSet>(set), order);
+    std::copy(m.values.begin(), m.values.end(), output);
+    meta[0] = m.diagonal_shift;
+    meta[1] = m.condition;
+    meta[2] = static_cast<double>(m.rng_seed);
   });
 }
 

@@ -12,6 +12,9 @@ them (src/storage_codecs.cpp, src/numerics.cpp, src/accelerate_backend.cpp,
   numerics.npz   makeSpdMatrix(n, cond) outputs, symmetricReferenceRoot of
                  them, and runAccelerateCase (src/accelerate_backend.cpp:
                  803-1091) residual/forward-error histories.
+  paper.npz      preparePaperMatrix (src/accelerate_backend.cpp:690-801)
+                 for the symmetric paper sets V, VI, VII at orders 32 and 64:
+                 the matrices, diagonal shifts and conditions.
   csv_headers.txt  writeSummaryHeader and writeIterationsHeader
                  (src/reporting.cpp:124-166, 305-327): the reference's CSV
                  schema, one header line each.
@@ -22,9 +25,9 @@ them (src/storage_codecs.cpp, src/numerics.cpp, src/accelerate_backend.cpp,
                  spectrum of checkStochasticQuantization and log-uniform
                  spectra with equal-valued blocks and a ragged tail.
 
-Usage: make -C oracle && python tests/golden/make_golden.py [csv | spectrum]
-(with `csv`, only csv_headers.txt is written; with `spectrum`, csv_headers.txt
-and spectrum.npz)
+Usage: make -C oracle && python tests/golden/make_golden.py [csv | paper | spectrum]
+(each option writes the files listed up to and including its own: csv_headers.txt,
+then paper.npz, then spectrum.npz)
 """
 from __future__ import annotations
 
@@ -127,11 +130,29 @@ def write_csv_headers() -> None:
     print("wrote", os.path.join(HERE, "csv_headers.txt"))
 
 
+def write_paper() -> None:
+    lib = O.ref()
+    lib.ref_paper_matrix.argtypes = [ctypes.c_int, ctypes.c_size_t, ctypes.c_void_p, ctypes.c_void_p]
+    out = {}
+    for test_set in (5, 6, 7):
+        for n in (32, 64):
+            a, meta = np.zeros(n * n), np.zeros(3)
+            assert lib.ref_paper_matrix(test_set, n, a.ctypes.data, meta.ctypes.data) == 0, \
+                lib.ref_last_error()
+            out[f"set{test_set}_n{n}"] = a
+            out[f"set{test_set}_n{n}_shift_condition"] = meta[:2]
+    np.savez_compressed(os.path.join(HERE, "paper.npz"), **out)
+    print("wrote", os.path.join(HERE, "paper.npz"))
+
+
 def main() -> None:
     if not O.ref_available():
         raise SystemExit("oracle/_ref/libmsq_ref.so missing: run `make -C oracle` first")
     write_csv_headers()
     if sys.argv[1:] == ["csv"]:
+        return
+    write_paper()
+    if sys.argv[1:] == ["paper"]:
         return
     write_spectrum()
     if sys.argv[1:] == ["spectrum"]:

@@ -149,3 +149,17 @@ def test_results_write_the_references_csv_schema(tmp_path):
         it = list(csv.reader(f))
     assert ",".join(it[0]) == golden[1]
     assert len(it) - 1 == int(r["iterations"]) + 1 and all(len(x) == len(it[0]) for x in it)
+
+
+@pytest.mark.parametrize("test_set,n", [(5, 1024), (6, 1024), (7, 1024), (5, 2048)])
+def test_paper_sets_reach_tolerance(tmp_path, test_set, n):
+    """The symmetric paper test sets (preparePaperMatrix, V: uniform, VI:
+    normal, shifted to a smallest eigenvalue of max(1, 0.01 ||A||_inf); VII:
+    Hilbert + 1e-6 I at its paper order 1024) through the mirror, against the
+    FP64 oracle root."""
+    a, shift, cond, seed = O.paper_matrix(test_set, n)
+    rc, r, err = _run(tmp_path, a, "bf16", 1e-12, 16)
+    assert rc == 0, err
+    assert r["status"] == "converged", r
+    assert float(r["final_residual"]) <= 1e-12
+    assert float(r["final_forward_error"]) < 1e-9 * max(1.0, cond / 1e3), r

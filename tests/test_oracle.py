@@ -1,5 +1,7 @@
 """CPU tests: the oracle restatement pinned against the reference's own
 outputs (tests/golden, produced by the reference's compiled CPU code)."""
+import os
+
 import numpy as np
 import pytest
 
@@ -117,3 +119,24 @@ def test_ff_residual_matches_fp64():
     rel, r = O.ff_residual(a, x)
     r64 = a.astype(np.float64) - x.astype(np.float64) @ x.astype(np.float64)
     assert abs(rel - np.linalg.norm(r64) / np.linalg.norm(a.astype(np.float64))) < 1e-12
+
+
+@pytest.mark.parametrize("test_set", [5, 6, 7])
+@pytest.mark.parametrize("n", [32, 64])
+def test_paper_sets_match_the_reference(test_set, n):
+    """preparePaperMatrix (src/accelerate_backend.cpp:690-801) for the
+    symmetric paper sets against the reference's own matrices
+    (tests/golden/paper.npz).  The shift of V and VI comes from FP64
+    extreme eigenvalues (numpy's LAPACK here, the reference's there), so the
+    diagonals agree to rounding of that eigenvalue."""
+    g = np.load(os.path.join(os.path.dirname(__file__), "golden", "paper.npz"))
+    ref = g[f"set{test_set}_n{n}"].reshape(n, n, order="F")
+    ref_shift, ref_cond = g[f"set{test_set}_n{n}_shift_condition"]
+    a, shift, cond, seed = O.paper_matrix(test_set, n)
+    off = ~np.eye(n, dtype=bool)
+    assert np.array_equal(a[off], ref[off])             # the generator, bit for bit
+    np.testing.assert_allclose(np.diag(a), np.diag(ref), rtol=1e-13, atol=0)
+    assert abs(shift - ref_shift) <= 1e-12 * max(1.0, ref_shift)
+    assert abs(cond - ref_cond) <= 1e-6 * ref_cond
+    if test_set != 7:
+        assert seed == (0x243F6A8885A308D3 ^ (0x9E3779B97F4A7C15 * test_set)) & (2**64 - 1)
