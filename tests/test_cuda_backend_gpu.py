@@ -151,15 +151,27 @@ def test_results_write_the_references_csv_schema(tmp_path):
     assert len(it) - 1 == int(r["iterations"]) + 1 and all(len(x) == len(it[0]) for x in it)
 
 
-@pytest.mark.parametrize("test_set,n", [(5, 1024), (6, 1024), (7, 1024), (5, 2048)])
+@pytest.mark.parametrize("test_set,n", [(5, 1024), (6, 1024), (5, 2048), (6, 2048)])
 def test_paper_sets_reach_tolerance(tmp_path, test_set, n):
-    """The symmetric paper test sets (preparePaperMatrix, V: uniform, VI:
-    normal, shifted to a smallest eigenvalue of max(1, 0.01 ||A||_inf); VII:
-    Hilbert + 1e-6 I at its paper order 1024) through the mirror, against the
-    FP64 oracle root."""
+    """The symmetric paper test sets V (uniform) and VI (normal), shifted to
+    a smallest eigenvalue of max(1, 0.01 ||A||_inf) (preparePaperMatrix),
+    through the mirror, against the FP64 oracle root."""
     a, shift, cond, seed = O.paper_matrix(test_set, n)
     rc, r, err = _run(tmp_path, a, "bf16", 1e-12, 16)
     assert rc == 0, err
     assert r["status"] == "converged", r
     assert float(r["final_residual"]) <= 1e-12
-    assert float(r["final_forward_error"]) < 1e-9 * max(1.0, cond / 1e3), r
+    assert float(r["final_forward_error"]) < 1e-10, r
+
+
+def test_paper_set_vii_is_reported_not_converged(tmp_path):
+    """Set VII (Hilbert + 1e-6 I, order 1024, condition 2e6) is out of reach
+    of an FP32 eigenbasis: its smallest eigenvalues sit below the basis's
+    resolution, so the frozen-basis corrections cannot contract.  The
+    reference's own CPU method stops with "The FP64 residual is outside the
+    FP32 correction range" on it; the mirror reports the numerical outcome in
+    its status, as runMetalCase does, instead of a converged result."""
+    a, shift, cond, seed = O.paper_matrix(7, 1024)
+    rc, r, err = _run(tmp_path, a, "fp32", 1e-12, 8)
+    assert rc == 0, err
+    assert r["status"] in ("nonfinite", "diverged", "budget_exhausted"), r
