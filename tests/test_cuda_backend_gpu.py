@@ -164,14 +164,24 @@ def test_paper_sets_reach_tolerance(tmp_path, test_set, n):
     assert float(r["final_forward_error"]) < 1e-10, r
 
 
-def test_paper_set_vii_is_reported_not_converged(tmp_path):
-    """Set VII (Hilbert + 1e-6 I, order 1024, condition 2e6) is out of reach
-    of an FP32 eigenbasis: its smallest eigenvalues sit below the basis's
-    resolution, so the frozen-basis corrections cannot contract.  The
-    reference's own CPU method stops with "The FP64 residual is outside the
-    FP32 correction range" on it; the mirror reports the numerical outcome in
-    its status, as runMetalCase does, instead of a converged result."""
+def test_paper_set_vii_with_the_fp32_basis(tmp_path):
+    """Set VII (Hilbert + 1e-6 I, order 1024, condition 2e6) with the FP32
+    basis converges: the float-float corrections from the FP32 root contract.
+    (The reference's CPU plain method stops on it with "The FP64 residual is
+    outside the FP32 correction range".)"""
     a, shift, cond, seed = O.paper_matrix(7, 1024)
-    rc, r, err = _run(tmp_path, a, "fp32", 1e-12, 8)
+    rc, r, err = _run(tmp_path, a, "fp32", 1e-12, 12)
+    assert rc == 0, err
+    assert r["status"] == "converged" and float(r["final_residual"]) <= 1e-12, r
+    assert float(r["final_forward_error"]) < 1e-8, r
+
+
+def test_paper_set_vii_with_a_bf16_basis_reports_its_outcome(tmp_path):
+    """With a BF16 basis the initial root of set VII is about 1e-3 off while
+    its smallest roots are about 1e-3: outside the frozen-basis corrections'
+    contraction region.  The mirror reports that numerical outcome in its
+    status, as runMetalCase does, instead of raising or claiming convergence."""
+    a, shift, cond, seed = O.paper_matrix(7, 1024)
+    rc, r, err = _run(tmp_path, a, "bf16", 1e-12, 8)
     assert rc == 0, err
     assert r["status"] in ("nonfinite", "diverged", "budget_exhausted"), r
