@@ -183,8 +183,11 @@ residualFFKernel(ResidualArgs args) {
             const f32x2 z = f2sub(t, s2[r][q]);
             const f32x2 se = f2sub(f2sub(s2[r][q], f2sub(t, z)), f2add(m, z));
             s2[r][q] = t;
-            const f32x2 cross = f2fma(a2, bl[q], f2mul(l2, bh[q]));
-            comp2[r][q] = f2add(comp2[r][q], f2add(f2add(se, pe), cross));
+            // low-order terms: the cross products hi*lo' and lo*hi' fused into
+            // comp (comp is ~2^-24 of s, so its roundings stay ~2^-48 of s)
+            f32x2 c = f2fma(a2, bl[q], comp2[r][q]);
+            c = f2fma(l2, bh[q], c);
+            comp2[r][q] = f2add(c, f2add(se, pe));
           }
         }
       }
