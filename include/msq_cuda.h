@@ -33,7 +33,7 @@ enum {
   MSQ_ERR_CUDA = 2,             /* a CUDA runtime/driver call failed        */
   MSQ_ERR_DEVICE_STATUS = 3,    /* a kernel reported an error flag (bounded
                                    wait expired, index out of range)         */
-  MSQ_ERR_UNSUPPORTED = 4       /* valid request this build does not serve  */
+  MSQ_ERR_UNSUPPORTED = 4       /* valid request the library does not serve */
 };
 
 /* ---- storage formats ----------------------------------------------------
