@@ -64,3 +64,81 @@ def test_two_level_oracle_converges_like_round_robin():
         assert ratio <= 1e-4 and abs(tl - rr) <= 1
         lam = np.linalg.eigvalsh(a)
         assert np.abs(np.sort(w) - lam).max() <= 3 * n * 2.0 ** -24 * lam.max()
+
+
+def _round_tables(pairs, nb):
+    slot, partner = [0] * nb, [0] * nb
+    for k, (i, j, on) in enumerate(pairs):
+        slot[i] = slot[j] = k
+        partner[i], partner[j] = (j, i) if on else (-1, -1)
+    return slot, partner
+
+
+def _folded(w, p):
+    """The sweep kernel's folded enumeration of the pairs k <= l."""
+    q = p + 1
+    r, c = divmod(w, q)
+    if c < p - r:
+        return r, r + c
+    if (p & 1) and r == p // 2:
+        return None
+    return p - 1 - r, c - 1
+
+
+def _check_overlap(nb, rounds):
+    """The overlapped round of the sweep kernel: each pivot quad of round
+    r+1 computes (or waits for the owner of) the super-tile of round r that
+    holds its cross tile; the other warps take every super-tile the
+    criticality test leaves.  Every super-tile of r must be updated exactly
+    once and every next cross tile must be covered.  Returns the number of
+    shared super-tiles (a quad waits on another's flag)."""
+    p = nb // 2
+    items = ((p + 1) // 2) * (p + 1)
+    shared = 0
+    for r in range(len(rounds) - 1):
+        cur, nxt = rounds[r], rounds[r + 1]
+        cs, _ = _round_tables(cur, nb)
+        ns, npart = _round_tables(nxt, nb)
+        owned, needs = {}, {}
+        for kk, (x, y, on) in enumerate(nxt):
+            if not on or cs[x] == cs[y]:
+                continue
+            k, l = cs[x], cs[y]
+            ox, oy = cur[k][0] + cur[k][1] - x, cur[l][0] + cur[l][1] - y
+            owner = ns[ox] if (npart[ox] == oy and min(ox, oy) < min(x, y)) else kk
+            shared += owner != kk
+            item = (min(k, l), max(k, l))
+            needs[kk] = (item, owner)
+            if owner == kk:
+                assert item not in owned
+                owned[item] = kk
+        assert all(owned.get(item) == owner for item, owner in needs.values())
+        done = set(owned)
+        for w in range(items):
+            f = _folded(w, p)
+            if f is None or f[0] == f[1]:
+                continue
+            k, l = f
+            p1, p2 = npart[cur[k][0]], npart[cur[k][1]]
+            critical = (p1 >= 0 and cs[p1] == l) or (p2 >= 0 and cs[p2] == l)
+            assert critical == (f in owned)
+            if not critical:
+                assert f not in done
+                done.add(f)
+        assert done == {(k, l) for k in range(p) for l in range(k + 1, p)}
+    return shared
+
+
+@pytest.mark.parametrize("nb", [2, 4, 6, 10, 16, 40, 64, 82, 128])
+def test_overlapped_round_covers_every_super_tile_round_robin(nb):
+    rounds = [[(*sorted(_rr_pair(k, r, nb)), True) for k in range(nb // 2)] for r in range(nb - 1)]
+    _check_overlap(nb, rounds)
+
+
+@pytest.mark.parametrize("nb", [66, 82, 98, 114, 128])
+def test_overlapped_round_covers_every_super_tile_two_level(nb):
+    table = O.two_level_schedule(nb).reshape(-1, 2)
+    p = nb // 2
+    rounds = [[(int(i), int(j) if j >= 0 else -1 - int(j), bool(j >= 0)) for i, j in table[r * p:(r + 1) * p]]
+              for r in range(len(table) // p)]
+    assert _check_overlap(nb, rounds) > 0   # shared super-tiles occur: the flag path is exercised
