@@ -242,8 +242,13 @@ int msq_autotune_reset(int enable);
  * on it and corrupt each other's results, so issue them on one stream.
  * `stream` is a cudaStream_t (NULL: the default stream); `matrix` is
  * overwritten as in msq_jacobi_batched; sweeps_done / off_ratio are device
- * pointers to one element each, or NULL.  The call is asynchronous; a CUDA
- * launch error returns MSQ_ERR_CUDA.                                        */
+ * pointers to one element each, or NULL.  The call is asynchronous and never
+ * synchronises, so a bounded device wait that expires (the condition
+ * msq_jacobi_batched returns as MSQ_ERR_DEVICE_STATUS) is reported in the
+ * outputs instead: every eigenvalue is NaN, *sweeps_done is -1 and
+ * *off_ratio NaN.  A CUDA error already pending on the calling thread is
+ * left in place and returned as MSQ_ERR_CUDA before anything is launched; a
+ * launch error of this call returns MSQ_ERR_CUDA.                           */
 #define MSQ_NOALLOC_MAX_ORDER 256
 int msq_jacobi_noalloc(float *matrix, float *vectors, float *eigenvalues, int n,
                        double tolerance, int max_sweeps, void *stream,

@@ -89,7 +89,7 @@ __device__ __forceinline__ SplitTiles tileMem(std::false_type, float *s, float *
 
 // Entries (16-bit) of one round table of the sweep kernel: pairs (I, J),
 // rotate flags, per block its pair and its partner (-1: not rotated).
-__host__ __device__ __forceinline__ int roundTableShorts(int nb) { return 3 * (nb / 2) + 2 * nb; }
+__host__ __device__ constexpr int roundTableShorts(int nb) { return 3 * (nb / 2) + 2 * nb; }
 
 // One round's table in shared memory and its P 8x8 rotations (kQS floats
 // apart).
@@ -110,8 +110,8 @@ constexpr int kFlagWaitLimit = 1 << 22;
 // Shared memory of the sweep kernel: reduction scratch; the tile table, two
 // work counters, P done flags and three round tables; the rotations of two
 // rounds; then the packed tiles (with_tiles).
-__host__ __device__ __forceinline__ size_t sweepSmemLayout(int n, bool with_tiles, size_t *q_off,
-                                                           size_t *tile_off) {
+__host__ __device__ constexpr size_t sweepSmemLayout(int n, bool with_tiles, size_t *q_off,
+                                                    size_t *tile_off) {
   const int m = padded8(n), nb = m / 4, P = nb / 2;
   size_t bytes = 32 * sizeof(double) + (nb + 1 + 2 + P) * sizeof(int) +
                  3 * roundTableShorts(nb) * sizeof(short);
@@ -1382,7 +1382,10 @@ static __device__ __align__(256) unsigned char g_noalloc_scratch[sizeof(NoAllocS
 // Device address of g_noalloc_scratch per device, looked up once per device
 // (cudaGetSymbolAddress with that device current).  Host code must not use
 // the symbol itself: on the host it names a stand-in, not device memory.
-NoAllocScratch *g_noalloc_address[64] = {};
+// The entries are atomic and the one-time set-up is serialised, so two host
+// threads making their first call on one device at once are safe.
+std::atomic<NoAllocScratch *> g_noalloc_address[64] = {};
+std::mutex g_noalloc_setup_mutex;
 
 // Resets what must start at zero (the sweep state and the kernels' status
 // word) and writes the one-matrix layout tables; the tiles and the log are
@@ -1405,6 +1408,32 @@ __global__ void noAllocSetupKernel(NoAllocScratch *s, int n) {
   }
 }
 
+// Writes the call's report and makes a bounded-wait expiry visible: with the
+// status word set, the eigenvalues become NaN, sweeps_done -1 and off_ratio
+// NaN, so a caller sees the failure even with NULL report pointers and
+// without a host synchronisation.
+__global__ void noAllocReportKernel(const NoAllocScratch *s, float *eigenvalues, int n,
+                                    int32_t *sweeps_done, float *off_ratio) {
+  const bool failed = s->status[0] != 0;
+  if (failed) {
+    for (int i = threadIdx.x; i < n; i += blockDim.x) eigenvalues[i] = __int_as_float(0x7fc00000);
+  }
+  if (threadIdx.x == 0) {
+    if (sweeps_done != nullptr) sweeps_done[0] = failed ? -1 : s->state[0].sweeps;
+    if (off_ratio != nullptr) {
+      off_ratio[0] = failed ? __int_as_float(0x7fc00000) : static_cast<float>(s->state[0].off_ratio);
+    }
+  }
+}
+
+// Every order the entry point accepts keeps its tiles in shared memory.
+constexpr size_t sharedTileSweepBytes(int n) {
+  size_t q_off = 0, tile_off = 0;
+  return sweepSmemLayout(n, true, &q_off, &tile_off);
+}
+static_assert(sharedTileSweepBytes(kNoAllocOrder) <= kSweepSmemLimit,
+              "orders up to MSQ_NOALLOC_MAX_ORDER use the shared-tile sweep");
+
 }  // namespace
 }  // namespace msq
 
@@ -1416,19 +1445,26 @@ extern "C" int msq_jacobi_noalloc(float *matrix, float *vectors, float *eigenval
   }
   if (n < 1 || n > kNoAllocOrder) return MSQ_ERR_INVALID_ARGUMENT;  // beyond the static scratch
   if (!(tolerance >= 0.0) || max_sweeps < 0 || max_sweeps > 64) return MSQ_ERR_INVALID_ARGUMENT;
+  // An error already pending on this thread belongs to the caller's earlier
+  // work: leave it in place for the caller and launch nothing.
+  if (cudaPeekAtLastError() != cudaSuccess) return MSQ_ERR_CUDA;
   int device = 0;
   if (cudaGetDevice(&device) != cudaSuccess || device < 0 || device >= 64) return MSQ_ERR_CUDA;
-  NoAllocScratch *s = g_noalloc_address[device];
+  NoAllocScratch *s = g_noalloc_address[device].load(std::memory_order_acquire);
   if (s == nullptr) {
     // One-time set-up for this device (so the first call on a device should
     // come before any stream capture).
-    void *address = nullptr;
-    if (cudaGetSymbolAddress(&address, g_noalloc_scratch) != cudaSuccess || address == nullptr) {
-      return MSQ_ERR_CUDA;
+    std::lock_guard<std::mutex> lock(g_noalloc_setup_mutex);
+    s = g_noalloc_address[device].load(std::memory_order_acquire);
+    if (s == nullptr) {
+      void *address = nullptr;
+      if (cudaGetSymbolAddress(&address, g_noalloc_scratch) != cudaSuccess || address == nullptr) {
+        return MSQ_ERR_CUDA;
+      }
+      if (setKernelAttributes() != MSQ_OK) return MSQ_ERR_CUDA;
+      s = static_cast<NoAllocScratch *>(address);
+      g_noalloc_address[device].store(s, std::memory_order_release);
     }
-    if (setKernelAttributes() != MSQ_OK) return MSQ_ERR_CUDA;
-    s = static_cast<NoAllocScratch *>(address);
-    g_noalloc_address[device] = s;
   }
   cudaStream_t st = static_cast<cudaStream_t>(stream);
   noAllocSetupKernel<<<1, 128, 0, st>>>(s, n);
@@ -1447,9 +1483,8 @@ extern "C" int msq_jacobi_noalloc(float *matrix, float *vectors, float *eigenval
   args.tol = tolerance;
   args.max_sweeps = max_sweeps;
   args.status = s->status;
-  const bool smem = fitsSmem(n);
   size_t q_off, tile_off;
-  const size_t sweep_smem = sweepSmemLayout(n, smem, &q_off, &tile_off);
+  const size_t sweep_smem = sweepSmemLayout(n, true, &q_off, &tile_off);
   const int rows = (n + kNoAllocRowsPerCta - 1) / kNoAllocRowsPerCta;
   VArgs vargs{vectors, s->a_offset, s->log_offset, s->n, s->log, s->state,
               s->work_matrix, s->work_row, kNoAllocRowsPerCta};
@@ -1457,15 +1492,10 @@ extern "C" int msq_jacobi_noalloc(float *matrix, float *vectors, float *eigenval
   identityKernel<<<dim3(64, 1), 256, 0, st>>>(vectors, s->a_offset, s->n, 1);
   for (int launch = 0; launch <= max_sweeps; ++launch) {
     args.first = launch == 0;
-    if (smem) {
-      jacobiSweepKernel<true><<<1, threadsFor(n), sweep_smem, st>>>(args);
-    } else {
-      jacobiSweepKernel<false><<<1, threadsFor(n), sweep_smem, st>>>(args);
-    }
+    jacobiSweepKernel<true><<<1, threadsFor(n), sweep_smem, st>>>(args);
     if (launch < max_sweeps) jacobiReplayKernel<<<rows, kReplayThreads, v_smem, st>>>(vargs);
   }
-  if (sweeps_done != nullptr || off_ratio != nullptr) {
-    jacobiReportKernel<<<1, 32, 0, st>>>(s->state, 1, sweeps_done, off_ratio);
-  }
+  noAllocReportKernel<<<1, 256, 0, st>>>(s, eigenvalues, n, sweeps_done, off_ratio);
+  // nothing was pending on entry, so an error here comes from these launches
   return cudaGetLastError() == cudaSuccess ? MSQ_OK : MSQ_ERR_CUDA;
 }

@@ -25,7 +25,7 @@ them (src/storage_codecs.cpp, src/numerics.cpp, src/accelerate_backend.cpp,
                  spectrum of checkStochasticQuantization and log-uniform
                  spectra with equal-valued blocks and a ragged tail.
 
-Usage: make -C oracle && python tests/golden/make_golden.py [csv | paper | spectrum]
+Usage: make -C oracle REF=<reference checkout> && python tests/golden/make_golden.py [csv | paper | spectrum]
 (each option writes the files listed up to and including its own: csv_headers.txt,
 then paper.npz, then spectrum.npz)
 """
@@ -147,7 +147,7 @@ def write_paper() -> None:
 
 def main() -> None:
     if not O.ref_available():
-        raise SystemExit("oracle/_ref/libmsq_ref.so missing: run `make -C oracle` first")
+        raise SystemExit("oracle/_ref/libmsq_ref.so missing: run `make -C oracle REF=<reference checkout>` first")
     write_csv_headers()
     if sys.argv[1:] == ["csv"]:
         return
