@@ -94,19 +94,29 @@ def whole_job(accepted: float, ms: float, world: int, device) -> tuple:
     return float(acc.item()), float(t.item())
 
 
+def wishart_matrix(n: int, seed: int) -> np.ndarray:
+    """Matrix `seed` of the workload: A = X^T X / m + 1e-6 I, X ~ N(0,1) of
+    shape m x n (m = 2n) from numpy's default_rng(seed), FP64, symmetrised.
+    Both arms of the benchmark solve these same matrices."""
+    x = np.random.default_rng(seed).standard_normal((2 * n, n))
+    a = x.T @ x / (2 * n) + 1e-6 * np.eye(n)
+    return 0.5 * (a + a.T)
+
+
+def matrix_seed(base: int, i: int) -> int:
+    return base * 1_000_003 + i
+
+
 def make_batch(msq, torch, orders, seed, device):
-    """Wishart matrices generated on the GPU (FP64), stored FP32, packed."""
+    """The workload's Wishart matrices (wishart_matrix, generated on the
+    host), stored FP32, packed column-major, copied to the device."""
     batch = msq.Batch.from_orders(orders)
-    flat = torch.zeros(batch.total, dtype=torch.float32, device=device)
-    g = torch.Generator(device=device).manual_seed(seed)
+    flat = np.zeros(batch.total, dtype=np.float32)
     for i, n in enumerate(orders):
         n = int(n)
-        x = torch.randn(2 * n, n, generator=g, device=device, dtype=torch.float64)
-        a = x.T @ x / (2 * n) + 1e-6 * torch.eye(n, device=device, dtype=torch.float64)
-        a = 0.5 * (a + a.T)
         o = int(batch.offset[i])
-        flat[o:o + n * n] = a.T.reshape(-1).to(torch.float32)  # column-major
-    return batch, flat
+        flat[o:o + n * n] = wishart_matrix(n, matrix_seed(seed, i)).reshape(-1, order="F")
+    return batch, torch.from_numpy(flat).to(device)
 
 
 class ClockSampler:
@@ -193,36 +203,49 @@ def cpu_baseline(oracle, mats, budget_s: float) -> dict:
 
 
 def run_reference(args):
-    """--impl reference: the reference's CPU path (oracle port of
-    runAccelerateCase; the reference's own build is x86-only here) on the
-    host cores, same metric and workload: each step times a stratified
-    sample of 64 of the 4096 matrices (bounded to ~20 s)."""
+    """--impl reference: the reference's CPU plain method (runAccelerateCase,
+    src/accelerate_backend.cpp:803-1091, as the oracle's numpy/LAPACK port:
+    the reference's own C++ is compiled only where its sources are, and the
+    GPU host has none) on the host cores.  Same matrices as the GPU arm
+    (wishart_matrix with the same seeds), same tolerance.  A step is one
+    pass over a stratified sample of 64 of the 4096 matrices; ms_per_step is
+    that pass's measured time and value its accepted solves per second."""
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
         return
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import oracle as O
-    orders = workload_orders(COUNT, 1234)
+    orders, base = rank_shard(COUNT, 0)
     sample = stratified(orders)
-    mats = {int(i): O.wishart(int(orders[i]), seed=int(i)) for i in sample}
+    # the FP32 rounding the GPU arm's input has, back in FP64
+    mats = {int(i): wishart_matrix(int(orders[i]), matrix_seed(base, int(i)))
+            .astype(np.float32).astype(np.float64) for i in sample}
     for _ in range(args.warmup):
         O.plain_method(mats[int(sample[0])], 12, TOL)
-    per, oks = [], []
+    ms_steps, oks = [], []
     for _ in range(args.steps):
-        p, ok, _ = time_plain(O, mats, sample, 20.0)
-        per.append(p)
+        t0 = time.perf_counter()
+        ok = 0
+        for idx in sample:
+            _, hist = O.plain_method(mats[int(idx)], 12, TOL)
+            ok += hist[-1] <= TOL
+        ms_steps.append((time.perf_counter() - t0) * 1e3)
         oks.append(ok)
-    per_solve = statistics.mean(per)
-    value = statistics.mean(oks) / per_solve
+    ms = statistics.mean(ms_steps)
+    value = statistics.mean(oks) / (ms / 1e3)
     cores = os.cpu_count() or 1
+    sample_text = (f"{len(sample)} of the {COUNT} matrices per step (stratified by n, the GPU "
+                   f"arm's matrices and seeds), OpenBLAS threads="
+                   f"{os.environ.get('OPENBLAS_NUM_THREADS', cores)}")
     line = {"metric": METRIC, "value": value, "unit": "solves/s", "n_gpus": args.gpus,
-            "steps": args.steps, "warmup": args.warmup, "ms_per_step": per_solve * COUNT * 1e3,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "fp32",
-            "data": "synthetic", "impl": "reference",
-            "config": {"workload": f"{COUNT} Wishart SPD (m=2n), n log-uniform [{N_LO},{N_HI}], tol 1e-5"},
+            "data": "synthetic (seeded Wishart, same matrices as the GPU arm)", "impl": "reference",
+            "config": {"workload": f"{COUNT} Wishart SPD A=X^T X/m+1e-6 I (m=2n), n log-uniform "
+                                   f"[{N_LO},{N_HI}], FP32 input, tol 1e-5",
+                       "sample_per_step": len(sample)},
             "cpu_baseline": {"value": value, "unit": "solves/s", "cores": cores, "kind": "port",
-                             "sample": f"{len(sample)} of {COUNT} matrices per step (stratified by n), "
-                                       f"<=20 s per step"},
+                             "sample": sample_text},
             "e2e": {"value": value, "unit": "solves/s", "h2d_bytes_per_step": 0,
                     "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
@@ -380,6 +403,213 @@ def run_selector(args):
     }), flush=True)
 
 
+def _spd_gpu(torch, lam, seed, device):
+    """A = Q diag(lam) Q^T in FP64 on the GPU, Q from QR of a seeded N(0,1)
+    matrix with the signs of R's diagonal fixed; returned rounded to FP32
+    (what the solver sees) and as the FP64 image of that rounding."""
+    n = lam.numel()
+    g = torch.Generator(device=device).manual_seed(seed)
+    q, r = torch.linalg.qr(torch.randn(n, n, generator=g, device=device, dtype=torch.float64))
+    q = q * torch.sign(torch.diagonal(r))
+    a = (q * lam) @ q.T
+    a32 = (0.5 * (a + a.T)).to(torch.float32)
+    return a32, a32.to(torch.float64)
+
+
+def _fp64_errors(torch, a64, x32, root):
+    """||A - X^2||_F / ||A||_F and ||X - X_fp64||_F / ||X_fp64||_F in FP64."""
+    x = x32.to(torch.float64)
+    resid = float(torch.linalg.norm(a64 - x @ x) / torch.linalg.norm(a64))
+    err = None if root is None else float(torch.linalg.norm(x - root) / torch.linalg.norm(root))
+    return resid, err
+
+
+def _plan_flops(n: int, jacobi_sweeps: int, corrections: int) -> float:
+    """Algorithmic flops of one solve: Jacobi 6 n^3 per sweep (A and V
+    updates), reconstruction 2 n^3, per correction 8 n^3 (four GEMMs) + 2 n^3
+    (residual), and the residual of X0 2 n^3."""
+    n3 = float(n) ** 3
+    return 6 * n3 * jacobi_sweeps + 2 * n3 + 10 * n3 * corrections + 2 * n3
+
+
+def _time_solve(torch, ctx, a, batch, plan, out, reps: int = 1, warm: bool = True):
+    if warm:
+        ctx.solve_batched(a, batch, [plan], TOL, out=out)  # layouts, graphs, tuner
+    torch.cuda.synchronize()
+    s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    s.record()
+    for _ in range(reps):
+        _, res = ctx.solve_batched(a, batch, [plan], TOL, out=out)
+    e.record()
+    torch.cuda.synchronize()
+    return s.elapsed_time(e) / reps, res[0]
+
+
+C2_ALL = [(n, c, p) for n in (1024, 2048, 4096) for c in (1e2, 1e4, 1e6)
+          for p in ("fp32", "bf16+0", "bf16+1", "bf16+2", "fp8row+0", "fp8row+1", "fp8row+2")]
+# the default line's share of the grid (about half a minute of GPU time):
+# every plan at n = 1024 and 2048, the two-sweep plans and FP32 at n = 4096
+C2_DEFAULT = [(n, c, p) for (n, c, p) in C2_ALL
+              if n < 4096 or (c == 1e2 and p in ("fp32", "bf16+2", "fp8row+2"))]
+
+
+def c2_table(msq, torch, ctx, cases=C2_ALL) -> list:
+    """The single-matrix low-bit grid: per (n, condition) one seeded
+    Gaussian-QR matrix with log-uniform spectrum, its FP64 root (dsyevd of the
+    FP32-rounded matrix, cuSOLVER, untimed), then each plan of `cases` among
+    {FP32 plain, BF16, FP8 per-row} x {0, 1, 2} corrections: device time of
+    one solve (after a warm-up below n = 2048, where first-call set-up is not
+    negligible), solves/s, algorithmic TFLOP/s, FP64 residual and forward
+    error, and whether the plan met 1e-5 itself or fell back to FP32."""
+    jt = {0: 1e-4, 1: 1e-4, 2: 1e-3}
+    fmt_id = {"fp32": msq.PLAN_FP32, "bf16": msq.PLAN_BF16, "fp8row": msq.PLAN_FP8}
+    rows = []
+    for n, cond in sorted({(n, c) for n, c, _ in cases}):
+        seed = n + int(np.log10(cond))
+        g = torch.Generator(device="cuda").manual_seed(seed + 1)
+        lam = torch.exp(torch.empty(n, dtype=torch.float64, device="cuda").uniform_(
+            float(np.log(1.0 / cond)), 0.0, generator=g))
+        lam[0], lam[-1] = 1.0, 1.0 / cond
+        a32, a64 = _spd_gpu(torch, lam, seed, "cuda")
+        w, v = torch.linalg.eigh(a64)
+        root = (v * torch.sqrt(w)) @ v.T
+        root = 0.5 * (root + root.T)
+        del w, v
+        batch = msq.Batch.from_orders([n])
+        a = a32.T.contiguous().reshape(-1)  # column-major (symmetric anyway)
+        out = torch.empty_like(a)
+        for nn, cc, p in cases:
+            if (nn, cc) != (n, cond):
+                continue
+            name, k = (p.split("+") + ["1"])[:2]
+            k = int(k)
+            plan = msq.plan(fmt_id[name], k, 1e-7 if name == "fp32" else jt[k], 20)
+            ms, r = _time_solve(torch, ctx, a, batch, plan, out, warm=n < 2048)
+            resid, err = _fp64_errors(torch, a64, out.view(n, n).T, root)
+            flops = _plan_flops(n, r.jacobi_sweeps, r.corrections)
+            rows.append({"n": n, "cond": cond, "format": name, "sweeps": k,
+                         "ms": round(ms, 3), "solves_s": round(1e3 / ms, 2),
+                         "tflops": round(flops / (ms / 1e3) / 1e12, 2),
+                         "residual_fp64": resid, "error_fp64": err,
+                         "plan_residual": r.plan_residual, "accepted": bool(r.accepted),
+                         "fallback": bool(r.fallback), "jacobi_sweeps": r.jacobi_sweeps,
+                         "corrections": r.corrections})
+        del a32, a64, root, a, out
+        torch.cuda.empty_cache()
+    return rows
+
+
+def c3_entry(msq, torch, ctx, warm: bool = False) -> dict:
+    """n = 8192, condition 1e4, clustered spectrum (90% of the eigenvalues in
+    [0.9, 1.1], 10% log-uniform down to 1e-4), MXFP4 basis + 2 corrections:
+    device time of one solve, whether the plan met 1e-5 or fell back, the
+    FP64 residual of the returned root, and the block-scaled reconstruction
+    stage (kind::mxf4) timed alone over five launches on an order-8192 FP32
+    factor (the launch timer), as TFLOP/s of its 2 n^3 flops."""
+    n, cond = 8192, 1e4
+    g = torch.Generator(device="cuda").manual_seed(8193)
+    k = n // 10
+    lam = torch.empty(n, dtype=torch.float64, device="cuda")
+    lam[: n - k].uniform_(0.9, 1.1, generator=g)
+    lam[n - k:] = torch.exp(torch.empty(k, dtype=torch.float64, device="cuda").uniform_(
+        float(np.log(1.0 / cond)), float(np.log(0.9)), generator=g))
+    lam[-1] = 1.0 / cond
+    a32, a64 = _spd_gpu(torch, lam, 8192, "cuda")
+    batch = msq.Batch.from_orders([n])
+    a = a32.T.contiguous().reshape(-1)
+    del a32
+    out = torch.empty_like(a)
+    plan = msq.plan(msq.PLAN_MXFP4, 2, 1e-3, 20)
+    ms, r = _time_solve(torch, ctx, a, batch, plan, out, warm=warm)
+    resid, _ = _fp64_errors(torch, a64, out.view(n, n).T, None)
+    del a64
+    ctx.reconstruct_factor(msq.PLAN_MXFP4, a, batch, out=out)  # the stage, warm
+    torch.cuda.synchronize()
+    msq.lib().msq_timing_begin(ctx.handle)
+    for _ in range(5):
+        ctx.reconstruct_factor(msq.PLAN_MXFP4, a, batch, out=out)
+    torch.cuda.synchronize()
+    rows = timing_report(msq, ctx)
+    rec = rows.get("tcgen05 reconstruction", (0, 0.0))
+    rec_ms = rec[1] / max(rec[0], 1)
+    pack = rows.get("pack block-scaled operand", (0, 0.0))
+    return {"n": n, "cond": cond, "plan": "MXFP4 + 2 corrections", "ms": round(ms, 2),
+            "solves_s": 1e3 / ms,
+            "tflops": _plan_flops(n, r.jacobi_sweeps, r.corrections) / (ms / 1e3) / 1e12,
+            "residual_fp64": resid, "plan_residual": r.plan_residual,
+            "initial_residual": r.initial_residual,
+            "accepted": bool(r.accepted), "fallback": bool(r.fallback),
+            "jacobi_sweeps": r.jacobi_sweeps, "corrections": r.corrections,
+            "reconstruction": {"kernel": "tcGemmKernel kind::mxf4 block_scale", "ms": rec_ms,
+                               "tflops": 2.0 * n ** 3 / (rec_ms / 1e3) / 1e12 if rec_ms > 0 else None,
+                               "pack_ms": pack[1] / max(pack[0], 1)}}
+
+
+def run_mxf4(args):
+    """Secondary line: the block-scaled reconstruction stage X = Q(W) Q(W)^T of
+    one order-8192 FP32 factor (256 MB, larger than L2) with W quantized to
+    MXFP4 per row block of 32 (kind::mxf4) and, for comparison, to BF16
+    (kind::f16).  2 n^3 flops per launch; device time of each stage's GEMM
+    kernel from the launch timer (CUDA events on the launching stream)."""
+    import torch
+    msq = importlib.import_module("mixed-mlx_gb300")
+    ctx = msq.Context(0)
+    n = 8192
+    g = torch.Generator(device="cuda").manual_seed(11)
+    f = torch.randn(n * n, generator=g, device="cuda") / float(np.sqrt(n))
+    batch = msq.Batch.from_orders([n])
+    out = torch.empty_like(f)
+    res = {}
+    for name, plan in (("mxfp4", msq.PLAN_MXFP4), ("bf16", msq.PLAN_BF16)):
+        for _ in range(max(1, args.warmup)):
+            ctx.reconstruct_factor(plan, f, batch, out=out)
+        torch.cuda.synchronize()
+        msq.lib().msq_timing_begin(ctx.handle)
+        for _ in range(args.steps):
+            ctx.reconstruct_factor(plan, f, batch, out=out)
+        torch.cuda.synchronize()
+        rows = timing_report(msq, ctx)
+        cnt, tot = rows.get("tcgen05 reconstruction", (0, 0.0))
+        res[name] = {"gemm_ms": tot / max(cnt, 1), "launches": cnt,
+                     "tflops": 2.0 * n ** 3 / (tot / max(cnt, 1) / 1e3) / 1e12,
+                     "pack_ms": sum(v[1] for k, v in rows.items() if k.startswith("pack")) / max(cnt, 1)}
+    peaks = {}
+    try:
+        peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+    except OSError:
+        pass
+    fp4_nominal = 13500.0
+    m = res["mxfp4"]
+    print(json.dumps({
+        "metric": "block-scaled MXFP4 reconstruction X = Q(W) Q(W)^T, n = 8192", "value": m["tflops"],
+        "unit": "TFLOP/s", "n_gpus": 1, "steps": args.steps, "warmup": max(1, args.warmup),
+        "ms_per_step": m["gemm_ms"], "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "e2m1 (ue8m0 / 32)", "data": "synthetic N(0,1)/sqrt(n), seeded",
+        "config": {"workload": "order-8192 FP32 factor quantized per row block of 32, tcgen05 kind::mxf4",
+                   "l2": "factor 256 MB > L2"},
+        "roofline": {"bound": "tensor", "achieved": m["tflops"], "peak": fp4_nominal,
+                     "unit": "TFLOP/s", "frac": m["tflops"] / fp4_nominal, "traffic": None,
+                     "kernel": "tcGemmKernel<kOpMxf4> (kind::mxf4 block_scale)",
+                     "peak_source": "nominal dense FP4 (no FP4 figure among the measured peaks); "
+                                    "of measured BF16 %.0f TFLOP/s: %.2f" % (
+                                        peaks.get("bf16_tflops", 1900.0),
+                                        m["tflops"] / peaks.get("bf16_tflops", 1900.0))},
+        "stages": res}), flush=True)
+
+
+def run_c2(args):
+    import torch
+    msq = importlib.import_module("mixed-mlx_gb300")
+    ctx = msq.Context(0)
+    t0 = time.perf_counter()
+    rows = c2_table(msq, torch, ctx)
+    t1 = time.perf_counter()
+    c3 = c3_entry(msq, torch, ctx)
+    print(json.dumps({"metric": "single-matrix low-bit grid (C2) and n=8192 MXFP4 (C3)",
+                      "c2": rows, "c3": c3, "wall_s": {"c2": t1 - t0, "c3": time.perf_counter() - t1}}),
+          flush=True)
+
+
 def timing_report(msq, ctx) -> dict:
     import ctypes
     buf = ctypes.create_string_buffer(1 << 16)
@@ -401,9 +631,11 @@ def main():
     ap.add_argument("--sweeps", type=int, default=1)
     ap.add_argument("--jacobi-tol", type=float, default=1e-3)
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-c2", action="store_true",
+                    help="skip the single-matrix grid and the n=8192 MXFP4 legs of the line")
     ap.add_argument("--selector", type=int, default=0,
                     help="batched workload: plans from the trained selector instead of BF16 + sweeps")
-    ap.add_argument("--workload", default="batched", choices=["batched", "codec", "selector"],
+    ap.add_argument("--workload", default="batched", choices=["batched", "codec", "selector", "c2", "mxf4"],
                     help="codec: MXFP4 round trip of 2^26 N(0,1) values; selector: learned plan "
                          "selection on held-out matrices (secondary lines)")
     args = ap.parse_args()
@@ -413,6 +645,10 @@ def main():
         return run_codec(args)
     if args.workload == "selector":
         return run_selector(args)
+    if args.workload == "c2":
+        return run_c2(args)
+    if args.workload == "mxf4":
+        return run_mxf4(args)
 
     import torch
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -553,17 +789,34 @@ def main():
             torch.distributed.barrier()
         return
 
-    # accuracy vs the FP64 oracle on a stratified sample (outside timing)
-    sys.path.insert(0, os.path.join(ROOT, "oracle"))
-    import oracle as O
+    # accuracy (outside timing): every root's FP64 residual on the host,
+    # ||A - X^2||_F / ||A||_F, and the forward error against the FP64
+    # eigendecomposition root (dsyevd) on a stratified sample of 512
     roots = root.cpu().numpy()
     a_host = a.cpu().numpy()
     mats = batch.unpack(a_host)
     xs = batch.unpack(roots)
-    idx = np.argsort(orders)[:: max(1, batch.count // 128)]
-    errs = [O.relative_error(xs[i], O.reference_root(mats[i])) for i in idx]
-    resid = [O.relative_residual(mats[i], xs[i]) for i in idx]
+    resid_all = np.array([np.linalg.norm(m - x @ x) / np.linalg.norm(m) for m, x in zip(mats, xs)])
+    idx = np.argsort(orders)[:: max(1, batch.count // 512)]
+
+    def fp64_root(m):
+        w, v = np.linalg.eigh(m)
+        return (v * np.sqrt(w)) @ v.T
+
+    errs = [float(np.linalg.norm(xs[i] - fp64_root(mats[i])) / np.linalg.norm(fp64_root(mats[i])))
+            for i in idx]
     fallback = sum(r.fallback for r in res)
+    reported = np.array([r.final_residual for r in res])
+    # matrices the solver counted as meeting 1e-5 whose FP64 residual of the
+    # returned (FP32-rounded) root is above it
+    miscounted = int(np.sum((reported <= TOL) & (resid_all > TOL * (1 + 1e-2) + 1e-7)))
+    # the single-matrix grid and the order-8192 MXFP4 case (untimed legs)
+    c2 = c3 = None
+    if not args.no_c2:
+        c2 = c2_table(msq, torch, ctx, C2_DEFAULT)
+        c3 = c3_entry(msq, torch, ctx)
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle as O  # the CPU baseline leg only
 
     # roofline of the dominant kernel (largest share of the timed region)
     top = max(rows.items(), key=lambda kv: kv[1][1]) if rows else ("", (0, 0.0))
@@ -650,9 +903,14 @@ def main():
         "speedup_vs_plain_fp32": (value / plain_value) if plain_value > 0 else None,
         "accepted": acc, "fallback": int(fallback),
         "error_vs_fp64": {"p50": float(np.percentile(errs, 50)), "p99": float(np.percentile(errs, 99)),
-                          "residual_p50": float(np.percentile(resid, 50)),
-                          "residual_p99": float(np.percentile(resid, 99)),
-                          "sample": len(idx)},
+                          "forward_error_sample": len(idx),
+                          "residual_p50": float(np.percentile(resid_all, 50)),
+                          "residual_p99": float(np.percentile(resid_all, 99)),
+                          "residual_max": float(resid_all.max()),
+                          "residual_checked": int(resid_all.size),
+                          "met_tolerance_fp64": int(np.sum(resid_all <= TOL * (1 + 1e-2) + 1e-7)),
+                          "counted_but_missed": miscounted},
+        "c2": c2, "c3": c3,
         "kernels": {k: {"launches": v[0], "ms": v[1], "share": v[1] / total_ms} for k, v in rows.items()},
         "kernels_source": "launch timer over one extra step with concurrency off (serial)",
         "autotune": [l for l in ctx.autotune_report().splitlines() if l],

@@ -73,6 +73,19 @@ int msq_set_concurrency(msq_ctx *ctx, int enable);
  * enable = 0 launches every kernel directly (same results, bit for bit).   */
 int msq_set_graphs(msq_ctx *ctx, int enable);
 int msq_synchronize(msq_ctx *ctx);
+/* Failure injection for tests of the bounded device waits (process-wide,
+ * default 0).  mode 1: the batched Jacobi sweep kernels' shared-memory flag
+ * waits look for a value no warp writes, and their tile loads between
+ * sweeps wait on an mbarrier with no copy behind it; mode 2: every tcgen05
+ * GEMM launch first
+ * waits on an mbarrier nothing arrives at (before it issues any copy or
+ * MMA).  Each such wait gives up after a short limit, the launch unwinds,
+ * and the call's status check returns MSQ_ERR_DEVICE_STATUS ("bounded ...
+ * wait expired"); the context stays usable.  Results of the affected launches
+ * are meaningless.  Launches captured in CUDA graphs before the mode changed
+ * keep their setting: turn graphs off (msq_set_graphs) around such a test.
+ * No counterpart in the reference (its Metal waits are host-side).        */
+int msq_debug_expire_waits(int mode);
 /* Number of this library's kernel launches enqueued so far on `ctx`. */
 uint64_t msq_launch_count(const msq_ctx *ctx);
 /* Launch timing for profiling: between begin and end, an event is recorded
@@ -264,7 +277,16 @@ int msq_jacobi_noalloc(float *matrix, float *vectors, float *eigenvalues, int n,
  *   MSQ_FMT_BF16        tcgen05 kind::f16 MMA, FP32 accumulate in TMEM
  *   MSQ_FMT_FP8_E4M3FN_ROWSCALE  tcgen05 kind::f8f6f4 (E4M3 x E4M3),
  *                       row scales applied in the epilogue
- * `values`/`scales` hold the encoded W^T (scales only for row-scaled).
+ *   MSQ_FMT_MXFP4_E2M1  tcgen05 kind::mxf4 block-scaled MMA (E2M1 x E2M1,
+ *                       UE8M0 per 32 along K) when every order and offset
+ *                       is divisible by 32 (the flat scale blocks are then
+ *                       row blocks); otherwise decoded exactly to BF16
+ *   MSQ_FMT_MXFP8_E4M3FN  tcgen05 kind::mxf8f6f4 block-scaled MMA; orders
+ *                       and offsets divisible by 32, else MSQ_ERR_UNSUPPORTED
+ * `values`/`scales` hold the encoded W^T (scales: FP32 per row for
+ * row-scaled, the codec's scale bytes for MX).  The solver's MXFP4 plan
+ * (msq_solve_batched) quantizes W^T per row block and always takes the
+ * kind::mxf4 path.
  * Output X (FP32) uses the same batched layout as the input.              */
 int msq_make_factor(msq_ctx *ctx, const float *vectors,
                     const float *eigenvalues, const int32_t *n,
@@ -272,6 +294,15 @@ int msq_make_factor(msq_ctx *ctx, const float *vectors,
 int msq_reconstruct(msq_ctx *ctx, int format, const void *values,
                     const void *scales, const int32_t *n,
                     const int64_t *offset, int count, float *root);
+/* The solver's own reconstruction stage: X0 = Q(W) Q(W)^T from the FP32
+ * factor W^T (msq_make_factor) quantized to the plan's format
+ * (msq_plan_format) on the way into the MMA tiles: FP32 SIMT GEMM, BF16
+ * kind::f16, FP8 per-row kind::f8f6f4, or MXFP4 per row block of 32
+ * (any order) kind::mxf4.  Same stage as reconstructLowFactorTiled
+ * (src/metal_runtime.cpp:500-534).                                        */
+int msq_reconstruct_factor(msq_ctx *ctx, int plan_format, const float *factor_t,
+                           const int32_t *n, const int64_t *offset, int count,
+                           float *root);
 
 /* ---- residual and Sylvester correction -------------------------------------
  * msq_residual: R = A - X*X with A = (a + a_lo) and X = (x_hi + x_lo) in
@@ -332,7 +363,9 @@ int msq_csv_headers(char *summary, size_t summary_capacity, char *iterations,
  * The GPU-resident solve of solveGpuResidentSpd (src/metal_solver.cpp:92-336)
  * over a batch: Jacobi -> (quantize W) -> reconstruct -> Sylvester sweeps ->
  * final float-float residual, per-matrix plan, with FP32 fallback for every
- * matrix whose final residual misses `tolerance` (plan MSQ_PLAN_FP32).     */
+ * matrix whose final residual misses `tolerance`: FP32 Jacobi to 1e-7, FP32
+ * reconstruction and FP32 correction sweeps until the tolerance is met
+ * (one to four; a matrix that still misses it reports its residual).      */
 typedef enum {
   MSQ_PLAN_FP32 = 0,   /* Jacobi to 1e-7, FP32 reconstruction, no sweeps    */
   MSQ_PLAN_BF16 = 1,   /* BF16 W, tcgen05 reconstruction                    */
@@ -355,6 +388,8 @@ typedef struct {
   int32_t corrections;     /* Sylvester sweeps applied                     */
   int32_t accepted;        /* 1: the plan met the tolerance; 0: fell back  */
   int32_t fallback;        /* 1: result comes from the FP32 fallback       */
+  double plan_residual;    /* the plan's own final residual (before any
+                              fallback; equals final_residual when accepted) */
 } msq_solve_result;
 
 /* a: FP32 matrices (device, batched layout); root: FP32 output (device).

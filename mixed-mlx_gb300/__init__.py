@@ -60,7 +60,8 @@ class SolveResult(ctypes.Structure):
     _fields_ = [("final_residual", ctypes.c_double),
                 ("initial_residual", ctypes.c_double),
                 ("jacobi_sweeps", ctypes.c_int32), ("corrections", ctypes.c_int32),
-                ("accepted", ctypes.c_int32), ("fallback", ctypes.c_int32)]
+                ("accepted", ctypes.c_int32), ("fallback", ctypes.c_int32),
+                ("plan_residual", ctypes.c_double)]
 
 
 _LIB = None
@@ -72,6 +73,7 @@ _SIGS = {
     "msq_last_error": (ctypes.c_char_p, [_P]),
     "msq_set_stream": (ctypes.c_int, [_P, _P]),
     "msq_synchronize": (ctypes.c_int, [_P]),
+    "msq_debug_expire_waits": (ctypes.c_int, [ctypes.c_int]),
     "msq_launch_count": (ctypes.c_uint64, [_P]),
     "msq_storage_bytes": (ctypes.c_size_t, [ctypes.c_int, ctypes.c_size_t]),
     "msq_scale_bytes": (ctypes.c_size_t, [ctypes.c_int, ctypes.c_size_t, ctypes.c_size_t]),
@@ -100,6 +102,7 @@ _SIGS = {
     "msq_timing_end": (ctypes.c_int, [_P, ctypes.c_char_p, ctypes.c_size_t]),
     "msq_make_factor": (ctypes.c_int, [_P, _P, _P, _P, _P, ctypes.c_int, _P]),
     "msq_reconstruct": (ctypes.c_int, [_P, ctypes.c_int, _P, _P, _P, _P, ctypes.c_int, _P]),
+    "msq_reconstruct_factor": (ctypes.c_int, [_P, ctypes.c_int, _P, _P, _P, ctypes.c_int, _P]),
     "msq_residual": (ctypes.c_int, [_P, _P, _P, _P, _P, _P, _P, ctypes.c_int, _P, _P]),
     "msq_sylvester_sweep": (ctypes.c_int, [_P, ctypes.c_int, _P, _P, _P, _P, _P,
                                            ctypes.c_int, _P, _P, _P]),
@@ -342,6 +345,15 @@ class Context:
         self.check(lib().msq_reconstruct(self.handle, fmt, _ptr(values), _ptr(scales),
                                          batch.n.ctypes.data, batch.offset.ctypes.data,
                                          batch.count, _ptr(out)), "msq_reconstruct")
+        return out
+
+    def reconstruct_factor(self, plan_format: int, factor_t, batch: Batch, out=None):
+        """X0 from the FP32 factor quantized to a plan format (the solver's stage)."""
+        if out is None:
+            out = self.torch.empty(batch.total, dtype=self.torch.float32, device=factor_t.device)
+        self.check(lib().msq_reconstruct_factor(self.handle, plan_format, _ptr(factor_t),
+                                                batch.n.ctypes.data, batch.offset.ctypes.data,
+                                                batch.count, _ptr(out)), "msq_reconstruct_factor")
         return out
 
     def residual(self, a, x_hi, x_lo, batch: Batch, want_r: bool = True, a_lo=None):

@@ -88,9 +88,19 @@ int codecFor(CudaBasisFormat format) {
     case CudaBasisFormat::Bf16: return MSQ_FMT_BF16;
     case CudaBasisFormat::Fp8E4M3FnRowScale: return MSQ_FMT_FP8_E4M3FN_ROWSCALE;
     case CudaBasisFormat::Mxfp4E2M1: return MSQ_FMT_MXFP4_E2M1;
+    case CudaBasisFormat::Fp8E4M3Fn: return MSQ_FMT_FP8_E4M3FN;
+    case CudaBasisFormat::Fp8E5M2: return MSQ_FMT_FP8_E5M2;
+    case CudaBasisFormat::Mxfp8E4M3Fn: return MSQ_FMT_MXFP8_E4M3FN;
+    case CudaBasisFormat::Mxfp8E5M2: return MSQ_FMT_MXFP8_E5M2;
+    case CudaBasisFormat::Fp4E2M1: return MSQ_FMT_FP4_E2M1;
     default: return MSQ_FMT_FP32;
   }
 }
+
+constexpr CudaBasisFormat kBasisFormats[] = {
+    CudaBasisFormat::Fp32,      CudaBasisFormat::Bf16,        CudaBasisFormat::Fp8E4M3FnRowScale,
+    CudaBasisFormat::Mxfp4E2M1, CudaBasisFormat::Fp8E4M3Fn,   CudaBasisFormat::Fp8E5M2,
+    CudaBasisFormat::Mxfp8E4M3Fn, CudaBasisFormat::Mxfp8E5M2, CudaBasisFormat::Fp4E2M1};
 
 }  // namespace
 
@@ -100,13 +110,17 @@ const char *cudaBasisFormatName(CudaBasisFormat format) {
     case CudaBasisFormat::Bf16: return "bf16";
     case CudaBasisFormat::Fp8E4M3FnRowScale: return "fp8_e4m3fn_rowscale";
     case CudaBasisFormat::Mxfp4E2M1: return "mxfp4_e2m1";
+    case CudaBasisFormat::Fp8E4M3Fn: return "fp8_e4m3fn";
+    case CudaBasisFormat::Fp8E5M2: return "fp8_e5m2";
+    case CudaBasisFormat::Mxfp8E4M3Fn: return "mxfp8_e4m3fn";
+    case CudaBasisFormat::Mxfp8E5M2: return "mxfp8_e5m2";
+    case CudaBasisFormat::Fp4E2M1: return "fp4_e2m1";
   }
   return "unknown";
 }
 
 CudaBasisFormat cudaBasisFormatForCliName(const std::string &name) {
-  for (CudaBasisFormat f : {CudaBasisFormat::Fp32, CudaBasisFormat::Bf16,
-                            CudaBasisFormat::Fp8E4M3FnRowScale, CudaBasisFormat::Mxfp4E2M1}) {
+  for (CudaBasisFormat f : kBasisFormats) {
     if (name == cudaBasisFormatName(f)) return f;
   }
   failCuda("Unsupported precision: " + name);
@@ -143,10 +157,10 @@ double cudaBasisOrthogonalityTolerance(CudaBasisFormat format) {
   switch (format) {
     case CudaBasisFormat::Fp32: return 1.0e-3;
     case CudaBasisFormat::Bf16: return 5.0e-3;
-    case CudaBasisFormat::Fp8E4M3FnRowScale: return 1.5e-1;
-    case CudaBasisFormat::Mxfp4E2M1: return 5.0e-1;
+    case CudaBasisFormat::Mxfp4E2M1:
+    case CudaBasisFormat::Fp4E2M1: return 5.0e-1;  // 4-bit storage
+    default: return 1.5e-1;                        // 8-bit storage
   }
-  return 0.0;
 }
 
 CudaRuntime::CudaRuntime(int device) {
@@ -367,9 +381,24 @@ CaseResult runCudaCase(CudaRuntime &runtime, const CudaSolverConfiguration &conf
     const int fcodec = codecFor(format);
     const size_t frow = fcodec == MSQ_FMT_FP8_E4M3FN_ROWSCALE ? n : 0;
     runtime.check(encode_basis(fcodec, f.as<float>(), frow), "quantize factor");
-    runtime.check(msq_reconstruct(ctx, fcodec, codes.as<uint8_t>(), scales.as<float>(), &nn, &off,
-                                  1, x_hi.as<float>()),
-                  "reconstructLowFactorTiled");
+    // Tensor-core paths straight from the codes: BF16, per-row FP8, MXFP4 and
+    // (row-aligned blocks) MXFP8.  The other reference formats decode to
+    // FP32 and run the FP32 GEMM, as reconstructLowFactorTiled does.
+    const bool tensor = fcodec == MSQ_FMT_BF16 || fcodec == MSQ_FMT_FP8_E4M3FN_ROWSCALE ||
+                        fcodec == MSQ_FMT_MXFP4_E2M1 ||
+                        (fcodec == MSQ_FMT_MXFP8_E4M3FN && n % 32 == 0);
+    if (tensor) {
+      runtime.check(msq_reconstruct(ctx, fcodec, codes.as<uint8_t>(), scales.as<float>(), &nn,
+                                    &off, 1, x_hi.as<float>()),
+                    "reconstructLowFactorTiled");
+    } else {
+      runtime.check(msq_decode(ctx, fcodec, codes.as<uint8_t>(), scales.as<uint8_t>(), elements,
+                               0, fq.as<float>()),
+                    "reconstructLowFactorTiled");
+      runtime.check(msq_reconstruct(ctx, MSQ_FMT_FP32, fq.as<float>(), nullptr, &nn, &off, 1,
+                                    x_hi.as<float>()),
+                    "reconstructLowFactorTiled");
+    }
   }
   if (cudaMemset(x_lo.as<float>(), 0, elements * sizeof(float)) != cudaSuccess)
     failCuda("initializeWorkingRoot failed");

@@ -149,7 +149,12 @@ namespace mixed_sqrt {
 
 // Basis storage of the frozen factor (the reference's Precision subset this
 // backend implements; FP8 is the per-row-scaled E4M3 format).
-enum class CudaBasisFormat { Fp32, Bf16, Fp8E4M3FnRowScale, Mxfp4E2M1 };
+// The reference's basis precisions (kPrecisionSpecs, src/precision.hpp:64-90)
+// plus the per-row-scaled FP8 format, which has no reference counterpart.
+enum class CudaBasisFormat {
+  Fp32, Bf16, Fp8E4M3FnRowScale, Mxfp4E2M1,
+  Fp8E4M3Fn, Fp8E5M2, Mxfp8E4M3Fn, Mxfp8E5M2, Fp4E2M1
+};
 
 const char *cudaBasisFormatName(CudaBasisFormat format);
 CudaBasisFormat cudaBasisFormatForCliName(const std::string &name);

@@ -1,6 +1,8 @@
 // Context, error handling, batch-layout upload and scratch management.
 #include "msq_internal.cuh"
 
+#include <atomic>
+
 #include <cstring>
 #include <string>
 
@@ -106,6 +108,12 @@ int streamWait(msq_ctx *ctx, cudaStream_t waiter, cudaStream_t source) {
   }
   return MSQ_OK;
 }
+
+namespace {
+std::atomic<int> g_wait_test{0};
+}  // namespace
+
+int waitTestMode() { return g_wait_test.load(std::memory_order_relaxed); }
 
 int checkDeviceStatus(msq_ctx *ctx) {
   int status = 0;
@@ -282,6 +290,12 @@ extern "C" int msq_set_concurrency(msq_ctx *ctx, int enable) {
 extern "C" int msq_set_graphs(msq_ctx *ctx, int enable) {
   if (ctx == nullptr) return MSQ_ERR_INVALID_ARGUMENT;
   ctx->graphs = enable != 0;
+  return MSQ_OK;
+}
+
+extern "C" int msq_debug_expire_waits(int mode) {
+  if (mode < msq::kWaitTestOff || mode > msq::kWaitTestMbarrier) return MSQ_ERR_INVALID_ARGUMENT;
+  msq::g_wait_test.store(mode, std::memory_order_relaxed);
   return MSQ_OK;
 }
 

@@ -29,6 +29,15 @@ enum DeviceStatus : int {
   kStatusBadSpectrum = 6,
 };
 
+// Failure injection for the bounded waits (msq_debug_expire_waits): 0 off;
+// kWaitTestFlag makes the Jacobi sweep's shared-memory flag waits look for a
+// value no warp writes and its tile-load barrier get no copy;
+// kWaitTestMbarrier makes the tcgen05 GEMM's producer
+// first wait on a barrier nothing arrives at, before it issues any copy.
+// Either wait gives up after a short limit and reports its status.
+enum WaitTest : int { kWaitTestOff = 0, kWaitTestFlag = 1, kWaitTestMbarrier = 2 };
+int waitTestMode();
+
 struct WorkList {
   int tile;
   int4 *work;

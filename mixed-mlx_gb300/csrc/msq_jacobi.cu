@@ -78,6 +78,8 @@ struct JacobiArgs {
   const int2 *sched;         // two-level pair tables (null: round-robin for all)
   const int32_t *sched_off;  // per matrix: its table in sched (int2 units), -1 = round-robin
   int smem_tiles;            // global-tile variant: tiles kept in shared memory
+  int wait_test;             // 1: flag waits look for a value nothing writes and
+                             //    the tile load's barrier gets no copy
 };
 
 __device__ __forceinline__ FlatTiles tileMem(std::true_type, float *s, float *, int) {
@@ -104,8 +106,10 @@ struct RoundTable {
   __device__ short &partner(int b) const { return t[5 * P + b]; }
 };
 
-// Polls of a done flag before the sweep kernel reports kStatusFlagTimeout.
+// Polls of a done flag before the sweep kernel reports kStatusFlagTimeout
+// (kFlagWaitTestLimit under the failure-injection mode).
 constexpr int kFlagWaitLimit = 1 << 22;
+constexpr int kFlagWaitTestLimit = 64;
 
 // Shared memory of the sweep kernel: reduction scratch; the tile table, two
 // work counters, P done flags and three round tables; the rotations of two
@@ -179,10 +183,14 @@ jacobiSweepKernel(JacobiArgs args) {
     }
   } else if (split > 0) {
     // the packed tiles kept between sweeps: one TMA bulk copy into shared
-    // memory (bounded wait; on expiry the launch reports and does nothing)
-    if (threadIdx.x == 0) bulkLoadTiles(stiles, gtiles, split * kTileF * sizeof(float), &tile_bar);
+    // memory (bounded wait; on expiry the launch reports and does nothing).
+    // Under failure injection no copy is issued, so nothing arrives.
+    if (threadIdx.x == 0) {
+      if (args.wait_test) barrierWithoutCopy(&tile_bar);
+      else bulkLoadTiles(stiles, gtiles, split * kTileF * sizeof(float), &tile_bar);
+    }
     __syncthreads();
-    if (!bulkWaitTiles(&tile_bar)) {
+    if (!bulkWaitTiles(&tile_bar, args.wait_test ? kFlagWaitTestLimit : kTileWaitLimit)) {
       if (threadIdx.x == 0) atomicExch(args.status, kStatusMbarrierTimeout);
       return;
     }
@@ -412,8 +420,10 @@ jacobiSweepKernel(JacobiArgs args) {
         if (wait && (lane & 3) == 0) {
           // bounded: on expiry the launch reports and goes on
           int spins = 0;
-          while (atomicAdd(&flags[owner], 0) != round + 1) {
-            if (++spins > kFlagWaitLimit) {
+          const int target = round + 1 + (args.wait_test ? (1 << 29) : 0);
+          const int limit = args.wait_test ? kFlagWaitTestLimit : kFlagWaitLimit;
+          while (atomicAdd(&flags[owner], 0) != target) {
+            if (++spins > limit) {
               atomicExch(args.status, kStatusFlagTimeout);
               break;
             }
@@ -1076,6 +1086,7 @@ int jacobiEnqueue(msq_ctx *ctx, const DeviceBatch *b, float *matrices, float *ve
   args.status = ctx->d_status;
   args.sched = plan->sched;
   args.sched_off = plan->sched_off;
+  args.wait_test = waitTestMode() == kWaitTestFlag;
   VArgs vargs{vectors, b->offset, plan->log_offset, b->n, log_base, args.state,
               plan->work_matrix, plan->work_row, 0, 0, plan->sched, plan->sched_off};
   // Launch shape per bucket: the tuned CTA size, or (while its class is
@@ -1110,7 +1121,8 @@ int jacobiEnqueue(msq_ctx *ctx, const DeviceBatch *b, float *matrices, float *ve
   uint64_t shape_hash = 1469598103934665603ull;
   for (const auto &per : shape)
     for (const auto &h : per) shape_hash = (shape_hash ^ static_cast<uint64_t>(h.threads)) * 1099511628211ull;
-  const bool graphable = !measuring && !ctx->timing && plan->grid_ids.empty() && ctx->graphs;
+  const bool graphable = !measuring && !ctx->timing && plan->grid_ids.empty() && ctx->graphs &&
+                         waitTestMode() == kWaitTestOff;
   const JacobiGraphKey key{plan->serial, b->key, b->offset, matrices, vectors, eigenvalues,
                            sweeps_done, off_ratio, work, tolerance, max_sweeps, ctx->concurrent,
                            shape_hash};
@@ -1483,6 +1495,7 @@ extern "C" int msq_jacobi_noalloc(float *matrix, float *vectors, float *eigenval
   args.tol = tolerance;
   args.max_sweeps = max_sweeps;
   args.status = s->status;
+  args.wait_test = waitTestMode() == kWaitTestFlag;
   size_t q_off, tile_off;
   const size_t sweep_smem = sweepSmemLayout(n, true, &q_off, &tile_off);
   const int rows = (n + kNoAllocRowsPerCta - 1) / kNoAllocRowsPerCta;

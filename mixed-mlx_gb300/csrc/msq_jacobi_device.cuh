@@ -568,10 +568,18 @@ __device__ __forceinline__ void bulkLoadTiles(void *smem, const void *gmem, uint
       : "memory");
 }
 
-// True once phase 0 of the barrier completed; false after kTileWaitLimit polls.
-__device__ __forceinline__ bool bulkWaitTiles(uint64_t *bar) {
+// The barrier alone, with no copy behind it: phase 0 never completes (the
+// failure-injection form of bulkLoadTiles).
+__device__ __forceinline__ void barrierWithoutCopy(uint64_t *bar) {
   const uint32_t b = smemAddr(bar);
-  for (long long i = 0; i < kTileWaitLimit; ++i) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(b) : "memory");
+  asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+
+// True once phase 0 of the barrier completed; false after `limit` polls.
+__device__ __forceinline__ bool bulkWaitTiles(uint64_t *bar, long long limit = kTileWaitLimit) {
+  const uint32_t b = smemAddr(bar);
+  for (long long i = 0; i < limit; ++i) {
     uint32_t done;
     asm volatile(
         "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], 0;\n"

@@ -95,6 +95,18 @@ extern "C" int msq_reconstruct(msq_ctx *ctx, int format, const void *values, con
   return reconstructEncoded(ctx, b, format, values, scales, root);
 }
 
+extern "C" int msq_reconstruct_factor(msq_ctx *ctx, int plan_format, const float *factor_t,
+                                      const int32_t *n, const int64_t *offset, int count,
+                                      float *root) {
+  if (ctx == nullptr) return MSQ_ERR_INVALID_ARGUMENT;
+  msq::DeviceGuard device_guard(ctx);
+  if (!factor_t || !root)
+    return setError(ctx, MSQ_ERR_INVALID_ARGUMENT, "msq_reconstruct_factor: null buffer");
+  const DeviceBatch *b = prepareBatch(ctx, n, offset, count);
+  if (b == nullptr) return MSQ_ERR_INVALID_ARGUMENT;
+  return reconstructFromFactor(ctx, b, plan_format, factor_t, root);
+}
+
 extern "C" int msq_residual(msq_ctx *ctx, const float *a, const float *a_lo, const float *x_hi,
                             const float *x_lo, const int32_t *n, const int64_t *offset, int count,
                             float *residual, double *norms) {
@@ -189,10 +201,16 @@ bool samePlan(const msq_plan &a, const msq_plan &b) {
 // Runs one plan over a sub-batch whose matrices are copied into the solver
 // arena (compact layout), writes X into `root` at the caller's offsets and
 // the per-matrix residuals into `final_res` / `initial_res`.
+// extra_sweeps > 0 (the FP32 fallback): after the plan's sweeps, further
+// FP32 sweeps while any member's residual misses `tolerance`, at most
+// extra_sweeps, as the reference's plain method corrects until its
+// tolerance is met (src/accelerate_backend.cpp:803-1091); *applied returns
+// the sweeps the group received.
 int runGroup(msq_ctx *ctx, const float *a_user, const int32_t *n_user,
              const int64_t *off_user, const Group &g, float *root,
              std::vector<double> &final_res, std::vector<double> &initial_res,
-             std::vector<int> &jsweeps) {
+             std::vector<int> &jsweeps, double tolerance = 0.0, int extra_sweeps = 0,
+             int *applied = nullptr) {
   const int count = static_cast<int>(g.members.size());
   std::vector<int32_t> n(count);
   std::vector<int64_t> off(count);
@@ -209,7 +227,10 @@ int runGroup(msq_ctx *ctx, const float *a_user, const int32_t *n_user,
   const size_t vec = alignUp(order_total * sizeof(float));
   const size_t norms_bytes = alignUp(2 * count * sizeof(double));
   const size_t sweeps_bytes = alignUp(count * sizeof(int32_t));
-  char *w = static_cast<char *>(scratch(ctx, 8 * mat + vec + norms_bytes + sweeps_bytes,
+  // the fallback's extra sweeps keep a copy of X to undo a sweep that did
+  // not lower a matrix's residual
+  const size_t backup = extra_sweeps > 0 ? 2 * mat : 0;
+  char *w = static_cast<char *>(scratch(ctx, 8 * mat + vec + norms_bytes + sweeps_bytes + backup,
                                         kScratchSolver));
   if (w == nullptr) return MSQ_ERR_CUDA;
   float *A = reinterpret_cast<float *>(w);
@@ -277,6 +298,47 @@ int runGroup(msq_ctx *ctx, const float *a_user, const int32_t *n_user,
     MSQ_TRY(cudaCheck(ctx, cudaMemcpyAsync(host_norms.data(), norms, 2 * count * sizeof(double),
                                            cudaMemcpyDeviceToHost, ctx->stream), "norms read"));
   }
+  int done_sweeps = g.plan.sweeps;
+  float *Bh = reinterpret_cast<float *>(w + 8 * mat + vec + norms_bytes + sweeps_bytes);
+  float *Bl = Bh + mat / sizeof(float);
+  for (int extra = 0; extra < extra_sweeps; ++extra) {
+    MSQ_TRY(cudaCheck(ctx, cudaStreamSynchronize(ctx->stream), "norms sync"));
+    bool all_met = true;
+    for (int i = 0; i < count; ++i)
+      all_met = all_met && std::sqrt(host_norms[2 * i] / host_norms[2 * i + 1]) <= tolerance;
+    if (all_met) break;
+    const std::vector<double> before = host_norms;
+    MSQ_TRY(cudaCheck(ctx, cudaMemcpyAsync(Bh, Xh, total * sizeof(float), cudaMemcpyDeviceToDevice,
+                                           ctx->stream), "x backup"));
+    MSQ_TRY(cudaCheck(ctx, cudaMemcpyAsync(Bl, Xl, total * sizeof(float), cudaMemcpyDeviceToDevice,
+                                           ctx->stream), "x backup"));
+    MSQ_TRY(sylvesterSweep(ctx, b, gemm_format, V, lam, R, Xh, Xl, F, W1));
+    MSQ_TRY(residual(true));
+    ++done_sweeps;
+    MSQ_TRY(cudaCheck(ctx, cudaMemcpyAsync(host_norms.data(), norms, 2 * count * sizeof(double),
+                                           cudaMemcpyDeviceToHost, ctx->stream), "norms read"));
+    MSQ_TRY(cudaCheck(ctx, cudaStreamSynchronize(ctx->stream), "norms sync"));
+    // a matrix whose residual did not drop keeps its previous root (the
+    // corrections stopped contracting: more of them would diverge), and the
+    // sweeps stop there
+    bool worse = false;
+    for (int i = 0; i < count; ++i) {
+      const double r_new = std::sqrt(host_norms[2 * i] / host_norms[2 * i + 1]);
+      const double r_old = std::sqrt(before[2 * i] / before[2 * i + 1]);
+      if (!(r_new < r_old)) {
+        worse = true;
+        const size_t elems = static_cast<size_t>(n[i]) * n[i];
+        MSQ_TRY(cudaCheck(ctx, cudaMemcpyAsync(Xh + off[i], Bh + off[i], elems * sizeof(float),
+                                               cudaMemcpyDeviceToDevice, ctx->stream), "x undo"));
+        MSQ_TRY(cudaCheck(ctx, cudaMemcpyAsync(Xl + off[i], Bl + off[i], elems * sizeof(float),
+                                               cudaMemcpyDeviceToDevice, ctx->stream), "x undo"));
+        host_norms[2 * i] = before[2 * i];
+        host_norms[2 * i + 1] = before[2 * i + 1];
+      }
+    }
+    if (worse) break;
+  }
+  if (applied != nullptr) *applied = done_sweeps;
   std::vector<int32_t> host_sweeps(count);
   MSQ_TRY(cudaCheck(ctx, cudaMemcpyAsync(host_sweeps.data(), sweeps, count * sizeof(int32_t),
                                          cudaMemcpyDeviceToHost, ctx->stream), "sweeps read"));
@@ -337,10 +399,14 @@ extern "C" int msq_solve_batched(msq_ctx *ctx, const float *a, const int32_t *n,
     MSQ_TRY(runGroup(ctx, a, n, offset, g, root, final_res, initial_res, jsweeps));
     for (int m : g.members) corrections[m] = g.plan.sweeps;
   }
-  // The fallback is the FP32 path with one FP32 correction sweep: FP32
-  // Jacobi + FP32 reconstruction alone leaves a residual near u * n, which
-  // misses tight tolerances at the larger orders.
-  const msq_plan fallback_plan{MSQ_PLAN_FP32, 1, 1e-7, 15, 0};
+  // The fallback is the FP32 path with FP32 correction sweeps until the
+  // tolerance is met (at least one, at most kFallbackSweeps): FP32 Jacobi +
+  // FP32 reconstruction alone leaves a residual near u * n, which misses
+  // tight tolerances at the larger orders, and ill-conditioned large
+  // matrices (n = 4096, condition 1e6) need a second sweep.
+  constexpr int kFallbackSweeps = 4;
+  // (Jacobi budget 20 sweeps: n = 4096 at condition 1e6 needs 16 to 1e-7)
+  const msq_plan fallback_plan{MSQ_PLAN_FP32, 1, 1e-7, 20, 0};
   Group retry{fallback_plan, {}};
   for (const Group &g : groups) {
     if (samePlan(g.plan, fallback_plan)) continue;
@@ -348,11 +414,14 @@ extern "C" int msq_solve_batched(msq_ctx *ctx, const float *a, const int32_t *n,
       if (!(final_res[m] <= tolerance)) retry.members.push_back(m);
   }
   for (int i = 0; i < count; ++i) accepted[i] = final_res[i] <= tolerance;
+  const std::vector<double> plan_res = final_res;
   if (!retry.members.empty()) {
-    MSQ_TRY(runGroup(ctx, a, n, offset, retry, root, final_res, initial_res, jsweeps));
+    int applied = 0;
+    MSQ_TRY(runGroup(ctx, a, n, offset, retry, root, final_res, initial_res, jsweeps, tolerance,
+                     kFallbackSweeps - fallback_plan.sweeps, &applied));
     for (int m : retry.members) {
       fallback[m] = 1;
-      corrections[m] = fallback_plan.sweeps;
+      corrections[m] = applied;
     }
   }
   if (results != nullptr) {
@@ -363,6 +432,7 @@ extern "C" int msq_solve_batched(msq_ctx *ctx, const float *a, const int32_t *n,
       results[i].corrections = corrections[i];
       results[i].accepted = accepted[i];
       results[i].fallback = fallback[i];
+      results[i].plan_residual = plan_res[i];
     }
   }
   return MSQ_OK;

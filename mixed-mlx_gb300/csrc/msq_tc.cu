@@ -16,8 +16,17 @@
 //     (kind::f16 for BF16, kind::f8f6f4 for FP8 E4M3) from one thread, and
 //     warps 0-3 drain the other accumulator with tcgen05.ld while the next
 //     tile accumulates, applying the per-row FP8 scales r_i r_j.
-// MXFP4 factors (E2M1 + E8M0 per 32 along K) are decoded into BF16 tiles,
-// which is exact (E2M1 x 2^e has at most 2 significant bits), and use
+// MX factors (E2M1 or E4M3 with one UE8M0 scale per 32 along K of a row;
+// the reference's K-major MX operand with scale stride ld / 32,
+// 3_spectral/lowbit_matmul.cpp:240-299) stay in their codes: packMxKernel
+// writes E2M1 (two per byte) or E4M3 tiles plus one scale-factor tile each,
+// the producer bulk-copies both, and the MMA thread moves each stage's
+// scale factors into TMEM with tcgen05.cp and issues tcgen05.mma
+// kind::mxf4 / kind::mxf8f6f4 .block_scale, which applies 2^(s - 127) per
+// 32-element block inside the tensor core (the reference's blockwise
+// ue8m0 / 32 product, 3_spectral/lowbit_matmul.metal:33).  Flat MXFP4 codes
+// whose blocks straddle rows (order not divisible by 32) are decoded exactly
+// into BF16 tiles (E2M1 x 2^e has at most 2 significant bits) and use
 // kind::f16.  Every mbarrier wait is bounded; on expiry the kernel records
 // kStatusMbarrierTimeout in the context's status word and unwinds.
 #include "msq_codec_device.cuh"
@@ -39,7 +48,22 @@ constexpr int kTcThreads = 192;    // warps 0-3 epilogue, 4 producer, 5 MMA
 constexpr uint32_t kTmemCols = 256;
 constexpr long long kWaitLimit = 1ll << 26;
 
-enum OperandKind : int { kOpBf16 = 0, kOpFp8 = 1 };
+// kOpMxf4 / kOpMxf8: block-scaled operands (E2M1 packed two per byte, or
+// E4M3) with one UE8M0 scale factor per 32 consecutive K of a row, run as
+// tcgen05.mma kind::mxf4 / kind::mxf8f6f4 .block_scale with the scale
+// factors staged in TMEM.
+enum OperandKind : int { kOpBf16 = 0, kOpFp8 = 1, kOpMxf4 = 2, kOpMxf8 = 3 };
+constexpr bool isBlockScaled(int kind) { return kind == kOpMxf4 || kind == kOpMxf8; }
+// Scale-factor tile of one operand tile: atoms of 128 rows x 4 K blocks,
+// byte 16 (r mod 32) + 4 (r / 32) + b of an atom holding row r, block b (the
+// 32-lane x 128-bit source of tcgen05.cp ... warpx4).  An E2M1 tile row (256
+// K) has 8 blocks (two atoms), an E4M3 row (128 K) 4 (one atom).
+constexpr int kScaleAtomBytes = 512;
+constexpr int kScaleTileBytes = 2 * kScaleAtomBytes;
+// TMEM: two 128-column accumulators, then per stage 16 scale-factor
+// columns (A atoms at +0, +4, B atoms at +8, +12).
+constexpr uint32_t kTmemColsMx = 512;
+constexpr uint32_t kScaleCol0 = 256;
 constexpr int kMaxSegments = 6;
 enum Epilogue : int {
   kEpiStore = 0,     // X = acc
@@ -50,8 +74,8 @@ enum Epilogue : int {
 
 // Bounded wait: false (and the status word set) if the phase never completes.
 __device__ __forceinline__ bool mbarWait(uint32_t bar, uint32_t parity, int *status,
-                                         volatile int *abort_flag) {
-  for (long long i = 0; i < kWaitLimit; ++i) {
+                                         volatile int *abort_flag, long long limit = kWaitLimit) {
+  for (long long i = 0; i < limit; ++i) {
     if (mbarTryWait(bar, parity)) return true;
     if (*abort_flag) return false;
   }
@@ -90,6 +114,8 @@ struct TcArgs {
   int segments;
   const uint8_t *tiles_a[kMaxSegments];
   const uint8_t *tiles_b[kMaxSegments];
+  const uint8_t *scales_a; // block-scaled kinds: scale-factor tiles (one segment)
+  const uint8_t *scales_b;
   const int64_t *tile_base;// per matrix: first tile index
   const int32_t *n;
   const int64_t *x_offset;
@@ -100,6 +126,7 @@ struct TcArgs {
   double *norms;           // kEpiResidual: ||R||^2, ||A||^2 per matrix
   float *x;
   int *status;
+  int wait_test;           // 1: the producer first waits on a barrier nothing arrives at
 };
 
 template <int kKind, int kEpi>
@@ -107,8 +134,13 @@ __global__ void __launch_bounds__(kTcThreads, 1) tcGemmKernel(TcArgs args) {
   extern __shared__ __align__(1024) unsigned char smem_raw[];
   unsigned char *base = reinterpret_cast<unsigned char *>(
       (reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~static_cast<uintptr_t>(1023));
+  constexpr bool kMx = isBlockScaled(kKind);
+  constexpr uint32_t kCols = kMx ? kTmemColsMx : kTmemCols;
   unsigned char *stage_mem = base;  // kStages x (A 16 KB, B 16 KB)
-  uint64_t *bars = reinterpret_cast<uint64_t *>(base + kStages * 2 * kTileBytes);
+  // block-scaled kinds: kStages x (SFA 1 KB, SFB 1 KB) after the operands
+  unsigned char *scale_mem = base + kStages * 2 * kTileBytes;
+  uint64_t *bars = reinterpret_cast<uint64_t *>(base + kStages * 2 * kTileBytes +
+                                                (kMx ? kStages * 2 * kScaleTileBytes : 0));
   uint64_t *full = bars, *empty = bars + kStages;
   uint64_t *acc_full = bars + 2 * kStages, *acc_empty = acc_full + 2;
   uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(acc_empty + 2);
@@ -130,7 +162,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) tcGemmKernel(TcArgs args) {
   if (warp == 5) {
     asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
                      smemAddr(tmem_slot)),
-                 "r"(kTmemCols));
+                 "r"(kCols));
     asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
   }
   asm volatile("tcgen05.fence::before_thread_sync;");
@@ -142,6 +174,13 @@ __global__ void __launch_bounds__(kTcThreads, 1) tcGemmKernel(TcArgs args) {
     if (lane == 0) {
       int stage = 0;
       uint32_t phase = 0;
+      if (args.wait_test) {
+        // failure injection: phase 0 of empty[0] completes only after an
+        // MMA commit, which needs a copy this thread has not issued; the
+        // wait expires, sets the status and the abort flag, and every role
+        // unwinds with no copy or MMA in flight
+        mbarWait(smemAddr(&empty[0]), 0, args.status, abort_flag, 4096);
+      }
       for (int item = blockIdx.x; item < args.items && !*abort_flag; item += gridDim.x) {
         const int4 w = args.work[item];
         const int64_t base = args.tile_base[w.x] * kTileBytes;
@@ -151,12 +190,21 @@ __global__ void __launch_bounds__(kTcThreads, 1) tcGemmKernel(TcArgs args) {
           for (int kt = 0; kt < w.w; ++kt) {
             if (!mbarWait(smemAddr(&empty[stage]), phase ^ 1, args.status, abort_flag)) break;
             const uint32_t bar = smemAddr(&full[stage]);
-            mbarArriveExpectTx(bar, 2 * kTileBytes);
+            mbarArriveExpectTx(bar, 2 * kTileBytes + (kMx ? 2 * kScaleTileBytes : 0));
             unsigned char *dst = stage_mem + stage * 2 * kTileBytes;
+            const int64_t tile_a = args.tile_base[w.x] + static_cast<int64_t>(w.y) * w.w + kt;
+            const int64_t tile_b = args.tile_base[w.x] + static_cast<int64_t>(w.z) * w.w + kt;
             bulkLoad(smemAddr(dst), ta + (static_cast<int64_t>(w.y) * w.w + kt) * kTileBytes,
                      kTileBytes, bar);
             bulkLoad(smemAddr(dst + kTileBytes),
                      tb + (static_cast<int64_t>(w.z) * w.w + kt) * kTileBytes, kTileBytes, bar);
+            if constexpr (kMx) {
+              unsigned char *sdst = scale_mem + stage * 2 * kScaleTileBytes;
+              bulkLoad(smemAddr(sdst), args.scales_a + tile_a * kScaleTileBytes, kScaleTileBytes,
+                       bar);
+              bulkLoad(smemAddr(sdst + kScaleTileBytes), args.scales_b + tile_b * kScaleTileBytes,
+                       kScaleTileBytes, bar);
+            }
             if (++stage == kStages) {
               stage = 0;
               phase ^= 1;
@@ -183,11 +231,39 @@ __global__ void __launch_bounds__(kTcThreads, 1) tcGemmKernel(TcArgs args) {
           const uint32_t a_addr = smemAddr(stage_mem + stage * 2 * kTileBytes);
           const uint64_t adesc = smemDesc(a_addr);
           const uint64_t bdesc = smemDesc(a_addr + kTileBytes);
-          // 128 bytes of K per stage: four MMAs of 32 bytes (K = 16 BF16 or
-          // 32 FP8); the start address advances inside the swizzle atom.
+          // 128 bytes of K per stage: four MMAs of 32 bytes (K = 16 BF16, 32
+          // FP8 or 64 E2M1); the start address advances inside the swizzle
+          // atom.
+          if constexpr (kMx) {
+            // the stage's scale-factor atoms into TMEM, then the MMAs (the
+            // copies and MMAs of this thread execute in issue order)
+            const uint32_t s_addr = smemAddr(scale_mem + stage * 2 * kScaleTileBytes);
+            const uint32_t sf = tmem + kScaleCol0 + 16u * stage;
+            const int atoms = kKind == kOpMxf4 ? 2 : 1;
+            for (int at = 0; at < atoms; ++at) {
+              tmemCopyScales(sf + 4u * at, smemDescPlain(s_addr + at * kScaleAtomBytes));
+              tmemCopyScales(sf + 8u + 4u * at,
+                             smemDescPlain(s_addr + kScaleTileBytes + at * kScaleAtomBytes));
+            }
 #pragma unroll
-          for (int kk = 0; kk < 4; ++kk) {
-            mmaIssue<kKind>(d, adesc + 2 * kk, bdesc + 2 * kk, (step | kk) != 0);
+            for (int kk = 0; kk < 4; ++kk) {
+              const uint32_t acc_on = (step | kk) != 0;
+              if constexpr (kKind == kOpMxf4) {
+                // K blocks 2kk, 2kk+1: atom kk/2, bytes 2(kk mod 2) and +1
+                const uint32_t id = 2u * (kk & 1);
+                mmaMxf4(d, adesc + 2 * kk, bdesc + 2 * kk, instrDescBlockScaled(true, id, id),
+                        sf + 4u * (kk >> 1), sf + 8u + 4u * (kk >> 1), acc_on);
+              } else {
+                // K block kk: byte kk of the one atom
+                mmaMxf8(d, adesc + 2 * kk, bdesc + 2 * kk,
+                        instrDescBlockScaled(false, kk, kk), sf, sf + 8u, acc_on);
+              }
+            }
+          } else {
+#pragma unroll
+            for (int kk = 0; kk < 4; ++kk) {
+              mmaIssue<kKind>(d, adesc + 2 * kk, bdesc + 2 * kk, (step | kk) != 0);
+            }
           }
           mmaCommit(smemAddr(&empty[stage]));
           if (++stage == kStages) {
@@ -279,7 +355,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) tcGemmKernel(TcArgs args) {
   asm volatile("tcgen05.fence::after_thread_sync;");
   if (warp == 5) {
     asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem),
-                 "r"(kTmemCols));
+                 "r"(kCols));
   }
 }
 
@@ -288,7 +364,6 @@ __global__ void __launch_bounds__(kTcThreads, 1) tcGemmKernel(TcArgs args) {
 enum PackSource : int {
   kPackF32Bf16 = 0,     // FP32 factor -> BF16
   kPackF32Fp8Row = 1,   // FP32 factor / row scale -> E4M3
-  kPackF32Mxfp4 = 2,    // FP32 factor -> MXFP4 values, decoded into BF16
   kPackBf16Codes = 3,   // flat BF16 codes
   kPackFp8Codes = 4,    // flat E4M3 codes (row scales separate)
   kPackMxfp4Codes = 5,  // flat MXFP4 codes + E8M0 scales, decoded into BF16
@@ -325,21 +400,6 @@ __global__ void __launch_bounds__(128) packKernel(PackArgs args) {
     const bool row_ok = i < n;
     float inv_scale_row = 1.0f;
     if (kSource == kPackF32Fp8Row && row_ok) inv_scale_row = args.row_scale[args.eig_offset[mi] + i];
-    // MX block exponents for the two 32-element blocks of this row segment
-    int mx_e[2] = {0, 0};
-    if (kSource == kPackF32Mxfp4 && row_ok) {
-      for (int blk = 0; blk < 2; ++blk) {
-        float m = 0.0f;
-        for (int e = 0; e < 32; ++e) {
-          const int k = k0 + blk * 32 + e;
-          if (k < n) {
-            const float a = fabsf(args.f[off + k + static_cast<int64_t>(i) * n]);
-            if (a <= 3.402823466e38f) m = fmaxf(m, a);
-          }
-        }
-        mx_e[blk] = mxExponent(m, 2);
-      }
-    }
 #pragma unroll 1
     for (int c = 0; c < 8; ++c) {
       uint32_t word[4] = {0, 0, 0, 0};
@@ -367,12 +427,7 @@ __global__ void __launch_bounds__(128) packKernel(PackArgs args) {
                 h = encodeBf16(args.f[at]);
               } else if (kSource == kPackBf16Codes) {
                 h = reinterpret_cast<const uint16_t *>(args.codes)[at];
-              } else if (kSource == kPackF32Mxfp4) {
-                const int ex = mx_e[(c * 8 + e) / 32];
-                const float q = mxScale(decodeE2M1(encodeE2M1(mxDivide(args.f[at], ex))),
-                                        static_cast<uint32_t>(ex + 127));
-                h = encodeBf16(q);  // exact: at most 2 significant bits
-              } else {  // kPackMxfp4Codes
+              } else {  // kPackMxfp4Codes: exact, at most 2 significant bits
                 const uint32_t byte = args.codes[at / 2];
                 const float d = decodeE2M1((byte >> ((at & 1) * 4)) & 0xfu);
                 h = encodeBf16(mxScale(d, args.mx_scales[at / 32]));
@@ -384,6 +439,113 @@ __global__ void __launch_bounds__(128) packKernel(PackArgs args) {
       }
       *reinterpret_cast<uint4 *>(tile + swizzle128(r, c)) =
           make_uint4(word[0], word[1], word[2], word[3]);
+    }
+  }
+}
+
+// Block-scaled operand tiles: codes in the SWIZZLE_128B K-major tile (E2M1
+// two per byte, the even K in the low nibble; or E4M3) and the tile's
+// scale-factor bytes in the atom layout of kScaleTileBytes.  Sources:
+//   kMxF32Fp4    FP32 factor -> E2M1 + UE8M0 per 32 K of a row (the
+//                reference's mxScaleExponent / floatToFp4E2M1 per block)
+//   kMxCodesFp4  flat MXFP4 codes and scales (order divisible by 32, so
+//                the flat 32-element blocks are row blocks)
+//   kMxCodesFp8  flat MXFP8 E4M3 codes and scales (same condition)
+// One CTA of 128 threads per tile; thread r packs row r.  Blocks beyond the
+// order get zero codes and the unit scale (byte 127).
+enum MxSource : int { kMxF32Fp4 = 0, kMxCodesFp4 = 1, kMxCodesFp8 = 2 };
+
+struct MxPackArgs {
+  const int4 *work;       // (matrix, tile_m, tile_k, k_tiles)
+  int items;
+  const float *f;
+  const uint8_t *codes;
+  const uint8_t *mx_scales;
+  const int64_t *f_offset;
+  const int64_t *tile_base;
+  const int32_t *n;
+  uint8_t *tiles;
+  uint8_t *scale_tiles;
+};
+
+template <int kSource>
+__global__ void __launch_bounds__(128) packMxKernel(MxPackArgs args) {
+  constexpr bool kFp4 = kSource != kMxCodesFp8;
+  constexpr int kElems = kFp4 ? 256 : 128;  // K per 128-byte tile row
+  constexpr int kBlocks = kElems / 32;
+  for (int item = blockIdx.x; item < args.items; item += gridDim.x) {
+    const int4 w = args.work[item];
+    const int mi = w.x, n = args.n[mi];
+    const int r = threadIdx.x;
+    const int i = w.y * kTileRows + r;
+    const int k0 = w.z * kElems;
+    const int64_t off = args.f_offset[mi];
+    const int64_t t = args.tile_base[mi] + static_cast<int64_t>(w.y) * w.w + w.z;
+    uint8_t *tile = args.tiles + t * kTileBytes;
+    uint8_t *sft = args.scale_tiles + t * kScaleTileBytes;
+    uint32_t sf_word[2] = {0x7f7f7f7fu, 0x7f7f7f7fu};
+#pragma unroll 1
+    for (int blk = 0; blk < kBlocks; ++blk) {
+      const int kb = k0 + 32 * blk;
+      uint32_t words[8] = {0, 0, 0, 0, 0, 0, 0, 0};  // 32 codes: 16 (E2M1) or 32 bytes
+      uint32_t sf = 127;
+      if (i < n && kb < n) {
+        const int64_t at = off + kb + static_cast<int64_t>(i) * n;
+        if constexpr (kSource == kMxF32Fp4) {
+          float x[32];
+          float m = 0.0f;
+#pragma unroll
+          for (int e = 0; e < 32; ++e) {
+            x[e] = kb + e < n ? args.f[at + e] : 0.0f;
+            const float a = fabsf(x[e]);
+            if (a <= 3.402823466e38f) m = fmaxf(m, a);
+          }
+          const int ex = mxExponent(m, 2);
+          sf = static_cast<uint32_t>(ex + 127);
+#pragma unroll
+          for (int e = 0; e < 32; ++e) {
+            const uint32_t code = kb + e < n ? encodeE2M1(mxDivide(x[e], ex)) : 0u;
+            words[e / 8] |= code << (4 * (e % 8));
+          }
+        } else if constexpr (kSource == kMxCodesFp4) {
+          // 16 bytes of codes at byte at / 2 (a multiple of 16), one scale
+          const uint4 c = *reinterpret_cast<const uint4 *>(args.codes + at / 2);
+          words[0] = c.x;
+          words[1] = c.y;
+          words[2] = c.z;
+          words[3] = c.w;
+          sf = args.mx_scales[at / 32];
+        } else {
+          const uint4 c0 = *reinterpret_cast<const uint4 *>(args.codes + at);
+          const uint4 c1 = *reinterpret_cast<const uint4 *>(args.codes + at + 16);
+          words[0] = c0.x;
+          words[1] = c0.y;
+          words[2] = c0.z;
+          words[3] = c0.w;
+          words[4] = c1.x;
+          words[5] = c1.y;
+          words[6] = c1.z;
+          words[7] = c1.w;
+          sf = args.mx_scales[at / 32];
+        }
+      }
+      if constexpr (kFp4) {
+        *reinterpret_cast<uint4 *>(tile + swizzle128(r, blk)) =
+            make_uint4(words[0], words[1], words[2], words[3]);
+      } else {
+        *reinterpret_cast<uint4 *>(tile + swizzle128(r, 2 * blk)) =
+            make_uint4(words[0], words[1], words[2], words[3]);
+        *reinterpret_cast<uint4 *>(tile + swizzle128(r, 2 * blk + 1)) =
+            make_uint4(words[4], words[5], words[6], words[7]);
+      }
+      const int shift = 8 * (blk % 4);
+      sf_word[blk / 4] = (sf_word[blk / 4] & ~(0xffu << shift)) | (sf << shift);
+    }
+    // row r of atom a: 4 bytes at 16 (r mod 32) + 4 (r / 32)
+    const int at_row = 16 * (r % 32) + 4 * (r / 32);
+#pragma unroll
+    for (int a = 0; a < kBlocks / 4; ++a) {
+      *reinterpret_cast<uint32_t *>(sft + a * kScaleAtomBytes + at_row) = sf_word[a];
     }
   }
 }
@@ -549,7 +711,8 @@ TcPlan *tcPlan(msq_ctx *ctx, const DeviceBatch *b, int kind) {
   for (TcPlan *p : plans)
     if (p->key == b->key && p->count == b->count && p->kind == kind && p->device_id == ctx->device)
       return p;
-  const int elems = kind == kOpFp8 ? 128 : 64;
+  // K per 128-byte tile row
+  const int elems = kind == kOpMxf4 ? 256 : (kind == kOpFp8 || kind == kOpMxf8) ? 128 : 64;
   std::vector<int64_t> base(b->count);
   std::vector<int4> pack, gemm;
   std::vector<int32_t> row_matrix;
@@ -607,7 +770,10 @@ TcPlan *tcPlan(msq_ctx *ctx, const DeviceBatch *b, int kind) {
   return p;
 }
 
-size_t tcSmemBytes() { return kStages * 2 * kTileBytes + 1024 + 256; }
+size_t tcSmemBytes(int kind = kOpBf16) {
+  return kStages * 2 * kTileBytes + (isBlockScaled(kind) ? kStages * 2 * kScaleTileBytes : 0) +
+         1024 + 256;
+}
 
 // Opt-in shared memory of the GEMM kernels, once per device.
 int tcAttributes(msq_ctx *ctx) {
@@ -620,6 +786,9 @@ int tcAttributes(msq_ctx *ctx) {
   MSQ_TRY(cudaCheck(ctx, cudaFuncSetAttribute(tcGemmKernel<kOpFp8, kEpiRowScale>, a, bytes), "tc attr"));
   MSQ_TRY(cudaCheck(ctx, cudaFuncSetAttribute(tcGemmKernel<kOpBf16, kEpiInverseH>, a, bytes), "tc attr"));
   MSQ_TRY(cudaCheck(ctx, cudaFuncSetAttribute(tcGemmKernel<kOpBf16, kEpiResidual>, a, bytes), "tc attr"));
+  const int mx_bytes = static_cast<int>(tcSmemBytes(kOpMxf4));
+  MSQ_TRY(cudaCheck(ctx, cudaFuncSetAttribute(tcGemmKernel<kOpMxf4, kEpiStore>, a, mx_bytes), "tc attr"));
+  MSQ_TRY(cudaCheck(ctx, cudaFuncSetAttribute(tcGemmKernel<kOpMxf8, kEpiStore>, a, mx_bytes), "tc attr"));
   done_mask.fetch_or(bit);
   return MSQ_OK;
 }
@@ -629,9 +798,12 @@ int tcAttributes(msq_ctx *ctx) {
 int launchTcGemm(msq_ctx *ctx, const DeviceBatch *b, TcPlan *p, int epilogue, int segments,
                  const uint8_t *const *a_tiles, const uint8_t *const *b_tiles,
                  const float *row_scale, const float *eigenvalues, const float *a_in,
-                 double *norms, float *x, const char *what) {
+                 double *norms, float *x, const char *what,
+                 const uint8_t *scale_tiles = nullptr) {
   MSQ_TRY(tcAttributes(ctx));
   TcArgs args{};
+  args.scales_a = scale_tiles;
+  args.scales_b = scale_tiles;
   args.work = p->gemm_work;
   args.items = p->gemm_items;
   args.segments = segments;
@@ -649,8 +821,20 @@ int launchTcGemm(msq_ctx *ctx, const DeviceBatch *b, TcPlan *p, int epilogue, in
   args.norms = norms;
   args.x = x;
   args.status = ctx->d_status;
+  args.wait_test = waitTestMode() == kWaitTestMbarrier;
   const unsigned grid = std::min(p->gemm_items, kSmCount);
-  const size_t smem = tcSmemBytes();
+  const size_t smem = tcSmemBytes(p->kind);
+  if (isBlockScaled(p->kind)) {
+    if (scale_tiles == nullptr || segments != 1 || epilogue != kEpiStore) {
+      return setError(ctx, MSQ_ERR_INVALID_ARGUMENT, "block-scaled GEMM: one segment, store");
+    }
+    if (p->kind == kOpMxf4) {
+      tcGemmKernel<kOpMxf4, kEpiStore><<<grid, kTcThreads, smem, ctx->stream>>>(args);
+    } else {
+      tcGemmKernel<kOpMxf8, kEpiStore><<<grid, kTcThreads, smem, ctx->stream>>>(args);
+    }
+    return launched(ctx, what);
+  }
   switch (epilogue) {
     case kEpiRowScale:
       tcGemmKernel<kOpFp8, kEpiRowScale><<<grid, kTcThreads, smem, ctx->stream>>>(args);
@@ -673,6 +857,41 @@ int runTcGemm(msq_ctx *ctx, const DeviceBatch *b, TcPlan *p, const uint8_t *tile
   const uint8_t *t[1] = {tiles};
   return launchTcGemm(ctx, b, p, p->kind == kOpFp8 ? kEpiRowScale : kEpiStore, 1, t, t,
                       row_scale, nullptr, nullptr, nullptr, x, "tcgen05 reconstruction");
+}
+
+template <int kSource>
+int launchPackMx(msq_ctx *ctx, const DeviceBatch *b, TcPlan *p, const float *f,
+                 const uint8_t *codes, const uint8_t *mx_scales, uint8_t *tiles,
+                 uint8_t *scale_tiles) {
+  MxPackArgs args{};
+  args.work = p->pack_work;
+  args.items = p->pack_items;
+  args.f = f;
+  args.codes = codes;
+  args.mx_scales = mx_scales;
+  args.f_offset = b->offset;
+  args.tile_base = p->tile_base;
+  args.n = b->n;
+  args.tiles = tiles;
+  args.scale_tiles = scale_tiles;
+  packMxKernel<kSource><<<std::min(p->pack_items, kSmCount * 16), 128, 0, ctx->stream>>>(args);
+  return launched(ctx, "pack block-scaled operand");
+}
+
+// X = (A * SF)(A * SF)^T from block-scaled operand tiles.
+int runMxGemm(msq_ctx *ctx, const DeviceBatch *b, TcPlan *p, const uint8_t *tiles,
+              const uint8_t *scale_tiles, float *x) {
+  const uint8_t *t[1] = {tiles};
+  return launchTcGemm(ctx, b, p, kEpiStore, 1, t, t, nullptr, nullptr, nullptr, nullptr, x,
+                      "tcgen05 reconstruction", scale_tiles);
+}
+
+// Every matrix of the batch starts a 32-element block and has an order
+// divisible by 32: the flat MX blocks of its codes are then row blocks.
+bool rowAlignedBlocks(const DeviceBatch *b) {
+  for (int i = 0; i < b->count; ++i)
+    if (b->host_n[i] % 32 != 0 || b->host_offset[i] % 32 != 0) return false;
+  return true;
 }
 
 template <int kSource>
@@ -791,6 +1010,18 @@ int residualTc(msq_ctx *ctx, const DeviceBatch *b, const float *a, const float *
 }
 
 int reconstructLowBit(msq_ctx *ctx, const DeviceBatch *b, int format, const float *f, float *x) {
+  if (format == MSQ_FMT_MXFP4_E2M1) {
+    // E2M1 codes with one UE8M0 scale per 32 K of a row, block-scaled MMA
+    TcPlan *p = tcPlan(ctx, b, kOpMxf4);
+    if (p == nullptr) return MSQ_ERR_CUDA;
+    const size_t tile_bytes = static_cast<size_t>(p->total_tiles) * kTileBytes;
+    uint8_t *mem = static_cast<uint8_t *>(
+        scratch(ctx, tile_bytes + static_cast<size_t>(p->total_tiles) * kScaleTileBytes,
+                kScratchOperand));
+    if (mem == nullptr) return MSQ_ERR_CUDA;
+    MSQ_TRY(launchPackMx<kMxF32Fp4>(ctx, b, p, f, nullptr, nullptr, mem, mem + tile_bytes));
+    return runMxGemm(ctx, b, p, mem, mem + tile_bytes, x);
+  }
   const int kind = format == MSQ_FMT_FP8_E4M3FN_ROWSCALE ? kOpFp8 : kOpBf16;
   TcPlan *p = tcPlan(ctx, b, kind);
   if (p == nullptr) return MSQ_ERR_CUDA;
@@ -809,9 +1040,6 @@ int reconstructLowBit(msq_ctx *ctx, const DeviceBatch *b, int format, const floa
       MSQ_TRY(launched(ctx, "row scales"));
       MSQ_TRY(launchPack<kPackF32Fp8Row>(ctx, b, p, f, nullptr, nullptr, row_scale, mem));
       break;
-    case MSQ_FMT_MXFP4_E2M1:
-      MSQ_TRY(launchPack<kPackF32Mxfp4>(ctx, b, p, f, nullptr, nullptr, nullptr, mem));
-      break;
     default:
       return setError(ctx, MSQ_ERR_UNSUPPORTED, "reconstruction format not supported");
   }
@@ -822,11 +1050,35 @@ int reconstructEncoded(msq_ctx *ctx, const DeviceBatch *b, int format, const voi
                        const void *scales, float *x) {
   const int kind = format == MSQ_FMT_FP8_E4M3FN_ROWSCALE ? kOpFp8 : kOpBf16;
   if (format != MSQ_FMT_BF16 && format != MSQ_FMT_FP8_E4M3FN_ROWSCALE &&
-      format != MSQ_FMT_MXFP4_E2M1) {
+      format != MSQ_FMT_MXFP4_E2M1 && format != MSQ_FMT_MXFP8_E4M3FN) {
     return setError(ctx, MSQ_ERR_UNSUPPORTED, "msq_reconstruct: format not supported");
   }
   if (format != MSQ_FMT_BF16 && scales == nullptr) {
     return setError(ctx, MSQ_ERR_INVALID_ARGUMENT, "msq_reconstruct: scales required");
+  }
+  const bool aligned = rowAlignedBlocks(b);
+  if (format == MSQ_FMT_MXFP8_E4M3FN && !aligned) {
+    return setError(ctx, MSQ_ERR_UNSUPPORTED,
+                    "msq_reconstruct: MXFP8 needs orders and offsets divisible by 32");
+  }
+  if ((format == MSQ_FMT_MXFP4_E2M1 || format == MSQ_FMT_MXFP8_E4M3FN) && aligned) {
+    // block-scaled MMA straight from the codes and their scale bytes
+    const bool fp4 = format == MSQ_FMT_MXFP4_E2M1;
+    TcPlan *p = tcPlan(ctx, b, fp4 ? kOpMxf4 : kOpMxf8);
+    if (p == nullptr) return MSQ_ERR_CUDA;
+    const size_t tile_bytes = static_cast<size_t>(p->total_tiles) * kTileBytes;
+    uint8_t *mem = static_cast<uint8_t *>(
+        scratch(ctx, tile_bytes + static_cast<size_t>(p->total_tiles) * kScaleTileBytes,
+                kScratchOperand));
+    if (mem == nullptr) return MSQ_ERR_CUDA;
+    const uint8_t *codes = static_cast<const uint8_t *>(values);
+    const uint8_t *sf = static_cast<const uint8_t *>(scales);
+    if (fp4) {
+      MSQ_TRY(launchPackMx<kMxCodesFp4>(ctx, b, p, nullptr, codes, sf, mem, mem + tile_bytes));
+    } else {
+      MSQ_TRY(launchPackMx<kMxCodesFp8>(ctx, b, p, nullptr, codes, sf, mem, mem + tile_bytes));
+    }
+    return runMxGemm(ctx, b, p, mem, mem + tile_bytes, x);
   }
   TcPlan *p = tcPlan(ctx, b, kind);
   if (p == nullptr) return MSQ_ERR_CUDA;

@@ -64,6 +64,56 @@ __device__ __forceinline__ uint64_t smemDesc(uint32_t addr) {
          (static_cast<uint64_t>(2) << 61);             // SWIZZLE_128B
 }
 
+// Shared-memory descriptor of a no-swizzle K-major matrix whose 8-row x
+// 16-byte core matrices are stored back to back (128 bytes apart along M):
+// the source of tcgen05.cp for a 32-row x 16-byte scale-factor atom.
+__device__ __forceinline__ uint64_t smemDescPlain(uint32_t addr) {
+  return static_cast<uint64_t>((addr >> 4) & 0x3FFFu) |
+         (static_cast<uint64_t>(128 >> 4) << 16) |     // LBO (one core matrix along K)
+         (static_cast<uint64_t>(128 >> 4) << 32) |     // SBO: next 8 rows
+         (static_cast<uint64_t>(1) << 46);             // descriptor version, no swizzle
+}
+
+// Copies a 32-row x 128-bit scale-factor atom from shared memory into four
+// consecutive TMEM columns of lanes 0-31, replicated into the lanes of all
+// four sub-partitions (lane l + 32q, q = 0..3).  Ordered with the issuing
+// thread's later tcgen05.mma.
+__device__ __forceinline__ void tmemCopyScales(uint32_t taddr, uint64_t sdesc) {
+  asm volatile("tcgen05.cp.cta_group::1.32x128b.warpx4 [%0], %1;" ::"r"(taddr), "l"(sdesc)
+               : "memory");
+}
+
+// Instruction descriptor of the block-scaled kinds (kind::mxf4 with E2M1
+// A and B, or kind::mxf8f6f4 with E4M3 A and B), FP32 D, K-major operands,
+// M = N = 128, UE8M0 scale factors; sf_a / sf_b pick the byte of each
+// scale-factor word that holds this MMA's first K block.
+__host__ __device__ constexpr uint32_t instrDescBlockScaled(bool fp4, uint32_t sf_a,
+                                                            uint32_t sf_b) {
+  return (sf_b << 4) | ((fp4 ? 1u : 0u) << 7) | ((fp4 ? 1u : 0u) << 10) | ((128u >> 3) << 17) |
+         (1u << 23) | ((128u >> 4) << 24) | (sf_a << 29);
+}
+
+// D (TMEM) = (A * SFA)(B * SFB)^T (+ D): E2M1 operands, K = 64 per MMA, two
+// UE8M0 scale factors per row (one per 32 K).
+__device__ __forceinline__ void mmaMxf4(uint32_t tmem, uint64_t a, uint64_t b, uint32_t idesc,
+                                        uint32_t sfa, uint32_t sfb, uint32_t accumulate) {
+  asm volatile(
+      "{\n .reg .pred p;\n setp.ne.b32 p, %6, 0;\n"
+      " tcgen05.mma.cta_group::1.kind::mxf4.block_scale.scale_vec::2X [%0], %1, %2, %3, [%4], "
+      "[%5], p;\n}\n" ::"r"(tmem),
+      "l"(a), "l"(b), "r"(idesc), "r"(sfa), "r"(sfb), "r"(accumulate));
+}
+
+// E4M3 operands, K = 32 per MMA, one UE8M0 scale factor per row.
+__device__ __forceinline__ void mmaMxf8(uint32_t tmem, uint64_t a, uint64_t b, uint32_t idesc,
+                                        uint32_t sfa, uint32_t sfb, uint32_t accumulate) {
+  asm volatile(
+      "{\n .reg .pred p;\n setp.ne.b32 p, %6, 0;\n"
+      " tcgen05.mma.cta_group::1.kind::mxf8f6f4.block_scale.scale_vec::1X [%0], %1, %2, %3, "
+      "[%4], [%5], p;\n}\n" ::"r"(tmem),
+      "l"(a), "l"(b), "r"(idesc), "r"(sfa), "r"(sfb), "r"(accumulate));
+}
+
 // Instruction descriptor of kind::f16 with BF16 A and B, FP32 D, both
 // operands K-major, shape M x N.
 __host__ __device__ constexpr uint32_t instrDescBf16(uint32_t m, uint32_t n) {

@@ -185,3 +185,55 @@ def test_paper_set_vii_with_a_bf16_basis_reports_its_outcome(tmp_path):
     rc, r, err = _run(tmp_path, a, "bf16", 1e-12, 8)
     assert rc == 0, err
     assert r["status"] in ("nonfinite", "diverged", "budget_exhausted"), r
+
+
+def _oracle_quantized_orthogonality(a, fmt):
+    """||Q(V) Q(V)^T - I||_F / sqrt(n) of the oracle's quantization of the
+    eigenbasis the mirror computes: the blocked Jacobi restatement is
+    bit-exact with the GPU's, so V is the same; V^T is stored K-major (row i
+    of V contiguous) and quantized by the flat codec as the mirror does."""
+    a32 = np.asarray(a, np.float32)
+    _, v, _, _ = O.jacobi_blocked(a32.astype(np.float64), 1e-7, 15)
+    n = a.shape[0]
+    flat = np.ascontiguousarray(np.asarray(v, np.float32).reshape(-1, order="C"))
+    row_length = n if fmt == 8 else 0
+    vals, scl = O.encode(fmt, flat, row_length=row_length)
+    vq = O.decode(fmt, vals, scl, n * n, row_length=row_length).reshape(n, n).astype(np.float64)
+    g = vq @ vq.T - np.eye(n)
+    return float(np.linalg.norm(g) / np.sqrt(n))
+
+
+# basis (CLI name), codec id, expected gate decision at n = 96 (entries of V
+# about 0.1): unscaled E2M1 rounds them to 0 or 0.5 and must be rejected;
+# the scaled and wider formats keep them and must be accepted
+GATE_CASES = [("bf16", 1, True), ("fp8_e4m3fn", 2, True), ("fp8_e5m2", 3, None),
+              ("mxfp8_e4m3fn", 4, True), ("mxfp8_e5m2", 5, None), ("fp4_e2m1", 6, False),
+              ("mxfp4_e2m1", 7, True), ("fp8_e4m3fn_rowscale", 8, True)]
+GATE_TOL = {1: 5e-3, 2: 0.15, 3: 0.15, 4: 0.15, 5: 0.15, 6: 0.5, 7: 0.5, 8: 0.15}
+
+
+@pytest.mark.parametrize("basis,fmt,accept", GATE_CASES)
+def test_orthogonality_gate_against_the_oracle(tmp_path, basis, fmt, accept):
+    """measureF32Orthogonality and the basis gate (src/metal_runtime.cpp:
+    742-776, src/metal_solver.cpp:217-263): the mirror's quantized-basis
+    orthogonality equals the oracle's ||Q(V) Q(V)^T - I||_F / sqrt(n), and the
+    basis is kept exactly when that is within basisOrthogonalityTolerance
+    (src/configuration.cpp:109-118), else escalated to FP32 (with the
+    escalation counted), and the case still converges."""
+    a = O.controlled(96, 1e2)
+    rc, r, err = _run(tmp_path, a, basis, 1e-12, 12)
+    assert rc == 0, err
+    measured = float(r["quantized_basis_orthogonality"])
+    expected = _oracle_quantized_orthogonality(a, fmt)
+    assert abs(measured - expected) <= 1e-4 * expected + 1e-7, (measured, expected)
+    kept = expected <= GATE_TOL[fmt]
+    if accept is not None:
+        assert kept == accept, (basis, expected)
+    if kept:
+        assert r["selected_basis_stage"] == basis and int(r["precision_escalations"]) == 0
+    else:
+        assert r["selected_basis_stage"] == basis + "_rejected_to_fp32"
+        assert int(r["precision_escalations"]) == 1
+    assert r["status"] == "converged" and float(r["final_residual"]) <= 1e-12
+    # the FP32 basis itself is orthonormal to FP32 accuracy
+    assert float(r["basis_orthogonality"]) < 1e-5
