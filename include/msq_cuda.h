@@ -69,7 +69,12 @@ int msq_set_stream(msq_ctx *ctx, void *stream);
  * context's stream, in serial order (same results, bit for bit).          */
 int msq_set_concurrency(msq_ctx *ctx, int enable);
 /* CUDA graphs (default on): the batched Jacobi's launch sequence is captured
- * once per plan, buffers, tolerance and launch shapes, then replayed.
+ * once per plan, buffers, tolerance and launch shapes, then replayed; and
+ * msq_solve_batched captures its whole plan-group sequence (gather, Jacobi,
+ * reconstruction, residuals, corrections, scatter, report copies) on its
+ * second call with the same layout, plans, buffers and tolerance, then
+ * replays it with one graph launch and one synchronisation (the FP32
+ * fallback of a miss, decided on the host, runs after it).
  * enable = 0 launches every kernel directly (same results, bit for bit).   */
 int msq_set_graphs(msq_ctx *ctx, int enable);
 int msq_synchronize(msq_ctx *ctx);
@@ -86,8 +91,11 @@ int msq_synchronize(msq_ctx *ctx);
  * keep their setting: turn graphs off (msq_set_graphs) around such a test.
  * No counterpart in the reference (its Metal waits are host-side).        */
 int msq_debug_expire_waits(int mode);
-/* Number of this library's kernel launches enqueued so far on `ctx`. */
+/* Number of this library's kernel launches enqueued so far on `ctx` (a
+ * replayed graph counts the launches it holds). */
 uint64_t msq_launch_count(const msq_ctx *ctx);
+/* Number of CUDA graph launches issued so far on `ctx`. */
+uint64_t msq_graph_launch_count(const msq_ctx *ctx);
 /* Launch timing for profiling: between begin and end, an event is recorded
  * on the context's stream after every launch (launches on internal streams
  * get a begin and an end event); end synchronises and writes one line per
@@ -358,6 +366,25 @@ int msq_native_sylvester_sweep(msq_ctx *ctx, int format, const float *vectors,
  * when a buffer is too small.                                             */
 int msq_csv_headers(char *summary, size_t summary_capacity, char *iterations,
                     size_t iterations_capacity);
+
+/* ---- general products for the stage-3 spectral plans -----------------------
+ * The pieces of run_spectral's FP32 products (3_spectral/spectral.cpp:
+ * 1145-1230: MPS GEMMs, apply_scale_f32, working_add, residual_and_norm)
+ * for operands that are not symmetric (an explicit basis inverse):
+ * msq_gemm: C = op(A) op(B) per matrix (FP32 FMA), op = transpose when
+ *   trans_* != 0; with `eigenvalues` (device, batched as lambda) each C_ij
+ *   is divided by sqrt(lambda_i) + sqrt(lambda_j) (the Sylvester step).
+ * msq_working_add: X <- X + E in float-float (x_hi, x_lo), no symmetrisation.
+ * msq_residual_general: msq_residual for a general X.                      */
+int msq_gemm(msq_ctx *ctx, int trans_a, int trans_b, const float *a, const float *b,
+             const int32_t *n, const int64_t *offset, int count,
+             const float *eigenvalues, float *c);
+int msq_working_add(msq_ctx *ctx, float *x_hi, float *x_lo, const float *e,
+                    const int32_t *n, const int64_t *offset, int count);
+int msq_residual_general(msq_ctx *ctx, const float *a, const float *a_lo,
+                         const float *x_hi, const float *x_lo, const int32_t *n,
+                         const int64_t *offset, int count, float *residual,
+                         double *norms);
 
 /* ---- whole-pipeline batched solve ------------------------------------------
  * The GPU-resident solve of solveGpuResidentSpd (src/metal_solver.cpp:92-336)

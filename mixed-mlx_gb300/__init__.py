@@ -75,6 +75,7 @@ _SIGS = {
     "msq_synchronize": (ctypes.c_int, [_P]),
     "msq_debug_expire_waits": (ctypes.c_int, [ctypes.c_int]),
     "msq_launch_count": (ctypes.c_uint64, [_P]),
+    "msq_graph_launch_count": (ctypes.c_uint64, [_P]),
     "msq_storage_bytes": (ctypes.c_size_t, [ctypes.c_int, ctypes.c_size_t]),
     "msq_scale_bytes": (ctypes.c_size_t, [ctypes.c_int, ctypes.c_size_t, ctypes.c_size_t]),
     "msq_encode": (ctypes.c_int, [_P, ctypes.c_int, _P, ctypes.c_size_t, ctypes.c_size_t, _P, _P]),
@@ -256,6 +257,10 @@ class Context:
     @property
     def launches(self) -> int:
         return int(lib().msq_launch_count(self.handle))
+
+    @property
+    def graph_launches(self) -> int:
+        return int(lib().msq_graph_launch_count(self.handle))
 
     def autotune_report(self) -> str:
         """The launch-shape autotuner's decisions for this context's device."""

@@ -241,6 +241,61 @@ struct CudaRunOptions {
   int device = 0;
 };
 
+// ---- stage-3 precision plans (3_spectral/spectral.cpp:769-1385) ----------
+// The factor formats of FactorFormat (3_spectral/spectral.hpp); names as
+// format_name (:321-339).
+enum class CudaFactorFormat { Fp32, Fp16, Bf16, Fp8E4M3, Fp8E5M2, MxFp8E4M3, MxFp4E2M1 };
+const char *cudaFactorFormatName(CudaFactorFormat format);
+
+struct CudaPrecisionPlan {
+  std::string name;
+  CudaFactorFormat basis;
+  CudaFactorFormat spectrum;
+};
+// precision_plans() (:769-786): the same 16 plans in the same order.
+std::vector<CudaPrecisionPlan> cudaPrecisionPlans();
+
+struct CudaSpectralIteration {
+  size_t iteration;
+  double residual;
+  double forward_error;
+  bool low_product;  // the correction ran on low-bit operands
+};
+
+// SpectralResult's fields that have a CUDA meaning.
+struct CudaSpectralResult {
+  std::string plan, basis_format, spectrum_format, product_backend, arithmetic_format;
+  std::string reason;  // converged, correction_limit, divergent, nonfinite_residual,
+                       // ill_conditioned_basis, invalid_spectrum
+  size_t order = 0;
+  double condition = 0.0;
+  bool accepted = false;
+  bool converged = false;
+  size_t iterations = 0;
+  size_t correction_count = 0;
+  size_t low_product_corrections = 0;
+  double basis_bits_per_value = 0.0;
+  double spectrum_bits_per_value = 0.0;
+  double weighted_factor_storage_bits = 0.0;
+  double basis_relative_error = 0.0;
+  double spectrum_relative_error = 0.0;
+  double basis_condition = 0.0;
+  double initial_error = 0.0;
+  double final_error = 0.0;
+  double final_residual = 0.0;
+  std::vector<CudaSpectralIteration> history;
+};
+
+// run_spectral's counterpart: the plan's factor formats, the initial root,
+// frozen-basis corrections (low-bit products with the stall fallback for a
+// low-bit basis below condition 1000) until `tolerance`, `max_corrections`
+// or divergence.  problem.condition selects the low-bit products as the
+// reference's problem.condition does; problem.supplied_reference (FP64
+// root) gives the forward errors.
+CudaSpectralResult runCudaSpectral(CudaRuntime &runtime, const CudaProblem &problem,
+                                   const CudaPrecisionPlan &plan, size_t max_corrections = 30,
+                                   double tolerance = 1.0e-12);
+
 // The reference's CSV schema (writeSummaryHeader / writeCaseCsv /
 // writeIterationsHeader, src/reporting.cpp:124-330): the same columns in the
 // same order, so analysis written for the reference's summary and

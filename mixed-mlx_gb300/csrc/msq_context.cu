@@ -202,6 +202,7 @@ const DeviceBatch *prepareBatch(msq_ctx *ctx, const int32_t *n,
     cudaFree(old->offset);
     delete old;
     ctx->batches.erase(ctx->batches.begin());
+    ++ctx->alloc_generation;
   }
   ctx->batches.push_back(b);
   return b;
@@ -214,6 +215,7 @@ void *scratch(msq_ctx *ctx, size_t bytes, int slot) {
     cudaFree(ctx->scratch[slot]);
     ctx->scratch[slot] = nullptr;
     ctx->scratch_bytes[slot] = 0;
+    ++ctx->alloc_generation;
   }
   const size_t rounded = (bytes + (1u << 20) - 1) & ~static_cast<size_t>((1u << 20) - 1);
   if (cudaCheck(ctx, cudaMalloc(&ctx->scratch[slot], rounded), "scratch alloc") != MSQ_OK) {
@@ -222,6 +224,24 @@ void *scratch(msq_ctx *ctx, size_t bytes, int slot) {
   }
   ctx->scratch_bytes[slot] = rounded;
   return ctx->scratch[slot];
+}
+
+void *pinnedScratch(msq_ctx *ctx, size_t bytes) {
+  if (bytes <= ctx->pinned_bytes) return ctx->pinned;
+  if (ctx->pinned != nullptr) {
+    cudaStreamSynchronize(ctx->stream);
+    cudaFreeHost(ctx->pinned);
+    ctx->pinned = nullptr;
+    ctx->pinned_bytes = 0;
+    ++ctx->alloc_generation;
+  }
+  const size_t rounded = (bytes + 65535) & ~static_cast<size_t>(65535);
+  if (cudaCheck(ctx, cudaMallocHost(&ctx->pinned, rounded), "pinned staging alloc") != MSQ_OK) {
+    ctx->pinned = nullptr;
+    return nullptr;
+  }
+  ctx->pinned_bytes = rounded;
+  return ctx->pinned;
 }
 
 }  // namespace msq
@@ -259,6 +279,8 @@ extern "C" void msq_destroy(msq_ctx *ctx) {
     if (ctx->scratch[slot] != nullptr) cudaFree(ctx->scratch[slot]);
   if (ctx->grid_exec != nullptr) cudaGraphExecDestroy(ctx->grid_exec);
   for (auto &g : ctx->jacobi_graphs) cudaGraphExecDestroy(g.exec);
+  for (auto &g : ctx->solve_graphs) cudaGraphExecDestroy(g.exec);
+  if (ctx->pinned != nullptr) cudaFreeHost(ctx->pinned);
   destroyJacobiPlans(ctx->jacobi_plans);
   destroyTcPlans(ctx->tc_plans);
   if (ctx->grid_host != nullptr) cudaFreeHost(ctx->grid_host);
@@ -308,6 +330,10 @@ extern "C" int msq_synchronize(msq_ctx *ctx) {
 
 extern "C" uint64_t msq_launch_count(const msq_ctx *ctx) {
   return ctx == nullptr ? 0 : ctx->launches;
+}
+
+extern "C" uint64_t msq_graph_launch_count(const msq_ctx *ctx) {
+  return ctx == nullptr ? 0 : ctx->graph_launches;
 }
 
 extern "C" int msq_timing_begin(msq_ctx *ctx) {

@@ -124,6 +124,10 @@ gemmTNKernel(GemmArgs args) {
 // X is symmetric, so X X is too: only tiles on or above the diagonal are
 // computed, and an off-diagonal tile also writes R_ji = A_ji - (X X)_ij
 // (the same products in the same order as a direct (j, i) tile).
+// kGeneral: X need not be symmetric (the stage-3 plans with an explicit
+// basis inverse): the left operand is read as rows of X, every tile is
+// computed and nothing is mirrored.
+template <bool kGeneral>
 __global__ void __launch_bounds__(kThreads)
 residualFFKernel(ResidualArgs args) {
   __shared__ __align__(16) float Hs[kBK][kTile + 4];
@@ -153,10 +157,13 @@ residualFFKernel(ResidualArgs args) {
         const int idx = threadIdx.x + e * kThreads;
         const int kk = idx % kBK, r = idx / kBK;
         const int k = k0 + kk, gi = i0 + r, gj = j0 + r;
-        // (X X)_ij = sum_k X_ki X_kj (X symmetric): column-contiguous loads
+        // (X X)_ij = sum_k X_ki X_kj (X symmetric): column-contiguous loads;
+        // general X: X_ik from row i
         const bool vi = k < n && gi < n, vj = k < n && gj < n;
-        Hs[kk][r] = vi ? Xh[k + static_cast<int64_t>(gi) * n] : 0.0f;
-        Ls[kk][r] = vi && Xl ? Xl[k + static_cast<int64_t>(gi) * n] : 0.0f;
+        const int64_t ai = kGeneral ? gi + static_cast<int64_t>(k) * n
+                                    : k + static_cast<int64_t>(gi) * n;
+        Hs[kk][r] = vi ? Xh[ai] : 0.0f;
+        Ls[kk][r] = vi && Xl ? Xl[ai] : 0.0f;
         Hb[kk][r] = vj ? Xh[k + static_cast<int64_t>(gj) * n] : 0.0f;
         Lb[kk][r] = vj && Xl ? Xl[k + static_cast<int64_t>(gj) * n] : 0.0f;
       }
@@ -204,7 +211,7 @@ residualFFKernel(ResidualArgs args) {
     const float *A = args.a + off;
     const float *AL = args.a_lo ? args.a_lo + off : nullptr;
     float *R = args.r ? args.r + off : nullptr;
-    const bool mirror = w.z > w.y;
+    const bool mirror = !kGeneral && w.z > w.y;
     double rn = 0.0, an = 0.0;
 #pragma unroll
     for (int c = 0; c < 4; ++c) {
@@ -342,6 +349,33 @@ __global__ void symmetricAddKernel(float *__restrict__ x_hi, float *__restrict__
   }
 }
 
+// X <- X + E in float-float (the reference's working_add,
+// metal_mixed_sqrt.metal:1955-1970): two-sum of the high word and E, the
+// error and the low word renormalised into (hi, lo).
+__global__ void workingAddKernel(float *__restrict__ x_hi, float *__restrict__ x_lo,
+                                 const float *__restrict__ e, const int32_t *__restrict__ nn,
+                                 const int64_t *__restrict__ off, const int4 *__restrict__ work,
+                                 int items) {
+  for (int item = blockIdx.x; item < items; item += gridDim.x) {
+    const int mi = work[item].x;
+    const int n = nn[mi];
+    const int i = work[item].y * 32 + threadIdx.x;
+    for (int jj = threadIdx.y; jj < 32; jj += blockDim.y) {
+      const int j = work[item].z * 32 + jj;
+      if (i >= n || j >= n) continue;
+      const int64_t idx = off[mi] + i + static_cast<int64_t>(j) * n;
+      const float corr = e[idx];
+      const float h = x_hi[idx], l = x_lo[idx];
+      const float s = h + corr;
+      const float vr = s - h;
+      const float err = (h - (s - vr)) + (corr - vr) + l;
+      const float hi = s + err;
+      x_hi[idx] = hi;
+      x_lo[idx] = err - (hi - s);
+    }
+  }
+}
+
 }  // namespace
 
 int gemmWork(msq_ctx *ctx, const DeviceBatch *b, int tile, const int4 **work, int *items) {
@@ -417,7 +451,7 @@ int residualFF(msq_ctx *ctx, const DeviceBatch *b, const float *a, const float *
   MSQ_TRY(cudaCheck(ctx, cudaMemsetAsync(norms, 0, 2 * b->count * sizeof(double), ctx->stream),
                     "norm reset"));
   const unsigned grid = std::min<unsigned>(args.items, kSmCount * 8);
-  residualFFKernel<<<grid, kThreads, 0, ctx->stream>>>(args);
+  residualFFKernel<false><<<grid, kThreads, 0, ctx->stream>>>(args);
   return launched(ctx, "residual float-float");
 }
 
@@ -490,6 +524,34 @@ int diagonalSylvester(msq_ctx *ctx, const float *w, const float *s, float *c, in
   const int grid = static_cast<int>(std::min<int64_t>((total + 255) / 256, kSmCount * 8));
   diagonalSylvesterKernel<<<grid, 256, 0, ctx->stream>>>(w, s, c, n);
   return launched(ctx, "native diagonal sylvester");
+}
+
+int residualFFGeneral(msq_ctx *ctx, const DeviceBatch *b, const float *a, const float *x_hi,
+                      const float *x_lo, float *r, double *norms, const float *a_lo) {
+  ResidualArgs args{};
+  MSQ_TRY(gemmWork(ctx, b, kTile, &args.work, &args.items));  // every tile
+  args.a = a;
+  args.a_lo = a_lo;
+  args.x_hi = x_hi;
+  args.x_lo = x_lo;
+  args.r = r;
+  args.norms = norms;
+  args.offset = b->offset;
+  args.n = b->n;
+  MSQ_TRY(cudaCheck(ctx, cudaMemsetAsync(norms, 0, 2 * b->count * sizeof(double), ctx->stream),
+                    "norm reset"));
+  const unsigned grid = std::min<unsigned>(args.items, kSmCount * 8);
+  residualFFKernel<true><<<grid, kThreads, 0, ctx->stream>>>(args);
+  return launched(ctx, "residual float-float (general X)");
+}
+
+int workingAdd(msq_ctx *ctx, const DeviceBatch *b, float *x_hi, float *x_lo, const float *e) {
+  const int4 *work;
+  int items;
+  MSQ_TRY(gemmWork(ctx, b, 32, &work, &items));
+  workingAddKernel<<<std::min(items, kSmCount * 16), dim3(32, 8), 0, ctx->stream>>>(
+      x_hi, x_lo, e, b->n, b->offset, work, items);
+  return launched(ctx, "working add");
 }
 
 int symmetricAdd(msq_ctx *ctx, const DeviceBatch *b, float *x_hi, float *x_lo, const float *e) {

@@ -46,6 +46,11 @@ int residualFF(msq_ctx *ctx, const DeviceBatch *b, const float *a, const float *
 int makeFactor(msq_ctx *ctx, const DeviceBatch *b, const float *v, const float *lam, float *f);
 int transpose(msq_ctx *ctx, const DeviceBatch *b, const float *src, float *dst);
 int symmetricAdd(msq_ctx *ctx, const DeviceBatch *b, float *x_hi, float *x_lo, const float *e);
+// The same residual for a general (not necessarily symmetric) X.
+int residualFFGeneral(msq_ctx *ctx, const DeviceBatch *b, const float *a, const float *x_hi,
+                      const float *x_lo, float *r, double *norms, const float *a_lo = nullptr);
+// X <- X + E in float-float, no symmetrisation.
+int workingAdd(msq_ctx *ctx, const DeviceBatch *b, float *x_hi, float *x_lo, const float *e);
 // One n x n matrix: C = A B with in-order FMA chains; C_ij = W_ij / (s_i + s_j).
 int matmulFma(msq_ctx *ctx, const float *a, const float *b, float *c, int n);
 int diagonalSylvester(msq_ctx *ctx, const float *w, const float *s, float *c, int n);

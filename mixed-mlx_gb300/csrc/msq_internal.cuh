@@ -142,6 +142,26 @@ struct msq_ctx {
   void *grid_work = nullptr;
   std::vector<cudaEvent_t> sync_pool;
   size_t sync_next = 0;
+  // Whole-solve graphs (msq_solve_batched): the plan groups' launch
+  // sequence of a call, captured once per (layout, plans, buffers,
+  // tolerance) after one direct run of that call (which sizes every
+  // scratch arena and cache), replayed while alloc_generation is unchanged.
+  // alloc_generation counts every free of memory a captured graph may use
+  // (scratch growth, evicted batch layouts and launch plans, pinned
+  // staging growth).
+  struct SolveGraph {
+    uint64_t key;
+    uint64_t generation;
+    cudaGraphExec_t exec;
+    uint64_t launches;
+  };
+  std::vector<SolveGraph> solve_graphs;
+  std::vector<uint64_t> solve_seen;  // keys already run directly once
+  uint64_t alloc_generation = 0;
+  bool capturing = false;            // a whole-solve capture is open
+  uint64_t graph_launches = 0;       // cudaGraphLaunch calls of this context
+  void *pinned = nullptr;            // host staging of the solve's reports
+  size_t pinned_bytes = 0;
 };
 
 namespace msq {
@@ -173,6 +193,8 @@ enum ScratchSlot : int {
   kScratchJacobi = 0, kScratchSolver = 1, kScratchOperand = 2, kScratchGemm = 3, kScratchGrid = 4
 };
 void *scratch(msq_ctx *ctx, size_t bytes, int slot);
+// Grow-only pinned host staging (for reports copied back inside a graph).
+void *pinnedScratch(msq_ctx *ctx, size_t bytes);
 
 // Makes the context's device current for one entry point and restores the
 // caller's device on return (a process may drive several GPUs).

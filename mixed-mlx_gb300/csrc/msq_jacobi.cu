@@ -1013,6 +1013,7 @@ JacobiPlan *planFor(msq_ctx *ctx, const DeviceBatch *b, int mode) {
   }
   if (plans.size() >= 8) {
     cudaFree(plans.front()->device);
+    ++ctx->alloc_generation;
     delete plans.front();
     plans.erase(plans.begin());
   }
@@ -1042,6 +1043,23 @@ int setKernelAttributes() {
 }  // namespace
 
 // Enqueues the whole solve on ctx->stream (Jacobi scratch arena).
+// Whether jacobiEnqueue on this batch can run inside a whole-solve capture:
+// every matrix on the batched kernels (the grid path synchronises per
+// sweep) and no size class still being timed by the launch-shape tuner.
+bool jacobiCapturable(msq_ctx *ctx, const DeviceBatch *b, bool low_bit_basis) {
+  if (b->max_n > kMaxOrder) return false;
+  const int mode = ctx->jacobi_vectors >= 0 ? ctx->jacobi_vectors : (low_bit_basis ? 2 : 0);
+  JacobiPlan *plan = planFor(ctx, b, mode);
+  if (plan == nullptr || !plan->grid_ids.empty()) return false;
+  std::lock_guard<std::mutex> lock(g_tune_mutex);
+  harvestTimings();
+  auto &tune = tuneFor(ctx->device);
+  for (const auto &bucket : plan->buckets) {
+    if (g_tune_enabled && tune[bucket.cls].best < 0) return false;
+  }
+  return true;
+}
+
 int jacobiEnqueue(msq_ctx *ctx, const DeviceBatch *b, float *matrices, float *vectors,
                   float *eigenvalues, double tolerance, int max_sweeps, int32_t *sweeps_done,
                   float *off_ratio, bool low_bit_basis) {
@@ -1122,7 +1140,7 @@ int jacobiEnqueue(msq_ctx *ctx, const DeviceBatch *b, float *matrices, float *ve
   for (const auto &per : shape)
     for (const auto &h : per) shape_hash = (shape_hash ^ static_cast<uint64_t>(h.threads)) * 1099511628211ull;
   const bool graphable = !measuring && !ctx->timing && plan->grid_ids.empty() && ctx->graphs &&
-                         waitTestMode() == kWaitTestOff;
+                         waitTestMode() == kWaitTestOff && !ctx->capturing;
   const JacobiGraphKey key{plan->serial, b->key, b->offset, matrices, vectors, eigenvalues,
                            sweeps_done, off_ratio, work, tolerance, max_sweeps, ctx->concurrent,
                            shape_hash};
@@ -1130,6 +1148,7 @@ int jacobiEnqueue(msq_ctx *ctx, const DeviceBatch *b, float *matrices, float *ve
     for (auto &e : ctx->jacobi_graphs) {
       if (e.key == key) {
         MSQ_TRY(cudaCheck(ctx, cudaGraphLaunch(e.exec, ctx->stream), "jacobi graph launch"));
+        ++ctx->graph_launches;
         ctx->launches += e.launches;
         return MSQ_OK;
       }
@@ -1282,6 +1301,7 @@ int jacobiEnqueue(msq_ctx *ctx, const DeviceBatch *b, float *matrices, float *ve
   }
   ctx->jacobi_graphs.push_back({key, exec, captured});
   MSQ_TRY(cudaCheck(ctx, cudaGraphLaunch(exec, ctx->stream), "jacobi graph launch"));
+  ++ctx->graph_launches;
   ctx->launches += captured;
   return MSQ_OK;
 }

@@ -321,6 +321,7 @@ int gridJacobiSolve(msq_ctx *ctx, float *matrix, float *vectors, float *eigenval
     if (ratio <= tolerance || sweeps >= max_sweeps) break;
     if (use_graph) {
       MSQ_TRY(cudaCheck(ctx, cudaGraphLaunch(ctx->grid_exec, s), "graph launch"));
+      ++ctx->graph_launches;
       ctx->launches += 2 * static_cast<uint64_t>(nb - 1);
     } else {
       MSQ_TRY(enqueueSweep(s));

@@ -16,6 +16,7 @@
 
 #include <algorithm>
 #include <cmath>
+#include <cstring>
 #include <map>
 #include <vector>
 
@@ -105,6 +106,44 @@ extern "C" int msq_reconstruct_factor(msq_ctx *ctx, int plan_format, const float
   const DeviceBatch *b = prepareBatch(ctx, n, offset, count);
   if (b == nullptr) return MSQ_ERR_INVALID_ARGUMENT;
   return reconstructFromFactor(ctx, b, plan_format, factor_t, root);
+}
+
+extern "C" int msq_gemm(msq_ctx *ctx, int trans_a, int trans_b, const float *a, const float *b,
+                        const int32_t *n, const int64_t *offset, int count,
+                        const float *eigenvalues, float *c) {
+  if (ctx == nullptr) return MSQ_ERR_INVALID_ARGUMENT;
+  msq::DeviceGuard device_guard(ctx);
+  if (!a || !b || !c) return setError(ctx, MSQ_ERR_INVALID_ARGUMENT, "msq_gemm: null buffer");
+  const DeviceBatch *batch = prepareBatch(ctx, n, offset, count);
+  if (batch == nullptr) return MSQ_ERR_INVALID_ARGUMENT;
+  // gemmTN reads A(i,k) at i + k n when M-major (op(A) = A) and at k + i n
+  // otherwise (op(A) = A^T); B(k,j) at k + j n (op(B) = B) or j + k n (B^T)
+  return gemmTN(ctx, batch, a, b, c, eigenvalues ? kEpilogueInverseH : kEpilogueStore,
+                eigenvalues, trans_a == 0, trans_b != 0);
+}
+
+extern "C" int msq_working_add(msq_ctx *ctx, float *x_hi, float *x_lo, const float *e,
+                               const int32_t *n, const int64_t *offset, int count) {
+  if (ctx == nullptr) return MSQ_ERR_INVALID_ARGUMENT;
+  msq::DeviceGuard device_guard(ctx);
+  if (!x_hi || !x_lo || !e)
+    return setError(ctx, MSQ_ERR_INVALID_ARGUMENT, "msq_working_add: null buffer");
+  const DeviceBatch *b = prepareBatch(ctx, n, offset, count);
+  if (b == nullptr) return MSQ_ERR_INVALID_ARGUMENT;
+  return workingAdd(ctx, b, x_hi, x_lo, e);
+}
+
+extern "C" int msq_residual_general(msq_ctx *ctx, const float *a, const float *a_lo,
+                                    const float *x_hi, const float *x_lo, const int32_t *n,
+                                    const int64_t *offset, int count, float *residual,
+                                    double *norms) {
+  if (ctx == nullptr) return MSQ_ERR_INVALID_ARGUMENT;
+  msq::DeviceGuard device_guard(ctx);
+  if (!a || !x_hi || !norms)
+    return setError(ctx, MSQ_ERR_INVALID_ARGUMENT, "msq_residual_general: null buffer");
+  const DeviceBatch *b = prepareBatch(ctx, n, offset, count);
+  if (b == nullptr) return MSQ_ERR_INVALID_ARGUMENT;
+  return residualFFGeneral(ctx, b, a, x_hi, x_lo, residual, norms, a_lo);
 }
 
 extern "C" int msq_residual(msq_ctx *ctx, const float *a, const float *a_lo, const float *x_hi,
@@ -198,75 +237,111 @@ bool samePlan(const msq_plan &a, const msq_plan &b) {
          a.jacobi_tolerance == b.jacobi_tolerance && a.jacobi_max_sweeps == b.jacobi_max_sweeps;
 }
 
-// Runs one plan over a sub-batch whose matrices are copied into the solver
-// arena (compact layout), writes X into `root` at the caller's offsets and
-// the per-matrix residuals into `final_res` / `initial_res`.
-// extra_sweeps > 0 (the FP32 fallback): after the plan's sweeps, further
-// FP32 sweeps while any member's residual misses `tolerance`, at most
-// extra_sweeps, as the reference's plain method corrects until its
-// tolerance is met (src/accelerate_backend.cpp:803-1091); *applied returns
-// the sweeps the group received.
-int runGroup(msq_ctx *ctx, const float *a_user, const int32_t *n_user,
-             const int64_t *off_user, const Group &g, float *root,
-             std::vector<double> &final_res, std::vector<double> &initial_res,
-             std::vector<int> &jsweeps, double tolerance = 0.0, int extra_sweeps = 0,
-             int *applied = nullptr) {
-  const int count = static_cast<int>(g.members.size());
-  std::vector<int32_t> n(count);
-  std::vector<int64_t> off(count);
-  int64_t total = 0, order_total = 0;
-  for (int i = 0; i < count; ++i) {
-    n[i] = n_user[g.members[i]];
-    off[i] = total;
-    total += (static_cast<int64_t>(n[i]) * n[i] + 3) & ~int64_t(3);
-    order_total += n[i];
-  }
-  const DeviceBatch *b = prepareBatch(ctx, n.data(), off.data(), count);
-  if (b == nullptr) return MSQ_ERR_INVALID_ARGUMENT;
-  const size_t mat = alignUp(total * sizeof(float));
-  const size_t vec = alignUp(order_total * sizeof(float));
-  const size_t norms_bytes = alignUp(2 * count * sizeof(double));
-  const size_t sweeps_bytes = alignUp(count * sizeof(int32_t));
-  // the fallback's extra sweeps keep a copy of X to undo a sweep that did
-  // not lower a matrix's residual
-  const size_t backup = extra_sweeps > 0 ? 2 * mat : 0;
-  char *w = static_cast<char *>(scratch(ctx, 8 * mat + vec + norms_bytes + sweeps_bytes + backup,
-                                        kScratchSolver));
-  if (w == nullptr) return MSQ_ERR_CUDA;
-  float *A = reinterpret_cast<float *>(w);
-  float *J = reinterpret_cast<float *>(w + mat);      // Jacobi working copy
-  float *V = reinterpret_cast<float *>(w + 2 * mat);
-  float *F = reinterpret_cast<float *>(w + 3 * mat);
-  float *Xh = reinterpret_cast<float *>(w + 4 * mat);
-  float *Xl = reinterpret_cast<float *>(w + 5 * mat);
-  float *R = reinterpret_cast<float *>(w + 6 * mat);
-  float *W1 = reinterpret_cast<float *>(w + 7 * mat);  // with F: the 2 sweep buffers
-  float *lam = reinterpret_cast<float *>(w + 8 * mat);
-  double *norms = reinterpret_cast<double *>(w + 8 * mat + vec);
-  int32_t *sweeps = reinterpret_cast<int32_t *>(w + 8 * mat + vec + norms_bytes);
+// A plan group's buffers in the solver arena (compact layout: the group's
+// matrices back to back) and its batch.
+struct GroupBuffers {
+  const DeviceBatch *b = nullptr;
+  std::vector<int32_t> n;
+  std::vector<int64_t> off;
+  int64_t total = 0;
+  size_t mat = 0;
+  float *A, *J, *V, *F, *Xh, *Xl, *R, *W1, *lam, *Bh, *Bl;
+  double *norms;
+  int32_t *sweeps;
+};
 
-  // Gather the group's matrices (contiguous groups copy in one go).
+// Stream-ordered copies of a group's outcome into pinned host memory:
+// ||R0||^2, ||A||^2 per member after the reconstruction, the same after the
+// plan's sweeps, and the Jacobi sweeps per member.
+struct GroupReport {
+  double *initial;
+  double *final;
+  int32_t *sweeps;
+};
+
+size_t reportBytes(int count) { return (4 * sizeof(double) + sizeof(int32_t)) * count + 64; }
+
+GroupReport reportAt(void *base, int count) {
+  auto *d = static_cast<double *>(base);
+  return {d, d + 2 * count, reinterpret_cast<int32_t *>(d + 4 * count)};
+}
+
+// Runs of members whose caller offsets are contiguous: one copy each.
+template <class Copy>
+int forEachRun(const Group &g, const int64_t *off_user, const GroupBuffers &gb, Copy copy) {
+  const int count = static_cast<int>(g.members.size());
   for (int i = 0; i < count;) {
     int j = i + 1;
     while (j < count && g.members[j] == g.members[j - 1] + 1 &&
-           off_user[g.members[j]] == off_user[g.members[j - 1]] +
-                                         ((static_cast<int64_t>(n[j - 1]) * n[j - 1] + 3) & ~int64_t(3)))
+           off_user[g.members[j]] ==
+               off_user[g.members[j - 1]] +
+                   ((static_cast<int64_t>(gb.n[j - 1]) * gb.n[j - 1] + 3) & ~int64_t(3)))
       ++j;
     const int64_t last = j - 1;
-    const int64_t bytes = (off[last] - off[i] + static_cast<int64_t>(n[last]) * n[last]) * sizeof(float);
-    MSQ_TRY(cudaCheck(ctx, cudaMemcpyAsync(A + off[i], a_user + off_user[g.members[i]], bytes,
-                                           cudaMemcpyDeviceToDevice, ctx->stream), "gather A"));
+    const int64_t bytes =
+        (gb.off[last] - gb.off[i] + static_cast<int64_t>(gb.n[last]) * gb.n[last]) * sizeof(float);
+    MSQ_TRY(copy(off_user[g.members[i]], gb.off[i], bytes));
     i = j;
   }
-  MSQ_TRY(cudaCheck(ctx, cudaMemcpyAsync(J, A, total * sizeof(float), cudaMemcpyDeviceToDevice,
-                                         ctx->stream), "jacobi copy"));
+  return MSQ_OK;
+}
+
+// Enqueues one plan over its sub-batch on ctx->stream with no host
+// synchronisation: gather into the arena, Jacobi, factor, reconstruction,
+// residual, the plan's sweeps, final residual, and the report copies.
+// `backup`: room for a copy of X (the fallback's undo).
+int enqueueGroup(msq_ctx *ctx, const float *a_user, const int32_t *n_user,
+                 const int64_t *off_user, const Group &g, GroupReport rep, bool backup,
+                 GroupBuffers *gb) {
+  const int count = static_cast<int>(g.members.size());
+  gb->n.resize(count);
+  gb->off.resize(count);
+  int64_t total = 0, order_total = 0;
+  for (int i = 0; i < count; ++i) {
+    gb->n[i] = n_user[g.members[i]];
+    gb->off[i] = total;
+    total += (static_cast<int64_t>(gb->n[i]) * gb->n[i] + 3) & ~int64_t(3);
+    order_total += gb->n[i];
+  }
+  gb->total = total;
+  const DeviceBatch *b = prepareBatch(ctx, gb->n.data(), gb->off.data(), count);
+  if (b == nullptr) return MSQ_ERR_INVALID_ARGUMENT;
+  gb->b = b;
+  const size_t mat = alignUp(total * sizeof(float));
+  gb->mat = mat;
+  const size_t vec = alignUp(order_total * sizeof(float));
+  const size_t norms_bytes = alignUp(2 * count * sizeof(double));
+  const size_t sweeps_bytes = alignUp(count * sizeof(int32_t));
+  const size_t backup_bytes = backup ? 2 * mat : 0;
+  char *w = static_cast<char *>(
+      scratch(ctx, 8 * mat + vec + norms_bytes + sweeps_bytes + backup_bytes, kScratchSolver));
+  if (w == nullptr) return MSQ_ERR_CUDA;
+  gb->A = reinterpret_cast<float *>(w);
+  gb->J = reinterpret_cast<float *>(w + mat);       // Jacobi working copy
+  gb->V = reinterpret_cast<float *>(w + 2 * mat);
+  gb->F = reinterpret_cast<float *>(w + 3 * mat);
+  gb->Xh = reinterpret_cast<float *>(w + 4 * mat);
+  gb->Xl = reinterpret_cast<float *>(w + 5 * mat);
+  gb->R = reinterpret_cast<float *>(w + 6 * mat);
+  gb->W1 = reinterpret_cast<float *>(w + 7 * mat);  // with F: the 2 sweep buffers
+  gb->lam = reinterpret_cast<float *>(w + 8 * mat);
+  gb->norms = reinterpret_cast<double *>(w + 8 * mat + vec);
+  gb->sweeps = reinterpret_cast<int32_t *>(w + 8 * mat + vec + norms_bytes);
+  gb->Bh = reinterpret_cast<float *>(w + 8 * mat + vec + norms_bytes + sweeps_bytes);
+  gb->Bl = gb->Bh + mat / sizeof(float);
+  MSQ_TRY(forEachRun(g, off_user, *gb, [&](int64_t user_off, int64_t arena_off, int64_t bytes) {
+    return cudaCheck(ctx, cudaMemcpyAsync(gb->A + arena_off, a_user + user_off, bytes,
+                                          cudaMemcpyDeviceToDevice, ctx->stream), "gather A");
+  }));
+  MSQ_TRY(cudaCheck(ctx, cudaMemcpyAsync(gb->J, gb->A, total * sizeof(float),
+                                         cudaMemcpyDeviceToDevice, ctx->stream), "jacobi copy"));
   const int max_sweeps = g.plan.jacobi_max_sweeps > 0 ? g.plan.jacobi_max_sweeps : 15;
-  MSQ_TRY(jacobiEnqueue(ctx, b, J, V, lam, g.plan.jacobi_tolerance, max_sweeps, sweeps, nullptr,
-                        g.plan.format != MSQ_PLAN_FP32));
-  MSQ_TRY(makeFactor(ctx, b, V, lam, F));
-  MSQ_TRY(reconstructFromFactor(ctx, b, g.plan.format, F, Xh));
-  MSQ_TRY(cudaCheck(ctx, cudaMemsetAsync(Xl, 0, total * sizeof(float), ctx->stream), "x_lo reset"));
-  std::vector<double> host_norms(2 * count);
+  MSQ_TRY(jacobiEnqueue(ctx, b, gb->J, gb->V, gb->lam, g.plan.jacobi_tolerance, max_sweeps,
+                        gb->sweeps, nullptr, g.plan.format != MSQ_PLAN_FP32));
+  MSQ_TRY(makeFactor(ctx, b, gb->V, gb->lam, gb->F));
+  MSQ_TRY(reconstructFromFactor(ctx, b, g.plan.format, gb->F, gb->Xh));
+  MSQ_TRY(cudaCheck(ctx, cudaMemsetAsync(gb->Xl, 0, total * sizeof(float), ctx->stream),
+                    "x_lo reset"));
   // Corrections use the FP32 stable basis V, as the reference's fp32_frozen
   // stage does (src/metal_solver.cpp:304-325).  The plain FP32 plan runs its
   // GEMMs and residuals on the CUDA cores in FP32 / float-float; low-bit
@@ -280,89 +355,118 @@ int runGroup(msq_ctx *ctx, const float *a_user, const int32_t *n_user,
   const bool low_bit = g.plan.format != MSQ_PLAN_FP32;
   const int gemm_format = low_bit ? MSQ_FMT_BF16 : MSQ_FMT_FP32;
   auto residual = [&](bool accurate) {
-    return low_bit && !accurate ? residualTc(ctx, b, A, Xh, Xl, R, norms)
-                                : residualFF(ctx, b, A, Xh, Xl, R, norms);
+    return low_bit && !accurate ? residualTc(ctx, b, gb->A, gb->Xh, gb->Xl, gb->R, gb->norms)
+                                : residualFF(ctx, b, gb->A, gb->Xh, gb->Xl, gb->R, gb->norms);
   };
   MSQ_TRY(residual(g.plan.sweeps == 0));
-  MSQ_TRY(cudaCheck(ctx, cudaMemcpyAsync(host_norms.data(), norms, 2 * count * sizeof(double),
+  MSQ_TRY(cudaCheck(ctx, cudaMemcpyAsync(rep.initial, gb->norms, 2 * count * sizeof(double),
                                          cudaMemcpyDeviceToHost, ctx->stream), "norms read"));
-  MSQ_TRY(cudaCheck(ctx, cudaStreamSynchronize(ctx->stream), "norms sync"));
-  for (int i = 0; i < count; ++i)
-    if (std::isnan(initial_res[g.members[i]]))  // keep the plan's, not the fallback's
-      initial_res[g.members[i]] = std::sqrt(host_norms[2 * i] / host_norms[2 * i + 1]);
   for (int s = 0; s < g.plan.sweeps; ++s) {
-    MSQ_TRY(sylvesterSweep(ctx, b, gemm_format, V, lam, R, Xh, Xl, F, W1));
+    MSQ_TRY(sylvesterSweep(ctx, b, gemm_format, gb->V, gb->lam, gb->R, gb->Xh, gb->Xl, gb->F,
+                           gb->W1));
     MSQ_TRY(residual(true));
   }
-  if (g.plan.sweeps > 0) {
-    MSQ_TRY(cudaCheck(ctx, cudaMemcpyAsync(host_norms.data(), norms, 2 * count * sizeof(double),
-                                           cudaMemcpyDeviceToHost, ctx->stream), "norms read"));
-  }
-  int done_sweeps = g.plan.sweeps;
-  float *Bh = reinterpret_cast<float *>(w + 8 * mat + vec + norms_bytes + sweeps_bytes);
-  float *Bl = Bh + mat / sizeof(float);
+  MSQ_TRY(cudaCheck(ctx, cudaMemcpyAsync(rep.final, gb->norms, 2 * count * sizeof(double),
+                                         cudaMemcpyDeviceToHost, ctx->stream), "norms read"));
+  return cudaCheck(ctx, cudaMemcpyAsync(rep.sweeps, gb->sweeps, count * sizeof(int32_t),
+                                        cudaMemcpyDeviceToHost, ctx->stream), "sweeps read");
+}
+
+// Scatter X (hi word; the lo word is below FP32 resolution of the output).
+int scatterGroup(msq_ctx *ctx, const Group &g, const int64_t *off_user, const GroupBuffers &gb,
+                 float *root) {
+  return forEachRun(g, off_user, gb, [&](int64_t user_off, int64_t arena_off, int64_t bytes) {
+    return cudaCheck(ctx, cudaMemcpyAsync(root + user_off, gb.Xh + arena_off, bytes,
+                                          cudaMemcpyDeviceToDevice, ctx->stream), "scatter X");
+  });
+}
+
+double ratio(const double *norms, int i) { return std::sqrt(norms[2 * i] / norms[2 * i + 1]); }
+
+// The FP32 fallback group, run with host decisions: the plan's pipeline,
+// then further FP32 sweeps while any member's residual misses `tolerance`
+// (at most extra_sweeps), as the reference's plain method corrects until its
+// tolerance is met (src/accelerate_backend.cpp:803-1091).  A sweep that does
+// not lower a member's residual is undone for that member and the sweeps
+// stop (Newton from a basis that no longer contracts diverges).
+int runFallback(msq_ctx *ctx, const float *a_user, const int32_t *n_user,
+                const int64_t *off_user, const Group &g, float *root, double tolerance,
+                int extra_sweeps, std::vector<double> &final_res, std::vector<int> &jsweeps,
+                int *applied) {
+  const int count = static_cast<int>(g.members.size());
+  void *host = pinnedScratch(ctx, reportBytes(count));
+  if (host == nullptr) return MSQ_ERR_CUDA;
+  const GroupReport rep = reportAt(host, count);
+  GroupBuffers gb;
+  MSQ_TRY(enqueueGroup(ctx, a_user, n_user, off_user, g, rep, true, &gb));
+  MSQ_TRY(cudaCheck(ctx, cudaStreamSynchronize(ctx->stream), "fallback sync"));
+  std::vector<double> norms(rep.final, rep.final + 2 * count);
+  int done = g.plan.sweeps;
   for (int extra = 0; extra < extra_sweeps; ++extra) {
-    MSQ_TRY(cudaCheck(ctx, cudaStreamSynchronize(ctx->stream), "norms sync"));
     bool all_met = true;
-    for (int i = 0; i < count; ++i)
-      all_met = all_met && std::sqrt(host_norms[2 * i] / host_norms[2 * i + 1]) <= tolerance;
+    for (int i = 0; i < count; ++i) all_met = all_met && ratio(norms.data(), i) <= tolerance;
     if (all_met) break;
-    const std::vector<double> before = host_norms;
-    MSQ_TRY(cudaCheck(ctx, cudaMemcpyAsync(Bh, Xh, total * sizeof(float), cudaMemcpyDeviceToDevice,
-                                           ctx->stream), "x backup"));
-    MSQ_TRY(cudaCheck(ctx, cudaMemcpyAsync(Bl, Xl, total * sizeof(float), cudaMemcpyDeviceToDevice,
-                                           ctx->stream), "x backup"));
-    MSQ_TRY(sylvesterSweep(ctx, b, gemm_format, V, lam, R, Xh, Xl, F, W1));
-    MSQ_TRY(residual(true));
-    ++done_sweeps;
-    MSQ_TRY(cudaCheck(ctx, cudaMemcpyAsync(host_norms.data(), norms, 2 * count * sizeof(double),
+    const std::vector<double> before = norms;
+    MSQ_TRY(cudaCheck(ctx, cudaMemcpyAsync(gb.Bh, gb.Xh, gb.total * sizeof(float),
+                                           cudaMemcpyDeviceToDevice, ctx->stream), "x backup"));
+    MSQ_TRY(cudaCheck(ctx, cudaMemcpyAsync(gb.Bl, gb.Xl, gb.total * sizeof(float),
+                                           cudaMemcpyDeviceToDevice, ctx->stream), "x backup"));
+    MSQ_TRY(sylvesterSweep(ctx, gb.b, MSQ_FMT_FP32, gb.V, gb.lam, gb.R, gb.Xh, gb.Xl, gb.F,
+                           gb.W1));
+    MSQ_TRY(residualFF(ctx, gb.b, gb.A, gb.Xh, gb.Xl, gb.R, gb.norms));
+    ++done;
+    MSQ_TRY(cudaCheck(ctx, cudaMemcpyAsync(norms.data(), gb.norms, 2 * count * sizeof(double),
                                            cudaMemcpyDeviceToHost, ctx->stream), "norms read"));
     MSQ_TRY(cudaCheck(ctx, cudaStreamSynchronize(ctx->stream), "norms sync"));
-    // a matrix whose residual did not drop keeps its previous root (the
-    // corrections stopped contracting: more of them would diverge), and the
-    // sweeps stop there
     bool worse = false;
     for (int i = 0; i < count; ++i) {
-      const double r_new = std::sqrt(host_norms[2 * i] / host_norms[2 * i + 1]);
-      const double r_old = std::sqrt(before[2 * i] / before[2 * i + 1]);
-      if (!(r_new < r_old)) {
+      if (!(ratio(norms.data(), i) < ratio(before.data(), i))) {
         worse = true;
-        const size_t elems = static_cast<size_t>(n[i]) * n[i];
-        MSQ_TRY(cudaCheck(ctx, cudaMemcpyAsync(Xh + off[i], Bh + off[i], elems * sizeof(float),
-                                               cudaMemcpyDeviceToDevice, ctx->stream), "x undo"));
-        MSQ_TRY(cudaCheck(ctx, cudaMemcpyAsync(Xl + off[i], Bl + off[i], elems * sizeof(float),
-                                               cudaMemcpyDeviceToDevice, ctx->stream), "x undo"));
-        host_norms[2 * i] = before[2 * i];
-        host_norms[2 * i + 1] = before[2 * i + 1];
+        const size_t elems = static_cast<size_t>(gb.n[i]) * gb.n[i];
+        MSQ_TRY(cudaCheck(ctx, cudaMemcpyAsync(gb.Xh + gb.off[i], gb.Bh + gb.off[i],
+                                               elems * sizeof(float), cudaMemcpyDeviceToDevice,
+                                               ctx->stream), "x undo"));
+        MSQ_TRY(cudaCheck(ctx, cudaMemcpyAsync(gb.Xl + gb.off[i], gb.Bl + gb.off[i],
+                                               elems * sizeof(float), cudaMemcpyDeviceToDevice,
+                                               ctx->stream), "x undo"));
+        norms[2 * i] = before[2 * i];
+        norms[2 * i + 1] = before[2 * i + 1];
       }
     }
     if (worse) break;
   }
-  if (applied != nullptr) *applied = done_sweeps;
-  std::vector<int32_t> host_sweeps(count);
-  MSQ_TRY(cudaCheck(ctx, cudaMemcpyAsync(host_sweeps.data(), sweeps, count * sizeof(int32_t),
-                                         cudaMemcpyDeviceToHost, ctx->stream), "sweeps read"));
-  // Scatter X (hi word; the lo word is below FP32 resolution of the output),
-  // one copy per run of members whose caller offsets are contiguous.
-  for (int i = 0; i < count;) {
-    int j = i + 1;
-    while (j < count && g.members[j] == g.members[j - 1] + 1 &&
-           off_user[g.members[j]] == off_user[g.members[j - 1]] +
-                                         ((static_cast<int64_t>(n[j - 1]) * n[j - 1] + 3) & ~int64_t(3)))
-      ++j;
-    const int64_t last = j - 1;
-    const int64_t bytes = (off[last] - off[i] + static_cast<int64_t>(n[last]) * n[last]) * sizeof(float);
-    MSQ_TRY(cudaCheck(ctx, cudaMemcpyAsync(root + off_user[g.members[i]], Xh + off[i], bytes,
-                                           cudaMemcpyDeviceToDevice, ctx->stream), "scatter X"));
-    i = j;
-  }
+  *applied = done;
+  MSQ_TRY(scatterGroup(ctx, g, off_user, gb, root));
   MSQ_TRY(cudaCheck(ctx, cudaStreamSynchronize(ctx->stream), "group sync"));
   MSQ_TRY(checkDeviceStatus(ctx));
   for (int i = 0; i < count; ++i) {
-    final_res[g.members[i]] = std::sqrt(host_norms[2 * i] / host_norms[2 * i + 1]);
-    jsweeps[g.members[i]] = host_sweeps[i];
+    final_res[g.members[i]] = ratio(norms.data(), i);
+    jsweeps[g.members[i]] = rep.sweeps[i];
   }
   return MSQ_OK;
+}
+
+uint64_t mix(uint64_t h, uint64_t v) { return (h ^ v) * 1099511628211ull; }
+
+// The whole-solve graph key: layout, plans, buffers, tolerance and the
+// context settings the launch sequence depends on.
+uint64_t solveKey(msq_ctx *ctx, const float *a, const int32_t *n, const int64_t *offset,
+                  int count, const std::vector<Group> &groups, double tolerance,
+                  const float *root) {
+  uint64_t h = 1469598103934665603ull;
+  h = mix(h, static_cast<uint64_t>(count));
+  for (int i = 0; i < count; ++i) h = mix(mix(h, static_cast<uint64_t>(n[i])), static_cast<uint64_t>(offset[i]));
+  for (const Group &g : groups) {
+    uint64_t t;
+    std::memcpy(&t, &g.plan.jacobi_tolerance, sizeof(t));
+    h = mix(mix(mix(mix(h, g.plan.format), g.plan.sweeps), t), g.plan.jacobi_max_sweeps);
+    for (int m : g.members) h = mix(h, static_cast<uint64_t>(m));
+  }
+  uint64_t tol;
+  std::memcpy(&tol, &tolerance, sizeof(tol));
+  h = mix(mix(mix(h, tol), reinterpret_cast<uintptr_t>(a)), reinterpret_cast<uintptr_t>(root));
+  h = mix(mix(h, ctx->concurrent ? 1 : 0), static_cast<uint64_t>(ctx->jacobi_vectors + 8));
+  return mix(h, reinterpret_cast<uintptr_t>(ctx->stream));
 }
 
 }  // namespace
@@ -395,9 +499,115 @@ extern "C" int msq_solve_batched(msq_ctx *ctx, const float *a, const int32_t *n,
   }
   std::vector<double> final_res(count, NAN), initial_res(count, NAN);
   std::vector<int> jsweeps(count, 0), fallback(count, 0), accepted(count, 0), corrections(count, 0);
-  for (const Group &g : groups) {
-    MSQ_TRY(runGroup(ctx, a, n, offset, g, root, final_res, initial_res, jsweeps));
-    for (int m : g.members) corrections[m] = g.plan.sweeps;
+  // The plan groups, enqueued back to back with no host synchronisation and
+  // their reports copied into pinned host memory; one synchronisation at the
+  // end.  From the second call with the same layout, plans, buffers and
+  // tolerance (the first sizes every arena and cache), the whole sequence is
+  // captured once into a CUDA graph and later calls replay it with one
+  // launch, while no freed allocation invalidates it.
+  size_t report_bytes = 0;
+  for (const Group &g : groups) report_bytes += reportBytes(static_cast<int>(g.members.size()));
+  void *host = pinnedScratch(ctx, report_bytes);
+  if (host == nullptr) return MSQ_ERR_CUDA;
+  std::vector<GroupReport> reports;
+  {
+    char *at = static_cast<char *>(host);
+    for (const Group &g : groups) {
+      const int c = static_cast<int>(g.members.size());
+      reports.push_back(reportAt(at, c));
+      at += reportBytes(c);
+    }
+  }
+  const uint64_t key = solveKey(ctx, a, n, offset, count, groups, tolerance, root);
+  bool replayed = false;
+  for (size_t k = 0; k < ctx->solve_graphs.size(); ++k) {
+    auto &e = ctx->solve_graphs[k];
+    if (e.key != key) continue;
+    if (e.generation != ctx->alloc_generation) {  // captured memory was freed since
+      cudaGraphExecDestroy(e.exec);
+      ctx->solve_graphs.erase(ctx->solve_graphs.begin() + k);
+      break;
+    }
+    MSQ_TRY(cudaCheck(ctx, cudaGraphLaunch(e.exec, ctx->stream), "solve graph launch"));
+    ++ctx->graph_launches;
+    ctx->launches += e.launches;
+    replayed = true;
+    break;
+  }
+  if (!replayed) {
+    const bool seen = std::find(ctx->solve_seen.begin(), ctx->solve_seen.end(), key) !=
+                      ctx->solve_seen.end();
+    bool capture = seen && ctx->graphs && !ctx->timing && waitTestMode() == kWaitTestOff;
+    std::vector<GroupBuffers> buffers(groups.size());
+    if (capture) {
+      // the capture must not allocate or synchronise: every group's batch,
+      // Jacobi plan and tuned launch shapes exist after the direct run
+      for (const Group &g : groups) {
+        std::vector<int32_t> gn;
+        std::vector<int64_t> go;
+        int64_t total = 0;
+        for (int m : g.members) {
+          gn.push_back(n[m]);
+          go.push_back(total);
+          total += (static_cast<int64_t>(n[m]) * n[m] + 3) & ~int64_t(3);
+        }
+        const DeviceBatch *b = prepareBatch(ctx, gn.data(), go.data(), static_cast<int>(gn.size()));
+        if (b == nullptr) return MSQ_ERR_INVALID_ARGUMENT;
+        capture = capture && jacobiCapturable(ctx, b, g.plan.format != MSQ_PLAN_FP32);
+      }
+    }
+    const uint64_t generation = ctx->alloc_generation;
+    cudaStream_t caller = ctx->stream;
+    cudaStream_t capture_stream = capture ? auxStream(ctx, 4) : nullptr;
+    if (capture && (capture_stream == nullptr || capture_stream == caller)) capture = false;
+    const uint64_t launches0 = ctx->launches;
+    if (capture) {
+      MSQ_TRY(cudaCheck(ctx, cudaStreamBeginCapture(capture_stream, cudaStreamCaptureModeThreadLocal),
+                        "solve capture"));
+      ctx->stream = capture_stream;
+      ctx->capturing = true;
+    }
+    int status = MSQ_OK;
+    for (size_t k = 0; k < groups.size() && status == MSQ_OK; ++k) {
+      status = enqueueGroup(ctx, a, n, offset, groups[k], reports[k], false, &buffers[k]);
+      if (status == MSQ_OK) status = scatterGroup(ctx, groups[k], offset, buffers[k], root);
+    }
+    if (capture) {
+      ctx->stream = caller;
+      ctx->capturing = false;
+      cudaGraph_t graph = nullptr;
+      const cudaError_t end = cudaStreamEndCapture(capture_stream, &graph);
+      cudaGraphExec_t exec = nullptr;
+      if (status == MSQ_OK && end == cudaSuccess && generation == ctx->alloc_generation &&
+          cudaGraphInstantiate(&exec, graph, 0) == cudaSuccess) {
+        status = cudaCheck(ctx, cudaGraphLaunch(exec, caller), "solve graph launch");
+        ++ctx->graph_launches;
+        if (ctx->solve_graphs.size() >= 4) {
+          cudaGraphExecDestroy(ctx->solve_graphs.front().exec);
+          ctx->solve_graphs.erase(ctx->solve_graphs.begin());
+        }
+        ctx->solve_graphs.push_back({key, generation, exec, ctx->launches - launches0});
+      } else if (status == MSQ_OK) {
+        status = setError(ctx, MSQ_ERR_CUDA, "solve graph capture failed");
+      }
+      if (graph != nullptr) cudaGraphDestroy(graph);
+    } else if (status == MSQ_OK && !seen) {
+      if (ctx->solve_seen.size() >= 16) ctx->solve_seen.erase(ctx->solve_seen.begin());
+      ctx->solve_seen.push_back(key);
+    }
+    MSQ_TRY(status);
+  }
+  MSQ_TRY(cudaCheck(ctx, cudaStreamSynchronize(ctx->stream), "solve sync"));
+  MSQ_TRY(checkDeviceStatus(ctx));
+  for (size_t k = 0; k < groups.size(); ++k) {
+    const Group &g = groups[k];
+    for (size_t i = 0; i < g.members.size(); ++i) {
+      const int m = g.members[i];
+      initial_res[m] = ratio(reports[k].initial, static_cast<int>(i));
+      final_res[m] = ratio(reports[k].final, static_cast<int>(i));
+      jsweeps[m] = reports[k].sweeps[i];
+      corrections[m] = g.plan.sweeps;
+    }
   }
   // The fallback is the FP32 path with FP32 correction sweeps until the
   // tolerance is met (at least one, at most kFallbackSweeps): FP32 Jacobi +
@@ -417,8 +627,8 @@ extern "C" int msq_solve_batched(msq_ctx *ctx, const float *a, const int32_t *n,
   const std::vector<double> plan_res = final_res;
   if (!retry.members.empty()) {
     int applied = 0;
-    MSQ_TRY(runGroup(ctx, a, n, offset, retry, root, final_res, initial_res, jsweeps, tolerance,
-                     kFallbackSweeps - fallback_plan.sweeps, &applied));
+    MSQ_TRY(runFallback(ctx, a, n, offset, retry, root, tolerance,
+                        kFallbackSweeps - fallback_plan.sweeps, final_res, jsweeps, &applied));
     for (int m : retry.members) {
       fallback[m] = 1;
       corrections[m] = applied;

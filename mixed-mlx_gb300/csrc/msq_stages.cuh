@@ -6,6 +6,9 @@
 namespace msq {
 
 // msq_jacobi.cu
+// True when jacobiEnqueue on this batch may run inside a whole-solve graph
+// capture (no grid-path matrix, no size class still being tuned).
+bool jacobiCapturable(msq_ctx *ctx, const DeviceBatch *b, bool low_bit_basis);
 // low_bit_basis: the caller quantizes the basis to BF16 or fewer bits, so the
 // automatic eigenvector mode may accumulate V on the tensor cores.
 int jacobiEnqueue(msq_ctx *ctx, const DeviceBatch *b, float *matrices, float *vectors,

@@ -763,6 +763,7 @@ TcPlan *tcPlan(msq_ctx *ctx, const DeviceBatch *b, int kind) {
              cudaMemcpyHostToDevice);
   if (plans.size() >= 16) {
     cudaFree(plans.front()->device);
+    ++ctx->alloc_generation;
     delete plans.front();
     plans.erase(plans.begin());
   }

@@ -22,9 +22,10 @@ import numpy as np
 # The 8 plans: {BF16, FP8-rowscale, MXFP4} x {0, 1, 2} sweeps minus MXFP4
 # with 0 sweeps (4-bit storage cannot meet a tight tolerance uncorrected).
 # The Jacobi tolerance loosens as more Sylvester sweeps follow it: one
-# correction of a BF16 root lands near 7e-6 whatever the basis, two reach
-# 1e-7 from a basis with off-norm 1e-2 (two Jacobi sweeps fewer than 1e-4).
-JACOBI_TOL = {0: 1e-7, 1: 1e-4, 2: 1e-2}
+# correction of a BF16 root lands near 7e-6 whatever the basis (off-norm
+# 1e-3 is as good as 1e-4 there, one sweep fewer), two reach 1e-7 from a
+# basis with off-norm 1e-2 (two Jacobi sweeps fewer than 1e-4).
+JACOBI_TOL = {0: 1e-7, 1: 1e-3, 2: 1e-2}
 PLANS = [(1, 0), (1, 1), (1, 2), (2, 0), (2, 1), (2, 2), (3, 1), (3, 2)]
 
 
@@ -33,14 +34,14 @@ def plan_structs(msq, index_list):
 
 
 def generate(torch, count: int, seed: int, n_lo: int = 32, n_hi: int = 512,
-             cond_lo: float = 1e1, cond_hi: float = 1e8, device="cuda"):
+             cond_lo: float = 1e1, cond_hi: float = 1e8, device="cuda", orders=None):
     """SPD matrices of three spectrum families (log-uniform, clustered, power
-    law i^-2) with n log-uniform in [n_lo, n_hi] and condition log-uniform in
-    [cond_lo, cond_hi]; Q from QR of a seeded Gaussian.  Returns (orders,
-    list of FP64 tensors)."""
+    law i^-2) with n log-uniform in [n_lo, n_hi] (or the given orders) and
+    condition log-uniform in [cond_lo, cond_hi]; Q from QR of a seeded
+    Gaussian.  Returns (orders, list of FP64 tensors)."""
     rng = np.random.default_rng(seed)
-    orders = np.floor(np.exp(rng.uniform(math.log(n_lo), math.log(n_hi + 1), count))).astype(np.int32)
-    orders = np.clip(orders, n_lo, n_hi)
+    drawn = np.floor(np.exp(rng.uniform(math.log(n_lo), math.log(n_hi + 1), count))).astype(np.int32)
+    orders = np.clip(drawn, n_lo, n_hi) if orders is None else np.asarray(orders, np.int32)
     conds = np.exp(rng.uniform(math.log(cond_lo), math.log(cond_hi), count))
     fams = rng.integers(0, 3, count)
     g = torch.Generator(device=device).manual_seed(seed)
@@ -62,6 +63,24 @@ def generate(torch, count: int, seed: int, n_lo: int = 32, n_hi: int = 512,
         q = q * torch.sign(torch.diagonal(r))
         lt = torch.as_tensor(lam, device=device, dtype=torch.float64)
         a = (q * lt) @ q.T
+        mats.append(0.5 * (a + a.T))
+    return orders, mats
+
+
+def generate_wishart(torch, count: int, seed: int, n_lo: int = 16, n_hi: int = 512,
+                     device="cuda"):
+    """Wishart covariances A = X^T X / m + 1e-6 I, X ~ N(0,1) of shape m x n,
+    m = 2n, n log-uniform in [n_lo, n_hi] (the batched workload's family).
+    Returns (orders, list of FP64 tensors)."""
+    rng = np.random.default_rng(seed)
+    orders = np.floor(np.exp(rng.uniform(math.log(n_lo), math.log(n_hi + 1), count))).astype(np.int32)
+    orders = np.clip(orders, n_lo, n_hi)
+    g = torch.Generator(device=device).manual_seed(seed)
+    mats = []
+    for n in orders:
+        n = int(n)
+        x = torch.randn(2 * n, n, generator=g, device=device, dtype=torch.float64)
+        a = x.T @ x / (2 * n) + 1e-6 * torch.eye(n, device=device, dtype=torch.float64)
         mats.append(0.5 * (a + a.T))
     return orders, mats
 
@@ -90,7 +109,10 @@ class Outcomes:
 
 def score_plans(ctx, msq, torch, batch, flat, tolerance: float) -> Outcomes:
     """Runs every plan on every matrix; records which plans met the tolerance
-    without the fallback and the GPU time each plan took."""
+    on their own (the plan's final float-float residual) and the GPU time
+    each plan took.  The solve runs with a tolerance every plan meets (1e30),
+    so no fallback spends time on the misses; the plan's own residual is
+    compared with `tolerance` here."""
     acc = np.zeros((batch.count, len(PLANS)), dtype=np.float32)
     secs = np.zeros(len(PLANS))
     out = torch.empty_like(flat)
@@ -98,11 +120,11 @@ def score_plans(ctx, msq, torch, batch, flat, tolerance: float) -> Outcomes:
         plans = plan_structs(msq, [k] * batch.count)
         start, end = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         start.record()
-        _, res = ctx.solve_batched(flat, batch, plans, tolerance, out=out)
+        _, res = ctx.solve_batched(flat, batch, plans, 1e30, out=out)
         end.record()
         torch.cuda.synchronize()
         secs[k] = start.elapsed_time(end) / 1e3
-        acc[:, k] = [r.accepted for r in res]
+        acc[:, k] = [r.plan_residual <= tolerance for r in res]
     return Outcomes(acc, secs)
 
 

@@ -1,15 +1,20 @@
 """Train the plan selector on the GPU and save its weights.
 
-  python mixed-mlx_gb300/train_selector.py --train 4096 --test 1024 \
-      --out mixed-mlx_gb300/selector_weights.npz
+  python mixed-mlx_gb300/train_selector.py --out mixed-mlx_gb300/selector_weights.npz
 
 Training data: SPD matrices of three spectrum families (log-uniform,
-clustered, power law), n log-uniform in [--n-lo, --n-hi] (default [32, 512]),
-condition log-uniform in [1e1, 1e8]; every plan is run on every matrix by msq_solve_batched and
-scored by its own float-float residual at the tolerance.  The network is
-trained by the library's CUDA kernels (msq_mlp_backward / msq_mlp_step).
-Prints accept rate, fallback rate and solves/s on held-out seeds for the
-selector and for the FP32 path alone.
+clustered, power law i^-2), n log-uniform in [--n-lo, --n-hi] (default
+[64, 2048]), condition log-uniform in [1e1, 1e8], plus --wishart Wishart
+covariances (n log-uniform in [16, 512], the batched workload's family);
+every plan is run on every
+matrix by msq_solve_batched and scored by its own float-float residual at the
+tolerance.  Orders up to 1024 are solved in batches of 1024; each order above
+1024 takes the whole GPU (grid eigensolver), so of those only the first
+--max-large drawn are run (the count is recorded).  The network is trained by
+the library's CUDA kernels (msq_mlp_backward / msq_mlp_step).  Then held-out
+seeds (--test, drawn the same way) are solved with the selected plans and
+with the FP32 path alone; accept rate, fallback rate, met-tolerance rate and
+solves/s are printed as JSON and stored with the weights.
 """
 from __future__ import annotations
 
@@ -18,33 +23,68 @@ import importlib
 import json
 import os
 import sys
+import time
 
 import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, os.path.dirname(HERE))
 
+BATCHED_MAX = 1024  # orders the batched eigensolver takes
+
+
+def draw_orders(count: int, seed: int, n_lo: int, n_hi: int, max_large: int):
+    """Orders log-uniform on [n_lo, n_hi]; the ones above BATCHED_MAX beyond
+    the first max_large are dropped.  Returns (small, large, drawn_large)."""
+    rng = np.random.default_rng(seed)
+    n = np.floor(np.exp(rng.uniform(np.log(n_lo), np.log(n_hi + 1), count))).astype(np.int32)
+    n = np.clip(n, n_lo, n_hi)
+    small, large = n[n <= BATCHED_MAX], n[n > BATCHED_MAX]
+    return small, large[:max_large], int(large.size)
+
+
+def chunks(orders, size: int):
+    for s in range(0, len(orders), size):
+        yield s, orders[s:s + size]
+
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--train", type=int, default=4096)
-    ap.add_argument("--test", type=int, default=1024)
+    ap.add_argument("--train", type=int, default=12288)
+    ap.add_argument("--test", type=int, default=20480)
     ap.add_argument("--tol", type=float, default=1e-5)
     ap.add_argument("--epochs", type=int, default=150)
     ap.add_argument("--threshold", type=float, default=0.9)
-    ap.add_argument("--n-lo", type=int, default=32)
-    ap.add_argument("--n-hi", type=int, default=512)
+    ap.add_argument("--n-lo", type=int, default=64)
+    ap.add_argument("--n-hi", type=int, default=2048)
+    ap.add_argument("--max-large", type=int, default=128,
+                    help="orders above 1024 run per set (each takes the whole GPU)")
+    ap.add_argument("--wishart", type=int, default=4096,
+                    help="Wishart covariances (n in [16, 512]) added to the training set")
     ap.add_argument("--out", default=os.path.join(HERE, "selector_weights.npz"))
     args = ap.parse_args()
     import torch
     msq = importlib.import_module("mixed-mlx_gb300")
     sel = importlib.import_module("mixed-mlx_gb300.selector")
     ctx = msq.Context(0)
+    t_start = time.time()
 
+    small, large, drawn_large = draw_orders(args.train, 1000, args.n_lo, args.n_hi, args.max_large)
     chunks_f, chunks_y, secs = [], [], np.zeros(len(sel.PLANS))
-    for c, start in enumerate(range(0, args.train, 1024)):
-        count = min(1024, args.train - start)
-        orders, mats = sel.generate(torch, count, seed=1000 + c, n_lo=args.n_lo, n_hi=args.n_hi)
+    for part, size in ((small, 1024), (large, 16)):
+        for c, (start, orders) in enumerate(chunks(part, size)):
+            if len(orders) == 0:
+                continue
+            seed = 10_000 * (1 + (part is large)) + c
+            _, mats = sel.generate(torch, len(orders), seed=seed, orders=orders)
+            batch, flat = sel.pack(msq, torch, orders, mats)
+            chunks_f.append(sel.features(ctx, torch, batch, flat, args.tol))
+            out = sel.score_plans(ctx, msq, torch, batch, flat, args.tol)
+            chunks_y.append(torch.from_numpy(out.accepted).cuda())
+            secs += out.seconds
+            del mats, flat
+    for c, start in enumerate(range(0, args.wishart, 1024)):
+        orders, mats = sel.generate_wishart(torch, min(1024, args.wishart - start), seed=30_000 + c)
         batch, flat = sel.pack(msq, torch, orders, mats)
         chunks_f.append(sel.features(ctx, torch, batch, flat, args.tol))
         out = sel.score_plans(ctx, msq, torch, batch, flat, args.tol)
@@ -56,34 +96,68 @@ def main():
     selector = sel.Selector(msq, torch, ctx, seed=0)
     selector.cost_order = [int(k) for k in np.argsort(secs)]
     losses = selector.fit(feats, targets, epochs=args.epochs)
+    t_train = time.time() - t_start
 
-    orders, mats = sel.generate(torch, args.test, seed=999_999, n_lo=args.n_lo, n_hi=args.n_hi)
-    batch, flat = sel.pack(msq, torch, orders, mats)
-    feats_t = sel.features(ctx, torch, batch, flat, args.tol)
-    choice = selector.choose(feats_t, args.threshold)
-    plans = [msq.plan(msq.PLAN_FP32, 1, 1e-7, 15) if k < 0 else sel.plan_structs(msq, [int(k)])[0]
-             for k in choice]
-    fp32 = [msq.plan(msq.PLAN_FP32, 1, 1e-7, 15)] * batch.count
-    report = {}
-    for name, p in (("selector", plans), ("fp32_path", fp32)):
-        outb = torch.empty_like(flat)
-        ctx.solve_batched(flat, batch, p, args.tol, out=outb)
-        s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        s.record()
-        _, res = ctx.solve_batched(flat, batch, p, args.tol, out=outb)
-        e.record()
-        torch.cuda.synchronize()
-        ms = s.elapsed_time(e)
-        report[name] = {"ms": ms, "solves_per_s": batch.count / (ms / 1e3),
-                        "accept_rate": float(np.mean([r.accepted for r in res])),
-                        "fallback_rate": float(np.mean([r.fallback for r in res])),
-                        "met_tolerance": float(np.mean([r.final_residual <= args.tol for r in res]))}
-    report["plan_histogram"] = {str(k): int(np.sum(choice == k)) for k in range(-1, len(sel.PLANS))}
-    report["train_loss_first_last"] = [losses[0], losses[-1]]
-    report["plan_seconds_on_training_set"] = secs.tolist()
+    # held-out seeds: selected plans against the FP32 path alone
+    small_t, large_t, drawn_large_t = draw_orders(args.test, 999_999, args.n_lo, args.n_hi,
+                                                  args.max_large // 2)
+    totals = {name: {"ms": 0.0, "met": 0, "accepted": 0, "fallback": 0, "count": 0}
+              for name in ("selector", "fp32_path")}
+    hist = np.zeros(len(sel.PLANS) + 1, dtype=np.int64)
+    for part, size in ((small_t, 1024), (large_t, 16)):
+        for c, (start, orders) in enumerate(chunks(part, size)):
+            if len(orders) == 0:
+                continue
+            seed = 500_000 + 1000 * (part is large_t) + c
+            _, mats = sel.generate(torch, len(orders), seed=seed, orders=orders)
+            batch, flat = sel.pack(msq, torch, orders, mats)
+            del mats
+            choice = selector.choose(sel.features(ctx, torch, batch, flat, args.tol),
+                                     args.threshold)
+            hist += np.bincount(choice + 1, minlength=len(sel.PLANS) + 1)
+            plans = [msq.plan(msq.PLAN_FP32, 1, 1e-7, 15) if k < 0 else
+                     sel.plan_structs(msq, [int(k)])[0] for k in choice]
+            fp32 = [msq.plan(msq.PLAN_FP32, 1, 1e-7, 15)] * batch.count
+            for name, p in (("selector", plans), ("fp32_path", fp32)):
+                outb = torch.empty_like(flat)
+                ctx.solve_batched(flat, batch, p, args.tol, out=outb)  # plan caches, graphs
+                s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                s.record()
+                _, res = ctx.solve_batched(flat, batch, p, args.tol, out=outb)
+                e.record()
+                torch.cuda.synchronize()
+                t = totals[name]
+                t["ms"] += s.elapsed_time(e)
+                t["met"] += sum(r.final_residual <= args.tol for r in res)
+                t["accepted"] += sum(r.accepted for r in res)
+                t["fallback"] += sum(r.fallback for r in res)
+                t["count"] += batch.count
+            del flat
+    report = {"train": {"matrices": int(small.size + large.size), "drawn": args.train,
+                        "wishart": args.wishart, "wishart_n": [16, 512],
+                        "above_1024_drawn": drawn_large, "above_1024_run": int(large.size),
+                        "n": [args.n_lo, args.n_hi], "cond": [1e1, 1e8],
+                        "families": ["log-uniform", "clustered", "power law i^-2"],
+                        "loss_first_last": [losses[0], losses[-1]],
+                        "plan_seconds": secs.tolist(), "seconds": t_train},
+              "held_out": {"matrices": int(small_t.size + large_t.size), "drawn": args.test,
+                           "above_1024_drawn": drawn_large_t, "above_1024_run": int(large_t.size),
+                           "tolerance": args.tol, "threshold": args.threshold,
+                           "plan_histogram": {("fp32+1" if k < 0 else
+                                               "%s+%d" % (("bf16", "fp8", "mxfp4")[sel.PLANS[k][0] - 1],
+                                                          sel.PLANS[k][1])): int(hist[k + 1])
+                                              for k in range(-1, len(sel.PLANS))}}}
+    for name, t in totals.items():
+        report["held_out"][name] = {
+            "solves_per_s": t["met"] / (t["ms"] / 1e3), "ms": t["ms"],
+            "accept_rate": t["accepted"] / t["count"], "fallback_rate": t["fallback"] / t["count"],
+            "met_tolerance": t["met"] / t["count"]}
+    report["held_out"]["speedup_vs_fp32_path"] = (report["held_out"]["selector"]["solves_per_s"] /
+                                                  report["held_out"]["fp32_path"]["solves_per_s"])
     np.savez(args.out, params=selector.params.cpu().numpy(), mean=selector.mean.cpu().numpy(),
              std=selector.std.cpu().numpy(), cost_order=np.array(selector.cost_order),
-             tol=np.array([args.tol]), threshold=np.array([args.threshold]))
+             tol=np.array([args.tol]), threshold=np.array([args.threshold]),
+             metadata=np.array(json.dumps(report)))
     print(json.dumps(report))
 
 

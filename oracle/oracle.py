@@ -356,6 +356,136 @@ def controlled(n: int, cond: float) -> np.ndarray:
     return (v * lam) @ v.T
 
 
+# ---------------------------------------- stage-3 precision plans (restated)
+
+# FactorFormat (3_spectral/spectral.hpp) -> codec id of encode/decode; FP16
+# is numpy's IEEE binary16 (round to nearest even).
+SPECTRAL_FORMATS = {"fp32": None, "fp16": "fp16", "bf16": 1, "fp8_e4m3": 2, "fp8_e5m2": 3,
+                    "mxfp8_e4m3": 4, "mxfp4_e2m1": 7}
+# precision_plans() (3_spectral/spectral.cpp:769-786)
+SPECTRAL_PLANS = [("fp32_baseline", "fp32", "fp32"), ("spectrum_fp16", "fp32", "fp16"),
+                  ("spectrum_bf16", "fp32", "bf16"), ("spectrum_e4m3", "fp32", "fp8_e4m3"),
+                  ("spectrum_e5m2", "fp32", "fp8_e5m2"), ("spectrum_mxfp8", "fp32", "mxfp8_e4m3"),
+                  ("spectrum_mxfp4", "fp32", "mxfp4_e2m1"), ("basis_fp16", "fp16", "fp32"),
+                  ("basis_bf16", "bf16", "fp32"), ("basis_e4m3", "fp8_e4m3", "fp32"),
+                  ("basis_e5m2", "fp8_e5m2", "fp32"), ("basis_mxfp8", "mxfp8_e4m3", "fp32"),
+                  ("basis_mxfp4", "mxfp4_e2m1", "fp32"), ("fp16_mxfp8", "fp16", "mxfp8_e4m3"),
+                  ("bf16_mxfp8", "bf16", "mxfp8_e4m3"), ("e4m3_mxfp4", "fp8_e4m3", "mxfp4_e2m1")]
+
+
+def _spectral_quantize(fmt: str, x: np.ndarray) -> np.ndarray:
+    """Nearest quantize + decode of a flat FP32 array (column-major order)."""
+    x = np.ascontiguousarray(x, np.float32).reshape(-1)
+    if fmt == "fp32":
+        return x.copy()
+    if fmt == "fp16":
+        return x.astype(np.float16).astype(np.float32)
+    codec = SPECTRAL_FORMATS[fmt]
+    vals, scl = encode(codec, x)
+    return decode(codec, vals, scl, x.size)
+
+
+def spectral_plan(a: np.ndarray, basis_fmt: str, spectrum_fmt: str, condition: float,
+                  max_corrections: int = 30, tol: float = 1e-12, reference=None) -> dict:
+    """run_spectral (3_spectral/spectral.cpp:787-1385) restated with FP64
+    products on the same operands: FP32 eigenbasis (the blocked Jacobi the
+    CUDA solver runs, bit for bit), root spectrum sqrt(lambda); basis and
+    spectrum quantized; Vinv = Q(V)^T, or for an FP16 basis the FP16 image of
+    the FP32 basis's inverse (invert_basis :600-637, rejected at 1-norm
+    condition >= 1e4); X0 = (Q(V) diag(Q(s))) Vinv; corrections
+    E = V ((Vinv R V) o H) Vinv, H_ij = 1/(s_i + s_j), with every operand
+    re-quantized to the basis format while a low-bit basis (E4M3, E5M2,
+    MXFP8, MXFP4) of a matrix below condition 1000 is above residual 1e-3
+    and has not stalled twice (no 2x drop); stop at tol, the budget, or
+    divergence (residual >= max(1, 1e4 initial))."""
+    n = a.shape[0]
+    a64 = np.asarray(a, np.float64)
+    a32 = a64.astype(np.float32)
+    w, v, _, _ = jacobi_blocked(a32.astype(np.float64), 1e-7, 20)
+    if not np.all(w > 0):
+        raise ValueError("The FP32 factor has an invalid spectrum.")
+    s = np.sqrt(w.astype(np.float32))
+    out = {"accepted": False, "reason": "", "basis_condition": float("nan")}
+    fp16_basis = basis_fmt == "fp16"
+    low = basis_fmt in ("fp8_e4m3", "fp8_e5m2", "mxfp8_e4m3", "mxfp4_e2m1") and condition < 1000.0
+    v32 = np.asarray(v, np.float32)
+    inverse = None
+    if fp16_basis:
+        vd = v32.astype(np.float64)
+        inverse = np.linalg.inv(vd)
+        cond = np.abs(vd).sum(0).max() * np.abs(inverse).sum(0).max()
+        out["basis_condition"] = float(cond)
+        if not cond < 1e4:
+            out["reason"] = "ill_conditioned_basis"
+            return out
+    else:
+        out["basis_condition"] = 1.0
+    vq = _spectral_quantize(basis_fmt, v32.reshape(-1, order="F")).reshape(n, n, order="F")
+    sq = _spectral_quantize(spectrum_fmt, s)
+    out["basis_error"] = float(np.linalg.norm(vq.astype(np.float64) - v32) / np.linalg.norm(v32.astype(np.float64)))
+    out["spectrum_error"] = float(np.linalg.norm(sq.astype(np.float64) - s) / np.linalg.norm(s.astype(np.float64)))
+    if not (np.all(sq > 0) and np.all(np.isfinite(sq))):
+        out["reason"] = "invalid_spectrum"
+        return out
+    if fp16_basis:
+        vinv = inverse.astype(np.float32).astype(np.float16).astype(np.float32)
+        if not np.all(np.isfinite(vinv)):
+            out["reason"] = "ill_conditioned_basis"
+            return out
+    else:
+        vinv = vq.T.copy()
+    out["accepted"] = True
+
+    def q(x):  # an operand re-encoded to the basis format (flat column-major)
+        return _spectral_quantize(basis_fmt, np.asarray(x, np.float32).reshape(-1, order="F")
+                                  ).reshape(n, n, order="F").astype(np.float64)
+
+    vs = (vq * sq[None, :]).astype(np.float32)
+    vs_op = q(vs) if low else (vs.astype(np.float16).astype(np.float64) if fp16_basis
+                               else vs.astype(np.float64))
+    vinv_op = q(vinv) if low else vinv.astype(np.float64)
+    V, Vinv = vq.astype(np.float64), vinv.astype(np.float64)
+    H = 1.0 / (sq.astype(np.float64)[:, None] + sq.astype(np.float64)[None, :])
+    x = vs_op @ vinv_op
+    norm_a = np.linalg.norm(a64)
+
+    def residual(x):
+        r = a64 - x @ x
+        return r, float(np.linalg.norm(r) / norm_a)
+
+    r, measured = residual(x)
+    history = [measured]
+    limit = max(1.0, 1e4 * measured)
+    low_on, low_prev, stalls, low_count = True, measured, 0, 0
+    it = 0
+    while measured > tol and it < max_corrections and measured < limit:
+        use_low = low and low_on and measured > 1e-3
+        if use_low:
+            wk = q(vinv_op @ q(r))
+            c = q((wk @ V) * H)
+            e = q(V @ c) @ vinv_op
+            low_count += 1
+        else:
+            c = ((Vinv @ r) @ V) * H
+            e = (V @ c) @ Vinv
+        x = x + e
+        r, measured = residual(x)
+        history.append(measured)
+        it += 1
+        if low and low_on and measured > tol:
+            stalls = stalls + 1 if measured > low_prev * 0.5 else 0
+            low_prev = measured
+            low_on = stalls < 2
+    out.update(iterations=it, residuals=history, final_residual=history[-1],
+               low_product_corrections=low_count, converged=history[-1] <= tol)
+    out["reason"] = ("converged" if history[-1] <= tol else "nonfinite_residual"
+                     if not np.isfinite(history[-1]) else "divergent" if history[-1] >= limit
+                     else "correction_limit")
+    if reference is not None:
+        out["final_error"] = relative_error(x, reference)
+    return out
+
+
 # ------------------------------------------------- CPU plain method (port)
 
 def plain_method(a: np.ndarray, max_corrections: int = 12, tol: float = 1e-12):

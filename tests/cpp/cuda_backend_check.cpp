@@ -1,7 +1,9 @@
 // Drives the C++ host mirror (runCudaCase) on one matrix, the way the
 // reference's CLI drives runMetalCase.  Input file: int32 n, n*n FP64 A
 // (column-major), optionally n*n FP64 reference root.  Prints key=value.
-// Usage: cuda_backend_check <matrix.bin> <basis: fp32|bf16|fp8_e4m3fn_rowscale|mxfp4_e2m1>
+// Usage: cuda_backend_check <matrix.bin> spectral <plan> <tolerance> <max_corrections> [condition]
+//        (a stage-3 precision plan through runCudaSpectral), or
+//        cuda_backend_check <matrix.bin> <basis: fp32|bf16|fp8_e4m3fn_rowscale|mxfp4_e2m1|...>
 //                           <tolerance> <max_iterations>
 //                           [spectrum: fp32|fp8_e4m3fn_log_s|fp4_e2m1_log_s]
 //                           [rounding: nearest|stochastic] [rounding seed]
@@ -38,6 +40,39 @@ int main(int argc, char **argv) {
     const bool have_ref = std::fread(ref.data(), sizeof(double), ref.size(), f) == ref.size();
     std::fclose(f);
     mixed_sqrt::CudaRuntime runtime(0);
+    if (std::string(argv[2]) == "spectral") {
+      // cuda_backend_check <matrix.bin> spectral <plan> <tolerance> <max_corrections> <condition>
+      mixed_sqrt::CudaProblem problem;
+      problem.order = m.order;
+      problem.condition = argc > 6 ? std::atof(argv[6]) : 0.0;
+      problem.prepared_matrix = &m;
+      problem.supplied_reference = have_ref ? &ref : nullptr;
+      const std::string name = argv[3];
+      for (const auto &plan : mixed_sqrt::cudaPrecisionPlans()) {
+        if (plan.name != name) continue;
+        const auto r = mixed_sqrt::runCudaSpectral(runtime, problem, plan,
+                                                   static_cast<size_t>(std::atoi(argv[5])),
+                                                   std::atof(argv[4]));
+        std::cout << std::setprecision(17) << "plan=" << r.plan << " accepted=" << r.accepted
+                  << " converged=" << r.converged << " reason=" << r.reason
+                  << " iterations=" << r.iterations
+                  << " low_product_corrections=" << r.low_product_corrections
+                  << " product_backend=" << r.product_backend
+                  << " basis_error=" << r.basis_relative_error
+                  << " spectrum_error=" << r.spectrum_relative_error
+                  << " basis_condition=" << r.basis_condition
+                  << " basis_bits=" << r.basis_bits_per_value
+                  << " spectrum_bits=" << r.spectrum_bits_per_value
+                  << " weighted_bits=" << r.weighted_factor_storage_bits
+                  << " initial_error=" << r.initial_error << " final_error=" << r.final_error
+                  << " final_residual=" << r.final_residual << " residuals=";
+        for (size_t k = 0; k < r.history.size(); ++k)
+          std::cout << (k ? "," : "") << r.history[k].residual;
+        std::cout << "\n";
+        return 0;
+      }
+      throw std::runtime_error("unknown plan " + name);
+    }
     mixed_sqrt::CudaSolverConfiguration config;
     config.basis_format = mixed_sqrt::cudaBasisFormatForCliName(argv[2]);
     // optional: spectrum precision, rounding mode, rounding seed

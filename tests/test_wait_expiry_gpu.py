@@ -39,7 +39,9 @@ def _batch(msq, orders, seed=0):
     # the two-level order (257..512) has pairs that share a super-tile, so
     # quads wait on each other's flags; the round-robin shared-tile classes
     # reload their tiles by TMA between sweeps
-    (1, [300, 400, 512]),     # MSQ_VECTORS_BLOCKED: two-level, FP32 replay
+    # MSQ_VECTORS_BLOCKED: two-level order, FP32 replay; more than eight
+    # orders above 256, so the batched kernels (not the grid path) take them
+    (1, [300, 400, 512] * 4),
     (0, [64, 128, 200, 256]),  # MSQ_VECTORS_REPLAY: round-robin
 ])
 def test_jacobi_wait_expiry_is_reported(msq, ctx, injection, mode, orders):
