@@ -338,42 +338,32 @@ def run_codec(args):
     print(json.dumps(line), flush=True)
 
 
-def run_selector(args):
+def selector_eval(msq, torch, ctx, count: int, steps: int = 1, warmup: int = 2):
     """Learned plan selection on held-out seeds: SPD matrices of the three
     spectrum families, n log-uniform in [64, 1024], condition log-uniform in
     [1e1, 1e8]; each matrix gets the cheapest plan the MLP predicts to meet
     1e-5 (FP32 fallback on a miss); compared with every matrix on the plain
-    FP32 path."""
-    import torch
-    msq = importlib.import_module("mixed-mlx_gb300")
+    FP32 path (device time of one call after the warm-ups that build the
+    plan caches and the solve graph)."""
     sel = importlib.import_module("mixed-mlx_gb300.selector")
     weights = os.path.join(ROOT, "mixed-mlx_gb300", "selector_weights.npz")
     if not os.path.exists(weights):
-        print(json.dumps({"metric": "selector", "unavailable": "no trained selector weights"}))
-        return
-    ctx = msq.Context(0)
-    w = np.load(weights)
-    selector = sel.Selector(msq, torch, ctx)
-    selector.params = torch.from_numpy(w["params"]).cuda()
-    selector.mean = torch.from_numpy(w["mean"]).cuda()
-    selector.std = torch.from_numpy(w["std"]).cuda()
-    selector.cost_order = [int(k) for k in w["cost_order"]]
-    count = args.count if args.count != COUNT else 2048
+        return None
+    selector, threshold, meta = sel.load(msq, torch, ctx, weights)
     orders, mats = sel.generate(torch, count, seed=777_777, n_lo=64, n_hi=1024)
     batch, flat = sel.pack(msq, torch, orders, mats)
     del mats
-    choice = selector.choose(sel.features(ctx, torch, batch, flat, TOL), float(w["threshold"][0]))
+    choice = selector.choose(sel.features(ctx, torch, batch, flat, TOL), threshold)
     plans = [msq.plan(msq.PLAN_FP32, 1, 1e-7, 15) if k < 0 else sel.plan_structs(msq, [int(k)])[0]
              for k in choice]
     fp32 = [msq.plan(msq.PLAN_FP32, 1, 1e-7, 15)] * batch.count
     out = torch.empty_like(flat)
 
     def timed(p):
-        for _ in range(max(1, args.warmup)):
+        for _ in range(max(2, warmup)):  # caches, then the solve's graph capture
             ctx.solve_batched(flat, batch, p, TOL, out=out)
         torch.cuda.synchronize()
         s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        steps = max(1, args.steps // 2)
         s.record()
         for _ in range(steps):
             _, res = ctx.solve_batched(flat, batch, p, TOL, out=out)
@@ -386,21 +376,35 @@ def run_selector(args):
     met = lambda res: sum(r.final_residual <= TOL for r in res)
     hist = {("fp32+1" if k < 0 else "%s+%d" % (("bf16", "fp8", "mxfp4")[sel.PLANS[k][0] - 1], sel.PLANS[k][1])):
             int(np.sum(choice == k)) for k in sorted(set(choice.tolist()))}
+    return {"matrices": batch.count, "ms": ms_sel,
+            "solves_s": met(res_sel) / (ms_sel / 1e3),
+            "fp32_path": {"solves_s": met(res_fp32) / (ms_fp32 / 1e3), "ms": ms_fp32},
+            "speedup_vs_fp32_path": (met(res_sel) / ms_sel) / max(met(res_fp32) / ms_fp32, 1e-30),
+            "accept_rate": float(np.mean([r.accepted for r in res_sel])),
+            "fallback_rate": float(np.mean([r.fallback for r in res_sel])),
+            "met_tolerance": float(met(res_sel)) / batch.count,
+            "plan_histogram": hist,
+            "training": meta.get("train"), "held_out_at_training": meta.get("held_out")}
+
+
+def run_selector(args):
+    import torch
+    msq = importlib.import_module("mixed-mlx_gb300")
+    ctx = msq.Context(0)
+    count = args.count if args.count != COUNT else 2048
+    r = selector_eval(msq, torch, ctx, count, max(1, args.steps // 2), args.warmup)
+    if r is None:
+        print(json.dumps({"metric": "selector", "unavailable": "no trained selector weights"}))
+        return
     print(json.dumps({
         "metric": "SPD sqrt solves/s at rel. residual <=1e-5 with learned plan selection (held-out seeds)",
-        "value": met(res_sel) / (ms_sel / 1e3), "unit": "solves/s", "n_gpus": 1,
-        "steps": max(1, args.steps // 2), "warmup": max(1, args.warmup), "ms_per_step": ms_sel,
+        "value": r["solves_s"], "unit": "solves/s", "n_gpus": 1,
+        "steps": max(1, args.steps // 2), "warmup": max(2, args.warmup), "ms_per_step": r["ms"],
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "bf16",
         "data": "synthetic (seeded Gaussian-QR spectra: log-uniform, clustered, power law)",
-        "config": {"workload": f"{batch.count} held-out SPD, n log-uniform [64,1024], cond [1e1,1e8], tol 1e-5",
+        "config": {"workload": f"{count} held-out SPD, n log-uniform [64,1024], cond [1e1,1e8], tol 1e-5",
                    "selector": "MLP 16-64-64-8, trained by the library's CUDA kernels"},
-        "fp32_path": {"value": met(res_fp32) / (ms_fp32 / 1e3), "ms_per_step": ms_fp32},
-        "speedup_vs_fp32_path": (met(res_sel) / ms_sel) / max(met(res_fp32) / ms_fp32, 1e-30),
-        "accept_rate": float(np.mean([r.accepted for r in res_sel])),
-        "fallback_rate": float(np.mean([r.fallback for r in res_sel])),
-        "met_tolerance": float(met(res_sel)) / batch.count,
-        "plan_histogram": hist,
-    }), flush=True)
+        **{k: v for k, v in r.items() if k not in ("ms", "solves_s")}}), flush=True)
 
 
 def _spd_gpu(torch, lam, seed, device):
@@ -497,6 +501,58 @@ def c2_table(msq, torch, ctx, cases=C2_ALL) -> list:
         del a32, a64, root, a, out
         torch.cuda.empty_cache()
     return rows
+
+
+def c1_entry(msq, torch, ctx) -> dict:
+    """The plain method on one matrix: n = 256, A = Q diag(lambda) Q^T with Q
+    from QR of a seeded N(0,1) matrix and lambda log-uniform on [1e-3, 1]
+    (condition 1e3), FP32 input; Jacobi to off-norm 1e-7 ||A||_F, FP32
+    reconstruction, no correction (plan FP32 + 0).  Device time of one solve
+    after warm-ups (latency) and of 1024 such matrices (different seeds) in
+    one call (throughput); FP64 residual and forward error of the single
+    solve against dsyevd of the FP32-rounded matrix."""
+    n, cond = 256, 1e3
+
+    def matrix(seed):
+        g = torch.Generator(device="cuda").manual_seed(seed)
+        lam = torch.exp(torch.empty(n, dtype=torch.float64, device="cuda").uniform_(
+            float(np.log(1.0 / cond)), 0.0, generator=g))
+        lam[0], lam[-1] = 1.0, 1.0 / cond
+        return _spd_gpu(torch, lam, seed, "cuda")
+
+    a32, a64 = matrix(257)
+    w, v = torch.linalg.eigh(a64)
+    root = (v * torch.sqrt(w)) @ v.T
+    batch = msq.Batch.from_orders([n])
+    a = a32.T.contiguous().reshape(-1)
+    out = torch.empty_like(a)
+    plan = msq.plan(msq.PLAN_FP32, 0, 1e-7, 20)
+    for _ in range(2):
+        ctx.solve_batched(a, batch, [plan], 1.0, out=out)
+    ms, r = _time_solve(torch, ctx, a, batch, plan, out, reps=5)
+    resid, err = _fp64_errors(torch, a64, out.view(n, n).T, root)
+    count = 1024
+    flat = torch.cat([matrix(10_000 + i)[0].T.contiguous().reshape(-1) for i in range(count)])
+    big = msq.Batch.from_orders([n] * count)
+    outb = torch.empty_like(flat)
+    plans = [plan] * count
+    for _ in range(3):
+        ctx.solve_batched(flat, big, plans, TOL, out=outb)
+    torch.cuda.synchronize()
+    s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    s.record()
+    _, res = ctx.solve_batched(flat, big, plans, TOL, out=outb)
+    e.record()
+    torch.cuda.synchronize()
+    ms_b = s.elapsed_time(e)
+    met = sum(x.final_residual <= TOL for x in res)
+    sweeps = float(np.mean([x.jacobi_sweeps for x in res]))
+    return {"n": n, "cond": cond, "plan": "FP32: Jacobi to 1e-7, FP32 reconstruction",
+            "latency_ms": round(ms, 3), "jacobi_sweeps": r.jacobi_sweeps,
+            "residual_fp64": resid, "error_fp64": err,
+            "batch": {"matrices": count, "ms": round(ms_b, 2), "solves_s": met / (ms_b / 1e3),
+                      "met_tolerance": int(met),
+                      "tflops": count * (6.0 * n ** 3 * sweeps + 4.0 * n ** 3) / (ms_b / 1e3) / 1e12}}
 
 
 def c3_entry(msq, torch, ctx, warm: bool = False) -> dict:
@@ -633,8 +689,9 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-c2", action="store_true",
                     help="skip the single-matrix grid and the n=8192 MXFP4 legs of the line")
-    ap.add_argument("--selector", type=int, default=0,
-                    help="batched workload: plans from the trained selector instead of BF16 + sweeps")
+    ap.add_argument("--selector", type=int, default=1,
+                    help="batched workload: plans from the trained selector (default); 0: the "
+                         "fixed BF16 plan with --sweeps corrections and --jacobi-tol")
     ap.add_argument("--workload", default="batched", choices=["batched", "codec", "selector", "c2", "mxf4"],
                     help="codec: MXFP4 round trip of 2^26 N(0,1) values; selector: learned plan "
                          "selection on held-out matrices (secondary lines)")
@@ -673,13 +730,8 @@ def main():
         # learned plan selection: features + MLP forward on the GPU (outside
         # the timed region, like the plan choice of a serving loop)
         sel = importlib.import_module("mixed-mlx_gb300.selector")
-        w = np.load(weights)
-        selector = sel.Selector(msq, torch, ctx)
-        selector.params = torch.from_numpy(w["params"]).cuda()
-        selector.mean = torch.from_numpy(w["mean"]).cuda()
-        selector.std = torch.from_numpy(w["std"]).cuda()
-        selector.cost_order = [int(k) for k in w["cost_order"]]
-        choice = selector.choose(sel.features(ctx, torch, batch, a, TOL), float(w["threshold"][0]))
+        selector, threshold, _ = sel.load(msq, torch, ctx, weights)
+        choice = selector.choose(sel.features(ctx, torch, batch, a, TOL), threshold)
         low_plan = [msq.plan(msq.PLAN_FP32, 1, 1e-7, 15) if k < 0 else
                     sel.plan_structs(msq, [int(k)])[0] for k in choice]
         plan_source = "learned selector (" + ", ".join(
@@ -745,11 +797,13 @@ def main():
     ev_in = [torch.cuda.Event(), torch.cuda.Event()]
     ev_solved = [torch.cuda.Event(), torch.cuda.Event()]
     ev_out = [None, None]  # D2H of the buffer's previous step done
-    # untimed warm-up: one solve per buffer pair (launch graphs are captured
-    # per set of buffers, so both pairs' graphs exist before the clock starts)
+    # untimed warm-up: two solves per buffer pair (launch graphs are captured
+    # per set of buffers on the second call, so both pairs' graphs exist
+    # before the clock starts)
     for k in range(2):
         dev_in[k].copy_(host_in, non_blocking=True)
-        ctx.solve_batched(dev_in[k], batch, low_plan, TOL, out=dev_out[k])
+        for _ in range(2):
+            ctx.solve_batched(dev_in[k], batch, low_plan, TOL, out=dev_out[k])
     torch.cuda.synchronize(device)
     barrier()
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
@@ -811,8 +865,10 @@ def main():
     # returned (FP32-rounded) root is above it
     miscounted = int(np.sum((reported <= TOL) & (resid_all > TOL * (1 + 1e-2) + 1e-7)))
     # the single-matrix grid and the order-8192 MXFP4 case (untimed legs)
-    c2 = c3 = None
+    c1 = c2 = c3 = None
+    selector_key = selector_eval(msq, torch, ctx, 1024) if not args.no_c2 else None
     if not args.no_c2:
+        c1 = c1_entry(msq, torch, ctx)
         c2 = c2_table(msq, torch, ctx, C2_DEFAULT)
         c3 = c3_entry(msq, torch, ctx)
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
@@ -910,7 +966,7 @@ def main():
                           "residual_checked": int(resid_all.size),
                           "met_tolerance_fp64": int(np.sum(resid_all <= TOL * (1 + 1e-2) + 1e-7)),
                           "counted_but_missed": miscounted},
-        "c2": c2, "c3": c3,
+        "c1": c1, "c2": c2, "c3": c3, "selector": selector_key,
         "kernels": {k: {"launches": v[0], "ms": v[1], "share": v[1] / total_ms} for k, v in rows.items()},
         "kernels_source": "launch timer over one extra step with concurrency off (serial)",
         "autotune": [l for l in ctx.autotune_report().splitlines() if l],

@@ -196,7 +196,7 @@ const DeviceBatch *prepareBatch(msq_ctx *ctx, const int32_t *n,
     delete b;
     return nullptr;
   }
-  if (ctx->batches.size() >= 8) {
+  if (ctx->batches.size() >= 32) {
     DeviceBatch *old = ctx->batches.front();
     for (auto &w : old->work_cache) cudaFree(w.work);
     cudaFree(old->offset);

@@ -70,7 +70,7 @@ void destroyTcPlans(TcPlanCache *cache);
 // A captured batched-Jacobi launch sequence and what it was captured for.
 struct JacobiGraphKey {
   uint64_t plan_serial, batch_key;
-  const void *batch, *a, *v, *w, *sweeps, *off, *work;
+  const void *batch, *a, *v, *w, *sweeps, *off, *work, *tols;
   double tol;
   int max_sweeps;
   bool concurrent;
@@ -78,6 +78,7 @@ struct JacobiGraphKey {
   bool operator==(const JacobiGraphKey &o) const {
     return plan_serial == o.plan_serial && batch_key == o.batch_key && batch == o.batch && a == o.a &&
            v == o.v && w == o.w && sweeps == o.sweeps && off == o.off && work == o.work &&
+           tols == o.tols &&
            tol == o.tol && max_sweeps == o.max_sweeps && concurrent == o.concurrent &&
            shapes == o.shapes;
   }
@@ -101,7 +102,7 @@ struct msq_ctx {
   // one per user so nested stages never share memory.
   void *scratch[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};
   size_t scratch_bytes[5] = {0, 0, 0, 0, 0};
-  // Batch layouts cached by content hash (small: a few entries).
+  // Batch layouts cached by content hash (at most 32, oldest evicted).
   std::vector<msq::DeviceBatch *> batches;
   // Launch timing (msq_timing_begin/end).  Launches on the context stream
   // record one event after each launch (duration = gap to the previous

@@ -71,6 +71,7 @@ struct JacobiArgs {
   JacobiState *state;
   const int32_t *order;      // matrix ids of this launch, largest first
   double tol;
+  const double *tols;        // per matrix (null: tol for all)
   int max_sweeps;
   int first;                 // 1 on the first launch (load A, set norm)
   int parity;                // log buffer of this sweep (log points at it)
@@ -214,7 +215,7 @@ jacobiSweepKernel(JacobiArgs args) {
   const int sweeps = args.first ? 0 : s0.sweeps;
   const double ratio = norm2 > 0.0 ? sqrt(off2 / norm2) : 0.0;
 
-  if (ratio <= args.tol || sweeps >= args.max_sweeps) {
+  if (ratio <= (args.tols ? args.tols[mi] : args.tol) || sweeps >= args.max_sweeps) {
     // Eigenvalues = diagonal (jacobi_root_eigenvalues_f32 takes the sqrt
     // later, :1436-1444); full symmetric write-back of the matrix.
     float *eig = args.eigenvalues + args.eig_offset[mi];
@@ -1062,7 +1063,8 @@ bool jacobiCapturable(msq_ctx *ctx, const DeviceBatch *b, bool low_bit_basis) {
 
 int jacobiEnqueue(msq_ctx *ctx, const DeviceBatch *b, float *matrices, float *vectors,
                   float *eigenvalues, double tolerance, int max_sweeps, int32_t *sweeps_done,
-                  float *off_ratio, bool low_bit_basis) {
+                  float *off_ratio, bool low_bit_basis, const double *tols_device,
+                  const double *tols_host) {
   if (b->max_n > kMaxOrder) {
     return setError(ctx, MSQ_ERR_UNSUPPORTED, "jacobi: order above 16384 is not supported");
   }
@@ -1100,6 +1102,7 @@ int jacobiEnqueue(msq_ctx *ctx, const DeviceBatch *b, float *matrices, float *ve
   args.n = b->n;
   args.eigenvalues = eigenvalues;
   args.tol = tolerance;
+  args.tols = tols_device;
   args.max_sweeps = max_sweeps;
   args.status = ctx->d_status;
   args.sched = plan->sched;
@@ -1142,8 +1145,8 @@ int jacobiEnqueue(msq_ctx *ctx, const DeviceBatch *b, float *matrices, float *ve
   const bool graphable = !measuring && !ctx->timing && plan->grid_ids.empty() && ctx->graphs &&
                          waitTestMode() == kWaitTestOff && !ctx->capturing;
   const JacobiGraphKey key{plan->serial, b->key, b->offset, matrices, vectors, eigenvalues,
-                           sweeps_done, off_ratio, work, tolerance, max_sweeps, ctx->concurrent,
-                           shape_hash};
+                           sweeps_done, off_ratio, work, tols_device, tolerance, max_sweeps,
+                           ctx->concurrent, shape_hash};
   if (graphable) {
     for (auto &e : ctx->jacobi_graphs) {
       if (e.key == key) {
@@ -1237,8 +1240,8 @@ int jacobiEnqueue(msq_ctx *ctx, const DeviceBatch *b, float *matrices, float *ve
       cudaStream_t s = ss[plan->buckets.size() % sweep_streams];
       MSQ_TRY(twoLevelEnqueue(ctx, s, plan->tl, plan->tcv, matrices, b_scratch, diag,
                               images + parity * image_set, b->offset, b->n, b->eig_offset,
-                              eigenvalues, args.state, tolerance, max_sweeps, launch == 0,
-                              launch < max_sweeps, parity));
+                              eigenvalues, args.state, tolerance, tols_device, max_sweeps,
+                              launch == 0, launch < max_sweeps, parity));
     }
     if (launch < max_sweeps) {
       for (int i = 0; i < sweep_streams; ++i) MSQ_TRY(streamWait(ctx, rs, ss[i]));
@@ -1265,7 +1268,8 @@ int jacobiEnqueue(msq_ctx *ctx, const DeviceBatch *b, float *matrices, float *ve
     int sweeps = 0;
     double ratio = 0.0, norm2 = 0.0;
     MSQ_TRY(gridJacobiSolve(ctx, matrices + b->host_offset[gi], vectors + b->host_offset[gi],
-                            eigenvalues + b->host_eig_offset[gi], b->host_n[gi], tolerance, max_sweeps,
+                            eigenvalues + b->host_eig_offset[gi], b->host_n[gi],
+                            tols_host ? tols_host[gi] : tolerance, max_sweeps,
                             &sweeps, &ratio, &norm2));
     gridStateKernel<<<1, 1, 0, ctx->stream>>>(args.state + gi, sweeps, ratio, norm2);
     MSQ_TRY(launched(ctx, "jacobi grid state"));
@@ -1368,7 +1372,7 @@ extern "C" int msq_jacobi_batched(msq_ctx *ctx, float *matrices, float *vectors,
   const DeviceBatch *b = prepareBatch(ctx, n, offset, count);
   if (b == nullptr) return MSQ_ERR_INVALID_ARGUMENT;
   return jacobiEnqueue(ctx, b, matrices, vectors, eigenvalues, tolerance,
-                       max_sweeps, sweeps_done, off_ratio, false);
+                       max_sweeps, sweeps_done, off_ratio, false, nullptr, nullptr);
 }
 
 // ---------------------------------------------------------------------------

@@ -489,6 +489,7 @@ struct CheckArgs {
   JacobiState *state;
   const int32_t *ids;
   double tol;
+  const double *tols;  // per matrix (null: tol for all)
   int max_sweeps;
   int first;
   int parity;
@@ -534,7 +535,7 @@ __global__ void __launch_bounds__(256) tlCheckKernel(CheckArgs args) {
   const double norm2 = args.first ? off2 + diag2 : s0.norm2;
   const int sweeps = args.first ? 0 : s0.sweeps;
   const double ratio = norm2 > 0.0 ? sqrt(off2 / norm2) : 0.0;
-  const bool stop = ratio <= args.tol || sweeps >= args.max_sweeps;
+  const bool stop = ratio <= (args.tols ? args.tols[mi] : args.tol) || sweeps >= args.max_sweeps;
   if (stop) {
     float *eig = args.eigenvalues + args.eig_offset[mi];
     for (int k = threadIdx.x; k < n; k += blockDim.x) eig[k] = A[k + static_cast<int64_t>(k) * n];
@@ -1066,11 +1067,11 @@ int twoLevelEnqueue(msq_ctx *ctx, cudaStream_t stream, const TwoLevelDevice &t,
                     const TcVectorsDevice &v, float *matrices, float *b_scratch, float *diag,
                     uint8_t *images, const int64_t *a_offset, const int32_t *n,
                     const int64_t *eig_offset, float *eigenvalues, void *state, double tol,
-                    int max_sweeps, bool first, bool sweep, int parity) {
+                    const double *tols, int max_sweeps, bool first, bool sweep, int parity) {
   if (t.count == 0) return MSQ_OK;
   if (setAttributes() != MSQ_OK) return cudaCheck(ctx, cudaGetLastError(), "two-level attributes");
   auto *st = static_cast<JacobiState *>(state);
-  CheckArgs ca{matrices, a_offset, n, eig_offset, eigenvalues, st, t.ids, tol, max_sweeps,
+  CheckArgs ca{matrices, a_offset, n, eig_offset, eigenvalues, st, t.ids, tol, tols, max_sweeps,
                first ? 1 : 0, parity};
   launchBegin(ctx, stream);
   tlCheckKernel<<<t.count, 256, 0, stream>>>(ca);

@@ -76,7 +76,7 @@ int twoLevelEnqueue(msq_ctx *ctx, cudaStream_t stream, const TwoLevelDevice &t,
                     const TcVectorsDevice &v, float *matrices, float *b_scratch, float *diag,
                     uint8_t *images, const int64_t *a_offset, const int32_t *n,
                     const int64_t *eig_offset, float *eigenvalues, void *state, double tol,
-                    int max_sweeps, bool first, bool sweep, int parity);
+                    const double *tols, int max_sweeps, bool first, bool sweep, int parity);
 
 // Enqueues, on `stream`, the update V <- V Z_1 ... Z_S of one logged sweep
 // for the matrices of `d`: the stage rotations Z_s (64x64 blocks, from the

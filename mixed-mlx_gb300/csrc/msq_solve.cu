@@ -237,10 +237,28 @@ bool samePlan(const msq_plan &a, const msq_plan &b) {
          a.jacobi_tolerance == b.jacobi_tolerance && a.jacobi_max_sweeps == b.jacobi_max_sweeps;
 }
 
-// A plan group's buffers in the solver arena (compact layout: the group's
-// matrices back to back) and its batch.
-struct GroupBuffers {
-  const DeviceBatch *b = nullptr;
+// One Jacobi pass: the plan groups of a call run one batched Jacobi over
+// their union, gathered group by group into the solver arena, each matrix to
+// its own plan's tolerance (the largest budget of the groups); the
+// eigenvector mode may use the tensor cores only when every group quantizes
+// its basis.  Each group then runs its reconstruction, residuals and
+// corrections on its own part of the arena (a sub-batch at the pass's
+// offsets), so a call with several plans does not pay one eigensolver
+// launch sequence per plan.
+struct Pass {
+  double jacobi_tolerance;
+  int jacobi_max_sweeps;
+  bool low_bit;
+  std::vector<int> groups;      // indices into the call's groups
+  double *tols_host = nullptr;  // per member (pinned), when the tolerances differ
+};
+
+struct PassBuffers {
+  const DeviceBatch *b = nullptr;          // the pass (members group by group)
+  std::vector<const DeviceBatch *> sub;    // per group: its members at pass offsets
+  std::vector<int> first;                  // per group: its first member in the pass
+  std::vector<int64_t> eig_base;           // per group: its first eigenvalue
+  std::vector<int> members;                // caller indices in pass order
   std::vector<int32_t> n;
   std::vector<int64_t> off;
   int64_t total = 0;
@@ -259,124 +277,156 @@ struct GroupReport {
   int32_t *sweeps;
 };
 
-size_t reportBytes(int count) { return (4 * sizeof(double) + sizeof(int32_t)) * count + 64; }
+// (rounded up to 16 bytes so the next report's doubles stay aligned)
+size_t reportBytes(int count) {
+  return ((4 * sizeof(double) + sizeof(int32_t)) * count + 64 + 15) & ~static_cast<size_t>(15);
+}
 
 GroupReport reportAt(void *base, int count) {
   auto *d = static_cast<double *>(base);
   return {d, d + 2 * count, reinterpret_cast<int32_t *>(d + 4 * count)};
 }
 
-// Runs of members whose caller offsets are contiguous: one copy each.
+// Members [lo, hi) of the pass in runs whose caller offsets are contiguous
+// (the arena offsets are contiguous by construction): one copy per run.
 template <class Copy>
-int forEachRun(const Group &g, const int64_t *off_user, const GroupBuffers &gb, Copy copy) {
-  const int count = static_cast<int>(g.members.size());
-  for (int i = 0; i < count;) {
+int forEachRun(const PassBuffers &pb, const int64_t *off_user, int lo, int hi, Copy copy) {
+  for (int i = lo; i < hi;) {
     int j = i + 1;
-    while (j < count && g.members[j] == g.members[j - 1] + 1 &&
-           off_user[g.members[j]] ==
-               off_user[g.members[j - 1]] +
-                   ((static_cast<int64_t>(gb.n[j - 1]) * gb.n[j - 1] + 3) & ~int64_t(3)))
+    while (j < hi && pb.members[j] == pb.members[j - 1] + 1 &&
+           off_user[pb.members[j]] ==
+               off_user[pb.members[j - 1]] +
+                   ((static_cast<int64_t>(pb.n[j - 1]) * pb.n[j - 1] + 3) & ~int64_t(3)))
       ++j;
-    const int64_t last = j - 1;
+    const int last = j - 1;
     const int64_t bytes =
-        (gb.off[last] - gb.off[i] + static_cast<int64_t>(gb.n[last]) * gb.n[last]) * sizeof(float);
-    MSQ_TRY(copy(off_user[g.members[i]], gb.off[i], bytes));
+        (pb.off[last] - pb.off[i] + static_cast<int64_t>(pb.n[last]) * pb.n[last]) * sizeof(float);
+    MSQ_TRY(copy(off_user[pb.members[i]], pb.off[i], bytes));
     i = j;
   }
   return MSQ_OK;
 }
 
-// Enqueues one plan over its sub-batch on ctx->stream with no host
-// synchronisation: gather into the arena, Jacobi, factor, reconstruction,
-// residual, the plan's sweeps, final residual, and the report copies.
-// `backup`: room for a copy of X (the fallback's undo).
-int enqueueGroup(msq_ctx *ctx, const float *a_user, const int32_t *n_user,
-                 const int64_t *off_user, const Group &g, GroupReport rep, bool backup,
-                 GroupBuffers *gb) {
-  const int count = static_cast<int>(g.members.size());
-  gb->n.resize(count);
-  gb->off.resize(count);
+// Enqueues one pass on ctx->stream with no host synchronisation: gather, the
+// pass's Jacobi, then per group factor, reconstruction, residual, the plan's
+// sweeps, final residual and the report copies.  `backup`: room for a copy
+// of X (the fallback's undo).
+int enqueuePass(msq_ctx *ctx, const float *a_user, const int32_t *n_user,
+                const int64_t *off_user, const std::vector<Group> &groups, const Pass &pass,
+                const std::vector<GroupReport> &reports, bool backup, PassBuffers *pb) {
   int64_t total = 0, order_total = 0;
-  for (int i = 0; i < count; ++i) {
-    gb->n[i] = n_user[g.members[i]];
-    gb->off[i] = total;
-    total += (static_cast<int64_t>(gb->n[i]) * gb->n[i] + 3) & ~int64_t(3);
-    order_total += gb->n[i];
+  for (int k : pass.groups) {
+    pb->first.push_back(static_cast<int>(pb->members.size()));
+    pb->eig_base.push_back(order_total);
+    for (int m : groups[k].members) {
+      pb->members.push_back(m);
+      pb->n.push_back(n_user[m]);
+      pb->off.push_back(total);
+      total += (static_cast<int64_t>(n_user[m]) * n_user[m] + 3) & ~int64_t(3);
+      order_total += n_user[m];
+    }
   }
-  gb->total = total;
-  const DeviceBatch *b = prepareBatch(ctx, gb->n.data(), gb->off.data(), count);
+  const int count = static_cast<int>(pb->members.size());
+  pb->total = total;
+  const DeviceBatch *b = prepareBatch(ctx, pb->n.data(), pb->off.data(), count);
   if (b == nullptr) return MSQ_ERR_INVALID_ARGUMENT;
-  gb->b = b;
+  pb->b = b;
+  for (size_t q = 0; q < pass.groups.size(); ++q) {
+    const int lo = pb->first[q];
+    const int c = static_cast<int>(groups[pass.groups[q]].members.size());
+    const DeviceBatch *sb =
+        pass.groups.size() == 1 ? b : prepareBatch(ctx, pb->n.data() + lo, pb->off.data() + lo, c);
+    if (sb == nullptr) return MSQ_ERR_INVALID_ARGUMENT;
+    pb->sub.push_back(sb);
+  }
   const size_t mat = alignUp(total * sizeof(float));
-  gb->mat = mat;
+  pb->mat = mat;
   const size_t vec = alignUp(order_total * sizeof(float));
   const size_t norms_bytes = alignUp(2 * count * sizeof(double));
   const size_t sweeps_bytes = alignUp(count * sizeof(int32_t));
   const size_t backup_bytes = backup ? 2 * mat : 0;
-  char *w = static_cast<char *>(
-      scratch(ctx, 8 * mat + vec + norms_bytes + sweeps_bytes + backup_bytes, kScratchSolver));
+  const size_t tols_bytes = pass.tols_host ? alignUp(count * sizeof(double)) : 0;
+  char *w = static_cast<char *>(scratch(
+      ctx, 8 * mat + vec + norms_bytes + sweeps_bytes + backup_bytes + tols_bytes, kScratchSolver));
   if (w == nullptr) return MSQ_ERR_CUDA;
-  gb->A = reinterpret_cast<float *>(w);
-  gb->J = reinterpret_cast<float *>(w + mat);       // Jacobi working copy
-  gb->V = reinterpret_cast<float *>(w + 2 * mat);
-  gb->F = reinterpret_cast<float *>(w + 3 * mat);
-  gb->Xh = reinterpret_cast<float *>(w + 4 * mat);
-  gb->Xl = reinterpret_cast<float *>(w + 5 * mat);
-  gb->R = reinterpret_cast<float *>(w + 6 * mat);
-  gb->W1 = reinterpret_cast<float *>(w + 7 * mat);  // with F: the 2 sweep buffers
-  gb->lam = reinterpret_cast<float *>(w + 8 * mat);
-  gb->norms = reinterpret_cast<double *>(w + 8 * mat + vec);
-  gb->sweeps = reinterpret_cast<int32_t *>(w + 8 * mat + vec + norms_bytes);
-  gb->Bh = reinterpret_cast<float *>(w + 8 * mat + vec + norms_bytes + sweeps_bytes);
-  gb->Bl = gb->Bh + mat / sizeof(float);
-  MSQ_TRY(forEachRun(g, off_user, *gb, [&](int64_t user_off, int64_t arena_off, int64_t bytes) {
-    return cudaCheck(ctx, cudaMemcpyAsync(gb->A + arena_off, a_user + user_off, bytes,
+  pb->A = reinterpret_cast<float *>(w);
+  pb->J = reinterpret_cast<float *>(w + mat);       // Jacobi working copy
+  pb->V = reinterpret_cast<float *>(w + 2 * mat);
+  pb->F = reinterpret_cast<float *>(w + 3 * mat);
+  pb->Xh = reinterpret_cast<float *>(w + 4 * mat);
+  pb->Xl = reinterpret_cast<float *>(w + 5 * mat);
+  pb->R = reinterpret_cast<float *>(w + 6 * mat);
+  pb->W1 = reinterpret_cast<float *>(w + 7 * mat);  // with F: the 2 sweep buffers
+  pb->lam = reinterpret_cast<float *>(w + 8 * mat);
+  pb->norms = reinterpret_cast<double *>(w + 8 * mat + vec);
+  pb->sweeps = reinterpret_cast<int32_t *>(w + 8 * mat + vec + norms_bytes);
+  pb->Bh = reinterpret_cast<float *>(w + 8 * mat + vec + norms_bytes + sweeps_bytes);
+  pb->Bl = pb->Bh + mat / sizeof(float);
+  MSQ_TRY(forEachRun(*pb, off_user, 0, count, [&](int64_t user_off, int64_t arena_off, int64_t bytes) {
+    return cudaCheck(ctx, cudaMemcpyAsync(pb->A + arena_off, a_user + user_off, bytes,
                                           cudaMemcpyDeviceToDevice, ctx->stream), "gather A");
   }));
-  MSQ_TRY(cudaCheck(ctx, cudaMemcpyAsync(gb->J, gb->A, total * sizeof(float),
+  MSQ_TRY(cudaCheck(ctx, cudaMemcpyAsync(pb->J, pb->A, total * sizeof(float),
                                          cudaMemcpyDeviceToDevice, ctx->stream), "jacobi copy"));
-  const int max_sweeps = g.plan.jacobi_max_sweeps > 0 ? g.plan.jacobi_max_sweeps : 15;
-  MSQ_TRY(jacobiEnqueue(ctx, b, gb->J, gb->V, gb->lam, g.plan.jacobi_tolerance, max_sweeps,
-                        gb->sweeps, nullptr, g.plan.format != MSQ_PLAN_FP32));
-  MSQ_TRY(makeFactor(ctx, b, gb->V, gb->lam, gb->F));
-  MSQ_TRY(reconstructFromFactor(ctx, b, g.plan.format, gb->F, gb->Xh));
-  MSQ_TRY(cudaCheck(ctx, cudaMemsetAsync(gb->Xl, 0, total * sizeof(float), ctx->stream),
-                    "x_lo reset"));
-  // Corrections use the FP32 stable basis V, as the reference's fp32_frozen
-  // stage does (src/metal_solver.cpp:304-325).  The plain FP32 plan runs its
-  // GEMMs and residuals on the CUDA cores in FP32 / float-float; low-bit
-  // plans run the correction GEMMs on the tensor cores (split BF16, FP32
-  // accumulation) and the residual of the low-bit X0 too.  A tensor-core
-  // residual carries the FP32 accumulation error of an n-long sum (about
-  // sqrt(n) 2^-24 of ||A||): negligible against the quantization residual of
-  // X0, not against the residual after a correction, which a further
-  // correction could not push below it.  So every residual after the first
-  // correction, and the one that decides acceptance, are float-float.
-  const bool low_bit = g.plan.format != MSQ_PLAN_FP32;
-  const int gemm_format = low_bit ? MSQ_FMT_BF16 : MSQ_FMT_FP32;
-  auto residual = [&](bool accurate) {
-    return low_bit && !accurate ? residualTc(ctx, b, gb->A, gb->Xh, gb->Xl, gb->R, gb->norms)
-                                : residualFF(ctx, b, gb->A, gb->Xh, gb->Xl, gb->R, gb->norms);
-  };
-  MSQ_TRY(residual(g.plan.sweeps == 0));
-  MSQ_TRY(cudaCheck(ctx, cudaMemcpyAsync(rep.initial, gb->norms, 2 * count * sizeof(double),
-                                         cudaMemcpyDeviceToHost, ctx->stream), "norms read"));
-  for (int s = 0; s < g.plan.sweeps; ++s) {
-    MSQ_TRY(sylvesterSweep(ctx, b, gemm_format, gb->V, gb->lam, gb->R, gb->Xh, gb->Xl, gb->F,
-                           gb->W1));
-    MSQ_TRY(residual(true));
+  const int max_sweeps = pass.jacobi_max_sweeps > 0 ? pass.jacobi_max_sweeps : 15;
+  double *tols = nullptr;
+  if (pass.tols_host != nullptr) {
+    tols = reinterpret_cast<double *>(w + 8 * mat + vec + norms_bytes + sweeps_bytes + backup_bytes);
+    MSQ_TRY(cudaCheck(ctx, cudaMemcpyAsync(tols, pass.tols_host, count * sizeof(double),
+                                           cudaMemcpyHostToDevice, ctx->stream), "tolerances"));
   }
-  MSQ_TRY(cudaCheck(ctx, cudaMemcpyAsync(rep.final, gb->norms, 2 * count * sizeof(double),
-                                         cudaMemcpyDeviceToHost, ctx->stream), "norms read"));
-  return cudaCheck(ctx, cudaMemcpyAsync(rep.sweeps, gb->sweeps, count * sizeof(int32_t),
-                                        cudaMemcpyDeviceToHost, ctx->stream), "sweeps read");
+  MSQ_TRY(jacobiEnqueue(ctx, b, pb->J, pb->V, pb->lam, pass.jacobi_tolerance, max_sweeps,
+                        pb->sweeps, nullptr, pass.low_bit, tols, pass.tols_host));
+  MSQ_TRY(cudaCheck(ctx, cudaMemsetAsync(pb->Xl, 0, total * sizeof(float), ctx->stream),
+                    "x_lo reset"));
+  for (size_t q = 0; q < pass.groups.size(); ++q) {
+    const Group &g = groups[pass.groups[q]];
+    const DeviceBatch *sb = pb->sub[q];
+    const int c = static_cast<int>(g.members.size());
+    const GroupReport &rep = reports[q];
+    float *lam = pb->lam + pb->eig_base[q];
+    double *norms = pb->norms + 2 * pb->first[q];
+    MSQ_TRY(makeFactor(ctx, sb, pb->V, lam, pb->F));
+    MSQ_TRY(reconstructFromFactor(ctx, sb, g.plan.format, pb->F, pb->Xh));
+    // Corrections use the FP32 stable basis V, as the reference's fp32_frozen
+    // stage does (src/metal_solver.cpp:304-325).  The plain FP32 plan runs its
+    // GEMMs and residuals on the CUDA cores in FP32 / float-float; low-bit
+    // plans run the correction GEMMs on the tensor cores (split BF16, FP32
+    // accumulation) and the residual of the low-bit X0 too.  A tensor-core
+    // residual carries the FP32 accumulation error of an n-long sum (about
+    // sqrt(n) 2^-24 of ||A||): negligible against the quantization residual of
+    // X0, not against the residual after a correction, which a further
+    // correction could not push below it.  So every residual after the first
+    // correction, and the one that decides acceptance, are float-float.
+    const bool low_bit = g.plan.format != MSQ_PLAN_FP32;
+    const int gemm_format = low_bit ? MSQ_FMT_BF16 : MSQ_FMT_FP32;
+    auto residual = [&](bool accurate) {
+      return low_bit && !accurate ? residualTc(ctx, sb, pb->A, pb->Xh, pb->Xl, pb->R, norms)
+                                  : residualFF(ctx, sb, pb->A, pb->Xh, pb->Xl, pb->R, norms);
+    };
+    MSQ_TRY(residual(g.plan.sweeps == 0));
+    MSQ_TRY(cudaCheck(ctx, cudaMemcpyAsync(rep.initial, norms, 2 * c * sizeof(double),
+                                           cudaMemcpyDeviceToHost, ctx->stream), "norms read"));
+    for (int s = 0; s < g.plan.sweeps; ++s) {
+      MSQ_TRY(sylvesterSweep(ctx, sb, gemm_format, pb->V, lam, pb->R, pb->Xh, pb->Xl, pb->F,
+                             pb->W1));
+      MSQ_TRY(residual(true));
+    }
+    MSQ_TRY(cudaCheck(ctx, cudaMemcpyAsync(rep.final, norms, 2 * c * sizeof(double),
+                                           cudaMemcpyDeviceToHost, ctx->stream), "norms read"));
+    MSQ_TRY(cudaCheck(ctx, cudaMemcpyAsync(rep.sweeps, pb->sweeps + pb->first[q],
+                                           c * sizeof(int32_t), cudaMemcpyDeviceToHost,
+                                           ctx->stream), "sweeps read"));
+  }
+  return MSQ_OK;
 }
 
-// Scatter X (hi word; the lo word is below FP32 resolution of the output).
-int scatterGroup(msq_ctx *ctx, const Group &g, const int64_t *off_user, const GroupBuffers &gb,
-                 float *root) {
-  return forEachRun(g, off_user, gb, [&](int64_t user_off, int64_t arena_off, int64_t bytes) {
-    return cudaCheck(ctx, cudaMemcpyAsync(root + user_off, gb.Xh + arena_off, bytes,
+// Scatter X of every member of the pass (hi word; the lo word is below FP32
+// resolution of the output).
+int scatterPass(msq_ctx *ctx, const int64_t *off_user, const PassBuffers &pb, float *root) {
+  return forEachRun(pb, off_user, 0, static_cast<int>(pb.members.size()),
+                    [&](int64_t user_off, int64_t arena_off, int64_t bytes) {
+    return cudaCheck(ctx, cudaMemcpyAsync(root + user_off, pb.Xh + arena_off, bytes,
                                           cudaMemcpyDeviceToDevice, ctx->stream), "scatter X");
   });
 }
@@ -396,9 +446,12 @@ int runFallback(msq_ctx *ctx, const float *a_user, const int32_t *n_user,
   const int count = static_cast<int>(g.members.size());
   void *host = pinnedScratch(ctx, reportBytes(count));
   if (host == nullptr) return MSQ_ERR_CUDA;
-  const GroupReport rep = reportAt(host, count);
-  GroupBuffers gb;
-  MSQ_TRY(enqueueGroup(ctx, a_user, n_user, off_user, g, rep, true, &gb));
+  const std::vector<GroupReport> reports{reportAt(host, count)};
+  const GroupReport &rep = reports[0];
+  const std::vector<Group> groups{g};
+  Pass pass{g.plan.jacobi_tolerance, g.plan.jacobi_max_sweeps, false, {0}};
+  PassBuffers gb;
+  MSQ_TRY(enqueuePass(ctx, a_user, n_user, off_user, groups, pass, reports, true, &gb));
   MSQ_TRY(cudaCheck(ctx, cudaStreamSynchronize(ctx->stream), "fallback sync"));
   std::vector<double> norms(rep.final, rep.final + 2 * count);
   int done = g.plan.sweeps;
@@ -436,7 +489,7 @@ int runFallback(msq_ctx *ctx, const float *a_user, const int32_t *n_user,
     if (worse) break;
   }
   *applied = done;
-  MSQ_TRY(scatterGroup(ctx, g, off_user, gb, root));
+  MSQ_TRY(scatterPass(ctx, off_user, gb, root));
   MSQ_TRY(cudaCheck(ctx, cudaStreamSynchronize(ctx->stream), "group sync"));
   MSQ_TRY(checkDeviceStatus(ctx));
   for (int i = 0; i < count; ++i) {
@@ -505,10 +558,37 @@ extern "C" int msq_solve_batched(msq_ctx *ctx, const float *a, const int32_t *n,
   // tolerance (the first sizes every arena and cache), the whole sequence is
   // captured once into a CUDA graph and later calls replay it with one
   // launch, while no freed allocation invalidates it.
+  // every group in one Jacobi pass, each matrix to its plan's tolerance
+  std::vector<Pass> passes(1);
+  {
+    Pass &ps = passes[0];
+    ps.jacobi_tolerance = groups[0].plan.jacobi_tolerance;
+    ps.jacobi_max_sweeps = 0;
+    ps.low_bit = true;
+    for (size_t k = 0; k < groups.size(); ++k) {
+      const msq_plan &p = groups[k].plan;
+      ps.groups.push_back(static_cast<int>(k));
+      ps.jacobi_max_sweeps =
+          std::max(ps.jacobi_max_sweeps, p.jacobi_max_sweeps > 0 ? p.jacobi_max_sweeps : 15);
+      ps.low_bit = ps.low_bit && p.format != MSQ_PLAN_FP32;
+    }
+  }
+  bool mixed_tols = false;
+  for (const Group &g : groups)
+    mixed_tols = mixed_tols || g.plan.jacobi_tolerance != groups[0].plan.jacobi_tolerance;
   size_t report_bytes = 0;
   for (const Group &g : groups) report_bytes += reportBytes(static_cast<int>(g.members.size()));
+  const size_t tols_at = report_bytes;
+  if (mixed_tols) report_bytes += count * sizeof(double);
   void *host = pinnedScratch(ctx, report_bytes);
   if (host == nullptr) return MSQ_ERR_CUDA;
+  if (mixed_tols) {
+    double *t = reinterpret_cast<double *>(static_cast<char *>(host) + tols_at);
+    size_t i = 0;
+    for (const Group &g : groups)
+      for (size_t j = 0; j < g.members.size(); ++j) t[i++] = g.plan.jacobi_tolerance;
+    passes[0].tols_host = t;
+  }
   std::vector<GroupReport> reports;
   {
     char *at = static_cast<char *>(host);
@@ -538,22 +618,23 @@ extern "C" int msq_solve_batched(msq_ctx *ctx, const float *a, const int32_t *n,
     const bool seen = std::find(ctx->solve_seen.begin(), ctx->solve_seen.end(), key) !=
                       ctx->solve_seen.end();
     bool capture = seen && ctx->graphs && !ctx->timing && waitTestMode() == kWaitTestOff;
-    std::vector<GroupBuffers> buffers(groups.size());
+    std::vector<PassBuffers> buffers(passes.size());
     if (capture) {
-      // the capture must not allocate or synchronise: every group's batch,
+      // the capture must not allocate or synchronise: every pass's batch,
       // Jacobi plan and tuned launch shapes exist after the direct run
-      for (const Group &g : groups) {
-        std::vector<int32_t> gn;
-        std::vector<int64_t> go;
+      for (const Pass &ps : passes) {
+        std::vector<int32_t> pn;
+        std::vector<int64_t> po;
         int64_t total = 0;
-        for (int m : g.members) {
-          gn.push_back(n[m]);
-          go.push_back(total);
-          total += (static_cast<int64_t>(n[m]) * n[m] + 3) & ~int64_t(3);
-        }
-        const DeviceBatch *b = prepareBatch(ctx, gn.data(), go.data(), static_cast<int>(gn.size()));
+        for (int k : ps.groups)
+          for (int m : groups[k].members) {
+            pn.push_back(n[m]);
+            po.push_back(total);
+            total += (static_cast<int64_t>(n[m]) * n[m] + 3) & ~int64_t(3);
+          }
+        const DeviceBatch *b = prepareBatch(ctx, pn.data(), po.data(), static_cast<int>(pn.size()));
         if (b == nullptr) return MSQ_ERR_INVALID_ARGUMENT;
-        capture = capture && jacobiCapturable(ctx, b, g.plan.format != MSQ_PLAN_FP32);
+        capture = capture && jacobiCapturable(ctx, b, ps.low_bit);
       }
     }
     const uint64_t generation = ctx->alloc_generation;
@@ -568,9 +649,11 @@ extern "C" int msq_solve_batched(msq_ctx *ctx, const float *a, const int32_t *n,
       ctx->capturing = true;
     }
     int status = MSQ_OK;
-    for (size_t k = 0; k < groups.size() && status == MSQ_OK; ++k) {
-      status = enqueueGroup(ctx, a, n, offset, groups[k], reports[k], false, &buffers[k]);
-      if (status == MSQ_OK) status = scatterGroup(ctx, groups[k], offset, buffers[k], root);
+    for (size_t q = 0; q < passes.size() && status == MSQ_OK; ++q) {
+      std::vector<GroupReport> pass_reports;
+      for (int k : passes[q].groups) pass_reports.push_back(reports[k]);
+      status = enqueuePass(ctx, a, n, offset, groups, passes[q], pass_reports, false, &buffers[q]);
+      if (status == MSQ_OK) status = scatterPass(ctx, offset, buffers[q], root);
     }
     if (capture) {
       ctx->stream = caller;

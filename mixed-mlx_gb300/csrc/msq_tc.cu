@@ -689,7 +689,7 @@ struct TcPlan {
 
 }  // namespace
 
-// The context's tile plans (at most 16 layouts and kinds, oldest evicted).
+// The context's tile plans (at most 32 layouts and kinds, oldest evicted).
 struct TcPlanCache {
   std::vector<TcPlan *> plans;
 };
@@ -761,7 +761,7 @@ TcPlan *tcPlan(msq_ctx *ctx, const DeviceBatch *b, int kind) {
   cudaMemcpy(p->tile_base, base.data(), base.size() * sizeof(int64_t), cudaMemcpyHostToDevice);
   cudaMemcpy(p->row_matrix, row_matrix.data(), row_matrix.size() * sizeof(int32_t),
              cudaMemcpyHostToDevice);
-  if (plans.size() >= 16) {
+  if (plans.size() >= 32) {
     cudaFree(plans.front()->device);
     ++ctx->alloc_generation;
     delete plans.front();

@@ -29,6 +29,32 @@ JACOBI_TOL = {0: 1e-7, 1: 1e-3, 2: 1e-2}
 PLANS = [(1, 0), (1, 1), (1, 2), (2, 0), (2, 1), (2, 2), (3, 1), (3, 2)]
 
 
+def cost_order(seconds, tie: float = 0.02) -> list:
+    """Plans from cheapest to dearest by measured GPU time; plans within
+    `tie` (relative) of each other count as equally cheap and are ordered by
+    basis precision (BF16, then FP8, then MXFP4), so a near-tie never trades
+    accuracy for noise."""
+    seconds = np.asarray(seconds, dtype=np.float64)
+    base = seconds.min()
+    buckets = np.floor(np.log(seconds / base) / np.log1p(tie)).astype(np.int64)
+    return sorted(range(len(PLANS)), key=lambda k: (buckets[k], PLANS[k][0], seconds[k]))
+
+
+def load(msq, torch, ctx, path):
+    """A Selector with the weights, normalisation and plan costs saved by
+    train_selector.py; returns (selector, threshold, metadata)."""
+    import json
+    w = np.load(path)
+    selector = Selector(msq, torch, ctx)
+    selector.params = torch.from_numpy(w["params"]).cuda()
+    selector.mean = torch.from_numpy(w["mean"]).cuda()
+    selector.std = torch.from_numpy(w["std"]).cuda()
+    meta = json.loads(str(w["metadata"])) if "metadata" in w.files else {}
+    secs = meta.get("train", {}).get("plan_seconds")
+    selector.cost_order = cost_order(secs) if secs else [int(k) for k in w["cost_order"]]
+    return selector, float(w["threshold"][0]), meta
+
+
 def plan_structs(msq, index_list):
     return [msq.plan(PLANS[k][0], PLANS[k][1], JACOBI_TOL[PLANS[k][1]], 15) for k in index_list]
 

@@ -96,7 +96,8 @@ def test_trained_selector_beats_the_method_without_it(ctx, msq, sel):
 
     def timed(p):
         out = torch.empty_like(flat_t)
-        ctx.solve_batched(flat_t, batch_t, p, tol, out=out)  # warm-up / plan caches
+        for _ in range(2):  # plan caches, then the solve's graph capture
+            ctx.solve_batched(flat_t, batch_t, p, tol, out=out)
         s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         s.record()
         _, res = ctx.solve_batched(flat_t, batch_t, p, tol, out=out)

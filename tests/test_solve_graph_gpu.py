@@ -43,9 +43,12 @@ def test_steady_state_is_one_graph_launch_with_the_same_bits(ctx, msq):
     finally:
         ctx.set_graphs(True)
     assert np.array_equal(root_graph.view(np.uint32), root_direct.view(np.uint32))
+    # the roots are the same bits; the reported norms are FP64 sums whose
+    # per-warp atomic order may differ run to run (last-bit differences)
     for rg, rd in zip(res_graph, res_direct):
-        assert rg.final_residual == rd.final_residual and rg.jacobi_sweeps == rd.jacobi_sweeps
-        assert rg.initial_residual == rd.initial_residual and rg.accepted == rd.accepted
+        assert rg.final_residual == pytest.approx(rd.final_residual, rel=1e-12)
+        assert rg.initial_residual == pytest.approx(rd.initial_residual, rel=1e-12)
+        assert rg.jacobi_sweeps == rd.jacobi_sweeps and rg.accepted == rd.accepted
     for m, x, r in zip(mats, b.unpack(root_graph), res_graph):
         assert r.final_residual <= 1e-5
         assert O.relative_residual(m, x) <= 2e-5
