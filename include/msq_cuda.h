@@ -96,6 +96,10 @@ int msq_debug_expire_waits(int mode);
 uint64_t msq_launch_count(const msq_ctx *ctx);
 /* Number of CUDA graph launches issued so far on `ctx`. */
 uint64_t msq_graph_launch_count(const msq_ctx *ctx);
+/* Measured FP32 FMA throughput of the device (TFLOP/s, best of three timed
+ * launches of independent FMA chains on every SM): the denominator of the
+ * FP32 rooflines (the Jacobi kernels).  Synchronises. */
+int msq_fma_rate(msq_ctx *ctx, double *tflops);
 /* Launch timing for profiling: between begin and end, an event is recorded
  * on the context's stream after every launch (launches on internal streams
  * get a begin and an end event); end synchronises and writes one line per
@@ -179,11 +183,13 @@ int msq_spectrum_decode(msq_ctx *ctx, int format, const uint8_t *values, const f
  * eigenvector j), eigenvalues (FP32, n[i] per matrix at value offset
  * eig_offset[i] = sum of previous n), sweeps_done / off_ratio per matrix
  * (device arrays, may be NULL).  `matrices` is overwritten (the converged,
- * nearly diagonal matrix).  Orders up to 16384: a matrix above 1024, or one
- * of at most 8 above 256 in the batch, is solved with every SM (the grid
- * kernels; the call then synchronises the context's stream once per sweep
- * to read the off-norm), the others one CTA each.  Results are the same
- * bits either way.                                                        */
+ * nearly diagonal matrix).  Orders up to 16384: a matrix above 1024 is
+ * solved with every SM (the grid kernels; the call then synchronises the
+ * context's stream once per sweep to read the off-norm), the others one CTA
+ * each, except the few largest above 256 whose one-CTA solves would outlast
+ * the rest of the batch (a cost model; in the tensor-core eigenvector modes:
+ * any above 256 when at most 8 are in the batch), which also go to the grid
+ * kernels.  Results are the same bits either way.                         */
 int msq_jacobi_batched(msq_ctx *ctx, float *matrices, float *vectors,
                        float *eigenvalues, const int32_t *n,
                        const int64_t *offset, int count, double tolerance,
@@ -390,7 +396,8 @@ int msq_residual_general(msq_ctx *ctx, const float *a, const float *a_lo,
  * The GPU-resident solve of solveGpuResidentSpd (src/metal_solver.cpp:92-336)
  * over a batch: Jacobi -> (quantize W) -> reconstruct -> Sylvester sweeps ->
  * final float-float residual, per-matrix plan, with FP32 fallback for every
- * matrix whose final residual misses `tolerance`: FP32 Jacobi to 1e-7, FP32
+ * matrix whose final residual misses `tolerance`: FP32 Jacobi to 1e-7
+ * (continuing the plan's rotations where those are FP32), FP32
  * reconstruction and FP32 correction sweeps until the tolerance is met
  * (one to four; a matrix that still misses it reports its residual).      */
 typedef enum {
@@ -411,7 +418,7 @@ typedef struct {
 typedef struct {
   double final_residual;   /* ||A - X^2||_F / ||A||_F, float-float         */
   double initial_residual; /* residual of the reconstruction X0            */
-  int32_t jacobi_sweeps;
+  int32_t jacobi_sweeps;    /* Jacobi sweeps (a continued fallback: both passes) */
   int32_t corrections;     /* Sylvester sweeps applied                     */
   int32_t accepted;        /* 1: the plan met the tolerance; 0: fell back  */
   int32_t fallback;        /* 1: result comes from the FP32 fallback       */

@@ -76,6 +76,7 @@ _SIGS = {
     "msq_debug_expire_waits": (ctypes.c_int, [ctypes.c_int]),
     "msq_launch_count": (ctypes.c_uint64, [_P]),
     "msq_graph_launch_count": (ctypes.c_uint64, [_P]),
+    "msq_fma_rate": (ctypes.c_int, [_P, _P]),
     "msq_storage_bytes": (ctypes.c_size_t, [ctypes.c_int, ctypes.c_size_t]),
     "msq_scale_bytes": (ctypes.c_size_t, [ctypes.c_int, ctypes.c_size_t, ctypes.c_size_t]),
     "msq_encode": (ctypes.c_int, [_P, ctypes.c_int, _P, ctypes.c_size_t, ctypes.c_size_t, _P, _P]),
@@ -261,6 +262,12 @@ class Context:
     @property
     def graph_launches(self) -> int:
         return int(lib().msq_graph_launch_count(self.handle))
+
+    def fma_rate(self) -> float:
+        """Measured FP32 FMA throughput of the device, TFLOP/s."""
+        out = ctypes.c_double()
+        self.check(lib().msq_fma_rate(self.handle, ctypes.byref(out)), "msq_fma_rate")
+        return out.value
 
     def autotune_report(self) -> str:
         """The launch-shape autotuner's decisions for this context's device."""

@@ -275,7 +275,7 @@ extern "C" void msq_destroy(msq_ctx *ctx) {
     cudaFree(b->offset);
     delete b;
   }
-  for (int slot = 0; slot < 5; ++slot)
+  for (int slot = 0; slot < msq::kScratchSlots; ++slot)
     if (ctx->scratch[slot] != nullptr) cudaFree(ctx->scratch[slot]);
   if (ctx->grid_exec != nullptr) cudaGraphExecDestroy(ctx->grid_exec);
   for (auto &g : ctx->jacobi_graphs) cudaGraphExecDestroy(g.exec);
@@ -334,6 +334,55 @@ extern "C" uint64_t msq_launch_count(const msq_ctx *ctx) {
 
 extern "C" uint64_t msq_graph_launch_count(const msq_ctx *ctx) {
   return ctx == nullptr ? 0 : ctx->graph_launches;
+}
+
+namespace msq {
+namespace {
+
+// FP32 FMA throughput: eight independent FMA chains per thread, enough
+// threads to fill every SM; the result keeps the chains live.
+__global__ void __launch_bounds__(256) fmaRateKernel(float *out, int iters, float a, float b) {
+  float x[8];
+#pragma unroll
+  for (int k = 0; k < 8; ++k) x[k] = static_cast<float>(threadIdx.x + k) * 1e-3f;
+  for (int i = 0; i < iters; ++i) {
+#pragma unroll
+    for (int k = 0; k < 8; ++k) x[k] = fmaf(x[k], a, b);
+  }
+  float sum = 0.0f;
+#pragma unroll
+  for (int k = 0; k < 8; ++k) sum += x[k];
+  out[blockIdx.x * blockDim.x + threadIdx.x] = sum;
+}
+
+}  // namespace
+}  // namespace msq
+
+extern "C" int msq_fma_rate(msq_ctx *ctx, double *tflops) {
+  if (ctx == nullptr || tflops == nullptr) return MSQ_ERR_INVALID_ARGUMENT;
+  msq::DeviceGuard device_guard(ctx);
+  constexpr int kBlocks = msq::kSmCount * 8, kThreads = 256, kIters = 1 << 15;
+  float *out = static_cast<float *>(scratch(ctx, kBlocks * kThreads * sizeof(float), msq::kScratchGemm));
+  if (out == nullptr) return MSQ_ERR_CUDA;
+  cudaEvent_t start = nullptr, stop = nullptr;
+  MSQ_TRY(cudaCheck(ctx, cudaEventCreate(&start), "fma rate event"));
+  MSQ_TRY(cudaCheck(ctx, cudaEventCreate(&stop), "fma rate event"));
+  float best = 0.0f;
+  for (int rep = 0; rep < 4; ++rep) {  // the first launch warms the clocks
+    cudaEventRecord(start, ctx->stream);
+    msq::fmaRateKernel<<<kBlocks, kThreads, 0, ctx->stream>>>(out, kIters, 0.999999f, 1e-6f);
+    cudaEventRecord(stop, ctx->stream);
+    MSQ_TRY(launched(ctx, "fma rate"));
+    MSQ_TRY(cudaCheck(ctx, cudaEventSynchronize(stop), "fma rate sync"));
+    float ms = 0.0f;
+    cudaEventElapsedTime(&ms, start, stop);
+    if (rep > 0 && ms > 0.0f && (best == 0.0f || ms < best)) best = ms;
+  }
+  cudaEventDestroy(start);
+  cudaEventDestroy(stop);
+  const double flops = 2.0 * 8.0 * kIters * static_cast<double>(kBlocks) * kThreads;
+  *tflops = best > 0.0f ? flops / (best * 1e-3) / 1e12 : 0.0;
+  return MSQ_OK;
 }
 
 extern "C" int msq_timing_begin(msq_ctx *ctx) {

@@ -100,8 +100,8 @@ struct msq_ctx {
   int *d_status = nullptr;  // device status word
   // Grow-only scratch arenas owned by the context (freed in msq_destroy);
   // one per user so nested stages never share memory.
-  void *scratch[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};
-  size_t scratch_bytes[5] = {0, 0, 0, 0, 0};
+  void *scratch[6] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
+  size_t scratch_bytes[6] = {0, 0, 0, 0, 0, 0};
   // Batch layouts cached by content hash (at most 32, oldest evicted).
   std::vector<msq::DeviceBatch *> batches;
   // Launch timing (msq_timing_begin/end).  Launches on the context stream
@@ -189,9 +189,11 @@ int checkDeviceStatus(msq_ctx *ctx);
 const DeviceBatch *prepareBatch(msq_ctx *ctx, const int32_t *n,
                                 const int64_t *offset, int count);
 // Grow-only context scratch arena `slot` (0: Jacobi, 1: solver,
-// 2: codec operands, 3: GEMM split operands, 4: grid Jacobi).
+// 2: codec operands, 3: GEMM split operands, 4: grid Jacobi, 5: the rotated
+// matrices and eigenvectors a fallback continues from).
 enum ScratchSlot : int {
-  kScratchJacobi = 0, kScratchSolver = 1, kScratchOperand = 2, kScratchGemm = 3, kScratchGrid = 4
+  kScratchJacobi = 0, kScratchSolver = 1, kScratchOperand = 2, kScratchGemm = 3, kScratchGrid = 4,
+  kScratchFallback = 5, kScratchSlots = 6
 };
 void *scratch(msq_ctx *ctx, size_t bytes, int slot);
 // Grow-only pinned host staging (for reports copied back inside a graph).

@@ -55,6 +55,67 @@ constexpr size_t kSweepSmemHalf = 110 * 1024;
 constexpr int kMaxOrder = 16384;    // grid kernels; the batched ones see n <= 1024
 constexpr int kGridMinOrder = 1024;
 constexpr int kGridFewLarge = 8;
+// Routing cost model of the FP32 (round-robin) eigenvector mode, fitted to
+// solves to 1e-7 on a GB300 (about ten sweeps; both paths scale alike with
+// the sweep count): one matrix on one CTA takes about 3.8e-7 n^3 ms, and
+// batched matrices above 256 saturate at about 40 in flight (their tiles
+// stream from L2 / HBM), those up to 256 at about 300; the grid kernels take
+// about 5 + 3.8e-5 n^2 ms per matrix, one matrix at a time.
+constexpr double kCtaSolveMs = 3.8e-7;    // x n^3
+constexpr double kGridSolveMs0 = 5.0;     // + kGridSolveMs2 x n^2
+constexpr double kGridSolveMs2 = 3.8e-5;
+constexpr double kLargeInFlight = 40.0;
+constexpr double kSmallInFlight = 300.0;
+constexpr int kGridCandidates = 16;
+
+double ctaSolveMs(int n) { return kCtaSolveMs * n * static_cast<double>(n) * n; }
+double gridSolveMs(int n) { return kGridSolveMs0 + kGridSolveMs2 * n * static_cast<double>(n); }
+
+// The matrices of orders 257..1024 that go to the grid kernels: the p
+// largest, p minimising the estimated time max(longest one-CTA solve left,
+// batched work / matrices in flight, grid solves in sequence), and only
+// where that beats the all-batched estimate by 10% (a batch without grid
+// matrices runs without host synchronisation and can be captured).
+std::vector<char> gridRouting(const int32_t *n, int count) {
+  std::vector<char> grid(count, 0);
+  std::vector<int> cand;
+  double work = 0.0, small_max = 0.0;
+  for (int i = 0; i < count; ++i) {
+    if (n[i] > kGridMinOrder) {
+      grid[i] = 1;
+      continue;
+    }
+    if (n[i] > 256) {
+      cand.push_back(i);
+      work += ctaSolveMs(n[i]) / kLargeInFlight;
+    } else {
+      work += ctaSolveMs(n[i]) / kSmallInFlight;
+      small_max = std::max(small_max, ctaSolveMs(n[i]));
+    }
+  }
+  std::sort(cand.begin(), cand.end(), [&](int a, int b) { return n[a] > n[b] || (n[a] == n[b] && a < b); });
+  const int limit = std::min<int>(kGridCandidates, static_cast<int>(cand.size()));
+  auto estimate = [&](int p, double grid_ms, double batched_work) {
+    const double longest = p < static_cast<int>(cand.size()) ? ctaSolveMs(n[cand[p]]) : small_max;
+    return std::max({longest, batched_work, grid_ms});
+  };
+  const double all_batched = estimate(0, 0.0, work);
+  double best = all_batched, grid_ms = 0.0;
+  int best_p = 0;
+  for (int p = 1; p <= limit; ++p) {
+    const int i = cand[p - 1];
+    grid_ms += gridSolveMs(n[i]);
+    work -= ctaSolveMs(n[i]) / kLargeInFlight;
+    const double t = estimate(p, grid_ms, work);
+    if (t < best) {
+      best = t;
+      best_p = p;
+    }
+  }
+  if (best_p > 0 && best < 0.9 * all_batched)
+    for (int p = 0; p < best_p; ++p) grid[cand[p]] = 1;
+  return grid;
+}
 constexpr int kSweepThreadsMax = 512;
 constexpr int kReplayThreads = 256;
 
@@ -852,12 +913,16 @@ JacobiPlan *planFor(msq_ctx *ctx, const DeviceBatch *b, int mode) {
   plan->count = b->count;
   plan->mode = mode;
   const int total = b->count;
-  // Routing: a matrix above kGridMinOrder, or above 256 when at most
-  // kGridFewLarge such matrices are in the batch (too few to fill the SMs one
-  // CTA each), is solved by the grid kernels with every SM; the rest by the
-  // batched kernels.
+  // Routing: a matrix above kGridMinOrder is solved by the grid kernels with
+  // every SM, the rest by the batched kernels one CTA each, except: in the
+  // FP32 mode the cost model picks the largest matrices to move to the grid
+  // kernels (a few large matrices whose one-CTA solves would outlast the
+  // batch); in the two-level modes (built for 256 < n <= 512) a matrix above
+  // 256 when at most kGridFewLarge such matrices are in the batch.
   int large = 0;
   for (int i = 0; i < total; ++i) large += b->host_n[i] > 256;
+  const std::vector<char> routed = mode == 0 ? gridRouting(b->host_n.data(), total)
+                                             : std::vector<char>();
   std::vector<int32_t> ids;
   std::vector<int64_t> t_off(total, 0), l_off(total, 0);
   std::vector<int32_t> sched_off(total, -1), sched_host, table;
@@ -866,7 +931,7 @@ JacobiPlan *planFor(msq_ctx *ctx, const DeviceBatch *b, int mode) {
   std::vector<char> on_tc(total, 0);
   for (int i = 0; i < total; ++i) {
     const int n = b->host_n[i];
-    if (n > kGridMinOrder || (n > 256 && large <= kGridFewLarge)) {
+    if (mode == 0 ? routed[i] != 0 : (n > kGridMinOrder || (n > 256 && large <= kGridFewLarge))) {
       plan->grid_ids.push_back(i);
       continue;
     }
@@ -1064,7 +1129,7 @@ bool jacobiCapturable(msq_ctx *ctx, const DeviceBatch *b, bool low_bit_basis) {
 int jacobiEnqueue(msq_ctx *ctx, const DeviceBatch *b, float *matrices, float *vectors,
                   float *eigenvalues, double tolerance, int max_sweeps, int32_t *sweeps_done,
                   float *off_ratio, bool low_bit_basis, const double *tols_device,
-                  const double *tols_host) {
+                  const double *tols_host, bool keep_vectors) {
   if (b->max_n > kMaxOrder) {
     return setError(ctx, MSQ_ERR_UNSUPPORTED, "jacobi: order above 16384 is not supported");
   }
@@ -1142,6 +1207,7 @@ int jacobiEnqueue(msq_ctx *ctx, const DeviceBatch *b, float *matrices, float *ve
   uint64_t shape_hash = 1469598103934665603ull;
   for (const auto &per : shape)
     for (const auto &h : per) shape_hash = (shape_hash ^ static_cast<uint64_t>(h.threads)) * 1099511628211ull;
+  shape_hash = (shape_hash ^ (keep_vectors ? 0x9e37u : 0u)) * 1099511628211ull;
   const bool graphable = !measuring && !ctx->timing && plan->grid_ids.empty() && ctx->graphs &&
                          waitTestMode() == kWaitTestOff && !ctx->capturing;
   const JacobiGraphKey key{plan->serial, b->key, b->offset, matrices, vectors, eigenvalues,
@@ -1169,7 +1235,7 @@ int jacobiEnqueue(msq_ctx *ctx, const DeviceBatch *b, float *matrices, float *ve
   }
   auto body = [&]() -> int {
   MSQ_TRY(cudaCheck(ctx, cudaMemsetAsync(args.state, 0, state_bytes, ctx->stream), "state reset"));
-  {
+  if (!keep_vectors) {
     dim3 grid(64, std::min(b->count, 65535));
     identityKernel<<<grid, 256, 0, ctx->stream>>>(vectors, b->offset, b->n, b->count);
     MSQ_TRY(launched(ctx, "jacobi identity"));
@@ -1270,7 +1336,7 @@ int jacobiEnqueue(msq_ctx *ctx, const DeviceBatch *b, float *matrices, float *ve
     MSQ_TRY(gridJacobiSolve(ctx, matrices + b->host_offset[gi], vectors + b->host_offset[gi],
                             eigenvalues + b->host_eig_offset[gi], b->host_n[gi],
                             tols_host ? tols_host[gi] : tolerance, max_sweeps,
-                            &sweeps, &ratio, &norm2));
+                            &sweeps, &ratio, &norm2, keep_vectors));
     gridStateKernel<<<1, 1, 0, ctx->stream>>>(args.state + gi, sweeps, ratio, norm2);
     MSQ_TRY(launched(ctx, "jacobi grid state"));
   }
@@ -1372,7 +1438,7 @@ extern "C" int msq_jacobi_batched(msq_ctx *ctx, float *matrices, float *vectors,
   const DeviceBatch *b = prepareBatch(ctx, n, offset, count);
   if (b == nullptr) return MSQ_ERR_INVALID_ARGUMENT;
   return jacobiEnqueue(ctx, b, matrices, vectors, eigenvalues, tolerance,
-                       max_sweeps, sweeps_done, off_ratio, false, nullptr, nullptr);
+                       max_sweeps, sweeps_done, off_ratio, false, nullptr, nullptr, false);
 }
 
 // ---------------------------------------------------------------------------

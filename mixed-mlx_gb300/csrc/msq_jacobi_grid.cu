@@ -33,6 +33,7 @@ constexpr int kGridThreads = 256;
 struct GridArgs {
   float *tiles;  // packed tiles of A
   float *v;      // V, row-major n x m
+  const float *v_in;  // column-major starting V (null: the identity)
   float *q;      // this round's rotations, P x 64 (row-major 8x8 each)
   double *acc;   // off2, diag2 accumulators
   int n, m, nb, P;
@@ -41,7 +42,8 @@ struct GridArgs {
 };
 
 // A (column-major, n x n) -> symmetrised tiles (the same averaged load as
-// the batched kernel); V = I.  grid.y = column block J.
+// the batched kernel); V = I, or the given starting V (a continued solve).
+// grid.y = column block J.
 __global__ void gridLoadKernel(const float *a, GridArgs g) {
   const int J = blockIdx.y;
   for (int idx = blockIdx.x * blockDim.x + threadIdx.x; idx < (J + 1) * kTileF;
@@ -57,7 +59,11 @@ __global__ void gridLoadKernel(const float *a, GridArgs g) {
   // V rows 4J .. 4J + 3
   for (int idx = blockIdx.x * blockDim.x + threadIdx.x; idx < 4 * g.m; idx += gridDim.x * blockDim.x) {
     const int r = 4 * J + idx / g.m, c = idx % g.m;
-    if (r < g.n) g.v[static_cast<int64_t>(r) * g.m + c] = r == c ? 1.0f : 0.0f;
+    if (r < g.n) {
+      g.v[static_cast<int64_t>(r) * g.m + c] =
+          g.v_in == nullptr ? (r == c ? 1.0f : 0.0f)
+                            : (c < g.n ? g.v_in[r + static_cast<int64_t>(c) * g.n] : 0.0f);
+    }
   }
 }
 
@@ -237,7 +243,7 @@ __global__ void gridFinishKernel(GridArgs g, float *a, float *vectors, float *ei
 
 int gridJacobiSolve(msq_ctx *ctx, float *matrix, float *vectors, float *eigenvalues, int n,
                     double tolerance, int max_sweeps, int *sweeps_out, double *off_ratio_out,
-                    double *norm2_out) {
+                    double *norm2_out, bool keep_vectors) {
   const int m = padded8(n), nb = m / 4, P = nb / 2;
   const int64_t tile_floats = static_cast<int64_t>(nb) * (nb + 1) / 2 * kTileF;
   const int64_t v_floats = static_cast<int64_t>(n) * m;
@@ -254,6 +260,7 @@ int gridJacobiSolve(msq_ctx *ctx, float *matrix, float *vectors, float *eigenval
   g.tiles = reinterpret_cast<float *>(work + 256);
   g.v = g.tiles + tile_floats;
   g.q = g.v + v_floats;
+  g.v_in = keep_vectors ? vectors : nullptr;
   g.n = n;
   g.m = m;
   g.nb = nb;

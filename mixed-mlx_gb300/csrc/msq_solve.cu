@@ -310,10 +310,14 @@ int forEachRun(const PassBuffers &pb, const int64_t *off_user, int lo, int hi, C
 // Enqueues one pass on ctx->stream with no host synchronisation: gather, the
 // pass's Jacobi, then per group factor, reconstruction, residual, the plan's
 // sweeps, final residual and the report copies.  `backup`: room for a copy
-// of X (the fallback's undo).
+// of X (the fallback's undo).  `warm`: the pass continues an earlier Jacobi
+// of the same matrices instead of starting from A and the identity: its
+// rotated matrices at warm[0, total) and their accumulated rotations at
+// warm[total, 2 total), in the pass's own layout.
 int enqueuePass(msq_ctx *ctx, const float *a_user, const int32_t *n_user,
                 const int64_t *off_user, const std::vector<Group> &groups, const Pass &pass,
-                const std::vector<GroupReport> &reports, bool backup, PassBuffers *pb) {
+                const std::vector<GroupReport> &reports, bool backup, PassBuffers *pb,
+                const float *warm = nullptr) {
   int64_t total = 0, order_total = 0;
   for (int k : pass.groups) {
     pb->first.push_back(static_cast<int>(pb->members.size()));
@@ -366,8 +370,14 @@ int enqueuePass(msq_ctx *ctx, const float *a_user, const int32_t *n_user,
     return cudaCheck(ctx, cudaMemcpyAsync(pb->A + arena_off, a_user + user_off, bytes,
                                           cudaMemcpyDeviceToDevice, ctx->stream), "gather A");
   }));
-  MSQ_TRY(cudaCheck(ctx, cudaMemcpyAsync(pb->J, pb->A, total * sizeof(float),
-                                         cudaMemcpyDeviceToDevice, ctx->stream), "jacobi copy"));
+  MSQ_TRY(cudaCheck(ctx, cudaMemcpyAsync(pb->J, warm != nullptr ? warm : pb->A,
+                                         total * sizeof(float), cudaMemcpyDeviceToDevice,
+                                         ctx->stream), "jacobi copy"));
+  if (warm != nullptr) {
+    MSQ_TRY(cudaCheck(ctx, cudaMemcpyAsync(pb->V, warm + total, total * sizeof(float),
+                                           cudaMemcpyDeviceToDevice, ctx->stream),
+                      "vectors copy"));
+  }
   const int max_sweeps = pass.jacobi_max_sweeps > 0 ? pass.jacobi_max_sweeps : 15;
   double *tols = nullptr;
   if (pass.tols_host != nullptr) {
@@ -376,7 +386,8 @@ int enqueuePass(msq_ctx *ctx, const float *a_user, const int32_t *n_user,
                                            cudaMemcpyHostToDevice, ctx->stream), "tolerances"));
   }
   MSQ_TRY(jacobiEnqueue(ctx, b, pb->J, pb->V, pb->lam, pass.jacobi_tolerance, max_sweeps,
-                        pb->sweeps, nullptr, pass.low_bit, tols, pass.tols_host));
+                        pb->sweeps, nullptr, pass.low_bit, tols, pass.tols_host,
+                        warm != nullptr));
   MSQ_TRY(cudaCheck(ctx, cudaMemsetAsync(pb->Xl, 0, total * sizeof(float), ctx->stream),
                     "x_lo reset"));
   for (size_t q = 0; q < pass.groups.size(); ++q) {
@@ -438,11 +449,14 @@ double ratio(const double *norms, int i) { return std::sqrt(norms[2 * i] / norms
 // (at most extra_sweeps), as the reference's plain method corrects until its
 // tolerance is met (src/accelerate_backend.cpp:803-1091).  A sweep that does
 // not lower a member's residual is undone for that member and the sweeps
-// stop (Newton from a basis that no longer contracts diverges).
+// stop (Newton from a basis that no longer contracts diverges).  `warm`:
+// the members' rotated matrices and rotations from the plan pass (enqueuePass
+// layout), which the fallback's Jacobi continues; their sweeps add to the
+// plan pass's in `jsweeps`.
 int runFallback(msq_ctx *ctx, const float *a_user, const int32_t *n_user,
                 const int64_t *off_user, const Group &g, float *root, double tolerance,
                 int extra_sweeps, std::vector<double> &final_res, std::vector<int> &jsweeps,
-                int *applied) {
+                int *applied, const float *warm) {
   const int count = static_cast<int>(g.members.size());
   void *host = pinnedScratch(ctx, reportBytes(count));
   if (host == nullptr) return MSQ_ERR_CUDA;
@@ -451,7 +465,7 @@ int runFallback(msq_ctx *ctx, const float *a_user, const int32_t *n_user,
   const std::vector<Group> groups{g};
   Pass pass{g.plan.jacobi_tolerance, g.plan.jacobi_max_sweeps, false, {0}};
   PassBuffers gb;
-  MSQ_TRY(enqueuePass(ctx, a_user, n_user, off_user, groups, pass, reports, true, &gb));
+  MSQ_TRY(enqueuePass(ctx, a_user, n_user, off_user, groups, pass, reports, true, &gb, warm));
   MSQ_TRY(cudaCheck(ctx, cudaStreamSynchronize(ctx->stream), "fallback sync"));
   std::vector<double> norms(rep.final, rep.final + 2 * count);
   int done = g.plan.sweeps;
@@ -494,8 +508,56 @@ int runFallback(msq_ctx *ctx, const float *a_user, const int32_t *n_user,
   MSQ_TRY(checkDeviceStatus(ctx));
   for (int i = 0; i < count; ++i) {
     final_res[g.members[i]] = ratio(norms.data(), i);
-    jsweeps[g.members[i]] = rep.sweeps[i];
+    jsweeps[g.members[i]] = (warm != nullptr ? jsweeps[g.members[i]] : 0) + rep.sweeps[i];
   }
+  return MSQ_OK;
+}
+
+// Copies the retry members' rotated matrices and rotations out of the plan
+// pass's arena (still in place after the pass or its graph replay: every
+// group's members in group order, enqueuePass's layout) into the fallback
+// arena, in the layout the fallback pass gives them: J of every member, then
+// V of every member.  *warm stays null when the plan pass's eigenvectors are
+// not FP32 accurate (the tensor-core eigenvector modes, 256 < n <= 512).
+int warmStart(msq_ctx *ctx, const int32_t *n, int count, const std::vector<Group> &groups,
+              bool low_bit, const std::vector<int> &retry, const float **warm) {
+  *warm = nullptr;
+  auto elems = [&](int m) { return (static_cast<int64_t>(n[m]) * n[m] + 3) & ~int64_t(3); };
+  const int mode = ctx->jacobi_vectors >= 0 ? ctx->jacobi_vectors : (low_bit ? 2 : 0);
+  int64_t retry_total = 0;
+  for (int m : retry) {
+    if (mode >= 2 && n[m] > 256 && n[m] <= 512) return MSQ_OK;
+    retry_total += elems(m);
+  }
+  std::vector<int64_t> member_off(count, -1);  // by caller index
+  int64_t total = 0;
+  for (const Group &g : groups)
+    for (int m : g.members) {
+      member_off[m] = total;
+      total += elems(m);
+    }
+  const char *arena = static_cast<const char *>(ctx->scratch[kScratchSolver]);
+  if (arena == nullptr) return MSQ_OK;
+  const size_t mat = alignUp(total * sizeof(float));
+  const float *J = reinterpret_cast<const float *>(arena + mat);
+  const float *V = reinterpret_cast<const float *>(arena + 2 * mat);
+  auto *out = static_cast<float *>(scratch(ctx, 2 * retry_total * sizeof(float), kScratchFallback));
+  if (out == nullptr) return MSQ_ERR_CUDA;
+  int64_t at = 0;
+  for (size_t i = 0; i < retry.size();) {
+    // a run of members adjacent in both layouts: one copy per buffer
+    size_t j = i + 1;
+    int64_t run = elems(retry[i]);
+    while (j < retry.size() && member_off[retry[j]] == member_off[retry[i]] + run) run += elems(retry[j++]);
+    const int64_t from = member_off[retry[i]];
+    MSQ_TRY(cudaCheck(ctx, cudaMemcpyAsync(out + at, J + from, run * sizeof(float),
+                                           cudaMemcpyDeviceToDevice, ctx->stream), "warm J"));
+    MSQ_TRY(cudaCheck(ctx, cudaMemcpyAsync(out + retry_total + at, V + from, run * sizeof(float),
+                                           cudaMemcpyDeviceToDevice, ctx->stream), "warm V"));
+    at += run;
+    i = j;
+  }
+  *warm = out;
   return MSQ_OK;
 }
 
@@ -710,8 +772,14 @@ extern "C" int msq_solve_batched(msq_ctx *ctx, const float *a, const int32_t *n,
   const std::vector<double> plan_res = final_res;
   if (!retry.members.empty()) {
     int applied = 0;
+    // the fallback's Jacobi continues from the plan pass's rotations (a plan
+    // stops its Jacobi at 1e-2 or 1e-3, so a few FP32 sweeps reach 1e-7
+    // instead of a full solve from A)
+    const float *warm = nullptr;
+    MSQ_TRY(warmStart(ctx, n, count, groups, passes[0].low_bit, retry.members, &warm));
     MSQ_TRY(runFallback(ctx, a, n, offset, retry, root, tolerance,
-                        kFallbackSweeps - fallback_plan.sweeps, final_res, jsweeps, &applied));
+                        kFallbackSweeps - fallback_plan.sweeps, final_res, jsweeps, &applied,
+                        warm));
     for (int m : retry.members) {
       fallback[m] = 1;
       corrections[m] = applied;

@@ -13,10 +13,14 @@ bool jacobiCapturable(msq_ctx *ctx, const DeviceBatch *b, bool low_bit_basis);
 // automatic eigenvector mode may accumulate V on the tensor cores.
 // tols_device / tols_host: optional per-matrix tolerances (device for the
 // batched kernels, host for the grid path), replacing `tolerance`.
+// keep_vectors: `vectors` already holds the accumulated rotations of an
+// earlier solve whose rotated matrix is `matrices` (the solve continues from
+// there instead of starting from the identity).
 int jacobiEnqueue(msq_ctx *ctx, const DeviceBatch *b, float *matrices, float *vectors,
                   float *eigenvalues, double tolerance, int max_sweeps,
                   int32_t *sweeps_done, float *off_ratio, bool low_bit_basis,
-                  const double *tols_device = nullptr, const double *tols_host = nullptr);
+                  const double *tols_device = nullptr, const double *tols_host = nullptr,
+                  bool keep_vectors = false);
 
 // msq_tc.cu — tcgen05 reconstruction X = W W^T from the FP32 factor F = W^T
 // (quantized to `format` on the fly) or from already encoded flat codes.

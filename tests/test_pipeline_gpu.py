@@ -219,3 +219,48 @@ def test_solve_tiny_orders(ctx, msq):
     torch.cuda.synchronize()
     for m, x in zip(mats, b.unpack(root.cpu().numpy())):
         assert O.relative_residual(m, x) < 1e-6
+
+
+def test_measured_fp32_fma_rate_is_plausible(ctx):
+    """msq_fma_rate (the measured denominator of the Jacobi kernels' FP32
+    roofline): a GB300 runs 152 SMs x 128 FMA lanes, so between a third of
+    and the nominal 2 x 152 x 128 x 2.07 GHz = 80.5 TFLOP/s."""
+    rate = ctx.fma_rate()
+    assert 25.0 < rate < 85.0, rate
+
+
+@pytest.mark.parametrize("vectors_mode", [-1, 2])
+def test_fallback_continues_the_plan_rotations(ctx, msq, vectors_mode):
+    """A miss falls back to the FP32 path, whose Jacobi continues from the
+    plan pass's rotated matrix and rotations (batched kernels, and the grid
+    kernels for the order-1100 matrix): the roots meet the tolerance, agree
+    with the FP32 path's, and the sweeps reported are both passes' together.
+    With the tensor-core eigenvector mode (2) the 256 < n <= 512 matrices'
+    basis is not FP32 accurate, so that fallback restarts from A."""
+    import torch
+    orders = [48, 130, 256, 300, 500, 700, 1100]
+    mats = [O.spd_loguniform(n, 1e3, 700 + i) for i, n in enumerate(orders)]
+    b = _batch(msq, mats)
+    a = _dev(b.pack(mats))
+    tol = 1e-6
+    lossy = [msq.plan(msq.PLAN_MXFP4, 0, 1e-2, 15)] * b.count
+    ctx.set_jacobi_vectors(vectors_mode)
+    try:
+        root, res = ctx.solve_batched(a, b, lossy, tolerance=tol)
+        root_fp32, res_fp32 = ctx.solve_batched(
+            a, b, [msq.plan(msq.PLAN_FP32, 1, 1e-7, 20)] * b.count, tolerance=tol)
+        torch.cuda.synchronize()
+    finally:
+        ctx.set_jacobi_vectors(-1)
+    xs = b.unpack(root.cpu().numpy())
+    xs_fp32 = b.unpack(root_fp32.cpu().numpy())
+    for i, (m, x, xf) in enumerate(zip(mats, xs, xs_fp32)):
+        r = res[i]
+        assert r.fallback and not r.accepted, i
+        assert r.plan_residual > tol
+        assert r.final_residual <= tol, (i, r.final_residual)
+        assert O.relative_residual(m, x) <= max(2 * r.final_residual, 2e-6)
+        assert O.relative_error(x, xf) < 1e-4, i
+        # the plan's sweeps to 1e-2 plus the continuation to 1e-7: no more
+        # than a cold FP32 solve needs, give or take the stopping sweep
+        assert r.jacobi_sweeps <= res_fp32[i].jacobi_sweeps + 2, (i, r.jacobi_sweeps)
