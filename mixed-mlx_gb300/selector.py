@@ -50,7 +50,8 @@ def load(msq, torch, ctx, path):
     selector.mean = torch.from_numpy(w["mean"]).cuda()
     selector.std = torch.from_numpy(w["std"]).cuda()
     meta = json.loads(str(w["metadata"])) if "metadata" in w.files else {}
-    secs = meta.get("train", {}).get("plan_seconds")
+    train = meta.get("train", {})
+    secs = train.get("plan_seconds_probe", train.get("plan_seconds"))
     selector.cost_order = cost_order(secs) if secs else [int(k) for k in w["cost_order"]]
     return selector, float(w["threshold"][0]), meta
 
@@ -133,16 +134,17 @@ class Outcomes:
     seconds: np.ndarray   # [8] GPU seconds per plan for the whole set
 
 
-def score_plans(ctx, msq, torch, batch, flat, tolerance: float) -> Outcomes:
-    """Runs every plan on every matrix; records which plans met the tolerance
-    on their own (the plan's final float-float residual) and the GPU time
-    each plan took.  The solve runs with a tolerance every plan meets (1e30),
-    so no fallback spends time on the misses; the plan's own residual is
-    compared with `tolerance` here."""
+def score_plans(ctx, msq, torch, batch, flat, tolerance: float, plans_run=None) -> Outcomes:
+    """Runs every plan (or those in `plans_run`; the others score 0 and 0 s)
+    on every matrix; records which plans met the tolerance on their own (the
+    plan's final float-float residual) and the GPU time each plan took.  The
+    solve runs with a tolerance every plan meets (1e30), so no fallback
+    spends time on the misses; the plan's own residual is compared with
+    `tolerance` here."""
     acc = np.zeros((batch.count, len(PLANS)), dtype=np.float32)
     secs = np.zeros(len(PLANS))
     out = torch.empty_like(flat)
-    for k in range(len(PLANS)):
+    for k in (range(len(PLANS)) if plans_run is None else plans_run):
         plans = plan_structs(msq, [k] * batch.count)
         start, end = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         start.record()

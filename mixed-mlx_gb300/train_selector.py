@@ -6,11 +6,16 @@ Training data: SPD matrices of three spectrum families (log-uniform,
 clustered, power law i^-2), n log-uniform in [--n-lo, --n-hi] (default
 [64, 2048]), condition log-uniform in [1e1, 1e8], plus --wishart Wishart
 covariances (n log-uniform in [16, 512], the batched workload's family);
-every plan is run on every
-matrix by msq_solve_batched and scored by its own float-float residual at the
-tolerance.  Orders up to 1024 are solved in batches of 1024; each order above
-1024 takes the whole GPU (grid eigensolver), so of those only the first
---max-large drawn are run (the count is recorded).  The network is trained by
+every plan is run by msq_solve_batched and scored by its own float-float
+residual at the tolerance.  Every plan runs on the first --probe matrices
+(the Wishart set first); a plan that met the tolerance on none of them is
+not run on the rest and scores 0 there (at 1e-5 the plans without a
+correction, and FP8 / MXFP4 with one, never do: the quantization error of
+X0 is above the tolerance), and the plan costs come from the probe, where
+every plan ran on the same matrices.  Orders up to 1024 are solved in
+batches of 1024; each order above 1024 takes the whole GPU (grid
+eigensolver), so of those only the first --max-large drawn are run (the
+count is recorded).  The network is trained by
 the library's CUDA kernels (msq_mlp_backward / msq_mlp_step).  Then held-out
 seeds (--test, drawn the same way) are solved with the selected plans and
 with the FP32 path alone; accept rate, fallback rate, met-tolerance rate and
@@ -50,14 +55,17 @@ def chunks(orders, size: int):
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--train", type=int, default=12288)
+    ap.add_argument("--train", type=int, default=200_000)
+    ap.add_argument("--probe", type=int, default=8192,
+                    help="matrices on which every plan runs (plans that never meet the "
+                         "tolerance there are not run on the rest)")
     ap.add_argument("--test", type=int, default=20480)
     ap.add_argument("--tol", type=float, default=1e-5)
-    ap.add_argument("--epochs", type=int, default=150)
+    ap.add_argument("--epochs", type=int, default=40)
     ap.add_argument("--threshold", type=float, default=0.9)
     ap.add_argument("--n-lo", type=int, default=64)
     ap.add_argument("--n-hi", type=int, default=2048)
-    ap.add_argument("--max-large", type=int, default=128,
+    ap.add_argument("--max-large", type=int, default=512,
                     help="orders above 1024 run per set (each takes the whole GPU)")
     ap.add_argument("--wishart", type=int, default=4096,
                     help="Wishart covariances (n in [16, 512]) added to the training set")
@@ -70,33 +78,48 @@ def main():
     t_start = time.time()
 
     small, large, drawn_large = draw_orders(args.train, 1000, args.n_lo, args.n_hi, args.max_large)
-    chunks_f, chunks_y, secs = [], [], np.zeros(len(sel.PLANS))
+    chunks_f, chunks_y = [], []
+    secs = np.zeros(len(sel.PLANS))        # every plan, probe matrices only
+    secs_all = np.zeros(len(sel.PLANS))    # whatever ran
+    probe_acc = np.zeros(len(sel.PLANS))
+    state = {"scored": 0, "run": list(range(len(sel.PLANS)))}
+
+    def score(orders, mats):
+        batch, flat = sel.pack(msq, torch, orders, mats)
+        chunks_f.append(sel.features(ctx, torch, batch, flat, args.tol))
+        probing = state["scored"] < args.probe
+        out = sel.score_plans(ctx, msq, torch, batch, flat, args.tol,
+                              None if probing else state["run"])
+        chunks_y.append(torch.from_numpy(out.accepted).cuda())
+        secs_all[:] += out.seconds
+        if probing:
+            secs[:] += out.seconds
+            probe_acc[:] += out.accepted.sum(0)
+        state["scored"] += batch.count
+        if probing and state["scored"] >= args.probe:
+            state["run"] = [k for k in range(len(sel.PLANS)) if probe_acc[k] > 0]
+        del flat
+
+    for c, start in enumerate(range(0, args.wishart, 1024)):
+        orders, mats = sel.generate_wishart(torch, min(1024, args.wishart - start), seed=30_000 + c)
+        score(orders, mats)
+        del mats
     for part, size in ((small, 1024), (large, 16)):
         for c, (start, orders) in enumerate(chunks(part, size)):
             if len(orders) == 0:
                 continue
             seed = 10_000 * (1 + (part is large)) + c
             _, mats = sel.generate(torch, len(orders), seed=seed, orders=orders)
-            batch, flat = sel.pack(msq, torch, orders, mats)
-            chunks_f.append(sel.features(ctx, torch, batch, flat, args.tol))
-            out = sel.score_plans(ctx, msq, torch, batch, flat, args.tol)
-            chunks_y.append(torch.from_numpy(out.accepted).cuda())
-            secs += out.seconds
-            del mats, flat
-    for c, start in enumerate(range(0, args.wishart, 1024)):
-        orders, mats = sel.generate_wishart(torch, min(1024, args.wishart - start), seed=30_000 + c)
-        batch, flat = sel.pack(msq, torch, orders, mats)
-        chunks_f.append(sel.features(ctx, torch, batch, flat, args.tol))
-        out = sel.score_plans(ctx, msq, torch, batch, flat, args.tol)
-        chunks_y.append(torch.from_numpy(out.accepted).cuda())
-        secs += out.seconds
-        del mats, flat
+            score(orders, mats)
+            del mats
     feats = torch.cat(chunks_f)
     targets = torch.cat(chunks_y)
     selector = sel.Selector(msq, torch, ctx, seed=0)
     selector.cost_order = sel.cost_order(secs)
     losses = selector.fit(feats, targets, epochs=args.epochs)
     t_train = time.time() - t_start
+    save(args, selector, {"train": {"matrices": int(small.size + large.size), "drawn": args.train,
+                                    "seconds": t_train, "plan_seconds_probe": secs.tolist()}})
 
     # held-out seeds: selected plans against the FP32 path alone
     small_t, large_t, drawn_large_t = draw_orders(args.test, 999_999, args.n_lo, args.n_hi,
@@ -139,8 +162,12 @@ def main():
                         "above_1024_drawn": drawn_large, "above_1024_run": int(large.size),
                         "n": [args.n_lo, args.n_hi], "cond": [1e1, 1e8],
                         "families": ["log-uniform", "clustered", "power law i^-2"],
-                        "loss_first_last": [losses[0], losses[-1]],
-                        "plan_seconds": secs.tolist(), "seconds": t_train},
+                        "loss_first_last": [losses[0], losses[-1]], "epochs": args.epochs,
+                        "probe": int(min(state["scored"], max(args.probe, 1))),
+                        "probe_accept_rate": (probe_acc / max(1, min(state["scored"], args.probe))).tolist(),
+                        "plans_run_after_probe": state["run"],
+                        "plan_seconds_probe": secs.tolist(),
+                        "plan_seconds_all": secs_all.tolist(), "seconds": t_train},
               "held_out": {"matrices": int(small_t.size + large_t.size), "drawn": args.test,
                            "above_1024_drawn": drawn_large_t, "above_1024_run": int(large_t.size),
                            "tolerance": args.tol, "threshold": args.threshold,
@@ -155,11 +182,17 @@ def main():
             "met_tolerance": t["met"] / t["count"]}
     report["held_out"]["speedup_vs_fp32_path"] = (report["held_out"]["selector"]["solves_per_s"] /
                                                   report["held_out"]["fp32_path"]["solves_per_s"])
+    save(args, selector, report)
+    print(json.dumps(report))
+
+
+def save(args, selector, report):
+    """Weights, normalisation, plan order and the report (written once after
+    training and again with the held-out results)."""
     np.savez(args.out, params=selector.params.cpu().numpy(), mean=selector.mean.cpu().numpy(),
              std=selector.std.cpu().numpy(), cost_order=np.array(selector.cost_order),
              tol=np.array([args.tol]), threshold=np.array([args.threshold]),
              metadata=np.array(json.dumps(report)))
-    print(json.dumps(report))
 
 
 if __name__ == "__main__":
