@@ -125,6 +125,27 @@ def test_large_2p26_roundtrip_properties(ctx, fmt):
     np.testing.assert_array_equal(d[sel].cpu().numpy().view(np.uint32), od.view(np.uint32))
 
 
+@pytest.mark.parametrize("dist", ["normal", "student_t3"])
+def test_mxfp4_2p26_full_tensor_bit_exact(ctx, dist):
+    """The MXFP4 round trip at 2^26 elements (E2M1 codes, one E8M0 scale per
+    32): every code, scale and decoded value equals the oracle's, for N(0,1)
+    and heavy-tailed Student-t(3) tensors."""
+    import torch
+    n = 1 << 26
+    rng = np.random.default_rng(26 + (dist == "student_t3"))
+    x = (rng.standard_normal(n) if dist == "normal" else rng.standard_t(3, n)).astype(np.float32)
+    fmt = 7  # MXFP4_E2M1
+    t = torch.from_numpy(x).cuda()
+    v, s = ctx.copy_to_storage(fmt, t)
+    d = ctx.storage_values(fmt, v, s, n)
+    torch.cuda.synchronize()
+    ov, os_ = O.encode(fmt, x)
+    np.testing.assert_array_equal(v.cpu().numpy()[:ov.size], ov)
+    np.testing.assert_array_equal(s.cpu().numpy()[:os_.size], os_)
+    od = O.decode(fmt, ov, os_, n)
+    np.testing.assert_array_equal(d.cpu().numpy().view(np.uint32), od.view(np.uint32))
+
+
 def test_misaligned_pointers_fall_back_to_scalar_path(ctx):
     import torch
     x = torch.randn(1001, device="cuda")
