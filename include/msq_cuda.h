@@ -356,9 +356,9 @@ int msq_sylvester_sweep(msq_ctx *ctx, int gemm_format, const float *vectors,
  * basis V and transposed basis V^T (stored separately, as the reference
  * stores them); spectrum: the decoded root eigenvalues s (sum(n) floats,
  * matrix i at the prefix sum of n).  workspace: 3 * E floats, E = max over
- * matrices of offset + n^2; codes / scales: msq_storage_bytes(format, n^2)
- * and msq_scale_bytes(format, n^2, n) bytes for the largest n (16-byte
- * aligned; unused for MSQ_FMT_FP32).                                      */
+ * matrices of offset + n^2.  Every step runs over the whole batch in one
+ * launch (the quantizer round-trips each matrix in place); codes / scales
+ * are not used and may be NULL.                                           */
 int msq_native_sylvester_sweep(msq_ctx *ctx, int format, const float *vectors,
                                const float *vectors_t, const float *spectrum,
                                const float *residual, const int32_t *n,

@@ -384,15 +384,11 @@ class Context:
         in `fmt`); v / vt: decoded stored V and V^T, s: decoded root
         eigenvalues (sum of n floats); updates x_hi / x_lo."""
         torch = self.torch
-        big = int(max(batch.n)) ** 2
         workspace = torch.empty(3 * batch.total, dtype=torch.float32, device=v.device)
-        codes = torch.empty(max(storage_bytes(fmt, big), 16) + 16, dtype=torch.uint8, device=v.device)
-        scales = torch.empty(max(scale_bytes(fmt, big, int(max(batch.n))), 16) + 16,
-                             dtype=torch.uint8, device=v.device)
         self.check(lib().msq_native_sylvester_sweep(
             self.handle, fmt, _ptr(v), _ptr(vt), _ptr(s), _ptr(r), batch.n.ctypes.data,
             batch.offset.ctypes.data, batch.count, _ptr(x_hi), _ptr(x_lo), _ptr(workspace),
-            _ptr(codes), _ptr(scales)), "msq_native_sylvester_sweep")
+            None, None), "msq_native_sylvester_sweep")
 
     def sylvester_sweep(self, gemm_fmt: int, v, w, r, batch: Batch, x_hi, x_lo, workspace=None):
         if workspace is None:

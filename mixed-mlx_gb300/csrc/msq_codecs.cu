@@ -11,6 +11,8 @@
 #include "msq_codec_device.cuh"
 #include "msq_internal.cuh"
 
+#include <algorithm>
+
 namespace msq {
 namespace {
 
@@ -587,7 +589,127 @@ spectrumDecodeKernel(const uint8_t *__restrict__ values, const float2 *__restric
   }
 }
 
+// Q(x) = decode(encode(x)) in place for every matrix of a batch, one
+// launch: the per-element steps of the encode and decode kernels above,
+// with MX blocks of 32 consecutive elements and scale rows of n elements
+// taken within each matrix (n^2 elements from its offset), so the result is
+// the encode -> decode round trip of each matrix on its own.
+template <int kFormat>
+__global__ void __launch_bounds__(kThreads)
+quantizeBatchKernel(float *__restrict__ x, const int64_t *__restrict__ offset,
+                    const int32_t *__restrict__ n, int count) {
+  constexpr bool kMx = kFormat == MSQ_FMT_MXFP8_E4M3FN || kFormat == MSQ_FMT_MXFP8_E5M2 ||
+                       kFormat == MSQ_FMT_MXFP4_E2M1;
+  constexpr int kEmax = kFormat == MSQ_FMT_MXFP8_E4M3FN ? 8 : kFormat == MSQ_FMT_MXFP8_E5M2 ? 15 : 2;
+  for (int mi = blockIdx.y; mi < count; mi += gridDim.y) {
+    const int nn = n[mi];
+    const int64_t elements = static_cast<int64_t>(nn) * nn;
+    float *p = x + offset[mi];
+    if constexpr (kFormat == MSQ_FMT_FP8_E4M3FN_ROWSCALE) {
+      // one warp per row of n consecutive elements (encodeRowScaleKernel)
+      const int lane = threadIdx.x % 32;
+      const int warps = gridDim.x * (blockDim.x / 32);
+      for (int row = blockIdx.x * (blockDim.x / 32) + threadIdx.x / 32; row < nn; row += warps) {
+        float *in = p + static_cast<int64_t>(row) * nn;
+        float m = 0.0f;
+        for (int i = lane; i < nn; i += 32) {
+          const float a = fabsf(in[i]);
+          if (a <= 3.402823466e38f) m = fmaxf(m, a);
+        }
+#pragma unroll
+        for (int sh = 16; sh > 0; sh >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, sh));
+        const float scale = m == 0.0f ? 1.0f : __fdiv_rn(m, 448.0f);
+        for (int i = lane; i < nn; i += 32)
+          in[i] = rowScaleDecode(decodeE4M3(encodeE4M3(rowDivide(in[i], scale))), scale);
+      }
+    } else if constexpr (kMx) {
+      // one thread per 32-element block (encodeMxKernel / decodeKernel)
+      const int64_t blocks = (elements + 31) / 32;
+      for (int64_t blk = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; blk < blocks;
+           blk += static_cast<int64_t>(gridDim.x) * blockDim.x) {
+        const int64_t base = blk * 32;
+        float v[32];
+        float m = 0.0f;
+#pragma unroll
+        for (int i = 0; i < 32; ++i) {
+          v[i] = base + i < elements ? p[base + i] : 0.0f;
+          const float a = fabsf(v[i]);
+          if (a <= 3.402823466e38f) m = fmaxf(m, a);  // finite only (NaN fails)
+        }
+        const int e = mxExponent(m, kEmax);
+        const uint32_t scale = static_cast<uint32_t>(e + 127);
+        if constexpr (kFormat == MSQ_FMT_MXFP4_E2M1) {
+          const bool exact = e >= -126 && e <= 126;
+          const float sc = exact ? exp2Int(-e) : 1.0f;
+#pragma unroll
+          for (int i = 0; i < 32; i += 2) {
+            uint32_t pair;
+            if (exact) {
+              pair = encodeE2M1Pair(v[i] * sc, v[i + 1] * sc, v[i], v[i + 1]);
+            } else {
+              const float a = mxDivide(v[i], e), b = mxDivide(v[i + 1], e);
+              pair = encodeE2M1Pair(a, b, a, b);
+            }
+            v[i] = mxScale(decodeE2M1(pair & 0xfu), scale);
+            v[i + 1] = mxScale(decodeE2M1((pair >> 4) & 0xfu), scale);
+          }
+        } else {
+#pragma unroll
+          for (int i = 0; i < 32; ++i) {
+            const float scaled = mxDivide(v[i], e);
+            const float d = kFormat == MSQ_FMT_MXFP8_E4M3FN ? decodeE4M3(encodeE4M3(scaled))
+                                                            : decodeE5M2(encodeE5M2(scaled));
+            v[i] = mxScale(d, scale);
+          }
+        }
+#pragma unroll
+        for (int i = 0; i < 32; ++i)
+          if (base + i < elements) p[base + i] = v[i];
+      }
+    } else {
+      for (int64_t i = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; i < elements;
+           i += static_cast<int64_t>(gridDim.x) * blockDim.x) {
+        const float y = p[i];
+        if constexpr (kFormat == MSQ_FMT_BF16) p[i] = decodeBf16(encodeBf16(y));
+        else if constexpr (kFormat == MSQ_FMT_FP8_E4M3FN) p[i] = decodeE4M3(encodeE4M3(y));
+        else if constexpr (kFormat == MSQ_FMT_FP8_E5M2) p[i] = decodeE5M2(encodeE5M2(y));
+        else p[i] = decodeE2M1(encodeE2M1(y));  // FP4 E2M1
+      }
+    }
+  }
+}
+
 }  // namespace
+
+int quantizeBatch(msq_ctx *ctx, int format, const DeviceBatch *b, float *x) {
+  if (format == MSQ_FMT_FP32) return MSQ_OK;
+  const int64_t nn = static_cast<int64_t>(b->max_n) * b->max_n;
+  int64_t units = nn;                                               // elements
+  if (format == MSQ_FMT_FP8_E4M3FN_ROWSCALE) units = static_cast<int64_t>(b->max_n) * 32;  // a warp per row
+  else if (format == MSQ_FMT_MXFP8_E4M3FN || format == MSQ_FMT_MXFP8_E5M2 ||
+           format == MSQ_FMT_MXFP4_E2M1) units = (nn + 31) / 32;   // a thread per block
+  const dim3 grid(static_cast<unsigned>(std::max<int64_t>(1, std::min<int64_t>((units + kThreads - 1) / kThreads, 64))),
+                  static_cast<unsigned>(std::min(b->count, 65535)));
+  switch (format) {
+#define MSQ_QUANTIZE_CASE(F)                                                                   \
+    case F:                                                                                   \
+      quantizeBatchKernel<F><<<grid, kThreads, 0, ctx->stream>>>(x, b->offset, b->n, b->count); \
+      break;
+    MSQ_QUANTIZE_CASE(MSQ_FMT_BF16)
+    MSQ_QUANTIZE_CASE(MSQ_FMT_FP8_E4M3FN)
+    MSQ_QUANTIZE_CASE(MSQ_FMT_FP8_E5M2)
+    MSQ_QUANTIZE_CASE(MSQ_FMT_MXFP8_E4M3FN)
+    MSQ_QUANTIZE_CASE(MSQ_FMT_MXFP8_E5M2)
+    MSQ_QUANTIZE_CASE(MSQ_FMT_FP4_E2M1)
+    MSQ_QUANTIZE_CASE(MSQ_FMT_MXFP4_E2M1)
+    MSQ_QUANTIZE_CASE(MSQ_FMT_FP8_E4M3FN_ROWSCALE)
+#undef MSQ_QUANTIZE_CASE
+    default:
+      return setError(ctx, MSQ_ERR_INVALID_ARGUMENT, "quantize: unknown format");
+  }
+  return launched(ctx, "quantize");
+}
+
 }  // namespace msq
 
 using namespace msq;

@@ -501,6 +501,33 @@ matmulFmaKernel(const float *__restrict__ a, const float *__restrict__ b, float 
   if (row < n && col < n) c[row + static_cast<int64_t>(col) * n] = sum;
 }
 
+// The same product for every matrix of a batch: one CTA per 16 x 16 output
+// tile of a (matrix, tile_i, tile_j) work list, the same FMA chains.
+__global__ void __launch_bounds__(kMmTile * kMmTile)
+matmulFmaBatchKernel(const float *__restrict__ a, const float *__restrict__ b, float *__restrict__ c,
+                     const int64_t *__restrict__ offset, const int32_t *__restrict__ n,
+                     const int4 *__restrict__ work, int items) {
+  __shared__ float as[kMmTile][kMmTile + 1];
+  __shared__ float bs[kMmTile][kMmTile + 1];
+  const int tr = threadIdx.x, tc = threadIdx.y;
+  for (int item = blockIdx.x; item < items; item += gridDim.x) {
+    const int4 w = work[item];
+    const int nn = n[w.x];
+    const int64_t o = offset[w.x];
+    const int row = w.y * kMmTile + tr, col = w.z * kMmTile + tc;
+    float sum = 0.0f;
+    for (int k0 = 0; k0 < nn; k0 += kMmTile) {
+      as[tr][tc] = row < nn && k0 + tc < nn ? a[o + row + static_cast<int64_t>(k0 + tc) * nn] : 0.0f;
+      bs[tr][tc] = k0 + tr < nn && col < nn ? b[o + (k0 + tr) + static_cast<int64_t>(col) * nn] : 0.0f;
+      __syncthreads();
+      const int kend = min(kMmTile, nn - k0);
+      for (int k = 0; k < kend; ++k) sum = fmaf(as[tr][k], bs[k][tc], sum);
+      __syncthreads();
+    }
+    if (row < nn && col < nn) c[o + row + static_cast<int64_t>(col) * nn] = sum;
+  }
+}
+
 // C_ij = W_ij / (s_i + s_j) (diagonal_sylvester_*, metal_mixed_sqrt.metal:58-74).
 __global__ void diagonalSylvesterKernel(const float *__restrict__ w, const float *__restrict__ s,
                                         float *__restrict__ c, int n) {
@@ -511,7 +538,43 @@ __global__ void diagonalSylvesterKernel(const float *__restrict__ w, const float
     c[idx] = __fdiv_rn(w[idx], s[i] + s[j]);
   }
 }
+// The same for every matrix of a batch (grid.y = matrix); s of matrix i at
+// eig_offset[i].
+__global__ void diagonalSylvesterBatchKernel(const float *__restrict__ w, const float *__restrict__ s,
+                                             float *__restrict__ c, const int64_t *__restrict__ offset,
+                                             const int64_t *__restrict__ eig_offset,
+                                             const int32_t *__restrict__ n, int count) {
+  for (int mi = blockIdx.y; mi < count; mi += gridDim.y) {
+    const int nn = n[mi];
+    const int64_t total = static_cast<int64_t>(nn) * nn, o = offset[mi];
+    const float *sm = s + eig_offset[mi];
+    for (int64_t idx = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; idx < total;
+         idx += static_cast<int64_t>(gridDim.x) * blockDim.x) {
+      const int i = static_cast<int>(idx % nn), j = static_cast<int>(idx / nn);
+      c[o + idx] = __fdiv_rn(w[o + idx], sm[i] + sm[j]);
+    }
+  }
+}
 }  // namespace
+
+int matmulFmaBatch(msq_ctx *ctx, const DeviceBatch *b, const float *a, const float *bm, float *c) {
+  const int4 *work = nullptr;
+  int items = 0;
+  MSQ_TRY(gemmWork(ctx, b, kMmTile, &work, &items));
+  matmulFmaBatchKernel<<<std::min(items, kSmCount * 16), dim3(kMmTile, kMmTile), 0, ctx->stream>>>(
+      a, bm, c, b->offset, b->n, work, items);
+  return launched(ctx, "native matmul");
+}
+
+int diagonalSylvesterBatch(msq_ctx *ctx, const DeviceBatch *b, const float *w, const float *s,
+                           float *c) {
+  const int64_t nn = static_cast<int64_t>(b->max_n) * b->max_n;
+  const dim3 grid(static_cast<unsigned>(std::max<int64_t>(1, std::min<int64_t>((nn + 255) / 256, 64))),
+                  static_cast<unsigned>(std::min(b->count, 65535)));
+  diagonalSylvesterBatchKernel<<<grid, 256, 0, ctx->stream>>>(w, s, c, b->offset, b->eig_offset,
+                                                              b->n, b->count);
+  return launched(ctx, "native diagonal sylvester");
+}
 
 int matmulFma(msq_ctx *ctx, const float *a, const float *b, float *c, int n) {
   const dim3 grid((n + kMmTile - 1) / kMmTile, (n + kMmTile - 1) / kMmTile);

@@ -54,5 +54,9 @@ int workingAdd(msq_ctx *ctx, const DeviceBatch *b, float *x_hi, float *x_lo, con
 // One n x n matrix: C = A B with in-order FMA chains; C_ij = W_ij / (s_i + s_j).
 int matmulFma(msq_ctx *ctx, const float *a, const float *b, float *c, int n);
 int diagonalSylvester(msq_ctx *ctx, const float *w, const float *s, float *c, int n);
+// The same for every matrix of a batch in one launch (s at eig_offset).
+int matmulFmaBatch(msq_ctx *ctx, const DeviceBatch *b, const float *a, const float *bm, float *c);
+int diagonalSylvesterBatch(msq_ctx *ctx, const DeviceBatch *b, const float *w, const float *s,
+                           float *c);
 
 }  // namespace msq

@@ -186,41 +186,31 @@ extern "C" int msq_native_sylvester_sweep(msq_ctx *ctx, int format, const float 
     return setError(ctx, MSQ_ERR_INVALID_ARGUMENT, "msq_native_sylvester_sweep: null buffer");
   if (format < MSQ_FMT_FP32 || format > MSQ_FMT_FP8_E4M3FN_ROWSCALE)
     return setError(ctx, MSQ_ERR_INVALID_ARGUMENT, "msq_native_sylvester_sweep: unknown format");
-  if (format != MSQ_FMT_FP32 && codes == nullptr)
-    return setError(ctx, MSQ_ERR_INVALID_ARGUMENT, "msq_native_sylvester_sweep: null code buffer");
+  (void)codes;  // the quantizer round-trips in place; no code buffers needed
+  (void)scales;
   const DeviceBatch *b = prepareBatch(ctx, n, offset, count);
   if (b == nullptr) return MSQ_ERR_INVALID_ARGUMENT;
   int64_t extent = 0;
   for (int i = 0; i < b->count; ++i)
     extent = std::max(extent, b->host_offset[i] + static_cast<int64_t>(b->host_n[i]) * b->host_n[i]);
   float *rq = workspace, *w1 = workspace + extent, *w2 = workspace + 2 * extent;
-  for (int i = 0; i < b->count; ++i) {
-    const int m = b->host_n[i];
-    const int64_t o = b->host_offset[i];
-    const size_t elements = static_cast<size_t>(m) * m;
-    const size_t row_length = format == MSQ_FMT_FP8_E4M3FN_ROWSCALE ? m : 0;
-    // Q(x): x quantized to `format` (nearest, per matrix) and decoded in place
-    auto quantize = [&](float *x) -> int {
-      if (format == MSQ_FMT_FP32) return MSQ_OK;
-      MSQ_TRY(msq_encode(ctx, format, x, elements, row_length, codes, scales));
-      return msq_decode(ctx, format, codes, scales, elements, row_length, x);
-    };
-    const float *v = vectors + o, *vt = vectors_t + o;
-    MSQ_TRY(cudaCheck(ctx, cudaMemcpyAsync(rq + o, residual + o, elements * sizeof(float),
-                                           cudaMemcpyDeviceToDevice, ctx->stream),
-                      "native residual copy"));
-    MSQ_TRY(quantize(rq + o));                                       // R in the format
-    MSQ_TRY(matmulFma(ctx, vt, rq + o, w1 + o, m));                  // W1 = V^T R
-    MSQ_TRY(quantize(w1 + o));
-    MSQ_TRY(matmulFma(ctx, w1 + o, v, w2 + o, m));                   // W2 = W1 V
-    MSQ_TRY(quantize(w2 + o));
-    MSQ_TRY(diagonalSylvester(ctx, w2 + o, spectrum + b->host_eig_offset[i], w1 + o, m));  // C
-    MSQ_TRY(quantize(w1 + o));
-    MSQ_TRY(matmulFma(ctx, v, w1 + o, w2 + o, m));                   // W1' = V C
-    MSQ_TRY(quantize(w2 + o));
-    MSQ_TRY(matmulFma(ctx, w2 + o, vt, w1 + o, m));                  // E = W1' V^T
-    MSQ_TRY(quantize(w1 + o));
-  }
+  // Every matrix of the batch per launch; Q(x) quantizes each matrix to
+  // `format` (nearest, per matrix; row length n for the row-scaled format)
+  // and decodes it in place.
+  MSQ_TRY(cudaCheck(ctx, cudaMemcpyAsync(rq, residual, extent * sizeof(float),
+                                         cudaMemcpyDeviceToDevice, ctx->stream),
+                    "native residual copy"));
+  MSQ_TRY(quantizeBatch(ctx, format, b, rq));                     // R in the format
+  MSQ_TRY(matmulFmaBatch(ctx, b, vectors_t, rq, w1));              // W1 = V^T R
+  MSQ_TRY(quantizeBatch(ctx, format, b, w1));
+  MSQ_TRY(matmulFmaBatch(ctx, b, w1, vectors, w2));                // W2 = W1 V
+  MSQ_TRY(quantizeBatch(ctx, format, b, w2));
+  MSQ_TRY(diagonalSylvesterBatch(ctx, b, w2, spectrum, w1));       // C
+  MSQ_TRY(quantizeBatch(ctx, format, b, w1));
+  MSQ_TRY(matmulFmaBatch(ctx, b, vectors, w1, w2));                // W1' = V C
+  MSQ_TRY(quantizeBatch(ctx, format, b, w2));
+  MSQ_TRY(matmulFmaBatch(ctx, b, w2, vectors_t, w1));              // E = W1' V^T
+  MSQ_TRY(quantizeBatch(ctx, format, b, w1));
   return symmetricAdd(ctx, b, x_hi, x_lo, w1);                       // X += (E + E^T)/2
 }
 

@@ -36,6 +36,10 @@ int sylvesterTc(msq_ctx *ctx, const DeviceBatch *b, const float *v, const float 
 int residualTc(msq_ctx *ctx, const DeviceBatch *b, const float *a, const float *x_hi,
                const float *x_lo, float *r, double *norms);
 
+// msq_codecs.cu — x <- decode(encode(x)) for every matrix of the batch in
+// one launch (MX blocks and scale rows within each matrix).
+int quantizeBatch(msq_ctx *ctx, int format, const DeviceBatch *b, float *x);
+
 // msq_solve.cu
 int sylvesterSweep(msq_ctx *ctx, const DeviceBatch *b, int gemm_format, const float *v,
                    const float *lam, const float *r, float *x_hi, float *x_lo, float *ws0,

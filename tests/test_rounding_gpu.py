@@ -161,3 +161,44 @@ def test_native_correction_equals_the_oracle(ctx, msq, fmt, n):
     want = (np.float32(0.5) * (e + e.T) + np.float32(0.0)).astype(np.float32)
     assert np.array_equal(np.ascontiguousarray(got).view(np.uint32),
                           np.ascontiguousarray(want).view(np.uint32))
+
+
+@pytest.mark.parametrize("fmt", [0, 1, 3, 5, 7, 8])
+def test_native_correction_batched_equals_the_oracle(ctx, msq, fmt):
+    """A batch of uneven orders in one call (each step one launch over the
+    batch; MX blocks and scale rows within each matrix): every matrix equals
+    the oracle's native correction of that matrix alone, bit for bit."""
+    import torch
+    orders = [1, 7, 33, 64, 100, 5]
+    rng = np.random.default_rng(900 + fmt)
+    rl = lambda n: n if fmt == 8 else 0
+
+    def stored(m, n):
+        if fmt == 0:
+            return np.asfortranarray(m, np.float32)
+        flat = np.asfortranarray(m, np.float32).reshape(-1, order="F")
+        return O.decode(fmt, *O.encode(fmt, flat, rl(n)), flat.size, rl(n)).reshape(n, n, order="F")
+
+    vqs, vtqs, ss, rs, want = [], [], [], [], []
+    for n in orders:
+        q, _ = np.linalg.qr(rng.standard_normal((n, n)))
+        v = q.astype(np.float32)
+        vq, vtq = stored(v, n), stored(v.T, n)
+        s = np.exp(rng.uniform(-1, 1, n)).astype(np.float32)
+        r = (1e-3 * rng.standard_normal((n, n))).astype(np.float32)
+        r = np.asfortranarray(0.5 * (r + r.T))
+        e = O.native_correction(fmt, vq, vtq, s, r)
+        vqs.append(vq); vtqs.append(vtq); ss.append(s); rs.append(r)
+        want.append((np.float32(0.5) * (e + e.T) + np.float32(0.0)).astype(np.float32))
+    b = msq.Batch.from_orders(orders)
+    col = lambda ms: torch.from_numpy(b.pack([np.asfortranarray(m, np.float32) for m in ms])).cuda()
+    x_hi = torch.zeros(b.total, dtype=torch.float32, device="cuda")
+    x_lo = torch.zeros_like(x_hi)
+    l0 = ctx.launches
+    ctx.native_sylvester_sweep(fmt, col(vqs), col(vtqs), torch.from_numpy(np.concatenate(ss)).cuda(),
+                               col(rs), b, x_hi, x_lo)
+    ctx.synchronize()
+    assert ctx.launches - l0 <= 13  # one launch per step, whatever the batch size
+    for n, got, w in zip(orders, b.unpack(x_hi.cpu().numpy(), dtype=np.float32), want):
+        assert np.array_equal(np.ascontiguousarray(got).view(np.uint32),
+                              np.ascontiguousarray(w).view(np.uint32)), n
