@@ -299,12 +299,22 @@ __global__ void __launch_bounds__(kTcThreads, 1) tcGemmKernel(TcArgs args) {
       }
       const float *lam = kEpi == kEpiInverseH ? args.eigenvalues + args.eig_offset[mi] : nullptr;
       const float si = kEpi == kEpiInverseH && i < n ? sqrtf(fmaxf(lam[i], 0.0f)) : 0.0f;
+
       const float *A = kEpi == kEpiResidual ? args.a_in + args.x_offset[mi] : nullptr;
       double rn = 0.0, an = 0.0;
 #pragma unroll 1
       for (int c = 0; c < 4; ++c) {
         float v[32];
         tmemLoad32(tmem + ((32u * warp) << 16) + acc * 128 + c * 32, v);
+        // s_j of this chunk's 32 columns: one square root per lane (not one
+        // per element), spread over the warp by shuffles that every lane runs
+        float sj[32];
+        if (kEpi == kEpiInverseH) {
+          const int jl = j0 + c * 32 + lane;
+          const float mine = jl < n ? sqrtf(fmaxf(lam[jl], 0.0f)) : 0.0f;
+#pragma unroll
+          for (int q = 0; q < 32; ++q) sj[q] = __shfl_sync(0xffffffffu, mine, q);
+        }
         if (i < n) {
 #pragma unroll
           for (int q = 0; q < 32; ++q) {
@@ -316,7 +326,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) tcGemmKernel(TcArgs args) {
               // for (i, j) and (j, i), so X stays exactly symmetric
               if (kEpi == kEpiRowScale) val = val * (ri * rs[j]);
               if (kEpi == kEpiInverseH) {
-                const float d = si + sqrtf(fmaxf(lam[j], 0.0f));
+                const float d = si + sj[q];
                 val = d > 0.0f ? val / d : 0.0f;  // both roots 0: no correction
               }
               if (kEpi == kEpiResidual) {
