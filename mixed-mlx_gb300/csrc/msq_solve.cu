@@ -40,10 +40,10 @@ int sylvesterFp32(msq_ctx *ctx, const DeviceBatch *b, const float *v, const floa
 
 int sylvesterSweep(msq_ctx *ctx, const DeviceBatch *b, int gemm_format, const float *v,
                    const float *lam, const float *r, float *x_hi, float *x_lo, float *ws0,
-                   float *ws1) {
+                   float *ws1, bool basis_packed) {
   if (gemm_format == MSQ_FMT_BF16) {
     float *e = nullptr;
-    MSQ_TRY(sylvesterTc(ctx, b, v, lam, r, ws0, ws1, &e));
+    MSQ_TRY(sylvesterTc(ctx, b, v, lam, r, ws0, ws1, &e, basis_packed));
     return symmetricAdd(ctx, b, x_hi, x_lo, e);
   }
   return sylvesterFp32(ctx, b, v, lam, r, x_hi, x_lo, ws0, ws1);
@@ -409,8 +409,10 @@ int enqueuePass(msq_ctx *ctx, const float *a_user, const int32_t *n_user,
     MSQ_TRY(cudaCheck(ctx, cudaMemcpyAsync(rep.initial, norms, 2 * c * sizeof(double),
                                            cudaMemcpyDeviceToHost, ctx->stream), "norms read"));
     for (int s = 0; s < g.plan.sweeps; ++s) {
+      // V's split operands from the previous sweep stay valid: between two
+      // sweeps only the float-float residual runs
       MSQ_TRY(sylvesterSweep(ctx, sb, gemm_format, pb->V, lam, pb->R, pb->Xh, pb->Xl, pb->F,
-                             pb->W1));
+                             pb->W1, s > 0));
       MSQ_TRY(residual(true));
     }
     MSQ_TRY(cudaCheck(ctx, cudaMemcpyAsync(rep.final, norms, 2 * c * sizeof(double),

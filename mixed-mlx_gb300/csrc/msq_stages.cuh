@@ -30,9 +30,13 @@ int reconstructEncoded(msq_ctx *ctx, const DeviceBatch *b, int format, const voi
                        const void *scales, float *x);
 
 // msq_tc.cu — tensor-core Sylvester GEMM chain (the correction is returned in
-// *correction, one of ws0/ws1) and the split-BF16 residual.
+// *correction, one of ws0/ws1) and the split-BF16 residual.  basis_packed:
+// the split operands of V and V^T are still those of the previous chain on
+// the same V and batch (no tensor-core call in between), so they are not
+// packed again.
 int sylvesterTc(msq_ctx *ctx, const DeviceBatch *b, const float *v, const float *lam,
-                const float *r, float *ws0, float *ws1, float **correction);
+                const float *r, float *ws0, float *ws1, float **correction,
+                bool basis_packed = false);
 int residualTc(msq_ctx *ctx, const DeviceBatch *b, const float *a, const float *x_hi,
                const float *x_lo, float *r, double *norms);
 
@@ -43,6 +47,6 @@ int quantizeBatch(msq_ctx *ctx, int format, const DeviceBatch *b, float *x);
 // msq_solve.cu
 int sylvesterSweep(msq_ctx *ctx, const DeviceBatch *b, int gemm_format, const float *v,
                    const float *lam, const float *r, float *x_hi, float *x_lo, float *ws0,
-                   float *ws1);
+                   float *ws1, bool basis_packed = false);
 
 }  // namespace msq

@@ -980,14 +980,16 @@ int gemmSplit2(msq_ctx *ctx, const DeviceBatch *b, TcPlan *p, uint8_t *const *a,
 // The correction is residual-sized, so the ~1e-5 relative error of the
 // two-piece products is far below what the next sweep can see.
 int sylvesterTc(msq_ctx *ctx, const DeviceBatch *b, const float *v, const float *lam,
-                const float *r, float *ws0, float *ws1, float **correction) {
+                const float *r, float *ws0, float *ws1, float **correction, bool basis_packed) {
   TcPlan *p = tcPlan(ctx, b, kOpBf16);
   if (p == nullptr) return MSQ_ERR_CUDA;
   uint8_t *buf[kBuffers];
   if (splitBuffers(ctx, p, buf) == nullptr) return MSQ_ERR_CUDA;
   uint8_t *vn[2] = {buf[0], buf[1]}, *vt[2] = {buf[2], buf[3]}, *op[2] = {buf[4], buf[5]};
-  MSQ_TRY(packSplit(ctx, b, p, v, nullptr, false, 2, vn));  // rows = columns of V
-  MSQ_TRY(packSplit(ctx, b, p, v, nullptr, true, 2, vt));   // rows = rows of V
+  if (!basis_packed) {
+    MSQ_TRY(packSplit(ctx, b, p, v, nullptr, false, 2, vn));  // rows = columns of V
+    MSQ_TRY(packSplit(ctx, b, p, v, nullptr, true, 2, vt));   // rows = rows of V
+  }
   MSQ_TRY(packSplit(ctx, b, p, r, nullptr, false, 2, op));  // R (symmetric)
   MSQ_TRY(gemmSplit2(ctx, b, p, op, vn, kEpiStore, nullptr, ws0, "tc sylvester G=RV"));
   MSQ_TRY(packSplit(ctx, b, p, ws0, nullptr, false, 2, op));
