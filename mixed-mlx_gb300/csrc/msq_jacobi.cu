@@ -646,14 +646,15 @@ jacobiReplayKernel(VArgs args) {
   }
 }
 
+// V = I per matrix (column-major): CTAs over columns, threads down a column
+// (coalesced stores, no per-element division).
 __global__ void identityKernel(float *v, const int64_t *a_offset, const int32_t *n, int count) {
   for (int mi = blockIdx.y; mi < count; mi += gridDim.y) {
-    const int64_t nn = static_cast<int64_t>(n[mi]) * n[mi];
+    const int nn = n[mi];
     float *out = v + a_offset[mi];
-    for (int64_t k = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; k < nn;
-         k += static_cast<int64_t>(gridDim.x) * blockDim.x) {
-      const int64_t r = k % n[mi], c = k / n[mi];
-      out[k] = r == c ? 1.0f : 0.0f;
+    for (int c = blockIdx.x; c < nn; c += gridDim.x) {
+      float *col = out + static_cast<int64_t>(c) * nn;
+      for (int r = threadIdx.x; r < nn; r += blockDim.x) col[r] = r == c ? 1.0f : 0.0f;
     }
   }
 }
@@ -1236,7 +1237,9 @@ int jacobiEnqueue(msq_ctx *ctx, const DeviceBatch *b, float *matrices, float *ve
   auto body = [&]() -> int {
   MSQ_TRY(cudaCheck(ctx, cudaMemsetAsync(args.state, 0, state_bytes, ctx->stream), "state reset"));
   if (!keep_vectors) {
-    dim3 grid(64, std::min(b->count, 65535));
+    // a few CTAs per matrix (most matrices of a batch are small: a wide grid
+    // would be mostly empty CTAs)
+    dim3 grid(std::max(1, std::min(8, b->max_n / 64)), std::min(b->count, 65535));
     identityKernel<<<grid, 256, 0, ctx->stream>>>(vectors, b->offset, b->n, b->count);
     MSQ_TRY(launched(ctx, "jacobi identity"));
   }
