@@ -955,7 +955,7 @@ def main():
         "metric": METRIC, "value": value, "unit": "solves/s", "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_max,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "bf16",
-        "data": "synthetic (seeded Wishart, generated on device)",
+        "data": "synthetic (seeded Wishart, generated on the host, the reference arm's matrices)",
         "config": {"workload": f"{batch.count} Wishart SPD A=X^T X/m+1e-6 I (m=2n), n log-uniform "
                                f"[{N_LO},{N_HI}], FP32 input, low-bit plan + Sylvester sweeps, "
                                f"FP32 fallback, tol 1e-5",
