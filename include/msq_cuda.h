@@ -235,6 +235,13 @@ int msq_set_jacobi_vectors(msq_ctx *ctx, int mode);
  * NULL and capacity >= rounds * blocks, rounds x blocks/2 pairs (I, J) with
  * I < J, J stored as -1 - J for a pair that keeps the identity rotation.   */
 int msq_jacobi_schedule(int blocks, int32_t *pairs, size_t capacity, int *rounds);
+/* Which eigensolver path each matrix of a batch of orders n[count] takes
+ * under eigenvector mode `mode` (MSQ_VECTORS_REPLAY .. MSQ_VECTORS_TENSOR_A;
+ * AUTO resolves to REPLAY for msq_jacobi_batched and the FP32 plans, to
+ * TENSOR for batches of low-bit plans): grid[i] = 1 when matrix i is solved
+ * by the grid kernels with every SM, 0 when by the batched kernels one CTA
+ * each.  Host only (no GPU, no context).                                   */
+int msq_jacobi_route(const int32_t *n, int count, int mode, int32_t *grid);
 
 /* ---- launch-shape autotuner -------------------------------------------------
  * The Jacobi sweep buckets matrices by size class and picks each class's CTA

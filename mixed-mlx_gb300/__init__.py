@@ -98,6 +98,7 @@ _SIGS = {
     "msq_set_jacobi_vectors": (ctypes.c_int, [_P, ctypes.c_int]),
     "msq_jacobi_schedule": (ctypes.c_int, [ctypes.c_int, _P, ctypes.c_size_t,
                                            ctypes.POINTER(ctypes.c_int)]),
+    "msq_jacobi_route": (ctypes.c_int, [_P, ctypes.c_int, ctypes.c_int, _P]),
     "msq_autotune_report": (ctypes.c_int, [ctypes.c_int, ctypes.c_char_p, ctypes.c_size_t]),
     "msq_autotune_reset": (ctypes.c_int, [ctypes.c_int]),
     "msq_timing_begin": (ctypes.c_int, [_P]),
@@ -200,6 +201,18 @@ def jacobi_schedule(blocks: int) -> np.ndarray:
     if status != 0:
         raise MsqError(f"msq_jacobi_schedule({blocks}): status {status}")
     return out.reshape(rounds.value, blocks // 2, 2)
+
+
+def jacobi_route(orders, mode: int = 0) -> np.ndarray:
+    """Which eigensolver path each matrix of a batch takes (host-side, no
+    GPU): 1 = the grid kernels with every SM, 0 = the batched kernels one CTA
+    each, under eigenvector mode `mode` (VECTORS_REPLAY .. VECTORS_TENSOR_A)."""
+    n = np.ascontiguousarray(orders, dtype=np.int32)
+    out = np.zeros(n.size, dtype=np.int32)
+    status = lib().msq_jacobi_route(n.ctypes.data, n.size, mode, out.ctypes.data)
+    if status != 0:
+        raise MsqError(f"msq_jacobi_route: status {status}")
+    return out
 
 
 class Context:

@@ -116,6 +116,22 @@ std::vector<char> gridRouting(const int32_t *n, int count) {
     for (int p = 0; p < best_p; ++p) grid[cand[p]] = 1;
   return grid;
 }
+
+// Routing: a matrix above kGridMinOrder is solved by the grid kernels with
+// every SM, the rest by the batched kernels one CTA each, except: in the
+// FP32 mode (0) the cost model picks the largest matrices to move to the grid
+// kernels (a few large matrices whose one-CTA solves would outlast the
+// batch); in the two-level modes (1-3, built for 256 < n <= 512) a matrix
+// above 256 when at most kGridFewLarge such matrices are in the batch.
+std::vector<char> routeToGrid(const int32_t *n, int count, int mode) {
+  if (mode == 0) return gridRouting(n, count);
+  int large = 0;
+  for (int i = 0; i < count; ++i) large += n[i] > 256;
+  std::vector<char> grid(count, 0);
+  for (int i = 0; i < count; ++i)
+    grid[i] = n[i] > kGridMinOrder || (n[i] > 256 && large <= kGridFewLarge);
+  return grid;
+}
 constexpr int kSweepThreadsMax = 512;
 constexpr int kReplayThreads = 256;
 
@@ -914,16 +930,7 @@ JacobiPlan *planFor(msq_ctx *ctx, const DeviceBatch *b, int mode) {
   plan->count = b->count;
   plan->mode = mode;
   const int total = b->count;
-  // Routing: a matrix above kGridMinOrder is solved by the grid kernels with
-  // every SM, the rest by the batched kernels one CTA each, except: in the
-  // FP32 mode the cost model picks the largest matrices to move to the grid
-  // kernels (a few large matrices whose one-CTA solves would outlast the
-  // batch); in the two-level modes (built for 256 < n <= 512) a matrix above
-  // 256 when at most kGridFewLarge such matrices are in the batch.
-  int large = 0;
-  for (int i = 0; i < total; ++i) large += b->host_n[i] > 256;
-  const std::vector<char> routed = mode == 0 ? gridRouting(b->host_n.data(), total)
-                                             : std::vector<char>();
+  const std::vector<char> routed = routeToGrid(b->host_n.data(), total, mode);
   std::vector<int32_t> ids;
   std::vector<int64_t> t_off(total, 0), l_off(total, 0);
   std::vector<int32_t> sched_off(total, -1), sched_host, table;
@@ -932,7 +939,7 @@ JacobiPlan *planFor(msq_ctx *ctx, const DeviceBatch *b, int mode) {
   std::vector<char> on_tc(total, 0);
   for (int i = 0; i < total; ++i) {
     const int n = b->host_n[i];
-    if (mode == 0 ? routed[i] != 0 : (n > kGridMinOrder || (n > 256 && large <= kGridFewLarge))) {
+    if (routed[i]) {
       plan->grid_ids.push_back(i);
       continue;
     }
@@ -1421,6 +1428,17 @@ extern "C" int msq_autotune_reset(int enable) {
   harvestTimings();
   g_tune.clear();
   g_tune_enabled = enable != 0;
+  return MSQ_OK;
+}
+
+extern "C" int msq_jacobi_route(const int32_t *n, int count, int mode, int32_t *grid) {
+  if (n == nullptr || grid == nullptr || count < 0 || mode < MSQ_VECTORS_REPLAY ||
+      mode > MSQ_VECTORS_TENSOR_A)
+    return MSQ_ERR_INVALID_ARGUMENT;
+  for (int i = 0; i < count; ++i)
+    if (n[i] < 1) return MSQ_ERR_INVALID_ARGUMENT;
+  const std::vector<char> routed = routeToGrid(n, count, mode);
+  for (int i = 0; i < count; ++i) grid[i] = routed[i];
   return MSQ_OK;
 }
 

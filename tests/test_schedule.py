@@ -142,3 +142,40 @@ def test_overlapped_round_covers_every_super_tile_two_level(nb):
     rounds = [[(int(i), int(j) if j >= 0 else -1 - int(j), bool(j >= 0)) for i, j in table[r * p:(r + 1) * p]]
               for r in range(len(table) // p)]
     assert _check_overlap(nb, rounds) > 0   # shared super-tiles occur: the flag path is exercised
+
+
+# ---- routing between the batched and the grid kernels (host side) ---------
+
+def test_routing_cost_model(msq):
+    """FP32 mode: the cost model moves the largest matrices to the grid
+    kernels only where their one-CTA solves would outlast the batch (GB300
+    timings: a lone n = 512 solves in 17.6 ms on the grid kernels against
+    52 ms on one CTA; eight n = 384 take 76 ms on the grid kernels one after
+    another against 20 ms batched)."""
+    route = lambda orders, mode=0: msq.jacobi_route(orders, mode).tolist()
+    assert route([300]) == [1]                       # lone: grid
+    assert route([300] * 9) == [0] * 9               # nine concurrent CTAs win
+    assert route([384] * 8) == [0] * 8
+    assert route([512, 512]) == [1, 1]
+    assert route([512] * 4) == [0] * 4
+    assert route([256]) == [0]                       # up to 256: always batched
+    assert route([2048, 64, 100]) == [1, 0, 0]       # above 1024: always grid
+    # a fallback-sized mix: only its largest member outlasts the rest
+    mix = [367, 230, 32, 399, 45, 83, 45, 125, 176, 275, 252, 330, 81, 300, 344,
+           153, 127, 36, 387, 154, 143, 119, 404, 387, 378, 105, 154, 510]
+    assert [n for n, g in zip(mix, route(mix)) if g] == [510]
+    # a throughput-bound batch stays on the batched kernels
+    rng = np.random.default_rng(0)
+    big = np.floor(np.exp(rng.uniform(np.log(16), np.log(513), 4096))).astype(int)
+    assert sum(route(big)) == 0
+
+
+def test_routing_two_level_modes(msq):
+    """The two-level modes keep the rule they were built with: a matrix
+    above 256 goes to the grid kernels when at most eight are in the batch."""
+    for mode in (1, 2, 3):
+        assert msq.jacobi_route([300] * 8, mode).tolist() == [1] * 8
+        assert msq.jacobi_route([300] * 9, mode).tolist() == [0] * 9
+        assert msq.jacobi_route([2048, 300] + [400] * 9, mode).tolist() == [1] + [0] * 10
+    with pytest.raises(Exception):
+        msq.jacobi_route([300], 4)
