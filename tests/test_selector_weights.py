@@ -53,3 +53,20 @@ def test_cost_order_comes_from_the_probe():
     # plans more than 2% apart keep their measured order
     for a, b in zip(order, order[1:]):
         assert secs[a] <= secs[b] * 1.02 or sel.PLANS[a][0] < sel.PLANS[b][0]
+
+
+def test_cost_order_ties_prefer_the_more_precise_basis():
+    """Plans within 2% of each other count as equally cheap and are ordered
+    by basis precision (BF16, then FP8, then MXFP4); otherwise by time."""
+    sel = importlib.import_module("mixed-mlx_gb300.selector")
+    # PLANS: 0 bf16+0, 1 bf16+1, 2 bf16+2, 3 fp8+0, 4 fp8+1, 5 fp8+2, 6 mxfp4+1, 7 mxfp4+2
+    secs = [4.0, 2.6, 2.10, 4.0, 2.5, 2.09, 2.5, 2.08]
+    order = sel.cost_order(secs)
+    # 2.08 / 2.09 / 2.10 tie: bf16+2 first, then fp8+2, then mxfp4+2
+    assert order[:3] == [2, 5, 7]
+    # fp8+1 and mxfp4+1 tie at 2.5 (FP8 first); bf16+1 at 2.6 is 4% dearer
+    assert order[3:6] == [4, 6, 1]
+    # the two 4.0 plans tie: BF16 before FP8
+    assert order[6:] == [0, 3]
+    # far apart: plain time order
+    assert sel.cost_order([1.0, 2.0, 3.0, 4.0, 5.0, 6.0, 7.0, 8.0]) == list(range(8))
