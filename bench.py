@@ -962,7 +962,8 @@ def main():
                    "plans": plan_source,
                    "matrices": batch.count, "sum_n3": float(np.sum(n64 ** 3)),
                    "l2": "inputs larger than L2 (%.0f MB)" % (batch.total * 4 / 1e6),
-                   "jacobi_tolerance": args.jacobi_tol},
+                   "jacobi_tolerance": ("per plan: 1e-7 / 1e-3 / 1e-2 for 0 / 1 / 2 corrections"
+                                        if plan_source.startswith("learned") else args.jacobi_tol)},
         "e2e": {"value": e2e_value, "unit": "solves/s", "ms_per_step": e2e_ms,
                 "h2d_bytes_per_step": batch.total * 4, "d2h_bytes_per_step": batch.total * 4},
         "roofline": roof,
