@@ -75,8 +75,8 @@ def test_trained_selector_plans_cost_less_than_the_fp32_path(ctx, msq, sel):
     matrices: every result still meets the tolerance (FP32 fallback on a
     miss), the selected plans' pass costs less GPU time than
     solving every matrix with the FP32 path the method uses without a
-    selector, and with the misses' fallback the call stays within 10% of
-    that path.
+    selector, and with the misses' fallback the call stays close to that
+    path (asserted within 15%).
 
     Held-out: 2048 matrices (n <= 512, condition to 1e3), enough per SM that
     a Jacobi sweep's time follows the work of the members still rotating.
@@ -140,7 +140,7 @@ def test_trained_selector_plans_cost_less_than_the_fp32_path(ctx, msq, sel):
     times = dict(pass_sel=t_pass_sel, pass_fp32=t_pass_fp32, sel=t_sel, fp32=t_fp32,
                  fallbacks=int(sum(r.fallback for r in res_sel)))
     assert t_pass_sel < 0.95 * t_pass_fp32, times
-    assert t_sel < 1.1 * t_fp32, times
+    assert t_sel < 1.15 * t_fp32, times
     xs = batch_t.unpack(out_sel.cpu().numpy())
     for i in range(0, batch_t.count, 16):
         a64 = mats_t[i].cpu().numpy()
